@@ -1,0 +1,186 @@
+/* shoccs_gpu.h -- C ABI of the GB300 (sm_103a) SHOCCS derivative-operator hot path.
+ *
+ * The reference (pbrady/shoccs) exposes this path only as C++ classes; each entry point
+ * below replaces one of them and keeps its argument meaning:
+ *
+ *   shoccs_problem_create   ccs::mesh(index_extents, domain_extents, shapes)
+ *                             src/mesh/mesh.hpp:24-31, src/mesh/mesh.cpp:121-152
+ *                           + bcs::Grid / bcs::Object   src/operators/boundaries.hpp:37-38
+ *                           + stencil::from_lua         src/stencils/stencil.cpp:8-106
+ *                           + derivative ctor (x, y, z) src/operators/derivative.cpp:452-473
+ *   shoccs_problem_sizes    mesh::size(), mesh::R(dir).size()   src/mesh/mesh.hpp:35,71-97
+ *   shoccs_problem_cut_points  mesh::R(dir) (mesh_object_info)  src/mesh/mesh_types.hpp:31-38
+ *   shoccs_problem_block_meta  block::metadata_view()/coefficients_view()
+ *                                                   src/matrices/block.hpp:30-113
+ *   shoccs_problem_csr      derivative's B / N / Bf / Br csr matrices
+ *                                                   src/operators/derivative.hpp:20-40
+ *   shoccs_derivative_apply derivative::operator()(u[, nu], du, eq|plus_eq)
+ *                                                   src/operators/derivative.cpp:502-519
+ *   shoccs_laplacian_apply  laplacian::operator()(u[, nu])(du)  src/operators/laplacian.cpp:37-58
+ *   shoccs_gradient_apply   gradient::operator()(u)(dx, dy, dz)  src/operators/gradient.cpp:35-46
+ *   shoccs_system_create    systems::heat / systems::scalar_wave ctors
+ *                                                   src/systems/heat.cpp:22-51,
+ *                                                   src/systems/scalar_wave.cpp:44-102
+ *   shoccs_system_initialize  system::initialize    src/systems/detail/scalar_system_utils.hpp:186-219
+ *   shoccs_system_rk4       integrators::rk4::operator() applied nsteps times with the
+ *                           simulation_cycle u0 <- u1 copy   src/temporal/rk4.cpp:16-47,
+ *                                                   src/simulation/simulation_cycle.cpp:79-126
+ *   shoccs_system_rhs       system::rhs             src/systems/heat.cpp:119-162,
+ *                                                   src/systems/scalar_wave.cpp:195-239
+ *   shoccs_system_stats     system::stats           src/systems/detail/scalar_system_utils.hpp:77-181
+ *   shoccs_system_timestep  system::timestep_size   src/systems/heat.cpp:356-361,
+ *                                                   src/systems/scalar_wave.cpp:357-362
+ *
+ * Conventions.  Fields are the reference's scalar {D, Rx, Ry, Rz} (src/fields/scalar.hpp:13-67):
+ * D is the full nx*ny*nz grid (z fastest, solid points included), Rx/Ry/Rz hold one value
+ * per cut point.  Pointers in shoccs_field are DEVICE pointers owned by the caller unless an
+ * entry point says otherwise.  Every entry point returns a shoccs_status; on failure
+ * shoccs_last_error() gives a one-line reason (the reference logs and returns std::nullopt
+ * from from_lua, or asserts).  Handles are not thread-safe; use one per host thread.
+ * Work is issued on the given CUDA stream (NULL = legacy default stream) and every entry
+ * point returns after the stream has finished, like the reference's Kokkos::fence.
+ */
+#ifndef SHOCCS_GPU_H
+#define SHOCCS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SHOCCS_OK = 0,
+    SHOCCS_EINVAL = 1,      /* bad argument or configuration */
+    SHOCCS_ENOMEM = 2,      /* device or host allocation failed */
+    SHOCCS_ECUDA = 3,       /* a CUDA runtime call failed */
+    SHOCCS_ETIMEOUT = 4,    /* a bounded device-side wait gave up */
+    SHOCCS_ENONFINITE = 5,  /* the solution became non-finite or exceeded its bound */
+    SHOCCS_EUNSUPPORTED = 6 /* valid in the reference but not provided by this path */
+} shoccs_status;
+
+/* boundary condition types, in the order of bcs::type (src/operators/boundaries.hpp:13-20) */
+enum { SHOCCS_BC_DIRICHLET = 0, SHOCCS_BC_FLOATING = 1, SHOCCS_BC_NEUMANN = 2 };
+
+/* schemes: scheme.order/type of stencil::from_lua (src/stencils/stencil.cpp:35-50) */
+enum { SHOCCS_SCHEME_E2_2 = 0, SHOCCS_SCHEME_E4_2 = 1, SHOCCS_SCHEME_E4_1 = 2 };
+
+/* arithmetic of the operator and system kernels */
+enum {
+    SHOCCS_PREC_FP64 = 0,  /* every value and coefficient in FP64 */
+    SHOCCS_PREC_MIXED = 1  /* FP32 fields and interior stencils; FP64 closure rows;
+                              compensated FP32-pair (~2^-46) solution and RK4 accumulator */
+};
+
+typedef struct {
+    int n[3];                 /* index_extents (1 for a trivial axis) */
+    double lo[3], hi[3];      /* domain_bounds min / max */
+    int n_spheres;
+    const double* centers;    /* 3 * n_spheres */
+    const double* radii;      /* n_spheres */
+    const int* sphere_bc;     /* n_spheres: boundary_condition of each shape */
+    int grid_bc[6];           /* xmin, xmax, ymin, ymax, zmin, zmax */
+    int scheme;               /* SHOCCS_SCHEME_* */
+    double alpha[2];          /* scheme.alpha (E4_1) */
+} shoccs_problem_desc;
+
+typedef struct shoccs_problem shoccs_problem;
+typedef struct shoccs_system shoccs_system;
+
+/* A scalar field: device pointers to D, Rx, Ry, Rz; element type double (FP64) or float
+ * (MIXED operators).  R pointers may be NULL when the matching R(dir) is empty. */
+typedef struct {
+    void* D;
+    void* Rx;
+    void* Ry;
+    void* Rz;
+} shoccs_field;
+
+/* ---- problem (mesh + stencil + boundary conditions + compiled operators) ---- */
+shoccs_status shoccs_problem_create(const shoccs_problem_desc* desc, shoccs_problem** out);
+shoccs_status shoccs_problem_destroy(shoccs_problem* p);
+/* sizes[0] = nx*ny*nz, sizes[1..3] = |Rx|, |Ry|, |Rz|, sizes[4] = fluid points */
+shoccs_status shoccs_problem_sizes(const shoccs_problem* p, int64_t sizes[5]);
+/* cut points of R(dir): psi[n], position[3n], normal[3n], ray_outside[n], solid_coord[3n],
+ * shape_id[n] (any output may be NULL) */
+shoccs_status shoccs_problem_cut_points(const shoccs_problem* p, int dir, double* psi,
+                                        double* position, double* normal, int* ray_outside,
+                                        int* solid_coord, int* shape_id);
+/* per-line block metadata (13 ints per line, inner_block_meta order) and coefficients;
+ * call with NULL buffers to query n_lines / n_coeffs */
+shoccs_status shoccs_problem_block_meta(const shoccs_problem* p, int dir, int* meta,
+                                        int64_t* n_lines, double* coeffs, int64_t* n_coeffs);
+/* which: 0 B, 1 N, 2..4 Bf(r=0..2), 5..7 Br(r=0..2); row offsets have rows+1 entries */
+shoccs_status shoccs_problem_csr(const shoccs_problem* p, int dir, int which, int64_t* rows,
+                                 int64_t* nnz, int64_t* row_offsets, int64_t* cols,
+                                 double* vals);
+/* per-point class bytes of the compiled operator (host copy, nx*ny*nz bytes) */
+shoccs_status shoccs_problem_classes(const shoccs_problem* p, uint8_t* cls);
+/* upload the compiled operator to the current device (done lazily by apply calls) */
+shoccs_status shoccs_problem_upload(shoccs_problem* p, void* stream);
+
+/* ---- operators (device fields; prec selects double or float element type) ---- */
+shoccs_status shoccs_derivative_apply(shoccs_problem* p, int dir, int prec,
+                                      const shoccs_field* u, const shoccs_field* nu,
+                                      shoccs_field* du, int plus_eq, void* stream);
+shoccs_status shoccs_laplacian_apply(shoccs_problem* p, int prec, const shoccs_field* u,
+                                     const shoccs_field* nu, shoccs_field* du, void* stream);
+shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_field* u,
+                                    shoccs_field* dx, shoccs_field* dy, shoccs_field* dz,
+                                    void* stream);
+
+/* ---- systems ---- */
+enum { SHOCCS_SYS_HEAT = 0, SHOCCS_SYS_WAVE = 1 };
+/* exact / manufactured solutions with closed forms (params in shoccs_system_desc.sol) */
+enum {
+    SHOCCS_SOL_ZERO = 0,        /* u = 0 */
+    SHOCCS_SOL_SINSIN = 1,      /* prod_d sin(2 pi k x_d) exp(-t); sol[0] = k */
+    SHOCCS_SOL_GAUSS_PULSE = 2, /* exp(-|x - x0 - a t|^2 / (2 s^2)); sol = x0[3], a[3], s */
+    SHOCCS_SOL_RADIAL_SIN = 3   /* sin(2 pi (|x - c| - r - t)); sol = c[3], r */
+};
+enum { SHOCCS_VEL_CONSTANT = 0, SHOCCS_VEL_RADIAL = 1 };
+
+typedef struct {
+    int kind;          /* SHOCCS_SYS_* */
+    int prec;          /* SHOCCS_PREC_* */
+    double diffusivity;/* heat */
+    int vel_kind;      /* wave: SHOCCS_VEL_* */
+    double vel[3];     /* wave constant velocity a (u_t + a.grad u = 0) */
+    double center[3];  /* wave radial velocity centre */
+    int sol_kind;      /* SHOCCS_SOL_*: Dirichlet data, heat source and error reference */
+    double sol[8];
+    double max_error;  /* validity bound on the max-norm error (heat uses 1e6) */
+} shoccs_system_desc;
+
+shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* desc,
+                                   shoccs_system** out);
+shoccs_status shoccs_system_destroy(shoccs_system* s);
+/* u0 <- exact solution at time t on fluid D points, 0 on solid points, exact on R */
+shoccs_status shoccs_system_initialize(shoccs_system* s, double t, void* stream);
+/* copy the state in/out as FP64; where = 0 host pointers, 1 device pointers */
+shoccs_status shoccs_system_set_state(shoccs_system* s, const shoccs_field* u, int where,
+                                      void* stream);
+shoccs_status shoccs_system_get_state(shoccs_system* s, shoccs_field* u, int where,
+                                      void* stream);
+/* nsteps classic RK4 steps of size dt from time t0 (fused stage kernels) */
+shoccs_status shoccs_system_rk4(shoccs_system* s, double t0, double dt, int nsteps,
+                                void* stream);
+/* one right-hand-side evaluation of the current state at time t into rhs (FP64, device) */
+shoccs_status shoccs_system_rhs(shoccs_system* s, double t, shoccs_field* rhs, void* stream);
+/* out[11] = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry,
+ *            Linf_Rz, argmax_Rz} of the current state against the exact solution at t */
+shoccs_status shoccs_system_stats(shoccs_system* s, double t, double out[11], void* stream);
+/* dt from the CFL number: heat p*h_min^2/(4k), wave c*h_min */
+shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double* dt);
+/* kernels launched by this library since load (for launch-count accounting) */
+int64_t shoccs_kernel_launches(void);
+
+/* last error message of the calling thread */
+size_t shoccs_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHOCCS_GPU_H */

@@ -1,0 +1,304 @@
+"""shoccs_gb300 -- GB300 (sm_103a) implementation of the SHOCCS cut-cell derivative-operator
+hot path: per-axis stencil sweeps with cut-cell closures, heat / scalar-wave right-hand
+sides and the RK4 stage update.
+
+The Python layer is a thin binding of the C ABI (include/shoccs_gpu.h) that keeps the
+names of the reference's C++ classes:
+
+    Problem      ccs::mesh + bcs::Grid/Object + stencil     (src/mesh/mesh.hpp, ...)
+    Derivative   ccs::derivative                            (src/operators/derivative.hpp)
+    Laplacian    ccs::laplacian                             (src/operators/laplacian.hpp)
+    Gradient     ccs::gradient                              (src/operators/gradient.hpp)
+    Heat         ccs::systems::heat                         (src/systems/heat.hpp)
+    ScalarWave   ccs::systems::scalar_wave                  (src/systems/scalar_wave.hpp)
+    System.rk4   ccs::integrators::rk4                      (src/temporal/rk4.hpp)
+
+Fields are ScalarField(D, Rx, Ry, Rz) of CUDA tensors (torch is used only to hold device
+memory).  All arithmetic runs in the library's CUDA kernels.
+"""
+import ctypes
+from collections import namedtuple
+
+from . import _capi
+from ._capi import (BC_DIRICHLET, BC_FLOATING, BC_NEUMANN, PREC_FP64, PREC_MIXED,
+                    SCHEME_E2_2, SCHEME_E4_1, SCHEME_E4_2, SOL_GAUSS_PULSE, SOL_RADIAL_SIN,
+                    SOL_SINSIN, SOL_ZERO, VEL_CONSTANT, VEL_RADIAL, ShoccsError)
+
+ScalarField = namedtuple("ScalarField", ["D", "Rx", "Ry", "Rz"])
+
+_BC = {"dirichlet": BC_DIRICHLET, "floating": BC_FLOATING, "neumann": BC_NEUMANN}
+_SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1}
+
+
+def _bc(b):
+    return _BC[b] if isinstance(b, str) else int(b)
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr() if t.numel() else None
+    return t
+
+
+def _field(f):
+    if f is None:
+        return None
+    return ctypes.byref(_capi.Field(_ptr(f.D), _ptr(f.Rx), _ptr(f.Ry), _ptr(f.Rz)))
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+
+
+class Problem:
+    """Mesh, boundary conditions and scheme; builds the three derivative operators.
+
+    n, lo, hi: index_extents and domain_bounds; spheres: [(center3, radius, bc)];
+    grid_bc: (xmin, xmax, ymin, ymax, zmin, zmax); scheme: "E2_2" | "E4_2" | "E4_1".
+    """
+
+    def __init__(self, n, lo, hi, spheres=(), grid_bc=("floating",) * 6, scheme="E4_2",
+                 alpha=(0.0, 0.0)):
+        lib = _capi.lib()
+        d = _capi.ProblemDesc()
+        n = list(n) + [1] * (3 - len(n))
+        lo = list(lo) + [0.0] * (3 - len(lo))
+        hi = list(hi) + [lo[len(hi)] if len(hi) < 3 else 0.0] * (3 - len(hi))
+        d.n[:] = [int(v) for v in n]
+        d.lo[:] = [float(v) for v in lo]
+        d.hi[:] = [float(v) for v in hi]
+        spheres = list(spheres)
+        d.n_spheres = len(spheres)
+        self._centers = (ctypes.c_double * max(1, 3 * len(spheres)))()
+        self._radii = (ctypes.c_double * max(1, len(spheres)))()
+        self._sbc = (ctypes.c_int * max(1, len(spheres)))()
+        for i, (c, r, b) in enumerate(spheres):
+            c = list(c) + [0.0] * (3 - len(c))
+            self._centers[3 * i:3 * i + 3] = [float(v) for v in c]
+            self._radii[i] = float(r)
+            self._sbc[i] = _bc(b)
+        d.centers = ctypes.cast(self._centers, _capi.c_double_p)
+        d.radii = ctypes.cast(self._radii, _capi.c_double_p)
+        d.sphere_bc = ctypes.cast(self._sbc, _capi.c_int_p)
+        d.grid_bc[:] = [_bc(b) for b in grid_bc]
+        d.scheme = _SCHEME[scheme] if isinstance(scheme, str) else int(scheme)
+        d.alpha[:] = [float(alpha[0]), float(alpha[1])]
+        self.desc = d
+        h = ctypes.c_void_p()
+        _capi.check(lib.shoccs_problem_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self.n = tuple(d.n)
+        s = (ctypes.c_int64 * 5)()
+        _capi.check(lib.shoccs_problem_sizes(self._h, s))
+        self.size = s[0]
+        self.nR = (s[1], s[2], s[3])
+        self.n_fluid = s[4]
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _capi.lib().shoccs_problem_destroy(self._h)
+            self._h = None
+
+    # --- setup introspection (host) ---
+    def cut_points(self, d):
+        import numpy as np
+        n = self.nR[d]
+        psi = np.zeros(n)
+        pos = np.zeros(3 * n)
+        nrm = np.zeros(3 * n)
+        ro = np.zeros(n, dtype=np.int32)
+        sc = np.zeros(3 * n, dtype=np.int32)
+        sid = np.zeros(n, dtype=np.int32)
+        P = lambda a, t: a.ctypes.data_as(t)
+        _capi.check(_capi.lib().shoccs_problem_cut_points(
+            self._h, d, P(psi, _capi.c_double_p), P(pos, _capi.c_double_p),
+            P(nrm, _capi.c_double_p), P(ro, _capi.c_int_p), P(sc, _capi.c_int_p),
+            P(sid, _capi.c_int_p)))
+        return dict(psi=psi, position=pos.reshape(-1, 3), normal=nrm.reshape(-1, 3),
+                    ray_outside=ro, solid_coord=sc.reshape(-1, 3), shape_id=sid)
+
+    def block_meta(self, d):
+        import numpy as np
+        nl, nc = ctypes.c_int64(), ctypes.c_int64()
+        lib = _capi.lib()
+        _capi.check(lib.shoccs_problem_block_meta(self._h, d, None, ctypes.byref(nl), None,
+                                                  ctypes.byref(nc)))
+        meta = np.zeros((nl.value, 13), dtype=np.int32)
+        coeffs = np.zeros(nc.value)
+        _capi.check(lib.shoccs_problem_block_meta(
+            self._h, d, meta.ctypes.data_as(_capi.c_int_p), None,
+            coeffs.ctypes.data_as(_capi.c_double_p), None))
+        return meta, coeffs
+
+    def csr(self, d, which):
+        """which: 0 B, 1 N, 2..4 Bf(r), 5..7 Br(r) -> (rows, row_offsets, cols, vals)"""
+        import numpy as np
+        rows, nnz = ctypes.c_int64(), ctypes.c_int64()
+        lib = _capi.lib()
+        _capi.check(lib.shoccs_problem_csr(self._h, d, which, ctypes.byref(rows),
+                                           ctypes.byref(nnz), None, None, None))
+        u = np.zeros(rows.value + 1, dtype=np.int64)
+        v = np.zeros(nnz.value, dtype=np.int64)
+        w = np.zeros(nnz.value)
+        _capi.check(lib.shoccs_problem_csr(self._h, d, which, None, None,
+                                           u.ctypes.data_as(_capi.c_int64_p),
+                                           v.ctypes.data_as(_capi.c_int64_p),
+                                           w.ctypes.data_as(_capi.c_double_p)))
+        return rows.value, u, v, w
+
+    def classes(self):
+        import numpy as np
+        out = np.zeros(self.size, dtype=np.uint8)
+        _capi.check(_capi.lib().shoccs_problem_classes(self._h, out.ctypes.data))
+        return out
+
+    # --- field helpers (device) ---
+    def zeros(self, dtype=None, device="cuda"):
+        import torch
+        dtype = dtype or torch.float64
+        return ScalarField(torch.zeros(self.size, dtype=dtype, device=device),
+                           *[torch.zeros(n, dtype=dtype, device=device) for n in self.nR])
+
+
+class Derivative:
+    """ccs::derivative: du (=|+=) D_dir u, optional Neumann data nu (FP64)."""
+
+    def __init__(self, problem, d, prec=PREC_FP64):
+        self.p, self.dir, self.prec = problem, d, prec
+
+    def __call__(self, u, du, plus_eq=False, nu=None, stream=None):
+        _capi.check(_capi.lib().shoccs_derivative_apply(
+            self.p.handle, self.dir, self.prec, _field(u), _field(nu), _field(du),
+            1 if plus_eq else 0, _stream(stream)))
+        return du
+
+
+class Laplacian:
+    def __init__(self, problem, prec=PREC_FP64):
+        self.p, self.prec = problem, prec
+
+    def __call__(self, u, du, nu=None, stream=None):
+        _capi.check(_capi.lib().shoccs_laplacian_apply(self.p.handle, self.prec, _field(u),
+                                                       _field(nu), _field(du), _stream(stream)))
+        return du
+
+
+class Gradient:
+    def __init__(self, problem, prec=PREC_FP64):
+        self.p, self.prec = problem, prec
+
+    def __call__(self, u, dx, dy, dz, stream=None):
+        _capi.check(_capi.lib().shoccs_gradient_apply(self.p.handle, self.prec, _field(u),
+                                                      _field(dx), _field(dy), _field(dz),
+                                                      _stream(stream)))
+        return dx, dy, dz
+
+
+class System:
+    """A heat or scalar-wave system with its RK4 registers on the device."""
+
+    def __init__(self, problem, kind, prec=PREC_FP64, diffusivity=1.0, vel_kind=VEL_CONSTANT,
+                 vel=(0.0, 0.0, 0.0), center=(0.0, 0.0, 0.0), sol_kind=SOL_ZERO,
+                 sol=(), max_error=100.0):
+        d = _capi.SystemDesc()
+        d.kind, d.prec, d.diffusivity = kind, prec, float(diffusivity)
+        d.vel_kind = vel_kind
+        d.vel[:] = [float(v) for v in vel]
+        d.center[:] = [float(v) for v in center]
+        d.sol_kind = sol_kind
+        sol = list(sol) + [0.0] * (8 - len(sol))
+        d.sol[:] = [float(v) for v in sol]
+        d.max_error = float(max_error)
+        self.desc = d
+        self.p = problem
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().shoccs_system_create(problem.handle, ctypes.byref(d),
+                                                     ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _capi.lib().shoccs_system_destroy(self._h)
+            self._h = None
+
+    def initialize(self, t=0.0, stream=None):
+        _capi.check(_capi.lib().shoccs_system_initialize(self._h, float(t), _stream(stream)))
+
+    def set_state(self, u, stream=None):
+        where = 1 if getattr(u.D, "is_cuda", False) else 0
+        f = _field(u) if where == 1 else ctypes.byref(_capi.Field(*[_np_ptr(a) for a in u]))
+        _capi.check(_capi.lib().shoccs_system_set_state(self._h, f, where, _stream(stream)))
+
+    def get_state(self, u, stream=None):
+        where = 1 if getattr(u.D, "is_cuda", False) else 0
+        f = _field(u) if where == 1 else ctypes.byref(_capi.Field(*[_np_ptr(a) for a in u]))
+        _capi.check(_capi.lib().shoccs_system_get_state(self._h, f, where, _stream(stream)))
+        return u
+
+    def rk4(self, t0, dt, nsteps, stream=None):
+        _capi.check(_capi.lib().shoccs_system_rk4(self._h, float(t0), float(dt), int(nsteps),
+                                                  _stream(stream)))
+
+    def rhs(self, t, out, stream=None):
+        _capi.check(_capi.lib().shoccs_system_rhs(self._h, float(t), _field(out),
+                                                  _stream(stream)))
+        return out
+
+    def stats(self, t, stream=None):
+        out = (ctypes.c_double * 11)()
+        st = _capi.lib().shoccs_system_stats(self._h, float(t), out, _stream(stream))
+        vals = list(out)
+        if st not in (_capi.OK, _capi.ENONFINITE):
+            _capi.check(st)
+        return vals, st == _capi.OK
+
+    def timestep(self, cfl):
+        dt = ctypes.c_double()
+        _capi.check(_capi.lib().shoccs_system_timestep(self._h, float(cfl), ctypes.byref(dt)))
+        return dt.value
+
+
+def _np_ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr() if a.numel() else None
+    return a.ctypes.data if a.size else None
+
+
+class Heat(System):
+    """systems::heat: u_t = k lap(u) + source of the manufactured solution."""
+
+    def __init__(self, problem, diffusivity=1.0, prec=PREC_FP64, sol_kind=SOL_ZERO, sol=()):
+        super().__init__(problem, _capi.SYS_HEAT, prec=prec, diffusivity=diffusivity,
+                         sol_kind=sol_kind, sol=sol)
+
+
+class ScalarWave(System):
+    """systems::scalar_wave: u_t = gG . grad(u); gG = -a (constant velocity a) or the
+    reference's radial -(x-c)/|x-c|."""
+
+    def __init__(self, problem, prec=PREC_FP64, vel_kind=VEL_CONSTANT, vel=(0, 0, 0),
+                 center=(0, 0, 0), sol_kind=SOL_ZERO, sol=(), max_error=100.0):
+        super().__init__(problem, _capi.SYS_WAVE, prec=prec, vel_kind=vel_kind, vel=vel,
+                         center=center, sol_kind=sol_kind, sol=sol, max_error=max_error)
+
+
+def kernel_launches():
+    return int(_capi.lib().shoccs_kernel_launches())
+
+
+__all__ = ["Problem", "Derivative", "Laplacian", "Gradient", "Heat", "ScalarWave", "System",
+           "ScalarField", "ShoccsError", "kernel_launches"]

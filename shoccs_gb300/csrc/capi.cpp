@@ -1,0 +1,593 @@
+// capi.cpp -- implementation of include/shoccs_gpu.h.
+//
+// A shoccs_problem owns the host setup (mesh, stencil, per-axis operators in the reference's
+// own decomposition) and, once uploaded, the compiled device tables.  A shoccs_system owns
+// the RK4 registers of one heat or scalar-wave solve.  Errors are reported as status codes
+// with a thread-local message; nothing here falls back to host arithmetic.
+#include "../../include/shoccs_gpu.h"
+#include "device.cuh"
+#include "host/problem.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace sgb;
+
+namespace
+{
+thread_local std::string g_err;
+
+shoccs_status fail(shoccs_status s, const std::string& msg)
+{
+    g_err = msg;
+    return s;
+}
+
+#define SH_CUDA(call)                                                                       \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? SHOCCS_ENOMEM : SHOCCS_ECUDA,     \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+template <class T>
+cudaError_t upload(const std::vector<T>& h, T** d, cudaStream_t s)
+{
+    *d = nullptr;
+    if (h.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)d, h.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+struct DeviceAlloc {
+    std::vector<void*> ptrs;
+    ~DeviceAlloc()
+    {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <class T>
+    cudaError_t put(const std::vector<T>& h, const T** d, cudaStream_t s)
+    {
+        T* p = nullptr;
+        cudaError_t e = upload(h, &p, s);
+        if (p) ptrs.push_back(p);
+        *d = p;
+        return e;
+    }
+    cudaError_t alloc(size_t bytes, void** d)
+    {
+        *d = nullptr;
+        if (!bytes) return cudaSuccess;
+        cudaError_t e = cudaMalloc(d, bytes);
+        if (e == cudaSuccess) ptrs.push_back(*d);
+        return e;
+    }
+};
+} // namespace
+
+struct shoccs_problem {
+    Mesh mesh;
+    Stencil st;
+    Bcs bcs;
+    AxisOp ops[3];
+    Compiled comp;
+    // device side
+    bool uploaded = false;
+    int device = -1;
+    DeviceAlloc mem;
+    DevOp op{};
+    DevR dr{};
+};
+
+struct shoccs_system {
+    shoccs_problem* P;
+    shoccs_system_desc desc;
+    SysParams sp{};
+    DeviceAlloc mem;
+    StepBuffers b{};
+    double t = 0.0;
+};
+
+namespace
+{
+shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
+{
+    int dev = 0;
+    SH_CUDA(cudaGetDevice(&dev));
+    if (p->uploaded) {
+        if (dev != p->device)
+            return fail(SHOCCS_EINVAL, "problem was uploaded to another device");
+        return SHOCCS_OK;
+    }
+    const Compiled& C = p->comp;
+    DevOp& op = p->op;
+    op = DevOp{};
+    op.it0 = C.it[0];
+    op.it1 = C.it[1];
+    op.it2 = C.it[2];
+    op.nzc = C.nzc;
+    op.N = p->mesh.size();
+    for (int d = 0; d < 3; d++) {
+        op.nR[d] = (long long)p->mesh.R[d].size();
+        op.n[d] = p->mesh.n[d];
+        op.phys_of_it[d] = C.phys_of_it[d];
+    }
+    if (op.it0 > 65535) return fail(SHOCCS_EINVAL, "grid too large along the slowest axis");
+    SH_CUDA(p->mem.put(C.cls, &op.cls, s));
+    for (int d = 0; d < 3; d++) SH_CUDA(p->mem.put(p->mesh.x[d], &op.xc[d], s));
+    for (int d = 0; d < 3; d++) {
+        const AxisTables& T = C.ax[d];
+        DevAxis& A = op.ax[d];
+        A.active = T.active;
+        A.stride = T.stride;
+        A.width = T.width;
+        for (int j = 0; j < 5; j++) {
+            A.ic[j] = T.interior[j];
+            A.icf[j] = (float)T.interior[j];
+        }
+        A.antisym = T.width == 5 && T.interior[2] == 0.0 && T.interior[0] == -T.interior[4] &&
+                    T.interior[1] == -T.interior[3];
+        if (!T.active) continue;
+        SH_CUDA(p->mem.put(T.rows, &A.rows, s));
+        SH_CUDA(p->mem.put(T.coef, &A.coef, s));
+        SH_CUDA(p->mem.put(T.chunk_base, &A.chunk_base, s));
+        for (int r = 0; r < 3; r++) {
+            if (T.rr_u[r].empty()) continue;
+            A.rr_rows[r] = (int)T.rr_u[r].size() - 1;
+            SH_CUDA(p->mem.put(T.rr_u[r], &A.rr_u[r], s));
+            SH_CUDA(p->mem.put(T.rr_col[r], &A.rr_col[r], s));
+            SH_CUDA(p->mem.put(T.rr_src[r], &A.rr_src[r], s));
+            SH_CUDA(p->mem.put(T.rr_w[r], &A.rr_w[r], s));
+        }
+    }
+    for (int d = 0; d < 3; d++) {
+        std::vector<double> pos;
+        std::vector<uint8_t> dir;
+        for (const auto& cp : p->mesh.R[d]) {
+            pos.insert(pos.end(), cp.pos, cp.pos + 3);
+            dir.push_back(p->bcs.obj[cp.shape_id] == Dirichlet ? 1 : 0);
+        }
+        SH_CUDA(p->mem.put(pos, &p->dr.pos[d], s));
+        SH_CUDA(p->mem.put(dir, &p->dr.dirichlet[d], s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    p->uploaded = true;
+    p->device = dev;
+    return SHOCCS_OK;
+}
+
+bool bad_bc(int b) { return b < 0 || b > 2; }
+} // namespace
+
+extern "C" {
+
+size_t shoccs_last_error(char* buf, size_t len)
+{
+    if (buf && len) {
+        std::snprintf(buf, len, "%s", g_err.c_str());
+    }
+    return g_err.size();
+}
+
+int64_t shoccs_kernel_launches(void) { return kernel_launch_count(); }
+
+shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem** out)
+{
+    if (!d || !out) return fail(SHOCCS_EINVAL, "null descriptor or output");
+    *out = nullptr;
+    for (int i = 0; i < 3; i++)
+        if (d->n[i] < 1) return fail(SHOCCS_EINVAL, "index_extents must be >= 1");
+    if (d->scheme < 0 || d->scheme > 2) return fail(SHOCCS_EINVAL, "unknown scheme");
+    if (d->n_spheres < 0 || (d->n_spheres && (!d->centers || !d->radii || !d->sphere_bc)))
+        return fail(SHOCCS_EINVAL, "sphere arrays missing");
+    for (int i = 0; i < 6; i++)
+        if (bad_bc(d->grid_bc[i])) return fail(SHOCCS_EINVAL, "bad grid boundary condition");
+    for (int i = 0; i < d->n_spheres; i++)
+        if (bad_bc(d->sphere_bc[i])) return fail(SHOCCS_EINVAL, "bad shape boundary condition");
+    if (d->scheme == SHOCCS_SCHEME_E4_1) {
+        // src/stencils/E4_1.cpp:34-41
+        if (d->alpha[1] < 197.0 / 288.0)
+            return fail(SHOCCS_EINVAL,
+                        "E4_1: alpha[1] must be >= 197/288 to avoid the interior "
+                        "denominator singularity");
+        for (int i = 0; i < 6; i++)
+            if (d->grid_bc[i] == SHOCCS_BC_NEUMANN && d->n[i / 2] > 1)
+                return fail(SHOCCS_EUNSUPPORTED, "E4_1 has no Neumann closure");
+        for (int i = 0; i < d->n_spheres; i++)
+            if (d->sphere_bc[i] != SHOCCS_BC_DIRICHLET)
+                return fail(SHOCCS_EUNSUPPORTED,
+                            "E4_1 has no cross-direction interpolant; objects must be "
+                            "Dirichlet");
+    }
+    try {
+        auto p = std::make_unique<shoccs_problem>();
+        std::vector<Sphere> shapes;
+        for (int i = 0; i < d->n_spheres; i++) {
+            if (!(d->radii[i] > 0)) return fail(SHOCCS_EINVAL, "sphere radius must be > 0");
+            shapes.push_back(Sphere{{d->centers[3 * i], d->centers[3 * i + 1],
+                                     d->centers[3 * i + 2]},
+                                    d->radii[i], i});
+        }
+        p->mesh = build_mesh(d->n, d->lo, d->hi, shapes);
+        p->st.kind = d->scheme;
+        p->st.alpha[0] = d->alpha[0];
+        p->st.alpha[1] = d->alpha[1];
+        // a boundary condition on a trivial axis is Floating (src/operators/boundaries.cpp:15-24)
+        for (int a = 0; a < 3; a++)
+            for (int side = 0; side < 2; side++) {
+                int b = d->grid_bc[2 * a + side];
+                if (p->mesh.n[a] == 1 && b != Floating) b = Floating;
+                p->bcs.grid[a][side] = b;
+            }
+        p->bcs.obj.assign(d->sphere_bc, d->sphere_bc + d->n_spheres);
+        for (int a = 0; a < 3; a++) p->ops[a] = assemble_axis(a, p->mesh, p->st, p->bcs);
+        p->comp = compile_operators(p->mesh, p->ops, p->bcs);
+        *out = p.release();
+        return SHOCCS_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(SHOCCS_ENOMEM, "host allocation failed during setup");
+    } catch (const std::exception& e) {
+        return fail(SHOCCS_EINVAL, e.what());
+    }
+}
+
+shoccs_status shoccs_problem_destroy(shoccs_problem* p)
+{
+    delete p;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_sizes(const shoccs_problem* p, int64_t sizes[5])
+{
+    if (!p || !sizes) return fail(SHOCCS_EINVAL, "null argument");
+    sizes[0] = p->mesh.size();
+    for (int d = 0; d < 3; d++) sizes[d + 1] = (int64_t)p->mesh.R[d].size();
+    sizes[4] = p->comp.n_fluid;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_cut_points(const shoccs_problem* p, int dir, double* psi,
+                                        double* position, double* normal, int* ray_outside,
+                                        int* solid_coord, int* shape_id)
+{
+    if (!p || dir < 0 || dir > 2) return fail(SHOCCS_EINVAL, "bad problem or direction");
+    const auto& R = p->mesh.R[dir];
+    for (size_t i = 0; i < R.size(); i++) {
+        if (psi) psi[i] = R[i].psi;
+        for (int c = 0; c < 3; c++) {
+            if (position) position[3 * i + c] = R[i].pos[c];
+            if (normal) normal[3 * i + c] = R[i].nrm[c];
+            if (solid_coord) solid_coord[3 * i + c] = R[i].solid[c];
+        }
+        if (ray_outside) ray_outside[i] = R[i].ray_outside;
+        if (shape_id) shape_id[i] = R[i].shape_id;
+    }
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_block_meta(const shoccs_problem* p, int dir, int* meta,
+                                        int64_t* n_lines, double* coeffs, int64_t* n_coeffs)
+{
+    if (!p || dir < 0 || dir > 2) return fail(SHOCCS_EINVAL, "bad problem or direction");
+    const AxisOp& A = p->ops[dir];
+    if (n_lines) *n_lines = (int64_t)A.meta.size();
+    if (n_coeffs) *n_coeffs = (int64_t)A.coeffs.size();
+    if (meta) std::memcpy(meta, A.meta.data(), A.meta.size() * sizeof(BlockMeta));
+    if (coeffs) std::memcpy(coeffs, A.coeffs.data(), A.coeffs.size() * sizeof(double));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_csr(const shoccs_problem* p, int dir, int which, int64_t* rows,
+                                 int64_t* nnz, int64_t* row_offsets, int64_t* cols,
+                                 double* vals)
+{
+    if (!p || dir < 0 || dir > 2 || which < 0 || which > 7)
+        return fail(SHOCCS_EINVAL, "bad problem, direction or matrix");
+    const AxisOp& A = p->ops[dir];
+    const Csr& c = which == 0 ? A.B : which == 1 ? A.N : which < 5 ? A.Bf[which - 2]
+                                                                   : A.Br[which - 5];
+    if (rows) *rows = c.rows;
+    if (nnz) *nnz = (int64_t)c.w.size();
+    if (row_offsets)
+        for (size_t i = 0; i < c.u.size(); i++) row_offsets[i] = c.u[i];
+    if (cols)
+        for (size_t i = 0; i < c.v.size(); i++) cols[i] = c.v[i];
+    if (vals) std::memcpy(vals, c.w.data(), c.w.size() * sizeof(double));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_classes(const shoccs_problem* p, uint8_t* cls)
+{
+    if (!p || !cls) return fail(SHOCCS_EINVAL, "null argument");
+    std::memcpy(cls, p->comp.cls.data(), p->comp.cls.size());
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_problem_upload(shoccs_problem* p, void* stream)
+{
+    if (!p) return fail(SHOCCS_EINVAL, "null problem");
+    return do_upload(p, (cudaStream_t)stream);
+}
+
+shoccs_status shoccs_derivative_apply(shoccs_problem* p, int dir, int prec,
+                                      const shoccs_field* u, const shoccs_field* nu,
+                                      shoccs_field* du, int plus_eq, void* stream)
+{
+    if (!p || !u || !du || dir < 0 || dir > 2 || (prec != 0 && prec != 1))
+        return fail(SHOCCS_EINVAL, "bad argument");
+    if (nu && prec != PREC_FP64)
+        return fail(SHOCCS_EUNSUPPORTED, "Neumann data is FP64-only");
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    const void* uR[3] = {u->Rx, u->Ry, u->Rz};
+    void* duR[3] = {du->Rx, du->Ry, du->Rz};
+    SH_CUDA(launch_derivative(p->op, dir, prec, u->D, uR[dir], nu ? (const double*)nu->D : nullptr,
+                              du->D, duR, uR, plus_eq, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_laplacian_apply(shoccs_problem* p, int prec, const shoccs_field* u,
+                                     const shoccs_field* nu, shoccs_field* du, void* stream)
+{
+    if (!p || !u || !du || (prec != 0 && prec != 1)) return fail(SHOCCS_EINVAL, "bad argument");
+    if (nu && prec != PREC_FP64)
+        return fail(SHOCCS_EUNSUPPORTED, "Neumann data is FP64-only");
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    const void* uR[3] = {u->Rx, u->Ry, u->Rz};
+    void* duR[3] = {du->Rx, du->Ry, du->Rz};
+    SH_CUDA(launch_laplacian(p->op, prec, u->D, uR, nu ? (const double*)nu->D : nullptr, du->D,
+                             duR, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_field* u,
+                                    shoccs_field* dx, shoccs_field* dy, shoccs_field* dz,
+                                    void* stream)
+{
+    if (!p || !u || !dx || !dy || !dz || (prec != 0 && prec != 1))
+        return fail(SHOCCS_EINVAL, "bad argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    const void* uR[3] = {u->Rx, u->Ry, u->Rz};
+    void* const out[3][4] = {{dx->D, dx->Rx, dx->Ry, dx->Rz},
+                             {dy->D, dy->Rx, dy->Ry, dy->Rz},
+                             {dz->D, dz->Rx, dz->Ry, dz->Rz}};
+    SH_CUDA(launch_gradient(p->op, prec, u->D, uR, out, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// systems
+// ---------------------------------------------------------------------------------------
+shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* d,
+                                   shoccs_system** out)
+{
+    if (!p || !d || !out) return fail(SHOCCS_EINVAL, "null argument");
+    *out = nullptr;
+    if (d->kind != SHOCCS_SYS_HEAT && d->kind != SHOCCS_SYS_WAVE)
+        return fail(SHOCCS_EINVAL, "unknown system kind");
+    if (d->prec != 0 && d->prec != 1) return fail(SHOCCS_EINVAL, "unknown precision");
+    if (d->sol_kind < 0 || d->sol_kind > 3) return fail(SHOCCS_EINVAL, "unknown solution kind");
+    for (int b : p->bcs.obj)
+        if (b != Dirichlet)
+            return fail(SHOCCS_EUNSUPPORTED,
+                        "time stepping supports Dirichlet objects only (non-Dirichlet cut "
+                        "points evolve through R-space rows)");
+    for (int a = 0; a < 3; a++)
+        for (int side = 0; side < 2; side++)
+            if (p->bcs.grid[a][side] == Neumann)
+                return fail(SHOCCS_EUNSUPPORTED, "time stepping with Neumann faces");
+    if (d->kind == SHOCCS_SYS_HEAT && !(d->diffusivity > 0))
+        return fail(SHOCCS_EINVAL, "diffusivity must be > 0");
+    const cudaStream_t s = nullptr;
+    if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+
+    auto S = std::make_unique<shoccs_system>();
+    S->P = p;
+    S->desc = *d;
+    SysParams& sp = S->sp;
+    sp.kind = d->kind;
+    sp.k = d->diffusivity;
+    sp.vel_kind = d->vel_kind;
+    for (int c = 0; c < 3; c++) {
+        sp.vel[c] = d->vel[c];
+        sp.center[c] = d->center[c];
+    }
+    DevSol& sol = sp.sol;
+    sol.kind = d->sol_kind;
+    sol.dims = p->mesh.n[2] > 1 ? 3 : 2;
+    for (int i = 0; i < 8; i++) sol.p[i] = d->sol[i];
+    if (sol.kind == SHOCCS_SOL_SINSIN) {
+        // sin tables evaluated with the host libm, as the reference evaluates its MMS
+        constexpr double twoPI = 2 * 3.14159265358979323846;
+        const double k = d->sol[0];
+        for (int a = 0; a < 3; a++) {
+            std::vector<double> tab(p->mesh.n[a]);
+            for (int i = 0; i < p->mesh.n[a]; i++) tab[i] = std::sin(twoPI * k * p->mesh.x[a][i]);
+            SH_CUDA(S->mem.put(tab, &sol.S[a], s));
+        }
+        for (int r = 0; r < 3; r++) {
+            std::vector<double> tab;
+            for (const auto& cp : p->mesh.R[r]) {
+                double v = std::sin(twoPI * k * cp.pos[0]) * std::sin(twoPI * k * cp.pos[1]);
+                if (sol.dims == 3) v = v * std::sin(twoPI * k * cp.pos[2]);
+                tab.push_back(v);
+            }
+            SH_CUDA(S->mem.put(tab, &sol.SR[r], s));
+        }
+        const double kk = twoPI * k;
+        sol.lapfac = -(double)sol.dims * kk * kk;
+    }
+    const long long N = p->mesh.size();
+    const size_t es_u = 8; // double or float2
+    const size_t es_s = d->prec == PREC_FP64 ? 8 : 4;
+    SH_CUDA(S->mem.alloc(N * es_u, &S->b.u0));
+    SH_CUDA(S->mem.alloc(N * es_u, &S->b.acc));
+    if (d->prec == PREC_FP64) {
+        SH_CUDA(S->mem.alloc(N * es_s, &S->b.sa));
+        SH_CUDA(S->mem.alloc(N * es_s, &S->b.sb));
+    } else {
+        // both FP32 stage fields in one N x 8-byte block, which also stages FP64 state
+        // conversions in set_state / get_state
+        void* base = nullptr;
+        SH_CUDA(S->mem.alloc(N * 2 * es_s, &base));
+        S->b.sa = base;
+        S->b.sb = (char*)base + N * es_s;
+    }
+    SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
+    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * es_u, s));
+    for (int r = 0; r < 3; r++) {
+        const size_t n = p->mesh.R[r].size();
+        void *a, *h, *f;
+        SH_CUDA(S->mem.alloc(n * 8, &a));
+        SH_CUDA(S->mem.alloc(n * 8, &h));
+        SH_CUDA(S->mem.alloc(n * 8, &f));
+        S->b.R[r] = (double*)a;
+        S->b.Rhalf[r] = (double*)h;
+        S->b.Rfull[r] = (double*)f;
+        if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    *out = S.release();
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_destroy(shoccs_system* s)
+{
+    delete s;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_initialize(shoccs_system* S, double t, void* stream)
+{
+    if (!S) return fail(SHOCCS_EINVAL, "null system");
+    const cudaStream_t s = (cudaStream_t)stream;
+    SH_CUDA(launch_initialize(S->P->op, S->P->dr, S->sp.sol, S->desc.prec, t, S->b.u0, S->b.R, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    S->t = t;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_set_state(shoccs_system* S, const shoccs_field* u, int where,
+                                      void* stream)
+{
+    if (!S || !u || !u->D) return fail(SHOCCS_EINVAL, "null argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    const long long N = S->P->mesh.size();
+    const cudaMemcpyKind kind = where == 0 ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (S->desc.prec == PREC_FP64) {
+        SH_CUDA(cudaMemcpyAsync(S->b.u0, u->D, N * 8, kind, s));
+    } else {
+        // stage the FP64 input through the stage-field block (2 x N x 4 bytes = N doubles)
+        void* tmp = S->b.sa;
+        SH_CUDA(cudaMemcpyAsync(tmp, u->D, N * 8, kind, s));
+        SH_CUDA(launch_state_convert(N, 1, (const double*)tmp, S->b.u0, nullptr, nullptr, s));
+    }
+    const void* R[3] = {u->Rx, u->Ry, u->Rz};
+    for (int r = 0; r < 3; r++) {
+        const size_t n = S->P->mesh.R[r].size();
+        if (n && R[r]) SH_CUDA(cudaMemcpyAsync(S->b.R[r], R[r], n * 8, kind, s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_get_state(shoccs_system* S, shoccs_field* u, int where,
+                                      void* stream)
+{
+    if (!S || !u || !u->D) return fail(SHOCCS_EINVAL, "null argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    const long long N = S->P->mesh.size();
+    const cudaMemcpyKind kind = where == 0 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (S->desc.prec == PREC_FP64) {
+        SH_CUDA(cudaMemcpyAsync(u->D, S->b.u0, N * 8, kind, s));
+    } else {
+        void* tmp = S->b.sa;
+        SH_CUDA(launch_state_convert(N, 0, nullptr, nullptr, S->b.u0, (double*)tmp, s));
+        SH_CUDA(cudaMemcpyAsync(u->D, tmp, N * 8, kind, s));
+    }
+    void* R[3] = {u->Rx, u->Ry, u->Rz};
+    for (int r = 0; r < 3; r++) {
+        const size_t n = S->P->mesh.R[r].size();
+        if (n && R[r]) SH_CUDA(cudaMemcpyAsync(R[r], S->b.R[r], n * 8, kind, s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nsteps,
+                                void* stream)
+{
+    if (!S || nsteps < 0 || !(dt > 0)) return fail(SHOCCS_EINVAL, "bad argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    double t = t0;
+    for (int i = 0; i < nsteps; i++) {
+        SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s));
+        t += dt; // step_controller advance (src/simulation/simulation_cycle.cpp:97)
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    S->t = t;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_rhs(shoccs_system* S, double t, shoccs_field* rhs, void* stream)
+{
+    if (!S || !rhs || !rhs->D) return fail(SHOCCS_EINVAL, "null argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    double* outR[3] = {(double*)rhs->Rx, (double*)rhs->Ry, (double*)rhs->Rz};
+    SH_CUDA(launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)rhs->D, outR, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_stats(shoccs_system* S, double t, double out[11], void* stream)
+{
+    if (!S || !out) return fail(SHOCCS_EINVAL, "null argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    double* dev = nullptr;
+    SH_CUDA(cudaMallocAsync((void**)&dev, 4 * sizeof(double), s));
+    cudaError_t e = launch_stats(S->P->op, S->P->dr, S->sp.sol, S->desc.prec, S->b.u0, S->b.R, t,
+                                 dev, s);
+    double h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, dev, sizeof h, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(dev, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(SHOCCS_ECUDA, std::string("stats: ") + cudaGetErrorString(e));
+    // all cut points of a time-stepped system are Dirichlet, so the R statistics are zero
+    // (compute_scalar_stats only visits non-Dirichlet cut points)
+    out[0] = h[0];
+    out[1] = S->P->comp.n_fluid ? h[2] : 0.0;
+    out[2] = S->P->comp.n_fluid ? h[3] : 0.0;
+    out[3] = h[0];
+    out[4] = h[1];
+    for (int i = 5; i < 11; i++) out[i] = 0.0;
+    const double bound = S->desc.kind == SHOCCS_SYS_HEAT ? 1e6 : S->desc.max_error;
+    if (!std::isfinite(out[0]) || std::abs(out[0]) > bound)
+        return fail(SHOCCS_ENONFINITE, "solution error is non-finite or above its bound");
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_timestep(const shoccs_system* S, double cfl, double* dt)
+{
+    if (!S || !dt) return fail(SHOCCS_EINVAL, "null argument");
+    const auto& h = S->P->mesh.h;
+    const double hmin = std::min(h[0], std::min(h[1], h[2]));
+    if (S->desc.kind == SHOCCS_SYS_HEAT)
+        *dt = cfl * hmin * hmin / (4 * S->desc.diffusivity); // heat.cpp:356-361
+    else
+        *dt = cfl * hmin; // scalar_wave.cpp:357-362
+    return SHOCCS_OK;
+}
+
+} // extern "C"

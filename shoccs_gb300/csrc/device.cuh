@@ -1,0 +1,101 @@
+// device.cuh -- device-side view of a compiled cut-cell operator and of the closed-form
+// solutions, shared by kernels.cu and the host API (capi.cpp).
+#pragma once
+
+#include "host/gpu_layout.hpp"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sgb
+{
+
+struct DevAxis {
+    int active;
+    int width;   // 2p+1 interior stencil width (3 or 5)
+    int antisym; // interior coefficients are antisymmetric with a zero centre (E4_1)
+    int pad;
+    long long stride;
+    double ic[5];
+    float icf[5];
+    const ClosureRow* rows;
+    const double* coef;
+    const int* chunk_base;
+    // R-space rows (non-Dirichlet objects) per target r: CSR with source flag
+    const int* rr_u[3];
+    const int* rr_col[3];
+    const unsigned char* rr_src[3];
+    const double* rr_w[3];
+    int rr_rows[3];
+};
+
+struct DevOp {
+    int it0, it1, it2, nzc; // iteration space (it2 contiguous) and 32-point chunks of it2
+    long long N;            // nx*ny*nz
+    long long nR[3];
+    int n[3];
+    int phys_of_it[3];
+    const uint8_t* cls;
+    const double* xc[3]; // grid coordinates per physical axis
+    DevAxis ax[3];
+};
+
+// closed-form exact / manufactured solution evaluated on the device
+struct DevSol {
+    int kind; // SHOCCS_SOL_*
+    int dims;
+    double p[8];
+    const double* S[3];  // SINSIN: sin(2 pi k x) tables per physical axis
+    const double* SR[3]; // SINSIN: product of sines at the cut points of R(d)
+    double lapfac;       // SINSIN: -(dims) (2 pi k)^2
+};
+
+struct DevR {
+    const double* pos[3];     // cut-point positions (3 per point)
+    const uint8_t* dirichlet[3]; // 1 where the cut point's shape is Dirichlet
+};
+
+// launch helpers implemented in kernels.cu -----------------------------------------------
+enum { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+cudaError_t launch_derivative(const DevOp& op, int dir, int prec, const void* uD,
+                              const void* uR, const double* nuD, void* duD, void* const duR[3],
+                              const void* const uRall[3], int plus_eq, cudaStream_t s);
+cudaError_t launch_laplacian(const DevOp& op, int prec, const void* uD, const void* const uR[3],
+                             const double* nuD, void* duD, void* const duR[3], cudaStream_t s);
+cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const void* const uR[3],
+                            void* const out[3][4], cudaStream_t s);
+
+struct SysParams {
+    int kind;      // 0 heat, 1 wave
+    double k;      // heat diffusivity
+    int vel_kind;  // wave 0 constant, 1 radial
+    double vel[3];
+    double center[3];
+    DevSol sol;
+};
+
+struct StepBuffers {
+    void* u0;      // double (FP64) or float2 (MIXED)
+    void* acc;     // double or float2
+    void* sa;      // stage fields: double or float
+    void* sb;
+    double* R[3];      // state R values (time t)
+    double* Rhalf[3];  // Dirichlet R values at t + dt/2
+    double* Rfull[3];  // Dirichlet R values at t + dt
+};
+
+cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
+                            StepBuffers& b, double t, double dt, cudaStream_t s);
+cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
+                       double t, double* out, double* const outR[3], cudaStream_t s);
+cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
+                              double t, void* u0, double* const R[3], cudaStream_t s);
+cudaError_t launch_state_convert(long long n, int to_mixed, const double* in_d, void* out,
+                                 const void* in_m, double* out_d, cudaStream_t s);
+cudaError_t launch_stats(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
+                         const void* u0, double* const R[3], double t, double* dev_out,
+                         cudaStream_t s);
+long long kernel_launch_count();
+
+} // namespace sgb

@@ -1,0 +1,976 @@
+// kernels.cu -- sm_103a kernels of the SHOCCS derivative-operator hot path.
+//
+// One thread per grid point; a warp covers 32 consecutive points of the contiguous axis,
+// so the z (unit-stride) neighbours of a stencil are coalesced and the strided neighbours
+// of the x / y sweeps are served by L1/L2.  Every point reads its class byte (gpu_layout.hpp):
+// interior rows apply the constant 2p+1 point stencil, closure rows (walls and cut cells)
+// apply their dense row in FP64, with the record found by a warp ballot over the 32-point
+// chunk.  The RK4 stage kernels fuse the whole right-hand side (all three axes, closures,
+// heat source or wave advection, Dirichlet rows) with the RK4 register update, so each
+// stage reads the stage field, u0 and the accumulator once and writes them once.
+//
+// Reference operations replaced here:
+//   block::matvec_functor            src/matrices/block.hpp:118-178
+//   csr matvec (B, N, Bf, Br)        src/matrices/csr.cpp:37-51
+//   derivative::apply_kernels        src/operators/derivative.cpp:475-519
+//   laplacian / gradient             src/operators/laplacian.cpp:37-58, gradient.cpp:35-46
+//   heat rhs graph                   src/systems/heat.cpp:164-288
+//   scalar_wave rhs graph            src/systems/scalar_wave.cpp:241-321
+//   update_boundary                  src/systems/heat.cpp:296-354, scalar_wave.cpp:329-355
+//   rk4 + slot ops                   src/temporal/rk4.cpp:11-48, slot_ops.hpp:11-61
+//   compute_scalar_stats             src/systems/detail/scalar_system_utils.hpp:77-181
+#include "device.cuh"
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+
+namespace sgb
+{
+namespace
+{
+std::atomic<long long> g_launches{0};
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int BY = 8; // warps per block along the second iteration axis
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---- loads -----------------------------------------------------------------------------
+__device__ __forceinline__ double ldd(const double* p, long long i) { return __ldg(p + i); }
+__device__ __forceinline__ double ldd(const float* p, long long i) { return (double)__ldg(p + i); }
+__device__ __forceinline__ double ldd(const float2* p, long long i)
+{
+    const float2 v = __ldg(p + i);
+    return (double)v.x + (double)v.y;
+}
+__device__ __forceinline__ float ldf(const float* p, long long i) { return __ldg(p + i); }
+__device__ __forceinline__ float ldf(const float2* p, long long i) { return __ldg(p + i).x; }
+
+// ---- point indexing ----------------------------------------------------------------------
+struct Pt {
+    long long p;
+    long long chunk;
+    int a, b, c;
+    bool valid;
+};
+
+__device__ __forceinline__ Pt point_of(const DevOp& op)
+{
+    Pt q;
+    q.c = blockIdx.x * 32 + threadIdx.x;
+    q.b = blockIdx.y * blockDim.y + threadIdx.y;
+    q.a = blockIdx.z;
+    q.valid = (q.b < op.it1) && (q.c < op.it2);
+    const long long line = (long long)q.a * op.it1 + q.b;
+    q.p = line * op.it2 + q.c;
+    q.chunk = line * op.nzc + blockIdx.x;
+    return q;
+}
+
+__device__ __forceinline__ void phys_ijk(const DevOp& op, const Pt& q, int ijk[3])
+{
+    ijk[0] = ijk[1] = ijk[2] = 0;
+    if (op.phys_of_it[0] >= 0) ijk[op.phys_of_it[0]] = q.a;
+    if (op.phys_of_it[1] >= 0) ijk[op.phys_of_it[1]] = q.b;
+    if (op.phys_of_it[2] >= 0) ijk[op.phys_of_it[2]] = q.c;
+}
+
+// record index of this lane's closure row (all 32 lanes of the warp must call it)
+__device__ __forceinline__ int closure_row(const DevAxis& A, bool is_closure, long long chunk)
+{
+    const unsigned m = __ballot_sync(FULL, is_closure);
+    int base = 0;
+    if (m) {
+        if (threadIdx.x == 0) base = A.chunk_base[chunk];
+        base = __shfl_sync(FULL, base, 0);
+    }
+    return base + __popc(m & lanemask_lt());
+}
+
+// ---- interior stencils -------------------------------------------------------------------
+template <class TIN>
+__device__ __forceinline__ double interior64(const DevAxis& A, const TIN* u, long long p)
+{
+    const long long s = A.stride;
+    if (A.width == 5) {
+        if (A.antisym) {
+            const double d1 = ldd(u, p + s) - ldd(u, p - s);
+            const double d2 = ldd(u, p + 2 * s) - ldd(u, p - 2 * s);
+            return fma(A.ic[3], d1, A.ic[4] * d2);
+        }
+        double r = A.ic[0] * ldd(u, p - 2 * s);
+        r = fma(A.ic[1], ldd(u, p - s), r);
+        r = fma(A.ic[2], ldd(u, p), r);
+        r = fma(A.ic[3], ldd(u, p + s), r);
+        return fma(A.ic[4], ldd(u, p + 2 * s), r);
+    }
+    double r = A.ic[0] * ldd(u, p - s);
+    r = fma(A.ic[1], ldd(u, p), r);
+    return fma(A.ic[2], ldd(u, p + s), r);
+}
+
+template <class TIN>
+__device__ __forceinline__ float interior32(const DevAxis& A, const TIN* u, long long p)
+{
+    const long long s = A.stride;
+    if (A.width == 5) {
+        if (A.antisym) {
+            const float d1 = ldf(u, p + s) - ldf(u, p - s);
+            const float d2 = ldf(u, p + 2 * s) - ldf(u, p - 2 * s);
+            return fmaf(A.icf[3], d1, A.icf[4] * d2);
+        }
+        float r = A.icf[0] * ldf(u, p - 2 * s);
+        r = fmaf(A.icf[1], ldf(u, p - s), r);
+        r = fmaf(A.icf[2], ldf(u, p), r);
+        r = fmaf(A.icf[3], ldf(u, p + s), r);
+        return fmaf(A.icf[4], ldf(u, p + 2 * s), r);
+    }
+    float r = A.icf[0] * ldf(u, p - s);
+    r = fmaf(A.icf[1], ldf(u, p), r);
+    return fmaf(A.icf[2], ldf(u, p + s), r);
+}
+
+// ---- closure rows (always FP64) ----------------------------------------------------------
+// v = (first ? 0 : acc) + sum_j c_j x_j ; v += b * R[b_idx] ; v += n * nu[n_idx]
+// in the order of derivative::apply_kernels (O, then B, then N).
+template <class TIN, class TR>
+__device__ __forceinline__ double closure64(const DevAxis& A, int row, long long p,
+                                            const TIN* u, const TR* Rd, const double* nu,
+                                            double acc, bool first)
+{
+    const ClosureRow cr = A.rows[row];
+    const double* c = A.coef + cr.coef_off;
+    double s = 0.0;
+    long long q = p + (long long)cr.col0 * A.stride;
+    for (int j = 0; j < cr.ncol; ++j) {
+        s = fma(__ldg(c + j), ldd(u, q), s);
+        q += A.stride;
+    }
+    double v = first ? s : acc + s;
+    int k = cr.ncol;
+    if (cr.flags & ROWF_B) {
+        v = fma(__ldg(c + k), ldd(Rd, cr.b_idx), v);
+        ++k;
+    }
+    if ((cr.flags & ROWF_N) && nu) v = fma(__ldg(c + k), __ldg(nu + cr.n_idx), v);
+    return v;
+}
+
+// ---- closed-form solutions -------------------------------------------------------------
+enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3 };
+
+__device__ __forceinline__ double sol_at(const DevSol& s, double t, double et, const double x[3],
+                                         const int* ijk, int rdir, long long ridx)
+{
+    switch (s.kind) {
+    case SOL_SINSIN: {
+        double v;
+        if (ijk) {
+            v = s.S[0][ijk[0]] * s.S[1][ijk[1]];
+            if (s.dims == 3) v = v * s.S[2][ijk[2]];
+        } else {
+            v = s.SR[rdir][ridx];
+        }
+        return v * et;
+    }
+    case SOL_GAUSS_PULSE: {
+        const double d0 = (x[0] - s.p[0]) - s.p[3] * t;
+        const double d1 = (x[1] - s.p[1]) - s.p[4] * t;
+        const double d2 = (x[2] - s.p[2]) - s.p[5] * t;
+        const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        return exp(-r2 / (2 * s.p[6] * s.p[6]));
+    }
+    case SOL_RADIAL_SIN: {
+        const double d0 = x[0] - s.p[0], d1 = x[1] - s.p[1], d2 = x[2] - s.p[2];
+        const double len = sqrt(d0 * d0 + (d1 * d1 + d2 * d2));
+        return sin(2 * 3.14159265358979323846 * (len - s.p[3] - t));
+    }
+    default: return 0.0;
+    }
+}
+
+__device__ __forceinline__ double sol_at_point(const DevOp& op, const DevSol& s, double t,
+                                               double et, const int ijk[3])
+{
+    const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+    return sol_at(s, t, et, x, ijk, 0, 0);
+}
+
+// ---- compensated FP32 pairs ("float-float", ~2^-46 relative) ------------------------------
+__device__ __forceinline__ float2 two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float e = b - (s - a);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 ff_add(float2 x, float2 y)
+{
+    float2 s = two_sum(x.x, y.x);
+    const float2 t = two_sum(x.y, y.y);
+    s.y += t.x;
+    s = fast_two_sum(s.x, s.y);
+    s.y += t.y;
+    return fast_two_sum(s.x, s.y);
+}
+__device__ __forceinline__ float2 ff_mul(float2 a, float b)
+{
+    const float p = a.x * b;
+    float e = fmaf(a.x, b, -p);
+    e = fmaf(a.y, b, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 ff_from_double(double d)
+{
+    const float hi = (float)d;
+    return make_float2(hi, (float)(d - (double)hi));
+}
+
+inline float2 ff_host(double d)
+{
+    const float hi = (float)d;
+    return make_float2(hi, (float)(d - (double)hi));
+}
+
+inline dim3 point_grid(const DevOp& op)
+{
+    return dim3(op.nzc, (op.it1 + BY - 1) / BY, op.it0);
+}
+
+// ===========================================================================================
+// Standalone operators
+// ===========================================================================================
+template <class T, bool PLUS>
+__global__ void __launch_bounds__(256) k_derivative(DevOp op, int dir, const T* __restrict__ u,
+                                                    const T* __restrict__ Rd,
+                                                    const double* __restrict__ nu,
+                                                    T* __restrict__ du)
+{
+    const Pt q = point_of(op);
+    const DevAxis& A = op.ax[dir];
+    const unsigned kind = q.valid ? (op.cls[q.p] >> (2 * dir)) & 3u : 0u;
+    const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+    if (kind == ROW_INTERIOR) {
+        if constexpr (sizeof(T) == 8) {
+            const double v = interior64(A, (const double*)u, q.p);
+            du[q.p] = PLUS ? du[q.p] + v : v;
+        } else {
+            const float v = interior32(A, (const float*)u, q.p);
+            du[q.p] = PLUS ? du[q.p] + v : v;
+        }
+    } else if (kind == ROW_CLOSURE) {
+        const double prev = PLUS ? (double)du[q.p] : 0.0;
+        du[q.p] = (T)closure64(A, row, q.p, u, Rd, nu, prev, !PLUS);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_laplacian(DevOp op, const T* __restrict__ u,
+                                                   const T* R0, const T* R1, const T* R2,
+                                                   const double* __restrict__ nu,
+                                                   T* __restrict__ du)
+{
+    const Pt q = point_of(op);
+    const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    const T* R[3] = {R0, R1, R2};
+    T acc = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) continue;
+        const unsigned kind = (c >> (2 * d)) & 3u;
+        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+        if (kind == ROW_INTERIOR) {
+            if constexpr (sizeof(T) == 8)
+                acc = acc + interior64(A, (const double*)u, q.p);
+            else
+                acc = acc + interior32(A, (const float*)u, q.p);
+        } else if (kind == ROW_CLOSURE) {
+            acc = (T)closure64(A, row, q.p, u, R[d], nu, (double)acc, false);
+        }
+    }
+    if (q.valid) du[q.p] = acc;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict__ u,
+                                                  const T* R0, const T* R1, const T* R2,
+                                                  T* o0, T* o1, T* o2)
+{
+    const Pt q = point_of(op);
+    const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    const T* R[3] = {R0, R1, R2};
+    T* out[3] = {o0, o1, o2};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) {
+            if (q.valid && out[d]) out[d][q.p] = 0;
+            continue;
+        }
+        const unsigned kind = (c >> (2 * d)) & 3u;
+        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+        T v = 0;
+        if (kind == ROW_INTERIOR) {
+            if constexpr (sizeof(T) == 8)
+                v = interior64(A, (const double*)u, q.p);
+            else
+                v = interior32(A, (const float*)u, q.p);
+        } else if (kind == ROW_CLOSURE) {
+            v = (T)closure64(A, row, q.p, u, R[d], (const double*)nullptr, 0.0, true);
+        }
+        if (q.valid) out[d][q.p] = v;
+    }
+}
+
+// R-space rows (Bf then Br of one derivative) accumulated into du.R_r (always +=)
+template <class T>
+__global__ void k_rspace(int nrows, const int* __restrict__ ru, const int* __restrict__ rc,
+                         const unsigned char* __restrict__ rs, const double* __restrict__ rw,
+                         const T* __restrict__ uD, const T* __restrict__ uR, T* __restrict__ duR)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrows) return;
+    double t = (double)duR[row];
+    for (int q = ru[row]; q < ru[row + 1]; q++) {
+        const double x = rs[q] ? (double)uR[rc[q]] : (double)uD[rc[q]];
+        t = fma(rw[q], x, t);
+    }
+    duR[row] = (T)t;
+}
+
+template <class T>
+cudaError_t rspace_for(const DevOp& op, int d, const void* uD, const void* const uR[3],
+                       void* const duR[3], cudaStream_t s)
+{
+    const DevAxis& A = op.ax[d];
+    for (int r = 0; r < 3; r++) {
+        if (A.rr_rows[r] == 0 || !A.rr_u[r]) continue;
+        const int n = A.rr_rows[r];
+        k_rspace<T><<<(n + 127) / 128, 128, 0, s>>>(n, A.rr_u[r], A.rr_col[r], A.rr_src[r],
+                                                   A.rr_w[r], (const T*)uD, (const T*)uR[r],
+                                                   (T*)duR[r]);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
+// ===========================================================================================
+// Fused RK4 stage kernels
+// ===========================================================================================
+struct StageArgs {
+    const void* s_in;
+    void* u0;
+    void* acc;
+    void* s_out;
+    const double* R[3];
+    double cf, ci;          // dt*rkf[s], dt*rki[s+1]
+    float2 cf_ff, ci_ff;    // same as compensated FP32 pairs
+    double t_stage, t_next; // RHS time and Dirichlet time of the stage output
+    double et_stage, et_next;
+};
+
+enum { SYS_HEAT = 0, SYS_WAVE = 1 };
+
+template <int SYS>
+__device__ __forceinline__ void wave_coef(const SysParams& sp, const DevOp& op, const Pt& q,
+                                          double g[3])
+{
+    if (sp.vel_kind == 0) {
+        g[0] = -sp.vel[0];
+        g[1] = -sp.vel[1];
+        g[2] = -sp.vel[2];
+    } else {
+        int ijk[3];
+        phys_ijk(op, q, ijk);
+        const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+        const double r[3] = {x[0] - sp.center[0], x[1] - sp.center[1], x[2] - sp.center[2]};
+        const double len = sqrt(r[0] * r[0] + (r[1] * r[1] + r[2] * r[2]));
+        g[0] = -r[0] / len;
+        g[1] = -r[1] / len;
+        g[2] = -r[2] / len;
+    }
+}
+
+// FP64 stage.  TIN: double (all stages).
+template <int STAGE, int SYS>
+__global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
+{
+    const Pt q = point_of(op);
+    const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    const double* __restrict__ in =
+        STAGE == 0 ? (const double*)sa.u0 : (const double*)sa.s_in;
+    double lap = 0.0;
+    double dd[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) continue;
+        const unsigned kind = (c >> (2 * d)) & 3u;
+        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+        if (SYS == SYS_HEAT) {
+            if (kind == ROW_INTERIOR)
+                lap = lap + interior64(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                lap = closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr, lap, false);
+        } else {
+            if (kind == ROW_INTERIOR)
+                dd[d] = interior64(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                dd[d] = closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr, 0.0, true);
+        }
+    }
+    if (!q.valid) return;
+    double rhs = 0.0;
+    if (c & 0x3Fu) {
+        if (SYS == SYS_HEAT) {
+            double src = 0.0;
+            if (sp.sol.kind == SOL_SINSIN) {
+                int ijk[3];
+                phys_ijk(op, q, ijk);
+                const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
+                src = (-u) - sp.k * (sp.sol.lapfac * u);
+            }
+            rhs = fma(lap, sp.k, src);
+        } else {
+            double g[3];
+            wave_coef<SYS>(sp, op, q, g);
+            rhs = fma(g[2], dd[2], fma(g[1], dd[1], g[0] * dd[0]));
+        }
+    }
+    double* __restrict__ u0 = (double*)sa.u0;
+    double* __restrict__ acc = (double*)sa.acc;
+    if (STAGE < 3) {
+        if (STAGE == 0)
+            acc[q.p] = sa.cf * rhs;
+        else
+            acc[q.p] = fma(sa.cf, rhs, acc[q.p]);
+        double un = fma(sa.ci, rhs, u0[q.p]);
+        if (c & CLS_DIRFACE) {
+            int ijk[3];
+            phys_ijk(op, q, ijk);
+            un = sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
+        }
+        ((double*)sa.s_out)[q.p] = un;
+    } else {
+        const double a = fma(sa.cf, rhs, acc[q.p]);
+        double un = u0[q.p] + a;
+        if (c & CLS_DIRFACE) {
+            int ijk[3];
+            phys_ijk(op, q, ijk);
+            un = sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
+        }
+        u0[q.p] = un;
+    }
+}
+
+// Mixed stage: FP32 stage field and interior stencils, FP64 closure rows, compensated
+// FP32-pair solution (u0) and accumulator.  Stage 0 reads u0 (float2) as its input.
+template <int STAGE, int SYS>
+__global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, StageArgs sa)
+{
+    const Pt q = point_of(op);
+    const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    float lap = 0.f;
+    float dd[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) continue;
+        const unsigned kind = (c >> (2 * d)) & 3u;
+        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+        float v = 0.f;
+        if (STAGE == 0) {
+            const float2* in = (const float2*)sa.u0;
+            if (kind == ROW_INTERIOR)
+                v = interior32(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                v = (float)closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr,
+                                     SYS == SYS_HEAT ? (double)lap : 0.0, SYS != SYS_HEAT);
+        } else {
+            const float* in = (const float*)sa.s_in;
+            if (kind == ROW_INTERIOR)
+                v = interior32(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                v = (float)closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr,
+                                     SYS == SYS_HEAT ? (double)lap : 0.0, SYS != SYS_HEAT);
+        }
+        if (SYS == SYS_HEAT)
+            lap = (kind == ROW_CLOSURE) ? v : lap + v;
+        else
+            dd[d] = v;
+    }
+    if (!q.valid) return;
+    float rhs = 0.f;
+    if (c & 0x3Fu) {
+        if (SYS == SYS_HEAT) {
+            float src = 0.f;
+            if (sp.sol.kind == SOL_SINSIN) {
+                int ijk[3];
+                phys_ijk(op, q, ijk);
+                const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
+                src = (float)((-u) - sp.k * (sp.sol.lapfac * u));
+            }
+            rhs = fmaf(lap, (float)sp.k, src);
+        } else {
+            double g[3];
+            wave_coef<SYS>(sp, op, q, g);
+            rhs = fmaf((float)g[2], dd[2], fmaf((float)g[1], dd[1], (float)g[0] * dd[0]));
+        }
+    }
+    float2* __restrict__ u0 = (float2*)sa.u0;
+    float2* __restrict__ acc = (float2*)sa.acc;
+    const float2 u = u0[q.p];
+    if (STAGE < 3) {
+        const float2 inc = ff_mul(sa.cf_ff, rhs);
+        acc[q.p] = STAGE == 0 ? inc : ff_add(acc[q.p], inc);
+        float un = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
+        if (c & CLS_DIRFACE) {
+            int ijk[3];
+            phys_ijk(op, q, ijk);
+            un = (float)sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
+        }
+        ((float*)sa.s_out)[q.p] = un;
+    } else {
+        const float2 a = ff_add(acc[q.p], ff_mul(sa.cf_ff, rhs));
+        float2 un = ff_add(u, a);
+        if (c & CLS_DIRFACE) {
+            int ijk[3];
+            phys_ijk(op, q, ijk);
+            un = ff_from_double(sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk));
+        }
+        u0[q.p] = un;
+    }
+}
+
+// Dirichlet cut-point values at t+dt/2 and t+dt (update_boundary on R)
+__global__ void k_bc_r(DevR dr, DevSol sol, int n, int d, double t1, double et1, double t2,
+                       double et2, double* out1, double* out2, const double* keep)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (dr.dirichlet[d][i]) {
+        const double* x = dr.pos[d] + 3 * (long long)i;
+        out1[i] = sol_at(sol, t1, et1, x, nullptr, d, i);
+        out2[i] = sol_at(sol, t2, et2, x, nullptr, d, i);
+    } else {
+        out1[i] = keep[i];
+        out2[i] = keep[i];
+    }
+}
+
+// one RHS evaluation into an FP64 field (system::rhs)
+template <int SYS, bool MIXED>
+__global__ void __launch_bounds__(256) k_rhs(DevOp op, SysParams sp, const void* uin,
+                                             const double* R0, const double* R1,
+                                             const double* R2, double t, double et,
+                                             double* out)
+{
+    const Pt q = point_of(op);
+    const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    const double* R[3] = {R0, R1, R2};
+    double lap = 0.0, dd[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) continue;
+        const unsigned kind = (c >> (2 * d)) & 3u;
+        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+        double v = 0.0;
+        if (MIXED) {
+            const float2* in = (const float2*)uin;
+            if (kind == ROW_INTERIOR) v = (double)interior32(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr,
+                              SYS == SYS_HEAT ? lap : 0.0, SYS != SYS_HEAT);
+        } else {
+            const double* in = (const double*)uin;
+            if (kind == ROW_INTERIOR) v = interior64(A, in, q.p);
+            else if (kind == ROW_CLOSURE)
+                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr,
+                              SYS == SYS_HEAT ? lap : 0.0, SYS != SYS_HEAT);
+        }
+        if (SYS == SYS_HEAT)
+            lap = (kind == ROW_CLOSURE) ? v : lap + v;
+        else
+            dd[d] = v;
+    }
+    if (!q.valid) return;
+    double rhs = 0.0;
+    if (c & 0x3Fu) {
+        if (SYS == SYS_HEAT) {
+            double src = 0.0;
+            if (sp.sol.kind == SOL_SINSIN) {
+                int ijk[3];
+                phys_ijk(op, q, ijk);
+                const double u = sol_at_point(op, sp.sol, t, et, ijk);
+                src = (-u) - sp.k * (sp.sol.lapfac * u);
+            }
+            rhs = fma(lap, sp.k, src);
+        } else {
+            double g[3];
+            wave_coef<SYS>(sp, op, q, g);
+            rhs = fma(g[2], dd[2], fma(g[1], dd[1], g[0] * dd[0]));
+        }
+    }
+    out[q.p] = rhs;
+}
+
+// initialize_scalar_field: 0 on non-fluid D points, exact on fluid D points
+__global__ void __launch_bounds__(256) k_init(DevOp op, DevSol sol, double t, double et,
+                                              int mixed, void* u0)
+{
+    const Pt q = point_of(op);
+    if (!q.valid) return;
+    const unsigned c = op.cls[q.p];
+    double v = 0.0;
+    if (c & CLS_FLUID) {
+        int ijk[3];
+        phys_ijk(op, q, ijk);
+        v = sol_at_point(op, sol, t, et, ijk);
+    }
+    if (mixed)
+        ((float2*)u0)[q.p] = ff_from_double(v);
+    else
+        ((double*)u0)[q.p] = v;
+}
+
+__global__ void k_init_r(DevR dr, DevSol sol, int n, int d, double t, double et, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = sol_at(sol, t, et, dr.pos[d] + 3 * (long long)i, nullptr, d, i);
+}
+
+__global__ void k_convert(long long n, int to_mixed, const double* in_d, float2* out_m,
+                          const float2* in_m, double* out_d)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (to_mixed)
+        out_m[i] = ff_from_double(in_d[i]);
+    else {
+        const float2 v = in_m[i];
+        out_d[i] = (double)v.x + (double)v.y;
+    }
+}
+
+// stats over fluid D points: per block max error (+index), min, max
+struct StatPart {
+    double err;
+    long long idx;
+    double mn, mx;
+};
+
+__global__ void __launch_bounds__(256) k_stats(DevOp op, DevSol sol, double t, double et,
+                                               int mixed, const void* u0, StatPart* parts)
+{
+    const Pt q = point_of(op);
+    StatPart s{-1.0, 0, 1e308, -1e308};
+    if (q.valid && (op.cls[q.p] & CLS_FLUID)) {
+        const double u = mixed ? ldd((const float2*)u0, q.p) : ((const double*)u0)[q.p];
+        int ijk[3];
+        phys_ijk(op, q, ijk);
+        const double e = fabs(u - sol_at_point(op, sol, t, et, ijk));
+        s = StatPart{e, q.p, u, u};
+    }
+    __shared__ StatPart sh[256];
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    sh[tid] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (tid < w) {
+            StatPart o = sh[tid + w];
+            StatPart& m = sh[tid];
+            if (o.err > m.err || (o.err == m.err && o.err >= 0 && o.idx < m.idx)) {
+                m.err = o.err;
+                m.idx = o.idx;
+            }
+            m.mn = fmin(m.mn, o.mn);
+            m.mx = fmax(m.mx, o.mx);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const long long b =
+            ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        parts[b] = sh[0];
+    }
+}
+
+__global__ void k_stats_final(long long nparts, const StatPart* parts, double* out)
+{
+    __shared__ StatPart sh[256];
+    StatPart s{-1.0, 0, 1e308, -1e308};
+    for (long long i = threadIdx.x; i < nparts; i += 256) {
+        const StatPart o = parts[i];
+        if (o.err > s.err || (o.err == s.err && o.err >= 0 && o.idx < s.idx)) {
+            s.err = o.err;
+            s.idx = o.idx;
+        }
+        s.mn = fmin(s.mn, o.mn);
+        s.mx = fmax(s.mx, o.mx);
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            StatPart o = sh[threadIdx.x + w];
+            StatPart& m = sh[threadIdx.x];
+            if (o.err > m.err || (o.err == m.err && o.err >= 0 && o.idx < m.idx)) {
+                m.err = o.err;
+                m.idx = o.idx;
+            }
+            m.mn = fmin(m.mn, o.mn);
+            m.mx = fmax(m.mx, o.mx);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0].err < 0 ? 0.0 : sh[0].err;
+        out[1] = (double)sh[0].idx;
+        out[2] = sh[0].mn;
+        out[3] = sh[0].mx;
+    }
+}
+
+} // namespace
+
+long long kernel_launch_count() { return g_launches.load(); }
+
+// ===========================================================================================
+// launchers
+// ===========================================================================================
+cudaError_t launch_derivative(const DevOp& op, int dir, int prec, const void* uD,
+                              const void* uR, const double* nuD, void* duD, void* const duR[3],
+                              const void* const uRall[3], int plus_eq, cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    if (!op.ax[dir].active) return cudaSuccess;
+    if (prec == PREC_FP64) {
+        if (plus_eq)
+            k_derivative<double, true><<<grid, block, 0, s>>>(op, dir, (const double*)uD,
+                                                              (const double*)uR, nuD,
+                                                              (double*)duD);
+        else
+            k_derivative<double, false><<<grid, block, 0, s>>>(op, dir, (const double*)uD,
+                                                               (const double*)uR, nuD,
+                                                               (double*)duD);
+        ++g_launches;
+        return rspace_for<double>(op, dir, uD, uRall, duR, s);
+    }
+    if (plus_eq)
+        k_derivative<float, true><<<grid, block, 0, s>>>(op, dir, (const float*)uD,
+                                                         (const float*)uR, nuD, (float*)duD);
+    else
+        k_derivative<float, false><<<grid, block, 0, s>>>(op, dir, (const float*)uD,
+                                                          (const float*)uR, nuD, (float*)duD);
+    ++g_launches;
+    return rspace_for<float>(op, dir, uD, uRall, duR, s);
+}
+
+cudaError_t launch_laplacian(const DevOp& op, int prec, const void* uD, const void* const uR[3],
+                             const double* nuD, void* duD, void* const duR[3], cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const size_t es = prec == PREC_FP64 ? 8 : 4;
+    for (int r = 0; r < 3; r++)
+        if (op.nR[r] && duR[r]) cudaMemsetAsync(duR[r], 0, op.nR[r] * es, s);
+    if (prec == PREC_FP64) {
+        k_laplacian<double><<<grid, block, 0, s>>>(op, (const double*)uD, (const double*)uR[0],
+                                                   (const double*)uR[1], (const double*)uR[2],
+                                                   nuD, (double*)duD);
+        ++g_launches;
+        for (int d = 0; d < 3; d++)
+            if (op.ax[d].active) rspace_for<double>(op, d, uD, uR, duR, s);
+    } else {
+        k_laplacian<float><<<grid, block, 0, s>>>(op, (const float*)uD, (const float*)uR[0],
+                                                  (const float*)uR[1], (const float*)uR[2], nuD,
+                                                  (float*)duD);
+        ++g_launches;
+        for (int d = 0; d < 3; d++)
+            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, duR, s);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const void* const uR[3],
+                            void* const out[3][4], cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const size_t es = prec == PREC_FP64 ? 8 : 4;
+    for (int d = 0; d < 3; d++)
+        for (int r = 0; r < 3; r++)
+            if (op.nR[r] && out[d][r + 1]) cudaMemsetAsync(out[d][r + 1], 0, op.nR[r] * es, s);
+    if (prec == PREC_FP64) {
+        k_gradient<double><<<grid, block, 0, s>>>(
+            op, (const double*)uD, (const double*)uR[0], (const double*)uR[1],
+            (const double*)uR[2], (double*)out[0][0], (double*)out[1][0], (double*)out[2][0]);
+        ++g_launches;
+        for (int d = 0; d < 3; d++) {
+            void* const dR[3] = {out[d][1], out[d][2], out[d][3]};
+            if (op.ax[d].active) rspace_for<double>(op, d, uD, uR, dR, s);
+        }
+    } else {
+        k_gradient<float><<<grid, block, 0, s>>>(
+            op, (const float*)uD, (const float*)uR[0], (const float*)uR[1], (const float*)uR[2],
+            (float*)out[0][0], (float*)out[1][0], (float*)out[2][0]);
+        ++g_launches;
+        for (int d = 0; d < 3; d++) {
+            void* const dR[3] = {out[d][1], out[d][2], out[d][3]};
+            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, dR, s);
+        }
+    }
+    return cudaGetLastError();
+}
+
+namespace
+{
+template <int SYS>
+void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[4],
+                   cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    if (prec == PREC_FP64) {
+        k_stage64<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
+        k_stage64<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
+        k_stage64<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
+        k_stage64<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
+    } else {
+        k_stage_mixed<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
+        k_stage_mixed<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
+        k_stage_mixed<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
+        k_stage_mixed<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
+    }
+    g_launches += 4;
+}
+} // namespace
+
+cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
+                            StepBuffers& b, double t, double dt, cudaStream_t s)
+{
+    // src/temporal/rk4.cpp:11-12
+    constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
+    constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    const bool sinsin = sp.sol.kind == SOL_SINSIN;
+    auto et = [&](double tt) { return sinsin ? std::exp(-tt) : 0.0; };
+
+    const double th = t + dt * rki[1], tf = t + dt * rki[3];
+    for (int d = 0; d < 3; d++) {
+        const int n = (int)op.nR[d];
+        if (!n) continue;
+        k_bc_r<<<(n + 127) / 128, 128, 0, s>>>(dr, sp.sol, n, d, th, et(th), tf, et(tf),
+                                               b.Rhalf[d], b.Rfull[d], b.R[d]);
+        ++g_launches;
+    }
+    StageArgs sa[4];
+    for (int i = 0; i < 4; i++) {
+        StageArgs& a = sa[i];
+        a.u0 = b.u0;
+        a.acc = b.acc;
+        a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
+        a.s_out = i == 1 ? b.sb : b.sa;
+        for (int d = 0; d < 3; d++)
+            a.R[d] = i == 0 ? b.R[d] : (i == 3 ? b.Rfull[d] : b.Rhalf[d]);
+        a.cf = dt * rkf[i];
+        a.ci = i < 3 ? dt * rki[i + 1] : 1.0;
+        a.cf_ff = ff_host(a.cf);
+        a.ci_ff = ff_host(a.ci);
+        a.t_stage = t + dt * rki[i];
+        a.t_next = i < 3 ? t + dt * rki[i + 1] : t + dt;
+        a.et_stage = et(a.t_stage);
+        a.et_next = et(a.t_next);
+    }
+    if (sp.kind == SYS_HEAT)
+        launch_stages<SYS_HEAT>(op, sp, prec, sa, s);
+    else
+        launch_stages<SYS_WAVE>(op, sp, prec, sa, s);
+    for (int d = 0; d < 3; d++) std::swap(b.R[d], b.Rfull[d]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
+                       double t, double* out, double* const outR[3], cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    if (sp.kind == SYS_HEAT) {
+        if (prec == PREC_FP64)
+            k_rhs<SYS_HEAT, false><<<grid, block, 0, s>>>(op, sp, b.u0, b.R[0], b.R[1], b.R[2], t,
+                                                          et, out);
+        else
+            k_rhs<SYS_HEAT, true><<<grid, block, 0, s>>>(op, sp, b.u0, b.R[0], b.R[1], b.R[2], t,
+                                                         et, out);
+    } else {
+        if (prec == PREC_FP64)
+            k_rhs<SYS_WAVE, false><<<grid, block, 0, s>>>(op, sp, b.u0, b.R[0], b.R[1], b.R[2], t,
+                                                          et, out);
+        else
+            k_rhs<SYS_WAVE, true><<<grid, block, 0, s>>>(op, sp, b.u0, b.R[0], b.R[1], b.R[2], t,
+                                                         et, out);
+    }
+    ++g_launches;
+    // Dirichlet cut points carry a zero right-hand side (heat.cpp:269-284; the wave's gG
+    // is zeroed there, scalar_wave.cpp:86-95)
+    for (int d = 0; d < 3; d++)
+        if (op.nR[d] && outR[d]) cudaMemsetAsync(outR[d], 0, op.nR[d] * sizeof(double), s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
+                              double t, void* u0, double* const R[3], cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const double et = sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    k_init<<<grid, block, 0, s>>>(op, sol, t, et, prec == PREC_MIXED, u0);
+    ++g_launches;
+    for (int d = 0; d < 3; d++) {
+        const int n = (int)op.nR[d];
+        if (!n) continue;
+        k_init_r<<<(n + 127) / 128, 128, 0, s>>>(dr, sol, n, d, t, et, R[d]);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_convert(long long n, int to_mixed, const double* in_d, void* out,
+                                 const void* in_m, double* out_d, cudaStream_t s)
+{
+    const int bs = 256;
+    const long long nb = (n + bs - 1) / bs;
+    k_convert<<<(unsigned)nb, bs, 0, s>>>(n, to_mixed, in_d, (float2*)out, (const float2*)in_m,
+                                          out_d);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stats(const DevOp& op, const DevR&, const DevSol& sol, int prec,
+                         const void* u0, double* const*, double t, double* dev_out,
+                         cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const long long nparts = (long long)grid.x * grid.y * grid.z;
+    StatPart* parts = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&parts, nparts * sizeof(StatPart), s);
+    if (e != cudaSuccess) return e;
+    const double et = sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    k_stats<<<grid, block, 0, s>>>(op, sol, t, et, prec == PREC_MIXED, u0, parts);
+    k_stats_final<<<1, 256, 0, s>>>(nparts, parts, dev_out);
+    g_launches += 2;
+    cudaFreeAsync(parts, s);
+    return cudaGetLastError();
+}
+
+} // namespace sgb

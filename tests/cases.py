@@ -1,0 +1,64 @@
+"""Problem configurations shared by the parity tests.
+
+Each case is a dict accepted by both shoccs_gb300.Problem and oracle.OracleProblem.
+"""
+import numpy as np
+
+DIR, FLT, NEU = "dirichlet", "floating", "neumann"
+
+
+def random_spheres(n_spheres, seed, lo=0.15, hi=0.85, rmin=0.03, rmax=0.08, gap=0.0, bcs=(DIR,)):
+    """Seeded non-overlapping spheres (rejection sampling with a clearance `gap`)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n_spheres:
+        c = rng.uniform(lo, hi, 3)
+        r = rng.uniform(rmin, rmax)
+        if all(np.linalg.norm(c - np.array(c2)) > r + r2 + gap for c2, r2, _ in out):
+            out.append((tuple(float(v) for v in c), float(r), bcs[len(out) % len(bcs)]))
+    return out
+
+
+def cases():
+    return {
+        # configuration 0 of the benchmark: 2-D heat, circle, E4_2, Dirichlet walls
+        "c0_circle_2d": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                             spheres=[((0.51, 0.49, 0.0), 0.2, DIR)],
+                             grid_bc=(DIR, DIR, DIR, DIR, FLT, FLT), scheme="E4_2"),
+        # small copy of the 3-D wave configuration: sphere r=0.3, inflow faces Dirichlet
+        "wave_sphere_3d": dict(n=(40, 38, 42), lo=(0, 0, 0), hi=(1, 1, 1),
+                               spheres=[((0.5, 0.5, 0.5), 0.22, DIR)],
+                               grid_bc=(DIR, FLT, DIR, FLT, DIR, FLT), scheme="E4_1",
+                               alpha=(0.1, 0.7)),
+        # the domain and sphere of the reference's geometry test (object_geometry.t.cpp:16-31)
+        # on a finer grid, so that the wall-to-sphere segments hold both closures
+        "ref_geometry_mesh": dict(n=(41, 44, 61), lo=(-1, -1, 0), hi=(1, 2, 2.2),
+                                  spheres=[((0.01, -0.01, 0.5), 0.25, DIR)],
+                                  grid_bc=(DIR, DIR, FLT, FLT, DIR, FLT), scheme="E4_2"),
+        # Floating object: cross-direction interpolation rows (E4_2)
+        "floating_sphere_e42": dict(n=(21, 19, 23), lo=(-1, -1, -1), hi=(1, 1, 1),
+                                    spheres=[((0.1, -0.05, 0.02), 0.45, FLT)],
+                                    grid_bc=(FLT, DIR, DIR, FLT, FLT, FLT), scheme="E4_2"),
+        # E2_2 with Neumann faces and a Floating object
+        "neumann_e22": dict(n=(17, 18, 16), lo=(0, 0, 0), hi=(1, 1, 1),
+                            spheres=[((0.45, 0.52, 0.5), 0.27, FLT)],
+                            grid_bc=(NEU, FLT, FLT, NEU, DIR, FLT), scheme="E2_2"),
+        # several seeded spheres, E4_1 (Dirichlet objects)
+        "multi_sphere_e41": dict(n=(64, 60, 66), lo=(0, 0, 0), hi=(1, 1, 1),
+                                 spheres=random_spheres(5, 20261204, lo=0.3, hi=0.7,
+                                                        rmin=0.04, rmax=0.07, gap=0.18),
+                                 grid_bc=(FLT, FLT, DIR, FLT, FLT, DIR), scheme="E4_1",
+                                 alpha=(0.1, 0.7)),
+        # several seeded spheres, E4_2, Dirichlet and Floating objects
+        "multi_sphere_e42": dict(n=(48, 44, 50), lo=(0, 0, 0), hi=(1, 1, 1),
+                                 spheres=random_spheres(5, 7, lo=0.25, hi=0.75, rmin=0.05,
+                                                        rmax=0.09, gap=0.12, bcs=(DIR, FLT)),
+                                 grid_bc=(DIR, DIR, FLT, FLT, DIR, DIR), scheme="E4_2"),
+        # no objects at all, all-Floating walls
+        "plain_box_e42": dict(n=(12, 9, 40), lo=(0, 0, 0), hi=(1, 2, 3), spheres=[],
+                              grid_bc=(FLT,) * 6, scheme="E4_2"),
+        # 1-D line
+        "line_1d_e41": dict(n=(64, 1, 1), lo=(0, 0, 0), hi=(1, 0, 0), spheres=[],
+                            grid_bc=(DIR, FLT, FLT, FLT, FLT, FLT), scheme="E4_1",
+                            alpha=(0.1, 0.7)),
+    }

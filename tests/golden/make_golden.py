@@ -1,0 +1,124 @@
+"""Generate the golden fixtures that pin the oracle (run in a container that has the
+reference tree; the fixtures are committed and used on machines that do not).
+
+Sources:
+  * src/mesh/object_geometry.t.cpp:11-330 ("sphere intersections"): expected cut-point
+    positions, solid coordinates and psi per axis, parsed from the reference test file as
+    text -> object_geometry_sphere.json
+  * oracle/_ref/libshoccs_ref.so: the reference's own src/stencils/{E2_2,E4_2,E4_1}.cpp and
+    src/mesh/sphere.cpp compiled unmodified by oracle/build_ref.sh -> stencils_ref.json
+    (closure blocks, interior rows, interpolants) and sphere_hits_ref.json (ray/sphere hits)
+
+Usage: python tests/golden/make_golden.py [reference_root]
+"""
+import ctypes
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SHOCCS_REFERENCE_ROOT",
+                                                             "/root/reference")
+
+
+def parse_sphere_intersections():
+    src = open(os.path.join(REF, "src/mesh/object_geometry.t.cpp")).read()
+    start = src.index('TEST_CASE("sphere intersections")')
+    end = src.index('TEST_CASE("rect_intersections")')
+    body = src[start:end]
+    out = {}
+    sections = re.split(r'SECTION\("([XYZxyz])"\)', body)
+    # sections = [pre, name1, text1, name2, text2, ...]
+    for name, text in zip(sections[1::2], sections[2::2]):
+        def grab(var):
+            m = re.search(r"\b%s\s*=\s*\{(.*?)\};" % var, text, re.S)
+            return m.group(1) if m else None
+        nums = lambda s: [float(v) for v in re.findall(r"-?\d+\.?\d*(?:e-?\d+)?", s)]
+        exact = nums(grab("exact"))
+        sc = [int(v) for v in re.findall(r"-?\d+", grab("sc"))]
+        psi = nums(grab("psi"))
+        out[name.lower()] = dict(position=exact, solid_coord=sc, psi=psi)
+    return dict(
+        source="src/mesh/object_geometry.t.cpp:11-330",
+        mesh=dict(n=[21, 22, 23], lo=[-1, -1, 0], hi=[1, 2, 2.2]),
+        sphere=dict(center=[0.01, -0.01, 0.5], radius=0.25),
+        tolerance=dict(position_abs=1e-14, psi_rel=1.1920929e-05 * 100),
+        axes=out,
+    )
+
+
+def ref_fixtures():
+    subprocess.check_call([os.path.join(REPO, "oracle", "build_ref.sh")])
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libshoccs_ref.so"))
+    D = ctypes.c_double
+    alpha = (D * 2)(0.1, 0.7)
+    nbs = []
+    rt = {0: {0: 4, 1: 8, 2: 8}, 1: {0: 10, 1: 15, 2: 15}, 2: {0: 28, 1: 35}}
+    rng = np.random.default_rng(20261203)
+    psis = [1e-12, 1e-5, 0.01, 0.25, 0.5, 0.75, 0.9, 0.999, 1.0 - 1e-12, 1.0]
+    psis += list(rng.uniform(0.0, 1.0, 6))
+    for scheme, bcs in rt.items():
+        for bc, n in bcs.items():
+            for psi in psis:
+                for right in (0, 1):
+                    for h in (2.0, 1.0 / 64, 0.1):
+                        c, x = (D * 64)(), (D * 8)()
+                        lib.ref_stencil_nbs(scheme, alpha, D(h), bc, D(psi), right, c, x)
+                        nbs.append(dict(scheme=scheme, bc=bc, psi=float(psi), right=right,
+                                        h=h, c=[float(v).hex() for v in c[:n]],
+                                        x=[float(v).hex() for v in x[:3]]))
+    interior = []
+    for scheme in (0, 1, 2):
+        for h in (2.0, 1.0 / 64, 1.0 / 255):
+            c = (D * 8)()
+            n = lib.ref_stencil_interior(scheme, alpha, D(h), c)
+            interior.append(dict(scheme=scheme, h=h, c=[float(v).hex() for v in c[:n]]))
+    interp = []
+    for scheme in (0, 1):
+        for y in (-0.7, -0.3, 0.0, 0.2, 0.5, 0.9):
+            c = (D * 8)()
+            n = lib.ref_stencil_interp_interior(scheme, D(y), c)
+            interp.append(dict(kind="interior", scheme=scheme, y=y, c=[float(v).hex() for v in c[:n]]))
+            for i in (0, 1, 2):
+                for psi in (0.1, 0.5, 0.95):
+                    for right in (0, 1):
+                        c = (D * 8)()
+                        n = lib.ref_stencil_interp_wall(scheme, i, D(y), D(psi), right, c)
+                        interp.append(dict(kind="wall", scheme=scheme, i=i, y=y, psi=psi,
+                                           right=right, c=[float(v).hex() for v in c[:n]]))
+    hits = []
+    for _ in range(400):
+        center = rng.uniform(-0.5, 1.5, 3)
+        radius = float(rng.uniform(0.05, 0.6))
+        axis = int(rng.integers(0, 3))
+        origin = center + rng.uniform(-1.2 * radius, 1.2 * radius, 3)
+        origin[axis] = center[axis] - rng.uniform(0.0, 1.5)
+        direction = [0.0, 0.0, 0.0]
+        direction[axis] = 1.0
+        t, pos, ro, nrm = D(), (D * 3)(), ctypes.c_int(), (D * 3)()
+        ok = lib.ref_sphere_hit((D * 3)(*center), D(radius), (D * 3)(*origin),
+                                (D * 3)(*direction), D(0.0), D(3.0), ctypes.byref(t), pos,
+                                ctypes.byref(ro), nrm)
+        hits.append(dict(center=[float(v).hex() for v in center], radius=radius.hex(),
+                         origin=[float(v).hex() for v in origin], axis=axis, hit=ok,
+                         t=t.value.hex(), pos=[v.hex() for v in pos], ray_outside=ro.value,
+                         normal=[v.hex() for v in nrm]))
+    return (dict(source="src/stencils/{E2_2,E4_2,E4_1}.cpp via oracle/_ref", alpha=[0.1, 0.7],
+                 nbs=nbs, interior=interior, interp=interp),
+            dict(source="src/mesh/sphere.cpp via oracle/_ref", hits=hits))
+
+
+if __name__ == "__main__":
+    with open(os.path.join(HERE, "object_geometry_sphere.json"), "w") as f:
+        json.dump(parse_sphere_intersections(), f, indent=1)
+    st, hits = ref_fixtures()
+    with open(os.path.join(HERE, "stencils_ref.json"), "w") as f:
+        json.dump(st, f)
+    with open(os.path.join(HERE, "sphere_hits_ref.json"), "w") as f:
+        json.dump(hits, f)
+    print("wrote fixtures to", HERE)

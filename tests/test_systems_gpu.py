@@ -1,0 +1,186 @@
+"""Heat and scalar-wave systems: right-hand side and fused RK4 time stepping against the
+oracle (the reference's rk4::operator() over heat / scalar_wave), plus the MMS accuracy
+of the mixed-precision path.
+
+Tolerances (relative max-norm against the oracle's FP64 result):
+  FP64 RHS                      1e-12
+  FP64 RK4, n steps             1e-11   (per-step rounding differences accumulate)
+  MIXED RK4 vs FP64 oracle      2e-5    (FP32 stage fields and interior stencils)
+  MIXED MMS error               <= 1.1 x FP64 MMS error (equal-accuracy criterion)
+"""
+import math
+
+import numpy as np
+import pytest
+
+import shoccs_gb300 as S
+from oracle.oracle import OracleProblem
+from tests.cases import cases
+
+CASES = cases()
+HEAT_CASE = CASES["c0_circle_2d"]
+WAVE_CASE = CASES["wave_sphere_3d"]
+# u_t + a.grad u = 0, Gaussian pulse (x0, a, sigma)
+PULSE = [0.3, 0.3, 0.3, 1.0, 0.7, 0.4, 0.08]
+VEL = (1.0, 0.7, 0.4)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def rel_err(got, want):
+    want = np.asarray(want)
+    if want.size == 0:
+        return 0.0
+    return float(np.abs(np.asarray(got) - want).max() / max(np.abs(want).max(), 1e-300))
+
+
+def get_state(sys_, o):
+    u = [np.zeros(o.size)] + [np.zeros(n) for n in o.nR]
+    sys_.get_state(S.ScalarField(*u))
+    return u
+
+
+def set_state(sys_, u):
+    sys_.set_state(S.ScalarField(*[np.ascontiguousarray(a) for a in u]))
+
+
+def heat_dt(o, cfl=0.4, k=1.0):
+    h = 1.0 / (o.n[0] - 1)
+    return cfl * h * h / (4 * k)
+
+
+@pytest.mark.gpu
+def test_heat_rhs_fp64():
+    torch = _torch()
+    p, o = S.Problem(**HEAT_CASE), OracleProblem(**HEAT_CASE)
+    sol = [1.0]
+    u = o.initialize(1, sol, 0.0)
+    rng = np.random.default_rng(3)
+    u = [a + 0.01 * rng.standard_normal(a.shape) for a in u]
+    for t in (0.0, 0.013):
+        want = o.heat_rhs(1.0, 1, sol, t, u)
+        h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, sol)
+        set_state(h, u)
+        got = p.zeros(torch.float64)
+        h.rhs(t, got)
+        assert rel_err(got.D.cpu().numpy(), want[0]) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_wave_rhs_fp64():
+    torch = _torch()
+    p, o = S.Problem(**WAVE_CASE), OracleProblem(**WAVE_CASE)
+    u = o.initialize(2, PULSE, 0.0)
+    for vel_kind, center in ((S.VEL_CONSTANT, (0, 0, 0)), (S.VEL_RADIAL, (0.5, 0.5, 0.5))):
+        want = o.wave_rhs(vel_kind, VEL, center, u)
+        w = S.ScalarWave(p, S.PREC_FP64, vel_kind, VEL, center, S.SOL_GAUSS_PULSE, PULSE)
+        set_state(w, u)
+        got = p.zeros(torch.float64)
+        w.rhs(0.0, got)
+        assert rel_err(got.D.cpu().numpy(), want[0]) <= 1e-12, vel_kind
+
+
+@pytest.mark.gpu
+def test_heat_rk4_fp64_matches_oracle():
+    p, o = S.Problem(**HEAT_CASE), OracleProblem(**HEAT_CASE)
+    sol, dt, n = [1.0], heat_dt(o), 25
+    u0 = o.initialize(1, sol, 0.0)
+    want = o.heat_rk4(1.0, 1, sol, 0.0, dt, n, u0)
+    h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, sol)
+    h.initialize(0.0)
+    got0 = get_state(h, o)
+    for a, b in zip(got0, u0):
+        assert rel_err(a, b) <= 1e-15
+    h.rk4(0.0, dt, n)
+    got = get_state(h, o)
+    assert rel_err(got[0], want[0]) <= 1e-11
+    for d in range(3):
+        assert rel_err(got[1 + d], want[1 + d]) <= 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vel_kind", [S.VEL_CONSTANT, S.VEL_RADIAL])
+def test_wave_rk4_fp64_matches_oracle(vel_kind):
+    p, o = S.Problem(**WAVE_CASE), OracleProblem(**WAVE_CASE)
+    center = (0.5, 0.5, 0.5)
+    if vel_kind == S.VEL_CONSTANT:
+        sol_kind, sol = 2, PULSE
+    else:
+        sol_kind, sol = 3, [0.5, 0.5, 0.5, 0.22]
+    h = 1.0 / (min(o.n) - 1)
+    dt, n = 0.5 * h, 12
+    u0 = o.initialize(sol_kind, sol, 0.0)
+    want = o.wave_rk4(vel_kind, VEL, center, sol_kind, sol, 0.0, dt, n, u0)
+    w = S.ScalarWave(p, S.PREC_FP64, vel_kind, VEL, center, sol_kind, sol)
+    w.initialize(0.0)
+    w.rk4(0.0, dt, n)
+    got = get_state(w, o)
+    assert rel_err(got[0], want[0]) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_mixed_rk4_close_to_fp64_oracle():
+    p, o = S.Problem(**WAVE_CASE), OracleProblem(**WAVE_CASE)
+    h = 1.0 / (min(o.n) - 1)
+    dt, n = 0.5 * h, 12
+    u0 = o.initialize(2, PULSE, 0.0)
+    want = o.wave_rk4(S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE, 0.0, dt, n, u0)
+    w = S.ScalarWave(p, S.PREC_MIXED, S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE)
+    w.initialize(0.0)
+    w.rk4(0.0, dt, n)
+    got = get_state(w, o)
+    assert rel_err(got[0], want[0]) <= 2e-5
+
+
+@pytest.mark.gpu
+def test_config0_heat_mms_error_and_mixed_equal_accuracy():
+    """2-D heat, circle, E4_2, sin(2 pi x) sin(2 pi y) exp(-t), dt = 0.1 h^2, 100 steps."""
+    p, o = S.Problem(**HEAT_CASE), OracleProblem(**HEAT_CASE)
+    sol, dt, n = [1.0], heat_dt(o), 100
+    t_end = n * dt
+    errs = {}
+    for prec in (S.PREC_FP64, S.PREC_MIXED):
+        hs = S.Heat(p, 1.0, prec, S.SOL_SINSIN, sol)
+        hs.initialize(0.0)
+        hs.rk4(0.0, dt, n)
+        stats, valid = hs.stats(t_end)
+        assert valid
+        errs[prec] = stats[0]
+    u0 = o.initialize(1, sol, 0.0)
+    want = o.heat_rk4(1.0, 1, sol, 0.0, dt, n, u0)
+    ostats = o.stats(1, sol, t_end, want)
+    assert errs[S.PREC_FP64] == pytest.approx(ostats[0], rel=1e-9)
+    assert errs[S.PREC_FP64] < 1e-3
+    assert errs[S.PREC_MIXED] <= 1.1 * errs[S.PREC_FP64]
+
+
+@pytest.mark.gpu
+def test_stats_match_oracle():
+    p, o = S.Problem(**WAVE_CASE), OracleProblem(**WAVE_CASE)
+    w = S.ScalarWave(p, S.PREC_FP64, S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE)
+    w.initialize(0.0)
+    h = 1.0 / (min(o.n) - 1)
+    w.rk4(0.0, 0.5 * h, 4)
+    t = 4 * 0.5 * h
+    u = get_state(w, o)
+    want = o.stats(2, PULSE, t, u)
+    got, valid = w.stats(t)
+    assert valid
+    assert got[0] == pytest.approx(want[0], rel=1e-12)
+    assert got[1] == want[1] and got[2] == want[2]
+    assert int(got[4]) == int(want[4])
+
+
+@pytest.mark.gpu
+def test_nonfinite_detected():
+    p = S.Problem(**WAVE_CASE)
+    w = S.ScalarWave(p, S.PREC_FP64, S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE)
+    u = [np.zeros(p.size)] + [np.zeros(n) for n in p.nR]
+    fluid = np.nonzero(p.classes() & 0x80)[0]
+    u[0][fluid[len(fluid) // 2]] = float("nan")
+    set_state(w, u)
+    _, valid = w.stats(0.0)
+    assert not valid
