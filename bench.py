@@ -1,0 +1,371 @@
+"""Benchmark: 3-D scalar-wave RK4 on one GB300 (the wave workload of the suite).
+
+Workload (synthetic, generated from its parameters): u_t + a.grad u = 0 with
+a = (1, 0.7, 0.4) on a 256^3 grid over [0,1]^3, a Dirichlet sphere (centre 0.5, r = 0.3),
+Dirichlet inflow faces xmin/ymin/zmin and Floating outflow faces, a Gaussian pulse
+(centre 0.2, sigma 0.05) as initial data and exact boundary data, E4_1 (alpha = 0.1, 0.7),
+dt = 0.5 h, 1000 RK4 steps.
+
+One benchmark "step" is one full solve of that workload (initial condition + 1000 RK4
+steps).  value = RK4 DOF-updates/s = nx*ny*nz * 1000 * K / time of the mixed-precision
+path (FP32 stage fields and interior stencils, FP64 closure rows, compensated FP32-pair
+solution/accumulator), with every buffer resident in HBM (the working set, ~470 MB, is
+larger than the 129 MB L2).  The FP64 path is timed beside it; both report their max-norm
+error against the exact solution.  e2e repeats the mixed solve through the C ABI with the
+initial state copied from pinned host memory and the final state copied back inside the
+timed region.
+
+The reference's E4_1 closures are unstable under explicit RK4 on this geometry (walls are
+evaluated at psi = 1, which its psi clamp turns into ~1e5/h coefficients, and small cut
+cells give large ones), so the workload's solution overflows within a few dozen steps in
+the reference algorithm and here alike; kernel time does not depend on the values.  The
+mixed-versus-FP64 equal-accuracy criterion is therefore measured on a stable companion on
+the same 256^3 grid and kernels: the same pulse and velocity with the reference's E4u_1
+scheme and no embedded sphere, 300 RK4 steps.
+
+--impl reference times the reference algorithm's CPU path (the oracle restatement of
+pbrady/shoccs, OpenMP over all host cores) on the same workload, one RK4 step per
+benchmark step, bounded to about a minute in total.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "RK4 DOF-updates/s (3-D scalar wave, 256^3, sphere, E4_1)"
+UNIT = "DOF-updates/s"
+N_GRID = 256
+N_STEPS = 1000
+VEL = (1.0, 0.7, 0.4)
+PULSE = [0.2, 0.2, 0.2, 1.0, 0.7, 0.4, 0.05]
+CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1),
+            spheres=[((0.5, 0.5, 0.5), 0.3, "dirichlet")],
+            grid_bc=("dirichlet", "floating", "dirichlet", "floating", "dirichlet", "floating"),
+            scheme="E4_1", alpha=(0.1, 0.7))
+ACC_CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1), spheres=[],
+                grid_bc=("dirichlet", "floating", "dirichlet", "floating", "dirichlet",
+                         "floating"),
+                scheme="E4u_1", alpha=(-0.7733323791884821, 0.1623961700641681))
+ACC_STEPS = 300
+# algorithmic HBM bytes per grid point per RK4 step (u0, accumulator, stage field read and
+# written once per stage): FP64 8+8+8 | 24+16 | 24+16 | 24+8 = 136; mixed (4-byte stage
+# field, 8-byte compensated u0 and accumulator) 20 + 32 + 32 + 28 = 112
+BYTES_PT_STEP = {"mixed": 112, "fp64": 136}
+BYTES_PT_STAGE = {"mixed": [20, 32, 32, 28], "fp64": [24, 40, 40, 32]}
+
+
+def config(nsteps):
+    return {"workload": "scalar_wave_3d_256cubed_sphere_E4_1", "grid": [N_GRID] * 3,
+            "rk4_steps_per_solve": nsteps, "velocity": list(VEL), "sphere_radius": 0.3,
+            "pulse_sigma": 0.05, "dt": "0.5*h", "l2": "working set > L2 (no flush needed)",
+            "replicas": "one independent solve per GPU"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def measured_peak():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    p = os.path.join(HERE, "profiles", "stage_kernel_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return None
+
+
+def cpu_rate(nsteps_cap, time_budget):
+    """Oracle (the reference algorithm on the host cores) on the benchmark workload."""
+    from oracle import oracle as orc
+    threads = orc.set_threads(os.cpu_count() or 1)
+    o = orc.OracleProblem(**CASE)
+    u0 = o.initialize(2, PULSE, 0.0)
+    h = 1.0 / (N_GRID - 1)
+    dt = 0.5 * h
+    t0 = time.perf_counter()
+    o.wave_rk4(0, VEL, (0, 0, 0), 2, PULSE, 0.0, dt, 0, u0)  # system setup only
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u = o.wave_rk4(0, VEL, (0, 0, 0), 2, PULSE, 0.0, dt, 1, u0)
+    t1 = time.perf_counter() - t0 - t_setup
+    n = max(1, min(nsteps_cap, int(time_budget / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.wave_rk4(0, VEL, (0, 0, 0), 2, PULSE, 0.0, dt, n, u0)
+    tn = time.perf_counter() - t0 - t_setup
+    npts = o.size
+    return dict(value=npts * n / tn, unit=UNIT, cores=threads, kind="port",
+                sample="%d RK4 step(s) of the 256^3 wave workload (setup excluded), "
+                       "%.2f s" % (n, tn)), n, tn
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return 0
+    cb, n, tn = cpu_rate(max(1, args.steps), 60.0)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": n, "warmup": 1, "ms_per_step": 1000.0 * tn / n,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(1), "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "one benchmark step = one RK4 step of the 256^3 workload on the host; "
+                    "the run is capped at about a minute"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rk4-steps", type=int, default=N_STEPS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws)
+
+    import numpy as np
+    import torch
+    import shoccs_gb300 as S
+
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    nsteps = args.rk4_steps
+    p = S.Problem(**CASE)
+    N = p.size
+    h = 1.0 / (N_GRID - 1)
+    dt = 0.5 * h
+    stream = torch.cuda.Stream()
+    sysm = S.ScalarWave(p, S.PREC_MIXED, S.VEL_CONSTANT, VEL, (0, 0, 0), S.SOL_GAUSS_PULSE,
+                        PULSE)
+    sysd = S.ScalarWave(p, S.PREC_FP64, S.VEL_CONSTANT, VEL, (0, 0, 0), S.SOL_GAUSS_PULSE,
+                        PULSE)
+
+    def solve(sys_, timed=False):
+        sys_.initialize(0.0, stream)
+        if timed:
+            return sys_.rk4_timed(0.0, dt, nsteps, stream)
+        sys_.rk4(0.0, dt, nsteps, stream)
+        return None
+
+    # warm-up (mixed)
+    for _ in range(args.warmup):
+        solve(sysm)
+    barrier()
+
+    # ---- timed region: K mixed solves, CUDA events on the launching stream ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = S.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    kms = {"bc": 0.0, "stage0": 0.0, "stage1": 0.0, "stage2": 0.0, "stage3": 0.0}
+    for _ in range(args.steps):
+        r = solve(sysm, timed=True)
+        for k in kms:
+            kms[k] += r[k]
+    ev1.record(stream)
+    barrier()
+    t_ms = ev0.elapsed_time(ev1)
+    launches = S.kernel_launches() - l0
+    clk = clocks.stop()
+    if pg:
+        tt = torch.tensor([t_ms], device="cuda")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    t_end = nsteps * dt
+    stats_m, valid_m = sysm.stats(t_end, stream)
+
+    # ---- FP64 path (timed beside it) ----
+    for _ in range(max(1, min(args.warmup, 1))):
+        solve(sysd)
+    barrier()
+    n64 = max(1, min(args.steps, 2))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    kms64 = {"bc": 0.0, "stage0": 0.0, "stage1": 0.0, "stage2": 0.0, "stage3": 0.0}
+    for _ in range(n64):
+        r = solve(sysd, timed=True)
+        for k in kms64:
+            kms64[k] += r[k]
+    e1.record(stream)
+    barrier()
+    t64_ms = e0.elapsed_time(e1)
+    stats_d, valid_d = sysd.stats(t_end, stream)
+
+    # ---- equal-accuracy companion (stable scheme, same grid and kernels) ----
+    pa = S.Problem(**ACC_CASE)
+    acc = {}
+    for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+        sa_ = S.ScalarWave(pa, prec, S.VEL_CONSTANT, VEL, (0, 0, 0), S.SOL_GAUSS_PULSE, PULSE)
+        sa_.initialize(0.0, stream)
+        sa_.rk4(0.0, dt, ACC_STEPS, stream)
+        st_, ok_ = sa_.stats(ACC_STEPS * dt, stream)
+        acc[name] = {"max_error": st_[0], "valid": bool(ok_)}
+        del sa_
+    acc["error_ratio_mixed_vs_fp64"] = acc["mixed"]["max_error"] / acc["fp64"]["max_error"]
+    acc["case"] = "256^3, E4u_1 (alpha -0.7733, 0.1624), no sphere, %d RK4 steps" % ACC_STEPS
+    del pa
+
+    # ---- e2e through the C ABI with host buffers ----
+    host_in = [torch.empty(N, dtype=torch.float64).pin_memory()] + \
+              [torch.empty(k, dtype=torch.float64).pin_memory() for k in p.nR]
+    host_out = [torch.empty(N, dtype=torch.float64).pin_memory()] + \
+               [torch.empty(k, dtype=torch.float64).pin_memory() for k in p.nR]
+    sysm.initialize(0.0, stream)
+    sysm.get_state(S.ScalarField(*host_in), stream)  # the synthetic initial state on the host
+    h2d = sum(a.numel() * 8 for a in host_in)
+    d2h = sum(a.numel() * 8 for a in host_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sysm.set_state(S.ScalarField(*host_in), stream)
+        sysm.rk4(0.0, dt, nsteps, stream)
+        sysm.get_state(S.ScalarField(*host_out), stream)
+    barrier()
+    te2e = time.perf_counter() - t0
+
+    value = N * nsteps * args.steps * ws / (t_ms / 1000.0)
+    value64 = N * nsteps * n64 / (t64_ms / 1000.0)
+    e2e = N * nsteps * args.steps * ws / te2e
+
+    # roofline of the dominant kernels (the four fused RK4 stage kernels)
+    peak, peak_kind = measured_peak()
+    stage_ms = sum(kms[k] for k in ("stage0", "stage1", "stage2", "stage3"))
+    n_launch = 4 * nsteps * args.steps
+    bytes_step = BYTES_PT_STEP["mixed"] * N
+    achieved = bytes_step * nsteps * args.steps / (stage_ms / 1000.0) / 1e9
+    per_stage = {}
+    for i in range(4):
+        ms = kms["stage%d" % i] / (nsteps * args.steps)
+        per_stage["stage%d" % i] = {"avg_ms": ms,
+                                    "gbs": BYTES_PT_STAGE["mixed"][i] * N / (ms / 1000) / 1e9}
+    tr = committed_traffic()
+    traffic = None
+    if tr and tr.get("n_points") == N:
+        traffic = tr.get("bytes_per_launch_avg")
+    stage64_ms = sum(kms64[k] for k in ("stage0", "stage1", "stage2", "stage3"))
+    achieved64 = BYTES_PT_STEP["fp64"] * N * nsteps * n64 / (stage64_ms / 1000.0) / 1e9
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
+        "data": "synthetic", "config": config(nsteps),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_stage_mixed<0..3, wave> (4 launches per RK4 step)",
+                     "algorithmic_bytes_per_launch_avg": bytes_step / 4,
+                     "avg_launch_ms": stage_ms / n_launch, "peak_kind": peak_kind,
+                     "per_stage": per_stage},
+        "clocks": clk,
+        "fp64": {"value": value64, "unit": UNIT, "solves": n64,
+                 "ms_per_solve": t64_ms / n64, "roofline_achieved_gbs": achieved64,
+                 "roofline_frac": achieved64 / peak, "workload_error": stats_d[0],
+                 "valid": bool(valid_d)},
+        "mixed": {"workload_error": stats_m[0], "valid": bool(valid_m)},
+        "equal_accuracy": acc,
+        "speedup_mixed_vs_fp64": value / value64,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cb, _, _ = cpu_rate(8, 15.0)
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

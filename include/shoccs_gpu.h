@@ -64,7 +64,8 @@ typedef enum {
 enum { SHOCCS_BC_DIRICHLET = 0, SHOCCS_BC_FLOATING = 1, SHOCCS_BC_NEUMANN = 2 };
 
 /* schemes: scheme.order/type of stencil::from_lua (src/stencils/stencil.cpp:35-50) */
-enum { SHOCCS_SCHEME_E2_2 = 0, SHOCCS_SCHEME_E4_2 = 1, SHOCCS_SCHEME_E4_1 = 2 };
+enum { SHOCCS_SCHEME_E2_2 = 0, SHOCCS_SCHEME_E4_2 = 1, SHOCCS_SCHEME_E4_1 = 2,
+       SHOCCS_SCHEME_E4U_1 = 3 /* type "E4u" (src/stencils/stencil.cpp:51-53) */ };
 
 /* arithmetic of the operator and system kernels */
 enum {
@@ -82,7 +83,7 @@ typedef struct {
     const int* sphere_bc;     /* n_spheres: boundary_condition of each shape */
     int grid_bc[6];           /* xmin, xmax, ymin, ymax, zmin, zmax */
     int scheme;               /* SHOCCS_SCHEME_* */
-    double alpha[2];          /* scheme.alpha (E4_1) */
+    double alpha[2];          /* scheme.alpha (E4_1, E4u_1) */
 } shoccs_problem_desc;
 
 typedef struct shoccs_problem shoccs_problem;
@@ -166,6 +167,11 @@ shoccs_status shoccs_system_get_state(shoccs_system* s, shoccs_field* u, int whe
 /* nsteps classic RK4 steps of size dt from time t0 (fused stage kernels) */
 shoccs_status shoccs_system_rk4(shoccs_system* s, double t0, double dt, int nsteps,
                                 void* stream);
+/* as shoccs_system_rk4, with CUDA events recorded on `stream` around every launch;
+ * kernel_ms[0] = total time of the Dirichlet cut-point kernels, kernel_ms[1..4] = total
+ * time of RK4 stage kernels 0..3, kernel_ms[5] = elapsed time of the whole run */
+shoccs_status shoccs_system_rk4_timed(shoccs_system* s, double t0, double dt, int nsteps,
+                                      void* stream, double kernel_ms[6]);
 /* one right-hand-side evaluation of the current state at time t into rhs (FP64, device) */
 shoccs_status shoccs_system_rhs(shoccs_system* s, double t, shoccs_field* rhs, void* stream);
 /* out[11] = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry,

@@ -10,7 +10,7 @@ FMT_INC=$(python3 -c "import torch, os; print(os.path.join(os.path.dirname(torch
 mkdir -p "$HERE/_ref"
 g++ -std=c++20 -O2 -fPIC -shared -ffp-contract=off -DNDEBUG -DFMT_HEADER_ONLY \
     -I"$HERE/ref_stubs" -I"$REF/src" -I"$FMT_INC" \
-    "$REF/src/stencils/E2_2.cpp" "$REF/src/stencils/E4_2.cpp" "$REF/src/stencils/E4_1.cpp" \
+    "$REF/src/stencils/E2_2.cpp" "$REF/src/stencils/E4_2.cpp" "$REF/src/stencils/E4_1.cpp" "$REF/src/stencils/E4u_1.cpp" \
     "$REF/src/mesh/sphere.cpp" "$HERE/ref_driver.cpp" \
     -o "$HERE/_ref/libshoccs_ref.so"
 echo "built $HERE/_ref/libshoccs_ref.so"

@@ -20,7 +20,7 @@ IP = ctypes.POINTER(ctypes.c_int)
 LP = ctypes.POINTER(ctypes.c_long)
 
 BC = {"dirichlet": 0, "floating": 1, "neumann": 2}
-SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2}
+SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2, "E4u_1": 3}
 
 
 def build(force=False):

@@ -1,7 +1,7 @@
 // ref_driver.cpp -- C entry points over the reference's OWN stencil and sphere code.
 //
 // TEST INFRASTRUCTURE ONLY.  Compiled by oracle/build_ref.sh together with the reference
-// translation units src/stencils/{E2_2,E4_2,E4_1}.cpp and src/mesh/sphere.cpp taken
+// translation units src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp and src/mesh/sphere.cpp taken
 // unmodified from the reference tree, into oracle/_ref/libshoccs_ref.so.  Used only by
 // tests/golden/make_golden.py to pin the oracle restatement bit-for-bit.
 #include "mesh/shapes.hpp"
@@ -19,6 +19,7 @@ static stencil make(int scheme, const double* alpha)
     switch (scheme) {
     case 0: return make_E2_2();
     case 1: return make_E4_2();
+    case 3: return make_E4u_1(a);
     default: return make_E4_1(a);
     }
 }

@@ -27,7 +27,7 @@ from ._capi import (BC_DIRICHLET, BC_FLOATING, BC_NEUMANN, PREC_FP64, PREC_MIXED
 ScalarField = namedtuple("ScalarField", ["D", "Rx", "Ry", "Rz"])
 
 _BC = {"dirichlet": BC_DIRICHLET, "floating": BC_FLOATING, "neumann": BC_NEUMANN}
-_SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1}
+_SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1, "E4u_1": 3}
 
 
 def _bc(b):
@@ -250,6 +250,14 @@ class System:
     def rk4(self, t0, dt, nsteps, stream=None):
         _capi.check(_capi.lib().shoccs_system_rk4(self._h, float(t0), float(dt), int(nsteps),
                                                   _stream(stream)))
+
+    def rk4_timed(self, t0, dt, nsteps, stream=None):
+        """rk4 with per-kernel CUDA-event timing: returns dict of total milliseconds."""
+        ms = (ctypes.c_double * 6)()
+        _capi.check(_capi.lib().shoccs_system_rk4_timed(self._h, float(t0), float(dt),
+                                                        int(nsteps), _stream(stream), ms))
+        return dict(bc=ms[0], stage0=ms[1], stage1=ms[2], stage2=ms[3], stage3=ms[4],
+                    total=ms[5])
 
     def rhs(self, t, out, stream=None):
         _capi.check(_capi.lib().shoccs_system_rhs(self._h, float(t), _field(out),

@@ -13,7 +13,7 @@ OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENONFINITE, EUNSUPPORTED = range(7)
 STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "ETIMEOUT", "ENONFINITE", "EUNSUPPORTED"]
 
 BC_DIRICHLET, BC_FLOATING, BC_NEUMANN = 0, 1, 2
-SCHEME_E2_2, SCHEME_E4_2, SCHEME_E4_1 = 0, 1, 2
+SCHEME_E2_2, SCHEME_E4_2, SCHEME_E4_1, SCHEME_E4U_1 = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 SYS_HEAT, SYS_WAVE = 0, 1
 SOL_ZERO, SOL_SINSIN, SOL_GAUSS_PULSE, SOL_RADIAL_SIN = 0, 1, 2, 3
@@ -89,6 +89,8 @@ SIGNATURES = {
                                 ctypes.c_void_p],
     "shoccs_system_rk4": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                           ctypes.c_void_p],
+    "shoccs_system_rk4_timed": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_int, ctypes.c_void_p, c_double_p],
     "shoccs_system_rhs": [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(Field),
                           ctypes.c_void_p],
     "shoccs_system_stats": [ctypes.c_void_p, ctypes.c_double, c_double_p, ctypes.c_void_p],

@@ -184,27 +184,27 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
     *out = nullptr;
     for (int i = 0; i < 3; i++)
         if (d->n[i] < 1) return fail(SHOCCS_EINVAL, "index_extents must be >= 1");
-    if (d->scheme < 0 || d->scheme > 2) return fail(SHOCCS_EINVAL, "unknown scheme");
+    if (d->scheme < 0 || d->scheme > 3) return fail(SHOCCS_EINVAL, "unknown scheme");
     if (d->n_spheres < 0 || (d->n_spheres && (!d->centers || !d->radii || !d->sphere_bc)))
         return fail(SHOCCS_EINVAL, "sphere arrays missing");
     for (int i = 0; i < 6; i++)
         if (bad_bc(d->grid_bc[i])) return fail(SHOCCS_EINVAL, "bad grid boundary condition");
     for (int i = 0; i < d->n_spheres; i++)
         if (bad_bc(d->sphere_bc[i])) return fail(SHOCCS_EINVAL, "bad shape boundary condition");
-    if (d->scheme == SHOCCS_SCHEME_E4_1) {
+    if (d->scheme == SHOCCS_SCHEME_E4_1 || d->scheme == SHOCCS_SCHEME_E4U_1) {
         // src/stencils/E4_1.cpp:34-41
-        if (d->alpha[1] < 197.0 / 288.0)
+        if (d->scheme == SHOCCS_SCHEME_E4_1 && d->alpha[1] < 197.0 / 288.0)
             return fail(SHOCCS_EINVAL,
                         "E4_1: alpha[1] must be >= 197/288 to avoid the interior "
                         "denominator singularity");
         for (int i = 0; i < 6; i++)
             if (d->grid_bc[i] == SHOCCS_BC_NEUMANN && d->n[i / 2] > 1)
-                return fail(SHOCCS_EUNSUPPORTED, "E4_1 has no Neumann closure");
+                return fail(SHOCCS_EUNSUPPORTED, "first-derivative schemes have no Neumann closure");
         for (int i = 0; i < d->n_spheres; i++)
             if (d->sphere_bc[i] != SHOCCS_BC_DIRICHLET)
                 return fail(SHOCCS_EUNSUPPORTED,
-                            "E4_1 has no cross-direction interpolant; objects must be "
-                            "Dirichlet");
+                            "first-derivative schemes have no cross-direction interpolant; "
+                            "objects must be Dirichlet");
     }
     try {
         auto p = std::make_unique<shoccs_problem>();
@@ -539,6 +539,47 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     SH_CUDA(cudaStreamSynchronize(s));
     S->t = t;
     return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, int nsteps,
+                                      void* stream, double kernel_ms[6])
+{
+    if (!S || nsteps < 1 || !(dt > 0) || !kernel_ms) return fail(SHOCCS_EINVAL, "bad argument");
+    const cudaStream_t s = (cudaStream_t)stream;
+    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps, nullptr);
+    shoccs_status st = SHOCCS_OK;
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            st = fail(SHOCCS_ECUDA, "cudaEventCreate failed");
+            break;
+        }
+    double t = t0;
+    for (int i = 0; st == SHOCCS_OK && i < nsteps; i++) {
+        cudaError_t e = launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt,
+                                        s, ev.data() + 6 * (size_t)i);
+        if (e != cudaSuccess) st = fail(SHOCCS_ECUDA, cudaGetErrorString(e));
+        t += dt;
+    }
+    if (st == SHOCCS_OK && cudaStreamSynchronize(s) != cudaSuccess)
+        st = fail(SHOCCS_ECUDA, "stream synchronize failed");
+    if (st == SHOCCS_OK) {
+        for (int k = 0; k < 6; k++) kernel_ms[k] = 0.0;
+        for (int i = 0; i < nsteps; i++) {
+            cudaEvent_t* e = ev.data() + 6 * (size_t)i;
+            for (int k = 0; k < 5; k++) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e[k], e[k + 1]);
+                kernel_ms[k] += ms;
+            }
+        }
+        float all = 0.f;
+        cudaEventElapsedTime(&all, ev.front(), ev.back());
+        kernel_ms[5] = all;
+        S->t = t;
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return st;
 }
 
 shoccs_status shoccs_system_rhs(shoccs_system* S, double t, shoccs_field* rhs, void* stream)

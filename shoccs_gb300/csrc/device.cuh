@@ -85,8 +85,10 @@ struct StepBuffers {
     double* Rfull[3];  // Dirichlet R values at t + dt
 };
 
+// ev (optional): 6 events recorded before the cut-point kernel and after it and each stage
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
-                            StepBuffers& b, double t, double dt, cudaStream_t s);
+                            StepBuffers& b, double t, double dt, cudaStream_t s,
+                            cudaEvent_t* ev = nullptr);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s);
 cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,

@@ -1,11 +1,12 @@
 // stencils.hpp -- closed-form stencil coefficients for the cut-cell schemes E2_2, E4_2
-// (second derivative) and E4_1 (first derivative).
+// (second derivative), E4_1 (cut-cell first derivative) and E4u_1 (uniform-grid first
+// derivative).
 //
-// Setup-time host code.  The formulas restate src/stencils/E2_2.cpp, src/stencils/E4_2.cpp
-// and src/stencils/E4_1.cpp of the reference (query / interior / nbs / interp_interior /
-// interp_wall), statement by statement so that the coefficients are bit-identical when
+// Setup-time host code.  The formulas restate src/stencils/E2_2.cpp, src/stencils/E4_2.cpp,
+// src/stencils/E4_1.cpp and src/stencils/E4u_1.cpp of the reference (query / interior /
+// nbs / interp_interior / interp_wall), statement by statement so that the coefficients are bit-identical when
 // compiled with -ffp-contract=off.  They are mathematics that must be alike; the closure
-// rows they produce are compiled into GPU tables by assembly.cpp.
+// rows they produce are compiled into GPU tables by problem.cpp.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -23,7 +24,7 @@ struct interp_info {
 };
 
 struct Stencil {
-    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1
+    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1, 3: E4u_1
     real alpha[2] = {0, 0};
 
     info query_max() const
@@ -31,13 +32,14 @@ struct Stencil {
         switch (kind) {
         case 0: return {1, 2, 4, 2};
         case 1: return {2, 3, 5, 3};
+        case 3: return {2, 3, 5, 0};
         default: return {2, 5, 7, 0};
         }
     }
     info query(int b) const
     {
         info mx = query_max();
-        if (kind == 2 && b == Neumann) return {0, 0, 0, 0};
+        if ((kind == 2 || kind == 3) && b == Neumann) return {0, 0, 0, 0};
         switch (b) {
         case Dirichlet: return {mx.p, mx.r - 1, mx.t, 0};
         case Floating: return {mx.p, mx.r, mx.t, 0};
@@ -66,6 +68,12 @@ struct Stencil {
             c[2] = -5 / (2. * (h * h));
             c[3] = 4 / (3. * (h * h));
             c[4] = -1 / (12. * (h * h));
+        } else if (kind == 3) { // E4u_1.cpp:49-58
+            c[0] = 1 / (12 * h);
+            c[1] = -2 / (3 * h);
+            c[2] = 0;
+            c[3] = -c[1];
+            c[4] = -c[0];
         } else { // E4_1.cpp:66-76
             c[0] = 0.083333333333333329;
             c[1] = -0.66666666666666663;
@@ -87,9 +95,55 @@ struct Stencil {
             if (b == Floating) e42_floating(h, psi, c, right);
             else if (b == Dirichlet) e42_dirichlet(h, psi, c, right);
             else e42_neumann(h, psi, c, x, right);
+        } else if (kind == 3) {
+            if (b == Floating) e4u_floating(h, c, right);
+            else if (b == Dirichlet) e4u_dirichlet(h, c, right);
         } else {
             if (b == Floating) e41_floating(h, psi, c, right);
             else if (b == Dirichlet) e41_dirichlet(h, psi, c, right);
+        }
+    }
+
+    // ---- E4u_1 (uniform-grid closures, psi ignored): src/stencils/E4u_1.cpp:77-127
+    void e4u_floating(real h, real* c, bool right) const
+    {
+        c[0] = (6 * alpha[0] - 11) / 6;
+        c[1] = 3 - 4 * alpha[0];
+        c[2] = (12 * alpha[0] - 3) / 2;
+        c[3] = -(12 * alpha[0] - 1) / 3;
+        c[4] = alpha[0];
+        c[5] = (3 * alpha[1] - 1) / 3;
+        c[6] = -(8 * alpha[1] + 1) / 2;
+        c[7] = 6 * alpha[1] + 1;
+        c[8] = -(24 * alpha[1] + 1) / 6;
+        c[9] = alpha[1];
+        c[10] = -(168 * alpha[1] + 54 * alpha[0] - 11) / 138;
+        c[11] = (112 * alpha[1] + 36 * alpha[0] - 15) / 23;
+        c[12] = -(336 * alpha[1] + 108 * alpha[0] + 1) / 46;
+        c[13] = (336 * alpha[1] + 108 * alpha[0] + 47) / 69;
+        c[14] = -(28 * alpha[1] + 9 * alpha[0] + 2) / 23;
+        for (int i = 0; i < 15; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 15; i++) c[i] *= -1;
+            reverse(c, 15);
+        }
+    }
+    void e4u_dirichlet(real h, real* c, bool right) const
+    {
+        c[0] = (3 * alpha[1] - 1) / 3;
+        c[1] = -(8 * alpha[1] + 1) / 2;
+        c[2] = 6 * alpha[1] + 1;
+        c[3] = -(24 * alpha[1] + 1) / 6;
+        c[4] = alpha[1];
+        c[5] = -(168 * alpha[1] + 54 * alpha[0] - 11) / 138;
+        c[6] = (112 * alpha[1] + 36 * alpha[0] - 15) / 23;
+        c[7] = -(336 * alpha[1] + 108 * alpha[0] + 1) / 46;
+        c[8] = (336 * alpha[1] + 108 * alpha[0] + 47) / 69;
+        c[9] = -(28 * alpha[1] + 9 * alpha[0] + 2) / 23;
+        for (int i = 0; i < 10; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 10; i++) c[i] *= -1;
+            reverse(c, 10);
         }
     }
 

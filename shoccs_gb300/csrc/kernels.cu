@@ -840,27 +840,40 @@ namespace
 {
 template <int SYS>
 void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[4],
-                   cudaStream_t s)
+                   cudaStream_t s, cudaEvent_t* ev)
 {
     const dim3 grid = point_grid(op), block(32, BY);
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], s);
+    };
     if (prec == PREC_FP64) {
         k_stage64<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
+        mark(2);
         k_stage64<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
+        mark(3);
         k_stage64<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
+        mark(4);
         k_stage64<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
+        mark(5);
     } else {
         k_stage_mixed<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
+        mark(2);
         k_stage_mixed<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
+        mark(3);
         k_stage_mixed<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
+        mark(4);
         k_stage_mixed<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
+        mark(5);
     }
     g_launches += 4;
 }
 } // namespace
 
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
-                            StepBuffers& b, double t, double dt, cudaStream_t s)
+                            StepBuffers& b, double t, double dt, cudaStream_t s,
+                            cudaEvent_t* ev)
 {
+    if (ev) cudaEventRecord(ev[0], s);
     // src/temporal/rk4.cpp:11-12
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -875,6 +888,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
                                                b.Rhalf[d], b.Rfull[d], b.R[d]);
         ++g_launches;
     }
+    if (ev) cudaEventRecord(ev[1], s);
     StageArgs sa[4];
     for (int i = 0; i < 4; i++) {
         StageArgs& a = sa[i];
@@ -894,9 +908,9 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.et_next = et(a.t_next);
     }
     if (sp.kind == SYS_HEAT)
-        launch_stages<SYS_HEAT>(op, sp, prec, sa, s);
+        launch_stages<SYS_HEAT>(op, sp, prec, sa, s, ev);
     else
-        launch_stages<SYS_WAVE>(op, sp, prec, sa, s);
+        launch_stages<SYS_WAVE>(op, sp, prec, sa, s, ev);
     for (int d = 0; d < 3; d++) std::swap(b.R[d], b.Rfull[d]);
     return cudaGetLastError();
 }

@@ -57,6 +57,10 @@ def cases():
         # no objects at all, all-Floating walls
         "plain_box_e42": dict(n=(12, 9, 40), lo=(0, 0, 0), hi=(1, 2, 3), spheres=[],
                               grid_bc=(FLT,) * 6, scheme="E4_2"),
+        # uniform-grid first-derivative scheme (E4u_1), Dirichlet inflow / Floating outflow
+        "box_e4u": dict(n=(34, 30, 36), lo=(0, 0, 0), hi=(1, 1, 1), spheres=[],
+                        grid_bc=(DIR, FLT, DIR, FLT, DIR, FLT), scheme="E4u_1",
+                        alpha=(-0.7733323791884821, 0.1623961700641681)),
         # 1-D line
         "line_1d_e41": dict(n=(64, 1, 1), lo=(0, 0, 0), hi=(1, 0, 0), spheres=[],
                             grid_bc=(DIR, FLT, FLT, FLT, FLT, FLT), scheme="E4_1",

@@ -57,8 +57,10 @@ def ref_fixtures():
     lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libshoccs_ref.so"))
     D = ctypes.c_double
     alpha = (D * 2)(0.1, 0.7)
+    alpha_u = (D * 2)(-0.7733323791884821, 0.1623961700641681)
     nbs = []
-    rt = {0: {0: 4, 1: 8, 2: 8}, 1: {0: 10, 1: 15, 2: 15}, 2: {0: 28, 1: 35}}
+    rt = {0: {0: 4, 1: 8, 2: 8}, 1: {0: 10, 1: 15, 2: 15}, 2: {0: 28, 1: 35},
+          3: {0: 10, 1: 15}}
     rng = np.random.default_rng(20261203)
     psis = [1e-12, 1e-5, 0.01, 0.25, 0.5, 0.75, 0.9, 0.999, 1.0 - 1e-12, 1.0]
     psis += list(rng.uniform(0.0, 1.0, 6))
@@ -68,15 +70,16 @@ def ref_fixtures():
                 for right in (0, 1):
                     for h in (2.0, 1.0 / 64, 0.1):
                         c, x = (D * 64)(), (D * 8)()
-                        lib.ref_stencil_nbs(scheme, alpha, D(h), bc, D(psi), right, c, x)
+                        lib.ref_stencil_nbs(scheme, alpha_u if scheme == 3 else alpha, D(h),
+                                            bc, D(psi), right, c, x)
                         nbs.append(dict(scheme=scheme, bc=bc, psi=float(psi), right=right,
                                         h=h, c=[float(v).hex() for v in c[:n]],
                                         x=[float(v).hex() for v in x[:3]]))
     interior = []
-    for scheme in (0, 1, 2):
+    for scheme in (0, 1, 2, 3):
         for h in (2.0, 1.0 / 64, 1.0 / 255):
             c = (D * 8)()
-            n = lib.ref_stencil_interior(scheme, alpha, D(h), c)
+            n = lib.ref_stencil_interior(scheme, alpha_u if scheme == 3 else alpha, D(h), c)
             interior.append(dict(scheme=scheme, h=h, c=[float(v).hex() for v in c[:n]]))
     interp = []
     for scheme in (0, 1):
@@ -108,7 +111,8 @@ def ref_fixtures():
                          origin=[float(v).hex() for v in origin], axis=axis, hit=ok,
                          t=t.value.hex(), pos=[v.hex() for v in pos], ray_outside=ro.value,
                          normal=[v.hex() for v in nrm]))
-    return (dict(source="src/stencils/{E2_2,E4_2,E4_1}.cpp via oracle/_ref", alpha=[0.1, 0.7],
+    return (dict(source="src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp via oracle/_ref",
+                 alpha=[0.1, 0.7], alpha_e4u=[-0.7733323791884821, 0.1623961700641681],
                  nbs=nbs, interior=interior, interp=interp),
             dict(source="src/mesh/sphere.cpp via oracle/_ref", hits=hits))
 

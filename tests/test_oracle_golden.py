@@ -28,14 +28,16 @@ def test_stencils_bit_exact_vs_reference_code():
     g = json.load(open(os.path.join(GOLD, "stencils_ref.json")))
     L = orc.lib()
     alpha = (D * 2)(*g["alpha"])
+    alpha_u = (D * 2)(*g["alpha_e4u"])
     for e in g["nbs"]:
         c, x = (D * 64)(), (D * 8)()
-        L.orc_stencil_nbs(e["scheme"], alpha, D(e["h"]), e["bc"], D(e["psi"]), e["right"], c, x)
+        L.orc_stencil_nbs(e["scheme"], alpha_u if e["scheme"] == 3 else alpha, D(e["h"]),
+                          e["bc"], D(e["psi"]), e["right"], c, x)
         want = _hex(e["c"])
         got = np.array(c[:len(want)])
         assert np.array_equal(got.view(np.int64), want.view(np.int64)), e
         wx = _hex(e["x"])
-        nx = {0: 2, 1: 3, 2: 0}[e["scheme"]] if e["bc"] == 2 else 0
+        nx = {0: 2, 1: 3, 2: 0, 3: 0}[e["scheme"]] if e["bc"] == 2 else 0
         assert np.array_equal(np.array(x[:nx]), wx[:nx]), e
     for e in g["interior"]:
         c = (D * 8)()
