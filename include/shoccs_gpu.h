@@ -167,9 +167,10 @@ shoccs_status shoccs_system_get_state(shoccs_system* s, shoccs_field* u, int whe
 /* nsteps classic RK4 steps of size dt from time t0 (fused stage kernels) */
 shoccs_status shoccs_system_rk4(shoccs_system* s, double t0, double dt, int nsteps,
                                 void* stream);
-/* as shoccs_system_rk4, with CUDA events recorded on `stream` around every launch;
- * kernel_ms[0] = total time of the Dirichlet cut-point kernels, kernel_ms[1..4] = total
- * time of RK4 stage kernels 0..3, kernel_ms[5] = elapsed time of the whole run */
+/* as shoccs_system_rk4, with CUDA events recorded on `stream` around the fused stage
+ * kernels; kernel_ms[1..4] = total time of the main kernels of RK4 stages 0..3,
+ * kernel_ms[0] = everything else (boundary-value and cut-cell row kernels),
+ * kernel_ms[5] = elapsed time of the whole run */
 shoccs_status shoccs_system_rk4_timed(shoccs_system* s, double t0, double dt, int nsteps,
                                       void* stream, double kernel_ms[6]);
 /* one right-hand-side evaluation of the current state at time t into rhs (FP64, device) */

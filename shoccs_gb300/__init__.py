@@ -256,7 +256,7 @@ class System:
         ms = (ctypes.c_double * 6)()
         _capi.check(_capi.lib().shoccs_system_rk4_timed(self._h, float(t0), float(dt),
                                                         int(nsteps), _stream(stream), ms))
-        return dict(bc=ms[0], stage0=ms[1], stage1=ms[2], stage2=ms[3], stage3=ms[4],
+        return dict(aux=ms[0], stage0=ms[1], stage1=ms[2], stage2=ms[3], stage3=ms[4],
                     total=ms[5])
 
     def rhs(self, t, out, stream=None):

@@ -121,6 +121,14 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
     }
     if (op.it0 > 65535) return fail(SHOCCS_EINVAL, "grid too large along the slowest axis");
     SH_CUDA(p->mem.put(C.cls, &op.cls, s));
+    {
+        std::vector<long long> faces;
+        for (long long i = 0; i < (long long)C.cls.size(); i++)
+            if (C.cls[i] & CLS_DIRFACE) faces.push_back(i);
+        if (faces.size() > 0x7fffffff) return fail(SHOCCS_EINVAL, "too many face points");
+        op.n_faces = (int)faces.size();
+        SH_CUDA(p->mem.put(faces, &op.faces, s));
+    }
     for (int d = 0; d < 3; d++) SH_CUDA(p->mem.put(p->mesh.x[d], &op.xc[d], s));
     for (int d = 0; d < 3; d++) {
         const AxisTables& T = C.ax[d];
@@ -128,6 +136,12 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
         A.active = T.active;
         A.stride = T.stride;
         A.width = T.width;
+        A.n = p->mesh.n[d];
+        A.wall[0] = T.wall[0];
+        A.wall[1] = T.wall[1];
+        A.row_base = op.n_cut_rows;
+        A.n_rows = (int)T.rows.size();
+        op.n_cut_rows += A.n_rows;
         for (int j = 0; j < 5; j++) {
             A.ic[j] = T.interior[j];
             A.icf[j] = (float)T.interior[j];
@@ -136,6 +150,7 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
                     T.interior[1] == -T.interior[3];
         if (!T.active) continue;
         SH_CUDA(p->mem.put(T.rows, &A.rows, s));
+        SH_CUDA(p->mem.put(T.row_out, (const long long**)&A.row_out, s));
         SH_CUDA(p->mem.put(T.coef, &A.coef, s));
         SH_CUDA(p->mem.put(T.chunk_base, &A.chunk_base, s));
         for (int r = 0; r < 3; r++) {
@@ -399,10 +414,13 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     SysParams& sp = S->sp;
     sp.kind = d->kind;
     sp.k = d->diffusivity;
+    sp.kf = (float)d->diffusivity;
     sp.vel_kind = d->vel_kind;
     for (int c = 0; c < 3; c++) {
         sp.vel[c] = d->vel[c];
+        sp.gf[c] = (float)(-d->vel[c]);
         sp.center[c] = d->center[c];
+        sp.centerf[c] = (float)d->center[c];
     }
     DevSol& sol = sp.sol;
     sol.kind = d->sol_kind;
@@ -416,6 +434,8 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
             std::vector<double> tab(p->mesh.n[a]);
             for (int i = 0; i < p->mesh.n[a]; i++) tab[i] = std::sin(twoPI * k * p->mesh.x[a][i]);
             SH_CUDA(S->mem.put(tab, &sol.S[a], s));
+            std::vector<float> tabf(tab.begin(), tab.end());
+            SH_CUDA(S->mem.put(tabf, &sol.Sf[a], s));
         }
         for (int r = 0; r < 3; r++) {
             std::vector<double> tab;
@@ -445,6 +465,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.sa = base;
         S->b.sb = (char*)base + N * es_s;
     }
+    SH_CUDA(S->mem.alloc((size_t)p->op.n_cut_rows * 8, &S->b.cval));
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
     SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * es_u, s));
     for (int r = 0; r < 3; r++) {
@@ -546,7 +567,8 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
 {
     if (!S || nsteps < 1 || !(dt > 0) || !kernel_ms) return fail(SHOCCS_EINVAL, "bad argument");
     const cudaStream_t s = (cudaStream_t)stream;
-    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps, nullptr);
+    constexpr int EV = 10;
+    std::vector<cudaEvent_t> ev(EV * (size_t)nsteps, nullptr);
     shoccs_status st = SHOCCS_OK;
     for (auto& e : ev)
         if (cudaEventCreate(&e) != cudaSuccess) {
@@ -556,7 +578,7 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
     double t = t0;
     for (int i = 0; st == SHOCCS_OK && i < nsteps; i++) {
         cudaError_t e = launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt,
-                                        s, ev.data() + 6 * (size_t)i);
+                                        s, ev.data() + EV * (size_t)i);
         if (e != cudaSuccess) st = fail(SHOCCS_ECUDA, cudaGetErrorString(e));
         t += dt;
     }
@@ -565,16 +587,24 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
     if (st == SHOCCS_OK) {
         for (int k = 0; k < 6; k++) kernel_ms[k] = 0.0;
         for (int i = 0; i < nsteps; i++) {
-            cudaEvent_t* e = ev.data() + 6 * (size_t)i;
-            for (int k = 0; k < 5; k++) {
+            cudaEvent_t* e = ev.data() + EV * (size_t)i;
+            for (int k = 0; k < 4; k++) {
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, e[k], e[k + 1]);
-                kernel_ms[k] += ms;
+                cudaEventElapsedTime(&ms, e[2 + 2 * k], e[3 + 2 * k]);
+                kernel_ms[1 + k] += ms;
             }
         }
+        // the run ends with the last stage's face kernel: time it up to the run's end
+        cudaEvent_t end;
         float all = 0.f;
-        cudaEventElapsedTime(&all, ev.front(), ev.back());
+        if (cudaEventCreate(&end) == cudaSuccess) {
+            cudaEventRecord(end, s);
+            cudaEventSynchronize(end);
+            cudaEventElapsedTime(&all, ev.front(), end);
+            cudaEventDestroy(end);
+        }
         kernel_ms[5] = all;
+        kernel_ms[0] = all - (kernel_ms[1] + kernel_ms[2] + kernel_ms[3] + kernel_ms[4]);
         S->t = t;
     }
     for (auto& e : ev)

@@ -13,12 +13,17 @@ namespace sgb
 struct DevAxis {
     int active;
     int width;   // 2p+1 interior stencil width (3 or 5)
-    int antisym; // interior coefficients are antisymmetric with a zero centre (E4_1)
-    int pad;
+    int antisym; // interior coefficients are antisymmetric with a zero centre (E4_1, E4u_1)
+    int n;       // grid points along the axis
     long long stride;
     double ic[5];
     float icf[5];
+    WallBlock wall[2]; // rows shared by every line ending at the left / right wall
+    // cut-cell closure rows, sorted by output index
+    int n_rows;
+    int row_base; // offset of this axis's rows in the concatenated cut-row value array
     const ClosureRow* rows;
+    const long long* row_out; // output flat index of each row
     const double* coef;
     const int* chunk_base;
     // R-space rows (non-Dirichlet objects) per target r: CSR with source flag
@@ -37,6 +42,9 @@ struct DevOp {
     int phys_of_it[3];
     const uint8_t* cls;
     const double* xc[3]; // grid coordinates per physical axis
+    int n_faces;         // Dirichlet-face points
+    const long long* faces;
+    int n_cut_rows;      // cut-cell rows of all axes
     DevAxis ax[3];
 };
 
@@ -46,12 +54,13 @@ struct DevSol {
     int dims;
     double p[8];
     const double* S[3];  // SINSIN: sin(2 pi k x) tables per physical axis
+    const float* Sf[3];  // SINSIN: the same tables rounded to FP32 (mixed heat source)
     const double* SR[3]; // SINSIN: product of sines at the cut points of R(d)
     double lapfac;       // SINSIN: -(dims) (2 pi k)^2
 };
 
 struct DevR {
-    const double* pos[3];     // cut-point positions (3 per point)
+    const double* pos[3];        // cut-point positions (3 per point)
     const uint8_t* dirichlet[3]; // 1 where the cut point's shape is Dirichlet
 };
 
@@ -69,9 +78,12 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
 struct SysParams {
     int kind;      // 0 heat, 1 wave
     double k;      // heat diffusivity
+    float kf;
     int vel_kind;  // wave 0 constant, 1 radial
     double vel[3];
+    float gf[3];   // -vel in FP32
     double center[3];
+    float centerf[3];
     DevSol sol;
 };
 
@@ -80,12 +92,12 @@ struct StepBuffers {
     void* acc;     // double or float2
     void* sa;      // stage fields: double or float
     void* sb;
+    void* cval;    // cut-cell row values of the current stage: double or float
     double* R[3];      // state R values (time t)
     double* Rhalf[3];  // Dirichlet R values at t + dt/2
     double* Rfull[3];  // Dirichlet R values at t + dt
 };
 
-// ev (optional): 6 events recorded before the cut-point kernel and after it and each stage
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev = nullptr);

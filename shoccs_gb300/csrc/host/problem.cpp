@@ -554,6 +554,7 @@ AxisOp assemble_axis(int dir, const Mesh& m, const Stencil& st, const Bcs& bcs)
         bm.right_col_offset = (int)(col_offset + stride * (cols - rcols));
         A.coeffs.insert(A.coeffs.end(), rv.begin(), rv.end());
         A.meta.push_back(bm);
+        A.block_wall.push_back((uint8_t)((ln.s.obj < 0 ? 1 : 0) | (ln.e.obj < 0 ? 2 : 0)));
     }
     A.B = to_csr(std::move(B), m.size());
     A.N = to_csr(std::move(N), m.size());
@@ -632,14 +633,47 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
         };
         std::vector<Pending> pend;
         const int shift = 2 * d;
-        for (const auto& bm : A.meta) {
+        const i64 sd = m.stride(d);
+        auto axis_coord = [&](i64 flat) { return (int)((flat / sd) % m.n[d]); };
+        // a wall row joins its side's shared block; the first line defines the block and
+        // every other line must reproduce it exactly
+        std::vector<std::vector<std::vector<real>>> wall_rows(2);
+        std::vector<int> wall_col0(2, -1), wall_first(2, -1), wall_cols(2, 0);
+        auto wall_row = [&](int side, int r, int nrows, int ncols, const real* c, i64 out,
+                            i64 col_start) {
+            const int coord = axis_coord(out);
+            const int col0 = axis_coord(col_start);
+            auto& rows = wall_rows[side];
+            if (rows.empty()) {
+                rows.assign(nrows, {});
+                wall_col0[side] = col0;
+                wall_first[side] = coord - r;
+                wall_cols[side] = ncols;
+            }
+            if ((int)rows.size() != nrows || wall_first[side] != coord - r ||
+                wall_col0[side] != col0 || wall_cols[side] != ncols)
+                throw std::runtime_error("domain-wall closure blocks differ between lines");
+            std::vector<real> v(c, c + ncols);
+            if (rows[r].empty())
+                rows[r] = v;
+            else if (rows[r] != v)
+                throw std::runtime_error("domain-wall closure rows differ between lines");
+            C.cls[out] |= (uint8_t)(ROW_WALL << shift);
+        };
+        for (size_t b = 0; b < A.meta.size(); b++) {
+            const auto& bm = A.meta[b];
+            const bool lwall = A.block_wall[b] & 1, rwall = A.block_wall[b] & 2;
             const i64 st = bm.stride;
             for (int r = 0; r < bm.left_rows; r++) {
                 const i64 out = bm.row_offset + (i64)r * st;
+                const real* c = A.coeffs.data() + bm.left_coeff_offset + r * bm.left_cols;
+                if (lwall) {
+                    wall_row(0, r, bm.left_rows, bm.left_cols, c, out, bm.col_offset);
+                    continue;
+                }
                 Pending p;
                 p.out = out;
-                p.c.assign(A.coeffs.begin() + bm.left_coeff_offset + r * bm.left_cols,
-                           A.coeffs.begin() + bm.left_coeff_offset + (r + 1) * bm.left_cols);
+                p.c.assign(c, c + bm.left_cols);
                 p.col0 = (int)((bm.col_offset - out) / st);
                 pend.push_back(std::move(p));
                 C.cls[out] |= (uint8_t)(ROW_CLOSURE << shift);
@@ -650,14 +684,34 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
             }
             for (int r = 0; r < bm.right_rows; r++) {
                 const i64 out = bm.row_offset + (i64)(bm.left_rows + bm.interior_rows + r) * st;
+                const real* c = A.coeffs.data() + bm.right_coeff_offset + r * bm.right_cols;
+                if (rwall) {
+                    wall_row(1, r, bm.right_rows, bm.right_cols, c, out, bm.right_col_offset);
+                    continue;
+                }
                 Pending p;
                 p.out = out;
-                p.c.assign(A.coeffs.begin() + bm.right_coeff_offset + r * bm.right_cols,
-                           A.coeffs.begin() + bm.right_coeff_offset + (r + 1) * bm.right_cols);
+                p.c.assign(c, c + bm.right_cols);
                 p.col0 = (int)((bm.right_col_offset - out) / st);
                 pend.push_back(std::move(p));
                 C.cls[out] |= (uint8_t)(ROW_CLOSURE << shift);
             }
+        }
+        for (int side = 0; side < 2; side++) {
+            WallBlock& W = T.wall[side];
+            W = WallBlock{};
+            W.wall = side == 0 ? 0 : m.n[d] - 1;
+            if (wall_rows[side].empty()) continue;
+            W.rows = (int)wall_rows[side].size();
+            W.cols = wall_cols[side];
+            W.first_row = wall_first[side];
+            W.col0 = wall_col0[side];
+            if (W.rows > 5 || W.cols > 7) throw std::runtime_error("wall block exceeds 5 x 7");
+            for (int r = 0; r < W.rows; r++)
+                for (int j = 0; j < W.cols; j++) {
+                    W.c[r * 7 + j] = wall_rows[side][r][j];
+                    W.cf[r * 7 + j] = (float)wall_rows[side][r][j];
+                }
         }
         std::sort(pend.begin(), pend.end(),
                   [](const Pending& a, const Pending& b) { return a.out < b.out; });
@@ -677,10 +731,29 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
             p.b_idx = A.B.v[A.B.u[row]];
             p.b = A.B.w[A.B.u[row]];
         }
+        bool n_set[2][5] = {};
         for (i64 row = 0; row < A.N.rows; row++) {
             const i64 nnz = A.N.u[row + 1] - A.N.u[row];
             if (nnz == 0) continue;
             if (nnz > 1) throw std::runtime_error("more than one N entry on a closure row");
+            if (((C.cls[row] >> shift) & 3u) == ROW_WALL) {
+                // Neumann data of a wall row: coefficient on the wall point of its line
+                const int coord = axis_coord(row);
+                const int side = coord < m.n[d] / 2 ? 0 : 1;
+                WallBlock& W = T.wall[side];
+                const int r = coord - W.first_row;
+                const i64 col = A.N.v[A.N.u[row]];
+                if (r < 0 || r >= W.rows || axis_coord(col) != W.wall ||
+                    col != row + (i64)(W.wall - coord) * sd)
+                    throw std::runtime_error("Neumann entry off its wall row");
+                const real v = A.N.w[A.N.u[row]];
+                if (n_set[side][r] && W.n[r] != v)
+                    throw std::runtime_error("Neumann wall rows differ between lines");
+                W.n[r] = v;
+                W.has_n = 1;
+                n_set[side][r] = true;
+                continue;
+            }
             auto& p = find_row(row);
             p.n_idx = A.N.v[A.N.u[row]];
             p.nn = A.N.w[A.N.u[row]];

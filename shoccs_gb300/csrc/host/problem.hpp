@@ -105,6 +105,7 @@ struct AxisOp {
     i64 stride = 1;
     std::vector<real> interior;
     std::vector<BlockMeta> meta;
+    std::vector<uint8_t> block_wall; // per block: bit0 left end is a wall, bit1 right end
     std::vector<real> coeffs;
     Csr B, N;
     Csr Bf[3], Br[3];
@@ -120,8 +121,9 @@ struct AxisTables {
     i64 stride = 1;
     int width = 0;
     real interior[5] = {0, 0, 0, 0, 0};
-    std::vector<ClosureRow> rows; // sorted by output index
-    std::vector<i64> row_out;     // output flat index of each row (host-side checks)
+    WallBlock wall[2] = {};       // left / right domain-wall closure blocks
+    std::vector<ClosureRow> rows; // cut-cell closure rows, sorted by output index
+    std::vector<i64> row_out;     // output flat index of each row
     std::vector<real> coef;       // deduplicated coefficient pool
     std::vector<int> chunk_base;  // exclusive prefix of closure rows per 32-point chunk
     // R-space rows (non-Dirichlet objects): per target r, Bf (cols in D) then Br (cols in R_r)

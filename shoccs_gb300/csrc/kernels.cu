@@ -162,6 +162,41 @@ __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long
     return v;
 }
 
+// ---- domain-wall closure rows (shared per axis and side) ---------------------------------
+// row r of the block at axis coordinate `coord`: sum_j c[r][j] * x[col0 + j] along the axis
+__device__ __forceinline__ int wall_side(const DevAxis& A, int coord) { return coord * 2 < A.n ? 0 : 1; }
+
+template <class TIN>
+__device__ __forceinline__ double wall64(const DevAxis& A, long long p, int coord, const TIN* u,
+                                         const double* nu, double acc, bool first)
+{
+    const WallBlock& W = A.wall[wall_side(A, coord)];
+    const int r = coord - W.first_row;
+    long long q = p + (long long)(W.col0 - coord) * A.stride;
+    double s = 0.0;
+    for (int j = 0; j < W.cols; ++j) {
+        s = fma(W.c[r * 7 + j], ldd(u, q), s);
+        q += A.stride;
+    }
+    double v = first ? s : acc + s;
+    if (W.has_n && nu) v = fma(W.n[r], __ldg(nu + p + (long long)(W.wall - coord) * A.stride), v);
+    return v;
+}
+
+template <class TIN>
+__device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord, const TIN* u)
+{
+    const WallBlock& W = A.wall[wall_side(A, coord)];
+    const int r = coord - W.first_row;
+    long long q = p + (long long)(W.col0 - coord) * A.stride;
+    float s = 0.f;
+    for (int j = 0; j < W.cols; ++j) {
+        s = fmaf(W.cf[r * 7 + j], ldf(u, q), s);
+        q += A.stride;
+    }
+    return s;
+}
+
 // ---- closed-form solutions -------------------------------------------------------------
 enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3 };
 
@@ -250,8 +285,36 @@ inline dim3 point_grid(const DevOp& op)
 }
 
 // ===========================================================================================
-// Standalone operators
+// Standalone operators (derivative / Laplacian / gradient)
 // ===========================================================================================
+// value of axis d's row at point q (kind != ROW_NONE); FP64 fields compute in FP64, FP32
+// fields compute interior and wall rows in FP32 and cut-cell rows in FP64
+template <class T>
+__device__ __forceinline__ T op_row(const DevAxis& A, unsigned kind, int row, long long p,
+                                    int coord, const T* u, const T* Rd, const double* nu,
+                                    T acc, bool first)
+{
+    if constexpr (sizeof(T) == 8) {
+        if (kind == ROW_INTERIOR) {
+            const double v = interior64(A, (const double*)u, p);
+            return first ? v : acc + v;
+        }
+        if (kind == ROW_WALL) return wall64(A, p, coord, (const double*)u, nu, acc, first);
+        return closure64(A, row, p, (const double*)u, (const double*)Rd, nu, acc, first);
+    } else {
+        if (kind == ROW_INTERIOR) {
+            const float v = interior32(A, (const float*)u, p);
+            return first ? v : acc + v;
+        }
+        if (kind == ROW_WALL) {
+            const float v = wall32(A, p, coord, (const float*)u);
+            return first ? v : acc + v;
+        }
+        return (float)closure64(A, row, p, (const float*)u, (const float*)Rd, nu, (double)acc,
+                                first);
+    }
+}
+
 template <class T, bool PLUS>
 __global__ void __launch_bounds__(256) k_derivative(DevOp op, int dir, const T* __restrict__ u,
                                                     const T* __restrict__ Rd,
@@ -262,18 +325,11 @@ __global__ void __launch_bounds__(256) k_derivative(DevOp op, int dir, const T* 
     const DevAxis& A = op.ax[dir];
     const unsigned kind = q.valid ? (op.cls[q.p] >> (2 * dir)) & 3u : 0u;
     const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-    if (kind == ROW_INTERIOR) {
-        if constexpr (sizeof(T) == 8) {
-            const double v = interior64(A, (const double*)u, q.p);
-            du[q.p] = PLUS ? du[q.p] + v : v;
-        } else {
-            const float v = interior32(A, (const float*)u, q.p);
-            du[q.p] = PLUS ? du[q.p] + v : v;
-        }
-    } else if (kind == ROW_CLOSURE) {
-        const double prev = PLUS ? (double)du[q.p] : 0.0;
-        du[q.p] = (T)closure64(A, row, q.p, u, Rd, nu, prev, !PLUS);
-    }
+    if (kind == ROW_NONE) return;
+    int ijk[3];
+    phys_ijk(op, q, ijk);
+    const T prev = PLUS ? du[q.p] : (T)0;
+    du[q.p] = op_row<T>(A, kind, row, q.p, ijk[dir], u, Rd, nu, prev, !PLUS);
 }
 
 template <class T>
@@ -285,6 +341,8 @@ __global__ void __launch_bounds__(256) k_laplacian(DevOp op, const T* __restrict
     const Pt q = point_of(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const T* R[3] = {R0, R1, R2};
+    int ijk[3];
+    phys_ijk(op, q, ijk);
     T acc = 0;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -292,14 +350,7 @@ __global__ void __launch_bounds__(256) k_laplacian(DevOp op, const T* __restrict
         if (!A.active) continue;
         const unsigned kind = (c >> (2 * d)) & 3u;
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-        if (kind == ROW_INTERIOR) {
-            if constexpr (sizeof(T) == 8)
-                acc = acc + interior64(A, (const double*)u, q.p);
-            else
-                acc = acc + interior32(A, (const float*)u, q.p);
-        } else if (kind == ROW_CLOSURE) {
-            acc = (T)closure64(A, row, q.p, u, R[d], nu, (double)acc, false);
-        }
+        if (kind != ROW_NONE) acc = op_row<T>(A, kind, row, q.p, ijk[d], u, R[d], nu, acc, false);
     }
     if (q.valid) du[q.p] = acc;
 }
@@ -313,6 +364,8 @@ __global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict_
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const T* R[3] = {R0, R1, R2};
     T* out[3] = {o0, o1, o2};
+    int ijk[3];
+    phys_ijk(op, q, ijk);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const DevAxis& A = op.ax[d];
@@ -323,14 +376,8 @@ __global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict_
         const unsigned kind = (c >> (2 * d)) & 3u;
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
         T v = 0;
-        if (kind == ROW_INTERIOR) {
-            if constexpr (sizeof(T) == 8)
-                v = interior64(A, (const double*)u, q.p);
-            else
-                v = interior32(A, (const float*)u, q.p);
-        } else if (kind == ROW_CLOSURE) {
-            v = (T)closure64(A, row, q.p, u, R[d], (const double*)nullptr, 0.0, true);
-        }
+        if (kind != ROW_NONE)
+            v = op_row<T>(A, kind, row, q.p, ijk[d], u, R[d], (const double*)nullptr, (T)0, true);
         if (q.valid) out[d][q.p] = v;
     }
 }
@@ -368,43 +415,56 @@ cudaError_t rspace_for(const DevOp& op, int d, const void* uD, const void* const
 }
 
 // ===========================================================================================
-// Fused RK4 stage kernels
+// Fused RK4 stages
+//
+// Per stage: k_cut_rows evaluates every cut-cell closure row (FP64, one thread per row, so
+// warps stay full), the main kernel applies interior and wall rows (FP32 in the mixed
+// path, FP64 in the FP64 path), reads the cut-row values, forms the right-hand side and
+// updates the RK4 registers, and k_faces writes the Dirichlet face values.
 // ===========================================================================================
 struct StageArgs {
     const void* s_in;
     void* u0;
     void* acc;
     void* s_out;
+    const void* cval;
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
     float2 cf_ff, ci_ff;    // same as compensated FP32 pairs
     double t_stage, t_next; // RHS time and Dirichlet time of the stage output
     double et_stage, et_next;
+    float etf_stage;
 };
 
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 
-template <int SYS>
-__device__ __forceinline__ void wave_coef(const SysParams& sp, const DevOp& op, const Pt& q,
-                                          double g[3])
+// cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b]  (FP64)
+template <class TIN, class TOUT>
+__global__ void k_cut_rows(DevOp op, const TIN* __restrict__ u, const double* R0,
+                           const double* R1, const double* R2, TOUT* __restrict__ cval)
 {
-    if (sp.vel_kind == 0) {
-        g[0] = -sp.vel[0];
-        g[1] = -sp.vel[1];
-        g[2] = -sp.vel[2];
-    } else {
-        int ijk[3];
-        phys_ijk(op, q, ijk);
-        const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
-        const double r[3] = {x[0] - sp.center[0], x[1] - sp.center[1], x[2] - sp.center[2]};
-        const double len = sqrt(r[0] * r[0] + (r[1] * r[1] + r[2] * r[2]));
-        g[0] = -r[0] / len;
-        g[1] = -r[1] / len;
-        g[2] = -r[2] / len;
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= op.n_cut_rows) return;
+    const double* R[3] = {R0, R1, R2};
+    const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
+    const DevAxis& A = op.ax[d];
+    const int row = i - A.row_base;
+    const long long p = A.row_out[row];
+    cval[i] = (TOUT)closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
 }
 
-// FP64 stage.  TIN: double (all stages).
+__device__ __forceinline__ void radial_g64(const SysParams& sp, const DevOp& op, const int ijk[3],
+                                           double g[3])
+{
+    const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+    const double r[3] = {x[0] - sp.center[0], x[1] - sp.center[1], x[2] - sp.center[2]};
+    const double len = sqrt(r[0] * r[0] + (r[1] * r[1] + r[2] * r[2]));
+    g[0] = -r[0] / len;
+    g[1] = -r[1] / len;
+    g[2] = -r[2] / len;
+}
+
+// FP64 stage
 template <int STAGE, int SYS>
 __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
 {
@@ -412,6 +472,9 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const double* __restrict__ in =
         STAGE == 0 ? (const double*)sa.u0 : (const double*)sa.s_in;
+    const double* __restrict__ cval = (const double*)sa.cval;
+    int ijk[3];
+    phys_ijk(op, q, ijk);
     double lap = 0.0;
     double dd[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -420,17 +483,17 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
         if (!A.active) continue;
         const unsigned kind = (c >> (2 * d)) & 3u;
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-        if (SYS == SYS_HEAT) {
-            if (kind == ROW_INTERIOR)
-                lap = lap + interior64(A, in, q.p);
-            else if (kind == ROW_CLOSURE)
-                lap = closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr, lap, false);
-        } else {
-            if (kind == ROW_INTERIOR)
-                dd[d] = interior64(A, in, q.p);
-            else if (kind == ROW_CLOSURE)
-                dd[d] = closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr, 0.0, true);
-        }
+        double v = 0.0;
+        if (kind == ROW_INTERIOR)
+            v = interior64(A, in, q.p);
+        else if (kind == ROW_WALL)
+            v = wall64(A, q.p, ijk[d], in, (const double*)nullptr, 0.0, true);
+        else if (kind == ROW_CLOSURE)
+            v = cval[A.row_base + row];
+        if (SYS == SYS_HEAT)
+            lap = lap + v;
+        else
+            dd[d] = v;
     }
     if (!q.valid) return;
     double rhs = 0.0;
@@ -438,15 +501,13 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
         if (SYS == SYS_HEAT) {
             double src = 0.0;
             if (sp.sol.kind == SOL_SINSIN) {
-                int ijk[3];
-                phys_ijk(op, q, ijk);
                 const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
                 src = (-u) - sp.k * (sp.sol.lapfac * u);
             }
             rhs = fma(lap, sp.k, src);
         } else {
-            double g[3];
-            wave_coef<SYS>(sp, op, q, g);
+            double g[3] = {-sp.vel[0], -sp.vel[1], -sp.vel[2]};
+            if (sp.vel_kind != 0) radial_g64(sp, op, ijk, g);
             rhs = fma(g[2], dd[2], fma(g[1], dd[1], g[0] * dd[0]));
         }
     }
@@ -457,32 +518,22 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
             acc[q.p] = sa.cf * rhs;
         else
             acc[q.p] = fma(sa.cf, rhs, acc[q.p]);
-        double un = fma(sa.ci, rhs, u0[q.p]);
-        if (c & CLS_DIRFACE) {
-            int ijk[3];
-            phys_ijk(op, q, ijk);
-            un = sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
-        }
-        ((double*)sa.s_out)[q.p] = un;
+        ((double*)sa.s_out)[q.p] = fma(sa.ci, rhs, u0[q.p]);
     } else {
-        const double a = fma(sa.cf, rhs, acc[q.p]);
-        double un = u0[q.p] + a;
-        if (c & CLS_DIRFACE) {
-            int ijk[3];
-            phys_ijk(op, q, ijk);
-            un = sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
-        }
-        u0[q.p] = un;
+        u0[q.p] = u0[q.p] + fma(sa.cf, rhs, acc[q.p]);
     }
 }
 
-// Mixed stage: FP32 stage field and interior stencils, FP64 closure rows, compensated
-// FP32-pair solution (u0) and accumulator.  Stage 0 reads u0 (float2) as its input.
+// Mixed stage: FP32 stage field, interior and wall rows; FP64 cut-cell rows (k_cut_rows);
+// compensated FP32-pair solution (u0) and accumulator.  Stage 0 reads u0 as its input.
 template <int STAGE, int SYS>
 __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, StageArgs sa)
 {
     const Pt q = point_of(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
+    const float* __restrict__ cval = (const float*)sa.cval;
+    int ijk[3];
+    phys_ijk(op, q, ijk);
     float lap = 0.f;
     float dd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -494,21 +545,16 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         float v = 0.f;
         if (STAGE == 0) {
             const float2* in = (const float2*)sa.u0;
-            if (kind == ROW_INTERIOR)
-                v = interior32(A, in, q.p);
-            else if (kind == ROW_CLOSURE)
-                v = (float)closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr,
-                                     SYS == SYS_HEAT ? (double)lap : 0.0, SYS != SYS_HEAT);
+            if (kind == ROW_INTERIOR) v = interior32(A, in, q.p);
+            else if (kind == ROW_WALL) v = wall32(A, q.p, ijk[d], in);
         } else {
             const float* in = (const float*)sa.s_in;
-            if (kind == ROW_INTERIOR)
-                v = interior32(A, in, q.p);
-            else if (kind == ROW_CLOSURE)
-                v = (float)closure64(A, row, q.p, in, sa.R[d], (const double*)nullptr,
-                                     SYS == SYS_HEAT ? (double)lap : 0.0, SYS != SYS_HEAT);
+            if (kind == ROW_INTERIOR) v = interior32(A, in, q.p);
+            else if (kind == ROW_WALL) v = wall32(A, q.p, ijk[d], in);
         }
+        if (kind == ROW_CLOSURE) v = cval[A.row_base + row];
         if (SYS == SYS_HEAT)
-            lap = (kind == ROW_CLOSURE) ? v : lap + v;
+            lap = lap + v;
         else
             dd[d] = v;
     }
@@ -518,16 +564,24 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         if (SYS == SYS_HEAT) {
             float src = 0.f;
             if (sp.sol.kind == SOL_SINSIN) {
-                int ijk[3];
-                phys_ijk(op, q, ijk);
-                const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
-                src = (float)((-u) - sp.k * (sp.sol.lapfac * u));
+                float u = sp.sol.Sf[0][ijk[0]] * sp.sol.Sf[1][ijk[1]];
+                if (sp.sol.dims == 3) u = u * sp.sol.Sf[2][ijk[2]];
+                u = u * sa.etf_stage;
+                src = (-u) - sp.kf * ((float)sp.sol.lapfac * u);
             }
-            rhs = fmaf(lap, (float)sp.k, src);
+            rhs = fmaf(lap, sp.kf, src);
         } else {
-            double g[3];
-            wave_coef<SYS>(sp, op, q, g);
-            rhs = fmaf((float)g[2], dd[2], fmaf((float)g[1], dd[1], (float)g[0] * dd[0]));
+            float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
+            if (sp.vel_kind != 0) {
+                const float r0 = (float)op.xc[0][ijk[0]] - sp.centerf[0];
+                const float r1 = (float)op.xc[1][ijk[1]] - sp.centerf[1];
+                const float r2 = (float)op.xc[2][ijk[2]] - sp.centerf[2];
+                const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
+                g0 = -r0 * il;
+                g1 = -r1 * il;
+                g2 = -r2 * il;
+            }
+            rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
         }
     }
     float2* __restrict__ u0 = (float2*)sa.u0;
@@ -536,22 +590,29 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
     if (STAGE < 3) {
         const float2 inc = ff_mul(sa.cf_ff, rhs);
         acc[q.p] = STAGE == 0 ? inc : ff_add(acc[q.p], inc);
-        float un = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
-        if (c & CLS_DIRFACE) {
-            int ijk[3];
-            phys_ijk(op, q, ijk);
-            un = (float)sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk);
-        }
-        ((float*)sa.s_out)[q.p] = un;
+        ((float*)sa.s_out)[q.p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
     } else {
-        const float2 a = ff_add(acc[q.p], ff_mul(sa.cf_ff, rhs));
-        float2 un = ff_add(u, a);
-        if (c & CLS_DIRFACE) {
-            int ijk[3];
-            phys_ijk(op, q, ijk);
-            un = ff_from_double(sol_at_point(op, sp.sol, sa.t_next, sa.et_next, ijk));
-        }
-        u0[q.p] = un;
+        u0[q.p] = ff_add(u, ff_add(acc[q.p], ff_mul(sa.cf_ff, rhs)));
+    }
+}
+
+// Dirichlet face values of the stage output (update_boundary on D)
+template <bool MIXED, bool LAST>
+__global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= op.n_faces) return;
+    const long long p = op.faces[i];
+    const long long nyz = (long long)op.n[1] * op.n[2];
+    const int ijk[3] = {(int)(p / nyz), (int)((p / op.n[2]) % op.n[1]), (int)(p % op.n[2])};
+    const double v = sol_at_point(op, sol, t, et, ijk);
+    if (MIXED) {
+        if (LAST)
+            ((float2*)out)[p] = ff_from_double(v);
+        else
+            ((float*)out)[p] = (float)v;
+    } else {
+        ((double*)out)[p] = v;
     }
 }
 
@@ -581,6 +642,8 @@ __global__ void __launch_bounds__(256) k_rhs(DevOp op, SysParams sp, const void*
     const Pt q = point_of(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const double* R[3] = {R0, R1, R2};
+    int ijk[3];
+    phys_ijk(op, q, ijk);
     double lap = 0.0, dd[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -592,18 +655,18 @@ __global__ void __launch_bounds__(256) k_rhs(DevOp op, SysParams sp, const void*
         if (MIXED) {
             const float2* in = (const float2*)uin;
             if (kind == ROW_INTERIOR) v = (double)interior32(A, in, q.p);
+            else if (kind == ROW_WALL) v = (double)wall32(A, q.p, ijk[d], in);
             else if (kind == ROW_CLOSURE)
-                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr,
-                              SYS == SYS_HEAT ? lap : 0.0, SYS != SYS_HEAT);
+                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr, 0.0, true);
         } else {
             const double* in = (const double*)uin;
             if (kind == ROW_INTERIOR) v = interior64(A, in, q.p);
+            else if (kind == ROW_WALL) v = wall64(A, q.p, ijk[d], in, nullptr, 0.0, true);
             else if (kind == ROW_CLOSURE)
-                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr,
-                              SYS == SYS_HEAT ? lap : 0.0, SYS != SYS_HEAT);
+                v = closure64(A, row, q.p, in, R[d], (const double*)nullptr, 0.0, true);
         }
         if (SYS == SYS_HEAT)
-            lap = (kind == ROW_CLOSURE) ? v : lap + v;
+            lap = lap + v;
         else
             dd[d] = v;
     }
@@ -613,15 +676,13 @@ __global__ void __launch_bounds__(256) k_rhs(DevOp op, SysParams sp, const void*
         if (SYS == SYS_HEAT) {
             double src = 0.0;
             if (sp.sol.kind == SOL_SINSIN) {
-                int ijk[3];
-                phys_ijk(op, q, ijk);
                 const double u = sol_at_point(op, sp.sol, t, et, ijk);
                 src = (-u) - sp.k * (sp.sol.lapfac * u);
             }
             rhs = fma(lap, sp.k, src);
         } else {
-            double g[3];
-            wave_coef<SYS>(sp, op, q, g);
+            double g[3] = {-sp.vel[0], -sp.vel[1], -sp.vel[2]};
+            if (sp.vel_kind != 0) radial_g64(sp, op, ijk, g);
             rhs = fma(g[2], dd[2], fma(g[1], dd[1], g[0] * dd[0]));
         }
     }
@@ -674,6 +735,16 @@ struct StatPart {
     double mn, mx;
 };
 
+__device__ __forceinline__ void stat_merge(StatPart& m, const StatPart& o)
+{
+    if (o.err > m.err || (o.err == m.err && o.err >= 0 && o.idx < m.idx)) {
+        m.err = o.err;
+        m.idx = o.idx;
+    }
+    m.mn = fmin(m.mn, o.mn);
+    m.mx = fmax(m.mx, o.mx);
+}
+
 __global__ void __launch_bounds__(256) k_stats(DevOp op, DevSol sol, double t, double et,
                                                int mixed, const void* u0, StatPart* parts)
 {
@@ -683,24 +754,17 @@ __global__ void __launch_bounds__(256) k_stats(DevOp op, DevSol sol, double t, d
         const double u = mixed ? ldd((const float2*)u0, q.p) : ((const double*)u0)[q.p];
         int ijk[3];
         phys_ijk(op, q, ijk);
-        const double e = fabs(u - sol_at_point(op, sol, t, et, ijk));
-        s = StatPart{e, q.p, u, u};
+        double e = fabs(u - sol_at_point(op, sol, t, et, ijk));
+        // a non-finite value counts as an infinite error so that system validity trips
+        if (!(e <= 1.7976931348623157e308)) e = __longlong_as_double(0x7ff0000000000000LL);
+        s = StatPart{e, q.p, isnan(u) ? 0.0 : u, isnan(u) ? 0.0 : u};
     }
     __shared__ StatPart sh[256];
     const int tid = threadIdx.y * 32 + threadIdx.x;
     sh[tid] = s;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
-        if (tid < w) {
-            StatPart o = sh[tid + w];
-            StatPart& m = sh[tid];
-            if (o.err > m.err || (o.err == m.err && o.err >= 0 && o.idx < m.idx)) {
-                m.err = o.err;
-                m.idx = o.idx;
-            }
-            m.mn = fmin(m.mn, o.mn);
-            m.mx = fmax(m.mx, o.mx);
-        }
+        if (tid < w) stat_merge(sh[tid], sh[tid + w]);
         __syncthreads();
     }
     if (tid == 0) {
@@ -714,28 +778,11 @@ __global__ void k_stats_final(long long nparts, const StatPart* parts, double* o
 {
     __shared__ StatPart sh[256];
     StatPart s{-1.0, 0, 1e308, -1e308};
-    for (long long i = threadIdx.x; i < nparts; i += 256) {
-        const StatPart o = parts[i];
-        if (o.err > s.err || (o.err == s.err && o.err >= 0 && o.idx < s.idx)) {
-            s.err = o.err;
-            s.idx = o.idx;
-        }
-        s.mn = fmin(s.mn, o.mn);
-        s.mx = fmax(s.mx, o.mx);
-    }
+    for (long long i = threadIdx.x; i < nparts; i += 256) stat_merge(s, parts[i]);
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) {
-            StatPart o = sh[threadIdx.x + w];
-            StatPart& m = sh[threadIdx.x];
-            if (o.err > m.err || (o.err == m.err && o.err >= 0 && o.idx < m.idx)) {
-                m.err = o.err;
-                m.idx = o.idx;
-            }
-            m.mn = fmin(m.mn, o.mn);
-            m.mx = fmax(m.mx, o.mx);
-        }
+        if ((int)threadIdx.x < w) stat_merge(sh[threadIdx.x], sh[threadIdx.x + w]);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -838,48 +885,73 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
 
 namespace
 {
+template <int STAGE, int SYS>
+void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArgs& a,
+                  cudaStream_t s, cudaEvent_t* ev)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const bool mixed = prec == PREC_MIXED;
+    if (op.n_cut_rows) {
+        const int nb = (op.n_cut_rows + 127) / 128;
+        const double* const* R = a.R;
+        if (!mixed)
+            k_cut_rows<double, double><<<nb, 128, 0, s>>>(
+                op, (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
+                (double*)a.cval);
+        else if (STAGE == 0)
+            k_cut_rows<float2, float><<<nb, 128, 0, s>>>(op, (const float2*)a.u0, R[0], R[1],
+                                                         R[2], (float*)a.cval);
+        else
+            k_cut_rows<float, float><<<nb, 128, 0, s>>>(op, (const float*)a.s_in, R[0], R[1],
+                                                        R[2], (float*)a.cval);
+        ++g_launches;
+    }
+    if (ev) cudaEventRecord(ev[0], s);
+    if (mixed)
+        k_stage_mixed<STAGE, SYS><<<grid, block, 0, s>>>(op, sp, a);
+    else
+        k_stage64<STAGE, SYS><<<grid, block, 0, s>>>(op, sp, a);
+    ++g_launches;
+    if (ev) cudaEventRecord(ev[1], s);
+    if (op.n_faces) {
+        const int nb = (op.n_faces + 255) / 256;
+        void* out = STAGE == 3 ? a.u0 : a.s_out;
+        if (mixed) {
+            if (STAGE == 3)
+                k_faces<true, true><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
+            else
+                k_faces<true, false><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
+        } else {
+            k_faces<false, false><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
+        }
+        ++g_launches;
+    }
+}
+
 template <int SYS>
 void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[4],
                    cudaStream_t s, cudaEvent_t* ev)
 {
-    const dim3 grid = point_grid(op), block(32, BY);
-    auto mark = [&](int i) {
-        if (ev) cudaEventRecord(ev[i], s);
-    };
-    if (prec == PREC_FP64) {
-        k_stage64<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
-        mark(2);
-        k_stage64<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
-        mark(3);
-        k_stage64<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
-        mark(4);
-        k_stage64<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
-        mark(5);
-    } else {
-        k_stage_mixed<0, SYS><<<grid, block, 0, s>>>(op, sp, sa[0]);
-        mark(2);
-        k_stage_mixed<1, SYS><<<grid, block, 0, s>>>(op, sp, sa[1]);
-        mark(3);
-        k_stage_mixed<2, SYS><<<grid, block, 0, s>>>(op, sp, sa[2]);
-        mark(4);
-        k_stage_mixed<3, SYS><<<grid, block, 0, s>>>(op, sp, sa[3]);
-        mark(5);
-    }
-    g_launches += 4;
+    launch_stage<0, SYS>(op, sp, prec, sa[0], s, ev ? ev + 2 : nullptr);
+    launch_stage<1, SYS>(op, sp, prec, sa[1], s, ev ? ev + 4 : nullptr);
+    launch_stage<2, SYS>(op, sp, prec, sa[2], s, ev ? ev + 6 : nullptr);
+    launch_stage<3, SYS>(op, sp, prec, sa[3], s, ev ? ev + 8 : nullptr);
 }
 } // namespace
 
+// ev (optional): 10 events -- [0] step start, [1] after the cut-point BC kernel,
+// [2+2i], [3+2i] around the main kernel of stage i
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev)
 {
-    if (ev) cudaEventRecord(ev[0], s);
     // src/temporal/rk4.cpp:11-12
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
     const bool sinsin = sp.sol.kind == SOL_SINSIN;
     auto et = [&](double tt) { return sinsin ? std::exp(-tt) : 0.0; };
 
+    if (ev) cudaEventRecord(ev[0], s);
     const double th = t + dt * rki[1], tf = t + dt * rki[3];
     for (int d = 0; d < 3; d++) {
         const int n = (int)op.nR[d];
@@ -894,6 +966,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         StageArgs& a = sa[i];
         a.u0 = b.u0;
         a.acc = b.acc;
+        a.cval = b.cval;
         a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
         a.s_out = i == 1 ? b.sb : b.sa;
         for (int d = 0; d < 3; d++)
@@ -906,6 +979,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.t_next = i < 3 ? t + dt * rki[i + 1] : t + dt;
         a.et_stage = et(a.t_stage);
         a.et_next = et(a.t_next);
+        a.etf_stage = (float)a.et_stage;
     }
     if (sp.kind == SYS_HEAT)
         launch_stages<SYS_HEAT>(op, sp, prec, sa, s, ev);
