@@ -53,11 +53,12 @@ ACC_CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1), spheres=
                          "floating"),
                 scheme="E4u_1", alpha=(-0.7733323791884821, 0.1623961700641681))
 ACC_STEPS = 300
-# algorithmic HBM bytes per grid point per RK4 step (u0, accumulator, stage field read and
-# written once per stage): FP64 8+8+8 | 24+16 | 24+16 | 24+8 = 136; mixed (4-byte stage
-# field, 8-byte compensated u0 and accumulator) 20 + 32 + 32 + 28 = 112
-BYTES_PT_STEP = {"mixed": 112, "fp64": 136}
-BYTES_PT_STAGE = {"mixed": [20, 32, 32, 28], "fp64": [24, 40, 40, 32]}
+# algorithmic HBM bytes per grid point per RK4 step (u0, accumulator, stage field each read
+# and written once per stage): FP64 (8-byte everything) 8+8+8 | 24+16 | 24+16 | 24+8 = 136;
+# mixed (4-byte stage field and accumulator, 8-byte compensated u0)
+# 8+4+4 | 16+8 | 16+8 | 16+8 = 88
+BYTES_PT_STEP = {"mixed": 88, "fp64": 136}
+BYTES_PT_STAGE = {"mixed": [16, 24, 24, 24], "fp64": [24, 40, 40, 32]}
 
 
 def config(nsteps):

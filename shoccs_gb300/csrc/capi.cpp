@@ -453,7 +453,8 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     const size_t es_u = 8; // double or float2
     const size_t es_s = d->prec == PREC_FP64 ? 8 : 4;
     SH_CUDA(S->mem.alloc(N * es_u, &S->b.u0));
-    SH_CUDA(S->mem.alloc(N * es_u, &S->b.acc));
+    // the mixed path keeps its stage accumulator in FP32 (the increments are FP32-accurate)
+    SH_CUDA(S->mem.alloc(N * (d->prec == PREC_FP64 ? 8 : 4), &S->b.acc));
     if (d->prec == PREC_FP64) {
         SH_CUDA(S->mem.alloc(N * es_s, &S->b.sa));
         SH_CUDA(S->mem.alloc(N * es_s, &S->b.sb));
@@ -467,7 +468,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     }
     SH_CUDA(S->mem.alloc((size_t)p->op.n_cut_rows * 8, &S->b.cval));
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
-    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * es_u, s));
+    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (d->prec == PREC_FP64 ? 8 : 4), s));
     for (int r = 0; r < 3; r++) {
         const size_t n = p->mesh.R[r].size();
         void *a, *h, *f;

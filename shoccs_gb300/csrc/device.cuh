@@ -89,7 +89,7 @@ struct SysParams {
 
 struct StepBuffers {
     void* u0;      // double (FP64) or float2 (MIXED)
-    void* acc;     // double or float2
+    void* acc;     // double (FP64) or float (MIXED)
     void* sa;      // stage fields: double or float
     void* sb;
     void* cval;    // cut-cell row values of the current stage: double or float

@@ -453,6 +453,88 @@ __global__ void k_cut_rows(DevOp op, const TIN* __restrict__ u, const double* R0
     cval[i] = (TOUT)closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
 }
 
+
+// Index arithmetic of the stage kernels runs in IDX (int when the grid has fewer than 2^31
+// points, which keeps every address a single 32-bit add).
+template <class IDX>
+struct StagePt {
+    IDX p;
+    long long chunk;
+    int a, b, c;
+    bool valid;
+};
+
+template <class IDX>
+__device__ __forceinline__ StagePt<IDX> stage_point(const DevOp& op)
+{
+    StagePt<IDX> q;
+    q.c = blockIdx.x * 32 + threadIdx.x;
+    q.b = blockIdx.y * blockDim.y + threadIdx.y;
+    q.a = blockIdx.z;
+    q.valid = (q.b < op.it1) && (q.c < op.it2);
+    const IDX line = (IDX)q.a * op.it1 + q.b;
+    q.p = line * op.it2 + q.c;
+    q.chunk = (long long)line * op.nzc + blockIdx.x;
+    return q;
+}
+
+template <class IDX>
+__device__ __forceinline__ void stage_ijk(const DevOp& op, const StagePt<IDX>& q, int ijk[3])
+{
+    ijk[0] = ijk[1] = ijk[2] = 0;
+    if (op.phys_of_it[0] >= 0) ijk[op.phys_of_it[0]] = q.a;
+    if (op.phys_of_it[1] >= 0) ijk[op.phys_of_it[1]] = q.b;
+    if (op.phys_of_it[2] >= 0) ijk[op.phys_of_it[2]] = q.c;
+}
+
+template <class T, class IDX>
+__device__ __forceinline__ T ld_in(const T* u, IDX i) { return __ldg(u + i); }
+
+// interior row with IDX addressing; FP32 (mixed) from a float or float2 (hi word) field
+template <class IDX, class TIN>
+__device__ __forceinline__ float interior_f(const DevAxis& A, const TIN* u, IDX p, IDX s)
+{
+    auto L = [&](IDX i) -> float {
+        if constexpr (sizeof(TIN) == 8) return __ldg(u + i).x;
+        else return __ldg(u + i);
+    };
+    if (A.width == 5) {
+        if (A.antisym) {
+            const float d1 = L(p + s) - L(p - s);
+            const float d2 = L(p + 2 * s) - L(p - 2 * s);
+            return fmaf(A.icf[3], d1, A.icf[4] * d2);
+        }
+        float r = A.icf[0] * L(p - 2 * s);
+        r = fmaf(A.icf[1], L(p - s), r);
+        r = fmaf(A.icf[2], L(p), r);
+        r = fmaf(A.icf[3], L(p + s), r);
+        return fmaf(A.icf[4], L(p + 2 * s), r);
+    }
+    float r = A.icf[0] * L(p - s);
+    r = fmaf(A.icf[1], L(p), r);
+    return fmaf(A.icf[2], L(p + s), r);
+}
+
+template <class IDX>
+__device__ __forceinline__ double interior_d(const DevAxis& A, const double* u, IDX p, IDX s)
+{
+    if (A.width == 5) {
+        if (A.antisym) {
+            const double d1 = __ldg(u + p + s) - __ldg(u + p - s);
+            const double d2 = __ldg(u + p + 2 * s) - __ldg(u + p - 2 * s);
+            return fma(A.ic[3], d1, A.ic[4] * d2);
+        }
+        double r = A.ic[0] * __ldg(u + p - 2 * s);
+        r = fma(A.ic[1], __ldg(u + p - s), r);
+        r = fma(A.ic[2], __ldg(u + p), r);
+        r = fma(A.ic[3], __ldg(u + p + s), r);
+        return fma(A.ic[4], __ldg(u + p + 2 * s), r);
+    }
+    double r = A.ic[0] * __ldg(u + p - s);
+    r = fma(A.ic[1], __ldg(u + p), r);
+    return fma(A.ic[2], __ldg(u + p + s), r);
+}
+
 __device__ __forceinline__ void radial_g64(const SysParams& sp, const DevOp& op, const int ijk[3],
                                            double g[3])
 {
@@ -464,17 +546,15 @@ __device__ __forceinline__ void radial_g64(const SysParams& sp, const DevOp& op,
     g[2] = -r[2] / len;
 }
 
-// FP64 stage
-template <int STAGE, int SYS>
+// FP64 stage: interior and wall rows in FP64, cut-cell rows from k_cut_rows.
+template <int STAGE, int SYS, class IDX>
 __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
 {
-    const Pt q = point_of(op);
+    const StagePt<IDX> q = stage_point<IDX>(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const double* __restrict__ in =
         STAGE == 0 ? (const double*)sa.u0 : (const double*)sa.s_in;
     const double* __restrict__ cval = (const double*)sa.cval;
-    int ijk[3];
-    phys_ijk(op, q, ijk);
     double lap = 0.0;
     double dd[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -482,14 +562,23 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
         const DevAxis& A = op.ax[d];
         if (!A.active) continue;
         const unsigned kind = (c >> (2 * d)) & 3u;
-        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-        double v = 0.0;
-        if (kind == ROW_INTERIOR)
-            v = interior64(A, in, q.p);
-        else if (kind == ROW_WALL)
-            v = wall64(A, q.p, ijk[d], in, (const double*)nullptr, 0.0, true);
-        else if (kind == ROW_CLOSURE)
-            v = cval[A.row_base + row];
+        const IDX s = (IDX)A.stride;
+        double v;
+        if (__all_sync(FULL, kind == ROW_INTERIOR)) {
+            v = interior_d<IDX>(A, in, q.p, s);
+        } else {
+            const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+            v = 0.0;
+            if (kind == ROW_INTERIOR) {
+                v = interior_d<IDX>(A, in, q.p, s);
+            } else if (kind == ROW_WALL) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
+                v = wall64(A, (long long)q.p, ijk[d], in, (const double*)nullptr, 0.0, true);
+            } else if (kind == ROW_CLOSURE) {
+                v = cval[A.row_base + row];
+            }
+        }
         if (SYS == SYS_HEAT)
             lap = lap + v;
         else
@@ -501,13 +590,19 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
         if (SYS == SYS_HEAT) {
             double src = 0.0;
             if (sp.sol.kind == SOL_SINSIN) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
                 const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
                 src = (-u) - sp.k * (sp.sol.lapfac * u);
             }
             rhs = fma(lap, sp.k, src);
         } else {
             double g[3] = {-sp.vel[0], -sp.vel[1], -sp.vel[2]};
-            if (sp.vel_kind != 0) radial_g64(sp, op, ijk, g);
+            if (sp.vel_kind != 0) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
+                radial_g64(sp, op, ijk, g);
+            }
             rhs = fma(g[2], dd[2], fma(g[1], dd[1], g[0] * dd[0]));
         }
     }
@@ -524,16 +619,16 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
     }
 }
 
-// Mixed stage: FP32 stage field, interior and wall rows; FP64 cut-cell rows (k_cut_rows);
-// compensated FP32-pair solution (u0) and accumulator.  Stage 0 reads u0 as its input.
-template <int STAGE, int SYS>
+// Mixed stage: FP32 stage field, interior and wall rows, FP32 stage accumulator; FP64
+// cut-cell rows (k_cut_rows); the solution u0 is a compensated FP32 pair (hi, lo) and
+// receives the step's accumulated increment through an error-free two-sum.  Stage 0 reads
+// u0 (hi word) as its input field.
+template <int STAGE, int SYS, class IDX>
 __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, StageArgs sa)
 {
-    const Pt q = point_of(op);
+    const StagePt<IDX> q = stage_point<IDX>(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const float* __restrict__ cval = (const float*)sa.cval;
-    int ijk[3];
-    phys_ijk(op, q, ijk);
     float lap = 0.f;
     float dd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -541,18 +636,32 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         const DevAxis& A = op.ax[d];
         if (!A.active) continue;
         const unsigned kind = (c >> (2 * d)) & 3u;
-        const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-        float v = 0.f;
-        if (STAGE == 0) {
-            const float2* in = (const float2*)sa.u0;
-            if (kind == ROW_INTERIOR) v = interior32(A, in, q.p);
-            else if (kind == ROW_WALL) v = wall32(A, q.p, ijk[d], in);
+        const IDX s = (IDX)A.stride;
+        float v;
+        if (__all_sync(FULL, kind == ROW_INTERIOR)) {
+            if (STAGE == 0)
+                v = interior_f<IDX>(A, (const float2*)sa.u0, q.p, s);
+            else
+                v = interior_f<IDX>(A, (const float*)sa.s_in, q.p, s);
         } else {
-            const float* in = (const float*)sa.s_in;
-            if (kind == ROW_INTERIOR) v = interior32(A, in, q.p);
-            else if (kind == ROW_WALL) v = wall32(A, q.p, ijk[d], in);
+            const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
+            v = 0.f;
+            if (kind == ROW_INTERIOR) {
+                if (STAGE == 0)
+                    v = interior_f<IDX>(A, (const float2*)sa.u0, q.p, s);
+                else
+                    v = interior_f<IDX>(A, (const float*)sa.s_in, q.p, s);
+            } else if (kind == ROW_WALL) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
+                if (STAGE == 0)
+                    v = wall32(A, (long long)q.p, ijk[d], (const float2*)sa.u0);
+                else
+                    v = wall32(A, (long long)q.p, ijk[d], (const float*)sa.s_in);
+            } else if (kind == ROW_CLOSURE) {
+                v = cval[A.row_base + row];
+            }
         }
-        if (kind == ROW_CLOSURE) v = cval[A.row_base + row];
         if (SYS == SYS_HEAT)
             lap = lap + v;
         else
@@ -564,6 +673,8 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         if (SYS == SYS_HEAT) {
             float src = 0.f;
             if (sp.sol.kind == SOL_SINSIN) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
                 float u = sp.sol.Sf[0][ijk[0]] * sp.sol.Sf[1][ijk[1]];
                 if (sp.sol.dims == 3) u = u * sp.sol.Sf[2][ijk[2]];
                 u = u * sa.etf_stage;
@@ -573,6 +684,8 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         } else {
             float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
             if (sp.vel_kind != 0) {
+                int ijk[3];
+                stage_ijk(op, q, ijk);
                 const float r0 = (float)op.xc[0][ijk[0]] - sp.centerf[0];
                 const float r1 = (float)op.xc[1][ijk[1]] - sp.centerf[1];
                 const float r2 = (float)op.xc[2][ijk[2]] - sp.centerf[2];
@@ -585,14 +698,18 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         }
     }
     float2* __restrict__ u0 = (float2*)sa.u0;
-    float2* __restrict__ acc = (float2*)sa.acc;
-    const float2 u = u0[q.p];
+    float* __restrict__ acc = (float*)sa.acc;
+    // increment dt*b_s*rhs with the weight held as an FP32 pair
+    const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
     if (STAGE < 3) {
-        const float2 inc = ff_mul(sa.cf_ff, rhs);
-        acc[q.p] = STAGE == 0 ? inc : ff_add(acc[q.p], inc);
+        const float2 u = u0[q.p];
+        acc[q.p] = STAGE == 0 ? inc : acc[q.p] + inc;
         ((float*)sa.s_out)[q.p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
     } else {
-        u0[q.p] = ff_add(u, ff_add(acc[q.p], ff_mul(sa.cf_ff, rhs)));
+        const float a = acc[q.p] + inc;
+        const float2 u = u0[q.p];
+        const float2 t = two_sum(u.x, a);
+        u0[q.p] = fast_two_sum(t.x, t.y + u.y);
     }
 }
 
@@ -605,6 +722,27 @@ __global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
     const long long p = op.faces[i];
     const long long nyz = (long long)op.n[1] * op.n[2];
     const int ijk[3] = {(int)(p / nyz), (int)((p / op.n[2]) % op.n[1]), (int)(p % op.n[2])};
+    if (MIXED && !LAST && (sol.kind == SOL_GAUSS_PULSE || sol.kind == SOL_RADIAL_SIN)) {
+        // FP32 stage field: the exact value in FP32 arithmetic
+        const float x0 = (float)op.xc[0][ijk[0]], x1 = (float)op.xc[1][ijk[1]],
+                    x2 = (float)op.xc[2][ijk[2]];
+        const float tf = (float)t;
+        float v;
+        if (sol.kind == SOL_GAUSS_PULSE) {
+            const float d0 = (x0 - (float)sol.p[0]) - (float)sol.p[3] * tf;
+            const float d1 = (x1 - (float)sol.p[1]) - (float)sol.p[4] * tf;
+            const float d2 = (x2 - (float)sol.p[2]) - (float)sol.p[5] * tf;
+            const float sg = (float)sol.p[6];
+            v = expf(-(d0 * d0 + d1 * d1 + d2 * d2) / (2.f * sg * sg));
+        } else {
+            const float d0 = x0 - (float)sol.p[0], d1 = x1 - (float)sol.p[1],
+                        d2 = x2 - (float)sol.p[2];
+            v = sinf(6.283185307179586f * (sqrtf(d0 * d0 + d1 * d1 + d2 * d2) -
+                                           (float)sol.p[3] - tf));
+        }
+        ((float*)out)[p] = v;
+        return;
+    }
     const double v = sol_at_point(op, sol, t, et, ijk);
     if (MIXED) {
         if (LAST)
@@ -616,12 +754,23 @@ __global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
     }
 }
 
-// Dirichlet cut-point values at t+dt/2 and t+dt (update_boundary on R)
-__global__ void k_bc_r(DevR dr, DevSol sol, int n, int d, double t1, double et1, double t2,
-                       double et2, double* out1, double* out2, const double* keep)
+// Dirichlet cut-point values at t+dt/2 and t+dt of all three R arrays (update_boundary on R)
+struct BcRArgs {
+    int n[3];
+    double* out1[3];
+    double* out2[3];
+    const double* keep[3];
+};
+__global__ void k_bc_r(DevR dr, DevSol sol, BcRArgs ra, double t1, double et1, double t2,
+                       double et2)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int d = 0;
+    while (d < 3 && i >= ra.n[d]) i -= ra.n[d++];
+    if (d == 3) return;
+    double* out1 = ra.out1[d];
+    double* out2 = ra.out2[d];
+    const double* keep = ra.keep[d];
     if (dr.dirichlet[d][i]) {
         const double* x = dr.pos[d] + 3 * (long long)i;
         out1[i] = sol_at(sol, t1, et1, x, nullptr, d, i);
@@ -907,10 +1056,18 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         ++g_launches;
     }
     if (ev) cudaEventRecord(ev[0], s);
-    if (mixed)
-        k_stage_mixed<STAGE, SYS><<<grid, block, 0, s>>>(op, sp, a);
-    else
-        k_stage64<STAGE, SYS><<<grid, block, 0, s>>>(op, sp, a);
+    const bool small = op.N < (1LL << 31) - 64;
+    if (mixed) {
+        if (small)
+            k_stage_mixed<STAGE, SYS, int><<<grid, block, 0, s>>>(op, sp, a);
+        else
+            k_stage_mixed<STAGE, SYS, long long><<<grid, block, 0, s>>>(op, sp, a);
+    } else {
+        if (small)
+            k_stage64<STAGE, SYS, int><<<grid, block, 0, s>>>(op, sp, a);
+        else
+            k_stage64<STAGE, SYS, long long><<<grid, block, 0, s>>>(op, sp, a);
+    }
     ++g_launches;
     if (ev) cudaEventRecord(ev[1], s);
     if (op.n_faces) {
@@ -953,12 +1110,21 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
 
     if (ev) cudaEventRecord(ev[0], s);
     const double th = t + dt * rki[1], tf = t + dt * rki[3];
-    for (int d = 0; d < 3; d++) {
-        const int n = (int)op.nR[d];
-        if (!n) continue;
-        k_bc_r<<<(n + 127) / 128, 128, 0, s>>>(dr, sp.sol, n, d, th, et(th), tf, et(tf),
-                                               b.Rhalf[d], b.Rfull[d], b.R[d]);
-        ++g_launches;
+    {
+        BcRArgs ra;
+        long long tot = 0;
+        for (int d = 0; d < 3; d++) {
+            ra.n[d] = (int)op.nR[d];
+            ra.out1[d] = b.Rhalf[d];
+            ra.out2[d] = b.Rfull[d];
+            ra.keep[d] = b.R[d];
+            tot += ra.n[d];
+        }
+        if (tot) {
+            k_bc_r<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(dr, sp.sol, ra, th, et(th), tf,
+                                                                 et(tf));
+            ++g_launches;
+        }
     }
     if (ev) cudaEventRecord(ev[1], s);
     StageArgs sa[4];
