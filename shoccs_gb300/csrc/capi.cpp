@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -179,6 +180,43 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
 }
 
 bool bad_bc(int b) { return b < 0 || b > 2; }
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn()
+{
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(ptr);
+    }
+    return fn;
+}
+
+// 3-D tensor map over a field of nx x ny x nz elements (z fastest): boxes of one plane of
+// (32 + 8) x (8 + 4) elements, the tile of k_stage_mixed_tma plus its halo
+bool make_plane_map(CUtensorMap* m, void* base, int esz, const int it[3])
+{
+    EncodeTiled enc = encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)it[2], (cuuint64_t)it[1], (cuuint64_t)it[0]};
+    const cuuint64_t strides[2] = {(cuuint64_t)it[2] * esz, (cuuint64_t)it[2] * it[1] * esz};
+    const cuuint32_t box[3] = {40, 12, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+               base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 } // namespace
 
 extern "C" {
@@ -467,6 +505,27 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.sb = (char*)base + N * es_s;
     }
     SH_CUDA(S->mem.alloc((size_t)p->op.n_cut_rows * 8, &S->b.cval));
+    {
+        void* e = nullptr;
+        SH_CUDA(S->mem.alloc(sizeof(unsigned), &e));
+        S->b.err = (unsigned*)e;
+        SH_CUDA(cudaMemsetAsync(e, 0, sizeof(unsigned), s));
+    }
+    // TMA plane-marching stages for 3-D mixed solves whose planes are 16-byte aligned
+    {
+        const int* it = p->comp.it;
+        const bool three_d = it[0] > 1 && it[1] > 1 && it[2] > 1;
+        if (d->prec == PREC_MIXED && three_d && it[2] % 4 == 0 && N < (1LL << 31) - 64 &&
+            !std::getenv("SHOCCS_DISABLE_TMA")) {
+            S->b.tma = make_plane_map(&S->b.tm_u0, S->b.u0, 8, it) &&
+                       make_plane_map(&S->b.tm_sa, S->b.sa, 4, it) &&
+                       make_plane_map(&S->b.tm_sb, S->b.sb, 4, it);
+            if (const char* px = std::getenv("SHOCCS_TMA_PX")) {
+                const int v = std::atoi(px);
+                if (v >= 4 && v <= 1024) S->b.tma_px = v;
+            }
+        }
+    }
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
     SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (d->prec == PREC_FP64 ? 8 : 4), s));
     for (int r = 0; r < 3; r++) {
@@ -548,6 +607,19 @@ shoccs_status shoccs_system_get_state(shoccs_system* S, shoccs_field* u, int whe
     return SHOCCS_OK;
 }
 
+static shoccs_status check_wait_flag(shoccs_system* S, cudaStream_t s)
+{
+    if (!S->b.tma) return SHOCCS_OK;
+    unsigned flag = 0;
+    SH_CUDA(cudaMemcpyAsync(&flag, S->b.err, sizeof flag, cudaMemcpyDeviceToHost, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    if (flag) {
+        SH_CUDA(cudaMemsetAsync(S->b.err, 0, sizeof flag, s));
+        return fail(SHOCCS_ETIMEOUT, "a stage kernel's bounded wait for its TMA copies gave up");
+    }
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nsteps,
                                 void* stream)
 {
@@ -560,7 +632,7 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     }
     SH_CUDA(cudaStreamSynchronize(s));
     S->t = t;
-    return SHOCCS_OK;
+    return check_wait_flag(S, s);
 }
 
 shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, int nsteps,
@@ -610,6 +682,7 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
     }
     for (auto& e : ev)
         if (e) cudaEventDestroy(e);
+    if (st == SHOCCS_OK) st = check_wait_flag(S, s);
     return st;
 }
 

@@ -5,6 +5,7 @@
 #include "host/gpu_layout.hpp"
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace sgb
@@ -96,6 +97,12 @@ struct StepBuffers {
     double* R[3];      // state R values (time t)
     double* Rhalf[3];  // Dirichlet R values at t + dt/2
     double* Rfull[3];  // Dirichlet R values at t + dt
+    // TMA plane-marching path of the mixed stages (3-D grids): tensor maps of the stage
+    // inputs, planes per block, and the device error flag of its bounded waits
+    int tma = 0;
+    int tma_px = 32;
+    unsigned* err = nullptr;
+    CUtensorMap tm_u0, tm_sa, tm_sb;
 };
 
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,

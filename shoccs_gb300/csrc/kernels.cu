@@ -22,6 +22,7 @@
 #include "device.cuh"
 
 #include <atomic>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 
@@ -250,22 +251,6 @@ __device__ __forceinline__ float2 fast_two_sum(float a, float b)
     const float s = a + b;
     const float e = b - (s - a);
     return make_float2(s, e);
-}
-__device__ __forceinline__ float2 ff_add(float2 x, float2 y)
-{
-    float2 s = two_sum(x.x, y.x);
-    const float2 t = two_sum(x.y, y.y);
-    s.y += t.x;
-    s = fast_two_sum(s.x, s.y);
-    s.y += t.y;
-    return fast_two_sum(s.x, s.y);
-}
-__device__ __forceinline__ float2 ff_mul(float2 a, float b)
-{
-    const float p = a.x * b;
-    float e = fmaf(a.x, b, -p);
-    e = fmaf(a.y, b, e);
-    return fast_two_sum(p, e);
 }
 __device__ __forceinline__ float2 ff_from_double(double d)
 {
@@ -713,6 +698,242 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
     }
 }
 
+// ---- TMA plane-marching mixed stage (3-D grids) -----------------------------------------
+// A block owns a TY x TZ column tile of the (y, z) plane and marches along x over `px`
+// planes.  Stage-field planes (tile + 2-point y halo + 4-point z halo, the z start rounded to
+// a 16-byte boundary) arrive in shared memory by cp.async.bulk.tensor into a ring of NS
+// slots, each guarded by an mbarrier; the ring keeps planes i-2 .. i+5 so four planes are in
+// flight while plane i is computed.  Interior rows read their 5-point stencils from shared
+// memory; wall and cut-cell rows (rare, and not warp-uniform) use the global-memory path.
+// Every mbarrier wait is bounded: on time-out the block records an error flag, stops issuing
+// copies and drains the ones in flight before it returns.
+constexpr int TMA_TY = 8, TMA_TZ = 32, TMA_HY = 2, TMA_HZ = 4, TMA_NS = 8;
+constexpr int TMA_BY = TMA_TY + 2 * TMA_HY; // 12
+constexpr int TMA_BZ = TMA_TZ + 2 * TMA_HZ; // 40
+constexpr unsigned TMA_WAIT_LIMIT = 1u << 20;
+
+__device__ __forceinline__ unsigned smem_u32(const void* ptr)
+{
+    return (unsigned)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity)
+{
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smem_u32(b)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity)
+{
+    for (unsigned it = 0; it < TMA_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1,
+                                            int c2, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+                 "l"((unsigned long long)tm), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <int STAGE, int SYS>
+__global__ void __launch_bounds__(256) k_stage_mixed_tma(const __grid_constant__ CUtensorMap tm_in,
+                                                         DevOp op, SysParams sp, StageArgs sa,
+                                                         int px, unsigned* err)
+{
+    using TIN = typename std::conditional<STAGE == 0, float2, float>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TIN* ring = reinterpret_cast<TIN*>(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + TMA_NS * TMA_BY * TMA_BZ * sizeof(TIN));
+    constexpr unsigned SLOT = TMA_BY * TMA_BZ;
+    constexpr unsigned BYTES = SLOT * sizeof(TIN);
+
+    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tz;
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int k0 = blockIdx.x * TMA_TZ, j0 = blockIdx.y * TMA_TY, x0 = blockIdx.z * px;
+    const int k = k0 + tz, j = j0 + ty;
+    const int xend = min(x0 + px, nx);
+    const bool col_valid = (j < ny) && (k < nz);
+    const int pfirst = x0 - 2, plast = xend + 1;
+
+    auto issue = [&](int plane) {
+        const int r = plane - pfirst;
+        const int slot = r % TMA_NS;
+        mbar_expect_tx(&bars[slot], BYTES);
+        tma_load_3d(ring + slot * SLOT, &tm_in, k0 - TMA_HZ, j0 - TMA_HY, plane, &bars[slot]);
+    };
+    if (tid == 0) {
+        for (int s2 = 0; s2 < TMA_NS; s2++) mbar_init(&bars[s2], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int issued_to = min(pfirst + TMA_NS - 1, plast);
+    if (tid == 0)
+        for (int pl = pfirst; pl <= issued_to; ++pl) issue(pl);
+
+    bool ok = true;
+    auto wait_plane = [&](int plane) {
+        const int r = plane - pfirst;
+        if (ok && !mbar_wait_bounded(&bars[r % TMA_NS], (unsigned)((r / TMA_NS) & 1))) {
+            ok = false;
+            atomicOr(err, 1u);
+        }
+    };
+    for (int pl = pfirst; pl <= min(x0 + 1, plast); ++pl) wait_plane(pl);
+
+    const float* __restrict__ cval = (const float*)sa.cval;
+    float2* __restrict__ u0g = (float2*)sa.u0;
+    float* __restrict__ accg = (float*)sa.acc;
+    const int cz = TMA_HZ + tz, cy = TMA_HY + ty;
+    const long long chunk_row = (long long)blockIdx.x; // chunk index along z within a line
+
+    for (int i = x0; i < xend; ++i) {
+        const int p = (i * ny + j) * nz + k;
+        float2 u = make_float2(0.f, 0.f);
+        float accv = 0.f;
+        if (col_valid) {
+            if (STAGE > 0) u = u0g[p];
+            if (STAGE > 0) accv = accg[p];
+        }
+        if (i + 2 <= plast) wait_plane(i + 2);
+        const unsigned c = (col_valid && ok) ? op.cls[p] : 0u;
+        const TIN* sl[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) sl[m] = ring + ((i - 2 + m - pfirst) % TMA_NS) * SLOT;
+        auto S = [&](int m, int yy, int zz) -> float {
+            if constexpr (STAGE == 0) return sl[m][yy * TMA_BZ + zz].x;
+            else return sl[m][yy * TMA_BZ + zz];
+        };
+        if constexpr (STAGE == 0) {
+            if (col_valid) u = sl[2][cy * TMA_BZ + cz];
+        }
+        float lap = 0.f;
+        float dd[3] = {0.f, 0.f, 0.f};
+        const long long chunk = ((long long)i * ny + j) * op.nzc + chunk_row;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const DevAxis& A = op.ax[d];
+            const unsigned kind = (c >> (2 * d)) & 3u;
+            float v;
+            if (__all_sync(FULL, kind == ROW_INTERIOR)) {
+                float xm2, xm1, x0v, xp1, xp2;
+                if (d == 0) {
+                    xm2 = S(0, cy, cz); xm1 = S(1, cy, cz); x0v = S(2, cy, cz);
+                    xp1 = S(3, cy, cz); xp2 = S(4, cy, cz);
+                } else if (d == 1) {
+                    xm2 = S(2, cy - 2, cz); xm1 = S(2, cy - 1, cz); x0v = S(2, cy, cz);
+                    xp1 = S(2, cy + 1, cz); xp2 = S(2, cy + 2, cz);
+                } else {
+                    xm2 = S(2, cy, cz - 2); xm1 = S(2, cy, cz - 1); x0v = S(2, cy, cz);
+                    xp1 = S(2, cy, cz + 1); xp2 = S(2, cy, cz + 2);
+                }
+                if (A.antisym) {
+                    v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
+                } else {
+                    float r = A.icf[0] * xm2;
+                    r = fmaf(A.icf[1], xm1, r);
+                    r = fmaf(A.icf[2], x0v, r);
+                    r = fmaf(A.icf[3], xp1, r);
+                    v = fmaf(A.icf[4], xp2, r);
+                }
+            } else {
+                const int row = closure_row(A, kind == ROW_CLOSURE, chunk);
+                v = 0.f;
+                const TIN* gin = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
+                if (kind == ROW_INTERIOR) {
+                    v = interior_f<int>(A, gin, p, (int)A.stride);
+                } else if (kind == ROW_WALL) {
+                    const int coord = d == 0 ? i : (d == 1 ? j : k);
+                    v = wall32(A, (long long)p, coord, gin);
+                } else if (kind == ROW_CLOSURE) {
+                    v = cval[A.row_base + row];
+                }
+            }
+            if (SYS == SYS_HEAT)
+                lap = lap + v;
+            else
+                dd[d] = v;
+        }
+        if (col_valid && ok) {
+            float rhs = 0.f;
+            if (c & 0x3Fu) {
+                if (SYS == SYS_HEAT) {
+                    float src = 0.f;
+                    if (sp.sol.kind == SOL_SINSIN) {
+                        float uu = sp.sol.Sf[0][i] * sp.sol.Sf[1][j];
+                        if (sp.sol.dims == 3) uu = uu * sp.sol.Sf[2][k];
+                        uu = uu * sa.etf_stage;
+                        src = (-uu) - sp.kf * ((float)sp.sol.lapfac * uu);
+                    }
+                    rhs = fmaf(lap, sp.kf, src);
+                } else {
+                    float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
+                    if (sp.vel_kind != 0) {
+                        const float r0 = (float)op.xc[0][i] - sp.centerf[0];
+                        const float r1 = (float)op.xc[1][j] - sp.centerf[1];
+                        const float r2 = (float)op.xc[2][k] - sp.centerf[2];
+                        const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
+                        g0 = -r0 * il;
+                        g1 = -r1 * il;
+                        g2 = -r2 * il;
+                    }
+                    rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
+                }
+            }
+            const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
+            if (STAGE < 3) {
+                accg[p] = STAGE == 0 ? inc : accv + inc;
+                ((float*)sa.s_out)[p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
+            } else {
+                const float a = accv + inc;
+                const float2 t = two_sum(u.x, a);
+                u0g[p] = fast_two_sum(t.x, t.y + u.y);
+            }
+        }
+        __syncthreads(); // every thread is done with the slot of plane i-2
+        if (tid == 0 && ok) {
+            const int nxt = i - 2 + TMA_NS;
+            if (nxt <= plast) {
+                fence_proxy_async();
+                issue(nxt);
+                issued_to = nxt;
+            }
+        }
+    }
+    // drain: a block that gave up waits (bounded) for the copies it issued before returning
+    if (!ok && tid == 0) {
+        for (int pl = pfirst; pl <= issued_to; ++pl) {
+            const int r = pl - pfirst;
+            mbar_wait_bounded(&bars[r % TMA_NS], (unsigned)((r / TMA_NS) & 1));
+        }
+    }
+}
+
 // Dirichlet face values of the stage output (update_boundary on D)
 template <bool MIXED, bool LAST>
 __global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
@@ -1036,7 +1257,7 @@ namespace
 {
 template <int STAGE, int SYS>
 void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArgs& a,
-                  cudaStream_t s, cudaEvent_t* ev)
+                  const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev)
 {
     const dim3 grid = point_grid(op), block(32, BY);
     const bool mixed = prec == PREC_MIXED;
@@ -1057,7 +1278,14 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
     }
     if (ev) cudaEventRecord(ev[0], s);
     const bool small = op.N < (1LL << 31) - 64;
-    if (mixed) {
+    if (mixed && b.tma) {
+        const CUtensorMap& tm = STAGE == 0 ? b.tm_u0 : (STAGE == 2 ? b.tm_sb : b.tm_sa);
+        const dim3 tgrid((op.it2 + TMA_TZ - 1) / TMA_TZ, (op.it1 + TMA_TY - 1) / TMA_TY,
+                         (op.it0 + b.tma_px - 1) / b.tma_px);
+        const size_t smem = TMA_NS * TMA_BY * TMA_BZ * (STAGE == 0 ? 8 : 4) + TMA_NS * 8;
+        k_stage_mixed_tma<STAGE, SYS><<<tgrid, dim3(32, TMA_TY), smem, s>>>(tm, op, sp, a,
+                                                                            b.tma_px, b.err);
+    } else if (mixed) {
         if (small)
             k_stage_mixed<STAGE, SYS, int><<<grid, block, 0, s>>>(op, sp, a);
         else
@@ -1087,12 +1315,12 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
 
 template <int SYS>
 void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[4],
-                   cudaStream_t s, cudaEvent_t* ev)
+                   const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev)
 {
-    launch_stage<0, SYS>(op, sp, prec, sa[0], s, ev ? ev + 2 : nullptr);
-    launch_stage<1, SYS>(op, sp, prec, sa[1], s, ev ? ev + 4 : nullptr);
-    launch_stage<2, SYS>(op, sp, prec, sa[2], s, ev ? ev + 6 : nullptr);
-    launch_stage<3, SYS>(op, sp, prec, sa[3], s, ev ? ev + 8 : nullptr);
+    launch_stage<0, SYS>(op, sp, prec, sa[0], b, s, ev ? ev + 2 : nullptr);
+    launch_stage<1, SYS>(op, sp, prec, sa[1], b, s, ev ? ev + 4 : nullptr);
+    launch_stage<2, SYS>(op, sp, prec, sa[2], b, s, ev ? ev + 6 : nullptr);
+    launch_stage<3, SYS>(op, sp, prec, sa[3], b, s, ev ? ev + 8 : nullptr);
 }
 } // namespace
 
@@ -1148,9 +1376,9 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.etf_stage = (float)a.et_stage;
     }
     if (sp.kind == SYS_HEAT)
-        launch_stages<SYS_HEAT>(op, sp, prec, sa, s, ev);
+        launch_stages<SYS_HEAT>(op, sp, prec, sa, b, s, ev);
     else
-        launch_stages<SYS_WAVE>(op, sp, prec, sa, s, ev);
+        launch_stages<SYS_WAVE>(op, sp, prec, sa, b, s, ev);
     for (int d = 0; d < 3; d++) std::swap(b.R[d], b.Rfull[d]);
     return cudaGetLastError();
 }
