@@ -272,7 +272,8 @@ def main():
                               "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": t_ms / args.steps, "higher_is_better": True,
                               "config": config(nsteps), "gpu_launches": int(launches),
-                              "kernel_ms": kms, "note": "mixed solves only"}), flush=True)
+                              "kernel_ms": kms, "stage_kernel": sysm.stage_kernel,
+                              "note": "mixed solves only"}), flush=True)
         return 0
 
     # ---- FP64 path (timed beside it) ----
@@ -356,7 +357,8 @@ def main():
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_stage_mixed<0..3, wave> (4 launches per RK4 step)",
+                     "kernel": "mixed RK4 stage kernels, %s variant (4 launches per RK4 step)"
+                               % sysm.stage_kernel,
                      "algorithmic_bytes_per_launch_avg": bytes_step / 4,
                      "avg_launch_ms": stage_ms / n_launch, "peak_kind": peak_kind,
                      "per_stage": per_stage},

@@ -272,6 +272,15 @@ class System:
             _capi.check(st)
         return vals, st == _capi.OK
 
+    STAGE_KERNELS = {0: "point", 1: "tma", 2: "col1", 3: "col2", 4: "col4"}
+
+    @property
+    def stage_kernel(self):
+        """name of the stage-kernel variant this system runs (see shoccs_system_path)"""
+        v = ctypes.c_int()
+        _capi.check(_capi.lib().shoccs_system_path(self._h, ctypes.byref(v)))
+        return self.STAGE_KERNELS[v.value]
+
     def timestep(self, cfl):
         dt = ctypes.c_double()
         _capi.check(_capi.lib().shoccs_system_timestep(self._h, float(cfl), ctypes.byref(dt)))

@@ -95,6 +95,7 @@ SIGNATURES = {
                           ctypes.c_void_p],
     "shoccs_system_stats": [ctypes.c_void_p, ctypes.c_double, c_double_p, ctypes.c_void_p],
     "shoccs_system_timestep": [ctypes.c_void_p, ctypes.c_double, c_double_p],
+    "shoccs_system_path": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)],
     "shoccs_kernel_launches": [],
     "shoccs_last_error": [ctypes.c_char_p, ctypes.c_size_t],
 }

@@ -203,16 +203,20 @@ EncodeTiled encode_fn()
 }
 
 // 3-D tensor map over a field of nx x ny x nz elements (z fastest): boxes of one plane of
-// (32 + 8) x (8 + 4) elements, the tile of k_stage_mixed_tma plus its halo
-bool make_plane_map(CUtensorMap* m, void* base, int esz, const int it[3])
+// (32 + 8) x (8 + 4) elements (the tile of k_stage_mixed_tma plus its halo) or, with
+// halo = false, of the 32 x 8 tile alone
+bool make_plane_map(CUtensorMap* m, void* base, int esz, const int it[3], bool halo = true)
 {
     EncodeTiled enc = encode_fn();
     if (!enc) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)it[2], (cuuint64_t)it[1], (cuuint64_t)it[0]};
     const cuuint64_t strides[2] = {(cuuint64_t)it[2] * esz, (cuuint64_t)it[2] * it[1] * esz};
-    const cuuint32_t box[3] = {40, 12, 1};
+    const cuuint32_t box[3] = {halo ? 40u : 32u, halo ? 12u : 8u, 1u};
     const cuuint32_t es[3] = {1, 1, 1};
-    return enc(m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+    const CUtensorMapDataType ty = esz == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                   : esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                              : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    return enc(m, ty, 3,
                base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -423,6 +427,71 @@ shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_fi
 // ---------------------------------------------------------------------------------------
 // systems
 // ---------------------------------------------------------------------------------------
+// Pick the mixed stage kernel for this system: every candidate runs a few RK4 steps on the
+// system's own buffers (timed with CUDA events), the fastest is kept, and the state is reset.
+// All candidates compute the same values; they differ only in data movement.
+static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
+{
+    struct Cand {
+        const char* name;
+        int tma, col;
+    };
+    std::vector<Cand> cands;
+    if (S->b.tma) cands.push_back({"tma", 1, 0});
+    cands.push_back({"col1", 0, 1});
+    cands.push_back({"col2", 0, 2});
+    cands.push_back({"col4", 0, 4});
+    cands.push_back({"point", 0, 0});
+    if (const char* force = std::getenv("SHOCCS_STAGE_KERNEL")) {
+        for (const auto& c : cands)
+            if (std::string(force) == c.name) {
+                S->b.tma = c.tma;
+                S->b.col_nx = c.col;
+                return SHOCCS_OK;
+            }
+        return fail(SHOCCS_EINVAL, std::string("SHOCCS_STAGE_KERNEL: unknown or unavailable ") +
+                                       force);
+    }
+    const long long N = S->P->mesh.size();
+    const double h = std::min(S->P->mesh.h[0], std::min(S->P->mesh.h[1], S->P->mesh.h[2]));
+    const double dt = 1e-3 * h;
+    cudaEvent_t e0, e1;
+    SH_CUDA(cudaEventCreate(&e0));
+    SH_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Cand pick = cands.back();
+    const int reps = N > (1 << 22) ? 3 : 2;
+    for (const auto& c : cands) {
+        S->b.tma = c.tma;
+        S->b.col_nx = c.col;
+        SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, 0.0, dt, s));
+        SH_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; r++)
+            SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, 0.0, dt, s));
+        SH_CUDA(cudaEventRecord(e1, s));
+        SH_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        SH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    S->b.tma = pick.tma;
+    S->b.col_nx = pick.col;
+    // reset the registers the trial steps touched
+    SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * 8, s));
+    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * 4, s));
+    for (int r = 0; r < 3; r++)
+        if (!S->P->mesh.R[r].empty())
+            SH_CUDA(cudaMemsetAsync(S->b.R[r], 0, S->P->mesh.R[r].size() * 8, s));
+    if (S->b.err) SH_CUDA(cudaMemsetAsync(S->b.err, 0, sizeof(unsigned), s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* d,
                                    shoccs_system** out)
 {
@@ -515,15 +584,17 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     {
         const int* it = p->comp.it;
         const bool three_d = it[0] > 1 && it[1] > 1 && it[2] > 1;
-        if (d->prec == PREC_MIXED && three_d && it[2] % 4 == 0 && N < (1LL << 31) - 64 &&
+        if (d->prec == PREC_MIXED && three_d && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
             !std::getenv("SHOCCS_DISABLE_TMA")) {
             S->b.tma = make_plane_map(&S->b.tm_u0, S->b.u0, 8, it) &&
                        make_plane_map(&S->b.tm_sa, S->b.sa, 4, it) &&
-                       make_plane_map(&S->b.tm_sb, S->b.sb, 4, it);
-            if (const char* px = std::getenv("SHOCCS_TMA_PX")) {
-                const int v = std::atoi(px);
-                if (v >= 4 && v <= 1024) S->b.tma_px = v;
-            }
+                       make_plane_map(&S->b.tm_sb, S->b.sb, 4, it) &&
+                       make_plane_map(&S->b.tm_u0t, S->b.u0, 8, it, false) &&
+                       make_plane_map(&S->b.tm_acct, S->b.acc, 4, it, false) &&
+                       make_plane_map(&S->b.tm_cls, (void*)p->op.cls, 1, it, false);
+        }
+        if (d->prec == PREC_MIXED && three_d) {
+            if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;
         }
     }
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));

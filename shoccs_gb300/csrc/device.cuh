@@ -100,9 +100,12 @@ struct StepBuffers {
     // TMA plane-marching path of the mixed stages (3-D grids): tensor maps of the stage
     // inputs, planes per block, and the device error flag of its bounded waits
     int tma = 0;
-    int tma_px = 32;
+    // column-blocked mixed stages (3-D grids): planes per thread, 0 = per-point kernel
+    int col_nx = 0;
     unsigned* err = nullptr;
-    CUtensorMap tm_u0, tm_sa, tm_sb;
+    CUtensorMap tm_u0, tm_sa, tm_sb; // stage inputs: one plane tile plus halo
+    CUtensorMap tm_u0t, tm_acct;     // u0 and accumulator: one plane tile, no halo
+    CUtensorMap tm_cls;              // class bytes: one plane tile
 };
 
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,

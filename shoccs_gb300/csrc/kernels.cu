@@ -21,6 +21,7 @@
 //   compute_scalar_stats             src/systems/detail/scalar_system_utils.hpp:77-181
 #include "device.cuh"
 
+#include <algorithm>
 #include <atomic>
 #include <type_traits>
 #include <cmath>
@@ -698,6 +699,149 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
     }
 }
 
+// ---- column-blocked mixed stage (3-D grids) ------------------------------------------------
+// Each thread owns NX consecutive x-planes of one (y, z) column.  The x-stencil values of
+// the column come from a register window of NX + 4 loads; the y / z stencil values, the
+// class bytes, u0 and the accumulator of all NX points are issued together, before any
+// class byte is decoded, with neighbour coordinates clamped into the grid so every
+// speculative load stays in bounds (values of rows that turn out not to be interior are
+// simply not used).  Warps whose 32 lanes all have interior rows along an axis take the
+// fast path; the others fall back to the per-lane wall / cut-cell path.
+template <int STAGE, int SYS, int NX>
+__global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp, StageArgs sa)
+{
+    using TIN = typename std::conditional<STAGE == 0, float2, float>::type;
+    const TIN* __restrict__ in = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
+    auto L = [&](int idx) -> float {
+        if constexpr (STAGE == 0) return __ldg(in + idx).x;
+        else return __ldg(in + idx);
+    };
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int i0 = blockIdx.z * NX;
+    const bool col_valid = (j < ny) && (k < nz);
+    const int plane = ny * nz;
+    const int jc = min(j, ny - 1), kc = min(k, nz - 1);
+    const int col = jc * nz + kc;
+    // clamped neighbour offsets within a plane
+    const int ym2 = (max(jc - 2, 0) - jc) * nz, ym1 = (max(jc - 1, 0) - jc) * nz;
+    const int yp1 = (min(jc + 1, ny - 1) - jc) * nz, yp2 = (min(jc + 2, ny - 1) - jc) * nz;
+    const int zm2 = max(kc - 2, 0) - kc, zm1 = max(kc - 1, 0) - kc;
+    const int zp1 = min(kc + 1, nz - 1) - kc, zp2 = min(kc + 2, nz - 1) - kc;
+
+    float w[NX + 4]; // x window: planes i0-2 .. i0+NX+1 of this column
+#pragma unroll
+    for (int m = 0; m < NX + 4; m++) w[m] = L(min(max(i0 - 2 + m, 0), nx - 1) * plane + col);
+    unsigned c[NX];
+    float yv[NX][4], zv[NX][4];
+    float2 uu[NX];
+    float av[NX];
+#pragma unroll
+    for (int t = 0; t < NX; t++) {
+        const int ic = min(i0 + t, nx - 1);
+        const int p = ic * plane + col;
+        const bool valid = col_valid && (i0 + t < nx);
+        c[t] = valid ? (unsigned)op.cls[p] : 0u;
+        yv[t][0] = L(p + ym2); yv[t][1] = L(p + ym1); yv[t][2] = L(p + yp1); yv[t][3] = L(p + yp2);
+        zv[t][0] = L(p + zm2); zv[t][1] = L(p + zm1); zv[t][2] = L(p + zp1); zv[t][3] = L(p + zp2);
+        if constexpr (STAGE > 0) {
+            uu[t] = ((const float2*)sa.u0)[p];
+            av[t] = ((const float*)sa.acc)[p];
+        }
+    }
+    const float* __restrict__ cval = (const float*)sa.cval;
+#pragma unroll
+    for (int t = 0; t < NX; t++) {
+        const int i = i0 + t;
+        const int p = min(i, nx - 1) * plane + col;
+        float lap = 0.f;
+        float dd[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const DevAxis& A = op.ax[d];
+            const unsigned kind = (c[t] >> (2 * d)) & 3u;
+            float v;
+            if (__all_sync(FULL, kind == ROW_INTERIOR)) {
+                float xm2, xm1, x0v, xp1, xp2;
+                if (d == 0) {
+                    xm2 = w[t]; xm1 = w[t + 1]; x0v = w[t + 2]; xp1 = w[t + 3]; xp2 = w[t + 4];
+                } else if (d == 1) {
+                    xm2 = yv[t][0]; xm1 = yv[t][1]; x0v = w[t + 2]; xp1 = yv[t][2]; xp2 = yv[t][3];
+                } else {
+                    xm2 = zv[t][0]; xm1 = zv[t][1]; x0v = w[t + 2]; xp1 = zv[t][2]; xp2 = zv[t][3];
+                }
+                if (A.antisym) {
+                    v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
+                } else {
+                    float r = A.icf[0] * xm2;
+                    r = fmaf(A.icf[1], xm1, r);
+                    r = fmaf(A.icf[2], x0v, r);
+                    r = fmaf(A.icf[3], xp1, r);
+                    v = fmaf(A.icf[4], xp2, r);
+                }
+            } else {
+                const long long chunk = ((long long)min(i, nx - 1) * ny + j) * op.nzc + blockIdx.x;
+                const int row = closure_row(A, kind == ROW_CLOSURE, chunk);
+                v = 0.f;
+                if (kind == ROW_INTERIOR) {
+                    v = interior_f<int>(A, in, p, (int)A.stride);
+                } else if (kind == ROW_WALL) {
+                    const int coord = d == 0 ? i : (d == 1 ? j : k);
+                    v = wall32(A, (long long)p, coord, in);
+                } else if (kind == ROW_CLOSURE) {
+                    v = cval[A.row_base + row];
+                }
+            }
+            if (SYS == SYS_HEAT)
+                lap = lap + v;
+            else
+                dd[d] = v;
+        }
+        if (!(col_valid && i < nx)) continue;
+        float rhs = 0.f;
+        if (c[t] & 0x3Fu) {
+            if (SYS == SYS_HEAT) {
+                float src = 0.f;
+                if (sp.sol.kind == SOL_SINSIN) {
+                    float q = sp.sol.Sf[0][i] * sp.sol.Sf[1][j];
+                    if (sp.sol.dims == 3) q = q * sp.sol.Sf[2][k];
+                    q = q * sa.etf_stage;
+                    src = (-q) - sp.kf * ((float)sp.sol.lapfac * q);
+                }
+                rhs = fmaf(lap, sp.kf, src);
+            } else {
+                float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
+                if (sp.vel_kind != 0) {
+                    const float r0 = (float)op.xc[0][i] - sp.centerf[0];
+                    const float r1 = (float)op.xc[1][j] - sp.centerf[1];
+                    const float r2 = (float)op.xc[2][k] - sp.centerf[2];
+                    const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
+                    g0 = -r0 * il;
+                    g1 = -r1 * il;
+                    g2 = -r2 * il;
+                }
+                rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
+            }
+        }
+        float2* __restrict__ u0 = (float2*)sa.u0;
+        float* __restrict__ acc = (float*)sa.acc;
+        const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
+        if constexpr (STAGE == 0) {
+            const float2 u = ((const float2*)sa.u0)[p];
+            acc[p] = inc;
+            ((float*)sa.s_out)[p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
+        } else if constexpr (STAGE < 3) {
+            acc[p] = av[t] + inc;
+            ((float*)sa.s_out)[p] = uu[t].x + fmaf(sa.ci_ff.x, rhs, uu[t].y);
+        } else {
+            const float a = av[t] + inc;
+            const float2 tt = two_sum(uu[t].x, a);
+            u0[p] = fast_two_sum(tt.x, tt.y + uu[t].y);
+        }
+    }
+}
+
 // ---- TMA plane-marching mixed stage (3-D grids) -----------------------------------------
 // A block owns a TY x TZ column tile of the (y, z) plane and marches along x over `px`
 // planes.  Stage-field planes (tile + 2-point y halo + 4-point z halo, the z start rounded to
@@ -761,125 +905,199 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+// Warp-specialised persistent stage.  Work is the list of (tile, plane) pairs in
+// tile-major order; CTA b owns the contiguous range [b*W/G, (b+1)*W/G), cut at tile
+// boundaries into segments, so one wave of CTAs covers the grid evenly.  Per segment the
+// producer warp (warp 8, lane 0) streams planes x_a-2 .. x_b+1 of its tile into a ring of
+// TMA_NS slots: each slot gets the stage-field plane with its halo and, for computed
+// planes, the class bytes, u0 and accumulator tiles of that plane.  full[s] completes when
+// a slot's copies have landed; empty[s] when all eight consumer warps are done with it.
+// Consumers (warps 0..7, one tile row each, one point per lane) read only shared memory on
+// the interior fast path.  Every wait is bounded; on time-out the CTA records an error
+// flag, stops issuing copies, and drains the ones in flight before it returns.
 template <int STAGE, int SYS>
-__global__ void __launch_bounds__(256) k_stage_mixed_tma(const __grid_constant__ CUtensorMap tm_in,
+__global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__ CUtensorMap tm_in,
+                                                         const __grid_constant__ CUtensorMap tm_u0,
+                                                         const __grid_constant__ CUtensorMap tm_acc,
+                                                         const __grid_constant__ CUtensorMap tm_cls,
                                                          DevOp op, SysParams sp, StageArgs sa,
-                                                         int px, unsigned* err)
+                                                         unsigned* err)
 {
     using TIN = typename std::conditional<STAGE == 0, float2, float>::type;
+    constexpr unsigned S_BYTES = TMA_BY * TMA_BZ * sizeof(TIN);
+    constexpr unsigned C_BYTES = TMA_TY * TMA_TZ;
+    constexpr unsigned U_BYTES = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 8u;
+    constexpr unsigned A_BYTES = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
+    constexpr unsigned SLOT = S_BYTES + C_BYTES + U_BYTES + A_BYTES;
+    static_assert(SLOT % 128 == 0 && S_BYTES % 128 == 0 && C_BYTES % 128 == 0 &&
+                      U_BYTES % 128 == 0,
+                  "TMA destinations stay 128-byte aligned");
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    TIN* ring = reinterpret_cast<TIN*>(smem_raw);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + TMA_NS * TMA_BY * TMA_BZ * sizeof(TIN));
-    constexpr unsigned SLOT = TMA_BY * TMA_BZ;
-    constexpr unsigned BYTES = SLOT * sizeof(TIN);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + TMA_NS * SLOT);
+    uint64_t* empty = full + TMA_NS;
 
-    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tz;
+    const int lane = threadIdx.x, warp = threadIdx.y;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
-    const int k0 = blockIdx.x * TMA_TZ, j0 = blockIdx.y * TMA_TY, x0 = blockIdx.z * px;
-    const int k = k0 + tz, j = j0 + ty;
-    const int xend = min(x0 + px, nx);
-    const bool col_valid = (j < ny) && (k < nz);
-    const int pfirst = x0 - 2, plast = xend + 1;
+    const int tiles_z = (nz + TMA_TZ - 1) / TMA_TZ;
+    const long long work = (long long)tiles_z * ((ny + TMA_TY - 1) / TMA_TY) * nx;
+    const long long w_begin = work * blockIdx.x / gridDim.x;
+    const long long w_end = work * (blockIdx.x + 1) / gridDim.x;
 
-    auto issue = [&](int plane) {
-        const int r = plane - pfirst;
-        const int slot = r % TMA_NS;
-        mbar_expect_tx(&bars[slot], BYTES);
-        tma_load_3d(ring + slot * SLOT, &tm_in, k0 - TMA_HZ, j0 - TMA_HY, plane, &bars[slot]);
-    };
-    if (tid == 0) {
-        for (int s2 = 0; s2 < TMA_NS; s2++) mbar_init(&bars[s2], 1);
+    if (warp == 0 && lane == 0) {
+        for (int s2 = 0; s2 < TMA_NS; s2++) {
+            mbar_init(&full[s2], 1);
+            mbar_init(&empty[s2], TMA_TY);
+        }
         mbar_fence_init();
     }
     __syncthreads();
-    int issued_to = min(pfirst + TMA_NS - 1, plast);
-    if (tid == 0)
-        for (int pl = pfirst; pl <= issued_to; ++pl) issue(pl);
 
+    if (warp == TMA_TY) {
+        // ---- producer ----
+        if (lane != 0) return;
+        bool ok = true;
+        unsigned r = 0; // stream index of the next plane
+        for (long long w = w_begin; ok && w < w_end;) {
+            const long long tile = w / nx;
+            const int xa = (int)(w % nx);
+            const int xb = (int)min((long long)nx, xa + (w_end - w));
+            const int k0 = (int)(tile % tiles_z) * TMA_TZ, j0 = (int)(tile / tiles_z) * TMA_TY;
+            for (int pl = xa - 2; pl <= xb + 1; ++pl, ++r) {
+                const unsigned slot = r % TMA_NS;
+                if (r >= TMA_NS && !mbar_wait_bounded(&empty[slot], ((r / TMA_NS) - 1) & 1u)) {
+                    ok = false;
+                    atomicOr(err, 1u);
+                    break;
+                }
+                unsigned char* base = smem_raw + slot * SLOT;
+                const bool own = pl >= xa && pl < xb;
+                mbar_expect_tx(&full[slot],
+                               S_BYTES + (own ? C_BYTES + U_BYTES + A_BYTES : 0u));
+                tma_load_3d(base, &tm_in, k0 - TMA_HZ, j0 - TMA_HY, pl, &full[slot]);
+                if (own) {
+                    tma_load_3d(base + S_BYTES, &tm_cls, k0, j0, pl, &full[slot]);
+                    if (STAGE > 0) {
+                        tma_load_3d(base + S_BYTES + C_BYTES, &tm_u0, k0, j0, pl, &full[slot]);
+                        tma_load_3d(base + S_BYTES + C_BYTES + U_BYTES, &tm_acc, k0, j0, pl,
+                                    &full[slot]);
+                    }
+                }
+            }
+            w += xb - xa;
+        }
+        if (!ok) {
+            // drain the copies that may still be in flight before returning
+            const unsigned lo = r >= TMA_NS ? r - TMA_NS : 0u;
+            for (unsigned q = lo; q < r; ++q) mbar_wait_bounded(&full[q % TMA_NS], (q / TMA_NS) & 1u);
+        }
+        return;
+    }
+
+    // ---- consumers: warp = tile row, lane = column ----
+    const int tz = lane, ty = warp;
+    const int s_off = (TMA_HY + ty) * TMA_BZ + (TMA_HZ + tz);
+    const int t_off = ty * TMA_TZ + tz;
+    const float* __restrict__ cval = (const float*)sa.cval;
+    float2* __restrict__ u0g = (float2*)sa.u0;
+    float* __restrict__ accg = (float*)sa.acc;
+    const TIN* __restrict__ gin = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
+    const int plane = ny * nz;
     bool ok = true;
-    auto wait_plane = [&](int plane) {
-        const int r = plane - pfirst;
-        if (ok && !mbar_wait_bounded(&bars[r % TMA_NS], (unsigned)((r / TMA_NS) & 1))) {
+    auto wait_full = [&](unsigned q) {
+        if (ok && !mbar_wait_bounded(&full[q % TMA_NS], (q / TMA_NS) & 1u)) {
             ok = false;
             atomicOr(err, 1u);
         }
     };
-    for (int pl = pfirst; pl <= min(x0 + 1, plast); ++pl) wait_plane(pl);
-
-    const float* __restrict__ cval = (const float*)sa.cval;
-    float2* __restrict__ u0g = (float2*)sa.u0;
-    float* __restrict__ accg = (float*)sa.acc;
-    const int cz = TMA_HZ + tz, cy = TMA_HY + ty;
-    const long long chunk_row = (long long)blockIdx.x; // chunk index along z within a line
-
-    for (int i = x0; i < xend; ++i) {
-        const int p = (i * ny + j) * nz + k;
-        float2 u = make_float2(0.f, 0.f);
-        float accv = 0.f;
-        if (col_valid) {
-            if (STAGE > 0) u = u0g[p];
-            if (STAGE > 0) accv = accg[p];
-        }
-        if (i + 2 <= plast) wait_plane(i + 2);
-        const unsigned c = (col_valid && ok) ? op.cls[p] : 0u;
-        const TIN* sl[5];
-#pragma unroll
-        for (int m = 0; m < 5; m++) sl[m] = ring + ((i - 2 + m - pfirst) % TMA_NS) * SLOT;
-        auto S = [&](int m, int yy, int zz) -> float {
-            if constexpr (STAGE == 0) return sl[m][yy * TMA_BZ + zz].x;
-            else return sl[m][yy * TMA_BZ + zz];
-        };
-        if constexpr (STAGE == 0) {
-            if (col_valid) u = sl[2][cy * TMA_BZ + cz];
-        }
-        float lap = 0.f;
-        float dd[3] = {0.f, 0.f, 0.f};
-        const long long chunk = ((long long)i * ny + j) * op.nzc + chunk_row;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            const DevAxis& A = op.ax[d];
-            const unsigned kind = (c >> (2 * d)) & 3u;
-            float v;
-            if (__all_sync(FULL, kind == ROW_INTERIOR)) {
-                float xm2, xm1, x0v, xp1, xp2;
-                if (d == 0) {
-                    xm2 = S(0, cy, cz); xm1 = S(1, cy, cz); x0v = S(2, cy, cz);
-                    xp1 = S(3, cy, cz); xp2 = S(4, cy, cz);
-                } else if (d == 1) {
-                    xm2 = S(2, cy - 2, cz); xm1 = S(2, cy - 1, cz); x0v = S(2, cy, cz);
-                    xp1 = S(2, cy + 1, cz); xp2 = S(2, cy + 2, cz);
-                } else {
-                    xm2 = S(2, cy, cz - 2); xm1 = S(2, cy, cz - 1); x0v = S(2, cy, cz);
-                    xp1 = S(2, cy, cz + 1); xp2 = S(2, cy, cz + 2);
-                }
-                if (A.antisym) {
-                    v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
-                } else {
-                    float r = A.icf[0] * xm2;
-                    r = fmaf(A.icf[1], xm1, r);
-                    r = fmaf(A.icf[2], x0v, r);
-                    r = fmaf(A.icf[3], xp1, r);
-                    v = fmaf(A.icf[4], xp2, r);
-                }
+    auto release = [&](unsigned q) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[q % TMA_NS]);
+    };
+    unsigned r0 = 0; // stream index of the segment's first (halo) plane
+    for (long long w = w_begin; w < w_end;) {
+        const long long tile = w / nx;
+        const int xa = (int)(w % nx);
+        const int xb = (int)min((long long)nx, xa + (w_end - w));
+        const int k = (int)(tile % tiles_z) * TMA_TZ + tz, j = (int)(tile / tiles_z) * TMA_TY + ty;
+        const bool col_valid = (j < ny) && (k < nz);
+        const long long chunk0 = (long long)j * op.nzc + (tile % tiles_z);
+        for (unsigned q = r0; q < r0 + 4; ++q) wait_full(q); // planes xa-2 .. xa+1
+        int p = (xa * ny + j) * nz + k;
+        for (int i = xa; i < xb; ++i, p += plane) {
+            const unsigned r = r0 + 2 + (unsigned)(i - xa); // stream index of plane i
+            wait_full(r + 2);
+            const unsigned char* cur = smem_raw + (r % TMA_NS) * SLOT;
+            const TIN* Sc = reinterpret_cast<const TIN*>(cur) + s_off;
+            auto Sx = [&](int m) -> float { // plane i-2+m, this column
+                const TIN* q2 =
+                    reinterpret_cast<const TIN*>(smem_raw + ((r - 2 + m) % TMA_NS) * SLOT) + s_off;
+                if constexpr (STAGE == 0) return q2->x;
+                else return *q2;
+            };
+            auto Sp = [&](int off) -> float {
+                if constexpr (STAGE == 0) return Sc[off].x;
+                else return Sc[off];
+            };
+            const unsigned c = (col_valid && ok) ? (unsigned)cur[S_BYTES + t_off] : 0u;
+            float2 u;
+            float accv = 0.f;
+            if constexpr (STAGE == 0) {
+                u = Sc[0];
             } else {
-                const int row = closure_row(A, kind == ROW_CLOSURE, chunk);
-                v = 0.f;
-                const TIN* gin = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
-                if (kind == ROW_INTERIOR) {
-                    v = interior_f<int>(A, gin, p, (int)A.stride);
-                } else if (kind == ROW_WALL) {
-                    const int coord = d == 0 ? i : (d == 1 ? j : k);
-                    v = wall32(A, (long long)p, coord, gin);
-                } else if (kind == ROW_CLOSURE) {
-                    v = cval[A.row_base + row];
-                }
+                u = reinterpret_cast<const float2*>(cur + S_BYTES + C_BYTES)[t_off];
+                accv = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + U_BYTES)[t_off];
             }
-            if (SYS == SYS_HEAT)
-                lap = lap + v;
-            else
-                dd[d] = v;
-        }
-        if (col_valid && ok) {
+            float lap = 0.f;
+            float dd[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const DevAxis& A = op.ax[d];
+                const unsigned kind = (c >> (2 * d)) & 3u;
+                float v;
+                if (__all_sync(FULL, kind == ROW_INTERIOR)) {
+                    float xm2, xm1, x0v, xp1, xp2;
+                    if (d == 0) {
+                        xm2 = Sx(0); xm1 = Sx(1); x0v = Sp(0); xp1 = Sx(3); xp2 = Sx(4);
+                    } else if (d == 1) {
+                        xm2 = Sp(-2 * TMA_BZ); xm1 = Sp(-TMA_BZ); x0v = Sp(0);
+                        xp1 = Sp(TMA_BZ); xp2 = Sp(2 * TMA_BZ);
+                    } else {
+                        xm2 = Sp(-2); xm1 = Sp(-1); x0v = Sp(0); xp1 = Sp(1); xp2 = Sp(2);
+                    }
+                    if (A.antisym) {
+                        v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
+                    } else {
+                        float t = A.icf[0] * xm2;
+                        t = fmaf(A.icf[1], xm1, t);
+                        t = fmaf(A.icf[2], x0v, t);
+                        t = fmaf(A.icf[3], xp1, t);
+                        v = fmaf(A.icf[4], xp2, t);
+                    }
+                } else {
+                    const long long chunk = (long long)i * ny * op.nzc + chunk0;
+                    const int row = closure_row(A, kind == ROW_CLOSURE, chunk);
+                    v = 0.f;
+                    if (kind == ROW_INTERIOR) {
+                        v = interior_f<int>(A, gin, p, (int)A.stride);
+                    } else if (kind == ROW_WALL) {
+                        const int coord = d == 0 ? i : (d == 1 ? j : k);
+                        v = wall32(A, (long long)p, coord, gin);
+                    } else if (kind == ROW_CLOSURE) {
+                        v = cval[A.row_base + row];
+                    }
+                }
+                if (SYS == SYS_HEAT)
+                    lap = lap + v;
+                else
+                    dd[d] = v;
+            }
+            release(r - 2); // plane i-2 is no longer read by this warp
+            if (!(col_valid && ok)) continue;
             float rhs = 0.f;
             if (c & 0x3Fu) {
                 if (SYS == SYS_HEAT) {
@@ -894,13 +1112,13 @@ __global__ void __launch_bounds__(256) k_stage_mixed_tma(const __grid_constant__
                 } else {
                     float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
                     if (sp.vel_kind != 0) {
-                        const float r0 = (float)op.xc[0][i] - sp.centerf[0];
-                        const float r1 = (float)op.xc[1][j] - sp.centerf[1];
-                        const float r2 = (float)op.xc[2][k] - sp.centerf[2];
-                        const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
-                        g0 = -r0 * il;
-                        g1 = -r1 * il;
-                        g2 = -r2 * il;
+                        const float r0f = (float)op.xc[0][i] - sp.centerf[0];
+                        const float r1f = (float)op.xc[1][j] - sp.centerf[1];
+                        const float r2f = (float)op.xc[2][k] - sp.centerf[2];
+                        const float il = rsqrtf(r0f * r0f + r1f * r1f + r2f * r2f);
+                        g0 = -r0f * il;
+                        g1 = -r1f * il;
+                        g2 = -r2f * il;
                     }
                     rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
                 }
@@ -915,22 +1133,11 @@ __global__ void __launch_bounds__(256) k_stage_mixed_tma(const __grid_constant__
                 u0g[p] = fast_two_sum(t.x, t.y + u.y);
             }
         }
-        __syncthreads(); // every thread is done with the slot of plane i-2
-        if (tid == 0 && ok) {
-            const int nxt = i - 2 + TMA_NS;
-            if (nxt <= plast) {
-                fence_proxy_async();
-                issue(nxt);
-                issued_to = nxt;
-            }
-        }
-    }
-    // drain: a block that gave up waits (bounded) for the copies it issued before returning
-    if (!ok && tid == 0) {
-        for (int pl = pfirst; pl <= issued_to; ++pl) {
-            const int r = pl - pfirst;
-            mbar_wait_bounded(&bars[r % TMA_NS], (unsigned)((r / TMA_NS) & 1));
-        }
+        // the segment's last four planes (xb-2 .. xb+1) are no longer needed
+        const unsigned rend = r0 + 4 + (unsigned)(xb - xa);
+        for (unsigned q = rend - 4; q < rend; ++q) release(q);
+        r0 = rend;
+        w += xb - xa;
     }
 }
 
@@ -1280,11 +1487,33 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
     const bool small = op.N < (1LL << 31) - 64;
     if (mixed && b.tma) {
         const CUtensorMap& tm = STAGE == 0 ? b.tm_u0 : (STAGE == 2 ? b.tm_sb : b.tm_sa);
-        const dim3 tgrid((op.it2 + TMA_TZ - 1) / TMA_TZ, (op.it1 + TMA_TY - 1) / TMA_TY,
-                         (op.it0 + b.tma_px - 1) / b.tma_px);
-        const size_t smem = TMA_NS * TMA_BY * TMA_BZ * (STAGE == 0 ? 8 : 4) + TMA_NS * 8;
-        k_stage_mixed_tma<STAGE, SYS><<<tgrid, dim3(32, TMA_TY), smem, s>>>(tm, op, sp, a,
-                                                                            b.tma_px, b.err);
+        const size_t slot = (STAGE == 0 ? TMA_BY * TMA_BZ * 8 : TMA_BY * TMA_BZ * 4 + TMA_TY * TMA_TZ * 12) +
+                            TMA_TY * TMA_TZ;
+        const size_t smem = TMA_NS * slot + 2 * TMA_NS * 8;
+        static int grid_n[4] = {0, 0, 0, 0};
+        if (!grid_n[STAGE]) {
+            cudaFuncSetAttribute(k_stage_mixed_tma<STAGE, SYS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+            int per_sm = 0, dev = 0, sms = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_mixed_tma<STAGE, SYS>,
+                                                          32 * (TMA_TY + 1), smem);
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            grid_n[STAGE] = std::max(1, per_sm) * std::max(1, sms);
+        }
+        const long long work = (long long)((op.it2 + TMA_TZ - 1) / TMA_TZ) *
+                               ((op.it1 + TMA_TY - 1) / TMA_TY) * op.it0;
+        const int grid = (int)std::min<long long>(grid_n[STAGE], work);
+        k_stage_mixed_tma<STAGE, SYS><<<grid, dim3(32, TMA_TY + 1), smem, s>>>(
+            tm, b.tm_u0t, b.tm_acct, b.tm_cls, op, sp, a, b.err);
+    } else if (mixed && b.col_nx) {
+        const dim3 cgrid(op.nzc, (op.it1 + BY - 1) / BY, (op.it0 + b.col_nx - 1) / b.col_nx);
+        if (b.col_nx == 2)
+            k_stage_mixed_col<STAGE, SYS, 2><<<cgrid, block, 0, s>>>(op, sp, a);
+        else if (b.col_nx == 4)
+            k_stage_mixed_col<STAGE, SYS, 4><<<cgrid, block, 0, s>>>(op, sp, a);
+        else
+            k_stage_mixed_col<STAGE, SYS, 1><<<cgrid, block, 0, s>>>(op, sp, a);
     } else if (mixed) {
         if (small)
             k_stage_mixed<STAGE, SYS, int><<<grid, block, 0, s>>>(op, sp, a);
