@@ -794,6 +794,13 @@ shoccs_status shoccs_system_stats(shoccs_system* S, double t, double out[11], vo
     return SHOCCS_OK;
 }
 
+shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
+{
+    if (!S || !kernel) return fail(SHOCCS_EINVAL, "null argument");
+    *kernel = S->b.tma ? 1 : (S->b.col_nx == 1 ? 2 : S->b.col_nx == 2 ? 3 : S->b.col_nx == 4 ? 4 : 0);
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_timestep(const shoccs_system* S, double cfl, double* dt)
 {
     if (!S || !dt) return fail(SHOCCS_EINVAL, "null argument");
