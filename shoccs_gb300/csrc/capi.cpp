@@ -580,6 +580,19 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.err = (unsigned*)e;
         SH_CUDA(cudaMemsetAsync(e, 0, sizeof(unsigned), s));
     }
+    SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
+    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (d->prec == PREC_FP64 ? 8 : 4), s));
+    for (int r = 0; r < 3; r++) {
+        const size_t n = p->mesh.R[r].size();
+        void *a, *h, *f;
+        SH_CUDA(S->mem.alloc(n * 8, &a));
+        SH_CUDA(S->mem.alloc(n * 8, &h));
+        SH_CUDA(S->mem.alloc(n * 8, &f));
+        S->b.R[r] = (double*)a;
+        S->b.Rhalf[r] = (double*)h;
+        S->b.Rfull[r] = (double*)f;
+        if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
+    }
     // TMA plane-marching stages for 3-D mixed solves whose planes are 16-byte aligned
     {
         const int* it = p->comp.it;
@@ -593,22 +606,11 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
                        make_plane_map(&S->b.tm_acct, S->b.acc, 4, it, false) &&
                        make_plane_map(&S->b.tm_cls, (void*)p->op.cls, 1, it, false);
         }
-        if (d->prec == PREC_MIXED && three_d) {
+        // the trial steps of the autotuner need every register allocated and zeroed; the
+        // column kernels index with 32-bit integers
+        if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
             if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;
         }
-    }
-    SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
-    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (d->prec == PREC_FP64 ? 8 : 4), s));
-    for (int r = 0; r < 3; r++) {
-        const size_t n = p->mesh.R[r].size();
-        void *a, *h, *f;
-        SH_CUDA(S->mem.alloc(n * 8, &a));
-        SH_CUDA(S->mem.alloc(n * 8, &h));
-        SH_CUDA(S->mem.alloc(n * 8, &f));
-        S->b.R[r] = (double*)a;
-        S->b.Rhalf[r] = (double*)h;
-        S->b.Rfull[r] = (double*)f;
-        if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
     }
     SH_CUDA(cudaStreamSynchronize(s));
     *out = S.release();
