@@ -178,6 +178,19 @@ shoccs_status shoccs_system_rhs(shoccs_system* s, double t, shoccs_field* rhs, v
 /* out[11] = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry,
  *            Linf_Rz, argmax_Rz} of the current state against the exact solution at t */
 shoccs_status shoccs_system_stats(shoccs_system* s, double t, double out[11], void* stream);
+/* Allocation-free variant of shoccs_system_stats; it has no counterpart in the reference.
+ * Some callers cannot allocate device memory while they call in: an application that has
+ * handed the whole device memory to its own pool allocator, or a time loop that must never
+ * block in (or fail in) the CUDA allocator between steps.  This entry point allocates
+ * nothing: its scratch is one fixed array inside the library's device image, sized for
+ * 65536 tiles of 256 grid points (16.7 M points, 2 MB), which every GPU that loads the
+ * library keeps until the process exits.  Larger grids are rejected with SHOCCS_EINVAL.
+ * The first call on a device looks up the array's device address (with that device
+ * current), so make that first call before any stream capture.  All calls share the array
+ * and it keeps the last call's contents (each call writes every slot it reads); calls that
+ * overlap on the GPU race on it.  Results equal shoccs_system_stats. */
+shoccs_status shoccs_system_stats_noalloc(shoccs_system* s, double t, double out[11],
+                                          void* stream);
 /* dt from the CFL number: heat p*h_min^2/(4k), wave c*h_min */
 shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double* dt);
 /* Stage-kernel variant of the system's RK4 path, chosen at creation by timing the

@@ -796,6 +796,35 @@ shoccs_status shoccs_system_stats(shoccs_system* S, double t, double out[11], vo
     return SHOCCS_OK;
 }
 
+shoccs_status shoccs_system_stats_noalloc(shoccs_system* S, double t, double out[11],
+                                          void* stream)
+{
+    if (!S || !out) return fail(SHOCCS_EINVAL, "null argument");
+    const DevOp& op = S->P->op;
+    const long long tiles = (long long)op.nzc * ((op.it1 + 7) / 8) * op.it0;
+    if (tiles > stats_noalloc_max_tiles())
+        return fail(SHOCCS_EINVAL,
+                    "shoccs_system_stats_noalloc: the grid has " + std::to_string(tiles) +
+                        " tiles of 256 points; its fixed scratch holds at most " +
+                        std::to_string(stats_noalloc_max_tiles()) +
+                        " (16.7 M points); use shoccs_system_stats");
+    double h[4] = {0, 0, 0, 0};
+    const cudaError_t e = launch_stats_noalloc(op, S->sp.sol, S->desc.prec, S->b.u0, t, h,
+                                               (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return fail(SHOCCS_ECUDA, std::string("stats_noalloc: ") + cudaGetErrorString(e));
+    out[0] = h[0];
+    out[1] = S->P->comp.n_fluid ? h[2] : 0.0;
+    out[2] = S->P->comp.n_fluid ? h[3] : 0.0;
+    out[3] = h[0];
+    out[4] = h[1];
+    for (int i = 5; i < 11; i++) out[i] = 0.0;
+    const double bound = S->desc.kind == SHOCCS_SYS_HEAT ? 1e6 : S->desc.max_error;
+    if (!std::isfinite(out[0]) || std::abs(out[0]) > bound)
+        return fail(SHOCCS_ENONFINITE, "solution error is non-finite or above its bound");
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
 {
     if (!S || !kernel) return fail(SHOCCS_EINVAL, "null argument");

@@ -120,6 +120,9 @@ cudaError_t launch_state_convert(long long n, int to_mixed, const double* in_d, 
 cudaError_t launch_stats(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
                          const void* u0, double* const R[3], double t, double* dev_out,
                          cudaStream_t s);
+cudaError_t launch_stats_noalloc(const DevOp& op, const DevSol& sol, int prec, const void* u0,
+                                 double t, double host_out[4], cudaStream_t s);
+long long stats_noalloc_max_tiles();
 long long kernel_launch_count();
 
 } // namespace sgb

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <type_traits>
 #include <cmath>
 #include <cstdio>
@@ -1682,6 +1683,67 @@ cudaError_t launch_stats(const DevOp& op, const DevR&, const DevSol& sol, int pr
     g_launches += 2;
     cudaFreeAsync(parts, s);
     return cudaGetLastError();
+}
+
+// ---- allocation-free statistics ------------------------------------------------------------
+// Some callers cannot allocate device memory while they call in: an application that has
+// handed the whole device memory to its own pool allocator, or a time loop that must never
+// block in (or fail in) the CUDA allocator between its steps.  For them the statistics
+// reduction can run out of one fixed scratch array that lives in the library's own device
+// image: the per-tile partial results (one per 256-point tile, 4 doubles each) followed by
+// the four results.  Every GPU that loads the library holds the array until the process
+// exits.  All calls share it and it keeps the last call's contents; every slot a call
+// reads is written earlier in the same call, so nothing has to be cleared first, but two
+// calls that overlap on the GPU (different streams, or different host threads on one
+// device) race on it.
+namespace
+{
+constexpr long long STATS_NOALLOC_MAX_TILES = 65536; // 16.7 M points (256^3), 2 MB
+static_assert(sizeof(StatPart) == 4 * sizeof(double), "StatPart is four 8-byte words");
+static __device__ __align__(256) double g_stats_scratch[4 * STATS_NOALLOC_MAX_TILES + 4];
+
+// device address of g_stats_scratch on each device, looked up once per device with that
+// device current (in host code the array's name is a host-side stand-in, not a device
+// address)
+constexpr int MAX_DEVICES = 64;
+double* g_scratch_addr[MAX_DEVICES] = {};
+std::mutex g_scratch_mutex;
+} // namespace
+
+long long stats_noalloc_max_tiles() { return STATS_NOALLOC_MAX_TILES; }
+
+cudaError_t launch_stats_noalloc(const DevOp& op, const DevSol& sol, int prec, const void* u0,
+                                 double t, double host_out[4], cudaStream_t s)
+{
+    const dim3 grid = point_grid(op), block(32, BY);
+    const long long nparts = (long long)grid.x * grid.y * grid.z;
+    if (nparts > STATS_NOALLOC_MAX_TILES) return cudaErrorInvalidValue;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    double* scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_addr[dev]) {
+            void* ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_stats_scratch);
+            if (e != cudaSuccess) return e;
+            g_scratch_addr[dev] = static_cast<double*>(ptr);
+        }
+        scratch = g_scratch_addr[dev];
+    }
+    StatPart* parts = reinterpret_cast<StatPart*>(scratch);
+    double* out = scratch + 4 * STATS_NOALLOC_MAX_TILES;
+    const double et = sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    k_stats<<<grid, block, 0, s>>>(op, sol, t, et, prec == PREC_MIXED, u0, parts);
+    k_stats_final<<<1, 256, 0, s>>>(nparts, parts, out);
+    g_launches += 2;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(host_out, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
 }
 
 } // namespace sgb
