@@ -434,19 +434,40 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
 {
     struct Cand {
         const char* name;
-        int tma, col;
+        int tma, col, vec;
     };
     std::vector<Cand> cands;
-    if (S->b.tma) cands.push_back({"tma", 1, 0});
-    cands.push_back({"col1", 0, 1});
-    cands.push_back({"col2", 0, 2});
-    cands.push_back({"col4", 0, 4});
-    cands.push_back({"point", 0, 0});
+    if (S->b.tma) cands.push_back({"tma", 1, 0, 0});
+    // the vectorised kernel is compiled for the stencil of each system: 5-point
+    // antisymmetric rows for the wave, 5- or 3-point symmetric rows for the heat equation
+    int form = FORM_ANY;
+    {
+        const DevOp& op = S->P->op;
+        auto f = [](const DevAxis& A) {
+            return A.width == 5 ? (A.antisym ? FORM_ANTI5 : FORM_SYM5)
+                                : (A.width == 3 && !A.antisym ? FORM_W3 : FORM_ANY);
+        };
+        form = f(op.ax[0]);
+        for (int d = 1; d < 3; d++)
+            if (f(op.ax[d]) != form) form = FORM_ANY;
+        const bool wave = S->desc.kind == SHOCCS_SYS_WAVE;
+        if (wave ? form != FORM_ANTI5 : (form != FORM_SYM5 && form != FORM_W3)) form = FORM_ANY;
+    }
+    if (S->P->comp.it[2] % 4 == 0 && S->b.zwall && form != FORM_ANY)
+        cands.push_back({"vec", 0, 0, form});
+    cands.push_back({"col1", 0, 1, 0});
+    cands.push_back({"col2", 0, 2, 0});
+    cands.push_back({"col4", 0, 4, 0});
+    cands.push_back({"point", 0, 0, 0});
+    auto use = [&](const Cand& c) {
+        S->b.tma = c.tma;
+        S->b.col_nx = c.col;
+        S->b.vec = c.vec;
+    };
     if (const char* force = std::getenv("SHOCCS_STAGE_KERNEL")) {
         for (const auto& c : cands)
             if (std::string(force) == c.name) {
-                S->b.tma = c.tma;
-                S->b.col_nx = c.col;
+                use(c);
                 return SHOCCS_OK;
             }
         return fail(SHOCCS_EINVAL, std::string("SHOCCS_STAGE_KERNEL: unknown or unavailable ") +
@@ -462,8 +483,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
     Cand pick = cands.back();
     const int reps = N > (1 << 22) ? 3 : 2;
     for (const auto& c : cands) {
-        S->b.tma = c.tma;
-        S->b.col_nx = c.col;
+        use(c);
         SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, 0.0, dt, s));
         SH_CUDA(cudaEventRecord(e0, s));
         for (int r = 0; r < reps; r++)
@@ -479,8 +499,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    S->b.tma = pick.tma;
-    S->b.col_nx = pick.col;
+    use(pick);
     // reset the registers the trial steps touched
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * 8, s));
     SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * 4, s));
@@ -599,16 +618,26 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         const bool three_d = it[0] > 1 && it[1] > 1 && it[2] > 1;
         if (d->prec == PREC_MIXED && three_d && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
             !std::getenv("SHOCCS_DISABLE_TMA")) {
-            S->b.tma = make_plane_map(&S->b.tm_u0, S->b.u0, 8, it) &&
+            float* hi = (float*)S->b.u0;
+            S->b.tma = make_plane_map(&S->b.tm_u0, hi, 4, it) &&
                        make_plane_map(&S->b.tm_sa, S->b.sa, 4, it) &&
                        make_plane_map(&S->b.tm_sb, S->b.sb, 4, it) &&
-                       make_plane_map(&S->b.tm_u0t, S->b.u0, 8, it, false) &&
+                       make_plane_map(&S->b.tm_u0t, hi, 4, it, false) &&
+                       make_plane_map(&S->b.tm_u0l, hi + N, 4, it, false) &&
                        make_plane_map(&S->b.tm_acct, S->b.acc, 4, it, false) &&
                        make_plane_map(&S->b.tm_cls, (void*)p->op.cls, 1, it, false);
         }
         // the trial steps of the autotuner need every register allocated and zeroed; the
-        // column kernels index with 32-bit integers
+        // column and vectorised kernels index with 32-bit integers
         if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
+            const WallBlock* W = p->op.ax[2].wall;
+            const long long nzw = (long long)it[0] * it[1] * (W[0].rows + W[1].rows);
+            if (it[2] % 4 == 0 && nzw + p->op.n_cut_rows < (1LL << 31) - 256) {
+                const size_t n = (size_t)nzw;
+                void* z = nullptr;
+                SH_CUDA(S->mem.alloc(std::max<size_t>(n, 1) * sizeof(float), &z));
+                S->b.zwall = (float*)z;
+            }
             if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;
         }
     }
@@ -828,7 +857,13 @@ shoccs_status shoccs_system_stats_noalloc(shoccs_system* S, double t, double out
 shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
 {
     if (!S || !kernel) return fail(SHOCCS_EINVAL, "null argument");
-    *kernel = S->b.tma ? 1 : (S->b.col_nx == 1 ? 2 : S->b.col_nx == 2 ? 3 : S->b.col_nx == 4 ? 4 : 0);
+    const StepBuffers& b = S->b;
+    *kernel = b.tma                ? 1
+              : b.col_nx == 1      ? 2
+              : b.col_nx == 2      ? 3
+              : b.col_nx == 4      ? 4
+              : b.vec              ? 5
+                                   : 0;
     return SHOCCS_OK;
 }
 

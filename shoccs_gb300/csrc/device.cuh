@@ -67,6 +67,9 @@ struct DevR {
 
 // launch helpers implemented in kernels.cu -----------------------------------------------
 enum { PREC_FP64 = 0, PREC_MIXED = 1 };
+// interior stencil shared by every active axis: 5-point antisymmetric (first derivative),
+// 5-point symmetric, 3-point; FORM_ANY when the axes differ
+enum { FORM_ANY = 0, FORM_ANTI5 = 1, FORM_SYM5 = 2, FORM_W3 = 3 };
 
 cudaError_t launch_derivative(const DevOp& op, int dir, int prec, const void* uD,
                               const void* uR, const double* nuD, void* duD, void* const duR[3],
@@ -89,7 +92,7 @@ struct SysParams {
 };
 
 struct StepBuffers {
-    void* u0;      // double (FP64) or float2 (MIXED)
+    void* u0;      // double (FP64), or the hi plane then the lo plane of FP32 pairs (MIXED)
     void* acc;     // double (FP64) or float (MIXED)
     void* sa;      // stage fields: double or float
     void* sb;
@@ -102,9 +105,13 @@ struct StepBuffers {
     int tma = 0;
     // column-blocked mixed stages (3-D grids): planes per thread, 0 = per-point kernel
     int col_nx = 0;
+    // vectorised mixed stages (3-D grids, nz a multiple of 4) and their table of z-wall row
+    // values (wall[0].rows + wall[1].rows per z line)
+    int vec = 0; // stencil form (FORM_*) of the vectorised kernel, 0 = not used
+    float* zwall = nullptr;
     unsigned* err = nullptr;
-    CUtensorMap tm_u0, tm_sa, tm_sb; // stage inputs: one plane tile plus halo
-    CUtensorMap tm_u0t, tm_acct;     // u0 and accumulator: one plane tile, no halo
+    CUtensorMap tm_u0, tm_sa, tm_sb;     // stage inputs (u0: hi plane): one plane tile plus halo
+    CUtensorMap tm_u0t, tm_u0l, tm_acct; // hi and lo planes of u0, accumulator: one tile, no halo
     CUtensorMap tm_cls;              // class bytes: one plane tile
 };
 

@@ -47,13 +47,31 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // ---- loads -----------------------------------------------------------------------------
 __device__ __forceinline__ double ldd(const double* p, long long i) { return __ldg(p + i); }
 __device__ __forceinline__ double ldd(const float* p, long long i) { return (double)__ldg(p + i); }
-__device__ __forceinline__ double ldd(const float2* p, long long i)
-{
-    const float2 v = __ldg(p + i);
-    return (double)v.x + (double)v.y;
-}
 __device__ __forceinline__ float ldf(const float* p, long long i) { return __ldg(p + i); }
-__device__ __forceinline__ float ldf(const float2* p, long long i) { return __ldg(p + i).x; }
+
+// The solution of the mixed path is a compensated FP32 pair held as two planes: the hi
+// words at [0, n) and the lo words at [n, 2n), so the hi plane doubles as the FP32 input
+// field of the first RK4 stage.  As a row input it reads as hi + lo (ldd) or hi (ldf).
+struct PairU {
+    const float* hi;
+    long long n;
+};
+__device__ __forceinline__ double ldd(const PairU& u, long long i)
+{
+    return (double)__ldg(u.hi + i) + (double)__ldg(u.hi + u.n + i);
+}
+__device__ __forceinline__ float ldf(const PairU& u, long long i) { return __ldg(u.hi + i); }
+__device__ __forceinline__ float2 ld_pair(const void* u0, long long n, long long i)
+{
+    const float* h = (const float*)u0;
+    return make_float2(h[i], h[n + i]);
+}
+__device__ __forceinline__ void st_pair(void* u0, long long n, long long i, float2 v)
+{
+    float* h = (float*)u0;
+    h[i] = v.x;
+    h[n + i] = v.y;
+}
 
 // ---- point indexing ----------------------------------------------------------------------
 struct Pt {
@@ -98,7 +116,7 @@ __device__ __forceinline__ int closure_row(const DevAxis& A, bool is_closure, lo
 
 // ---- interior stencils -------------------------------------------------------------------
 template <class TIN>
-__device__ __forceinline__ double interior64(const DevAxis& A, const TIN* u, long long p)
+__device__ __forceinline__ double interior64(const DevAxis& A, TIN u, long long p)
 {
     const long long s = A.stride;
     if (A.width == 5) {
@@ -119,7 +137,7 @@ __device__ __forceinline__ double interior64(const DevAxis& A, const TIN* u, lon
 }
 
 template <class TIN>
-__device__ __forceinline__ float interior32(const DevAxis& A, const TIN* u, long long p)
+__device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p)
 {
     const long long s = A.stride;
     if (A.width == 5) {
@@ -144,7 +162,7 @@ __device__ __forceinline__ float interior32(const DevAxis& A, const TIN* u, long
 // in the order of derivative::apply_kernels (O, then B, then N).
 template <class TIN, class TR>
 __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long p,
-                                            const TIN* u, const TR* Rd, const double* nu,
+                                            TIN u, const TR* Rd, const double* nu,
                                             double acc, bool first)
 {
     const ClosureRow cr = A.rows[row];
@@ -170,7 +188,7 @@ __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long
 __device__ __forceinline__ int wall_side(const DevAxis& A, int coord) { return coord * 2 < A.n ? 0 : 1; }
 
 template <class TIN>
-__device__ __forceinline__ double wall64(const DevAxis& A, long long p, int coord, const TIN* u,
+__device__ __forceinline__ double wall64(const DevAxis& A, long long p, int coord, TIN u,
                                          const double* nu, double acc, bool first)
 {
     const WallBlock& W = A.wall[wall_side(A, coord)];
@@ -187,7 +205,7 @@ __device__ __forceinline__ double wall64(const DevAxis& A, long long p, int coor
 }
 
 template <class TIN>
-__device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord, const TIN* u)
+__device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord, TIN u)
 {
     const WallBlock& W = A.wall[wall_side(A, coord)];
     const int r = coord - W.first_row;
@@ -415,6 +433,7 @@ struct StageArgs {
     void* acc;
     void* s_out;
     const void* cval;
+    float* zw;              // z-wall row values of the stage (vectorised mixed stages), or null
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
     float2 cf_ff, ci_ff;    // same as compensated FP32 pairs
@@ -425,13 +444,40 @@ struct StageArgs {
 
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 
-// cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b]  (FP64)
+// z-wall rows: slot of the table row of z coordinate k (the left block's rows, then the
+// right block's) and the number of slots per z line
+__device__ __forceinline__ int zwall_slots(const DevAxis& A) { return A.wall[0].rows + A.wall[1].rows; }
+__device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
+{
+    return k * 2 < A.n ? k - A.wall[0].first_row : A.wall[0].rows + (k - A.wall[1].first_row);
+}
+
+// cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b]  (FP64); with zw, threads past
+// the cut-cell rows also evaluate the domain-wall rows of the z axis (FP32, wall32) into a
+// table of zwall_slots() values per z line, which the vectorised mixed stage reads: those
+// rows sit at both ends of every z line, so every warp of that kernel holds some.
 template <class TIN, class TOUT>
-__global__ void k_cut_rows(DevOp op, const TIN* __restrict__ u, const double* R0,
-                           const double* R1, const double* R2, TOUT* __restrict__ cval)
+__global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
+                           const double* R1, const double* R2, TOUT* __restrict__ cval,
+                           float* __restrict__ zw)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= op.n_cut_rows) return;
+    if (i >= op.n_cut_rows) {
+        if (!zw) return;
+        const DevAxis& A = op.ax[2];
+        // 32-bit: the table and the cut-cell rows together stay below 2^31 entries
+        const int ns = zwall_slots(A);
+        const int e = i - op.n_cut_rows;
+        if (ns == 0 || e >= op.it0 * op.it1 * ns) return;
+        const int line = e / ns;
+        const int slot = e - line * ns;
+        const int k = slot < A.wall[0].rows ? A.wall[0].first_row + slot
+                                            : A.wall[1].first_row + (slot - A.wall[0].rows);
+        const long long p = (long long)line * op.it2 + k;
+        if constexpr (!std::is_same<TIN, const double*>::value)
+            if (((op.cls[p] >> 4) & 3u) == ROW_WALL) zw[e] = wall32(A, p, k, u);
+        return;
+    }
     const double* R[3] = {R0, R1, R2};
     const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
     const DevAxis& A = op.ax[d];
@@ -477,14 +523,11 @@ __device__ __forceinline__ void stage_ijk(const DevOp& op, const StagePt<IDX>& q
 template <class T, class IDX>
 __device__ __forceinline__ T ld_in(const T* u, IDX i) { return __ldg(u + i); }
 
-// interior row with IDX addressing; FP32 (mixed) from a float or float2 (hi word) field
-template <class IDX, class TIN>
-__device__ __forceinline__ float interior_f(const DevAxis& A, const TIN* u, IDX p, IDX s)
+// interior row with IDX addressing, FP32 (mixed) field
+template <class IDX>
+__device__ __forceinline__ float interior_f(const DevAxis& A, const float* u, IDX p, IDX s)
 {
-    auto L = [&](IDX i) -> float {
-        if constexpr (sizeof(TIN) == 8) return __ldg(u + i).x;
-        else return __ldg(u + i);
-    };
+    auto L = [&](IDX i) -> float { return __ldg(u + i); };
     if (A.width == 5) {
         if (A.antisym) {
             const float d1 = L(p + s) - L(p - s);
@@ -606,16 +649,68 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
     }
 }
 
+// Right-hand side of one point of the mixed path from its axis values (heat: lap, the sum
+// of the second-derivative rows; wave: d0..d2, the first-derivative rows).  Products are
+// written with explicit rounding (__fmul_rn never fuses into an FMA), so every stage-kernel
+// variant yields the same bits from the same inputs.
+template <int SYS, int VK = -1> // VK: velocity field of the wave, -1 from sp, 0 constant, 1 radial
+__device__ __forceinline__ float rhs_mixed(const DevOp& op, const SysParams& sp, float etf, int i,
+                                           int j, int k, float lap, float d0, float d1, float d2)
+{
+    if constexpr (SYS == SYS_HEAT) {
+        float src = 0.f;
+        if (sp.sol.kind == SOL_SINSIN) {
+            float u = __fmul_rn(sp.sol.Sf[0][i], sp.sol.Sf[1][j]);
+            if (sp.sol.dims == 3) u = __fmul_rn(u, sp.sol.Sf[2][k]);
+            u = __fmul_rn(u, etf);
+            src = __fsub_rn(-u, __fmul_rn(sp.kf, __fmul_rn((float)sp.sol.lapfac, u)));
+        }
+        return fmaf(lap, sp.kf, src);
+    } else {
+        float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
+        if (VK == 1 || (VK < 0 && sp.vel_kind != 0)) {
+            const float r0 = __fsub_rn((float)op.xc[0][i], sp.centerf[0]);
+            const float r1 = __fsub_rn((float)op.xc[1][j], sp.centerf[1]);
+            const float r2 = __fsub_rn((float)op.xc[2][k], sp.centerf[2]);
+            const float il = rsqrtf(fmaf(r2, r2, fmaf(r1, r1, __fmul_rn(r0, r0))));
+            g0 = __fmul_rn(-r0, il);
+            g1 = __fmul_rn(-r1, il);
+            g2 = __fmul_rn(-r2, il);
+        }
+        return fmaf(g2, d2, fmaf(g1, d1, __fmul_rn(g0, d0)));
+    }
+}
+
+// RK4 register update of one point of the mixed path: the increment dt*b_s*rhs with the
+// weight held as an FP32 pair; stages 0-2 write the accumulator and the next stage field,
+// stage 3 adds the accumulated increment to the (hi, lo) solution by an error-free two-sum.
+template <int STAGE>
+__device__ __forceinline__ void rk_mixed(const StageArgs& sa, float rhs, float2 u, float accv,
+                                         float& acc_out, float& s_out, float2& u_out)
+{
+    const float inc = fmaf(sa.cf_ff.x, rhs, __fmul_rn(sa.cf_ff.y, rhs));
+    if constexpr (STAGE < 3) {
+        acc_out = STAGE == 0 ? inc : __fadd_rn(accv, inc);
+        s_out = __fadd_rn(u.x, fmaf(sa.ci_ff.x, rhs, u.y));
+    } else {
+        const float a = __fadd_rn(accv, inc);
+        const float2 t = two_sum(u.x, a);
+        u_out = fast_two_sum(t.x, __fadd_rn(t.y, u.y));
+    }
+}
+
 // Mixed stage: FP32 stage field, interior and wall rows, FP32 stage accumulator; FP64
 // cut-cell rows (k_cut_rows); the solution u0 is a compensated FP32 pair (hi, lo) and
 // receives the step's accumulated increment through an error-free two-sum.  Stage 0 reads
-// u0 (hi word) as its input field.
+// u0 (hi word) as its input field.  The 32 lanes of a warp hold 32 consecutive points of
+// one 32-point chunk (q.chunk), which the cut-cell row lookup relies on.
 template <int STAGE, int SYS, class IDX>
-__global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, StageArgs sa)
+__device__ __forceinline__ void stage_mixed_at(const DevOp& op, const SysParams& sp,
+                                               const StageArgs& sa, const StagePt<IDX>& q)
 {
-    const StagePt<IDX> q = stage_point<IDX>(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const float* __restrict__ cval = (const float*)sa.cval;
+    const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     float lap = 0.f;
     float dd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -626,78 +721,68 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
         const IDX s = (IDX)A.stride;
         float v;
         if (__all_sync(FULL, kind == ROW_INTERIOR)) {
-            if (STAGE == 0)
-                v = interior_f<IDX>(A, (const float2*)sa.u0, q.p, s);
-            else
-                v = interior_f<IDX>(A, (const float*)sa.s_in, q.p, s);
+            v = interior_f<IDX>(A, in, q.p, s);
         } else {
             const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
             v = 0.f;
             if (kind == ROW_INTERIOR) {
-                if (STAGE == 0)
-                    v = interior_f<IDX>(A, (const float2*)sa.u0, q.p, s);
-                else
-                    v = interior_f<IDX>(A, (const float*)sa.s_in, q.p, s);
+                v = interior_f<IDX>(A, in, q.p, s);
             } else if (kind == ROW_WALL) {
                 int ijk[3];
                 stage_ijk(op, q, ijk);
-                if (STAGE == 0)
-                    v = wall32(A, (long long)q.p, ijk[d], (const float2*)sa.u0);
-                else
-                    v = wall32(A, (long long)q.p, ijk[d], (const float*)sa.s_in);
+                v = wall32(A, (long long)q.p, ijk[d], in);
             } else if (kind == ROW_CLOSURE) {
                 v = cval[A.row_base + row];
             }
         }
         if (SYS == SYS_HEAT)
-            lap = lap + v;
+            lap = __fadd_rn(lap, v);
         else
             dd[d] = v;
     }
     if (!q.valid) return;
     float rhs = 0.f;
     if (c & 0x3Fu) {
-        if (SYS == SYS_HEAT) {
-            float src = 0.f;
-            if (sp.sol.kind == SOL_SINSIN) {
-                int ijk[3];
-                stage_ijk(op, q, ijk);
-                float u = sp.sol.Sf[0][ijk[0]] * sp.sol.Sf[1][ijk[1]];
-                if (sp.sol.dims == 3) u = u * sp.sol.Sf[2][ijk[2]];
-                u = u * sa.etf_stage;
-                src = (-u) - sp.kf * ((float)sp.sol.lapfac * u);
-            }
-            rhs = fmaf(lap, sp.kf, src);
-        } else {
-            float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
-            if (sp.vel_kind != 0) {
-                int ijk[3];
-                stage_ijk(op, q, ijk);
-                const float r0 = (float)op.xc[0][ijk[0]] - sp.centerf[0];
-                const float r1 = (float)op.xc[1][ijk[1]] - sp.centerf[1];
-                const float r2 = (float)op.xc[2][ijk[2]] - sp.centerf[2];
-                const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
-                g0 = -r0 * il;
-                g1 = -r1 * il;
-                g2 = -r2 * il;
-            }
-            rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
-        }
+        int ijk[3];
+        stage_ijk(op, q, ijk);
+        rhs = rhs_mixed<SYS>(op, sp, sa.etf_stage, ijk[0], ijk[1], ijk[2], lap, dd[0], dd[1],
+                             dd[2]);
     }
-    float2* __restrict__ u0 = (float2*)sa.u0;
     float* __restrict__ acc = (float*)sa.acc;
-    // increment dt*b_s*rhs with the weight held as an FP32 pair
-    const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
-    if (STAGE < 3) {
-        const float2 u = u0[q.p];
-        acc[q.p] = STAGE == 0 ? inc : acc[q.p] + inc;
-        ((float*)sa.s_out)[q.p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
+    float a_out = 0.f, s_out = 0.f;
+    float2 u_out;
+    rk_mixed<STAGE>(sa, rhs, ld_pair(sa.u0, op.N, q.p), STAGE == 0 ? 0.f : acc[q.p], a_out,
+                    s_out, u_out);
+    if constexpr (STAGE < 3) {
+        acc[q.p] = a_out;
+        ((float*)sa.s_out)[q.p] = s_out;
     } else {
-        const float a = acc[q.p] + inc;
-        const float2 u = u0[q.p];
-        const float2 t = two_sum(u.x, a);
-        u0[q.p] = fast_two_sum(t.x, t.y + u.y);
+        st_pair(sa.u0, op.N, q.p, u_out);
     }
+}
+
+template <int STAGE, int SYS, class IDX>
+__global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, StageArgs sa)
+{
+    stage_mixed_at<STAGE, SYS, IDX>(op, sp, sa, stage_point<IDX>(op));
+}
+
+// interior row from five register values (m2 .. p2 along the axis); the operation order is
+// interior_f's
+__device__ __forceinline__ float interior_row(const DevAxis& A, float m2, float m1, float c0,
+                                              float p1, float p2)
+{
+    if (A.width == 5) {
+        if (A.antisym) return fmaf(A.icf[3], p1 - m1, A.icf[4] * (p2 - m2));
+        float r = A.icf[0] * m2;
+        r = fmaf(A.icf[1], m1, r);
+        r = fmaf(A.icf[2], c0, r);
+        r = fmaf(A.icf[3], p1, r);
+        return fmaf(A.icf[4], p2, r);
+    }
+    float r = A.icf[0] * m1;
+    r = fmaf(A.icf[1], c0, r);
+    return fmaf(A.icf[2], p1, r);
 }
 
 // ---- column-blocked mixed stage (3-D grids) ------------------------------------------------
@@ -706,17 +791,15 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
 // class bytes, u0 and the accumulator of all NX points are issued together, before any
 // class byte is decoded, with neighbour coordinates clamped into the grid so every
 // speculative load stays in bounds (values of rows that turn out not to be interior are
-// simply not used).  Warps whose 32 lanes all have interior rows along an axis take the
-// fast path; the others fall back to the per-lane wall / cut-cell path.
+// simply not used).  Per axis every lane evaluates the interior row from these registers
+// and keeps it where its row is interior (points without a row contribute 0); only warps
+// that hold a cut-cell or wall row along that axis branch to read the cut-row values and
+// evaluate the wall rows.
 template <int STAGE, int SYS, int NX>
 __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp, StageArgs sa)
 {
-    using TIN = typename std::conditional<STAGE == 0, float2, float>::type;
-    const TIN* __restrict__ in = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
-    auto L = [&](int idx) -> float {
-        if constexpr (STAGE == 0) return __ldg(in + idx).x;
-        else return __ldg(in + idx);
-    };
+    const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
+    auto L = [&](int idx) -> float { return __ldg(in + idx); };
     const int nx = op.it0, ny = op.it1, nz = op.it2;
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
@@ -747,7 +830,7 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
         yv[t][0] = L(p + ym2); yv[t][1] = L(p + ym1); yv[t][2] = L(p + yp1); yv[t][3] = L(p + yp2);
         zv[t][0] = L(p + zm2); zv[t][1] = L(p + zm1); zv[t][2] = L(p + zp1); zv[t][3] = L(p + zp2);
         if constexpr (STAGE > 0) {
-            uu[t] = ((const float2*)sa.u0)[p];
+            uu[t] = ld_pair(sa.u0, op.N, p);
             av[t] = ((const float*)sa.acc)[p];
         }
     }
@@ -762,32 +845,23 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
         for (int d = 0; d < 3; d++) {
             const DevAxis& A = op.ax[d];
             const unsigned kind = (c[t] >> (2 * d)) & 3u;
-            float v;
-            if (__all_sync(FULL, kind == ROW_INTERIOR)) {
-                float xm2, xm1, x0v, xp1, xp2;
-                if (d == 0) {
-                    xm2 = w[t]; xm1 = w[t + 1]; x0v = w[t + 2]; xp1 = w[t + 3]; xp2 = w[t + 4];
-                } else if (d == 1) {
-                    xm2 = yv[t][0]; xm1 = yv[t][1]; x0v = w[t + 2]; xp1 = yv[t][2]; xp2 = yv[t][3];
-                } else {
-                    xm2 = zv[t][0]; xm1 = zv[t][1]; x0v = w[t + 2]; xp1 = zv[t][2]; xp2 = zv[t][3];
-                }
-                if (A.antisym) {
-                    v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
-                } else {
-                    float r = A.icf[0] * xm2;
-                    r = fmaf(A.icf[1], xm1, r);
-                    r = fmaf(A.icf[2], x0v, r);
-                    r = fmaf(A.icf[3], xp1, r);
-                    v = fmaf(A.icf[4], xp2, r);
-                }
+            // the interior row from the registers, kept where the point has one (the
+            // speculative loads are exact for such points); no-row points contribute 0
+            float xm2, xm1, x0v, xp1, xp2;
+            if (d == 0) {
+                xm2 = w[t]; xm1 = w[t + 1]; x0v = w[t + 2]; xp1 = w[t + 3]; xp2 = w[t + 4];
+            } else if (d == 1) {
+                xm2 = yv[t][0]; xm1 = yv[t][1]; x0v = w[t + 2]; xp1 = yv[t][2]; xp2 = yv[t][3];
             } else {
+                xm2 = zv[t][0]; xm1 = zv[t][1]; x0v = w[t + 2]; xp1 = zv[t][2]; xp2 = zv[t][3];
+            }
+            const float s_int = interior_row(A, xm2, xm1, x0v, xp1, xp2);
+            float v = kind == ROW_INTERIOR ? s_int : 0.f;
+            // cut-cell and wall rows: only warps that hold one take this branch
+            if (__any_sync(FULL, kind >= ROW_CLOSURE)) {
                 const long long chunk = ((long long)min(i, nx - 1) * ny + j) * op.nzc + blockIdx.x;
                 const int row = closure_row(A, kind == ROW_CLOSURE, chunk);
-                v = 0.f;
-                if (kind == ROW_INTERIOR) {
-                    v = interior_f<int>(A, in, p, (int)A.stride);
-                } else if (kind == ROW_WALL) {
+                if (kind == ROW_WALL) {
                     const int coord = d == 0 ? i : (d == 1 ? j : k);
                     v = wall32(A, (long long)p, coord, in);
                 } else if (kind == ROW_CLOSURE) {
@@ -795,51 +869,195 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
                 }
             }
             if (SYS == SYS_HEAT)
-                lap = lap + v;
+                lap = __fadd_rn(lap, v);
             else
                 dd[d] = v;
         }
         if (!(col_valid && i < nx)) continue;
-        float rhs = 0.f;
-        if (c[t] & 0x3Fu) {
-            if (SYS == SYS_HEAT) {
-                float src = 0.f;
-                if (sp.sol.kind == SOL_SINSIN) {
-                    float q = sp.sol.Sf[0][i] * sp.sol.Sf[1][j];
-                    if (sp.sol.dims == 3) q = q * sp.sol.Sf[2][k];
-                    q = q * sa.etf_stage;
-                    src = (-q) - sp.kf * ((float)sp.sol.lapfac * q);
+        const float rhs = (c[t] & 0x3Fu) ? rhs_mixed<SYS>(op, sp, sa.etf_stage, i, j, k, lap,
+                                                          dd[0], dd[1], dd[2])
+                                         : 0.f;
+        float a_out = 0.f, s_out = 0.f;
+        float2 u_out;
+        if constexpr (STAGE == 0)
+            rk_mixed<STAGE>(sa, rhs, ld_pair(sa.u0, op.N, p), 0.f, a_out, s_out, u_out);
+        else
+            rk_mixed<STAGE>(sa, rhs, uu[t], av[t], a_out, s_out, u_out);
+        if constexpr (STAGE < 3) {
+            ((float*)sa.acc)[p] = a_out;
+            ((float*)sa.s_out)[p] = s_out;
+        } else {
+            st_pair(sa.u0, op.N, p, u_out);
+        }
+    }
+}
+
+// ---- vectorised mixed stage (3-D grids, nz a multiple of 4) --------------------------------
+// A thread owns four consecutive z points of one x plane, so a warp covers 128 points of one
+// z line and every field moves as float4 (stage input, class bytes as one 32-bit word, the
+// hi and lo planes of u0, accumulator).  The z neighbours come from the float4s on either
+// side, the y neighbours from the float4s of rows j-2..j+2, the x neighbours from those of
+// planes i-2..i+2; all loads are issued before any class byte is decoded, with coordinates
+// clamped into the grid so they stay in bounds.  Per axis every point evaluates its interior
+// row from these registers and keeps it where the row is interior (points without a row
+// contribute 0); only warps that hold a cut-cell or wall row along that axis branch.  There,
+// cut-cell rows are found from the chunk's prefix count plus the rank among the chunk's
+// cut-cell points (lanes 8s..8s+7 hold the 32-point chunk s of the warp, four ballots give
+// the rank); z-wall rows, which sit at both ends of every z line, come from the table that
+// k_cut_rows fills; x- and y-wall rows (whole planes / rows, uniform across a warp) are
+// evaluated from global memory.  FORM fixes the interior stencil (5-point antisymmetric,
+// 5-point symmetric, 3-point) and VK the velocity field of the wave system (constant or
+// radial), so the per-point code has no run-time branch on either.  The arithmetic of each
+// point is the per-point kernel's, operation for operation.
+template <int FORM>
+__device__ __forceinline__ float interior_row_t(const DevAxis& A, float m2, float m1, float c0,
+                                                float p1, float p2)
+{
+    if constexpr (FORM == FORM_ANTI5) {
+        return fmaf(A.icf[3], p1 - m1, A.icf[4] * (p2 - m2));
+    } else if constexpr (FORM == FORM_SYM5) {
+        float r = A.icf[0] * m2;
+        r = fmaf(A.icf[1], m1, r);
+        r = fmaf(A.icf[2], c0, r);
+        r = fmaf(A.icf[3], p1, r);
+        return fmaf(A.icf[4], p2, r);
+    } else if constexpr (FORM == FORM_W3) {
+        float r = A.icf[0] * m1;
+        r = fmaf(A.icf[1], c0, r);
+        return fmaf(A.icf[2], p1, r);
+    } else {
+        return interior_row(A, m2, m1, c0, p1, p2);
+    }
+}
+
+__device__ __forceinline__ float4 ld4(const float* base, int idx)
+{
+    return __ldg((const float4*)(base + idx));
+}
+
+__device__ __forceinline__ float f4(const float4& v, int q)
+{
+    return q == 0 ? v.x : (q == 1 ? v.y : (q == 2 ? v.z : v.w));
+}
+
+template <int STAGE, int SYS, int FORM, int VK>
+__global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
+{
+    const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int lane = threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (j >= ny) return; // whole warp
+    const int i = blockIdx.z;
+    const int k = blockIdx.x * 128 + 4 * lane;
+    const bool kvalid = k < nz;
+    const int plane = ny * nz;
+    const int kc = min(k, nz - 4);
+    const int p = i * plane + j * nz + kc;
+    const int xm2 = (max(i - 2, 0) - i) * plane, xm1 = (max(i - 1, 0) - i) * plane;
+    const int xp1 = (min(i + 1, nx - 1) - i) * plane, xp2 = (min(i + 2, nx - 1) - i) * plane;
+    const int ym2 = (max(j - 2, 0) - j) * nz, ym1 = (max(j - 1, 0) - j) * nz;
+    const int yp1 = (min(j + 1, ny - 1) - j) * nz, yp2 = (min(j + 2, ny - 1) - j) * nz;
+    const int zl = kc >= 4 ? -4 : 0, zr = kc + 8 <= nz ? 4 : 0;
+
+    const unsigned c4 = kvalid ? __ldg((const unsigned*)(op.cls + p)) : 0u;
+    const float4 C = ld4(in, p);
+    const float4 xa = ld4(in, p + xm2), xb = ld4(in, p + xm1), xc = ld4(in, p + xp1),
+                 xd = ld4(in, p + xp2);
+    const float4 ya = ld4(in, p + ym2), yb = ld4(in, p + ym1), yc = ld4(in, p + yp1),
+                 yd = ld4(in, p + yp2);
+    const float4 zL = ld4(in, p + zl), zR = ld4(in, p + zr);
+    const float* __restrict__ u0 = (const float*)sa.u0;
+    const float4 uh = STAGE == 0 ? C : *(const float4*)(u0 + p);
+    const float4 ul = *(const float4*)(u0 + op.N + p);
+    float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (STAGE > 0) av = *((const float4*)((const float*)sa.acc + p));
+    const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
+
+    float v[3][4];
+    unsigned kq[3][4];
+    bool special = false;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
+            special = special || kq[d][q] >= ROW_CLOSURE;
+        }
+        const float sx = interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q));
+        const float sy = interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q));
+        const float sz = interior_row_t<FORM>(op.ax[2], zz[q], zz[q + 1], zz[q + 2], zz[q + 3], zz[q + 4]);
+        v[0][q] = kq[0][q] == ROW_INTERIOR ? sx : 0.f;
+        v[1][q] = kq[1][q] == ROW_INTERIOR ? sy : 0.f;
+        v[2][q] = kq[2][q] == ROW_INTERIOR ? sz : 0.f;
+    }
+    if (__any_sync(FULL, special)) {
+        const float* __restrict__ cval = (const float*)sa.cval;
+        const int sub = lane >> 3; // 32-point chunk of the warp holding this lane's points
+        const unsigned chunk_before = lanemask_lt() & (0xFFu << (8 * sub));
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const DevAxis& A = op.ax[d];
+            bool has_cut = false, has_wall = false;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                has_cut = has_cut || kq[d][q] == ROW_CLOSURE;
+                has_wall = has_wall || kq[d][q] == ROW_WALL;
+            }
+            if (__any_sync(FULL, has_cut)) {
+                int before = 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    before += __popc(__ballot_sync(FULL, kq[d][q] == ROW_CLOSURE) & chunk_before);
+                if (has_cut) {
+                    int r = A.row_base + before +
+                            A.chunk_base[((long long)i * ny + j) * op.nzc + blockIdx.x * 4 + sub];
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (kq[d][q] == ROW_CLOSURE) v[d][q] = cval[r++];
                 }
-                rhs = fmaf(lap, sp.kf, src);
-            } else {
-                float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
-                if (sp.vel_kind != 0) {
-                    const float r0 = (float)op.xc[0][i] - sp.centerf[0];
-                    const float r1 = (float)op.xc[1][j] - sp.centerf[1];
-                    const float r2 = (float)op.xc[2][k] - sp.centerf[2];
-                    const float il = rsqrtf(r0 * r0 + r1 * r1 + r2 * r2);
-                    g0 = -r0 * il;
-                    g1 = -r1 * il;
-                    g2 = -r2 * il;
+            }
+            if (has_wall) {
+                if (d == 2) { // rows at the ends of the z line: from the z-wall table
+                    const float* __restrict__ zrow =
+                        sa.zw + (long long)(i * ny + j) * zwall_slots(A);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (kq[d][q] == ROW_WALL) v[d][q] = zrow[zwall_slot(A, k + q)];
+                } else { // whole x / y wall planes: uniform across the warp
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (kq[d][q] == ROW_WALL)
+                            v[d][q] = wall32(A, (long long)(p + q), d == 0 ? i : j, in);
                 }
-                rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
             }
         }
-        float2* __restrict__ u0 = (float2*)sa.u0;
-        float* __restrict__ acc = (float*)sa.acc;
-        const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
-        if constexpr (STAGE == 0) {
-            const float2 u = ((const float2*)sa.u0)[p];
-            acc[p] = inc;
-            ((float*)sa.s_out)[p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
-        } else if constexpr (STAGE < 3) {
-            acc[p] = av[t] + inc;
-            ((float*)sa.s_out)[p] = uu[t].x + fmaf(sa.ci_ff.x, rhs, uu[t].y);
-        } else {
-            const float a = av[t] + inc;
-            const float2 tt = two_sum(uu[t].x, a);
-            u0[p] = fast_two_sum(tt.x, tt.y + uu[t].y);
+    }
+    if (!kvalid) return;
+    float ao[4], so[4];
+    float2 uo[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float lap = 0.f;
+        if constexpr (SYS == SYS_HEAT) {
+            lap = __fadd_rn(lap, v[0][q]);
+            lap = __fadd_rn(lap, v[1][q]);
+            lap = __fadd_rn(lap, v[2][q]);
         }
+        const float rhs = ((c4 >> (8 * q)) & 0x3Fu)
+                              ? rhs_mixed<SYS, VK>(op, sp, sa.etf_stage, i, j, k + q, lap,
+                                                   v[0][q], v[1][q], v[2][q])
+                              : 0.f;
+        rk_mixed<STAGE>(sa, rhs, make_float2(f4(uh, q), f4(ul, q)), f4(av, q), ao[q], so[q],
+                        uo[q]);
+    }
+    if constexpr (STAGE < 3) {
+        *((float4*)((float*)sa.acc + p)) = make_float4(ao[0], ao[1], ao[2], ao[3]);
+        *((float4*)((float*)sa.s_out + p)) = make_float4(so[0], so[1], so[2], so[3]);
+    } else {
+        float* __restrict__ w0 = (float*)sa.u0;
+        *((float4*)(w0 + p)) = make_float4(uo[0].x, uo[1].x, uo[2].x, uo[3].x);
+        *((float4*)(w0 + op.N + p)) = make_float4(uo[0].y, uo[1].y, uo[2].y, uo[3].y);
     }
 }
 
@@ -921,23 +1139,34 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b)
 // Consumers (warps 0..7, one tile row each, one point per lane) read only shared memory on
 // the interior fast path.  Every wait is bounded; on time-out the CTA records an error
 // flag, stops issuing copies, and drains the ones in flight before it returns.
+//
+// Slot layout: stage-field plane with halo (FP32; the hi plane of u0 in stage 0), class
+// bytes, hi tile of u0 (stages 1-3; stage 0 has it in the halo plane), lo tile of u0,
+// accumulator tile (stages 1-3).
+template <int STAGE>
+struct TmaSlot {
+    static constexpr unsigned S = TMA_BY * TMA_BZ * 4u;
+    static constexpr unsigned C = TMA_TY * TMA_TZ;
+    static constexpr unsigned UH = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
+    static constexpr unsigned UL = TMA_TY * TMA_TZ * 4u;
+    static constexpr unsigned A = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
+    static constexpr unsigned BYTES = S + C + UH + UL + A;
+    static_assert(BYTES % 128 == 0 && S % 128 == 0 && C % 128 == 0 && UH % 128 == 0 &&
+                      UL % 128 == 0,
+                  "TMA destinations stay 128-byte aligned");
+};
+
 template <int STAGE, int SYS>
 __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__ CUtensorMap tm_in,
-                                                         const __grid_constant__ CUtensorMap tm_u0,
+                                                         const __grid_constant__ CUtensorMap tm_u0h,
+                                                         const __grid_constant__ CUtensorMap tm_u0l,
                                                          const __grid_constant__ CUtensorMap tm_acc,
                                                          const __grid_constant__ CUtensorMap tm_cls,
                                                          DevOp op, SysParams sp, StageArgs sa,
                                                          unsigned* err)
 {
-    using TIN = typename std::conditional<STAGE == 0, float2, float>::type;
-    constexpr unsigned S_BYTES = TMA_BY * TMA_BZ * sizeof(TIN);
-    constexpr unsigned C_BYTES = TMA_TY * TMA_TZ;
-    constexpr unsigned U_BYTES = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 8u;
-    constexpr unsigned A_BYTES = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
-    constexpr unsigned SLOT = S_BYTES + C_BYTES + U_BYTES + A_BYTES;
-    static_assert(SLOT % 128 == 0 && S_BYTES % 128 == 0 && C_BYTES % 128 == 0 &&
-                      U_BYTES % 128 == 0,
-                  "TMA destinations stay 128-byte aligned");
+    using L = TmaSlot<STAGE>;
+    constexpr unsigned S_BYTES = L::S, C_BYTES = L::C, SLOT = L::BYTES;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + TMA_NS * SLOT);
     uint64_t* empty = full + TMA_NS;
@@ -977,16 +1206,17 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
                 }
                 unsigned char* base = smem_raw + slot * SLOT;
                 const bool own = pl >= xa && pl < xb;
-                mbar_expect_tx(&full[slot],
-                               S_BYTES + (own ? C_BYTES + U_BYTES + A_BYTES : 0u));
+                mbar_expect_tx(&full[slot], own ? SLOT : S_BYTES);
                 tma_load_3d(base, &tm_in, k0 - TMA_HZ, j0 - TMA_HY, pl, &full[slot]);
                 if (own) {
                     tma_load_3d(base + S_BYTES, &tm_cls, k0, j0, pl, &full[slot]);
-                    if (STAGE > 0) {
-                        tma_load_3d(base + S_BYTES + C_BYTES, &tm_u0, k0, j0, pl, &full[slot]);
-                        tma_load_3d(base + S_BYTES + C_BYTES + U_BYTES, &tm_acc, k0, j0, pl,
-                                    &full[slot]);
-                    }
+                    if (STAGE > 0)
+                        tma_load_3d(base + S_BYTES + C_BYTES, &tm_u0h, k0, j0, pl, &full[slot]);
+                    tma_load_3d(base + S_BYTES + C_BYTES + L::UH, &tm_u0l, k0, j0, pl,
+                                &full[slot]);
+                    if (STAGE > 0)
+                        tma_load_3d(base + S_BYTES + C_BYTES + L::UH + L::UL, &tm_acc, k0, j0,
+                                    pl, &full[slot]);
                 }
             }
             w += xb - xa;
@@ -1004,9 +1234,8 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
     const int s_off = (TMA_HY + ty) * TMA_BZ + (TMA_HZ + tz);
     const int t_off = ty * TMA_TZ + tz;
     const float* __restrict__ cval = (const float*)sa.cval;
-    float2* __restrict__ u0g = (float2*)sa.u0;
     float* __restrict__ accg = (float*)sa.acc;
-    const TIN* __restrict__ gin = STAGE == 0 ? (const TIN*)sa.u0 : (const TIN*)sa.s_in;
+    const float* __restrict__ gin = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     const int plane = ny * nz;
     bool ok = true;
     auto wait_full = [&](unsigned q) {
@@ -1033,26 +1262,18 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
             const unsigned r = r0 + 2 + (unsigned)(i - xa); // stream index of plane i
             wait_full(r + 2);
             const unsigned char* cur = smem_raw + (r % TMA_NS) * SLOT;
-            const TIN* Sc = reinterpret_cast<const TIN*>(cur) + s_off;
+            const float* Sc = reinterpret_cast<const float*>(cur) + s_off;
             auto Sx = [&](int m) -> float { // plane i-2+m, this column
-                const TIN* q2 =
-                    reinterpret_cast<const TIN*>(smem_raw + ((r - 2 + m) % TMA_NS) * SLOT) + s_off;
-                if constexpr (STAGE == 0) return q2->x;
-                else return *q2;
+                return reinterpret_cast<const float*>(smem_raw + ((r - 2 + m) % TMA_NS) * SLOT)[s_off];
             };
-            auto Sp = [&](int off) -> float {
-                if constexpr (STAGE == 0) return Sc[off].x;
-                else return Sc[off];
-            };
+            auto Sp = [&](int off) -> float { return Sc[off]; };
             const unsigned c = (col_valid && ok) ? (unsigned)cur[S_BYTES + t_off] : 0u;
             float2 u;
             float accv = 0.f;
-            if constexpr (STAGE == 0) {
-                u = Sc[0];
-            } else {
-                u = reinterpret_cast<const float2*>(cur + S_BYTES + C_BYTES)[t_off];
-                accv = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + U_BYTES)[t_off];
-            }
+            u.x = STAGE == 0 ? Sc[0] : reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES)[t_off];
+            u.y = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + L::UH)[t_off];
+            if constexpr (STAGE > 0)
+                accv = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + L::UH + L::UL)[t_off];
             float lap = 0.f;
             float dd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -1093,45 +1314,23 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
                     }
                 }
                 if (SYS == SYS_HEAT)
-                    lap = lap + v;
+                    lap = __fadd_rn(lap, v);
                 else
                     dd[d] = v;
             }
             release(r - 2); // plane i-2 is no longer read by this warp
             if (!(col_valid && ok)) continue;
-            float rhs = 0.f;
-            if (c & 0x3Fu) {
-                if (SYS == SYS_HEAT) {
-                    float src = 0.f;
-                    if (sp.sol.kind == SOL_SINSIN) {
-                        float uu = sp.sol.Sf[0][i] * sp.sol.Sf[1][j];
-                        if (sp.sol.dims == 3) uu = uu * sp.sol.Sf[2][k];
-                        uu = uu * sa.etf_stage;
-                        src = (-uu) - sp.kf * ((float)sp.sol.lapfac * uu);
-                    }
-                    rhs = fmaf(lap, sp.kf, src);
-                } else {
-                    float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
-                    if (sp.vel_kind != 0) {
-                        const float r0f = (float)op.xc[0][i] - sp.centerf[0];
-                        const float r1f = (float)op.xc[1][j] - sp.centerf[1];
-                        const float r2f = (float)op.xc[2][k] - sp.centerf[2];
-                        const float il = rsqrtf(r0f * r0f + r1f * r1f + r2f * r2f);
-                        g0 = -r0f * il;
-                        g1 = -r1f * il;
-                        g2 = -r2f * il;
-                    }
-                    rhs = fmaf(g2, dd[2], fmaf(g1, dd[1], g0 * dd[0]));
-                }
-            }
-            const float inc = fmaf(sa.cf_ff.x, rhs, sa.cf_ff.y * rhs);
-            if (STAGE < 3) {
-                accg[p] = STAGE == 0 ? inc : accv + inc;
-                ((float*)sa.s_out)[p] = u.x + fmaf(sa.ci_ff.x, rhs, u.y);
+            const float rhs = (c & 0x3Fu) ? rhs_mixed<SYS>(op, sp, sa.etf_stage, i, j, k, lap,
+                                                           dd[0], dd[1], dd[2])
+                                          : 0.f;
+            float a_out = 0.f, s_out = 0.f;
+            float2 u_out;
+            rk_mixed<STAGE>(sa, rhs, u, accv, a_out, s_out, u_out);
+            if constexpr (STAGE < 3) {
+                accg[p] = a_out;
+                ((float*)sa.s_out)[p] = s_out;
             } else {
-                const float a = accv + inc;
-                const float2 t = two_sum(u.x, a);
-                u0g[p] = fast_two_sum(t.x, t.y + u.y);
+                st_pair(sa.u0, op.N, p, u_out);
             }
         }
         // the segment's last four planes (xb-2 .. xb+1) are no longer needed
@@ -1175,7 +1374,7 @@ __global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
     const double v = sol_at_point(op, sol, t, et, ijk);
     if (MIXED) {
         if (LAST)
-            ((float2*)out)[p] = ff_from_double(v);
+            st_pair(out, op.N, p, ff_from_double(v));
         else
             ((float*)out)[p] = (float)v;
     } else {
@@ -1231,7 +1430,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevOp op, SysParams sp, const void*
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
         double v = 0.0;
         if (MIXED) {
-            const float2* in = (const float2*)uin;
+            const PairU in{(const float*)uin, op.N};
             if (kind == ROW_INTERIOR) v = (double)interior32(A, in, q.p);
             else if (kind == ROW_WALL) v = (double)wall32(A, q.p, ijk[d], in);
             else if (kind == ROW_CLOSURE)
@@ -1281,7 +1480,7 @@ __global__ void __launch_bounds__(256) k_init(DevOp op, DevSol sol, double t, do
         v = sol_at_point(op, sol, t, et, ijk);
     }
     if (mixed)
-        ((float2*)u0)[q.p] = ff_from_double(v);
+        st_pair(u0, op.N, q.p, ff_from_double(v));
     else
         ((double*)u0)[q.p] = v;
 }
@@ -1293,15 +1492,15 @@ __global__ void k_init_r(DevR dr, DevSol sol, int n, int d, double t, double et,
     out[i] = sol_at(sol, t, et, dr.pos[d] + 3 * (long long)i, nullptr, d, i);
 }
 
-__global__ void k_convert(long long n, int to_mixed, const double* in_d, float2* out_m,
-                          const float2* in_m, double* out_d)
+__global__ void k_convert(long long n, int to_mixed, const double* in_d, float* out_m,
+                          const float* in_m, double* out_d)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (to_mixed)
-        out_m[i] = ff_from_double(in_d[i]);
-    else {
-        const float2 v = in_m[i];
+    if (to_mixed) {
+        st_pair(out_m, n, i, ff_from_double(in_d[i]));
+    } else {
+        const float2 v = ld_pair(in_m, n, i);
         out_d[i] = (double)v.x + (double)v.y;
     }
 }
@@ -1329,7 +1528,7 @@ __global__ void __launch_bounds__(256) k_stats(DevOp op, DevSol sol, double t, d
     const Pt q = point_of(op);
     StatPart s{-1.0, 0, 1e308, -1e308};
     if (q.valid && (op.cls[q.p] & CLS_FLUID)) {
-        const double u = mixed ? ldd((const float2*)u0, q.p) : ((const double*)u0)[q.p];
+        const double u = mixed ? ldd(PairU{(const float*)u0, op.N}, q.p) : ((const double*)u0)[q.p];
         int ijk[3];
         phys_ijk(op, q, ijk);
         double e = fabs(u - sol_at_point(op, sol, t, et, ijk));
@@ -1469,28 +1668,29 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
 {
     const dim3 grid = point_grid(op), block(32, BY);
     const bool mixed = prec == PREC_MIXED;
-    if (op.n_cut_rows) {
-        const int nb = (op.n_cut_rows + 127) / 128;
+    float* zw = mixed && b.vec ? a.zw : nullptr;
+    const long long n_zw =
+        zw ? (long long)op.it0 * op.it1 * (op.ax[2].wall[0].rows + op.ax[2].wall[1].rows) : 0;
+    if (op.n_cut_rows || n_zw) {
+        const int nb = (int)((op.n_cut_rows + n_zw + 127) / 128);
         const double* const* R = a.R;
         if (!mixed)
-            k_cut_rows<double, double><<<nb, 128, 0, s>>>(
+            k_cut_rows<const double*, double><<<nb, 128, 0, s>>>(
                 op, (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
-                (double*)a.cval);
+                (double*)a.cval, nullptr);
         else if (STAGE == 0)
-            k_cut_rows<float2, float><<<nb, 128, 0, s>>>(op, (const float2*)a.u0, R[0], R[1],
-                                                         R[2], (float*)a.cval);
+            k_cut_rows<PairU, float><<<nb, 128, 0, s>>>(op, PairU{(const float*)a.u0, op.N},
+                                                        R[0], R[1], R[2], (float*)a.cval, zw);
         else
-            k_cut_rows<float, float><<<nb, 128, 0, s>>>(op, (const float*)a.s_in, R[0], R[1],
-                                                        R[2], (float*)a.cval);
+            k_cut_rows<const float*, float><<<nb, 128, 0, s>>>(op, (const float*)a.s_in, R[0],
+                                                               R[1], R[2], (float*)a.cval, zw);
         ++g_launches;
     }
     if (ev) cudaEventRecord(ev[0], s);
     const bool small = op.N < (1LL << 31) - 64;
     if (mixed && b.tma) {
         const CUtensorMap& tm = STAGE == 0 ? b.tm_u0 : (STAGE == 2 ? b.tm_sb : b.tm_sa);
-        const size_t slot = (STAGE == 0 ? TMA_BY * TMA_BZ * 8 : TMA_BY * TMA_BZ * 4 + TMA_TY * TMA_TZ * 12) +
-                            TMA_TY * TMA_TZ;
-        const size_t smem = TMA_NS * slot + 2 * TMA_NS * 8;
+        const size_t smem = TMA_NS * TmaSlot<STAGE>::BYTES + 2 * TMA_NS * 8;
         static int grid_n[4] = {0, 0, 0, 0};
         if (!grid_n[STAGE]) {
             cudaFuncSetAttribute(k_stage_mixed_tma<STAGE, SYS>,
@@ -1506,7 +1706,20 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
                                ((op.it1 + TMA_TY - 1) / TMA_TY) * op.it0;
         const int grid = (int)std::min<long long>(grid_n[STAGE], work);
         k_stage_mixed_tma<STAGE, SYS><<<grid, dim3(32, TMA_TY + 1), smem, s>>>(
-            tm, b.tm_u0t, b.tm_acct, b.tm_cls, op, sp, a, b.err);
+            tm, b.tm_u0t, b.tm_u0l, b.tm_acct, b.tm_cls, op, sp, a, b.err);
+    } else if (mixed && b.vec) {
+        const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0);
+        if constexpr (SYS == SYS_WAVE) {
+            if (sp.vel_kind)
+                k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1><<<vgrid, block, 0, s>>>(op, sp, a);
+            else
+                k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+        } else {
+            if (b.vec == FORM_SYM5)
+                k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+            else
+                k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+        }
     } else if (mixed && b.col_nx) {
         const dim3 cgrid(op.nzc, (op.it1 + BY - 1) / BY, (op.it0 + b.col_nx - 1) / b.col_nx);
         if (b.col_nx == 2)
@@ -1591,6 +1804,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.u0 = b.u0;
         a.acc = b.acc;
         a.cval = b.cval;
+        a.zw = b.zwall;
         a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
         a.s_out = i == 1 ? b.sb : b.sa;
         for (int d = 0; d < 3; d++)
@@ -1662,7 +1876,7 @@ cudaError_t launch_state_convert(long long n, int to_mixed, const double* in_d, 
 {
     const int bs = 256;
     const long long nb = (n + bs - 1) / bs;
-    k_convert<<<(unsigned)nb, bs, 0, s>>>(n, to_mixed, in_d, (float2*)out, (const float2*)in_m,
+    k_convert<<<(unsigned)nb, bs, 0, s>>>(n, to_mixed, in_d, (float*)out, (const float*)in_m,
                                           out_d);
     ++g_launches;
     return cudaGetLastError();

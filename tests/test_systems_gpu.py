@@ -226,33 +226,55 @@ def test_nonfinite_detected():
     assert not valid
 
 
+STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec")
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["heat", "wave"])
-def test_stage_kernel_variants_agree_bitwise(kind, monkeypatch):
+@pytest.mark.parametrize("kind,nz", [("heat", 48), ("heat", 128), ("wave", 48), ("wave", 128),
+                                     ("wave_radial", 128), ("wave_sphere_radial", 128)])
+def test_stage_kernel_variants_agree_bitwise(kind, nz, monkeypatch):
     """Every mixed stage-kernel variant (TMA plane marching, column-blocked with 1/2/4
-    planes per thread, per-point) gives the same bits: same arithmetic, different data
-    movement.  The autotuner may therefore pick any of them."""
+    planes per thread, vectorised with four z points per thread, per-point) gives the same
+    bits: same arithmetic, different data movement.  The autotuner may therefore pick any of
+    them.  The cases cover warps without special rows (nz = 128), partially filled warps
+    (nz = 48), cut-cell rows, domain-wall rows and both velocity fields."""
+    steps = 17
     if kind == "heat":
-        case = dict(n=(36, 34, 48), lo=(0, 0, 0), hi=(1, 1, 1),
+        case = dict(n=(36, 34, nz), lo=(0, 0, 0), hi=(1, 1, 1),
                     spheres=[((0.5, 0.45, 0.52), 0.2, "dirichlet")],
                     grid_bc=("dirichlet",) * 6, scheme="E4_2")
         make = lambda p: S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, [1.0])
         dt = 0.4 * (1.0 / 35) ** 2 / 4
-    else:
-        case = dict(BOX_CASE, n=(34, 30, 48))
+    elif kind == "wave":
+        case = dict(BOX_CASE, n=(34, 30, nz))
         make = lambda p: S.ScalarWave(p, S.PREC_MIXED, S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE)
         dt = 0.5 / 35
+    elif kind == "wave_radial":  # velocity field pointing away from a centre outside the box
+        case = dict(BOX_CASE, n=(34, 30, nz))
+        make = lambda p: S.ScalarWave(p, S.PREC_MIXED, S.VEL_RADIAL, (0, 0, 0),
+                                      (-0.3, -0.2, -0.1), 2, PULSE)
+        dt = 0.5 / 35
+    else:
+        # cut-cell rows of a sphere, radial velocity.  E4_1's wall and small-cell rows
+        # (~1e5/h) grow the solution by ~dt*3e6 per stage, so a short dt keeps three steps
+        # finite in FP32.
+        case = dict(WAVE_CASE, n=(40, 38, nz))
+        make = lambda p: S.ScalarWave(p, S.PREC_MIXED, S.VEL_RADIAL, (0, 0, 0),
+                                      tuple(WAVE_CASE["spheres"][0][0]), 2, PULSE)
+        dt = 1e-5
+        steps = 3
     p = S.Problem(**case)
     out = {}
-    for name in ("point", "tma", "col1", "col2", "col4"):
+    for name in STAGE_VARIANTS:
         monkeypatch.setenv("SHOCCS_STAGE_KERNEL", name)
         s = make(p)
         assert s.stage_kernel == name
         s.initialize(0.0)
-        s.rk4(0.0, dt, 17)
+        s.rk4(0.0, dt, steps)
         u = [np.zeros(p.size)] + [np.zeros(k) for k in p.nR]
         s.get_state(S.ScalarField(*u))
         out[name] = u[0]
+    assert np.isfinite(out["point"]).all()
     for name, v in out.items():
         assert np.array_equal(v, out["point"]), name
     monkeypatch.delenv("SHOCCS_STAGE_KERNEL")
