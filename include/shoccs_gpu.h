@@ -195,9 +195,10 @@ shoccs_status shoccs_system_stats_noalloc(shoccs_system* s, double t, double out
 shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double* dt);
 /* Stage-kernel variant of the system's RK4 path, chosen at creation by timing the
  * candidates on the system's own grid (the SHOCCS_STAGE_KERNEL environment variable --
- * point, tma, col1, col2, col4, vec -- forces one):
+ * point, tma, col1, col2, col4, vec, vec3 -- forces one):
  * 0 per-point kernel, 1 TMA plane-marching, 2/3/4 column-blocked with 1/2/4 planes per
- * thread, 5 vectorised (four z points per thread; nz a multiple of 4).  All variants give
+ * thread, 5/6 vectorised (four z points per thread; nz a multiple of 4) with 4/3 resident
+ * blocks per SM.  All variants give
  * the same bits.  FP64 systems and 2-D / 1-D grids always use the per-point kernel. */
 shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);
 /* kernels launched by this library since load (for launch-count accounting) */

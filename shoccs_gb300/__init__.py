@@ -272,7 +272,8 @@ class System:
             _capi.check(st)
         return vals, st == _capi.OK
 
-    STAGE_KERNELS = {0: "point", 1: "tma", 2: "col1", 3: "col2", 4: "col4", 5: "vec"}
+    STAGE_KERNELS = {0: "point", 1: "tma", 2: "col1", 3: "col2", 4: "col4", 5: "vec",
+                     6: "vec3"}
 
     @property
     def stage_kernel(self):

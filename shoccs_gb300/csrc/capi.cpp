@@ -94,6 +94,13 @@ struct shoccs_system {
     DeviceAlloc mem;
     StepBuffers b{};
     double t = 0.0;
+    ~shoccs_system()
+    {
+        if (b.side) cudaStreamDestroy(b.side);
+        if (b.fork) cudaEventDestroy(b.fork);
+        if (b.join) cudaEventDestroy(b.join);
+        if (b.join_next) cudaEventDestroy(b.join_next);
+    }
 };
 
 namespace
@@ -153,6 +160,14 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
         SH_CUDA(p->mem.put(T.rows, &A.rows, s));
         SH_CUDA(p->mem.put(T.row_out, (const long long**)&A.row_out, s));
         SH_CUDA(p->mem.put(T.coef, &A.coef, s));
+        {
+            std::vector<float2> ff(T.coef.size());
+            for (size_t m = 0; m < ff.size(); m++) {
+                const float hi = (float)T.coef[m];
+                ff[m] = make_float2(hi, (float)(T.coef[m] - (double)hi));
+            }
+            SH_CUDA(p->mem.put(ff, &A.coef_ff, s));
+        }
         SH_CUDA(p->mem.put(T.chunk_base, &A.chunk_base, s));
         for (int r = 0; r < 3; r++) {
             if (T.rr_u[r].empty()) continue;
@@ -434,7 +449,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
 {
     struct Cand {
         const char* name;
-        int tma, col, vec;
+        int tma, col, vec, minb = 4;
     };
     std::vector<Cand> cands;
     if (S->b.tma) cands.push_back({"tma", 1, 0, 0});
@@ -453,8 +468,10 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         const bool wave = S->desc.kind == SHOCCS_SYS_WAVE;
         if (wave ? form != FORM_ANTI5 : (form != FORM_SYM5 && form != FORM_W3)) form = FORM_ANY;
     }
-    if (S->P->comp.it[2] % 4 == 0 && S->b.zwall && form != FORM_ANY)
-        cands.push_back({"vec", 0, 0, form});
+    if (S->P->comp.it[2] % 4 == 0 && S->b.zwall && form != FORM_ANY) {
+        cands.push_back({"vec", 0, 0, form, 4});
+        cands.push_back({"vec3", 0, 0, form, 3});
+    }
     cands.push_back({"col1", 0, 1, 0});
     cands.push_back({"col2", 0, 2, 0});
     cands.push_back({"col4", 0, 4, 0});
@@ -463,6 +480,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         S->b.tma = c.tma;
         S->b.col_nx = c.col;
         S->b.vec = c.vec;
+        S->b.vec_minb = c.minb;
     };
     if (const char* force = std::getenv("SHOCCS_STAGE_KERNEL")) {
         for (const auto& c : cands)
@@ -612,6 +630,36 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.Rfull[r] = (double*)f;
         if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
     }
+    if (d->prec == PREC_MIXED) {
+        // exact values on the Dirichlet faces, evaluated once per step on a side stream
+        for (int f = 0; f < 6; f++) {
+            if (p->bcs.grid[f / 2][f % 2] != Dirichlet) continue;
+            const int a = f / 2;
+            const size_t n = a == 0   ? (size_t)p->mesh.n[1] * p->mesh.n[2]
+                             : a == 1 ? (size_t)p->mesh.n[0] * p->mesh.n[2]
+                                      : (size_t)p->mesh.n[0] * p->mesh.n[1];
+            void* fp = nullptr;
+            SH_CUDA(S->mem.alloc(n * sizeof(float4), &fp));
+            S->b.fplane[f] = (float4*)fp;
+            SH_CUDA(S->mem.alloc(n * sizeof(float4), &fp));
+            S->b.fplane_next[f] = (float4*)fp;
+        }
+        // second set of cut-point boundary values (the next step's, evaluated ahead)
+        for (int r = 0; r < 3; r++) {
+            const size_t n = p->mesh.R[r].size();
+            void *h = nullptr, *f = nullptr;
+            SH_CUDA(S->mem.alloc(n * 8, &h));
+            SH_CUDA(S->mem.alloc(n * 8, &f));
+            S->b.Rhalf_next[r] = (double*)h;
+            S->b.Rfull_next[r] = (double*)f;
+        }
+        int lo = 0, hi = 0;
+        SH_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        SH_CUDA(cudaStreamCreateWithPriority(&S->b.side, cudaStreamNonBlocking, hi));
+        SH_CUDA(cudaEventCreateWithFlags(&S->b.fork, cudaEventDisableTiming));
+        SH_CUDA(cudaEventCreateWithFlags(&S->b.join, cudaEventDisableTiming));
+        SH_CUDA(cudaEventCreateWithFlags(&S->b.join_next, cudaEventDisableTiming));
+    }
     // TMA plane-marching stages for 3-D mixed solves whose planes are 16-byte aligned
     {
         const int* it = p->comp.it;
@@ -729,7 +777,8 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     const cudaStream_t s = (cudaStream_t)stream;
     double t = t0;
     for (int i = 0; i < nsteps; i++) {
-        SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s));
+        SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
+                                nullptr, i + 1 < nsteps));
         t += dt; // step_controller advance (src/simulation/simulation_cycle.cpp:97)
     }
     SH_CUDA(cudaStreamSynchronize(s));
@@ -753,7 +802,7 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
     double t = t0;
     for (int i = 0; st == SHOCCS_OK && i < nsteps; i++) {
         cudaError_t e = launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt,
-                                        s, ev.data() + EV * (size_t)i);
+                                        s, ev.data() + EV * (size_t)i, i + 1 < nsteps);
         if (e != cudaSuccess) st = fail(SHOCCS_ECUDA, cudaGetErrorString(e));
         t += dt;
     }
@@ -862,7 +911,7 @@ shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
               : b.col_nx == 1      ? 2
               : b.col_nx == 2      ? 3
               : b.col_nx == 4      ? 4
-              : b.vec              ? 5
+              : b.vec              ? (b.vec_minb == 4 ? 5 : 6)
                                    : 0;
     return SHOCCS_OK;
 }

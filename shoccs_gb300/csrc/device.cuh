@@ -26,6 +26,7 @@ struct DevAxis {
     const ClosureRow* rows;
     const long long* row_out; // output flat index of each row
     const double* coef;
+    const float2* coef_ff; // the same pool as FP32 pairs (hi, lo = coef - hi)
     const int* chunk_base;
     // R-space rows (non-Dirichlet objects) per target r: CSR with source flag
     const int* rr_u[3];
@@ -107,17 +108,36 @@ struct StepBuffers {
     int col_nx = 0;
     // vectorised mixed stages (3-D grids, nz a multiple of 4) and their table of z-wall row
     // values (wall[0].rows + wall[1].rows per z line)
-    int vec = 0; // stencil form (FORM_*) of the vectorised kernel, 0 = not used
+    int vec = 0;      // stencil form (FORM_*) of the vectorised kernel, 0 = not used
+    int vec_minb = 4; // its resident blocks per SM (4: 64 registers, 3: 85 registers)
     float* zwall = nullptr;
     unsigned* err = nullptr;
+    // exact values on the Dirichlet domain faces (mixed path): per face (x lo, x hi, y lo,
+    // y hi, z lo, z hi; null where the face is not Dirichlet) a plane of {FP32 value at
+    // t+dt/2, FP32 value at t+dt, hi and lo words of the value at t+dt}, in the face's two
+    // other axes (lower axis slower); filled each step together with the cut-point values
+    float4* fplane[6] = {};
+    // side stream of those per-step boundary evaluations and its fork / join events.  With
+    // a side stream, each step also evaluates the next step's boundary values into a second
+    // set (the *_next buffers, swapped in when that step starts), so the FP64-heavy boundary
+    // kernel overlaps a whole step instead of delaying the first stage.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    double* Rhalf_next[3] = {};
+    double* Rfull_next[3] = {};
+    float4* fplane_next[6] = {};
+    cudaEvent_t join_next = nullptr;
+    bool next_pending = false; // the *_next set holds the step starting at next_t, next_dt
+    double next_t = 0.0, next_dt = 0.0;
     CUtensorMap tm_u0, tm_sa, tm_sb;     // stage inputs (u0: hi plane): one plane tile plus halo
     CUtensorMap tm_u0t, tm_u0l, tm_acct; // hi and lo planes of u0, accumulator: one tile, no halo
     CUtensorMap tm_cls;              // class bytes: one plane tile
 };
 
+// one RK4 step; prefetch_next: also start the next step's (t + dt, same dt) boundary values
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
-                            cudaEvent_t* ev = nullptr);
+                            cudaEvent_t* ev = nullptr, bool prefetch_next = false);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s);
 cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,

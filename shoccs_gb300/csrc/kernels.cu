@@ -183,6 +183,70 @@ __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long
     return v;
 }
 
+// ---- closure rows in compensated FP32 (mixed path) --------------------------------------
+// The mixed path's row inputs are FP32 (stage fields) or FP32 pairs (the solution), so a
+// cut-cell row needs no FP64 arithmetic to be evaluated well: every product of an FP32-pair
+// coefficient with an input is formed exactly to ~2^-48 (the leading product's rounding
+// error recovered by an FMA) and accumulated as an unevaluated FP32 pair (two-sum), which
+// keeps ~44 bits of the sum of terms as large as 1e7 x |u| -- far below the FP32 rounding
+// of the inputs themselves, and at FP32 rather than FP64 throughput.  All roundings are
+// explicit (__f*_rn), so no step is contracted into an FMA.
+__device__ __forceinline__ float2 ldff(const float* u, long long i) { return make_float2(__ldg(u + i), 0.f); }
+__device__ __forceinline__ float2 ldff(const PairU& u, long long i)
+{
+    return make_float2(__ldg(u.hi + i), __ldg(u.hi + u.n + i));
+}
+
+// (sh, sl) += (c.x + c.y) * (x.x + x.y), the term c.y * x.y (~2^-48 relative) dropped
+__device__ __forceinline__ void ff_mac(float& sh, float& sl, float2 c, float2 x)
+{
+    const float ph = __fmul_rn(c.x, x.x);
+    const float pe = fmaf(c.x, x.x, -ph); // exact rounding error of ph
+    const float pl = __fadd_rn(pe, fmaf(c.x, x.y, __fmul_rn(c.y, x.x)));
+    const float s = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+    const float t = __fadd_rn(__fadd_rn(e, sl), pl);
+    sh = __fadd_rn(s, t);
+    sl = __fsub_rn(t, __fsub_rn(sh, s));
+}
+
+// cut-cell row of the mixed path: sum_j c_j u_j + b R_d[b] (no Neumann term: systems have
+// no Neumann faces or objects)
+template <class TIN>
+__device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long p, TIN u,
+                                            const double* Rd)
+{
+    const ClosureRow cr = A.rows[row];
+    const float2* c = A.coef_ff + cr.coef_off;
+    const long long q0 = p + (long long)cr.col0 * A.stride;
+    // issue every load of the row before the first use, so the gathers overlap
+    constexpr int PF = 8;
+    float2 cv[PF], xv[PF];
+#pragma unroll
+    for (int j = 0; j < PF; ++j)
+        if (j < cr.ncol) {
+            cv[j] = __ldg(c + j);
+            xv[j] = ldff(u, q0 + j * A.stride);
+        }
+    double r = 0.0;
+    float2 cb = make_float2(0.f, 0.f);
+    if (cr.flags & ROWF_B) {
+        r = __ldg(Rd + cr.b_idx);
+        cb = __ldg(c + cr.ncol);
+    }
+    float sh = 0.f, sl = 0.f;
+#pragma unroll
+    for (int j = 0; j < PF; ++j)
+        if (j < cr.ncol) ff_mac(sh, sl, cv[j], xv[j]);
+    for (int j = PF; j < cr.ncol; ++j) ff_mac(sh, sl, __ldg(c + j), ldff(u, q0 + j * A.stride));
+    if (cr.flags & ROWF_B) {
+        const float rh = (float)r;
+        ff_mac(sh, sl, cb, make_float2(rh, (float)(r - (double)rh)));
+    }
+    return __fadd_rn(sh, sl);
+}
+
 // ---- domain-wall closure rows (shared per axis and side) ---------------------------------
 // row r of the block at axis coordinate `coord`: sum_j c[r][j] * x[col0 + j] along the axis
 __device__ __forceinline__ int wall_side(const DevAxis& A, int coord) { return coord * 2 < A.n ? 0 : 1; }
@@ -209,12 +273,14 @@ __device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord
 {
     const WallBlock& W = A.wall[wall_side(A, coord)];
     const int r = coord - W.first_row;
-    long long q = p + (long long)(W.col0 - coord) * A.stride;
+    const long long q = p + (long long)(W.col0 - coord) * A.stride;
+    float x[7]; // a wall block has at most 7 columns; all loads issued before the first use
+#pragma unroll
+    for (int j = 0; j < 7; ++j) x[j] = j < W.cols ? ldf(u, q + j * A.stride) : 0.f;
     float s = 0.f;
-    for (int j = 0; j < W.cols; ++j) {
-        s = fmaf(W.cf[r * 7 + j], ldf(u, q), s);
-        q += A.stride;
-    }
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j < W.cols) s = fmaf(W.cf[r * 7 + j], x[j], s);
     return s;
 }
 
@@ -434,6 +500,7 @@ struct StageArgs {
     void* s_out;
     const void* cval;
     float* zw;              // z-wall row values of the stage (vectorised mixed stages), or null
+    const float4* fplane[6]; // Dirichlet face values of the step (mixed path), see StepBuffers
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
     float2 cf_ff, ci_ff;    // same as compensated FP32 pairs
@@ -452,7 +519,8 @@ __device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
     return k * 2 < A.n ? k - A.wall[0].first_row : A.wall[0].rows + (k - A.wall[1].first_row);
 }
 
-// cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b]  (FP64); with zw, threads past
+// cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b] (FP64 path: FP64; mixed path:
+// compensated FP32, closure_ff); with zw, threads past
 // the cut-cell rows also evaluate the domain-wall rows of the z axis (FP32, wall32) into a
 // table of zwall_slots() values per z line, which the vectorised mixed stage reads: those
 // rows sit at both ends of every z line, so every warp of that kernel holds some.
@@ -463,19 +531,31 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= op.n_cut_rows) {
-        if (!zw) return;
-        const DevAxis& A = op.ax[2];
-        // 32-bit: the table and the cut-cell rows together stay below 2^31 entries
-        const int ns = zwall_slots(A);
-        const int e = i - op.n_cut_rows;
-        if (ns == 0 || e >= op.it0 * op.it1 * ns) return;
-        const int line = e / ns;
-        const int slot = e - line * ns;
-        const int k = slot < A.wall[0].rows ? A.wall[0].first_row + slot
-                                            : A.wall[1].first_row + (slot - A.wall[0].rows);
-        const long long p = (long long)line * op.it2 + k;
-        if constexpr (!std::is_same<TIN, const double*>::value)
-            if (((op.cls[p] >> 4) & 3u) == ROW_WALL) zw[e] = wall32(A, p, k, u);
+        if constexpr (!std::is_same<TIN, const double*>::value) {
+            // one thread per z line: both wall blocks from the line's end values (slots of
+            // lines whose ends are not wall rows are written too and never read)
+            const int line = i - op.n_cut_rows;
+            if (!zw || line >= op.it0 * op.it1) return;
+            const DevAxis& A = op.ax[2];
+            float* __restrict__ out = zw + (long long)line * zwall_slots(A);
+            const long long base = (long long)line * op.it2;
+            int slot = 0;
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                const WallBlock& W = A.wall[side];
+                float x[7];
+#pragma unroll
+                for (int jj = 0; jj < 7; jj++)
+                    x[jj] = jj < W.cols ? ldf(u, base + W.col0 + jj) : 0.f;
+                for (int r = 0; r < W.rows; r++, slot++) {
+                    float acc = 0.f; // wall32's operation order
+#pragma unroll
+                    for (int jj = 0; jj < 7; jj++)
+                        if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
+                    out[slot] = acc;
+                }
+            }
+        }
         return;
     }
     const double* R[3] = {R0, R1, R2};
@@ -483,7 +563,10 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
     const DevAxis& A = op.ax[d];
     const int row = i - A.row_base;
     const long long p = A.row_out[row];
-    cval[i] = (TOUT)closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
+    if constexpr (std::is_same<TOUT, double>::value)
+        cval[i] = closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
+    else
+        cval[i] = closure_ff(A, row, p, u, R[d]);
 }
 
 
@@ -892,6 +975,77 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
     }
 }
 
+// ---- Dirichlet face values of the mixed path ------------------------------------------------
+// The exact solution on the Dirichlet domain faces depends only on the time, so each RK4
+// step evaluates it once, for every face point, into per-face planes (StepBuffers::fplane):
+// the FP32 stage fields take the value computed in FP32 arithmetic at t+dt/2 (stages 0, 1)
+// and t+dt (stage 2), the solution takes the compensated pair of the FP64 value at t+dt.
+inline int face_plane_size_host(const DevOp& op, int f)
+{
+    const int a = f >> 1;
+    return a == 0 ? op.n[1] * op.n[2] : (a == 1 ? op.n[0] * op.n[2] : op.n[0] * op.n[1]);
+}
+
+// the exact value in FP32 arithmetic (the stage fields' precision)
+__device__ float face_f32(const DevOp& op, const DevSol& sol, double t, double et,
+                          const int ijk[3])
+{
+    if (sol.kind == SOL_GAUSS_PULSE || sol.kind == SOL_RADIAL_SIN) {
+        const float x0 = (float)op.xc[0][ijk[0]], x1 = (float)op.xc[1][ijk[1]],
+                    x2 = (float)op.xc[2][ijk[2]];
+        const float tf = (float)t;
+        if (sol.kind == SOL_GAUSS_PULSE) {
+            const float d0 = (x0 - (float)sol.p[0]) - (float)sol.p[3] * tf;
+            const float d1 = (x1 - (float)sol.p[1]) - (float)sol.p[4] * tf;
+            const float d2 = (x2 - (float)sol.p[2]) - (float)sol.p[5] * tf;
+            const float sg = (float)sol.p[6];
+            return expf(-(d0 * d0 + d1 * d1 + d2 * d2) / (2.f * sg * sg));
+        }
+        const float d0 = x0 - (float)sol.p[0], d1 = x1 - (float)sol.p[1],
+                    d2 = x2 - (float)sol.p[2];
+        return sinf(6.283185307179586f * (sqrtf(d0 * d0 + d1 * d1 + d2 * d2) -
+                                          (float)sol.p[3] - tf));
+    }
+    return (float)sol_at_point(op, sol, t, et, ijk);
+}
+
+// plane entry of the face point (i, j, k): the first Dirichlet face that holds it (every
+// face holding it has the same values)
+__device__ __forceinline__ const float4* face_entry(const StageArgs& sa, const DevOp& op, int i,
+                                                    int j, int k)
+{
+    const int ijk[3] = {i, j, k};
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        const int a = f >> 1;
+        if (!sa.fplane[f] || ijk[a] != ((f & 1) ? op.n[a] - 1 : 0)) continue;
+        const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        return sa.fplane[f] + (ijk[b] * op.n[c] + ijk[c]);
+    }
+    return nullptr;
+}
+
+// face values of the stage output from the planes, for the stage kernels without the
+// face write fused in
+template <int STAGE>
+__global__ void k_faces_mixed(DevOp op, StageArgs sa)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= op.n_faces) return;
+    const long long p = op.faces[e];
+    const long long nyz = (long long)op.n[1] * op.n[2];
+    const int i = (int)(p / nyz), j = (int)((p / op.n[2]) % op.n[1]), k = (int)(p % op.n[2]);
+    const float4* f = face_entry(sa, op, i, j, k);
+    if (!f) return;
+    const float4 v = *f;
+    if constexpr (STAGE < 2)
+        ((float*)sa.s_out)[p] = v.x;
+    else if constexpr (STAGE == 2)
+        ((float*)sa.s_out)[p] = v.y;
+    else
+        st_pair(sa.u0, op.N, p, make_float2(v.z, v.w));
+}
+
 // ---- vectorised mixed stage (3-D grids, nz a multiple of 4) --------------------------------
 // A thread owns four consecutive z points of one x plane, so a warp covers 128 points of one
 // z line and every field moves as float4 (stage input, class bytes as one 32-bit word, the
@@ -903,9 +1057,9 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
 // contribute 0); only warps that hold a cut-cell or wall row along that axis branch.  There,
 // cut-cell rows are found from the chunk's prefix count plus the rank among the chunk's
 // cut-cell points (lanes 8s..8s+7 hold the 32-point chunk s of the warp, four ballots give
-// the rank); z-wall rows, which sit at both ends of every z line, come from the table that
-// k_cut_rows fills; x- and y-wall rows (whole planes / rows, uniform across a warp) are
-// evaluated from global memory.  FORM fixes the interior stencil (5-point antisymmetric,
+// the rank); x- and y-wall rows (whole planes / rows, uniform across a warp) are evaluated
+// from global memory.  z-wall rows sit at both ends of every z line, i.e. in a few lanes of
+// every warp; those lanes read them from the table that k_cut_rows fills, without a vote.  FORM fixes the interior stencil (5-point antisymmetric,
 // 5-point symmetric, 3-point) and VK the velocity field of the wave system (constant or
 // radial), so the per-point code has no run-time branch on either.  The arithmetic of each
 // point is the per-point kernel's, operation for operation.
@@ -940,8 +1094,8 @@ __device__ __forceinline__ float f4(const float4& v, int q)
     return q == 0 ? v.x : (q == 1 ? v.y : (q == 2 ? v.z : v.w));
 }
 
-template <int STAGE, int SYS, int FORM, int VK>
-__global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
+template <int STAGE, int SYS, int FORM, int VK, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
 {
     const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
@@ -976,13 +1130,18 @@ __global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams 
 
     float v[3][4];
     unsigned kq[3][4];
-    bool special = false;
+    bool special = false, zwall = false; // cut-cell or x/y-wall rows; z-wall rows
 #pragma unroll
     for (int q = 0; q < 4; q++) {
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
-            special = special || kq[d][q] >= ROW_CLOSURE;
+            if (d < 2)
+                special = special || kq[d][q] >= ROW_CLOSURE;
+            else {
+                special = special || kq[d][q] == ROW_CLOSURE;
+                zwall = zwall || kq[d][q] == ROW_WALL;
+            }
         }
         const float sx = interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q));
         const float sy = interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q));
@@ -990,6 +1149,13 @@ __global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams 
         v[0][q] = kq[0][q] == ROW_INTERIOR ? sx : 0.f;
         v[1][q] = kq[1][q] == ROW_INTERIOR ? sy : 0.f;
         v[2][q] = kq[2][q] == ROW_INTERIOR ? sz : 0.f;
+    }
+    if (zwall) { // rows at the ends of the z line (a few lanes): from the z-wall table
+        const DevAxis& A = op.ax[2];
+        const float* __restrict__ zrow = sa.zw + (long long)(i * ny + j) * zwall_slots(A);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (kq[2][q] == ROW_WALL) v[2][q] = zrow[zwall_slot(A, k + q)];
     }
     if (__any_sync(FULL, special)) {
         const float* __restrict__ cval = (const float*)sa.cval;
@@ -1002,7 +1168,7 @@ __global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams 
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 has_cut = has_cut || kq[d][q] == ROW_CLOSURE;
-                has_wall = has_wall || kq[d][q] == ROW_WALL;
+                has_wall = has_wall || (d < 2 && kq[d][q] == ROW_WALL);
             }
             if (__any_sync(FULL, has_cut)) {
                 int before = 0;
@@ -1017,19 +1183,11 @@ __global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams 
                         if (kq[d][q] == ROW_CLOSURE) v[d][q] = cval[r++];
                 }
             }
-            if (has_wall) {
-                if (d == 2) { // rows at the ends of the z line: from the z-wall table
-                    const float* __restrict__ zrow =
-                        sa.zw + (long long)(i * ny + j) * zwall_slots(A);
+            if (has_wall) { // whole x / y wall planes: uniform across the warp
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (kq[d][q] == ROW_WALL) v[d][q] = zrow[zwall_slot(A, k + q)];
-                } else { // whole x / y wall planes: uniform across the warp
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (kq[d][q] == ROW_WALL)
-                            v[d][q] = wall32(A, (long long)(p + q), d == 0 ? i : j, in);
-                }
+                for (int q = 0; q < 4; q++)
+                    if (kq[d][q] == ROW_WALL)
+                        v[d][q] = wall32(A, (long long)(p + q), d == 0 ? i : j, in);
             }
         }
     }
@@ -1050,6 +1208,21 @@ __global__ void __launch_bounds__(256, 4) k_stage_mixed_vec(DevOp op, SysParams 
                               : 0.f;
         rk_mixed<STAGE>(sa, rhs, make_float2(f4(uh, q), f4(ul, q)), f4(av, q), ao[q], so[q],
                         uo[q]);
+    }
+    if (c4 & 0x40404040u) { // Dirichlet face points (whole planes, or one lane of a line)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (!((c4 >> (8 * q)) & CLS_DIRFACE)) continue;
+            const float4* f = face_entry(sa, op, i, j, k + q);
+            if (!f) continue;
+            const float4 fv = *f;
+            if constexpr (STAGE < 2)
+                so[q] = fv.x;
+            else if constexpr (STAGE == 2)
+                so[q] = fv.y;
+            else
+                uo[q] = make_float2(fv.z, fv.w);
+        }
     }
     if constexpr (STAGE < 3) {
         *((float4*)((float*)sa.acc + p)) = make_float4(ao[0], ao[1], ao[2], ao[3]);
@@ -1341,45 +1514,15 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
     }
 }
 
-// Dirichlet face values of the stage output (update_boundary on D)
-template <bool MIXED, bool LAST>
-__global__ void k_faces(DevOp op, DevSol sol, double t, double et, void* out)
+// Dirichlet face values of the stage output (update_boundary on D), FP64 path
+__global__ void k_faces64(DevOp op, DevSol sol, double t, double et, double* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= op.n_faces) return;
     const long long p = op.faces[i];
     const long long nyz = (long long)op.n[1] * op.n[2];
     const int ijk[3] = {(int)(p / nyz), (int)((p / op.n[2]) % op.n[1]), (int)(p % op.n[2])};
-    if (MIXED && !LAST && (sol.kind == SOL_GAUSS_PULSE || sol.kind == SOL_RADIAL_SIN)) {
-        // FP32 stage field: the exact value in FP32 arithmetic
-        const float x0 = (float)op.xc[0][ijk[0]], x1 = (float)op.xc[1][ijk[1]],
-                    x2 = (float)op.xc[2][ijk[2]];
-        const float tf = (float)t;
-        float v;
-        if (sol.kind == SOL_GAUSS_PULSE) {
-            const float d0 = (x0 - (float)sol.p[0]) - (float)sol.p[3] * tf;
-            const float d1 = (x1 - (float)sol.p[1]) - (float)sol.p[4] * tf;
-            const float d2 = (x2 - (float)sol.p[2]) - (float)sol.p[5] * tf;
-            const float sg = (float)sol.p[6];
-            v = expf(-(d0 * d0 + d1 * d1 + d2 * d2) / (2.f * sg * sg));
-        } else {
-            const float d0 = x0 - (float)sol.p[0], d1 = x1 - (float)sol.p[1],
-                        d2 = x2 - (float)sol.p[2];
-            v = sinf(6.283185307179586f * (sqrtf(d0 * d0 + d1 * d1 + d2 * d2) -
-                                           (float)sol.p[3] - tf));
-        }
-        ((float*)out)[p] = v;
-        return;
-    }
-    const double v = sol_at_point(op, sol, t, et, ijk);
-    if (MIXED) {
-        if (LAST)
-            st_pair(out, op.N, p, ff_from_double(v));
-        else
-            ((float*)out)[p] = (float)v;
-    } else {
-        ((double*)out)[p] = v;
-    }
+    out[p] = sol_at_point(op, sol, t, et, ijk);
 }
 
 // Dirichlet cut-point values at t+dt/2 and t+dt of all three R arrays (update_boundary on R)
@@ -1388,14 +1531,30 @@ struct BcRArgs {
     double* out1[3];
     double* out2[3];
     const double* keep[3];
+    float4* fplane[6]; // face planes to fill (mixed path), null where not Dirichlet
+    int fn[6];         // points per face plane (0 where not filled)
 };
-__global__ void k_bc_r(DevR dr, DevSol sol, BcRArgs ra, double t1, double et1, double t2,
-                       double et2)
+// threads past the cut points fill the Dirichlet face planes of the mixed path
+__global__ void k_bc_r(DevOp op, DevR dr, DevSol sol, BcRArgs ra, double t1, double et1,
+                       double t2, double et2)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int d = 0;
     while (d < 3 && i >= ra.n[d]) i -= ra.n[d++];
-    if (d == 3) return;
+    if (d == 3) {
+        int f = 0;
+        while (f < 6 && i >= ra.fn[f]) i -= ra.fn[f++];
+        if (f == 6) return;
+        const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        int ijk[3];
+        ijk[a] = (f & 1) ? op.n[a] - 1 : 0;
+        ijk[b] = i / op.n[c];
+        ijk[c] = i - ijk[b] * op.n[c];
+        const float2 u = ff_from_double(sol_at_point(op, sol, t2, et2, ijk));
+        ra.fplane[f][i] = make_float4(face_f32(op, sol, t1, et1, ijk),
+                                      face_f32(op, sol, t2, et2, ijk), u.x, u.y);
+        return;
+    }
     double* out1 = ra.out1[d];
     double* out2 = ra.out2[d];
     const double* keep = ra.keep[d];
@@ -1664,13 +1823,12 @@ namespace
 {
 template <int STAGE, int SYS>
 void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArgs& a,
-                  const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev)
+                  const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev, cudaEvent_t join)
 {
     const dim3 grid = point_grid(op), block(32, BY);
     const bool mixed = prec == PREC_MIXED;
     float* zw = mixed && b.vec ? a.zw : nullptr;
-    const long long n_zw =
-        zw ? (long long)op.it0 * op.it1 * (op.ax[2].wall[0].rows + op.ax[2].wall[1].rows) : 0;
+    const long long n_zw = zw ? (long long)op.it0 * op.it1 : 0; // one thread per z line
     if (op.n_cut_rows || n_zw) {
         const int nb = (int)((op.n_cut_rows + n_zw + 127) / 128);
         const double* const* R = a.R;
@@ -1686,6 +1844,7 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
                                                                R[1], R[2], (float*)a.cval, zw);
         ++g_launches;
     }
+    if (join) cudaStreamWaitEvent(s, join, 0); // boundary values of the step are ready
     if (ev) cudaEventRecord(ev[0], s);
     const bool small = op.N < (1LL << 31) - 64;
     if (mixed && b.tma) {
@@ -1709,16 +1868,23 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
             tm, b.tm_u0t, b.tm_u0l, b.tm_acct, b.tm_cls, op, sp, a, b.err);
     } else if (mixed && b.vec) {
         const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0);
+        // 4 or 3 resident blocks per SM (64 or 85 registers per thread)
+        auto go = [&](auto kern) { kern<<<vgrid, block, 0, s>>>(op, sp, a); };
+        const bool b4 = b.vec_minb == 4;
         if constexpr (SYS == SYS_WAVE) {
             if (sp.vel_kind)
-                k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1><<<vgrid, block, 0, s>>>(op, sp, a);
+                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1, 4>)
+                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1, 3>);
             else
-                k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0, 4>)
+                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0, 3>);
         } else {
             if (b.vec == FORM_SYM5)
-                k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0, 4>)
+                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0, 3>);
             else
-                k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0><<<vgrid, block, 0, s>>>(op, sp, a);
+                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0, 4>)
+                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0, 3>);
         }
     } else if (mixed && b.col_nx) {
         const dim3 cgrid(op.nzc, (op.it1 + BY - 1) / BY, (op.it0 + b.col_nx - 1) / b.col_nx);
@@ -1741,17 +1907,14 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
     }
     ++g_launches;
     if (ev) cudaEventRecord(ev[1], s);
-    if (op.n_faces) {
+    // Dirichlet faces: the vectorised kernel writes them itself
+    if (op.n_faces && !(mixed && b.vec)) {
         const int nb = (op.n_faces + 255) / 256;
-        void* out = STAGE == 3 ? a.u0 : a.s_out;
-        if (mixed) {
-            if (STAGE == 3)
-                k_faces<true, true><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
-            else
-                k_faces<true, false><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
-        } else {
-            k_faces<false, false><<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next, out);
-        }
+        if (mixed)
+            k_faces_mixed<STAGE><<<nb, 256, 0, s>>>(op, a);
+        else
+            k_faces64<<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next,
+                                         (double*)(STAGE == 3 ? a.u0 : a.s_out));
         ++g_launches;
     }
 }
@@ -1760,10 +1923,11 @@ template <int SYS>
 void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[4],
                    const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev)
 {
-    launch_stage<0, SYS>(op, sp, prec, sa[0], b, s, ev ? ev + 2 : nullptr);
-    launch_stage<1, SYS>(op, sp, prec, sa[1], b, s, ev ? ev + 4 : nullptr);
-    launch_stage<2, SYS>(op, sp, prec, sa[2], b, s, ev ? ev + 6 : nullptr);
-    launch_stage<3, SYS>(op, sp, prec, sa[3], b, s, ev ? ev + 8 : nullptr);
+    // the boundary values of the step come from the side stream when there is one
+    launch_stage<0, SYS>(op, sp, prec, sa[0], b, s, ev ? ev + 2 : nullptr, b.side ? b.join : nullptr);
+    launch_stage<1, SYS>(op, sp, prec, sa[1], b, s, ev ? ev + 4 : nullptr, nullptr);
+    launch_stage<2, SYS>(op, sp, prec, sa[2], b, s, ev ? ev + 6 : nullptr, nullptr);
+    launch_stage<3, SYS>(op, sp, prec, sa[3], b, s, ev ? ev + 8 : nullptr, nullptr);
 }
 } // namespace
 
@@ -1771,7 +1935,7 @@ void launch_stages(const DevOp& op, const SysParams& sp, int prec, StageArgs sa[
 // [2+2i], [3+2i] around the main kernel of stage i
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
-                            cudaEvent_t* ev)
+                            cudaEvent_t* ev, bool prefetch_next)
 {
     // src/temporal/rk4.cpp:11-12
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
@@ -1779,22 +1943,61 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
     const bool sinsin = sp.sol.kind == SOL_SINSIN;
     auto et = [&](double tt) { return sinsin ? std::exp(-tt) : 0.0; };
 
-    if (ev) cudaEventRecord(ev[0], s);
-    const double th = t + dt * rki[1], tf = t + dt * rki[3];
-    {
+    // Dirichlet values of the step starting at tt on the cut points (tt+dt/2, tt+dt) and,
+    // in the mixed path, on the domain faces.  keep: the R values at tt (kept where the
+    // cut point is not Dirichlet).
+    auto launch_bc = [&](double tt, double* const keep[3], double* const rh[3],
+                         double* const rf[3], float4* const fp[6], cudaStream_t bs) {
+        const double h = tt + dt * rki[1], f = tt + dt * rki[3];
         BcRArgs ra;
         long long tot = 0;
         for (int d = 0; d < 3; d++) {
             ra.n[d] = (int)op.nR[d];
-            ra.out1[d] = b.Rhalf[d];
-            ra.out2[d] = b.Rfull[d];
-            ra.keep[d] = b.R[d];
+            ra.out1[d] = rh[d];
+            ra.out2[d] = rf[d];
+            ra.keep[d] = keep[d];
             tot += ra.n[d];
         }
+        for (int k = 0; k < 6; k++) {
+            ra.fplane[k] = fp[k];
+            ra.fn[k] = fp[k] ? face_plane_size_host(op, k) : 0;
+            tot += ra.fn[k];
+        }
         if (tot) {
-            k_bc_r<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(dr, sp.sol, ra, th, et(th), tf,
-                                                                 et(tf));
+            k_bc_r<<<(unsigned)((tot + 127) / 128), 128, 0, bs>>>(op, dr, sp.sol, ra, h, et(h),
+                                                                  f, et(f));
             ++g_launches;
+        }
+    };
+
+    if (ev) cudaEventRecord(ev[0], s);
+    if (!b.side) {
+        launch_bc(t, b.R, b.Rhalf, b.Rfull, b.fplane, s);
+    } else {
+        // the side stream starts after everything issued so far on s (the previous step,
+        // the last reader of the buffers it overwrites)
+        cudaEventRecord(b.fork, s);
+        cudaStreamWaitEvent(b.side, b.fork, 0);
+        if (b.next_pending && b.next_t == t && b.next_dt == dt) {
+            // evaluated during the previous step: make that set the current one
+            for (int d = 0; d < 3; d++) {
+                std::swap(b.Rhalf[d], b.Rhalf_next[d]);
+                std::swap(b.Rfull[d], b.Rfull_next[d]);
+            }
+            for (int k = 0; k < 6; k++) std::swap(b.fplane[k], b.fplane_next[k]);
+            std::swap(b.join, b.join_next);
+        } else {
+            launch_bc(t, b.R, b.Rhalf, b.Rfull, b.fplane, b.side);
+            cudaEventRecord(b.join, b.side);
+        }
+        b.next_pending = false;
+        if (prefetch_next) {
+            // the next step starts from this step's R at t + dt (Rfull)
+            launch_bc(t + dt, b.Rfull, b.Rhalf_next, b.Rfull_next, b.fplane_next, b.side);
+            cudaEventRecord(b.join_next, b.side);
+            b.next_pending = true;
+            b.next_t = t + dt;
+            b.next_dt = dt;
         }
     }
     if (ev) cudaEventRecord(ev[1], s);
@@ -1805,6 +2008,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.acc = b.acc;
         a.cval = b.cval;
         a.zw = b.zwall;
+        for (int f = 0; f < 6; f++) a.fplane[f] = b.fplane[f];
         a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
         a.s_out = i == 1 ? b.sb : b.sa;
         for (int d = 0; d < 3; d++)

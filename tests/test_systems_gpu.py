@@ -226,7 +226,7 @@ def test_nonfinite_detected():
     assert not valid
 
 
-STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec")
+STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec", "vec3")
 
 
 @pytest.mark.gpu
