@@ -187,6 +187,54 @@ def run_reference(args, rank, ws):
     return 0
 
 
+MICRO_N = 512
+
+
+def operator_microbench(stream, peak, n=MICRO_N, reps=10):
+    """The operator microbenchmark: 512^3 field u ~ U[-1, 1], 8 seeded non-overlapping
+    spheres; d/dx, d/dy, d/dz (E4_1, Dirichlet spheres) and the Laplacian (E4_2, spheres
+    alternately Dirichlet and Floating), each in FP64 and mixed, through the C ABI.  GB/s
+    counts the algorithmic bytes: read u and write du once per point (16 B FP64, 8 B mixed)."""
+    import torch
+    import shoccs_gb300 as S
+    from shoccs_gb300 import workloads as W
+    out = {"grid": [n, n, n], "spheres": 8, "field_seed": W.SEED_MICRO_FIELD,
+           "sphere_seed": W.SEED_MICRO_SPHERES,
+           "bytes_per_point": {"fp64": 16, "mixed": 8}}
+    for scheme, bcs, ops in (("E4_1", ("dirichlet",), ("dx", "dy", "dz")),
+                             ("E4_2", ("dirichlet", "floating"), ("laplacian",))):
+        p = S.Problem(**W.micro_case(n, scheme, bcs))
+        N = p.size
+        for pname, prec, dtype, B in (("fp64", S.PREC_FP64, torch.float64, 16),
+                                      ("mixed", S.PREC_MIXED, torch.float32, 8)):
+            u = S.ScalarField(W.micro_field(N, dtype),
+                              *[W.micro_field(k, dtype, seed=W.SEED_MICRO_FIELD + 1 + r)
+                                for r, k in enumerate(p.nR)])
+            du = p.zeros(dtype)
+            for op in ops:
+                if op == "laplacian":
+                    f = lambda: S.Laplacian(p, prec)(u, du, stream=stream)
+                else:
+                    d = "xyz".index(op[1])
+                    f = lambda d=d: S.Derivative(p, d, prec)(u, du, stream=stream)
+                for _ in range(2):
+                    f()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                for _ in range(reps):
+                    f()
+                e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                gbs = B * N / (ms / 1000) / 1e9
+                out.setdefault(op, {})[pname] = {"ms": ms, "gbs": gbs, "frac": gbs / peak}
+            del u, du
+        del p
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,6 +245,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time the mixed solves only (used for short profiling runs)")
+    ap.add_argument("--no-micro", action="store_true", help="skip the operator microbenchmark")
+    ap.add_argument("--micro-only", action="store_true",
+                    help="run the operator microbenchmark alone and print its JSON")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -217,6 +268,11 @@ def main():
         if pg:
             pg.barrier()
         torch.cuda.synchronize()
+
+    if args.micro_only:
+        peak, _ = measured_peak()
+        print(json.dumps(operator_microbench(torch.cuda.Stream(), peak)), flush=True)
+        return 0
 
     nsteps = args.rk4_steps
     p = S.Problem(**CASE)
@@ -371,6 +427,9 @@ def main():
         "equal_accuracy": acc,
         "speedup_mixed_vs_fp64": value / value64,
     }
+    if not args.no_micro:
+        del sysm, sysd, p
+        line["operator_microbench"] = operator_microbench(stream, peak)
     if rank == 0 and not args.no_cpu_baseline:
         cb, _, _ = cpu_rate(8, 15.0)
         line["cpu_baseline"] = cb
