@@ -235,6 +235,57 @@ def operator_microbench(stream, peak, n=MICRO_N, reps=10):
     return out
 
 
+def batched_bench(stream, count=256, steps=200):
+    """The batched configuration: 256 independent 2-D heat instances (N ~ U{32..192}, one
+    circle each, manufactured solution with k in {1, 2, 3}), 200 RK4 steps at dt = 0.1 h^2,
+    in FP64 and mixed.  Timed: one run of the batch (a replay of the captured graph) against
+    the same instances advanced one system after another."""
+    import torch
+    import shoccs_gb300 as S
+    from shoccs_gb300 import workloads as W
+    insts = W.batch_heat_2d(count)
+    probs = [S.Problem(**it["case"]) for it in insts]
+    dts = [it["dt"] for it in insts]
+    dof = sum(p.size for p in probs) * steps
+    out = {"instances": count, "rk4_steps": steps, "points": sum(p.size for p in probs),
+           "seed": W.SEED_BATCH}
+    for pname, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+        systems = [S.Heat(p, 1.0, prec, S.SOL_SINSIN, [float(it["k"])])
+                   for p, it in zip(probs, insts)]
+        for s in systems:
+            s.initialize(0.0, stream)
+        batch = S.Batch(systems)
+        batch.rk4(0.0, dts, steps, stream)  # capture + warm-up
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        reps = 3
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            batch.rk4(0.0, dts, steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        # the same instances one system after another (no batching, no graph)
+        for s in systems[:4]:
+            s.rk4(0.0, dts[0], 2, stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s, dt in zip(systems, dts):
+            s.rk4(0.0, dt, steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms_loop = e0.elapsed_time(e1)
+        errs = [s.stats(steps * dt, stream)[0][0] for s, dt in zip(systems[:16], dts[:16])]
+        info = batch.info()
+        out[pname] = {"ms_per_run": ms, "dof_updates_per_s": dof / (ms / 1000.0),
+                      "looped_ms": ms_loop, "looped_dof_updates_per_s": dof / (ms_loop / 1000.0),
+                      "speedup_vs_looped": ms_loop / ms, "max_error_first16": max(errs),
+                      "tile_warps": info["tile_warps"], "graph_nodes": info["graph_nodes"]}
+        del batch, systems
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -248,6 +299,9 @@ def main():
     ap.add_argument("--no-micro", action="store_true", help="skip the operator microbenchmark")
     ap.add_argument("--micro-only", action="store_true",
                     help="run the operator microbenchmark alone and print its JSON")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched heat solves")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run the batched heat solves alone and print their JSON")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -272,6 +326,9 @@ def main():
     if args.micro_only:
         peak, _ = measured_peak()
         print(json.dumps(operator_microbench(torch.cuda.Stream(), peak)), flush=True)
+        return 0
+    if args.batched_only:
+        print(json.dumps(batched_bench(torch.cuda.Stream())), flush=True)
         return 0
 
     nsteps = args.rk4_steps
@@ -427,9 +484,11 @@ def main():
         "equal_accuracy": acc,
         "speedup_mixed_vs_fp64": value / value64,
     }
+    del sysm, sysd, p
     if not args.no_micro:
-        del sysm, sysd, p
         line["operator_microbench"] = operator_microbench(stream, peak)
+    if not args.no_batched:
+        line["batched"] = batched_bench(stream)
     if rank == 0 and not args.no_cpu_baseline:
         cb, _, _ = cpu_rate(8, 15.0)
         line["cpu_baseline"] = cb

@@ -201,6 +201,27 @@ shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double*
  * blocks per SM.  All variants give
  * the same bits.  FP64 systems and 2-D / 1-D grids always use the per-point kernel. */
 shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);
+/* ---- batched heat solves ---------------------------------------------------------------
+ * Many independent heat systems (each with the manufactured sin-sin solution, Dirichlet
+ * objects, one precision for the whole batch) advance together: per RK4 stage one launch
+ * evaluates the cut-cell rows of every instance and one persistent launch updates every
+ * instance, and the whole nsteps-step loop is captured once as a CUDA graph and replayed.
+ * Each instance gets the bits shoccs_system_rk4 would give it alone.  The reference runs
+ * such solves one after another through integrators::rk4 (src/temporal/rk4.cpp:16-47);
+ * the batch itself has no counterpart there. */
+typedef struct shoccs_batch shoccs_batch;
+/* the systems stay owned by the caller and must outlive the batch; creation picks the tile
+ * shape of the stage kernel by timing the candidates on the batch */
+shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_batch** out);
+shoccs_status shoccs_batch_destroy(shoccs_batch* b);
+/* nsteps RK4 steps of instance i from t0[i] with step dt[i]; afterwards each system holds
+ * its state as after shoccs_system_rk4(system_i, t0[i], dt[i], nsteps) */
+shoccs_status shoccs_batch_rk4(shoccs_batch* b, const double* t0, const double* dt, int nsteps,
+                               void* stream);
+/* info[6] = {instances, tiles, cut-cell rows, tile warps (autotuned), persistent grid,
+ *            kernel nodes of the captured graph (0 before the first run)} */
+shoccs_status shoccs_batch_info(const shoccs_batch* b, int64_t info[6]);
+
 /* kernels launched by this library since load (for launch-count accounting) */
 int64_t shoccs_kernel_launches(void);
 

@@ -314,9 +314,40 @@ class ScalarWave(System):
                          center=center, sol_kind=sol_kind, sol=sol, max_error=max_error)
 
 
+class Batch:
+    """Independent heat systems (sin-sin manufactured solution) advanced together: one launch
+    per stage for the whole batch, the RK4 loop captured as a CUDA graph (see
+    shoccs_batch_create in include/shoccs_gpu.h).  The systems must outlive the batch."""
+
+    def __init__(self, systems):
+        self.systems = list(systems)
+        arr = (ctypes.c_void_p * len(self.systems))(*[s.handle.value for s in self.systems])
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().shoccs_batch_create(arr, len(self.systems), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _capi.lib().shoccs_batch_destroy(self._h)
+            self._h = None
+
+    def rk4(self, t0, dt, nsteps, stream=None):
+        n = len(self.systems)
+        t0 = [float(t0)] * n if not hasattr(t0, "__len__") else [float(v) for v in t0]
+        dt = [float(dt)] * n if not hasattr(dt, "__len__") else [float(v) for v in dt]
+        a, b = (ctypes.c_double * n)(*t0), (ctypes.c_double * n)(*dt)
+        _capi.check(_capi.lib().shoccs_batch_rk4(self._h, a, b, int(nsteps), _stream(stream)))
+
+    def info(self):
+        v = (ctypes.c_int64 * 6)()
+        _capi.check(_capi.lib().shoccs_batch_info(self._h, v))
+        return dict(instances=v[0], tiles=v[1], cut_rows=v[2], tile_warps=v[3], grid=v[4],
+                    graph_nodes=v[5])
+
+
 def kernel_launches():
     return int(_capi.lib().shoccs_kernel_launches())
 
 
 __all__ = ["Problem", "Derivative", "Laplacian", "Gradient", "Heat", "ScalarWave", "System",
-           "ScalarField", "ShoccsError", "kernel_launches"]
+           "Batch", "ScalarField", "ShoccsError", "kernel_launches"]

@@ -98,6 +98,11 @@ SIGNATURES = {
                                     ctypes.c_void_p],
     "shoccs_system_timestep": [ctypes.c_void_p, ctypes.c_double, c_double_p],
     "shoccs_system_path": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)],
+    "shoccs_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_void_p)],
+    "shoccs_batch_destroy": [ctypes.c_void_p],
+    "shoccs_batch_rk4": [ctypes.c_void_p, c_double_p, c_double_p, ctypes.c_int, ctypes.c_void_p],
+    "shoccs_batch_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)],
     "shoccs_kernel_launches": [],
     "shoccs_last_error": [ctypes.c_char_p, ctypes.c_size_t],
 }

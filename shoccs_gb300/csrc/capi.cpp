@@ -916,6 +916,269 @@ shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
     return SHOCCS_OK;
 }
 
+} // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// batched heat solves
+// ---------------------------------------------------------------------------------------
+struct shoccs_batch {
+    std::vector<shoccs_system*> sys;
+    int prec = 0;
+    DeviceAlloc mem;
+    std::vector<BatchInst> h_inst;
+    BatchInst* d_inst = nullptr;
+    const int* d_row_inst = nullptr;
+    int n_rows = 0;
+    const int2* d_tiles[4] = {};
+    int n_tiles[4] = {};
+    const int* d_r_inst = nullptr;
+    int n_r = 0;
+    int cfg = 3, grid = 1;
+    BatchTime* d_times = nullptr;
+    long long times_cap = 0; // steps the time table holds
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_steps = 0;
+    int64_t graph_nodes = 0;
+    ~shoccs_batch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cap) cudaStreamDestroy(cap);
+    }
+};
+
+namespace
+{
+constexpr double RKI[4] = {0.0, 0.5, 0.5, 1.0}; // src/temporal/rk4.cpp:11-12
+constexpr double RKF[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+
+shoccs_status batch_set_steps(shoccs_batch* B, const double* t0, const double* dt, int nsteps,
+                              cudaStream_t s)
+{
+    const int n = (int)B->sys.size();
+    // the time points and e^-t of every step, as shoccs_system_rk4 forms them
+    std::vector<BatchTime> h((size_t)nsteps * n);
+    for (int i = 0; i < n; i++) {
+        double t = t0[i];
+        for (int k = 0; k < nsteps; k++) {
+            BatchTime& bt = h[(size_t)k * n + i];
+            bt.t[0] = t + dt[i] * RKI[0];
+            bt.t[1] = t + dt[i] * RKI[1];
+            bt.t[2] = t + dt[i] * RKI[3];
+            for (int m = 0; m < 3; m++) bt.et[m] = std::exp(-bt.t[m]);
+            t += dt[i];
+        }
+        BatchInst& I = B->h_inst[i];
+        for (int st = 0; st < 4; st++) {
+            I.cf[st] = dt[i] * RKF[st];
+            I.ci[st] = st < 3 ? dt[i] * RKI[st + 1] : 1.0;
+            const float ch = (float)I.cf[st], ih = (float)I.ci[st];
+            I.cf_ff[st] = make_float2(ch, (float)(I.cf[st] - (double)ch));
+            I.ci_ff[st] = make_float2(ih, (float)(I.ci[st] - (double)ih));
+        }
+    }
+    if ((long long)nsteps > B->times_cap) {
+        void* p = nullptr;
+        SH_CUDA(B->mem.alloc(h.size() * sizeof(BatchTime), &p));
+        B->d_times = (BatchTime*)p;
+        B->times_cap = nsteps;
+        if (B->exec) { // the captured graph points at the old table
+            cudaGraphExecDestroy(B->exec);
+            B->exec = nullptr;
+            B->graph_steps = 0;
+        }
+    }
+    SH_CUDA(cudaMemcpyAsync(B->d_times, h.data(), h.size() * sizeof(BatchTime),
+                            cudaMemcpyHostToDevice, s));
+    SH_CUDA(cudaMemcpyAsync(B->d_inst, B->h_inst.data(), n * sizeof(BatchInst),
+                            cudaMemcpyHostToDevice, s));
+    return SHOCCS_OK;
+}
+
+// pick the tile shape: time a stage-1 pass of every candidate (stage 1 writes only the
+// accumulator and a stage field, which hold nothing between runs)
+shoccs_status batch_autotune(shoccs_batch* B, cudaStream_t s)
+{
+    const int n = (int)B->sys.size();
+    std::vector<double> t0(n, 0.0), dt(n, 1e-6);
+    if (auto st = batch_set_steps(B, t0.data(), dt.data(), 1, s); st != SHOCCS_OK) return st;
+    if (const char* f = std::getenv("SHOCCS_BATCH_TILE_WARPS")) {
+        for (int c = 0; c < 4; c++)
+            if (std::atoi(f) == BATCH_TILE_WARPS[c]) {
+                B->cfg = c;
+                B->grid = batch_stage_grid(c, B->prec, B->n_tiles[c]);
+                return SHOCCS_OK;
+            }
+        return fail(SHOCCS_EINVAL, "SHOCCS_BATCH_TILE_WARPS must be 1, 2, 4 or 8");
+    }
+    cudaEvent_t e0, e1;
+    SH_CUDA(cudaEventCreate(&e0));
+    SH_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int c = 0; c < 4; c++) {
+        const int grid = batch_stage_grid(c, B->prec, B->n_tiles[c]);
+        SH_CUDA(launch_batch_probe(B->d_inst, B->d_tiles[c], B->n_tiles[c], c, grid,
+                                   B->d_times, B->prec, s));
+        SH_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 5; r++)
+            SH_CUDA(launch_batch_probe(B->d_inst, B->d_tiles[c], B->n_tiles[c], c, grid,
+                                       B->d_times, B->prec, s));
+        SH_CUDA(cudaEventRecord(e1, s));
+        SH_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        SH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            B->cfg = c;
+            B->grid = grid;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return SHOCCS_OK;
+}
+} // namespace
+
+extern "C" {
+
+shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_batch** out)
+{
+    if (!systems || n < 1 || !out) return fail(SHOCCS_EINVAL, "bad argument");
+    *out = nullptr;
+    auto B = std::make_unique<shoccs_batch>();
+    B->prec = systems[0] ? systems[0]->desc.prec : 0;
+    int dev = 0;
+    SH_CUDA(cudaGetDevice(&dev));
+    std::vector<int> row_inst, r_inst;
+    std::vector<int2> tiles[4];
+    for (int i = 0; i < n; i++) {
+        shoccs_system* S = systems[i];
+        if (!S) return fail(SHOCCS_EINVAL, "null system");
+        for (int k = 0; k < i; k++)
+            if (systems[k] == S) return fail(SHOCCS_EINVAL, "a system appears twice in the batch");
+        if (S->desc.kind != SHOCCS_SYS_HEAT || S->desc.sol_kind != SHOCCS_SOL_SINSIN)
+            return fail(SHOCCS_EUNSUPPORTED,
+                        "batched solves take heat systems with the sin-sin manufactured solution");
+        if (S->desc.prec != B->prec) return fail(SHOCCS_EINVAL, "mixed precisions in one batch");
+        if (S->P->device != dev) return fail(SHOCCS_EINVAL, "systems on different devices");
+        const DevOp& op = S->P->op;
+        if (op.N >= (1LL << 31) - 64) return fail(SHOCCS_EUNSUPPORTED, "instance above 2^31 points");
+        B->sys.push_back(S);
+        BatchInst I{};
+        I.op = op;
+        I.sp = S->sp;
+        I.u0 = S->b.u0;
+        I.acc = S->b.acc;
+        I.sa = S->b.sa;
+        I.sb = S->b.sb;
+        I.cval = S->b.cval;
+        for (int d = 0; d < 3; d++) I.R[d] = S->b.R[d];
+        I.row0 = (int)row_inst.size();
+        if ((long long)row_inst.size() + op.n_cut_rows >= (1LL << 31))
+            return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 cut-cell rows");
+        row_inst.insert(row_inst.end(), op.n_cut_rows, i);
+        for (int c = 0; c < 4; c++) {
+            const int w = BATCH_TILE_WARPS[c];
+            const long long nt = (long long)op.nzc * ((op.it1 + w - 1) / w) * op.it0;
+            if ((long long)tiles[c].size() + nt >= (1LL << 31))
+                return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 tiles");
+            for (long long t = 0; t < nt; t++) tiles[c].push_back(make_int2(i, (int)t));
+        }
+        for (int d = 0; d < 3; d++)
+            for (long long k = 0; k < op.nR[d]; k++) {
+                r_inst.push_back(i);
+                r_inst.push_back(d);
+                r_inst.push_back((int)k);
+            }
+        B->h_inst.push_back(I);
+    }
+    const cudaStream_t s = nullptr;
+    void* p = nullptr;
+    SH_CUDA(B->mem.alloc(n * sizeof(BatchInst), &p));
+    B->d_inst = (BatchInst*)p;
+    SH_CUDA(B->mem.put(row_inst, &B->d_row_inst, s));
+    B->n_rows = (int)row_inst.size();
+    for (int c = 0; c < 4; c++) {
+        SH_CUDA(B->mem.put(tiles[c], &B->d_tiles[c], s));
+        B->n_tiles[c] = (int)tiles[c].size();
+    }
+    SH_CUDA(B->mem.put(r_inst, &B->d_r_inst, s));
+    B->n_r = (int)(r_inst.size() / 3);
+    SH_CUDA(cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking));
+    if (auto st = batch_autotune(B.get(), s); st != SHOCCS_OK) return st;
+    SH_CUDA(cudaStreamSynchronize(s));
+    *out = B.release();
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_batch_destroy(shoccs_batch* b)
+{
+    delete b;
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_batch_rk4(shoccs_batch* B, const double* t0, const double* dt, int nsteps,
+                               void* stream)
+{
+    if (!B || !t0 || !dt || nsteps < 0) return fail(SHOCCS_EINVAL, "bad argument");
+    const int n = (int)B->sys.size();
+    for (int i = 0; i < n; i++)
+        if (!(dt[i] > 0)) return fail(SHOCCS_EINVAL, "dt must be > 0");
+    if (nsteps == 0) return SHOCCS_OK;
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = batch_set_steps(B, t0, dt, nsteps, s); st != SHOCCS_OK) return st;
+    if (!B->exec || B->graph_steps != nsteps) {
+        // capture the whole loop once; later runs of the same length replay it (the time
+        // table and the RK4 weights it reads are refreshed above)
+        if (B->exec) {
+            cudaGraphExecDestroy(B->exec);
+            B->exec = nullptr;
+        }
+        SH_CUDA(cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < nsteps && e == cudaSuccess; k++)
+            e = launch_batch_step(B->d_inst, B->d_row_inst, B->n_rows, B->d_tiles[B->cfg],
+                                  B->n_tiles[B->cfg], B->cfg, B->grid,
+                                  B->d_times + (size_t)k * n, B->prec, B->cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(B->cap, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(SHOCCS_ECUDA, std::string("graph capture: ") +
+                                          cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        const cudaError_t e3 = cudaGraphInstantiate(&B->exec, g, 0);
+        cudaGraphDestroy(g);
+        SH_CUDA(e3);
+        B->graph_steps = nsteps;
+        B->graph_nodes = (int64_t)nn;
+    }
+    SH_CUDA(cudaGraphLaunch(B->exec, s));
+    SH_CUDA(launch_batch_finish(B->d_inst, n, B->d_times + (size_t)(nsteps - 1) * n,
+                                B->d_r_inst, B->n_r, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; i++) {
+        double t = t0[i];
+        for (int k = 0; k < nsteps; k++) t += dt[i];
+        B->sys[i]->t = t;
+    }
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_batch_info(const shoccs_batch* B, int64_t info[6])
+{
+    if (!B || !info) return fail(SHOCCS_EINVAL, "null argument");
+    info[0] = (int64_t)B->sys.size();
+    info[1] = B->n_tiles[B->cfg];
+    info[2] = B->n_rows;
+    info[3] = BATCH_TILE_WARPS[B->cfg];
+    info[4] = B->grid;
+    info[5] = B->graph_nodes;
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_timestep(const shoccs_system* S, double cfl, double* dt)
 {
     if (!S || !dt) return fail(SHOCCS_EINVAL, "null argument");

@@ -135,6 +135,46 @@ struct StepBuffers {
 };
 
 // one RK4 step; prefetch_next: also start the next step's (t + dt, same dt) boundary values
+// ---- batched heat solves ------------------------------------------------------------------
+// One instance of a batch: its operator, system parameters and RK4 registers (the
+// instance's own system's buffers), the RK4 weights of its time step, and where its tiles
+// and cut-cell rows start in the batch's flattened lists.
+struct BatchInst {
+    DevOp op;
+    SysParams sp;
+    void* u0;
+    void* acc;
+    void* sa;
+    void* sb;
+    void* cval;
+    double* R[3];
+    double cf[4], ci[4];     // dt*rkf[s], dt*rki[s+1] (ci[3] unused)
+    float2 cf_ff[4], ci_ff[4];
+    int row0;                // first cut-cell row of the instance in the batch's row list
+};
+// the three time points of one RK4 step of one instance (t, t+dt/2, t+dt) and e^-t of each,
+// computed on the host exactly as the single-system path computes them
+struct BatchTime {
+    double t[3];
+    double et[3];
+};
+// tile shapes of the batched stage kernel: warps per block (tile = 32 x warps points)
+constexpr int BATCH_TILE_WARPS[4] = {1, 2, 4, 8};
+// one RK4 step of every instance: per stage, the cut-cell rows of all instances, then the
+// stage update of all instances (persistent blocks over the (instance, tile) list)
+cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
+                              const int2* tiles, int n_tiles, int tile_cfg, int grid,
+                              const BatchTime* times, int prec, cudaStream_t s);
+// one stage-1 pass (timing probe of a tile shape for the autotuner)
+cudaError_t launch_batch_probe(const BatchInst* inst, const int2* tiles, int n_tiles,
+                               int tile_cfg, int grid, const BatchTime* times, int prec,
+                               cudaStream_t s);
+// persistent grid size of the batched stage kernel for a tile shape
+int batch_stage_grid(int tile_cfg, int prec, int n_tiles);
+// state R arrays (Dirichlet cut points) of every instance at the end of a run
+cudaError_t launch_batch_finish(const BatchInst* inst, int n_inst, const BatchTime* last,
+                                const int* r_inst, int n_r, cudaStream_t s);
+
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev = nullptr, bool prefetch_next = false);

@@ -158,11 +158,21 @@ __device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p
 }
 
 // ---- closure rows (always FP64) ----------------------------------------------------------
+// R values of a cut-cell row's boundary term: an array, or -- for a manufactured solution
+// whose value at a cut point is a fixed table entry times e^{-t} -- that product formed on
+// the fly (the batched solves use it; the product is the one the array would hold).
+struct RScaled {
+    const double* tab;
+    double et;
+};
+__device__ __forceinline__ double ldr(const double* R, long long i) { return __ldg(R + i); }
+__device__ __forceinline__ double ldr(const float* R, long long i) { return (double)__ldg(R + i); }
+__device__ __forceinline__ double ldr(const RScaled& R, long long i) { return __ldg(R.tab + i) * R.et; }
 // v = (first ? 0 : acc) + sum_j c_j x_j ; v += b * R[b_idx] ; v += n * nu[n_idx]
 // in the order of derivative::apply_kernels (O, then B, then N).
 template <class TIN, class TR>
 __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long p,
-                                            TIN u, const TR* Rd, const double* nu,
+                                            TIN u, TR Rd, const double* nu,
                                             double acc, bool first)
 {
     const ClosureRow cr = A.rows[row];
@@ -176,7 +186,7 @@ __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long
     double v = first ? s : acc + s;
     int k = cr.ncol;
     if (cr.flags & ROWF_B) {
-        v = fma(__ldg(c + k), ldd(Rd, cr.b_idx), v);
+        v = fma(__ldg(c + k), ldr(Rd, cr.b_idx), v);
         ++k;
     }
     if ((cr.flags & ROWF_N) && nu) v = fma(__ldg(c + k), __ldg(nu + cr.n_idx), v);
@@ -213,9 +223,8 @@ __device__ __forceinline__ void ff_mac(float& sh, float& sl, float2 c, float2 x)
 
 // cut-cell row of the mixed path: sum_j c_j u_j + b R_d[b] (no Neumann term: systems have
 // no Neumann faces or objects)
-template <class TIN>
-__device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long p, TIN u,
-                                            const double* Rd)
+template <class TIN, class TR>
+__device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long p, TIN u, TR Rd)
 {
     const ClosureRow cr = A.rows[row];
     const float2* c = A.coef_ff + cr.coef_off;
@@ -232,7 +241,7 @@ __device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long
     double r = 0.0;
     float2 cb = make_float2(0.f, 0.f);
     if (cr.flags & ROWF_B) {
-        r = __ldg(Rd + cr.b_idx);
+        r = ldr(Rd, cr.b_idx);
         cb = __ldg(c + cr.ncol);
     }
     float sh = 0.f, sl = 0.f;
@@ -659,11 +668,13 @@ __device__ __forceinline__ void radial_g64(const SysParams& sp, const DevOp& op,
     g[2] = -r[2] / len;
 }
 
-// FP64 stage: interior and wall rows in FP64, cut-cell rows from k_cut_rows.
+// FP64 stage: interior and wall rows in FP64, cut-cell rows from k_cut_rows.  The source
+// term is written with explicit rounding so that every kernel that inlines this body (the
+// single-system and the batched stages) rounds it the same way.
 template <int STAGE, int SYS, class IDX>
-__global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
+__device__ __forceinline__ void stage64_at(const DevOp& op, const SysParams& sp,
+                                           const StageArgs& sa, const StagePt<IDX>& q)
 {
-    const StagePt<IDX> q = stage_point<IDX>(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
     const double* __restrict__ in =
         STAGE == 0 ? (const double*)sa.u0 : (const double*)sa.s_in;
@@ -706,7 +717,7 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
                 int ijk[3];
                 stage_ijk(op, q, ijk);
                 const double u = sol_at_point(op, sp.sol, sa.t_stage, sa.et_stage, ijk);
-                src = (-u) - sp.k * (sp.sol.lapfac * u);
+                src = __dsub_rn(-u, __dmul_rn(sp.k, __dmul_rn(sp.sol.lapfac, u)));
             }
             rhs = fma(lap, sp.k, src);
         } else {
@@ -730,6 +741,12 @@ __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageAr
     } else {
         u0[q.p] = u0[q.p] + fma(sa.cf, rhs, acc[q.p]);
     }
+}
+
+template <int STAGE, int SYS, class IDX>
+__global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
+{
+    stage64_at<STAGE, SYS, IDX>(op, sp, sa, stage_point<IDX>(op));
 }
 
 // Right-hand side of one point of the mixed path from its axis values (heat: lap, the sum
@@ -2162,6 +2179,196 @@ cudaError_t launch_stats_noalloc(const DevOp& op, const DevSol& sol, int prec, c
     e = cudaMemcpyAsync(host_out, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(s);
+}
+
+// ===========================================================================================
+// Batched heat solves (the manufactured sin-sin solution): many independent systems of
+// different grids and cut geometries advance together, one launch per kernel kind and
+// stage for the whole batch.  Boundary values are the solution's tables times e^{-t}, formed
+// inline (RScaled, face values) rather than stored, with the same products the single-system
+// path stores; the per-point stage bodies are the single-system ones, so every instance
+// gets the bits it would get alone.
+// ===========================================================================================
+namespace
+{
+template <bool MIXED, int STAGE>
+__global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restrict__ B,
+                                                        const int* __restrict__ row_inst,
+                                                        int n_rows, const BatchTime* __restrict__ bt)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_rows) return;
+    const int ii = row_inst[g];
+    const BatchInst& I = B[ii];
+    const DevOp& op = I.op;
+    const int i = g - I.row0;
+    const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
+    const DevAxis& A = op.ax[d];
+    const int row = i - A.row_base;
+    const long long p = A.row_out[row];
+    const int tp = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // R at t, t+dt/2, t+dt
+    const RScaled R{I.sp.sol.SR[d], bt[ii].et[tp]};
+    const void* in = STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa);
+    if constexpr (MIXED) {
+        if constexpr (STAGE == 0)
+            ((float*)I.cval)[i] = closure_ff(A, row, p, PairU{(const float*)in, op.N}, R);
+        else
+            ((float*)I.cval)[i] = closure_ff(A, row, p, (const float*)in, R);
+    } else {
+        ((double*)I.cval)[i] =
+            closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
+    }
+}
+
+template <int STAGE, bool MIXED, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_batch_stage(const BatchInst* __restrict__ B,
+                                                            const int2* __restrict__ tiles,
+                                                            int n_tiles,
+                                                            const BatchTime* __restrict__ bt)
+{
+    for (int T = blockIdx.x; T < n_tiles; T += gridDim.x) {
+        const int2 tl = tiles[T]; // (instance, tile within the instance)
+        const BatchInst& I = B[tl.x];
+        const DevOp& op = I.op;
+        const int nyb = (op.it1 + WARPS - 1) / WARPS;
+        const int bx = tl.y % op.nzc, rest = tl.y / op.nzc;
+        StagePt<int> q;
+        q.c = bx * 32 + threadIdx.x;
+        q.b = (rest % nyb) * WARPS + threadIdx.y;
+        q.a = rest / nyb;
+        q.valid = (q.b < op.it1) && (q.c < op.it2);
+        const int line = q.a * op.it1 + q.b;
+        q.p = line * op.it2 + q.c;
+        q.chunk = (long long)line * op.nzc + bx;
+        const BatchTime& tm = bt[tl.x];
+        const int ts = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // stage time
+        const int tn = STAGE < 2 ? 1 : 2;                      // time of the stage output
+        StageArgs sa{};
+        sa.u0 = I.u0;
+        sa.acc = I.acc;
+        sa.cval = I.cval;
+        sa.s_in = STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa);
+        sa.s_out = STAGE == 1 ? I.sb : I.sa;
+        sa.cf = I.cf[STAGE];
+        sa.ci = I.ci[STAGE];
+        sa.cf_ff = I.cf_ff[STAGE];
+        sa.ci_ff = I.ci_ff[STAGE];
+        sa.t_stage = tm.t[ts];
+        sa.t_next = tm.t[tn];
+        sa.et_stage = tm.et[ts];
+        sa.et_next = tm.et[tn];
+        sa.etf_stage = (float)tm.et[ts];
+        if constexpr (MIXED)
+            stage_mixed_at<STAGE, SYS_HEAT, int>(op, I.sp, sa, q);
+        else
+            stage64_at<STAGE, SYS_HEAT, int>(op, I.sp, sa, q);
+        // Dirichlet faces: the exact value at the stage output's time
+        if (q.valid && (op.cls[q.p] & CLS_DIRFACE)) {
+            int ijk[3];
+            stage_ijk(op, q, ijk);
+            const double v = sol_at_point(op, I.sp.sol, sa.t_next, sa.et_next, ijk);
+            if constexpr (!MIXED)
+                ((double*)(STAGE == 3 ? sa.u0 : sa.s_out))[q.p] = v;
+            else if constexpr (STAGE < 3)
+                ((float*)sa.s_out)[q.p] = (float)v;
+            else
+                st_pair(sa.u0, op.N, q.p, ff_from_double(v));
+        }
+    }
+}
+
+__global__ void k_batch_finish(const BatchInst* __restrict__ B, const BatchTime* __restrict__ last,
+                               const int* __restrict__ r_inst, int n_r)
+{
+    // r_inst: instance of each cut point of the batch, axis-major within an instance
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_r) return;
+    const int ii = r_inst[3 * g], d = r_inst[3 * g + 1], k = r_inst[3 * g + 2];
+    const BatchInst& I = B[ii];
+    I.R[d][k] = __ldg(I.sp.sol.SR[d] + k) * last[ii].et[2];
+}
+
+template <int STAGE, bool MIXED>
+void batch_stage(const BatchInst* inst, const int2* tiles, int n_tiles, int cfg, int grid,
+                 const BatchTime* times, cudaStream_t s)
+{
+    switch (cfg) {
+    case 0: k_batch_stage<STAGE, MIXED, 1><<<grid, dim3(32, 1), 0, s>>>(inst, tiles, n_tiles, times); break;
+    case 1: k_batch_stage<STAGE, MIXED, 2><<<grid, dim3(32, 2), 0, s>>>(inst, tiles, n_tiles, times); break;
+    case 2: k_batch_stage<STAGE, MIXED, 4><<<grid, dim3(32, 4), 0, s>>>(inst, tiles, n_tiles, times); break;
+    default: k_batch_stage<STAGE, MIXED, 8><<<grid, dim3(32, 8), 0, s>>>(inst, tiles, n_tiles, times); break;
+    }
+    ++g_launches;
+}
+
+template <bool MIXED>
+void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const int2* tiles,
+                int n_tiles, int cfg, int grid, const BatchTime* times, cudaStream_t s)
+{
+    const int nb = (n_rows + 127) / 128;
+    if (n_rows) { k_batch_cut_rows<MIXED, 0><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
+    batch_stage<0, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+    if (n_rows) { k_batch_cut_rows<MIXED, 1><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
+    batch_stage<1, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+    if (n_rows) { k_batch_cut_rows<MIXED, 2><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
+    batch_stage<2, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+    if (n_rows) { k_batch_cut_rows<MIXED, 3><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
+    batch_stage<3, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+}
+} // namespace
+
+cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
+                              const int2* tiles, int n_tiles, int tile_cfg, int grid,
+                              const BatchTime* times, int prec, cudaStream_t s)
+{
+    if (prec == PREC_MIXED)
+        batch_step<true>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, times, s);
+    else
+        batch_step<false>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, times, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_probe(const BatchInst* inst, const int2* tiles, int n_tiles,
+                               int tile_cfg, int grid, const BatchTime* times, int prec,
+                               cudaStream_t s)
+{
+    if (prec == PREC_MIXED)
+        batch_stage<1, true>(inst, tiles, n_tiles, tile_cfg, grid, times, s);
+    else
+        batch_stage<1, false>(inst, tiles, n_tiles, tile_cfg, grid, times, s);
+    return cudaGetLastError();
+}
+
+int batch_stage_grid(int tile_cfg, int prec, int n_tiles)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int warps = BATCH_TILE_WARPS[tile_cfg & 3];
+    const void* fn = nullptr;
+    if (prec == PREC_MIXED) {
+        const void* f[4] = {(const void*)k_batch_stage<1, true, 1>, (const void*)k_batch_stage<1, true, 2>,
+                            (const void*)k_batch_stage<1, true, 4>, (const void*)k_batch_stage<1, true, 8>};
+        fn = f[tile_cfg & 3];
+    } else {
+        const void* f[4] = {(const void*)k_batch_stage<1, false, 1>, (const void*)k_batch_stage<1, false, 2>,
+                            (const void*)k_batch_stage<1, false, 4>, (const void*)k_batch_stage<1, false, 8>};
+        fn = f[tile_cfg & 3];
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * warps, 0);
+    const long long g = (long long)std::max(1, per_sm) * std::max(1, sms);
+    return (int)std::max(1LL, std::min<long long>(g, n_tiles));
+}
+
+cudaError_t launch_batch_finish(const BatchInst* inst, int n_inst, const BatchTime* last,
+                                const int* r_inst, int n_r, cudaStream_t s)
+{
+    (void)n_inst;
+    if (n_r) {
+        k_batch_finish<<<(n_r + 127) / 128, 128, 0, s>>>(inst, last, r_inst, n_r);
+        ++g_launches;
+    }
+    return cudaGetLastError();
 }
 
 } // namespace sgb
