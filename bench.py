@@ -286,6 +286,121 @@ def batched_bench(stream, count=256, steps=200):
     return out
 
 
+def adjoint_bench(stream, n=128, steps=200, every=20, ndir=32, eps=1e-6, cg_iters=10):
+    """The adjoint configuration: 3-D heat 128^3, sphere r = 0.25, homogeneous Dirichlet,
+    u0 = seeded sum of 16 Gaussians, 200 RK4 steps (FP64) with a checkpoint every 20.
+    J(u0) = 1/2 ||u(T) - u_obs||^2 over the fluid points, u_obs = u(T) of the true u0.
+    Reports the forward and backward (gradient) times, central finite differences of J
+    along 32 seeded directions against the adjoint gradient, and an initial-condition
+    inversion by conjugate gradients on the normal equations started from u0 = 0."""
+    import numpy as np
+    import torch
+    import shoccs_gb300 as S
+    from shoccs_gb300 import workloads as W
+    p = S.Problem(**W.adjoint_case(n))
+    sys_ = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_ZERO)
+    dt = W.heat_dt(n)
+    dev = "cuda"
+    R = [torch.zeros(k, dtype=torch.float64, device=dev) for k in p.nR]
+    fluid = torch.tensor((p.classes() & 0x80) != 0, dtype=torch.float64, device=dev)
+    u_true = torch.tensor(W.adjoint_u0(n), dtype=torch.float64, device=dev)
+    out = torch.empty_like(u_true)
+
+    def forward(u0, ckpt=every):
+        sys_.set_state(S.ScalarField(u0, *R), stream)
+        tape = sys_.forward(0.0, dt, steps, ckpt, stream)
+        sys_.get_state(S.ScalarField(out, *R), stream)
+        return tape, out.clone()
+
+    _, u_obs = forward(u_true)
+
+    def loss_grad(u0, grad=True):
+        tape, uT = forward(u0)
+        r = (uT - u_obs) * fluid
+        J = 0.5 * float(torch.dot(r, r))
+        if not grad:
+            return J, None
+        g = torch.empty_like(u0)
+        sys_.backward(tape, S.ScalarField(r, *R), S.ScalarField(g, *R), stream)
+        return J, g
+
+    # timing: forward (with checkpoints) and backward of one gradient
+    u0 = 0.5 * u_true
+    loss_grad(u0)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    tape, uT = forward(u0)
+    e[1].record(stream)
+    r = (uT - u_obs) * fluid
+    g = torch.empty_like(u0)
+    sys_.backward(tape, S.ScalarField(r, *R), S.ScalarField(g, *R), stream)
+    e[2].record(stream)
+    e[2].synchronize()
+    t_fwd, t_bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    # finite differences along seeded random directions
+    J0, g = loss_grad(u0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(W.SEED_ADJOINT_DIRECTIONS)
+    rel = []
+    # directions: seeded random sums of 16 Gaussian bumps (centres U[0.1, 0.9]^3, widths
+    # U[0.03, 0.1], weights N(0, 1)) -- white-noise directions lie almost entirely in modes
+    # that 200 heat steps damp below rounding, where neither the gradient nor a finite
+    # difference carries information
+    xs = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device=dev)
+    X, Y, Z = torch.meshgrid(xs, xs, xs, indexing="ij")
+    X, Y, Z = X.reshape(-1), Y.reshape(-1), Z.reshape(-1)
+
+    def direction():
+        c = 0.1 + 0.8 * torch.rand(16, 3, dtype=torch.float64, device=dev, generator=gen)
+        sg = 0.03 + 0.07 * torch.rand(16, dtype=torch.float64, device=dev, generator=gen)
+        a = torch.randn(16, dtype=torch.float64, device=dev, generator=gen)
+        v = torch.zeros(p.size, dtype=torch.float64, device=dev)
+        for m in range(16):
+            d2 = (X - c[m, 0]) ** 2 + (Y - c[m, 1]) ** 2 + (Z - c[m, 2]) ** 2
+            v += a[m] * torch.exp(-d2 / (2 * sg[m] ** 2))
+        return v / torch.linalg.norm(v)
+
+    for _ in range(ndir):
+        v = direction()
+        # J(u0 + eps v) - J(u0 - eps v) = 1/2 (r+ - r-) . (r+ + r-) exactly; evaluated in
+        # that form the difference keeps its digits (J itself is ~1e3 while the difference is
+        # ~1e-8: subtracting two J values would leave rounding noise)
+        _, up = forward(u0 + eps * v)
+        _, um = forward(u0 - eps * v)
+        rp, rm = (up - u_obs) * fluid, (um - u_obs) * fluid
+        fd = 0.5 * float(torch.dot(rp - rm, rp + rm)) / (2 * eps)
+        gv = float(torch.dot(g, v))
+        rel.append(abs(fd - gv) / max(abs(gv), 1e-300))
+    # inversion: CG on (F^T F) u0 = F^T u_obs from u0 = 0 (F: the linear solve)
+    x = torch.zeros_like(u_true)
+    Jx, gx = loss_grad(x)
+    J_start = Jx
+    rvec = -gx
+    pvec = rvec.clone()
+    for _ in range(cg_iters):
+        # F^T F p = gradient at p of 1/2 ||F p||^2: a solve and an adjoint from the zero
+        # observation, computed as the gradient difference along p
+        _, gp = loss_grad(x + pvec)
+        Ap = gp - gx
+        alpha = float(torch.dot(rvec, rvec)) / float(torch.dot(pvec, Ap))
+        x = x + alpha * pvec
+        r_new = rvec - alpha * Ap
+        beta = float(torch.dot(r_new, r_new)) / float(torch.dot(rvec, rvec))
+        pvec = r_new + beta * pvec
+        rvec = r_new
+        Jx, gx = loss_grad(x)
+    err0 = float(torch.linalg.norm(u_true * fluid))
+    return {"grid": [n, n, n], "rk4_steps": steps, "checkpoint_every": every,
+            "dtype": "f64", "forward_ms": t_fwd, "backward_ms": t_bwd,
+            "backward_over_forward": t_bwd / t_fwd,
+            "fd_check": {"directions": ndir, "eps": eps, "max_rel_error": max(rel),
+                         "median_rel_error": sorted(rel)[len(rel) // 2]},
+            "inversion": {"method": "conjugate gradients on the normal equations",
+                          "iterations": cg_iters, "J_start": J_start, "J_end": Jx,
+                          "u0_rel_error": float(torch.linalg.norm((x - u_true) * fluid)) / err0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,6 +415,9 @@ def main():
     ap.add_argument("--micro-only", action="store_true",
                     help="run the operator microbenchmark alone and print its JSON")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched heat solves")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint configuration")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run the adjoint configuration alone and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
                     help="run the batched heat solves alone and print their JSON")
     args = ap.parse_args()
@@ -323,12 +441,16 @@ def main():
             pg.barrier()
         torch.cuda.synchronize()
 
-    if args.micro_only:
-        peak, _ = measured_peak()
-        print(json.dumps(operator_microbench(torch.cuda.Stream(), peak)), flush=True)
-        return 0
-    if args.batched_only:
-        print(json.dumps(batched_bench(torch.cuda.Stream())), flush=True)
+    if args.micro_only or args.batched_only or args.adjoint_only:
+        st = torch.cuda.Stream()
+        with torch.cuda.stream(st):  # torch arithmetic and library calls on one stream
+            if args.micro_only:
+                peak, _ = measured_peak()
+                print(json.dumps(operator_microbench(st, peak)), flush=True)
+            elif args.batched_only:
+                print(json.dumps(batched_bench(st)), flush=True)
+            else:
+                print(json.dumps(adjoint_bench(st)), flush=True)
         return 0
 
     nsteps = args.rk4_steps
@@ -485,10 +607,14 @@ def main():
         "speedup_mixed_vs_fp64": value / value64,
     }
     del sysm, sysd, p
-    if not args.no_micro:
-        line["operator_microbench"] = operator_microbench(stream, peak)
-    if not args.no_batched:
-        line["batched"] = batched_bench(stream)
+    # the sections below mix torch tensor arithmetic with library calls: both run on `stream`
+    with torch.cuda.stream(stream):
+        if not args.no_micro:
+            line["operator_microbench"] = operator_microbench(stream, peak)
+        if not args.no_batched:
+            line["batched"] = batched_bench(stream)
+        if not args.no_adjoint:
+            line["adjoint"] = adjoint_bench(stream)
     if rank == 0 and not args.no_cpu_baseline:
         cb, _, _ = cpu_rate(8, 15.0)
         line["cpu_baseline"] = cb

@@ -222,6 +222,33 @@ shoccs_status shoccs_batch_rk4(shoccs_batch* b, const double* t0, const double* 
  *            kernel nodes of the captured graph (0 before the first run)} */
 shoccs_status shoccs_batch_info(const shoccs_batch* b, int64_t info[6]);
 
+/* ---- discrete adjoint (FP64 heat systems) ------------------------------------------------
+ * An autograd-shaped pair: shoccs_system_forward advances the system like shoccs_system_rk4
+ * and records a tape (the step size, the step count and a copy of the state every
+ * checkpoint_every steps); shoccs_system_backward maps the gradient of a loss with respect
+ * to the final state to its gradient with respect to the state the forward run started from
+ * (the vector-Jacobian product of the nsteps RK4 steps: the reverse stage sweep with the
+ * transposed operator).  The heat right-hand side is linear in the state, so the reverse
+ * sweep reads no forward state; the checkpoints make the tape self-contained (the states a
+ * caller may want to inspect or restart from) and are not recomputed.  R entries of the
+ * gradients are zero (cut-point values are boundary data, not state).  The reference has no
+ * adjoint; its operators' transposes are what shoccs_system_rhs_transpose applies. */
+typedef struct shoccs_tape shoccs_tape;
+/* y = A^T x with A the linear part of system::rhs (src/systems/heat.cpp:119-162): the
+ * transposed interior sweeps plus the transposed closure rows */
+shoccs_status shoccs_system_rhs_transpose(shoccs_system* s, const shoccs_field* x,
+                                          shoccs_field* y, void* stream);
+shoccs_status shoccs_system_forward(shoccs_system* s, double t0, double dt, int nsteps,
+                                    int checkpoint_every, shoccs_tape** tape, void* stream);
+shoccs_status shoccs_system_backward(shoccs_system* s, const shoccs_tape* tape,
+                                     const shoccs_field* grad_uT, shoccs_field* grad_u0,
+                                     void* stream);
+/* number of checkpoints in the tape and, with state != NULL, a copy of checkpoint i (the D
+ * array, FP64, device pointer) */
+shoccs_status shoccs_tape_checkpoint(const shoccs_tape* tape, int i, double* state,
+                                     int* count, void* stream);
+shoccs_status shoccs_tape_destroy(shoccs_tape* tape);
+
 /* kernels launched by this library since load (for launch-count accounting) */
 int64_t shoccs_kernel_launches(void);
 

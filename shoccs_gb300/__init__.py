@@ -282,6 +282,27 @@ class System:
         _capi.check(_capi.lib().shoccs_system_path(self._h, ctypes.byref(v)))
         return self.STAGE_KERNELS[v.value]
 
+    # --- discrete adjoint (FP64 heat systems) ---
+    def rhs_transpose(self, x, y, stream=None):
+        """y = A^T x, A the linear part of rhs (fields of FP64 CUDA tensors)"""
+        _capi.check(_capi.lib().shoccs_system_rhs_transpose(self._h, _field(x), _field(y),
+                                                            _stream(stream)))
+        return y
+
+    def forward(self, t0, dt, nsteps, checkpoint_every=0, stream=None):
+        """rk4 from the current state, recording a Tape for backward()"""
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().shoccs_system_forward(self._h, float(t0), float(dt),
+                                                      int(nsteps), int(checkpoint_every),
+                                                      ctypes.byref(h), _stream(stream)))
+        return Tape(h)
+
+    def backward(self, tape, grad_uT, grad_u0, stream=None):
+        """grad_u0 = (d u(T) / d u(0))^T grad_uT for the forward run recorded in tape"""
+        _capi.check(_capi.lib().shoccs_system_backward(self._h, tape.handle, _field(grad_uT),
+                                                       _field(grad_u0), _stream(stream)))
+        return grad_u0
+
     def timestep(self, cfl):
         dt = ctypes.c_double()
         _capi.check(_capi.lib().shoccs_system_timestep(self._h, float(cfl), ctypes.byref(dt)))
@@ -294,6 +315,32 @@ def _np_ptr(a):
     if hasattr(a, "data_ptr"):
         return a.data_ptr() if a.numel() else None
     return a.ctypes.data if a.size else None
+
+
+class Tape:
+    """Record of a forward run (step size, step count, checkpoints every k steps)."""
+
+    def __init__(self, h):
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __len__(self):
+        n = ctypes.c_int()
+        _capi.check(_capi.lib().shoccs_tape_checkpoint(self._h, 0, None, ctypes.byref(n), None))
+        return n.value
+
+    def checkpoint(self, i, out):
+        """copy checkpoint i (D array) into the FP64 CUDA tensor out"""
+        _capi.check(_capi.lib().shoccs_tape_checkpoint(self._h, int(i), _ptr(out), None, None))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _capi.lib().shoccs_tape_destroy(self._h)
+            self._h = None
 
 
 class Heat(System):
@@ -349,5 +396,32 @@ def kernel_launches():
     return int(_capi.lib().shoccs_kernel_launches())
 
 
+def rk4_solve(system, u0, t0, dt, nsteps, checkpoint_every=0):
+    """torch.autograd-compatible RK4 solve: u(T) from the D array u0 (FP64 CUDA tensor);
+    backward maps dL/du(T) to dL/du0 through the system's discrete adjoint."""
+    import torch
+
+    class _Solve(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, u):
+            p = system.p
+            R = [torch.zeros(n, dtype=torch.float64, device=u.device) for n in p.nR]
+            system.set_state(ScalarField(u.detach().contiguous(), *R))
+            ctx.tape = system.forward(t0, dt, nsteps, checkpoint_every)
+            out = ScalarField(torch.empty_like(u), *R)
+            system.get_state(out)
+            return out.D
+
+        @staticmethod
+        def backward(ctx, g):
+            p = system.p
+            R = [torch.zeros(n, dtype=torch.float64, device=g.device) for n in p.nR]
+            gu = torch.empty_like(g)
+            system.backward(ctx.tape, ScalarField(g.contiguous(), *R), ScalarField(gu, *R))
+            return gu
+
+    return _Solve.apply(u0)
+
+
 __all__ = ["Problem", "Derivative", "Laplacian", "Gradient", "Heat", "ScalarWave", "System",
-           "Batch", "ScalarField", "ShoccsError", "kernel_launches"]
+           "Batch", "Tape", "rk4_solve", "ScalarField", "ShoccsError", "kernel_launches"]

@@ -103,6 +103,15 @@ SIGNATURES = {
     "shoccs_batch_destroy": [ctypes.c_void_p],
     "shoccs_batch_rk4": [ctypes.c_void_p, c_double_p, c_double_p, ctypes.c_int, ctypes.c_void_p],
     "shoccs_batch_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)],
+    "shoccs_system_rhs_transpose": [ctypes.c_void_p, ctypes.POINTER(Field),
+                                    ctypes.POINTER(Field), ctypes.c_void_p],
+    "shoccs_system_forward": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                              ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p],
+    "shoccs_system_backward": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Field),
+                               ctypes.POINTER(Field), ctypes.c_void_p],
+    "shoccs_tape_checkpoint": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                               ctypes.POINTER(ctypes.c_int), ctypes.c_void_p],
+    "shoccs_tape_destroy": [ctypes.c_void_p],
     "shoccs_kernel_launches": [],
     "shoccs_last_error": [ctypes.c_char_p, ctypes.c_size_t],
 }

@@ -87,6 +87,17 @@ struct shoccs_problem {
     DevR dr{};
 };
 
+// adjoint state of a system, built on first use
+struct AdjointState {
+    bool built = false;
+    DeviceAlloc mem;
+    AdjClosure cl{};
+    double* lam = nullptr; // adjoint of the current state
+    double* acc = nullptr;
+    double* za = nullptr;
+    double* zb = nullptr;
+};
+
 struct shoccs_system {
     shoccs_problem* P;
     shoccs_system_desc desc;
@@ -94,6 +105,7 @@ struct shoccs_system {
     DeviceAlloc mem;
     StepBuffers b{};
     double t = 0.0;
+    AdjointState adj;
     ~shoccs_system()
     {
         if (b.side) cudaStreamDestroy(b.side);
@@ -1176,6 +1188,235 @@ shoccs_status shoccs_batch_info(const shoccs_batch* B, int64_t info[6])
     info[3] = BATCH_TILE_WARPS[B->cfg];
     info[4] = B->grid;
     info[5] = B->graph_nodes;
+    return SHOCCS_OK;
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// discrete adjoint
+// ---------------------------------------------------------------------------------------
+struct shoccs_tape {
+    double t0 = 0.0, dt = 0.0;
+    int nsteps = 0, every = 0;
+    long long n = 0;
+    std::vector<double*> ckpt;
+    DeviceAlloc mem;
+};
+
+namespace
+{
+// transposed closure rows: for each column point of a cut-cell or wall row whose output point
+// evolves (fluid, has a row, not on a Dirichlet face), the (output point, coefficient) pairs
+shoccs_status build_adjoint(shoccs_system* S, cudaStream_t s)
+{
+    AdjointState& A = S->adj;
+    if (A.built) return SHOCCS_OK;
+    const shoccs_problem* P = S->P;
+    const Compiled& C = P->comp;
+    const Mesh& m = P->mesh;
+    const i64 N = m.size();
+    auto evolves = [&](i64 p) {
+        const uint8_t c = C.cls[p];
+        return (c & 0x3F) && !(c & CLS_DIRFACE);
+    };
+    struct Trip {
+        i64 tgt, src;
+        double w;
+    };
+    std::vector<Trip> trip;
+    for (int d = 0; d < 3; d++) {
+        const AxisTables& T = C.ax[d];
+        if (!T.active) continue;
+        const i64 sd = T.stride;
+        for (size_t r = 0; r < T.rows.size(); r++) {
+            const i64 p = T.row_out[r];
+            if (!evolves(p)) continue;
+            const ClosureRow& cr = T.rows[r];
+            for (int j = 0; j < cr.ncol; j++)
+                trip.push_back({p + (i64)(cr.col0 + j) * sd, p, T.coef[cr.coef_off + j]});
+        }
+        const i64 nyz = (i64)m.n[1] * m.n[2];
+        for (i64 p = 0; p < N; p++) {
+            if (((C.cls[p] >> (2 * d)) & 3) != ROW_WALL || !evolves(p)) continue;
+            const int coord = d == 0 ? (int)(p / nyz) : (d == 1 ? (int)((p / m.n[2]) % m.n[1])
+                                                                : (int)(p % m.n[2]));
+            const WallBlock& W = T.wall[coord * 2 < m.n[d] ? 0 : 1];
+            const int r = coord - W.first_row;
+            for (int j = 0; j < W.cols; j++)
+                trip.push_back({p + (i64)(W.col0 - coord + j) * sd, p, W.c[r * 7 + j]});
+        }
+    }
+    std::sort(trip.begin(), trip.end(), [](const Trip& a, const Trip& b) {
+        return a.tgt != b.tgt ? a.tgt < b.tgt : a.src < b.src;
+    });
+    std::vector<long long> tgt, src;
+    std::vector<int> ptr{0};
+    std::vector<double> w;
+    for (size_t e = 0; e < trip.size(); e++) {
+        if (e == 0 || trip[e].tgt != trip[e - 1].tgt) {
+            if (e) ptr.push_back((int)e);
+            tgt.push_back(trip[e].tgt);
+        }
+        src.push_back(trip[e].src);
+        w.push_back(trip[e].w);
+    }
+    if (!trip.empty()) ptr.push_back((int)trip.size());
+    if (trip.size() >= (size_t)INT32_MAX) return fail(SHOCCS_EUNSUPPORTED, "closure too large");
+    SH_CUDA(A.mem.put(tgt, &A.cl.tgt, s));
+    SH_CUDA(A.mem.put(ptr, &A.cl.ptr, s));
+    SH_CUDA(A.mem.put(src, &A.cl.src, s));
+    SH_CUDA(A.mem.put(w, &A.cl.w, s));
+    A.cl.n_tgt = (int)tgt.size();
+    void* q = nullptr;
+    for (double** b : {&A.lam, &A.acc, &A.za, &A.zb}) {
+        SH_CUDA(A.mem.alloc(N * sizeof(double), &q));
+        *b = (double*)q;
+    }
+    A.built = true;
+    return SHOCCS_OK;
+}
+
+shoccs_status adjoint_supported(const shoccs_system* S)
+{
+    if (S->desc.kind != SHOCCS_SYS_HEAT)
+        return fail(SHOCCS_EUNSUPPORTED, "the adjoint is implemented for heat systems");
+    if (S->desc.prec != PREC_FP64)
+        return fail(SHOCCS_EUNSUPPORTED, "the adjoint is implemented for FP64 systems");
+    return SHOCCS_OK;
+}
+} // namespace
+
+extern "C" {
+
+shoccs_status shoccs_system_rhs_transpose(shoccs_system* S, const shoccs_field* x,
+                                          shoccs_field* y, void* stream)
+{
+    if (!S || !x || !y || !x->D || !y->D) return fail(SHOCCS_EINVAL, "null argument");
+    if (auto st = adjoint_supported(S); st != SHOCCS_OK) return st;
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = build_adjoint(S, s); st != SHOCCS_OK) return st;
+    AdjArgs a{};
+    a.z = (const double*)x->D;
+    a.zscale = 1.0;
+    a.out = (double*)y->D;
+    a.k = S->desc.diffusivity;
+    SH_CUDA(launch_adjoint_stage(S->P->op, S->adj.cl, 0, a, s));
+    for (int r = 0; r < 3; r++) {
+        void* yr = r == 0 ? y->Rx : (r == 1 ? y->Ry : y->Rz);
+        if (yr && S->P->mesh.R[r].size())
+            SH_CUDA(cudaMemsetAsync(yr, 0, S->P->mesh.R[r].size() * 8, s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_system_forward(shoccs_system* S, double t0, double dt, int nsteps,
+                                    int checkpoint_every, shoccs_tape** tape, void* stream)
+{
+    if (!S || !tape || nsteps < 0 || !(dt > 0) || checkpoint_every < 0)
+        return fail(SHOCCS_EINVAL, "bad argument");
+    *tape = nullptr;
+    if (auto st = adjoint_supported(S); st != SHOCCS_OK) return st;
+    const cudaStream_t s = (cudaStream_t)stream;
+    auto T = std::make_unique<shoccs_tape>();
+    T->t0 = t0;
+    T->dt = dt;
+    T->nsteps = nsteps;
+    T->every = checkpoint_every;
+    T->n = S->P->mesh.size();
+    auto save = [&]() -> shoccs_status {
+        void* q = nullptr;
+        SH_CUDA(T->mem.alloc(T->n * sizeof(double), &q));
+        SH_CUDA(cudaMemcpyAsync(q, S->b.u0, T->n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        T->ckpt.push_back((double*)q);
+        return SHOCCS_OK;
+    };
+    if (checkpoint_every > 0)
+        if (auto st = save(); st != SHOCCS_OK) return st;
+    double t = t0;
+    int done = 0;
+    while (done < nsteps) {
+        const int k = checkpoint_every > 0 ? std::min(checkpoint_every, nsteps - done)
+                                           : nsteps - done;
+        for (int i = 0; i < k; i++) {
+            SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
+                                    nullptr, i + 1 < k));
+            t += dt;
+        }
+        done += k;
+        if (checkpoint_every > 0)
+            if (auto st = save(); st != SHOCCS_OK) return st;
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    S->t = t;
+    *tape = T.release();
+    return check_wait_flag(S, s);
+}
+
+shoccs_status shoccs_system_backward(shoccs_system* S, const shoccs_tape* T,
+                                     const shoccs_field* g, shoccs_field* out, void* stream)
+{
+    if (!S || !T || !g || !out || !g->D || !out->D) return fail(SHOCCS_EINVAL, "null argument");
+    if (auto st = adjoint_supported(S); st != SHOCCS_OK) return st;
+    if (T->n != S->P->mesh.size()) return fail(SHOCCS_EINVAL, "tape of another system");
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (auto st = build_adjoint(S, s); st != SHOCCS_OK) return st;
+    AdjointState& A = S->adj;
+    const long long N = T->n;
+    constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0}; // src/temporal/rk4.cpp:11-12
+    constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    const double dt = T->dt;
+    // lam = dJ/du(T); its Dirichlet-face entries are dropped (the last stage resets faces)
+    SH_CUDA(cudaMemcpyAsync(A.lam, g->D, N * sizeof(double), cudaMemcpyDefault, s));
+    SH_CUDA(launch_adjoint_mask_faces(S->P->op, A.lam, s));
+    for (int n = T->nsteps - 1; n >= 0; n--) {
+        double* zin = nullptr;
+        for (int st = 4; st >= 1; st--) {
+            AdjArgs a{};
+            a.k = S->desc.diffusivity;
+            a.lam = A.lam;
+            a.acc = A.acc;
+            a.z = st == 4 ? A.lam : zin;
+            a.zscale = st == 4 ? dt * rkf[3] : 1.0;
+            if (st > 1) {
+                a.out = (st % 2 == 0) ? A.za : A.zb;
+                a.bl = dt * rkf[st - 2];
+                a.ay = dt * rki[st - 1];
+            } else {
+                a.out = A.lam; // in place: S = 1 reads lam only at the point it writes
+                a.first_step = n == 0;
+            }
+            SH_CUDA(launch_adjoint_stage(S->P->op, A.cl, st, a, s));
+            zin = a.out;
+        }
+    }
+    SH_CUDA(cudaMemcpyAsync(out->D, A.lam, N * sizeof(double), cudaMemcpyDefault, s));
+    for (int r = 0; r < 3; r++) {
+        void* yr = r == 0 ? out->Rx : (r == 1 ? out->Ry : out->Rz);
+        if (yr && S->P->mesh.R[r].size())
+            SH_CUDA(cudaMemsetAsync(yr, 0, S->P->mesh.R[r].size() * 8, s));
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_tape_checkpoint(const shoccs_tape* T, int i, double* state, int* count,
+                                     void* stream)
+{
+    if (!T) return fail(SHOCCS_EINVAL, "null tape");
+    if (count) *count = (int)T->ckpt.size();
+    if (!state) return SHOCCS_OK;
+    if (i < 0 || i >= (int)T->ckpt.size()) return fail(SHOCCS_EINVAL, "no such checkpoint");
+    const cudaStream_t s = (cudaStream_t)stream;
+    SH_CUDA(cudaMemcpyAsync(state, T->ckpt[i], T->n * sizeof(double), cudaMemcpyDefault, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_tape_destroy(shoccs_tape* T)
+{
+    delete T;
     return SHOCCS_OK;
 }
 

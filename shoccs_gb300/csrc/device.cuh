@@ -175,6 +175,36 @@ int batch_stage_grid(int tile_cfg, int prec, int n_tiles);
 cudaError_t launch_batch_finish(const BatchInst* inst, int n_inst, const BatchTime* last,
                                 const int* r_inst, int n_r, cudaStream_t s);
 
+// ---- discrete adjoint of the heat RK4 path (FP64) -----------------------------------------
+// The heat right-hand side is linear in the state: rhs = A u + (boundary and source terms),
+// A = k (sum over axes of the derivative rows of evolving points -- fluid points with a row
+// that are not on a Dirichlet face).  A^T splits into the transposed interior sweep (a point
+// gathers from the neighbours whose interior rows reference it) and the transposed closure
+// rows (cut-cell and wall rows), a CSR grouped by column built once on the host.
+struct AdjClosure {
+    int n_tgt = 0;
+    const long long* tgt = nullptr; // column points that closure rows reference
+    const int* ptr = nullptr;       // entries of target t: [ptr[t], ptr[t+1])
+    const long long* src = nullptr; // output point of the row
+    const double* w = nullptr;      // coefficient
+};
+// one reverse RK4 stage S (4..1), or mode 0: out = A^T z (the transposed operator alone)
+struct AdjArgs {
+    const double* z;  // stencil input: the stage adjoint z_S (lam for S = 4, scaled by zscale)
+    double zscale;
+    const double* lam; // adjoint of the step's end state
+    double* acc;       // sum of the stage adjoints of the step
+    double* out;       // z_{S-1} (S = 4..2), the step's start adjoint (S = 1), A^T z (mode 0)
+    double bl, ay;     // out = bl * lam + ay * (A^T z) for S = 4..2
+    int first_step;    // S = 1 of the solve's first step: the adjoint of the caller's
+                       // Dirichlet-face values (read by its first stage) is kept
+    double k;          // diffusivity
+};
+cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, const AdjArgs& a,
+                                 cudaStream_t s);
+// zero lam on the Dirichlet-face points
+cudaError_t launch_adjoint_mask_faces(const DevOp& op, double* lam, cudaStream_t s);
+
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev = nullptr, bool prefetch_next = false);

@@ -2371,4 +2371,116 @@ cudaError_t launch_batch_finish(const BatchInst* inst, int n_inst, const BatchTi
     return cudaGetLastError();
 }
 
+// ===========================================================================================
+// Discrete adjoint of the heat RK4 path (FP64).  Forward step (rk4.cpp:16-47):
+//   Y1 = u, k_s = A Y_s, Y_{s+1} = u + dt a_s k_s, u' = u + dt sum_s b_s k_s,
+// with Dirichlet faces reset after every stage.  Reverse step, given lam = adjoint of u':
+//   z4 = dt b4 lam; for S = 4..1: Ybar_S = A^T z_S, z_{S-1} = dt b_{S-1} lam + dt a_{S-1} Ybar_S;
+//   lam <- lam + sum_S Ybar_S,
+// all restricted to the evolving points E; solid points keep their adjoint (their value never
+// changes), Dirichlet-face points get one only from the solve's first stage, which reads the
+// caller's face values.
+// ===========================================================================================
+namespace
+{
+__device__ __forceinline__ bool evolves(unsigned c) { return (c & 0x3Fu) && !(c & CLS_DIRFACE); }
+
+// transposed interior rows at point p (coordinates ijk): sum over axes and offsets of the
+// neighbours i = p - m s whose interior row (an evolving point's) reads p with weight c_m
+__device__ __forceinline__ double interior_t(const DevOp& op, long long p, const int ijk[3],
+                                             const double* __restrict__ z)
+{
+    double y = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const DevAxis& A = op.ax[d];
+        if (!A.active) continue;
+        const int half = A.width / 2;
+        for (int m = -half; m <= half; m++) {
+            const int ci = ijk[d] - m;
+            if (ci < 0 || ci >= A.n) continue;
+            const long long i = p - (long long)m * A.stride;
+            const unsigned c = op.cls[i];
+            if (((c >> (2 * d)) & 3u) != ROW_INTERIOR || (c & CLS_DIRFACE)) continue;
+            y = fma(A.ic[half + m], __ldg(z + i), y); // row i's weight on offset m
+        }
+    }
+    return y;
+}
+
+__global__ void __launch_bounds__(256) k_adj_stage(DevOp op, int S, AdjArgs a)
+{
+    const Pt q = point_of(op);
+    if (!q.valid) return;
+    const unsigned c = op.cls[q.p];
+    int ijk[3];
+    phys_ijk(op, q, ijk);
+    const double y = a.k * (interior_t(op, q.p, ijk, a.z) * a.zscale);
+    const bool e = evolves(c);
+    if (S == 0) {
+        a.out[q.p] = y;
+    } else if (S > 1) {
+        const double acc = S == 4 ? 0.0 : a.acc[q.p];
+        a.acc[q.p] = e ? acc + y : 0.0;
+        a.out[q.p] = e ? fma(a.ay, y, a.bl * a.lam[q.p]) : 0.0;
+    } else {
+        const double l = a.lam[q.p];
+        a.out[q.p] = e ? l + a.acc[q.p] + y
+                       : ((c & CLS_DIRFACE) ? (a.first_step ? y : 0.0) : l);
+    }
+}
+
+// transposed closure rows, added after k_adj_stage: target t gets k sum w z[src]
+__global__ void k_adj_closure(DevOp op, AdjClosure cl, int S, AdjArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cl.n_tgt) return;
+    double y = 0.0;
+    for (int e = cl.ptr[t]; e < cl.ptr[t + 1]; e++) y = fma(cl.w[e], __ldg(a.z + cl.src[e]), y);
+    y = a.k * (y * a.zscale);
+    const long long p = cl.tgt[t];
+    const unsigned c = op.cls[p];
+    if (S == 0) {
+        a.out[p] += y;
+    } else if (S > 1) {
+        if (evolves(c)) {
+            a.acc[p] += y;
+            a.out[p] += a.ay * y;
+        }
+    } else if (evolves(c) || ((c & CLS_DIRFACE) && a.first_step)) {
+        a.out[p] += y;
+    }
+}
+} // namespace
+
+namespace
+{
+__global__ void k_adj_mask_faces(DevOp op, double* lam)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < op.n_faces) lam[op.faces[e]] = 0.0;
+}
+} // namespace
+
+cudaError_t launch_adjoint_mask_faces(const DevOp& op, double* lam, cudaStream_t s)
+{
+    if (op.n_faces) {
+        k_adj_mask_faces<<<(op.n_faces + 255) / 256, 256, 0, s>>>(op, lam);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, const AdjArgs& a,
+                                 cudaStream_t s)
+{
+    k_adj_stage<<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
+    ++g_launches;
+    if (cl.n_tgt) {
+        k_adj_closure<<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
 } // namespace sgb

@@ -102,6 +102,20 @@ def adjoint_gaussians(count=16, seed=SEED_ADJOINT, center=(0.5, 0.5, 0.5), radiu
     return out
 
 
+def adjoint_case(n=128):
+    """3-D heat, sphere (0.5, 0.5, 0.5) r = 0.25, homogeneous Dirichlet walls and sphere."""
+    return dict(n=(n, n, n), lo=(0, 0, 0), hi=(1, 1, 1),
+                spheres=[((0.5, 0.5, 0.5), 0.25, "dirichlet")],
+                grid_bc=("dirichlet",) * 6, scheme="E4_2")
+
+
+def adjoint_u0(n=128):
+    """the sum-of-Gaussians initial field on the n^3 grid (flat, z fastest)"""
+    x = np.linspace(0.0, 1.0, n)
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    return gaussian_sum(X, Y, Z, adjoint_gaussians()).ravel()
+
+
 def gaussian_sum(x, y, z, gs):
     v = 0.0
     for (c, s, a) in gs:
