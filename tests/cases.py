@@ -20,7 +20,14 @@ def random_spheres(n_spheres, seed, lo=0.15, hi=0.85, rmin=0.03, rmax=0.08, gap=
 
 
 def cases():
+    from shoccs_gb300 import workloads as W
     return {
+        # the operator microbenchmark's generator (8 seeded spheres, gap >= 8h) at 96^3:
+        # E4_1 derivative with Dirichlet spheres, E4_2 Laplacian with Dirichlet and Floating
+        "micro_e41_96": W.micro_case(96, "E4_1", (DIR,)),
+        "micro_e42_96": W.micro_case(96, "E4_2", (DIR, FLT)),
+        # the adjoint configuration's geometry at 24^3
+        "adjoint_24": W.adjoint_case(24),
         # configuration 0 of the benchmark: 2-D heat, circle, E4_2, Dirichlet walls
         "c0_circle_2d": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
                              spheres=[((0.51, 0.49, 0.0), 0.2, DIR)],
