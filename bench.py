@@ -75,6 +75,36 @@ def dist_env():
     return ws, rank, local
 
 
+# ---- replicas: every rank runs its own solves; no collective touches the data path ----
+def reduce_max(x, pg=None, device="cuda"):
+    """the maximum of x over the ranks (x itself without a process group)"""
+    if pg is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x, pg=None, device="cuda"):
+    if pg is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_rate(local_units, local_seconds, pg=None, device="cuda"):
+    """whole-job rate: the units all ranks processed over the slowest rank's time"""
+    return reduce_sum(local_units, pg, device) / reduce_max(local_seconds, pg, device)
+
+
+def partition(count, rank, world):
+    """the instances a rank owns when independent instances are spread over ranks"""
+    return list(range(rank, count, world))
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -235,7 +265,7 @@ def operator_microbench(stream, peak, n=MICRO_N, reps=10):
     return out
 
 
-def batched_bench(stream, count=256, steps=200):
+def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1):
     """The batched configuration: 256 independent 2-D heat instances (N ~ U{32..192}, one
     circle each, manufactured solution with k in {1, 2, 3}), 200 RK4 steps at dt = 0.1 h^2,
     in FP64 and mixed.  Timed: one run of the batch (a replay of the captured graph) against
@@ -243,7 +273,8 @@ def batched_bench(stream, count=256, steps=200):
     import torch
     import shoccs_gb300 as S
     from shoccs_gb300 import workloads as W
-    insts = W.batch_heat_2d(count)
+    # over several GPUs the instances are partitioned by rank (no collective on the data)
+    insts = [W.batch_heat_2d(count)[i] for i in partition(count, rank, world)]
     probs = [S.Problem(**it["case"]) for it in insts]
     dts = [it["dt"] for it in insts]
     dof = sum(p.size for p in probs) * steps
@@ -265,7 +296,7 @@ def batched_bench(stream, count=256, steps=200):
             batch.rk4(0.0, dts, steps, stream)
         e1.record(stream)
         e1.synchronize()
-        ms = e0.elapsed_time(e1) / reps
+        ms = reduce_max(e0.elapsed_time(e1) / reps, pg)
         # the same instances one system after another (no batching, no graph)
         for s in systems[:4]:
             s.rk4(0.0, dts[0], 2, stream)
@@ -275,11 +306,12 @@ def batched_bench(stream, count=256, steps=200):
             s.rk4(0.0, dt, steps, stream)
         e1.record(stream)
         e1.synchronize()
-        ms_loop = e0.elapsed_time(e1)
+        ms_loop = reduce_max(e0.elapsed_time(e1), pg)
         errs = [s.stats(steps * dt, stream)[0][0] for s, dt in zip(systems[:16], dts[:16])]
         info = batch.info()
-        out[pname] = {"ms_per_run": ms, "dof_updates_per_s": dof / (ms / 1000.0),
-                      "looped_ms": ms_loop, "looped_dof_updates_per_s": dof / (ms_loop / 1000.0),
+        dof_all = reduce_sum(dof, pg)
+        out[pname] = {"ms_per_run": ms, "dof_updates_per_s": dof_all / (ms / 1000.0),
+                      "looped_ms": ms_loop, "looped_dof_updates_per_s": dof_all / (ms_loop / 1000.0),
                       "speedup_vs_looped": ms_loop / ms, "max_error_first16": max(errs),
                       "tile_warps": info["tile_warps"], "graph_nodes": info["graph_nodes"]}
         del batch, systems
@@ -558,7 +590,7 @@ def main():
         sysm.rk4(0.0, dt, nsteps, stream)
         sysm.get_state(S.ScalarField(*host_out), stream)
     barrier()
-    te2e = time.perf_counter() - t0
+    te2e = reduce_max(time.perf_counter() - t0, pg)
 
     value = N * nsteps * args.steps * ws / (t_ms / 1000.0)
     value64 = N * nsteps * n64 / (t64_ms / 1000.0)
@@ -612,7 +644,7 @@ def main():
         if not args.no_micro:
             line["operator_microbench"] = operator_microbench(stream, peak)
         if not args.no_batched:
-            line["batched"] = batched_bench(stream)
+            line["batched"] = batched_bench(stream, pg=pg, rank=rank, world=ws)
         if not args.no_adjoint:
             line["adjoint"] = adjoint_bench(stream)
     if rank == 0 and not args.no_cpu_baseline:
