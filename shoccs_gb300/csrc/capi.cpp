@@ -480,7 +480,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         const bool wave = S->desc.kind == SHOCCS_SYS_WAVE;
         if (wave ? form != FORM_ANTI5 : (form != FORM_SYM5 && form != FORM_W3)) form = FORM_ANY;
     }
-    if (S->P->comp.it[2] % 4 == 0 && S->b.zwall && form != FORM_ANY) {
+    if (S->P->comp.it[2] % 4 == 0 && S->b.rowv && S->b.zwall && form != FORM_ANY) {
         cands.push_back({"vec", 0, 0, form, 4});
         cands.push_back({"vec3", 0, 0, form, 3});
     }
@@ -690,12 +690,15 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         // the trial steps of the autotuner need every register allocated and zeroed; the
         // column and vectorised kernels index with 32-bit integers
         if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
-            const WallBlock* W = p->op.ax[2].wall;
-            const long long nzw = (long long)it[0] * it[1] * (W[0].rows + W[1].rows);
-            if (it[2] % 4 == 0 && nzw + p->op.n_cut_rows < (1LL << 31) - 256) {
-                const size_t n = (size_t)nzw;
+            // the cut-row kernel runs one thread per cut-cell row and per z line
+            const long long nthreads = (long long)it[0] * it[1] + p->op.n_cut_rows;
+            if (it[2] % 4 == 0 && nthreads < (1LL << 31) - 256) {
                 void* z = nullptr;
-                SH_CUDA(S->mem.alloc(std::max<size_t>(n, 1) * sizeof(float), &z));
+                SH_CUDA(S->mem.alloc((size_t)3 * N * sizeof(float), &z));
+                S->b.rowv = (float*)z;
+                const WallBlock* W = p->op.ax[2].wall;
+                const size_t nzw = (size_t)it[0] * it[1] * (W[0].rows + W[1].rows);
+                SH_CUDA(S->mem.alloc(std::max<size_t>(nzw, 1) * sizeof(float), &z));
                 S->b.zwall = (float*)z;
             }
             if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;

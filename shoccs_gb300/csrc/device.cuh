@@ -106,10 +106,12 @@ struct StepBuffers {
     int tma = 0;
     // column-blocked mixed stages (3-D grids): planes per thread, 0 = per-point kernel
     int col_nx = 0;
-    // vectorised mixed stages (3-D grids, nz a multiple of 4) and their table of z-wall row
-    // values (wall[0].rows + wall[1].rows per z line)
+    // vectorised mixed stages (3-D grids, nz a multiple of 4): the cut-cell row values they
+    // read, at their points (3 x N floats, axis-major), and the z-wall row values
+    // (wall[0].rows + wall[1].rows slots x z lines, slot-major)
     int vec = 0;      // stencil form (FORM_*) of the vectorised kernel, 0 = not used
     int vec_minb = 4; // its resident blocks per SM (4: 64 registers, 3: 85 registers)
+    float* rowv = nullptr;
     float* zwall = nullptr;
     unsigned* err = nullptr;
     // exact values on the Dirichlet domain faces (mixed path): per face (x lo, x hi, y lo,

@@ -508,7 +508,9 @@ struct StageArgs {
     void* acc;
     void* s_out;
     const void* cval;
-    float* zw;              // z-wall row values of the stage (vectorised mixed stages), or null
+    float* rowv;            // vectorised mixed stages: cut-cell row values of the stage at
+                            // their points, axis-major (3 x N), or null
+    float* zw;              // and the z-wall row values, slot-major (slot x z lines)
     const float4* fplane[6]; // Dirichlet face values of the step (mixed path), see StepBuffers
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
@@ -520,34 +522,35 @@ struct StageArgs {
 
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 
-// z-wall rows: slot of the table row of z coordinate k (the left block's rows, then the
-// right block's) and the number of slots per z line
-__device__ __forceinline__ int zwall_slots(const DevAxis& A) { return A.wall[0].rows + A.wall[1].rows; }
+// z-wall rows: slot of the row of z coordinate k (the left block's rows, then the right
+// block's) in the slot-major table of the vectorised stage
 __device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
 {
     return k * 2 < A.n ? k - A.wall[0].first_row : A.wall[0].rows + (k - A.wall[1].first_row);
 }
 
 // cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b] (FP64 path: FP64; mixed path:
-// compensated FP32, closure_ff); with zw, threads past
-// the cut-cell rows also evaluate the domain-wall rows of the z axis (FP32, wall32) into a
-// table of zwall_slots() values per z line, which the vectorised mixed stage reads: those
-// rows sit at both ends of every z line, so every warp of that kernel holds some.
+// compensated FP32, closure_ff), stored compacted in row order (cval) or -- for the
+// vectorised mixed stage -- scattered to their points in rowv (3 x N, axis-major), where a
+// lane finds its value with one load at its own index.  With rowv, threads past the cut-cell
+// rows also evaluate the domain-wall rows of the z axis (FP32, wall32's arithmetic) into the
+// slot-major table zw (consecutive lines at consecutive addresses): those rows sit at both
+// ends of every z line, i.e. in some lane of every warp of that kernel.  One thread per z
+// line reads the line's end values once for both wall blocks.
 template <class TIN, class TOUT>
 __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
                            const double* R1, const double* R2, TOUT* __restrict__ cval,
-                           float* __restrict__ zw)
+                           float* __restrict__ rowv, float* __restrict__ zw)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= op.n_cut_rows) {
         if constexpr (!std::is_same<TIN, const double*>::value) {
-            // one thread per z line: both wall blocks from the line's end values (slots of
-            // lines whose ends are not wall rows are written too and never read)
             const int line = i - op.n_cut_rows;
-            if (!zw || line >= op.it0 * op.it1) return;
+            const int nlines = op.it0 * op.it1;
+            if (!zw || line >= nlines) return;
             const DevAxis& A = op.ax[2];
-            float* __restrict__ out = zw + (long long)line * zwall_slots(A);
             const long long base = (long long)line * op.it2;
+            float* __restrict__ out = zw + line;
             int slot = 0;
 #pragma unroll
             for (int side = 0; side < 2; side++) {
@@ -561,7 +564,7 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
 #pragma unroll
                     for (int jj = 0; jj < 7; jj++)
                         if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
-                    out[slot] = acc;
+                    out[(long long)slot * nlines] = acc; // read only where the row is a wall row
                 }
             }
         }
@@ -572,10 +575,15 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
     const DevAxis& A = op.ax[d];
     const int row = i - A.row_base;
     const long long p = A.row_out[row];
-    if constexpr (std::is_same<TOUT, double>::value)
+    if constexpr (std::is_same<TOUT, double>::value) {
         cval[i] = closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
-    else
-        cval[i] = closure_ff(A, row, p, u, R[d]);
+    } else {
+        const float v = closure_ff(A, row, p, u, R[d]);
+        if (rowv)
+            rowv[d * op.N + p] = v;
+        else
+            cval[i] = v;
+    }
 }
 
 
@@ -1147,18 +1155,17 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
 
     float v[3][4];
     unsigned kq[3][4];
-    bool special = false, zwall = false; // cut-cell or x/y-wall rows; z-wall rows
+    bool cut = false, zwall = false, xywall = false; // cut-cell rows; z-wall rows; x/y walls
 #pragma unroll
     for (int q = 0; q < 4; q++) {
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
-            if (d < 2)
-                special = special || kq[d][q] >= ROW_CLOSURE;
-            else {
-                special = special || kq[d][q] == ROW_CLOSURE;
+            cut = cut || kq[d][q] == ROW_CLOSURE;
+            if (d == 2)
                 zwall = zwall || kq[d][q] == ROW_WALL;
-            }
+            else
+                xywall = xywall || kq[d][q] == ROW_WALL;
         }
         const float sx = interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q));
         const float sy = interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q));
@@ -1167,46 +1174,29 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
         v[1][q] = kq[1][q] == ROW_INTERIOR ? sy : 0.f;
         v[2][q] = kq[2][q] == ROW_INTERIOR ? sz : 0.f;
     }
-    if (zwall) { // rows at the ends of the z line (a few lanes): from the z-wall table
-        const DevAxis& A = op.ax[2];
-        const float* __restrict__ zrow = sa.zw + (long long)(i * ny + j) * zwall_slots(A);
+    if (cut) { // cut-cell rows: one load each, at the point's own index
+        const float* __restrict__ rv = sa.rowv + p;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (kq[d][q] == ROW_CLOSURE) v[d][q] = rv[d * op.N + q];
+    }
+    if (zwall) { // z-wall rows (lanes at the ends of a line): the lane's slots are consecutive
+        const long long nlines = (long long)nx * ny;
+        const float* __restrict__ zt =
+            sa.zw + (long long)zwall_slot(op.ax[2], k) * nlines + (i * ny + j);
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if (kq[2][q] == ROW_WALL) v[2][q] = zrow[zwall_slot(A, k + q)];
+            if (kq[2][q] == ROW_WALL) v[2][q] = zt[q * nlines];
     }
-    if (__any_sync(FULL, special)) {
-        const float* __restrict__ cval = (const float*)sa.cval;
-        const int sub = lane >> 3; // 32-point chunk of the warp holding this lane's points
-        const unsigned chunk_before = lanemask_lt() & (0xFFu << (8 * sub));
+    if (__any_sync(FULL, xywall)) { // whole x / y wall planes: uniform across the warp
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-            const DevAxis& A = op.ax[d];
-            bool has_cut = false, has_wall = false;
+        for (int d = 0; d < 2; d++)
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                has_cut = has_cut || kq[d][q] == ROW_CLOSURE;
-                has_wall = has_wall || (d < 2 && kq[d][q] == ROW_WALL);
-            }
-            if (__any_sync(FULL, has_cut)) {
-                int before = 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    before += __popc(__ballot_sync(FULL, kq[d][q] == ROW_CLOSURE) & chunk_before);
-                if (has_cut) {
-                    int r = A.row_base + before +
-                            A.chunk_base[((long long)i * ny + j) * op.nzc + blockIdx.x * 4 + sub];
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (kq[d][q] == ROW_CLOSURE) v[d][q] = cval[r++];
-                }
-            }
-            if (has_wall) { // whole x / y wall planes: uniform across the warp
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (kq[d][q] == ROW_WALL)
-                        v[d][q] = wall32(A, (long long)(p + q), d == 0 ? i : j, in);
-            }
-        }
+            for (int q = 0; q < 4; q++)
+                if (kq[d][q] == ROW_WALL)
+                    v[d][q] = wall32(op.ax[d], (long long)(p + q), d == 0 ? i : j, in);
     }
     if (!kvalid) return;
     float ao[4], so[4];
@@ -1844,6 +1834,7 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
 {
     const dim3 grid = point_grid(op), block(32, BY);
     const bool mixed = prec == PREC_MIXED;
+    float* rowv = mixed && b.vec ? a.rowv : nullptr;
     float* zw = mixed && b.vec ? a.zw : nullptr;
     const long long n_zw = zw ? (long long)op.it0 * op.it1 : 0; // one thread per z line
     if (op.n_cut_rows || n_zw) {
@@ -1852,13 +1843,15 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         if (!mixed)
             k_cut_rows<const double*, double><<<nb, 128, 0, s>>>(
                 op, (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
-                (double*)a.cval, nullptr);
+                (double*)a.cval, nullptr, nullptr);
         else if (STAGE == 0)
             k_cut_rows<PairU, float><<<nb, 128, 0, s>>>(op, PairU{(const float*)a.u0, op.N},
-                                                        R[0], R[1], R[2], (float*)a.cval, zw);
+                                                        R[0], R[1], R[2], (float*)a.cval, rowv,
+                                                        zw);
         else
             k_cut_rows<const float*, float><<<nb, 128, 0, s>>>(op, (const float*)a.s_in, R[0],
-                                                               R[1], R[2], (float*)a.cval, zw);
+                                                               R[1], R[2], (float*)a.cval, rowv,
+                                                               zw);
         ++g_launches;
     }
     if (join) cudaStreamWaitEvent(s, join, 0); // boundary values of the step are ready
@@ -2024,6 +2017,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.u0 = b.u0;
         a.acc = b.acc;
         a.cval = b.cval;
+        a.rowv = b.rowv;
         a.zw = b.zwall;
         for (int f = 0; f < 6; f++) a.fplane[f] = b.fplane[f];
         a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
