@@ -248,6 +248,38 @@ bool make_plane_map(CUtensorMap* m, void* base, int esz, const int it[3], bool h
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+// scratch of the vectorised FP32 operators, allocated on the first mixed-precision apply of
+// a 3-D grid whose z extent is a multiple of 4 and whose axes share one interior stencil
+shoccs_status ensure_op_scratch(shoccs_problem* p)
+{
+    DevOp& op = p->op;
+    if (op.op_rowv || op.op_form == -1) return SHOCCS_OK;
+    const int* it = p->comp.it;
+    auto f = [](const DevAxis& A) {
+        return A.width == 5 ? (A.antisym ? FORM_ANTI5 : FORM_SYM5)
+                            : (A.width == 3 && !A.antisym ? FORM_W3 : FORM_ANY);
+    };
+    int form = f(op.ax[0]);
+    for (int d = 1; d < 3; d++)
+        if (f(op.ax[d]) != form) form = FORM_ANY;
+    const bool ok = it[0] > 1 && it[1] > 1 && it[2] > 1 && it[2] % 4 == 0 && form != FORM_ANY &&
+                    op.N < (1LL << 31) - 64 &&
+                    (long long)op.n_cut_rows + (long long)it[0] * it[1] < (1LL << 31) - 256;
+    if (!ok) {
+        op.op_form = -1; // not applicable: the per-point kernels serve this problem
+        return SHOCCS_OK;
+    }
+    void* r = nullptr;
+    SH_CUDA(p->mem.alloc((size_t)3 * op.N * sizeof(float), &r));
+    const WallBlock* W = op.ax[2].wall;
+    const size_t nzw = (size_t)it[0] * it[1] * (W[0].rows + W[1].rows);
+    void* z = nullptr;
+    SH_CUDA(p->mem.alloc(std::max<size_t>(nzw, 1) * sizeof(float), &z));
+    op.op_rowv = (float*)r;
+    op.op_zw = (float*)z;
+    op.op_form = form;
+    return SHOCCS_OK;
+}
 } // namespace
 
 extern "C" {
@@ -406,10 +438,10 @@ shoccs_status shoccs_derivative_apply(shoccs_problem* p, int dir, int prec,
 {
     if (!p || !u || !du || dir < 0 || dir > 2 || (prec != 0 && prec != 1))
         return fail(SHOCCS_EINVAL, "bad argument");
-    if (nu && prec != PREC_FP64)
-        return fail(SHOCCS_EUNSUPPORTED, "Neumann data is FP64-only");
     const cudaStream_t s = (cudaStream_t)stream;
     if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    if (prec == PREC_MIXED)
+        if (auto st = ensure_op_scratch(p); st != SHOCCS_OK) return st;
     const void* uR[3] = {u->Rx, u->Ry, u->Rz};
     void* duR[3] = {du->Rx, du->Ry, du->Rz};
     SH_CUDA(launch_derivative(p->op, dir, prec, u->D, uR[dir], nu ? (const double*)nu->D : nullptr,
@@ -422,10 +454,10 @@ shoccs_status shoccs_laplacian_apply(shoccs_problem* p, int prec, const shoccs_f
                                      const shoccs_field* nu, shoccs_field* du, void* stream)
 {
     if (!p || !u || !du || (prec != 0 && prec != 1)) return fail(SHOCCS_EINVAL, "bad argument");
-    if (nu && prec != PREC_FP64)
-        return fail(SHOCCS_EUNSUPPORTED, "Neumann data is FP64-only");
     const cudaStream_t s = (cudaStream_t)stream;
     if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    if (prec == PREC_MIXED)
+        if (auto st = ensure_op_scratch(p); st != SHOCCS_OK) return st;
     const void* uR[3] = {u->Rx, u->Ry, u->Rz};
     void* duR[3] = {du->Rx, du->Ry, du->Rz};
     SH_CUDA(launch_laplacian(p->op, prec, u->D, uR, nu ? (const double*)nu->D : nullptr, du->D,
@@ -442,6 +474,8 @@ shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_fi
         return fail(SHOCCS_EINVAL, "bad argument");
     const cudaStream_t s = (cudaStream_t)stream;
     if (auto st = do_upload(p, s); st != SHOCCS_OK) return st;
+    if (prec == PREC_MIXED)
+        if (auto st = ensure_op_scratch(p); st != SHOCCS_OK) return st;
     const void* uR[3] = {u->Rx, u->Ry, u->Rz};
     void* const out[3][4] = {{dx->D, dx->Rx, dx->Ry, dx->Rz},
                              {dy->D, dy->Rx, dy->Ry, dy->Rz},

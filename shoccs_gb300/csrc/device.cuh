@@ -48,6 +48,13 @@ struct DevOp {
     const long long* faces;
     int n_cut_rows;      // cut-cell rows of all axes
     DevAxis ax[3];
+    // scratch of the vectorised FP32 operators (3-D grids, nz a multiple of 4): cut-cell row
+    // values at their points (3 x N floats, axis-major) and z-wall row values (slot-major);
+    // allocated on the first mixed-precision apply, null before
+    float* op_rowv = nullptr;
+    float* op_zw = nullptr;
+    int op_form = 0; // FORM_* of the interior rows; 0 before the first mixed apply, -1 when
+                     // the vectorised operators do not apply to this grid
 };
 
 // closed-form exact / manufactured solution evaluated on the device

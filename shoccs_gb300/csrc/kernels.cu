@@ -293,6 +293,17 @@ __device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord
     return s;
 }
 
+// the Neumann term of a wall row (FP64 data, FP64 product) added to an FP32 row value
+__device__ __forceinline__ float wall_neumann32(const DevAxis& A, long long p, int coord,
+                                                const double* nu, float v)
+{
+    const WallBlock& W = A.wall[wall_side(A, coord)];
+    if (!W.has_n || !nu) return v;
+    const double t = fma(W.n[coord - W.first_row],
+                         __ldg(nu + p + (long long)(W.wall - coord) * A.stride), (double)v);
+    return (float)t;
+}
+
 // ---- closed-form solutions -------------------------------------------------------------
 enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3 };
 
@@ -387,7 +398,8 @@ __device__ __forceinline__ T op_row(const DevAxis& A, unsigned kind, int row, lo
             return first ? v : acc + v;
         }
         if (kind == ROW_WALL) {
-            const float v = wall32(A, p, coord, (const float*)u);
+            float v = wall32(A, p, coord, (const float*)u);
+            v = wall_neumann32(A, p, coord, nu, v);
             return first ? v : acc + v;
         }
         return (float)closure64(A, row, p, (const float*)u, (const float*)Rd, nu, (double)acc,
@@ -1743,6 +1755,222 @@ long long kernel_launch_count() { return g_launches.load(); }
 // ===========================================================================================
 // launchers
 // ===========================================================================================
+// ---- vectorised FP32 operators (3-D grids, nz a multiple of 4) -----------------------------
+// The layout of k_stage_mixed_vec: four z points per thread, float4 loads of the field at
+// the points and their stencil neighbours, interior rows from registers kept where the class
+// says "interior".  Cut-cell rows (FP64 arithmetic as op_row, Neumann-aware) and the z-wall
+// rows are evaluated first by k_op_rows into the problem's scratch, at the points / in a
+// slot-major table; x- and y-wall rows (whole planes, uniform across a warp) inline.
+// MODE 0..2: derivative along x, y, z (eq or, PLUS, plus_eq: only points with a row are
+// written); 3: Laplacian (every point, 0 where no axis has a row); 4: gradient (three
+// outputs, 0 where the axis has no row).
+namespace
+{
+__global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
+                          const float* R0, const float* R1, const float* R2,
+                          const double* __restrict__ nu)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r0 = op.ax[d0].row_base, r1 = d1 < 3 ? op.ax[d1].row_base : op.n_cut_rows;
+    if (i < r1 - r0) {
+        const int g = r0 + i;
+        const int d = g < op.ax[1].row_base ? 0 : (g < op.ax[2].row_base ? 1 : 2);
+        const DevAxis& A = op.ax[d];
+        const int row = g - A.row_base;
+        const long long p = A.row_out[row];
+        const float* Rd = d == 0 ? R0 : (d == 1 ? R1 : R2);
+        op.op_rowv[d * op.N + p] = (float)closure64(A, row, p, u, Rd, nu, 0.0, true);
+        return;
+    }
+    i -= r1 - r0;
+    const int nlines = op.it0 * op.it1;
+    if (d1 < 3 || i >= nlines) return; // z walls only with the z axis
+    const DevAxis& A = op.ax[2];
+    const long long base = (long long)i * op.it2;
+    int slot = 0;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const WallBlock& W = A.wall[side];
+        float x[7];
+#pragma unroll
+        for (int jj = 0; jj < 7; jj++) x[jj] = jj < W.cols ? __ldg(u + base + W.col0 + jj) : 0.f;
+        for (int r = 0; r < W.rows; r++, slot++) {
+            float acc = 0.f;
+#pragma unroll
+            for (int jj = 0; jj < 7; jj++)
+                if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
+            if (W.has_n && nu) acc = (float)fma(W.n[r], __ldg(nu + base + W.wall), (double)acc);
+            op.op_zw[(long long)slot * nlines + i] = acc;
+        }
+    }
+}
+
+template <int MODE, bool PLUS, int FORM>
+__global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __restrict__ u,
+                                                   const double* __restrict__ nu,
+                                                   float* __restrict__ o0, float* __restrict__ o1,
+                                                   float* __restrict__ o2)
+{
+    constexpr bool NX = MODE == 0 || MODE >= 3, NY = MODE == 1 || MODE >= 3,
+                   NZ = MODE == 2 || MODE >= 3;
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (j >= ny) return; // whole warp
+    const int i = blockIdx.z;
+    const int k = blockIdx.x * 128 + 4 * threadIdx.x;
+    const bool kvalid = k < nz;
+    const int plane = ny * nz;
+    const int kc = min(k, nz - 4);
+    const int p = i * plane + j * nz + kc;
+    const unsigned c4 = kvalid ? __ldg((const unsigned*)(op.cls + p)) : 0u;
+    const float4 C = ld4(u, p);
+    float4 xa{}, xb{}, xc{}, xd{}, ya{}, yb{}, yc{}, yd{}, zL{}, zR{};
+    if constexpr (NX) {
+        xa = ld4(u, p + (max(i - 2, 0) - i) * plane);
+        xb = ld4(u, p + (max(i - 1, 0) - i) * plane);
+        xc = ld4(u, p + (min(i + 1, nx - 1) - i) * plane);
+        xd = ld4(u, p + (min(i + 2, nx - 1) - i) * plane);
+    }
+    if constexpr (NY) {
+        ya = ld4(u, p + (max(j - 2, 0) - j) * nz);
+        yb = ld4(u, p + (max(j - 1, 0) - j) * nz);
+        yc = ld4(u, p + (min(j + 1, ny - 1) - j) * nz);
+        yd = ld4(u, p + (min(j + 2, ny - 1) - j) * nz);
+    }
+    if constexpr (NZ) {
+        zL = ld4(u, p + (kc >= 4 ? -4 : 0));
+        zR = ld4(u, p + (kc + 8 <= nz ? 4 : 0));
+    }
+    const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
+    float v[3][4] = {};
+    unsigned kq[3][4];
+    bool cut = false, zwall = false, xywall = false;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
+            const bool need = d == 0 ? NX : (d == 1 ? NY : NZ);
+            if (!need) continue;
+            cut = cut || kq[d][q] == ROW_CLOSURE;
+            if (d == 2)
+                zwall = zwall || kq[d][q] == ROW_WALL;
+            else
+                xywall = xywall || kq[d][q] == ROW_WALL;
+        }
+        if constexpr (NX)
+            v[0][q] = kq[0][q] == ROW_INTERIOR
+                          ? interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q))
+                          : 0.f;
+        if constexpr (NY)
+            v[1][q] = kq[1][q] == ROW_INTERIOR
+                          ? interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q))
+                          : 0.f;
+        if constexpr (NZ)
+            v[2][q] = kq[2][q] == ROW_INTERIOR
+                          ? interior_row_t<FORM>(op.ax[2], zz[q], zz[q + 1], zz[q + 2], zz[q + 3], zz[q + 4])
+                          : 0.f;
+    }
+    if (cut) {
+        const float* __restrict__ rv = op.op_rowv + p;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if ((d == 0 ? NX : (d == 1 ? NY : NZ)) && kq[d][q] == ROW_CLOSURE)
+                    v[d][q] = rv[d * op.N + q];
+    }
+    if constexpr (NZ) {
+        if (zwall) {
+            const long long nlines = (long long)nx * ny;
+            const float* __restrict__ zt =
+                op.op_zw + (long long)zwall_slot(op.ax[2], k) * nlines + (i * ny + j);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (kq[2][q] == ROW_WALL) v[2][q] = zt[q * nlines];
+        }
+    }
+    if constexpr (NX || NY) {
+        if (__any_sync(FULL, xywall)) {
+#pragma unroll
+            for (int d = 0; d < 2; d++) {
+                if (!(d == 0 ? NX : NY)) continue;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (kq[d][q] == ROW_WALL) {
+                        const int coord = d == 0 ? i : j;
+                        const float w = wall32(op.ax[d], (long long)(p + q), coord, u);
+                        v[d][q] = wall_neumann32(op.ax[d], (long long)(p + q), coord, nu, w);
+                    }
+            }
+        }
+    }
+    if (!kvalid) return;
+    if constexpr (MODE <= 2) {
+        constexpr int d = MODE;
+        const bool all = kq[d][0] && kq[d][1] && kq[d][2] && kq[d][3];
+        if (all) {
+            float4 r = make_float4(v[d][0], v[d][1], v[d][2], v[d][3]);
+            if constexpr (PLUS) {
+                const float4 o = *(const float4*)(o0 + p);
+                r = make_float4(o.x + r.x, o.y + r.y, o.z + r.z, o.w + r.w);
+            }
+            *(float4*)(o0 + p) = r;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (kq[d][q] != ROW_NONE) o0[p + q] = PLUS ? o0[p + q] + v[d][q] : v[d][q];
+        }
+    } else if constexpr (MODE == 3) {
+        float lap[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float a = 0.f; // op_row's order: axes x, y, z, only those with a row
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                if (kq[d][q] != ROW_NONE) a = a + v[d][q];
+            lap[q] = a;
+        }
+        *(float4*)(o0 + p) = make_float4(lap[0], lap[1], lap[2], lap[3]);
+    } else {
+        float* outs[3] = {o0, o1, o2};
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            *(float4*)(outs[d] + p) = make_float4(v[d][0], v[d][1], v[d][2], v[d][3]);
+    }
+}
+
+template <int MODE, bool PLUS>
+void op_vec(const DevOp& op, const float* u, const double* nu, float* o0, float* o1, float* o2,
+            cudaStream_t s)
+{
+    const dim3 grid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0), block(32, BY);
+    if (op.op_form == FORM_ANTI5)
+        k_op_vec<MODE, PLUS, FORM_ANTI5><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+    else if (op.op_form == FORM_SYM5)
+        k_op_vec<MODE, PLUS, FORM_SYM5><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+    else
+        k_op_vec<MODE, PLUS, FORM_W3><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+    ++g_launches;
+}
+
+void op_rows(const DevOp& op, int d0, int d1, const float* u, const void* const R[3],
+             const double* nu, cudaStream_t s)
+{
+    const int r0 = op.ax[d0].row_base, r1 = d1 < 3 ? op.ax[d1].row_base : op.n_cut_rows;
+    const long long n = (long long)(r1 - r0) + (d1 == 3 ? (long long)op.it0 * op.it1 : 0);
+    if (n <= 0) return;
+    k_op_rows<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+        op, d0, d1, u, (const float*)R[0], (const float*)R[1], (const float*)R[2], nu);
+    ++g_launches;
+}
+
+bool op_vec_ok(const DevOp& op)
+{
+    return op.op_form > 0 && op.op_rowv && op.op_zw;
+}
+} // namespace
+
 cudaError_t launch_derivative(const DevOp& op, int dir, int prec, const void* uD,
                               const void* uR, const double* nuD, void* duD, void* const duR[3],
                               const void* const uRall[3], int plus_eq, cudaStream_t s)
@@ -1760,6 +1988,23 @@ cudaError_t launch_derivative(const DevOp& op, int dir, int prec, const void* uD
                                                                (double*)duD);
         ++g_launches;
         return rspace_for<double>(op, dir, uD, uRall, duR, s);
+    }
+    if (op_vec_ok(op)) {
+        const void* Rs[3] = {nullptr, nullptr, nullptr};
+        Rs[dir] = uR;
+        op_rows(op, dir, dir + 1, (const float*)uD, Rs, nuD, s);
+        float* o = (float*)duD;
+        const float* u = (const float*)uD;
+        if (plus_eq) {
+            if (dir == 0) op_vec<0, true>(op, u, nuD, o, nullptr, nullptr, s);
+            else if (dir == 1) op_vec<1, true>(op, u, nuD, o, nullptr, nullptr, s);
+            else op_vec<2, true>(op, u, nuD, o, nullptr, nullptr, s);
+        } else {
+            if (dir == 0) op_vec<0, false>(op, u, nuD, o, nullptr, nullptr, s);
+            else if (dir == 1) op_vec<1, false>(op, u, nuD, o, nullptr, nullptr, s);
+            else op_vec<2, false>(op, u, nuD, o, nullptr, nullptr, s);
+        }
+        return rspace_for<float>(op, dir, uD, uRall, duR, s);
     }
     if (plus_eq)
         k_derivative<float, true><<<grid, block, 0, s>>>(op, dir, (const float*)uD,
@@ -1785,6 +2030,11 @@ cudaError_t launch_laplacian(const DevOp& op, int prec, const void* uD, const vo
         ++g_launches;
         for (int d = 0; d < 3; d++)
             if (op.ax[d].active) rspace_for<double>(op, d, uD, uR, duR, s);
+    } else if (op_vec_ok(op)) {
+        op_rows(op, 0, 3, (const float*)uD, uR, nuD, s);
+        op_vec<3, false>(op, (const float*)uD, nuD, (float*)duD, nullptr, nullptr, s);
+        for (int d = 0; d < 3; d++)
+            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, duR, s);
     } else {
         k_laplacian<float><<<grid, block, 0, s>>>(op, (const float*)uD, (const float*)uR[0],
                                                   (const float*)uR[1], (const float*)uR[2], nuD,
@@ -1812,6 +2062,14 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
         for (int d = 0; d < 3; d++) {
             void* const dR[3] = {out[d][1], out[d][2], out[d][3]};
             if (op.ax[d].active) rspace_for<double>(op, d, uD, uR, dR, s);
+        }
+    } else if (op_vec_ok(op) && out[0][0] && out[1][0] && out[2][0]) {
+        op_rows(op, 0, 3, (const float*)uD, uR, nullptr, s);
+        op_vec<4, false>(op, (const float*)uD, nullptr, (float*)out[0][0], (float*)out[1][0],
+                         (float*)out[2][0], s);
+        for (int d = 0; d < 3; d++) {
+            void* const dR[3] = {out[d][1], out[d][2], out[d][3]};
+            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, dR, s);
         }
     } else {
         k_gradient<float><<<grid, block, 0, s>>>(

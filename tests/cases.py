@@ -28,6 +28,11 @@ def cases():
         "micro_e42_96": W.micro_case(96, "E4_2", (DIR, FLT)),
         # the adjoint configuration's geometry at 24^3
         "adjoint_24": W.adjoint_case(24),
+        # Neumann walls on both z faces (the z-wall rows of the vectorised operators carry
+        # the Neumann term), Floating sphere
+        "neumann_z_e42": dict(n=(20, 18, 24), lo=(0, 0, 0), hi=(1, 1, 1),
+                              spheres=[((0.5, 0.52, 0.47), 0.22, FLT)],
+                              grid_bc=(DIR, FLT, FLT, DIR, NEU, NEU), scheme="E4_2"),
         # configuration 0 of the benchmark: 2-D heat, circle, E4_2, Dirichlet walls
         "c0_circle_2d": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
                              spheres=[((0.51, 0.49, 0.0), 0.2, DIR)],

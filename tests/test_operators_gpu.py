@@ -61,7 +61,7 @@ def test_derivative(name, prec):
     has_neumann = "neumann" in c.get("grid_bc", ())
     for d in range(3):
         for plus_eq in (False, True):
-            for use_nu in ((False, True) if has_neumann and prec == S.PREC_FP64 else (False,)):
+            for use_nu in ((False, True) if has_neumann else (False,)):
                 du0 = rand_field(o, 10 + d)
                 if prec == S.PREC_MIXED:
                     du0 = [a.astype(np.float32).astype(np.float64) for a in du0]
@@ -89,7 +89,7 @@ def test_laplacian(name, prec):
     if prec == S.PREC_MIXED:
         u = [a.astype(np.float32).astype(np.float64) for a in u]
     nus = [None]
-    if "neumann" in c.get("grid_bc", ()) and prec == S.PREC_FP64:
+    if "neumann" in c.get("grid_bc", ()):
         nus.append(np.random.default_rng(6).uniform(-1, 1, o.size))
     for nu in nus:
         want = o.laplacian(u, o.zeros(), nu=nu)
