@@ -423,9 +423,30 @@ def adjoint_bench(stream, n=128, steps=200, every=20, ndir=32, eps=1e-6, cg_iter
         rvec = r_new
         Jx, gx = loss_grad(x)
     err0 = float(torch.linalg.norm(u_true * fluid))
+    # the mixed system: FP32 stage fields forward, FP32 reverse sweep
+    sysm = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_ZERO)
+    sysm.set_state(S.ScalarField(u0, *R), stream)
+    tm = sysm.forward(0.0, dt, steps, every, stream)
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    sysm.set_state(S.ScalarField(u0, *R), stream)
+    tm = sysm.forward(0.0, dt, steps, every, stream)
+    e[1].record(stream)
+    uTm = torch.empty_like(u0)
+    sysm.get_state(S.ScalarField(uTm, *R), stream)
+    rm_ = (uTm - u_obs) * fluid
+    g32 = torch.empty_like(u0)
+    e[1].record(stream)
+    sysm.backward(tm, S.ScalarField(rm_, *R), S.ScalarField(g32, *R), stream)
+    e[2].record(stream)
+    e[2].synchronize()
+    _, g64 = loss_grad(u0)
+    mixed = {"forward_ms": e[0].elapsed_time(e[1]), "backward_ms": e[1].elapsed_time(e[2]),
+             "gradient_rel_diff_vs_fp64": float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))}
+    mixed["backward_over_forward"] = mixed["backward_ms"] / mixed["forward_ms"]
     return {"grid": [n, n, n], "rk4_steps": steps, "checkpoint_every": every,
             "dtype": "f64", "forward_ms": t_fwd, "backward_ms": t_bwd,
-            "backward_over_forward": t_bwd / t_fwd,
+            "backward_over_forward": t_bwd / t_fwd, "mixed": mixed,
             "fd_check": {"directions": ndir, "eps": eps, "max_rel_error": max(rel),
                          "median_rel_error": sorted(rel)[len(rel) // 2]},
             "inversion": {"method": "conjugate gradients on the normal equations",

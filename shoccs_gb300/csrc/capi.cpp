@@ -92,10 +92,10 @@ struct AdjointState {
     bool built = false;
     DeviceAlloc mem;
     AdjClosure cl{};
-    double* lam = nullptr; // adjoint of the current state
-    double* acc = nullptr;
-    double* za = nullptr;
-    double* zb = nullptr;
+    void* lam = nullptr; // adjoint of the current state (FP64, or FP32 for a mixed system)
+    void* acc = nullptr;
+    void* za = nullptr;
+    void* zb = nullptr;
 };
 
 struct shoccs_system {
@@ -1305,11 +1305,9 @@ shoccs_status build_adjoint(shoccs_system* S, cudaStream_t s)
     SH_CUDA(A.mem.put(src, &A.cl.src, s));
     SH_CUDA(A.mem.put(w, &A.cl.w, s));
     A.cl.n_tgt = (int)tgt.size();
-    void* q = nullptr;
-    for (double** b : {&A.lam, &A.acc, &A.za, &A.zb}) {
-        SH_CUDA(A.mem.alloc(N * sizeof(double), &q));
-        *b = (double*)q;
-    }
+    const size_t es = S->desc.prec == PREC_MIXED ? sizeof(float) : sizeof(double);
+    for (void** b : {&A.lam, &A.acc, &A.za, &A.zb})
+        SH_CUDA(A.mem.alloc(N * es, b));
     A.built = true;
     return SHOCCS_OK;
 }
@@ -1318,8 +1316,6 @@ shoccs_status adjoint_supported(const shoccs_system* S)
 {
     if (S->desc.kind != SHOCCS_SYS_HEAT)
         return fail(SHOCCS_EUNSUPPORTED, "the adjoint is implemented for heat systems");
-    if (S->desc.prec != PREC_FP64)
-        return fail(SHOCCS_EUNSUPPORTED, "the adjoint is implemented for FP64 systems");
     return SHOCCS_OK;
 }
 } // namespace
@@ -1331,6 +1327,8 @@ shoccs_status shoccs_system_rhs_transpose(shoccs_system* S, const shoccs_field* 
 {
     if (!S || !x || !y || !x->D || !y->D) return fail(SHOCCS_EINVAL, "null argument");
     if (auto st = adjoint_supported(S); st != SHOCCS_OK) return st;
+    if (S->desc.prec != PREC_FP64)
+        return fail(SHOCCS_EUNSUPPORTED, "the transposed operator takes FP64 fields");
     const cudaStream_t s = (cudaStream_t)stream;
     if (auto st = build_adjoint(S, s); st != SHOCCS_OK) return st;
     AdjArgs a{};
@@ -1338,7 +1336,7 @@ shoccs_status shoccs_system_rhs_transpose(shoccs_system* S, const shoccs_field* 
     a.zscale = 1.0;
     a.out = (double*)y->D;
     a.k = S->desc.diffusivity;
-    SH_CUDA(launch_adjoint_stage(S->P->op, S->adj.cl, 0, a, s));
+    SH_CUDA(launch_adjoint_stage(S->P->op, S->adj.cl, 0, a, PREC_FP64, s));
     for (int r = 0; r < 3; r++) {
         void* yr = r == 0 ? y->Rx : (r == 1 ? y->Ry : y->Rz);
         if (yr && S->P->mesh.R[r].size())
@@ -1362,10 +1360,13 @@ shoccs_status shoccs_system_forward(shoccs_system* S, double t0, double dt, int 
     T->nsteps = nsteps;
     T->every = checkpoint_every;
     T->n = S->P->mesh.size();
-    auto save = [&]() -> shoccs_status {
+    auto save = [&]() -> shoccs_status { // checkpoints hold the state in FP64
         void* q = nullptr;
         SH_CUDA(T->mem.alloc(T->n * sizeof(double), &q));
-        SH_CUDA(cudaMemcpyAsync(q, S->b.u0, T->n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (S->desc.prec == PREC_MIXED)
+            SH_CUDA(launch_state_convert(T->n, 0, nullptr, nullptr, S->b.u0, (double*)q, s));
+        else
+            SH_CUDA(cudaMemcpyAsync(q, S->b.u0, T->n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         T->ckpt.push_back((double*)q);
         return SHOCCS_OK;
     };
@@ -1404,11 +1405,17 @@ shoccs_status shoccs_system_backward(shoccs_system* S, const shoccs_tape* T,
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0}; // src/temporal/rk4.cpp:11-12
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
     const double dt = T->dt;
-    // lam = dJ/du(T); its Dirichlet-face entries are dropped (the last stage resets faces)
-    SH_CUDA(cudaMemcpyAsync(A.lam, g->D, N * sizeof(double), cudaMemcpyDefault, s));
-    SH_CUDA(launch_adjoint_mask_faces(S->P->op, A.lam, s));
+    const int prec = S->desc.prec;
+    // lam = dJ/du(T); its Dirichlet-face entries are dropped (the last stage resets faces).
+    // A mixed system runs the reverse sweep in FP32 (the forward's stage precision).
+    if (prec == PREC_MIXED) {
+        SH_CUDA(launch_cast(N, 1, g->D, A.lam, s)); // field pointers are device pointers
+    } else {
+        SH_CUDA(cudaMemcpyAsync(A.lam, g->D, N * sizeof(double), cudaMemcpyDefault, s));
+    }
+    SH_CUDA(launch_adjoint_mask_faces(S->P->op, A.lam, prec, s));
     for (int n = T->nsteps - 1; n >= 0; n--) {
-        double* zin = nullptr;
+        void* zin = nullptr;
         for (int st = 4; st >= 1; st--) {
             AdjArgs a{};
             a.k = S->desc.diffusivity;
@@ -1424,11 +1431,14 @@ shoccs_status shoccs_system_backward(shoccs_system* S, const shoccs_tape* T,
                 a.out = A.lam; // in place: S = 1 reads lam only at the point it writes
                 a.first_step = n == 0;
             }
-            SH_CUDA(launch_adjoint_stage(S->P->op, A.cl, st, a, s));
+            SH_CUDA(launch_adjoint_stage(S->P->op, A.cl, st, a, prec, s));
             zin = a.out;
         }
     }
-    SH_CUDA(cudaMemcpyAsync(out->D, A.lam, N * sizeof(double), cudaMemcpyDefault, s));
+    if (prec == PREC_MIXED)
+        SH_CUDA(launch_cast(N, 0, A.lam, out->D, s));
+    else
+        SH_CUDA(cudaMemcpyAsync(out->D, A.lam, N * sizeof(double), cudaMemcpyDefault, s));
     for (int r = 0; r < 3; r++) {
         void* yr = r == 0 ? out->Rx : (r == 1 ? out->Ry : out->Rz);
         if (yr && S->P->mesh.R[r].size())

@@ -197,22 +197,25 @@ struct AdjClosure {
     const long long* src = nullptr; // output point of the row
     const double* w = nullptr;      // coefficient
 };
-// one reverse RK4 stage S (4..1), or mode 0: out = A^T z (the transposed operator alone)
+// one reverse RK4 stage S (4..1), or mode 0: out = A^T z (the transposed operator alone).
+// The vectors are FP64 (PREC_FP64) or FP32 (PREC_MIXED: the reverse sweep of a mixed system)
 struct AdjArgs {
-    const double* z;  // stencil input: the stage adjoint z_S (lam for S = 4, scaled by zscale)
+    const void* z;     // stencil input: the stage adjoint z_S (lam for S = 4, scaled by zscale)
     double zscale;
-    const double* lam; // adjoint of the step's end state
-    double* acc;       // sum of the stage adjoints of the step
-    double* out;       // z_{S-1} (S = 4..2), the step's start adjoint (S = 1), A^T z (mode 0)
+    const void* lam;   // adjoint of the step's end state
+    void* acc;         // sum of the stage adjoints of the step
+    void* out;         // z_{S-1} (S = 4..2), the step's start adjoint (S = 1), A^T z (mode 0)
     double bl, ay;     // out = bl * lam + ay * (A^T z) for S = 4..2
     int first_step;    // S = 1 of the solve's first step: the adjoint of the caller's
                        // Dirichlet-face values (read by its first stage) is kept
     double k;          // diffusivity
 };
 cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, const AdjArgs& a,
-                                 cudaStream_t s);
+                                 int prec, cudaStream_t s);
 // zero lam on the Dirichlet-face points
-cudaError_t launch_adjoint_mask_faces(const DevOp& op, double* lam, cudaStream_t s);
+cudaError_t launch_adjoint_mask_faces(const DevOp& op, void* lam, int prec, cudaStream_t s);
+// n values between FP64 and FP32 (to_f32: double -> float, else float -> double)
+cudaError_t launch_cast(long long n, int to_f32, const void* in, void* out, cudaStream_t s);
 
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,

@@ -2639,10 +2639,11 @@ __device__ __forceinline__ bool evolves(unsigned c) { return (c & 0x3Fu) && !(c 
 
 // transposed interior rows at point p (coordinates ijk): sum over axes and offsets of the
 // neighbours i = p - m s whose interior row (an evolving point's) reads p with weight c_m
-__device__ __forceinline__ double interior_t(const DevOp& op, long long p, const int ijk[3],
-                                             const double* __restrict__ z)
+template <class T>
+__device__ __forceinline__ T interior_t(const DevOp& op, long long p, const int ijk[3],
+                                        const T* __restrict__ z)
 {
-    double y = 0.0;
+    T y = 0;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const DevAxis& A = op.ax[d];
@@ -2654,12 +2655,16 @@ __device__ __forceinline__ double interior_t(const DevOp& op, long long p, const
             const long long i = p - (long long)m * A.stride;
             const unsigned c = op.cls[i];
             if (((c >> (2 * d)) & 3u) != ROW_INTERIOR || (c & CLS_DIRFACE)) continue;
-            y = fma(A.ic[half + m], __ldg(z + i), y); // row i's weight on offset m
+            if constexpr (sizeof(T) == 8)
+                y = fma(A.ic[half + m], __ldg(z + i), y); // row i's weight on offset m
+            else
+                y = fmaf(A.icf[half + m], __ldg(z + i), y);
         }
     }
     return y;
 }
 
+template <class T>
 __global__ void __launch_bounds__(256) k_adj_stage(DevOp op, int S, AdjArgs a)
 {
     const Pt q = point_of(op);
@@ -2667,69 +2672,103 @@ __global__ void __launch_bounds__(256) k_adj_stage(DevOp op, int S, AdjArgs a)
     const unsigned c = op.cls[q.p];
     int ijk[3];
     phys_ijk(op, q, ijk);
-    const double y = a.k * (interior_t(op, q.p, ijk, a.z) * a.zscale);
+    const T* z = (const T*)a.z;
+    const T* lam = (const T*)a.lam;
+    T* acc = (T*)a.acc;
+    T* out = (T*)a.out;
+    const T y = (T)a.k * (interior_t<T>(op, q.p, ijk, z) * (T)a.zscale);
     const bool e = evolves(c);
     if (S == 0) {
-        a.out[q.p] = y;
+        out[q.p] = y;
     } else if (S > 1) {
-        const double acc = S == 4 ? 0.0 : a.acc[q.p];
-        a.acc[q.p] = e ? acc + y : 0.0;
-        a.out[q.p] = e ? fma(a.ay, y, a.bl * a.lam[q.p]) : 0.0;
+        const T ac = S == 4 ? T(0) : acc[q.p];
+        acc[q.p] = e ? ac + y : T(0);
+        out[q.p] = e ? (T)a.ay * y + (T)a.bl * lam[q.p] : T(0);
     } else {
-        const double l = a.lam[q.p];
-        a.out[q.p] = e ? l + a.acc[q.p] + y
-                       : ((c & CLS_DIRFACE) ? (a.first_step ? y : 0.0) : l);
+        const T l = lam[q.p];
+        out[q.p] = e ? l + acc[q.p] + y : ((c & CLS_DIRFACE) ? (a.first_step ? y : T(0)) : l);
     }
 }
 
-// transposed closure rows, added after k_adj_stage: target t gets k sum w z[src]
+// transposed closure rows, added after k_adj_stage: target t gets k sum w z[src] (FP64 sum)
+template <class T>
 __global__ void k_adj_closure(DevOp op, AdjClosure cl, int S, AdjArgs a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cl.n_tgt) return;
-    double y = 0.0;
-    for (int e = cl.ptr[t]; e < cl.ptr[t + 1]; e++) y = fma(cl.w[e], __ldg(a.z + cl.src[e]), y);
-    y = a.k * (y * a.zscale);
+    const T* z = (const T*)a.z;
+    T* acc = (T*)a.acc;
+    T* out = (T*)a.out;
+    double yd = 0.0;
+    for (int e = cl.ptr[t]; e < cl.ptr[t + 1]; e++)
+        yd = fma(cl.w[e], (double)__ldg(z + cl.src[e]), yd);
+    const T y = (T)(a.k * (yd * a.zscale));
     const long long p = cl.tgt[t];
     const unsigned c = op.cls[p];
     if (S == 0) {
-        a.out[p] += y;
+        out[p] += y;
     } else if (S > 1) {
         if (evolves(c)) {
-            a.acc[p] += y;
-            a.out[p] += a.ay * y;
+            acc[p] += y;
+            out[p] += (T)a.ay * y;
         }
     } else if (evolves(c) || ((c & CLS_DIRFACE) && a.first_step)) {
-        a.out[p] += y;
+        out[p] += y;
     }
 }
-} // namespace
 
-namespace
-{
-__global__ void k_adj_mask_faces(DevOp op, double* lam)
+template <class T>
+__global__ void k_adj_mask_faces(DevOp op, T* lam)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < op.n_faces) lam[op.faces[e]] = 0.0;
+    if (e < op.n_faces) lam[op.faces[e]] = T(0);
+}
+
+__global__ void k_cast(long long n, int to_f32, const void* in, void* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (to_f32)
+        ((float*)out)[i] = (float)((const double*)in)[i];
+    else
+        ((double*)out)[i] = (double)((const float*)in)[i];
 }
 } // namespace
 
-cudaError_t launch_adjoint_mask_faces(const DevOp& op, double* lam, cudaStream_t s)
+cudaError_t launch_adjoint_mask_faces(const DevOp& op, void* lam, int prec, cudaStream_t s)
 {
     if (op.n_faces) {
-        k_adj_mask_faces<<<(op.n_faces + 255) / 256, 256, 0, s>>>(op, lam);
+        if (prec == PREC_MIXED)
+            k_adj_mask_faces<float><<<(op.n_faces + 255) / 256, 256, 0, s>>>(op, (float*)lam);
+        else
+            k_adj_mask_faces<double><<<(op.n_faces + 255) / 256, 256, 0, s>>>(op, (double*)lam);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cast(long long n, int to_f32, const void* in, void* out, cudaStream_t s)
+{
+    if (n > 0) {
+        k_cast<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, to_f32, in, out);
         ++g_launches;
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, const AdjArgs& a,
-                                 cudaStream_t s)
+                                 int prec, cudaStream_t s)
 {
-    k_adj_stage<<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
+    if (prec == PREC_MIXED)
+        k_adj_stage<float><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
+    else
+        k_adj_stage<double><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
     ++g_launches;
     if (cl.n_tgt) {
-        k_adj_closure<<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
+        if (prec == PREC_MIXED)
+            k_adj_closure<float><<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
+        else
+            k_adj_closure<double><<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
         ++g_launches;
     }
     return cudaGetLastError();

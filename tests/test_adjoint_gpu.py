@@ -227,11 +227,39 @@ def test_tape_checkpoints_are_the_forward_states():
 
 
 @pytest.mark.gpu
+def test_mixed_adjoint_matches_fp64_gradient():
+    """A mixed system records its tape in FP64 and runs the reverse sweep in FP32: its
+    gradient equals the FP64 system's to FP32 accuracy, and it is the transpose of the mixed
+    solve to FP32 accuracy."""
+    n, steps = 24, 30
+    p = S.Problem(**case(n))
+    s64 = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_ZERO)
+    s32 = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_ZERO)
+    _, fluid = _masks(p)
+    dt = W.heat_dt(n)
+    u0 = _grid_u0(n)
+    obs = np.zeros(p.size)
+    _, g64 = _loss_and_grad(s64, p, u0, obs, fluid, 0.0, dt, steps)
+    _, g32 = _loss_and_grad(s32, p, u0, obs, fluid, 0.0, dt, steps)
+    assert np.linalg.norm(g32 - g64) <= 1e-5 * np.linalg.norm(g64)
+    rng = np.random.default_rng(12)
+    v, w = _smooth_direction(n, rng), _smooth_direction(n, rng)
+    s32.set_state(_field(p, v))
+    tape = s32.forward(0.0, dt, steps)
+    Fv = _field(p, np.zeros(p.size))
+    s32.get_state(Fv)
+    FTw = _field(p, np.zeros(p.size))
+    s32.backward(tape, _field(p, w), FTw)
+    a, b = float(np.dot(w, Fv.D.cpu().numpy())), float(np.dot(FTw.D.cpu().numpy(), v))
+    assert abs(a - b) <= 1e-5 * (np.linalg.norm(w) * np.linalg.norm(Fv.D.cpu().numpy())), (a, b)
+
+
+@pytest.mark.gpu
 def test_adjoint_rejects_unsupported_systems():
     p = S.Problem(**case(20))
     m = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_ZERO)
-    with pytest.raises(S.ShoccsError):
-        m.forward(0.0, 1e-4, 2)
+    with pytest.raises(S.ShoccsError):  # the transposed operator alone takes FP64 fields
+        m.rhs_transpose(_field(p, np.zeros(p.size)), _field(p, np.zeros(p.size)))
     w = S.ScalarWave(S.Problem(**W.wave_3d(16, radius=0)), S.PREC_FP64, S.VEL_CONSTANT,
                      W.WAVE_VEL, (0, 0, 0), S.SOL_GAUSS_PULSE, W.WAVE_PULSE)
     with pytest.raises(S.ShoccsError):
