@@ -427,6 +427,8 @@ def adjoint_bench(stream, n=128, steps=200, every=20, ndir=32, eps=1e-6, cg_iter
     sysm = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_ZERO)
     sysm.set_state(S.ScalarField(u0, *R), stream)
     tm = sysm.forward(0.0, dt, steps, every, stream)
+    gw = torch.empty_like(u0)  # warm-up: the first backward builds the transposed closure
+    sysm.backward(tm, S.ScalarField(torch.zeros_like(u0), *R), S.ScalarField(gw, *R), stream)
     torch.cuda.synchronize()
     e[0].record(stream)
     sysm.set_state(S.ScalarField(u0, *R), stream)

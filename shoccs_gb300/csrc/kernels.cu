@@ -2717,6 +2717,109 @@ __global__ void k_adj_closure(DevOp op, AdjClosure cl, int S, AdjArgs a)
     }
 }
 
+// FP32 reverse stage in the vectorised layout (3-D grids, nz a multiple of 4): four z points
+// per thread; the stage adjoint and the class words of the 12 stencil neighbours arrive as
+// float4 / 32-bit loads, and each point gathers from the neighbour rows that read it (their
+// class says interior, not on a Dirichlet face, and they lie in the grid).  The closure part
+// follows in k_adj_closure as in the per-point path.
+__device__ __forceinline__ unsigned cbyte(unsigned w, int q) { return (w >> (8 * q)) & 0xFFu; }
+__device__ __forceinline__ bool row_reads(unsigned c, int d)
+{
+    return ((c >> (2 * d)) & 3u) == ROW_INTERIOR && !(c & CLS_DIRFACE);
+}
+
+__global__ void __launch_bounds__(256, 4) k_adj_stage_vec(DevOp op, int S, AdjArgs a)
+{
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (j >= ny) return;
+    const int i = blockIdx.z;
+    const int k = blockIdx.x * 128 + 4 * threadIdx.x;
+    if (k >= nz) return;
+    const int plane = ny * nz;
+    const int p = i * plane + j * nz + k;
+    const float* __restrict__ z = (const float*)a.z;
+    const unsigned* __restrict__ cw = (const unsigned*)op.cls;
+    auto C4 = [&](int idx) { return __ldg(cw + idx / 4); };
+    // neighbours along x and y: offsets of planes / rows i-2 .. i+2 (clamped; the range
+    // checks below drop the clamped ones)
+    const int ox[5] = {(max(i - 2, 0) - i) * plane, (max(i - 1, 0) - i) * plane, 0,
+                       (min(i + 1, nx - 1) - i) * plane, (min(i + 2, nx - 1) - i) * plane};
+    const int oy[5] = {(max(j - 2, 0) - j) * nz, (max(j - 1, 0) - j) * nz, 0,
+                       (min(j + 1, ny - 1) - j) * nz, (min(j + 2, ny - 1) - j) * nz};
+    const bool inx[5] = {i >= 2, i >= 1, true, i + 1 < nx, i + 2 < nx};
+    const bool iny[5] = {j >= 2, j >= 1, true, j + 1 < ny, j + 2 < ny};
+    float4 zx[5], zy[5];
+    unsigned cx[5], cy[5];
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        zx[m] = ld4(z, p + ox[m]);
+        cx[m] = C4(p + ox[m]);
+        zy[m] = ld4(z, p + oy[m]);
+        cy[m] = C4(p + oy[m]);
+    }
+    const int zl = k >= 4 ? -4 : 0, zr = k + 8 <= nz ? 4 : 0;
+    const float4 zL = ld4(z, p + zl), zR = ld4(z, p + zr);
+    const unsigned cL = C4(p + zl), cR = C4(p + zr);
+    const float4 zc = zx[2];
+    const unsigned cc = cx[2];
+    const float zz[12] = {zL.x, zL.y, zL.z, zL.w, zc.x, zc.y, zc.z, zc.w, zR.x, zR.y, zR.z, zR.w};
+    const unsigned czw[3] = {cL, cc, cR};
+    float y[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float t = 0.f;
+        // x: the row at plane i - (m - 2) reads this point with weight icf[half + (m - 2)]
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            const DevAxis& A = op.ax[0];
+            const int off = 2 - m; // this point's offset in that row
+            const int half = A.width / 2;
+            if (off < -half || off > half || !inx[m]) continue;
+            if (row_reads(cbyte(cx[m], q), 0)) t = fmaf(A.icf[half + off], f4(zx[m], q), t);
+        }
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            const DevAxis& A = op.ax[1];
+            const int off = 2 - m;
+            const int half = A.width / 2;
+            if (off < -half || off > half || !iny[m]) continue;
+            if (row_reads(cbyte(cy[m], q), 1)) t = fmaf(A.icf[half + off], f4(zy[m], q), t);
+        }
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            const DevAxis& A = op.ax[2];
+            const int off = 2 - m;
+            const int half = A.width / 2;
+            const int kk = k + q - off; // the row's point
+            if (off < -half || off > half || kk < 0 || kk >= nz) continue;
+            const int w = 4 + q - off; // position in the 12-value window
+            if (row_reads(cbyte(czw[w >> 2], w & 3), 2)) t = fmaf(A.icf[half + off], zz[w], t);
+        }
+        y[q] = (float)a.k * (t * (float)a.zscale);
+    }
+    const float* __restrict__ lam = (const float*)a.lam;
+    float* __restrict__ acc = (float*)a.acc;
+    float* __restrict__ out = (float*)a.out;
+    float o[4], ac[4];
+    const float4 l4 = *(const float4*)(lam + p);
+    const float4 a4 = S == 4 ? make_float4(0.f, 0.f, 0.f, 0.f) : *(const float4*)(acc + p);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const unsigned c = cbyte(cc, q);
+        const bool e = evolves(c);
+        const float l = f4(l4, q);
+        if (S > 1) {
+            ac[q] = e ? f4(a4, q) + y[q] : 0.f;
+            o[q] = e ? (float)a.ay * y[q] + (float)a.bl * l : 0.f;
+        } else {
+            o[q] = e ? l + f4(a4, q) + y[q] : ((c & CLS_DIRFACE) ? (a.first_step ? y[q] : 0.f) : l);
+        }
+    }
+    if (S > 1) *(float4*)(acc + p) = make_float4(ac[0], ac[1], ac[2], ac[3]);
+    *(float4*)(out + p) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
 template <class T>
 __global__ void k_adj_mask_faces(DevOp op, T* lam)
 {
@@ -2759,7 +2862,12 @@ cudaError_t launch_cast(long long n, int to_f32, const void* in, void* out, cuda
 cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, const AdjArgs& a,
                                  int prec, cudaStream_t s)
 {
-    if (prec == PREC_MIXED)
+    const bool vec = prec == PREC_MIXED && S > 0 && op.it0 > 1 && op.it1 > 1 && op.it2 > 1 &&
+                     op.it2 % 4 == 0 && op.N < (1LL << 31) - 64;
+    if (vec)
+        k_adj_stage_vec<<<dim3((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0),
+                          dim3(32, BY), 0, s>>>(op, S, a);
+    else if (prec == PREC_MIXED)
         k_adj_stage<float><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
     else
         k_adj_stage<double><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
