@@ -44,6 +44,14 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
+// ---- programmatic dependent launch -------------------------------------------------------
+// Kernels of the mixed stage chain (cut-cell rows -> stage -> cut-cell rows ...) are launched
+// with programmatic stream serialisation: a kernel's blocks may be scheduled while the
+// previous kernel drains, and wait here until its writes are visible.  Without that launch
+// attribute both instructions return at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // ---- loads -----------------------------------------------------------------------------
 __device__ __forceinline__ double ldd(const double* p, long long i) { return __ldg(p + i); }
 __device__ __forceinline__ double ldd(const float* p, long long i) { return (double)__ldg(p + i); }
@@ -554,6 +562,8 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
                            const double* R1, const double* R2, TOUT* __restrict__ cval,
                            float* __restrict__ rowv, float* __restrict__ zw)
 {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= op.n_cut_rows) {
         if constexpr (!std::is_same<TIN, const double*>::value) {
@@ -1134,6 +1144,8 @@ __device__ __forceinline__ float f4(const float4& v, int q)
 template <int STAGE, int SYS, int FORM, int VK, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
 {
+    pdl_wait();
+    pdl_trigger();
     const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
     const int lane = threadIdx.x;
@@ -2086,6 +2098,24 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
 
 namespace
 {
+// launch with programmatic stream serialisation when pdl is set (see pdl_wait)
+template <class... KArgs, class... Args>
+cudaError_t launch_ex(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, bool pdl,
+                      Args&&... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <int STAGE, int SYS>
 void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArgs& a,
                   const StepBuffers& b, cudaStream_t s, cudaEvent_t* ev, cudaEvent_t join)
@@ -2103,13 +2133,12 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
                 op, (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
                 (double*)a.cval, nullptr, nullptr);
         else if (STAGE == 0)
-            k_cut_rows<PairU, float><<<nb, 128, 0, s>>>(op, PairU{(const float*)a.u0, op.N},
-                                                        R[0], R[1], R[2], (float*)a.cval, rowv,
-                                                        zw);
+            launch_ex(k_cut_rows<PairU, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
+                      PairU{(const float*)a.u0, op.N}, R[0], R[1], R[2], (float*)a.cval, rowv,
+                      zw);
         else
-            k_cut_rows<const float*, float><<<nb, 128, 0, s>>>(op, (const float*)a.s_in, R[0],
-                                                               R[1], R[2], (float*)a.cval, rowv,
-                                                               zw);
+            launch_ex(k_cut_rows<const float*, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
+                      (const float*)a.s_in, R[0], R[1], R[2], (float*)a.cval, rowv, zw);
         ++g_launches;
     }
     if (join) cudaStreamWaitEvent(s, join, 0); // boundary values of the step are ready
@@ -2137,7 +2166,7 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
     } else if (mixed && b.vec) {
         const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0);
         // 4 or 3 resident blocks per SM (64 or 85 registers per thread)
-        auto go = [&](auto kern) { kern<<<vgrid, block, 0, s>>>(op, sp, a); };
+        auto go = [&](auto kern) { launch_ex(kern, vgrid, block, s, true, op, sp, a); };
         const bool b4 = b.vec_minb == 4;
         if constexpr (SYS == SYS_WAVE) {
             if (sp.vel_kind)
