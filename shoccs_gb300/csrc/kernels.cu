@@ -776,6 +776,8 @@ __device__ __forceinline__ void stage64_at(const DevOp& op, const SysParams& sp,
 template <int STAGE, int SYS, class IDX>
 __global__ void __launch_bounds__(256) k_stage64(DevOp op, SysParams sp, StageArgs sa)
 {
+    pdl_wait();
+    pdl_trigger();
     stage64_at<STAGE, SYS, IDX>(op, sp, sa, stage_point<IDX>(op));
 }
 
@@ -1548,6 +1550,8 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
 // Dirichlet face values of the stage output (update_boundary on D), FP64 path
 __global__ void k_faces64(DevOp op, DevSol sol, double t, double et, double* out)
 {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= op.n_faces) return;
     const long long p = op.faces[i];
@@ -2129,9 +2133,9 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         const int nb = (int)((op.n_cut_rows + n_zw + 127) / 128);
         const double* const* R = a.R;
         if (!mixed)
-            k_cut_rows<const double*, double><<<nb, 128, 0, s>>>(
-                op, (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
-                (double*)a.cval, nullptr, nullptr);
+            launch_ex(k_cut_rows<const double*, double>, dim3(nb), dim3(128), s, true, op,
+                      (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
+                      (double*)a.cval, nullptr, nullptr);
         else if (STAGE == 0)
             launch_ex(k_cut_rows<PairU, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
                       PairU{(const float*)a.u0, op.N}, R[0], R[1], R[2], (float*)a.cval, rowv,
@@ -2198,9 +2202,9 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
             k_stage_mixed<STAGE, SYS, long long><<<grid, block, 0, s>>>(op, sp, a);
     } else {
         if (small)
-            k_stage64<STAGE, SYS, int><<<grid, block, 0, s>>>(op, sp, a);
+            launch_ex(k_stage64<STAGE, SYS, int>, grid, block, s, true, op, sp, a);
         else
-            k_stage64<STAGE, SYS, long long><<<grid, block, 0, s>>>(op, sp, a);
+            launch_ex(k_stage64<STAGE, SYS, long long>, grid, block, s, true, op, sp, a);
     }
     ++g_launches;
     if (ev) cudaEventRecord(ev[1], s);
@@ -2210,8 +2214,8 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         if (mixed)
             k_faces_mixed<STAGE><<<nb, 256, 0, s>>>(op, a);
         else
-            k_faces64<<<nb, 256, 0, s>>>(op, sp.sol, a.t_next, a.et_next,
-                                         (double*)(STAGE == 3 ? a.u0 : a.s_out));
+            launch_ex(k_faces64, dim3(nb), dim3(256), s, true, op, sp.sol, a.t_next, a.et_next,
+                      (double*)(STAGE == 3 ? a.u0 : a.s_out));
         ++g_launches;
     }
 }
@@ -2477,6 +2481,8 @@ __global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restr
                                                         const int* __restrict__ row_inst,
                                                         int n_rows, const BatchTime* __restrict__ bt)
 {
+    pdl_wait();
+    pdl_trigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n_rows) return;
     const int ii = row_inst[g];
@@ -2507,6 +2513,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_batch_stage(const BatchInst* __r
                                                             int n_tiles,
                                                             const BatchTime* __restrict__ bt)
 {
+    pdl_wait();
+    pdl_trigger();
     for (int T = blockIdx.x; T < n_tiles; T += gridDim.x) {
         const int2 tl = tiles[T]; // (instance, tile within the instance)
         const BatchInst& I = B[tl.x];
