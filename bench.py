@@ -55,10 +55,11 @@ ACC_CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1), spheres=
 ACC_STEPS = 300
 # algorithmic HBM bytes per grid point per RK4 step (u0, accumulator, stage field each read
 # and written once per stage): FP64 (8-byte everything) 8+8+8 | 24+16 | 24+16 | 24+8 = 136;
-# mixed (4-byte stage field and accumulator, 8-byte compensated u0)
-# 8+4+4 | 16+8 | 16+8 | 16+8 = 88
-BYTES_PT_STEP = {"mixed": 88, "fp64": 136}
-BYTES_PT_STAGE = {"mixed": [16, 24, 24, 24], "fp64": [24, 40, 40, 32]}
+# mixed (4-byte stage field and accumulator, 8-byte compensated u0 of which stages 0-2 read
+# only the 4-byte hi word)
+# 4+4+4 | 12+8 | 12+8 | 16+8 = 76
+BYTES_PT_STEP = {"mixed": 76, "fp64": 136}
+BYTES_PT_STAGE = {"mixed": [12, 20, 20, 24], "fp64": [24, 40, 40, 32]}
 
 
 def config(nsteps):

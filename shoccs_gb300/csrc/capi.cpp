@@ -488,6 +488,25 @@ shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_fi
 // ---------------------------------------------------------------------------------------
 // systems
 // ---------------------------------------------------------------------------------------
+// The vectorised stage kernels take the z-wall rows of a line from its 16-word record
+// (k_cut_rows): at most 6 rows per wall block (words 0..5 and 8..13), each block entirely on
+// its side of the line's middle (wall_side), no Neumann term, and nz >= 8 so that the first
+// and last points of a line sit in different lanes.
+static bool line_records_fit(const DevOp& op)
+{
+    const int nz = op.it2;
+    const WallBlock& L = op.ax[2].wall[0];
+    const WallBlock& R = op.ax[2].wall[1];
+    if (nz < 8) return false;
+    if (L.rows && (L.has_n || L.rows > 6 || L.cols > 7 || L.first_row < 0 ||
+                   2 * (L.first_row + L.rows - 1) >= nz))
+        return false;
+    if (R.rows && (R.has_n || R.rows > 6 || R.cols > 7 || 2 * R.first_row < nz ||
+                   R.first_row + R.rows > nz))
+        return false;
+    return true;
+}
+
 // Pick the mixed stage kernel for this system: every candidate runs a few RK4 steps on the
 // system's own buffers (timed with CUDA events), the fastest is kept, and the state is reset.
 // All candidates compute the same values; they differ only in data movement.
@@ -514,7 +533,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         const bool wave = S->desc.kind == SHOCCS_SYS_WAVE;
         if (wave ? form != FORM_ANTI5 : (form != FORM_SYM5 && form != FORM_W3)) form = FORM_ANY;
     }
-    if (S->P->comp.it[2] % 4 == 0 && S->b.rowv && S->b.zwall && form != FORM_ANY) {
+    if (S->P->comp.it[2] % 4 == 0 && S->b.rowv && S->b.lrec && form != FORM_ANY) {
         cands.push_back({"vec", 0, 0, form, 4});
         cands.push_back({"vec3", 0, 0, form, 3});
     }
@@ -724,16 +743,15 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         // the trial steps of the autotuner need every register allocated and zeroed; the
         // column and vectorised kernels index with 32-bit integers
         if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
-            // the cut-row kernel runs one thread per cut-cell row and per z line
+            // the vectorised stage: cut-cell row values at their points, line records; the
+            // cut-row kernel runs one thread per cut-cell row and per z line
             const long long nthreads = (long long)it[0] * it[1] + p->op.n_cut_rows;
-            if (it[2] % 4 == 0 && nthreads < (1LL << 31) - 256) {
+            if (it[2] % 4 == 0 && line_records_fit(p->op) && nthreads < (1LL << 31) - 256) {
                 void* z = nullptr;
                 SH_CUDA(S->mem.alloc((size_t)3 * N * sizeof(float), &z));
                 S->b.rowv = (float*)z;
-                const WallBlock* W = p->op.ax[2].wall;
-                const size_t nzw = (size_t)it[0] * it[1] * (W[0].rows + W[1].rows);
-                SH_CUDA(S->mem.alloc(std::max<size_t>(nzw, 1) * sizeof(float), &z));
-                S->b.zwall = (float*)z;
+                SH_CUDA(S->mem.alloc((size_t)it[0] * it[1] * 16 * sizeof(float), &z));
+                S->b.lrec = (float*)z;
             }
             if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;
         }

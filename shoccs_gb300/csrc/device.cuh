@@ -114,12 +114,12 @@ struct StepBuffers {
     // column-blocked mixed stages (3-D grids): planes per thread, 0 = per-point kernel
     int col_nx = 0;
     // vectorised mixed stages (3-D grids, nz a multiple of 4): the cut-cell row values they
-    // read, at their points (3 x N floats, axis-major), and the z-wall row values
-    // (wall[0].rows + wall[1].rows slots x z lines, slot-major)
+    // read, at their points (3 x N floats, axis-major), and the line records (z-wall rows
+    // and z-face values of every z line, 16 floats per line)
     int vec = 0;      // stencil form (FORM_*) of the vectorised kernel, 0 = not used
     int vec_minb = 4; // its resident blocks per SM (4: 64 registers, 3: 85 registers)
     float* rowv = nullptr;
-    float* zwall = nullptr;
+    float* lrec = nullptr;
     unsigned* err = nullptr;
     // exact values on the Dirichlet domain faces (mixed path): per face (x lo, x hi, y lo,
     // y hi, z lo, z hi; null where the face is not Dirichlet) a plane of {FP32 value at

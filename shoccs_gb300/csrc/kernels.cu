@@ -74,6 +74,17 @@ __device__ __forceinline__ float2 ld_pair(const void* u0, long long n, long long
     const float* h = (const float*)u0;
     return make_float2(h[i], h[n + i]);
 }
+// The u0 words a mixed RK4 stage reads: stages 0-2 form the next FP32 stage field from the
+// hi word alone (one FP32 rounding of hi + c dt rhs; the lo word is below half an ulp of hi),
+// only stage 3, which adds the step's increment to the pair, reads the lo word.
+template <int STAGE>
+__device__ __forceinline__ float2 ld_u0(const void* u0, long long n, long long i)
+{
+    if constexpr (STAGE == 3)
+        return ld_pair(u0, n, i);
+    else
+        return make_float2(((const float*)u0)[i], 0.f);
+}
 __device__ __forceinline__ void st_pair(void* u0, long long n, long long i, float2 v)
 {
     float* h = (float*)u0;
@@ -530,7 +541,7 @@ struct StageArgs {
     const void* cval;
     float* rowv;            // vectorised mixed stages: cut-cell row values of the stage at
                             // their points, axis-major (3 x N), or null
-    float* zw;              // and the z-wall row values, slot-major (slot x z lines)
+    float* lrec;            // and the line records (16 words per z line, k_cut_rows)
     const float4* fplane[6]; // Dirichlet face values of the step (mixed path), see StepBuffers
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
@@ -543,7 +554,7 @@ struct StageArgs {
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 
 // z-wall rows: slot of the row of z coordinate k (the left block's rows, then the right
-// block's) in the slot-major table of the vectorised stage
+// block's) in the slot-major table of the vectorised operators
 __device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
 {
     return k * 2 < A.n ? k - A.wall[0].first_row : A.wall[0].rows + (k - A.wall[1].first_row);
@@ -552,15 +563,48 @@ __device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
 // cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b] (FP64 path: FP64; mixed path:
 // compensated FP32, closure_ff), stored compacted in row order (cval) or -- for the
 // vectorised mixed stage -- scattered to their points in rowv (3 x N, axis-major), where a
-// lane finds its value with one load at its own index.  With rowv, threads past the cut-cell
-// rows also evaluate the domain-wall rows of the z axis (FP32, wall32's arithmetic) into the
-// slot-major table zw (consecutive lines at consecutive addresses): those rows sit at both
-// ends of every z line, i.e. in some lane of every warp of that kernel.  One thread per z
-// line reads the line's end values once for both wall blocks.
+// lane finds its value with one load at its own index.
+//
+// With line records (lrec), threads past the cut-cell rows each fill the 16-word record of
+// one z line for the vectorised stage: words 0..5 the line's left z-wall rows (coordinate
+// first_row + w, wall32's arithmetic), 6..7 the stage output's value at the line's first
+// point where that point is on a Dirichlet face (face_entry, face_pick), 8..13 and 14..15
+// the same for the right wall and the last point.  The record is written as four aligned
+// float4s, and the stage kernel reads it with one load per lane at entry: it needs no class
+// byte to know where the words are.
+// plane entry of the face point (i, j, k): the first Dirichlet face that holds it (every
+// face holding it has the same values)
+__device__ __forceinline__ const float4* face_entry(const StageArgs& sa, const DevOp& op, int i,
+                                                    int j, int k)
+{
+    const int ijk[3] = {i, j, k};
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        const int a = f >> 1;
+        if (!sa.fplane[f] || ijk[a] != ((f & 1) ? op.n[a] - 1 : 0)) continue;
+        const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        return sa.fplane[f] + (ijk[b] * op.n[c] + ijk[c]);
+    }
+    return nullptr;
+}
+
+// the words of a face entry that the stage output takes: the FP32 value at t+dt/2 (stages 0,
+// 1), at t+dt (stage 2), the hi and lo words of the value at t+dt (stage 3, the solution)
+template <int STAGE>
+__device__ __forceinline__ float2 face_pick(const float4* f)
+{
+    if constexpr (STAGE < 2)
+        return make_float2(f->x, 0.f);
+    else if constexpr (STAGE == 2)
+        return make_float2(f->y, 0.f);
+    else
+        return make_float2(f->z, f->w);
+}
+
 template <class TIN, class TOUT>
 __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
                            const double* R1, const double* R2, TOUT* __restrict__ cval,
-                           float* __restrict__ rowv, float* __restrict__ zw)
+                           float* __restrict__ rowv, StageArgs sa, int stage)
 {
     pdl_wait();
     pdl_trigger();
@@ -569,11 +613,13 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
         if constexpr (!std::is_same<TIN, const double*>::value) {
             const int line = i - op.n_cut_rows;
             const int nlines = op.it0 * op.it1;
-            if (!zw || line >= nlines) return;
+            if (!sa.lrec || line >= nlines) return;
             const DevAxis& A = op.ax[2];
-            const long long base = (long long)line * op.it2;
-            float* __restrict__ out = zw + line;
-            int slot = 0;
+            const int nz = op.it2;
+            const long long base = (long long)line * nz;
+            float w[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) w[m] = 0.f;
 #pragma unroll
             for (int side = 0; side < 2; side++) {
                 const WallBlock& W = A.wall[side];
@@ -581,14 +627,32 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
 #pragma unroll
                 for (int jj = 0; jj < 7; jj++)
                     x[jj] = jj < W.cols ? ldf(u, base + W.col0 + jj) : 0.f;
-                for (int r = 0; r < W.rows; r++, slot++) {
+#pragma unroll
+                for (int r = 0; r < 6; r++) {
+                    if (r >= W.rows) continue;
                     float acc = 0.f; // wall32's operation order
 #pragma unroll
                     for (int jj = 0; jj < 7; jj++)
                         if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
-                    out[(long long)slot * nlines] = acc; // read only where the row is a wall row
+                    w[side * 8 + r] = acc;
                 }
             }
+            const int li = line / op.it1, lj = line - li * op.it1;
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                const float4* f = face_entry(sa, op, li, lj, side ? nz - 1 : 0);
+                if (!f) continue;
+                const float2 fv = stage == 0   ? face_pick<0>(f)
+                                  : stage == 1 ? face_pick<1>(f)
+                                  : stage == 2 ? face_pick<2>(f)
+                                               : face_pick<3>(f);
+                w[side * 8 + 6] = fv.x;
+                w[side * 8 + 7] = fv.y;
+            }
+            float4* o = (float4*)(sa.lrec + (long long)line * 16);
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+                o[m] = make_float4(w[4 * m], w[4 * m + 1], w[4 * m + 2], w[4 * m + 3]);
         }
         return;
     }
@@ -814,8 +878,9 @@ __device__ __forceinline__ float rhs_mixed(const DevOp& op, const SysParams& sp,
 }
 
 // RK4 register update of one point of the mixed path: the increment dt*b_s*rhs with the
-// weight held as an FP32 pair; stages 0-2 write the accumulator and the next stage field,
-// stage 3 adds the accumulated increment to the (hi, lo) solution by an error-free two-sum.
+// weight held as an FP32 pair; stages 0-2 write the accumulator and the next stage field
+// fl(hi + c dt rhs) (one rounding; u.y is not read), stage 3 adds the accumulated increment
+// to the (hi, lo) solution by an error-free two-sum.
 template <int STAGE>
 __device__ __forceinline__ void rk_mixed(const StageArgs& sa, float rhs, float2 u, float accv,
                                          float& acc_out, float& s_out, float2& u_out)
@@ -823,7 +888,7 @@ __device__ __forceinline__ void rk_mixed(const StageArgs& sa, float rhs, float2 
     const float inc = fmaf(sa.cf_ff.x, rhs, __fmul_rn(sa.cf_ff.y, rhs));
     if constexpr (STAGE < 3) {
         acc_out = STAGE == 0 ? inc : __fadd_rn(accv, inc);
-        s_out = __fadd_rn(u.x, fmaf(sa.ci_ff.x, rhs, u.y));
+        s_out = fmaf(sa.ci_ff.x, rhs, u.x);
     } else {
         const float a = __fadd_rn(accv, inc);
         const float2 t = two_sum(u.x, a);
@@ -883,7 +948,7 @@ __device__ __forceinline__ void stage_mixed_at(const DevOp& op, const SysParams&
     float* __restrict__ acc = (float*)sa.acc;
     float a_out = 0.f, s_out = 0.f;
     float2 u_out;
-    rk_mixed<STAGE>(sa, rhs, ld_pair(sa.u0, op.N, q.p), STAGE == 0 ? 0.f : acc[q.p], a_out,
+    rk_mixed<STAGE>(sa, rhs, ld_u0<STAGE>(sa.u0, op.N, q.p), STAGE == 0 ? 0.f : acc[q.p], a_out,
                     s_out, u_out);
     if constexpr (STAGE < 3) {
         acc[q.p] = a_out;
@@ -962,7 +1027,7 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
         yv[t][0] = L(p + ym2); yv[t][1] = L(p + ym1); yv[t][2] = L(p + yp1); yv[t][3] = L(p + yp2);
         zv[t][0] = L(p + zm2); zv[t][1] = L(p + zm1); zv[t][2] = L(p + zp1); zv[t][3] = L(p + zp2);
         if constexpr (STAGE > 0) {
-            uu[t] = ld_pair(sa.u0, op.N, p);
+            uu[t] = ld_u0<STAGE>(sa.u0, op.N, p);
             av[t] = ((const float*)sa.acc)[p];
         }
     }
@@ -1012,7 +1077,7 @@ __global__ void __launch_bounds__(256) k_stage_mixed_col(DevOp op, SysParams sp,
         float a_out = 0.f, s_out = 0.f;
         float2 u_out;
         if constexpr (STAGE == 0)
-            rk_mixed<STAGE>(sa, rhs, ld_pair(sa.u0, op.N, p), 0.f, a_out, s_out, u_out);
+            rk_mixed<STAGE>(sa, rhs, ld_u0<STAGE>(sa.u0, op.N, p), 0.f, a_out, s_out, u_out);
         else
             rk_mixed<STAGE>(sa, rhs, uu[t], av[t], a_out, s_out, u_out);
         if constexpr (STAGE < 3) {
@@ -1058,22 +1123,6 @@ __device__ float face_f32(const DevOp& op, const DevSol& sol, double t, double e
     return (float)sol_at_point(op, sol, t, et, ijk);
 }
 
-// plane entry of the face point (i, j, k): the first Dirichlet face that holds it (every
-// face holding it has the same values)
-__device__ __forceinline__ const float4* face_entry(const StageArgs& sa, const DevOp& op, int i,
-                                                    int j, int k)
-{
-    const int ijk[3] = {i, j, k};
-#pragma unroll
-    for (int f = 0; f < 6; f++) {
-        const int a = f >> 1;
-        if (!sa.fplane[f] || ijk[a] != ((f & 1) ? op.n[a] - 1 : 0)) continue;
-        const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
-        return sa.fplane[f] + (ijk[b] * op.n[c] + ijk[c]);
-    }
-    return nullptr;
-}
-
 // face values of the stage output from the planes, for the stage kernels without the
 // face write fused in
 template <int STAGE>
@@ -1098,20 +1147,26 @@ __global__ void k_faces_mixed(DevOp op, StageArgs sa)
 // ---- vectorised mixed stage (3-D grids, nz a multiple of 4) --------------------------------
 // A thread owns four consecutive z points of one x plane, so a warp covers 128 points of one
 // z line and every field moves as float4 (stage input, class bytes as one 32-bit word, the
-// hi and lo planes of u0, accumulator).  The z neighbours come from the float4s on either
-// side, the y neighbours from the float4s of rows j-2..j+2, the x neighbours from those of
-// planes i-2..i+2; all loads are issued before any class byte is decoded, with coordinates
-// clamped into the grid so they stay in bounds.  Per axis every point evaluates its interior
-// row from these registers and keeps it where the row is interior (points without a row
-// contribute 0); only warps that hold a cut-cell or wall row along that axis branch.  There,
-// cut-cell rows are found from the chunk's prefix count plus the rank among the chunk's
-// cut-cell points (lanes 8s..8s+7 hold the 32-point chunk s of the warp, four ballots give
-// the rank); x- and y-wall rows (whole planes / rows, uniform across a warp) are evaluated
-// from global memory.  z-wall rows sit at both ends of every z line, i.e. in a few lanes of
-// every warp; those lanes read them from the table that k_cut_rows fills, without a vote.  FORM fixes the interior stencil (5-point antisymmetric,
-// 5-point symmetric, 3-point) and VK the velocity field of the wave system (constant or
-// radial), so the per-point code has no run-time branch on either.  The arithmetic of each
-// point is the per-point kernel's, operation for operation.
+// hi plane of u0 and, in stage 3, its lo plane, accumulator).  The z neighbours come from
+// the float4s on either side, the y neighbours from the float4s of rows j-2..j+2, the x
+// neighbours from those of planes i-2..i+2; all loads are issued before any class byte is
+// decoded, with coordinates clamped into the grid so they stay in bounds.  Per axis every
+// point evaluates its interior row from these registers and keeps it where the row is
+// interior (points without a row contribute 0).  The rows that are not interior cost each
+// warp at most one extra round trip to memory, overlapped with the stencil loads where the
+// position alone says what is needed:
+//  * cut-cell rows: one load at the point's own index of the dense per-axis value array that
+//    k_cut_rows fills, issued as soon as the class word arrives;
+//  * x- and y-wall rows (whole planes / rows, uniform across a warp): the wall block's
+//    columns of the four points as float4s, all in one round trip;
+//  * z-wall rows (a lane or two at either end of every line): from the z window already in
+//    registers (zwall_row), no load at all;
+//  * Dirichlet z-face points (the first and last point of a line): their values are loaded
+//    with the stencil inputs; x- and y-face planes (uniform across a warp) after the update.
+// FORM fixes the interior stencil (5-point antisymmetric, 5-point symmetric, 3-point) and VK
+// the velocity field of the wave system (constant or radial), so the per-point code has no
+// run-time branch on either.  The arithmetic of each point is the per-point kernel's,
+// operation for operation.
 template <int FORM>
 __device__ __forceinline__ float interior_row_t(const DevAxis& A, float m2, float m1, float c0,
                                                 float p1, float p2)
@@ -1174,10 +1229,15 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     const float4 zL = ld4(in, p + zl), zR = ld4(in, p + zr);
     const float* __restrict__ u0 = (const float*)sa.u0;
     const float4 uh = STAGE == 0 ? C : *(const float4*)(u0 + p);
-    const float4 ul = *(const float4*)(u0 + op.N + p);
     float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
     if constexpr (STAGE > 0) av = *((const float4*)((const float*)sa.acc + p));
     const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
+    // the line record (k_cut_rows): words 0..7 on lanes 0..7 of the warp that holds the
+    // line's first point, words 8..15 on lanes 8..15 of the one that holds its last point
+    const bool rec_l = blockIdx.x == 0, rec_r = blockIdx.x + 1 == gridDim.x;
+    const float rec = (lane < 8 ? rec_l : (lane < 16 && rec_r))
+                          ? __ldg(sa.lrec + (long long)(i * ny + j) * 16 + lane)
+                          : 0.f;
 
     float v[3][4];
     unsigned kq[3][4];
@@ -1200,6 +1260,9 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
         v[1][q] = kq[1][q] == ROW_INTERIOR ? sy : 0.f;
         v[2][q] = kq[2][q] == ROW_INTERIOR ? sz : 0.f;
     }
+    // the lo plane of u0 (stage 3 only) is loaded here, after the stencil registers are
+    // free: issued before it, it pushed stage 3 past the 64-register budget
+    const float4 ul = STAGE == 3 ? *(const float4*)(u0 + op.N + p) : make_float4(0.f, 0.f, 0.f, 0.f);
     if (cut) { // cut-cell rows: one load each, at the point's own index
         const float* __restrict__ rv = sa.rowv + p;
 #pragma unroll
@@ -1208,13 +1271,16 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
             for (int q = 0; q < 4; q++)
                 if (kq[d][q] == ROW_CLOSURE) v[d][q] = rv[d * op.N + q];
     }
-    if (zwall) { // z-wall rows (lanes at the ends of a line): the lane's slots are consecutive
-        const long long nlines = (long long)nx * ny;
-        const float* __restrict__ zt =
-            sa.zw + (long long)zwall_slot(op.ax[2], k) * nlines + (i * ny + j);
+    if (__any_sync(FULL, zwall)) { // z-wall rows: the record word of each row to its lane
+        const DevAxis& A = op.ax[2];
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (kq[2][q] == ROW_WALL) v[2][q] = zt[q * nlines];
+        for (int q = 0; q < 4; q++) {
+            const int kk = k + q;
+            const bool use = kq[2][q] == ROW_WALL;
+            const int w = kk * 2 < nz ? kk - A.wall[0].first_row : 8 + kk - A.wall[1].first_row;
+            const float val = __shfl_sync(FULL, rec, use ? w : 0);
+            if (use) v[2][q] = val;
+        }
     }
     if (__any_sync(FULL, xywall)) { // whole x / y wall planes: uniform across the warp
 #pragma unroll
@@ -1224,7 +1290,6 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
                 if (kq[d][q] == ROW_WALL)
                     v[d][q] = wall32(op.ax[d], (long long)(p + q), d == 0 ? i : j, in);
     }
-    if (!kvalid) return;
     float ao[4], so[4];
     float2 uo[4];
 #pragma unroll
@@ -1242,19 +1307,28 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
         rk_mixed<STAGE>(sa, rhs, make_float2(f4(uh, q), f4(ul, q)), f4(av, q), ao[q], so[q],
                         uo[q]);
     }
+    // the z-face values of the line's first and last point (record words 6, 7 and 14, 15);
+    // every lane takes part in the shuffles, lanes past the line's end store nothing
+    const int fw = k == 0 ? 6 : 14;
+    const float fa = __shfl_sync(FULL, rec, fw);
+    const float fb = STAGE == 3 ? __shfl_sync(FULL, rec, fw + 1) : 0.f;
+    if (!kvalid) return;
     if (c4 & 0x40404040u) { // Dirichlet face points (whole planes, or one lane of a line)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (!((c4 >> (8 * q)) & CLS_DIRFACE)) continue;
-            const float4* f = face_entry(sa, op, i, j, k + q);
-            if (!f) continue;
-            const float4 fv = *f;
-            if constexpr (STAGE < 2)
+            float2 fv;
+            if ((q == 0 && k == 0) || (q == 3 && k + 4 == nz)) {
+                fv = make_float2(fa, fb); // z faces: from the line record
+            } else {                      // x / y face planes, uniform across the warp
+                const float4* f = face_entry(sa, op, i, j, k + q);
+                if (!f) continue;
+                fv = face_pick<STAGE>(f);
+            }
+            if constexpr (STAGE < 3)
                 so[q] = fv.x;
-            else if constexpr (STAGE == 2)
-                so[q] = fv.y;
             else
-                uo[q] = make_float2(fv.z, fv.w);
+                uo[q] = fv;
         }
     }
     if constexpr (STAGE < 3) {
@@ -1347,14 +1421,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b)
 // flag, stops issuing copies, and drains the ones in flight before it returns.
 //
 // Slot layout: stage-field plane with halo (FP32; the hi plane of u0 in stage 0), class
-// bytes, hi tile of u0 (stages 1-3; stage 0 has it in the halo plane), lo tile of u0,
-// accumulator tile (stages 1-3).
+// bytes, hi tile of u0 (stages 1-3; stage 0 has it in the halo plane), lo tile of u0
+// (stage 3), accumulator tile (stages 1-3).
 template <int STAGE>
 struct TmaSlot {
     static constexpr unsigned S = TMA_BY * TMA_BZ * 4u;
     static constexpr unsigned C = TMA_TY * TMA_TZ;
     static constexpr unsigned UH = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
-    static constexpr unsigned UL = TMA_TY * TMA_TZ * 4u;
+    static constexpr unsigned UL = STAGE == 3 ? TMA_TY * TMA_TZ * 4u : 0u;
     static constexpr unsigned A = STAGE == 0 ? 0u : TMA_TY * TMA_TZ * 4u;
     static constexpr unsigned BYTES = S + C + UH + UL + A;
     static_assert(BYTES % 128 == 0 && S % 128 == 0 && C % 128 == 0 && UH % 128 == 0 &&
@@ -1418,8 +1492,9 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
                     tma_load_3d(base + S_BYTES, &tm_cls, k0, j0, pl, &full[slot]);
                     if (STAGE > 0)
                         tma_load_3d(base + S_BYTES + C_BYTES, &tm_u0h, k0, j0, pl, &full[slot]);
-                    tma_load_3d(base + S_BYTES + C_BYTES + L::UH, &tm_u0l, k0, j0, pl,
-                                &full[slot]);
+                    if (STAGE == 3)
+                        tma_load_3d(base + S_BYTES + C_BYTES + L::UH, &tm_u0l, k0, j0, pl,
+                                    &full[slot]);
                     if (STAGE > 0)
                         tma_load_3d(base + S_BYTES + C_BYTES + L::UH + L::UL, &tm_acc, k0, j0,
                                     pl, &full[slot]);
@@ -1477,7 +1552,7 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
             float2 u;
             float accv = 0.f;
             u.x = STAGE == 0 ? Sc[0] : reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES)[t_off];
-            u.y = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + L::UH)[t_off];
+            u.y = STAGE == 3 ? reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + L::UH)[t_off] : 0.f;
             if constexpr (STAGE > 0)
                 accv = reinterpret_cast<const float*>(cur + S_BYTES + C_BYTES + L::UH + L::UL)[t_off];
             float lap = 0.f;
@@ -2127,25 +2202,28 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
     const dim3 grid = point_grid(op), block(32, BY);
     const bool mixed = prec == PREC_MIXED;
     float* rowv = mixed && b.vec ? a.rowv : nullptr;
-    float* zw = mixed && b.vec ? a.zw : nullptr;
-    const long long n_zw = zw ? (long long)op.it0 * op.it1 : 0; // one thread per z line
-    if (op.n_cut_rows || n_zw) {
-        const int nb = (int)((op.n_cut_rows + n_zw + 127) / 128);
+    // the vectorised stage's line records (one thread per z line after the cut-cell rows);
+    // they hold face values, so the boundary values of the step must be ready first
+    StageArgs ca = a;
+    ca.lrec = mixed && b.vec ? a.lrec : nullptr;
+    const long long n_lines = ca.lrec ? (long long)op.it0 * op.it1 : 0;
+    if (join) cudaStreamWaitEvent(s, join, 0); // boundary values of the step are ready
+    if (op.n_cut_rows || n_lines) {
+        const int nb = (int)((op.n_cut_rows + n_lines + 127) / 128);
         const double* const* R = a.R;
         if (!mixed)
             launch_ex(k_cut_rows<const double*, double>, dim3(nb), dim3(128), s, true, op,
                       (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
-                      (double*)a.cval, nullptr, nullptr);
+                      (double*)a.cval, nullptr, ca, STAGE);
         else if (STAGE == 0)
             launch_ex(k_cut_rows<PairU, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
                       PairU{(const float*)a.u0, op.N}, R[0], R[1], R[2], (float*)a.cval, rowv,
-                      zw);
+                      ca, STAGE);
         else
             launch_ex(k_cut_rows<const float*, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
-                      (const float*)a.s_in, R[0], R[1], R[2], (float*)a.cval, rowv, zw);
+                      (const float*)a.s_in, R[0], R[1], R[2], (float*)a.cval, rowv, ca, STAGE);
         ++g_launches;
     }
-    if (join) cudaStreamWaitEvent(s, join, 0); // boundary values of the step are ready
     if (ev) cudaEventRecord(ev[0], s);
     const bool small = op.N < (1LL << 31) - 64;
     if (mixed && b.tma) {
@@ -2309,7 +2387,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.acc = b.acc;
         a.cval = b.cval;
         a.rowv = b.rowv;
-        a.zw = b.zwall;
+        a.lrec = b.lrec;
         for (int f = 0; f < 6; f++) a.fplane[f] = b.fplane[f];
         a.s_in = i == 0 ? b.u0 : (i == 2 ? b.sb : b.sa);
         a.s_out = i == 1 ? b.sb : b.sa;
