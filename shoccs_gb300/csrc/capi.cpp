@@ -996,7 +996,7 @@ struct shoccs_batch {
     BatchInst* d_inst = nullptr;
     const int* d_row_inst = nullptr;
     int n_rows = 0;
-    const int2* d_tiles[4] = {};
+    const int4* d_tiles[4] = {}; // (instance, it0 index, first it1 index, it2 chunk)
     int n_tiles[4] = {};
     const int* d_r_inst = nullptr;
     int n_r = 0;
@@ -1117,7 +1117,7 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
     int dev = 0;
     SH_CUDA(cudaGetDevice(&dev));
     std::vector<int> row_inst, r_inst;
-    std::vector<int2> tiles[4];
+    std::vector<int4> tiles[4];
     for (int i = 0; i < n; i++) {
         shoccs_system* S = systems[i];
         if (!S) return fail(SHOCCS_EINVAL, "null system");
@@ -1146,10 +1146,16 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         row_inst.insert(row_inst.end(), op.n_cut_rows, i);
         for (int c = 0; c < 4; c++) {
             const int w = BATCH_TILE_WARPS[c];
-            const long long nt = (long long)op.nzc * ((op.it1 + w - 1) / w) * op.it0;
+            const int nyb = (op.it1 + w - 1) / w;
+            const long long nt = (long long)op.nzc * nyb * op.it0;
             if ((long long)tiles[c].size() + nt >= (1LL << 31))
                 return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 tiles");
-            for (long long t = 0; t < nt; t++) tiles[c].push_back(make_int2(i, (int)t));
+            // tile t of the instance: it2 chunk t % nzc, it1 block of w rows, it0 index
+            for (long long t = 0; t < nt; t++) {
+                const long long rest = t / op.nzc;
+                tiles[c].push_back(make_int4(i, (int)(rest / nyb), (int)(rest % nyb) * w,
+                                             (int)(t % op.nzc)));
+            }
         }
         for (int d = 0; d < 3; d++)
             for (long long k = 0; k < op.nR[d]; k++) {

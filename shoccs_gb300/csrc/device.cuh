@@ -172,10 +172,10 @@ constexpr int BATCH_TILE_WARPS[4] = {1, 2, 4, 8};
 // one RK4 step of every instance: per stage, the cut-cell rows of all instances, then the
 // stage update of all instances (persistent blocks over the (instance, tile) list)
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
-                              const int2* tiles, int n_tiles, int tile_cfg, int grid,
+                              const int4* tiles, int n_tiles, int tile_cfg, int grid,
                               const BatchTime* times, int prec, cudaStream_t s);
 // one stage-1 pass (timing probe of a tile shape for the autotuner)
-cudaError_t launch_batch_probe(const BatchInst* inst, const int2* tiles, int n_tiles,
+cudaError_t launch_batch_probe(const BatchInst* inst, const int4* tiles, int n_tiles,
                                int tile_cfg, int grid, const BatchTime* times, int prec,
                                cudaStream_t s);
 // persistent grid size of the batched stage kernel for a tile shape

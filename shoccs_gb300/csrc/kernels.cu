@@ -2587,22 +2587,21 @@ __global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restr
 
 template <int STAGE, bool MIXED, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_batch_stage(const BatchInst* __restrict__ B,
-                                                            const int2* __restrict__ tiles,
+                                                            const int4* __restrict__ tiles,
                                                             int n_tiles,
                                                             const BatchTime* __restrict__ bt)
 {
     pdl_wait();
     pdl_trigger();
     for (int T = blockIdx.x; T < n_tiles; T += gridDim.x) {
-        const int2 tl = tiles[T]; // (instance, tile within the instance)
+        const int4 tl = __ldg(tiles + T); // (instance, it0 index, first it1 index, it2 chunk)
         const BatchInst& I = B[tl.x];
         const DevOp& op = I.op;
-        const int nyb = (op.it1 + WARPS - 1) / WARPS;
-        const int bx = tl.y % op.nzc, rest = tl.y / op.nzc;
+        const int bx = tl.w;
         StagePt<int> q;
         q.c = bx * 32 + threadIdx.x;
-        q.b = (rest % nyb) * WARPS + threadIdx.y;
-        q.a = rest / nyb;
+        q.b = tl.z + threadIdx.y;
+        q.a = tl.y;
         q.valid = (q.b < op.it1) && (q.c < op.it2);
         const int line = q.a * op.it1 + q.b;
         q.p = line * op.it2 + q.c;
@@ -2656,7 +2655,7 @@ __global__ void k_batch_finish(const BatchInst* __restrict__ B, const BatchTime*
 }
 
 template <int STAGE, bool MIXED>
-void batch_stage(const BatchInst* inst, const int2* tiles, int n_tiles, int cfg, int grid,
+void batch_stage(const BatchInst* inst, const int4* tiles, int n_tiles, int cfg, int grid,
                  const BatchTime* times, cudaStream_t s)
 {
     switch (cfg) {
@@ -2669,7 +2668,7 @@ void batch_stage(const BatchInst* inst, const int2* tiles, int n_tiles, int cfg,
 }
 
 template <bool MIXED>
-void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const int2* tiles,
+void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const int4* tiles,
                 int n_tiles, int cfg, int grid, const BatchTime* times, cudaStream_t s)
 {
     const int nb = (n_rows + 127) / 128;
@@ -2685,7 +2684,7 @@ void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const in
 } // namespace
 
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
-                              const int2* tiles, int n_tiles, int tile_cfg, int grid,
+                              const int4* tiles, int n_tiles, int tile_cfg, int grid,
                               const BatchTime* times, int prec, cudaStream_t s)
 {
     if (prec == PREC_MIXED)
@@ -2695,7 +2694,7 @@ cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_probe(const BatchInst* inst, const int2* tiles, int n_tiles,
+cudaError_t launch_batch_probe(const BatchInst* inst, const int4* tiles, int n_tiles,
                                int tile_cfg, int grid, const BatchTime* times, int prec,
                                cudaStream_t s)
 {
