@@ -1,0 +1,611 @@
+// shoccs_gb300.hpp -- C++20 classes with the reference's names over the C ABI (shoccs_gpu.h).
+//
+// pbrady/shoccs exposes its derivative-operator path as C++ classes; this header gives a
+// caller of those classes the same names, constructor arguments, call shapes and error
+// behaviour, backed by the sm_103a library:
+//
+//   ccs::mesh                 src/mesh/mesh.hpp:24-31 (index_extents, domain_extents, shapes)
+//   ccs::make_sphere          src/mesh/shapes.hpp:123
+//   ccs::stencils::make_E2_2 / make_E4_2 / make_E4_1 / make_E4u_1
+//                             src/stencils/stencil.hpp:275-279
+//   ccs::bcs::{type, Line, Grid, Object, dd, df, ...}   src/operators/boundaries.hpp:11-47
+//   ccs::eq / ccs::plus_eq    src/types.hpp:69-86
+//   ccs::derivative           src/operators/derivative.hpp:20-80
+//   ccs::laplacian            src/operators/laplacian.hpp:10-33
+//   ccs::gradient             src/operators/gradient.hpp:10-30
+//   ccs::systems::heat        src/systems/heat.hpp:16-70
+//   ccs::systems::scalar_wave src/systems/scalar_wave.hpp:16-80
+//   ccs::integrators::rk4     src/temporal/rk4.hpp:10-20
+//
+// Differences a caller sees.  Fields are device buffers (scalar_span / scalar_view hold
+// device pointers and sizes), because the kernels run on the GPU; the reference's fields are
+// host Kokkos views.  Systems own their state on the device (the reference keeps it in a
+// sim_registry slot), so rk4 takes the system, the time and the step size.  Failures throw
+// ccs::error (a std::runtime_error carrying the library's status and message) where the
+// reference returns std::nullopt from from_lua or asserts; make_E4_1 throws
+// std::invalid_argument for alpha[1] < 197/288 exactly as src/stencils/E4_1.cpp:37-40 does.
+// Every call returns after the stream has finished, like the reference's Kokkos::fence.
+#pragma once
+
+#include "shoccs_gpu.h"
+
+#include <array>
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <span>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace ccs
+{
+using real = double;
+using real3 = std::array<real, 3>;
+using int3 = std::array<int, 3>;
+using integer = std::int64_t;
+
+// thrown for every non-OK status of the C ABI
+class error : public std::runtime_error
+{
+    shoccs_status status_;
+
+public:
+    error(shoccs_status s, const std::string& what) : std::runtime_error(what), status_{s} {}
+    shoccs_status status() const { return status_; }
+};
+
+namespace detail
+{
+inline void check(shoccs_status s, const char* call)
+{
+    if (s == SHOCCS_OK) return;
+    char buf[512] = {};
+    shoccs_last_error(buf, sizeof(buf));
+    throw error(s, std::string(call) + ": " + buf);
+}
+} // namespace detail
+
+// ---- index / domain extents, shapes (src/index_extents.hpp:9-19, src/mesh/mesh_types.hpp:25-28)
+struct index_extents {
+    int3 extents;
+    constexpr operator const int3&() const { return extents; }
+    constexpr integer size() const { return (integer)extents[0] * extents[1] * extents[2]; }
+};
+
+struct domain_extents {
+    real3 min;
+    real3 max;
+};
+
+// the embedded shapes this path supports: spheres (circles in 2-D)
+struct shape {
+    int id;
+    real3 origin;
+    real radius;
+};
+
+inline shape make_sphere(int id, const real3& origin, real radius) { return {id, origin, radius}; }
+
+// ---- boundary conditions (src/operators/boundaries.hpp:11-47) -------------------------------
+namespace bcs
+{
+enum class type { Dirichlet, D = Dirichlet, Floating, F = Floating, Neumann, N = Neumann };
+
+constexpr auto Dirichlet = type::Dirichlet;
+constexpr auto Neumann = type::Neumann;
+constexpr auto Floating = type::Floating;
+
+struct Line {
+    type left;
+    type right;
+    friend auto operator<=>(const Line&, const Line&) = default;
+};
+
+using X = Line;
+using Y = Line;
+using Z = Line;
+using Grid = std::array<Line, 3>;
+using Object = std::vector<type>;
+
+constexpr auto dd = Line{type::D, type::D};
+constexpr auto ff = Line{type::F, type::F};
+constexpr auto nn = Line{type::N, type::N};
+constexpr auto dn = Line{type::D, type::N};
+constexpr auto nd = Line{type::N, type::D};
+constexpr auto df = Line{type::D, type::F};
+constexpr auto fd = Line{type::F, type::D};
+constexpr auto fn = Line{type::F, type::N};
+constexpr auto nf = Line{type::N, type::F};
+
+// bcs::type -> SHOCCS_BC_* (same order as the enum)
+constexpr int to_c(type t) { return static_cast<int>(t); }
+} // namespace bcs
+
+// ---- stencils (src/stencils/stencil.hpp:275-279) --------------------------------------------
+namespace stencils
+{
+struct stencil {
+    int scheme;                  // SHOCCS_SCHEME_*
+    std::array<real, 2> alpha{}; // E4_1 / E4u_1 closure parameters
+};
+
+inline stencil make_E2_2() { return {SHOCCS_SCHEME_E2_2, {}}; }
+inline stencil make_E4_2() { return {SHOCCS_SCHEME_E4_2, {}}; }
+
+namespace detail
+{
+// src/stencils/E4_1.cpp:37-40: the closure is unstable below this bound
+inline std::array<real, 2> e4_alpha(std::span<const real> a, const char* name)
+{
+    if (a.size() < 2) throw std::invalid_argument(std::string(name) + " needs two alpha values");
+    if (a[1] < 197.0 / 288.0)
+        throw std::invalid_argument(std::string(name) + ": alpha[1] must be >= 197/288");
+    return {a[0], a[1]};
+}
+} // namespace detail
+
+inline stencil make_E4_1(std::span<const real> alpha)
+{
+    return {SHOCCS_SCHEME_E4_1, detail::e4_alpha(alpha, "E4_1")};
+}
+inline stencil make_E4u_1(std::span<const real> alpha)
+{
+    return {SHOCCS_SCHEME_E4U_1, {alpha.size() > 0 ? alpha[0] : 0.0, alpha.size() > 1 ? alpha[1] : 0.0}};
+}
+} // namespace stencils
+using stencils::stencil;
+
+// ---- mesh (src/mesh/mesh.hpp:24-31) ---------------------------------------------------------
+// Geometry only; the cut points and line segments are built with the operators (by the
+// library, bit-exact with the reference's mesh) the first time a problem is created.
+class mesh
+{
+    index_extents ex_;
+    domain_extents bounds_;
+    std::vector<shape> shapes_;
+
+public:
+    mesh() = default;
+    mesh(const index_extents& extents, const domain_extents& bounds) : ex_{extents}, bounds_{bounds} {}
+    mesh(const index_extents& extents, const domain_extents& bounds, const std::vector<shape>& shapes)
+        : ex_{extents}, bounds_{bounds}, shapes_{shapes}
+    {
+    }
+    const index_extents& extents() const { return ex_; }
+    const domain_extents& bounds() const { return bounds_; }
+    const std::vector<shape>& shapes() const { return shapes_; }
+    integer size() const { return ex_.size(); }
+    int dims() const
+    {
+        return (ex_.extents[0] > 1) + (ex_.extents[1] > 1) + (ex_.extents[2] > 1);
+    }
+    real h(int i) const
+    {
+        return ex_.extents[i] > 1 ? (bounds_.max[i] - bounds_.min[i]) / (ex_.extents[i] - 1) : 0.0;
+    }
+    // flat index of (i, j, k), z fastest (src/mesh/mesh.hpp:64-68)
+    integer ic(int3 ijk) const
+    {
+        const auto& n = ex_.extents;
+        return (integer)ijk[0] * n[1] * n[2] + (integer)ijk[1] * n[2] + ijk[2];
+    }
+};
+
+// ---- fields (src/fields/scalar.hpp:13-67) -----------------------------------------------------
+// {D, Rx, Ry, Rz} as DEVICE pointers with their element counts.  The element type is double
+// for FP64 operators and systems, float for mixed-precision operators.
+template <typename T>
+struct scalar_ref {
+    std::span<T> D, Rx, Ry, Rz;
+};
+using scalar_span = scalar_ref<real>;
+using scalar_view = scalar_ref<const real>;
+using scalar_span_f = scalar_ref<float>;
+using scalar_view_f = scalar_ref<const float>;
+
+namespace detail
+{
+template <typename T>
+shoccs_field field(const scalar_ref<T>& s)
+{
+    auto p = [](auto sp) { return (void*)sp.data(); };
+    return {p(s.D), p(s.Rx), p(s.Ry), p(s.Rz)};
+}
+} // namespace detail
+
+// ---- assignment operators (src/types.hpp:69-86) ---------------------------------------------
+struct eq_t {
+    constexpr void operator()(real& a, real b) const { a = b; }
+};
+struct plus_eq_t {
+    constexpr void operator()(real& a, real b) const { a += b; }
+};
+inline constexpr eq_t eq{};
+inline constexpr plus_eq_t plus_eq{};
+
+// arithmetic of an operator or system (SHOCCS_PREC_*)
+enum class precision { fp64 = SHOCCS_PREC_FP64, mixed = SHOCCS_PREC_MIXED };
+
+// ---- the compiled operators of one (mesh, stencil, bcs) triple ------------------------------
+// derivative(x), derivative(y), derivative(z), laplacian, gradient and the systems of the
+// same triple share one library problem (the three axes' operators, built once).
+class problem
+{
+    std::shared_ptr<shoccs_problem> p_;
+    std::array<integer, 5> sizes_{};
+
+public:
+    problem() = default;
+    problem(const mesh& m, const stencil& st, const bcs::Grid& grid_bcs, const bcs::Object& object_bcs)
+    {
+        shoccs_problem_desc d{};
+        const auto& sh = m.shapes();
+        if (object_bcs.size() < sh.size())
+            throw std::invalid_argument("bcs::Object needs one boundary condition per shape");
+        std::vector<real> centers;
+        std::vector<real> radii;
+        std::vector<int> sbc;
+        for (std::size_t i = 0; i < sh.size(); i++) {
+            centers.insert(centers.end(), sh[i].origin.begin(), sh[i].origin.end());
+            radii.push_back(sh[i].radius);
+            sbc.push_back(bcs::to_c(object_bcs[i]));
+        }
+        for (int a = 0; a < 3; a++) {
+            d.n[a] = m.extents().extents[a];
+            d.lo[a] = m.bounds().min[a];
+            d.hi[a] = m.bounds().max[a];
+            d.grid_bc[2 * a] = bcs::to_c(grid_bcs[a].left);
+            d.grid_bc[2 * a + 1] = bcs::to_c(grid_bcs[a].right);
+        }
+        d.n_spheres = (int)sh.size();
+        d.centers = centers.data();
+        d.radii = radii.data();
+        d.sphere_bc = sbc.data();
+        d.scheme = st.scheme;
+        d.alpha[0] = st.alpha[0];
+        d.alpha[1] = st.alpha[1];
+        shoccs_problem* raw = nullptr;
+        detail::check(shoccs_problem_create(&d, &raw), "shoccs_problem_create");
+        p_.reset(raw, [](shoccs_problem* q) { shoccs_problem_destroy(q); });
+        int64_t s[5];
+        detail::check(shoccs_problem_sizes(raw, s), "shoccs_problem_sizes");
+        for (int i = 0; i < 5; i++) sizes_[i] = s[i];
+    }
+    shoccs_problem* get() const { return p_.get(); }
+    explicit operator bool() const { return (bool)p_; }
+    // N_D, |Rx|, |Ry|, |Rz|, fluid points (mesh::size(), mesh::R(dir).size())
+    integer size() const { return sizes_[0]; }
+    integer R(int dir) const { return sizes_[1 + dir]; }
+    integer fluid() const { return sizes_[4]; }
+};
+
+namespace detail
+{
+inline int plus(eq_t) { return 0; }
+inline int plus(plus_eq_t) { return 1; }
+} // namespace detail
+
+// ---- derivative (src/operators/derivative.hpp:20-80) -------------------------------------------
+// du (=|+=) D_dir u, with optional Neumann data nu (FP64 in both precisions).
+// precision::mixed applies the FP32 operator to float fields (scalar_view_f / scalar_span_f).
+class derivative
+{
+    int dir_ = 0;
+    problem p_;
+    precision prec_ = precision::fp64;
+    void* stream_ = nullptr;
+
+    template <typename V, typename S>
+    void apply(const V& u, const scalar_view* nu, const S& du, int plus) const
+    {
+        shoccs_field fu = detail::field(u), fdu = detail::field(du), fnu{};
+        if (nu) fnu = detail::field(*nu);
+        detail::check(shoccs_derivative_apply(p_.get(), dir_, (int)prec_, &fu, nu ? &fnu : nullptr,
+                                              &fdu, plus, stream_),
+                      "shoccs_derivative_apply");
+    }
+
+public:
+    derivative() = default;
+    derivative(int dir, const mesh& m, const stencil& st, const bcs::Grid& grid_bcs,
+               const bcs::Object& object_bcs, precision prec = precision::fp64)
+        : dir_{dir}, p_{m, st, grid_bcs, object_bcs}, prec_{prec}
+    {
+    }
+    // share the operators of an existing problem
+    derivative(int dir, const problem& p, precision prec = precision::fp64) : dir_{dir}, p_{p}, prec_{prec} {}
+
+    void set_stream(void* cuda_stream) { stream_ = cuda_stream; }
+    const problem& get_problem() const { return p_; }
+
+    template <typename Op = eq_t>
+    void operator()(scalar_view u, scalar_span du, Op op = {}) const { apply(u, nullptr, du, detail::plus(op)); }
+    template <typename Op = eq_t>
+    void operator()(scalar_view u, scalar_view nu, scalar_span du, Op op = {}) const
+    {
+        apply(u, &nu, du, detail::plus(op));
+    }
+    template <typename Op = eq_t>
+    void operator()(scalar_view_f u, scalar_span_f du, Op op = {}) const { apply(u, nullptr, du, detail::plus(op)); }
+    template <typename Op = eq_t>
+    void operator()(scalar_view_f u, scalar_view nu, scalar_span_f du, Op op = {}) const
+    {
+        apply(u, &nu, du, detail::plus(op));
+    }
+};
+
+// ---- laplacian (src/operators/laplacian.hpp:10-33) ---------------------------------------------
+// operator()(u[, nu]) returns the apply as a callable, like the reference:  lap(u)(du).
+class laplacian
+{
+    problem p_;
+    precision prec_ = precision::fp64;
+    void* stream_ = nullptr;
+
+    template <typename V, typename S>
+    void apply(const V& u, const scalar_view* nu, const S& du) const
+    {
+        shoccs_field fu = detail::field(u), fdu = detail::field(du), fnu{};
+        if (nu) fnu = detail::field(*nu);
+        detail::check(shoccs_laplacian_apply(p_.get(), (int)prec_, &fu, nu ? &fnu : nullptr, &fdu, stream_),
+                      "shoccs_laplacian_apply");
+    }
+
+public:
+    laplacian() = default;
+    laplacian(const mesh& m, const stencil& st, const bcs::Grid& grid_bcs, const bcs::Object& object_bcs,
+              precision prec = precision::fp64)
+        : p_{m, st, grid_bcs, object_bcs}, prec_{prec}
+    {
+    }
+    laplacian(const problem& p, precision prec = precision::fp64) : p_{p}, prec_{prec} {}
+    void set_stream(void* cuda_stream) { stream_ = cuda_stream; }
+
+    std::function<void(scalar_span)> operator()(scalar_view u) const
+    {
+        return [this, u](scalar_span du) { apply(u, nullptr, du); };
+    }
+    std::function<void(scalar_span)> operator()(scalar_view u, scalar_view nu) const
+    {
+        return [this, u, nu](scalar_span du) { apply(u, &nu, du); };
+    }
+    std::function<void(scalar_span_f)> operator()(scalar_view_f u) const
+    {
+        return [this, u](scalar_span_f du) { apply(u, nullptr, du); };
+    }
+    std::function<void(scalar_span_f)> operator()(scalar_view_f u, scalar_view nu) const
+    {
+        return [this, u, nu](scalar_span_f du) { apply(u, &nu, du); };
+    }
+};
+
+// ---- gradient (src/operators/gradient.hpp:10-30) -----------------------------------------------
+class gradient
+{
+    problem p_;
+    precision prec_ = precision::fp64;
+    void* stream_ = nullptr;
+
+    template <typename V, typename S>
+    void apply(const V& u, const S& dx, const S& dy, const S& dz) const
+    {
+        shoccs_field fu = detail::field(u), fx = detail::field(dx), fy = detail::field(dy),
+                     fz = detail::field(dz);
+        detail::check(shoccs_gradient_apply(p_.get(), (int)prec_, &fu, &fx, &fy, &fz, stream_),
+                      "shoccs_gradient_apply");
+    }
+
+public:
+    gradient() = default;
+    gradient(const mesh& m, const stencil& st, const bcs::Grid& grid_bcs, const bcs::Object& object_bcs,
+             precision prec = precision::fp64)
+        : p_{m, st, grid_bcs, object_bcs}, prec_{prec}
+    {
+    }
+    gradient(const problem& p, precision prec = precision::fp64) : p_{p}, prec_{prec} {}
+    void set_stream(void* cuda_stream) { stream_ = cuda_stream; }
+
+    std::function<void(scalar_span, scalar_span, scalar_span)> operator()(scalar_view u) const
+    {
+        return [this, u](scalar_span dx, scalar_span dy, scalar_span dz) { apply(u, dx, dy, dz); };
+    }
+    std::function<void(scalar_span_f, scalar_span_f, scalar_span_f)> operator()(scalar_view_f u) const
+    {
+        return [this, u](scalar_span_f dx, scalar_span_f dy, scalar_span_f dz) { apply(u, dx, dy, dz); };
+    }
+};
+
+// ---- statistics (src/types.hpp:57-60) ---------------------------------------------------------
+// stats = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry, Linf_Rz,
+//          argmax_Rz} of the state against the exact solution
+struct system_stats {
+    std::vector<real> stats;
+    real wall_time_s = 0.0;
+};
+
+// ---- closed-form manufactured / exact solutions (the Dirichlet data, the heat source and
+// the error reference; src/mms/manufactured_solutions.hpp) -------------------------------------
+struct manufactured_solution {
+    int kind = SHOCCS_SOL_ZERO;
+    std::array<real, 8> params{};
+};
+namespace mms
+{
+inline manufactured_solution zero() { return {}; }
+// prod_d sin(2 pi k x_d) e^{-t}
+inline manufactured_solution sinsin(real k) { return {SHOCCS_SOL_SINSIN, {k}}; }
+// exp(-|x - x0 - a t|^2 / (2 sigma^2)), the translated pulse of a constant velocity a
+inline manufactured_solution gauss_pulse(const real3& x0, const real3& a, real sigma)
+{
+    return {SHOCCS_SOL_GAUSS_PULSE, {x0[0], x0[1], x0[2], a[0], a[1], a[2], sigma}};
+}
+// sin(2 pi (|x - c| - r - t)), the reference's circular wave (src/systems/scalar_wave.cpp:28-40)
+inline manufactured_solution radial_sin(const real3& c, real r)
+{
+    return {SHOCCS_SOL_RADIAL_SIN, {c[0], c[1], c[2], r}};
+}
+} // namespace mms
+
+namespace systems
+{
+// the state, the RK4 registers and the boundary data of a system live on the device
+class scalar_system
+{
+protected:
+    problem p_;
+    std::shared_ptr<shoccs_system> s_;
+    real max_error_ = 0.0;
+    void* stream_ = nullptr;
+
+    scalar_system(const mesh& m, const stencil& st, const bcs::Grid& g, const bcs::Object& o,
+                  const shoccs_system_desc& d)
+        : p_{m, st, g, o}, max_error_{d.max_error}
+    {
+        shoccs_system* raw = nullptr;
+        detail::check(shoccs_system_create(p_.get(), &d, &raw), "shoccs_system_create");
+        s_.reset(raw, [](shoccs_system* q) { shoccs_system_destroy(q); });
+    }
+
+public:
+    shoccs_system* get() const { return s_.get(); }
+    const problem& get_problem() const { return p_; }
+    void set_stream(void* cuda_stream) { stream_ = cuda_stream; }
+
+    // u0 <- the exact solution at time t (system::initialize)
+    void initialize(real t)
+    {
+        detail::check(shoccs_system_initialize(s_.get(), t, stream_), "shoccs_system_initialize");
+    }
+    // rhs of the current state at time t into du (FP64 device field)
+    void rhs(real t, scalar_span du) const
+    {
+        shoccs_field f = detail::field(du);
+        detail::check(shoccs_system_rhs(s_.get(), t, &f, stream_), "shoccs_system_rhs");
+    }
+    // the state as FP64: on_device selects device (true) or host (false) buffers
+    void get_state(scalar_span u, bool on_device = true) const
+    {
+        shoccs_field f = detail::field(u);
+        detail::check(shoccs_system_get_state(s_.get(), &f, on_device ? 1 : 0, stream_),
+                      "shoccs_system_get_state");
+    }
+    void set_state(scalar_view u, bool on_device = true)
+    {
+        shoccs_field f = detail::field(u);
+        detail::check(shoccs_system_set_state(s_.get(), &f, on_device ? 1 : 0, stream_),
+                      "shoccs_system_set_state");
+    }
+    system_stats stats(real t) const
+    {
+        system_stats st;
+        st.stats.resize(11);
+        detail::check(shoccs_system_stats(s_.get(), t, st.stats.data(), stream_), "shoccs_system_stats");
+        return st;
+    }
+    // system::valid: a finite max-norm error within the system's bound
+    bool valid(const system_stats& st) const
+    {
+        const real v = st.stats.empty() ? 0.0 : st.stats[0];
+        return v == v && v <= max_error_ && v >= -max_error_;
+    }
+    // system::timestep_size: heat p h_min^2 / (4k), wave c h_min
+    real timestep_size(real cfl) const
+    {
+        real dt = 0.0;
+        detail::check(shoccs_system_timestep(s_.get(), cfl, &dt), "shoccs_system_timestep");
+        return dt;
+    }
+};
+
+// dT/dt = k lap T + the manufactured source (src/systems/heat.hpp:16-70)
+class heat : public scalar_system
+{
+    static shoccs_system_desc desc(const manufactured_solution& ms, real k, precision prec)
+    {
+        shoccs_system_desc d{};
+        d.kind = SHOCCS_SYS_HEAT;
+        d.prec = (int)prec;
+        d.diffusivity = k;
+        d.sol_kind = ms.kind;
+        for (int i = 0; i < 8; i++) d.sol[i] = ms.params[i];
+        d.max_error = 1e6; // src/systems/heat.cpp:54-58
+        return d;
+    }
+
+public:
+    heat(mesh&& m, bcs::Grid&& grid_bcs, bcs::Object&& object_bcs, manufactured_solution&& m_sol,
+         stencil st, real diffusivity, precision prec = precision::fp64)
+        : scalar_system(m, st, grid_bcs, object_bcs, desc(m_sol, diffusivity, prec))
+    {
+    }
+};
+
+// u_t + a . grad u = 0 written as u_t = gG . grad u (src/systems/scalar_wave.hpp:16-80)
+class scalar_wave : public scalar_system
+{
+    static shoccs_system_desc radial(const real3& center, real radius, real max_error, precision prec)
+    {
+        shoccs_system_desc d{};
+        d.kind = SHOCCS_SYS_WAVE;
+        d.prec = (int)prec;
+        d.vel_kind = SHOCCS_VEL_RADIAL;
+        for (int i = 0; i < 3; i++) d.center[i] = center[i];
+        const auto ms = mms::radial_sin(center, radius);
+        d.sol_kind = ms.kind;
+        for (int i = 0; i < 8; i++) d.sol[i] = ms.params[i];
+        d.max_error = max_error;
+        return d;
+    }
+    static shoccs_system_desc constant(const real3& a, const manufactured_solution& ms, real max_error,
+                                       precision prec)
+    {
+        shoccs_system_desc d{};
+        d.kind = SHOCCS_SYS_WAVE;
+        d.prec = (int)prec;
+        d.vel_kind = SHOCCS_VEL_CONSTANT;
+        for (int i = 0; i < 3; i++) d.vel[i] = a[i];
+        d.sol_kind = ms.kind;
+        for (int i = 0; i < 8; i++) d.sol[i] = ms.params[i];
+        d.max_error = max_error;
+        return d;
+    }
+
+public:
+    // the reference's circular wave: gG = -(x - c)/|x - c|, exact sin(2 pi (|x - c| - r - t))
+    scalar_wave(mesh&& m, bcs::Grid&& grid_bcs, bcs::Object&& object_bcs, stencil st, real3 center,
+                real radius, real max_error = 100.0, precision prec = precision::fp64)
+        : scalar_system(m, st, grid_bcs, object_bcs, radial(center, radius, max_error, prec))
+    {
+    }
+    // extension: a constant velocity a with a closed-form exact solution (e.g. mms::gauss_pulse)
+    scalar_wave(mesh&& m, bcs::Grid&& grid_bcs, bcs::Object&& object_bcs, stencil st, real3 velocity,
+                manufactured_solution&& exact, real max_error = 100.0, precision prec = precision::fp64)
+        : scalar_system(m, st, grid_bcs, object_bcs, constant(velocity, exact, max_error, prec))
+    {
+    }
+};
+} // namespace systems
+
+// ---- integrators (src/temporal/rk4.hpp:10-20, src/temporal/rk4.cpp:11-48) ----------------------
+namespace integrators
+{
+// classic RK4: one step of size dt from time t advances the system's state in place (the
+// reference's rk4 writes u1 and simulation_cycle copies it back into u0)
+class rk4
+{
+public:
+    rk4() = default;
+    void operator()(systems::scalar_system& sys, real t, real dt, void* stream = nullptr) const
+    {
+        run(sys, t, dt, 1, stream);
+    }
+    // nsteps steps in one call (the fused stage kernels stay on the device throughout)
+    void run(systems::scalar_system& sys, real t0, real dt, int nsteps, void* stream = nullptr) const
+    {
+        detail::check(shoccs_system_rk4(sys.get(), t0, dt, nsteps, stream), "shoccs_system_rk4");
+    }
+};
+} // namespace integrators
+} // namespace ccs
