@@ -998,6 +998,9 @@ struct shoccs_batch {
     int n_rows = 0;
     const int4* d_tiles[4] = {}; // (instance, it0 index, first it1 index, it2 chunk)
     int n_tiles[4] = {};
+    // 2-D instances go to the flat stage: warp tiles (instance, first point) of BATCH2D_TILE points
+    const int2* d_wtiles = nullptr;
+    int n_wtiles = 0, grid2d = 1;
     const int* d_r_inst = nullptr;
     int n_r = 0;
     int cfg = 3, grid = 1;
@@ -1078,6 +1081,7 @@ shoccs_status batch_autotune(shoccs_batch* B, cudaStream_t s)
             }
         return fail(SHOCCS_EINVAL, "SHOCCS_BATCH_TILE_WARPS must be 1, 2, 4 or 8");
     }
+    if (B->n_tiles[0] == 0) return SHOCCS_OK; // every instance takes the flat 2-D stage
     cudaEvent_t e0, e1;
     SH_CUDA(cudaEventCreate(&e0));
     SH_CUDA(cudaEventCreate(&e1));
@@ -1118,6 +1122,14 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
     SH_CUDA(cudaGetDevice(&dev));
     std::vector<int> row_inst, r_inst;
     std::vector<int4> tiles[4];
+    std::vector<int2> wtiles;
+    // SHOCCS_BATCH_KERNEL=point sends every instance through the per-point stage
+    const char* kenv = std::getenv("SHOCCS_BATCH_KERNEL");
+    // FP64 batches take the per-point stage unless SHOCCS_BATCH_KERNEL=flat asks otherwise:
+    // with FP64 arithmetic at 1/64 of the FP32 rate the flat stage's register-heavy body
+    // measured slower there
+    const bool allow2d = kenv ? std::string(kenv) == "flat"
+                              : B->prec == PREC_MIXED;
     for (int i = 0; i < n; i++) {
         shoccs_system* S = systems[i];
         if (!S) return fail(SHOCCS_EINVAL, "null system");
@@ -1141,10 +1153,23 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         I.cval = S->b.cval;
         for (int d = 0; d < 3; d++) I.R[d] = S->b.R[d];
         I.row0 = (int)row_inst.size();
+        const bool flat2d = allow2d && op.it0 == 1 && op.it1 > 1 && op.phys_of_it[1] >= 0 &&
+                            op.phys_of_it[2] >= 0 && op.N < (1LL << 31) - 256;
+        if (flat2d) {
+            // cut-cell row values at their points, per axis (3 x N, the batch's own buffer)
+            void* rv = nullptr;
+            const size_t elem = B->prec == PREC_MIXED ? sizeof(float) : sizeof(double);
+            SH_CUDA(B->mem.alloc((size_t)3 * op.N * elem, &rv));
+            SH_CUDA(cudaMemset(rv, 0, (size_t)3 * op.N * elem));
+            I.rowv = rv;
+            if ((long long)wtiles.size() + op.N / BATCH2D_TILE + 1 >= (1LL << 31))
+                return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 tiles");
+            for (long long t = 0; t < op.N; t += BATCH2D_TILE) wtiles.push_back(make_int2(i, (int)t));
+        }
         if ((long long)row_inst.size() + op.n_cut_rows >= (1LL << 31))
             return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 cut-cell rows");
         row_inst.insert(row_inst.end(), op.n_cut_rows, i);
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < 4 && !flat2d; c++) {
             const int w = BATCH_TILE_WARPS[c];
             const int nyb = (op.it1 + w - 1) / w;
             const long long nt = (long long)op.nzc * nyb * op.it0;
@@ -1175,6 +1200,9 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         SH_CUDA(B->mem.put(tiles[c], &B->d_tiles[c], s));
         B->n_tiles[c] = (int)tiles[c].size();
     }
+    SH_CUDA(B->mem.put(wtiles, &B->d_wtiles, s));
+    B->n_wtiles = (int)wtiles.size();
+    B->grid2d = batch_stage2d_grid(B->prec, B->n_wtiles);
     SH_CUDA(B->mem.put(r_inst, &B->d_r_inst, s));
     B->n_r = (int)(r_inst.size() / 3);
     SH_CUDA(cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking));
@@ -1211,8 +1239,9 @@ shoccs_status shoccs_batch_rk4(shoccs_batch* B, const double* t0, const double* 
         cudaError_t e = cudaSuccess;
         for (int k = 0; k < nsteps && e == cudaSuccess; k++)
             e = launch_batch_step(B->d_inst, B->d_row_inst, B->n_rows, B->d_tiles[B->cfg],
-                                  B->n_tiles[B->cfg], B->cfg, B->grid,
-                                  B->d_times + (size_t)k * n, B->prec, B->cap);
+                                  B->n_tiles[B->cfg], B->cfg, B->grid, B->d_wtiles,
+                                  B->n_wtiles, B->grid2d, B->d_times + (size_t)k * n, B->prec,
+                                  B->cap);
         cudaGraph_t g = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(B->cap, &g);
         if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -1244,7 +1273,7 @@ shoccs_status shoccs_batch_info(const shoccs_batch* B, int64_t info[6])
 {
     if (!B || !info) return fail(SHOCCS_EINVAL, "null argument");
     info[0] = (int64_t)B->sys.size();
-    info[1] = B->n_tiles[B->cfg];
+    info[1] = B->n_tiles[B->cfg] + B->n_wtiles;
     info[2] = B->n_rows;
     info[3] = BATCH_TILE_WARPS[B->cfg];
     info[4] = B->grid;

@@ -156,6 +156,7 @@ struct BatchInst {
     void* sa;
     void* sb;
     void* cval;
+    void* rowv;              // 2-D instances: cut-cell row values at their points (3 x N), else null
     double* R[3];
     double cf[4], ci[4];     // dt*rkf[s], dt*rki[s+1] (ci[3] unused)
     float2 cf_ff[4], ci_ff[4];
@@ -171,9 +172,19 @@ struct BatchTime {
 constexpr int BATCH_TILE_WARPS[4] = {1, 2, 4, 8};
 // one RK4 step of every instance: per stage, the cut-cell rows of all instances, then the
 // stage update of all instances (persistent blocks over the (instance, tile) list)
+// per stage: the cut-cell rows of every instance, then the per-point stage over `tiles`
+// (instances that are not 2-D) and the flat 2-D stage over the warp tiles `wtiles`
+// (instance, first point; BATCH2D_TILE points each)
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
                               const int4* tiles, int n_tiles, int tile_cfg, int grid,
+                              const int2* wtiles, int n_wtiles, int grid2d,
                               const BatchTime* times, int prec, cudaStream_t s);
+// persistent grid of the flat 2-D batched stage (128-thread blocks), and the points of one
+// of its warp tiles
+int batch_stage2d_grid(int prec, int n_wtiles);
+constexpr int BATCH2D_PPL = 4;                // points per lane
+constexpr int BATCH2D_TILE = 32 * BATCH2D_PPL; // points per warp tile
+int batch2d_tile_points();
 // one stage-1 pass (timing probe of a tile shape for the autotuner)
 cudaError_t launch_batch_probe(const BatchInst* inst, const int4* tiles, int n_tiles,
                                int tile_cfg, int grid, const BatchTime* times, int prec,

@@ -2574,14 +2574,16 @@ __global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restr
     const int tp = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // R at t, t+dt/2, t+dt
     const RScaled R{I.sp.sol.SR[d], bt[ii].et[tp]};
     const void* in = STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa);
+    // compacted in row order (the per-point stage) and, for the 2-D stage, at the point
     if constexpr (MIXED) {
-        if constexpr (STAGE == 0)
-            ((float*)I.cval)[i] = closure_ff(A, row, p, PairU{(const float*)in, op.N}, R);
-        else
-            ((float*)I.cval)[i] = closure_ff(A, row, p, (const float*)in, R);
+        const float v = STAGE == 0 ? closure_ff(A, row, p, PairU{(const float*)in, op.N}, R)
+                                   : closure_ff(A, row, p, (const float*)in, R);
+        ((float*)I.cval)[i] = v;
+        if (I.rowv) ((float*)I.rowv)[(long long)d * op.N + p] = v;
     } else {
-        ((double*)I.cval)[i] =
-            closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
+        const double v = closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
+        ((double*)I.cval)[i] = v;
+        if (I.rowv) ((double*)I.rowv)[(long long)d * op.N + p] = v;
     }
 }
 
@@ -2643,6 +2645,170 @@ __global__ void __launch_bounds__(32 * WARPS) k_batch_stage(const BatchInst* __r
     }
 }
 
+// interior row of the FP64 path from register values, in interior_d's operation order
+__device__ __forceinline__ double interior_row64(const DevAxis& A, double m2, double m1, double c0,
+                                                double p1, double p2)
+{
+    if (A.width == 5) {
+        if (A.antisym) return fma(A.ic[3], p1 - m1, A.ic[4] * (p2 - m2));
+        double r = A.ic[0] * m2;
+        r = fma(A.ic[1], m1, r);
+        r = fma(A.ic[2], c0, r);
+        r = fma(A.ic[3], p1, r);
+        return fma(A.ic[4], p2, r);
+    }
+    double r = A.ic[0] * m1;
+    r = fma(A.ic[1], c0, r);
+    return fma(A.ic[2], p1, r);
+}
+
+// Batched stage of the 2-D heat instances (iteration space (1, n1, n2), it2 contiguous).  A
+// warp takes BATCH2D_TILE consecutive points of one instance's flat array, BATCH2D_PPL per
+// lane, running
+// across the ends of the it2 lines: a point within two points of a line end has no interior
+// row along it2, so the flat neighbours read for it there are never used, and every lane of
+// the warp has work.  All of a lane's loads are issued before any class byte is decoded
+// (coordinates clamped into the array); the instance's parameters are read once per warp
+// tile.  Per point the arithmetic is the per-point stage body's, with the same helpers in the
+// same order (interior_row / interior_row64, wall32 / wall64, rhs_mixed or the FP64 source,
+// rk_mixed or the FP64 update, the exact face values), so every instance gets the bits a
+// single-system solve gives it.  Cut-cell row values come from the dense per-point array
+// (BatchInst::rowv) that k_batch_cut_rows fills.  No warp-collective operation is used, so
+// lanes past an instance's last point simply skip the tile.
+template <int STAGE, bool MIXED>
+__global__ void __launch_bounds__(128) k_batch_stage2d(const BatchInst* __restrict__ B,
+                                                       const int2* __restrict__ wt, int n_wt,
+                                                       const BatchTime* __restrict__ bt)
+{
+    using T = typename std::conditional<MIXED, float, double>::type;
+    pdl_wait();
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n_wt; w += nwarps) {
+        const int2 tl = __ldg(wt + w); // (instance, first point of the tile)
+        const BatchInst& I = B[tl.x];
+        const DevOp& op = I.op;
+        const int n2 = op.it2, N = (int)op.N;
+        const int da = op.phys_of_it[1], db = op.phys_of_it[2]; // physical axes of it1, it2
+        const DevAxis& Aa = op.ax[da];
+        const DevAxis& Ab = op.ax[db];
+        const T* __restrict__ in = (const T*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
+        auto cl = [N](int x) { return min(max(x, 0), N - 1); };
+        const BatchTime& tm = bt[tl.x];
+        const int ts = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // stage time
+        const int tn = STAGE < 2 ? 1 : 2;                      // time of the stage output
+        StageArgs sa{};
+        sa.u0 = I.u0;
+        sa.acc = I.acc;
+        sa.s_out = STAGE == 1 ? I.sb : I.sa;
+        sa.cf = I.cf[STAGE];
+        sa.ci = I.ci[STAGE];
+        sa.cf_ff = I.cf_ff[STAGE];
+        sa.ci_ff = I.ci_ff[STAGE];
+        sa.t_stage = tm.t[ts];
+        sa.t_next = tm.t[tn];
+        sa.et_stage = tm.et[ts];
+        sa.et_next = tm.et[tn];
+        sa.etf_stage = (float)tm.et[ts];
+        const T* __restrict__ rowv = (const T*)I.rowv;
+        // the tile's 512 points in four passes of 128 (the parameters above are read once)
+        for (int sub = 0; sub < BATCH2D_TILE / (32 * BATCH2D_PPL); sub++) {
+        const int p0 = tl.y + sub * (32 * BATCH2D_PPL) + BATCH2D_PPL * lane;
+        if (p0 >= N) break;
+        T wv[BATCH2D_PPL + 4]; // it2 neighbours: points p0-2 .. p0+PPL+1
+#pragma unroll
+        for (int m = 0; m < BATCH2D_PPL + 4; m++) wv[m] = __ldg(in + cl(p0 - 2 + m));
+        T am2[BATCH2D_PPL], am1[BATCH2D_PPL], ap1[BATCH2D_PPL], ap2[BATCH2D_PPL]; // it1 neighbours
+        unsigned c[BATCH2D_PPL];
+#pragma unroll
+        for (int q = 0; q < BATCH2D_PPL; q++) {
+            const int p = p0 + q;
+            am2[q] = __ldg(in + cl(p - 2 * n2));
+            am1[q] = __ldg(in + cl(p - n2));
+            ap1[q] = __ldg(in + cl(p + n2));
+            ap2[q] = __ldg(in + cl(p + 2 * n2));
+            c[q] = p < N ? (unsigned)op.cls[p] : 0u;
+        }
+        const int i0 = p0 / n2;
+        int ja = i0, jb = p0 - i0 * n2; // iteration coordinates (it1, it2) of the point
+#pragma unroll
+        for (int q = 0; q < BATCH2D_PPL; q++) {
+            const int p = p0 + q;
+            if (p >= N) break;
+            if (q > 0 && ++jb == n2) {
+                jb = 0;
+                ++ja;
+            }
+            const unsigned ka = (c[q] >> (2 * da)) & 3u, kb = (c[q] >> (2 * db)) & 3u;
+            T va = 0, vb = 0;
+            if constexpr (MIXED) {
+                if (ka == ROW_INTERIOR) va = interior_row(Aa, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+                if (kb == ROW_INTERIOR) vb = interior_row(Ab, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+                if (ka == ROW_WALL) va = wall32(Aa, (long long)p, ja, in);
+                if (kb == ROW_WALL) vb = wall32(Ab, (long long)p, jb, in);
+            } else {
+                if (ka == ROW_INTERIOR) va = interior_row64(Aa, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+                if (kb == ROW_INTERIOR) vb = interior_row64(Ab, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+                if (ka == ROW_WALL) va = wall64(Aa, (long long)p, ja, in, (const double*)nullptr, 0.0, true);
+                if (kb == ROW_WALL) vb = wall64(Ab, (long long)p, jb, in, (const double*)nullptr, 0.0, true);
+            }
+            if (ka == ROW_CLOSURE) va = rowv[(long long)da * N + p];
+            if (kb == ROW_CLOSURE) vb = rowv[(long long)db * N + p];
+            // physical coordinates (da < db; the third axis has extent 1)
+            const int ijk[3] = {da == 0 ? ja : 0, da == 1 ? ja : (db == 1 ? jb : 0), db == 2 ? jb : 0};
+            const bool face = (c[q] & CLS_DIRFACE) != 0;
+            if constexpr (MIXED) {
+                const float lap = __fadd_rn(__fadd_rn(0.f, va), vb);
+                const float rhs = (c[q] & 0x3Fu) ? rhs_mixed<SYS_HEAT>(op, I.sp, sa.etf_stage, ijk[0],
+                                                                      ijk[1], ijk[2], lap, 0.f, 0.f, 0.f)
+                                                 : 0.f;
+                float a_out = 0.f, s_out = 0.f;
+                float2 u_out;
+                rk_mixed<STAGE>(sa, rhs, ld_u0<STAGE>(I.u0, N, p),
+                                STAGE == 0 ? 0.f : ((const float*)I.acc)[p], a_out, s_out, u_out);
+                if (face) { // the exact value at the stage output's time
+                    const double v = sol_at_point(op, I.sp.sol, sa.t_next, sa.et_next, ijk);
+                    if constexpr (STAGE < 3)
+                        s_out = (float)v;
+                    else
+                        u_out = ff_from_double(v);
+                }
+                if constexpr (STAGE < 3) {
+                    ((float*)I.acc)[p] = a_out;
+                    ((float*)sa.s_out)[p] = s_out;
+                } else {
+                    st_pair(I.u0, N, p, u_out);
+                }
+            } else {
+                const double lap = (0.0 + va) + vb;
+                double rhs = 0.0;
+                if (c[q] & 0x3Fu) {
+                    double src = 0.0;
+                    if (I.sp.sol.kind == SOL_SINSIN) {
+                        const double u = sol_at_point(op, I.sp.sol, sa.t_stage, sa.et_stage, ijk);
+                        src = __dsub_rn(-u, __dmul_rn(I.sp.k, __dmul_rn(I.sp.sol.lapfac, u)));
+                    }
+                    rhs = fma(lap, I.sp.k, src);
+                }
+                double* __restrict__ u0 = (double*)I.u0;
+                double* __restrict__ acc = (double*)I.acc;
+                if constexpr (STAGE < 3) {
+                    acc[p] = STAGE == 0 ? sa.cf * rhs : fma(sa.cf, rhs, acc[p]);
+                    double so = fma(sa.ci, rhs, u0[p]);
+                    if (face) so = sol_at_point(op, I.sp.sol, sa.t_next, sa.et_next, ijk);
+                    ((double*)sa.s_out)[p] = so;
+                } else {
+                    double un = u0[p] + fma(sa.cf, rhs, acc[p]);
+                    if (face) un = sol_at_point(op, I.sp.sol, sa.t_next, sa.et_next, ijk);
+                    u0[p] = un;
+                }
+            }
+        }
+        }
+    }
+}
+
 __global__ void k_batch_finish(const BatchInst* __restrict__ B, const BatchTime* __restrict__ last,
                                const int* __restrict__ r_inst, int n_r)
 {
@@ -2667,31 +2833,61 @@ void batch_stage(const BatchInst* inst, const int4* tiles, int n_tiles, int cfg,
     ++g_launches;
 }
 
+template <int STAGE, bool MIXED>
+void batch_stage_all(const BatchInst* inst, const int* row_inst, int n_rows, const int4* tiles,
+                     int n_tiles, int cfg, int grid, const int2* wt, int n_wt, int grid2d,
+                     const BatchTime* times, cudaStream_t s)
+{
+    if (n_rows) {
+        k_batch_cut_rows<MIXED, STAGE><<<(n_rows + 127) / 128, 128, 0, s>>>(inst, row_inst, n_rows, times);
+        ++g_launches;
+    }
+    if (n_tiles) batch_stage<STAGE, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+    if (n_wt) {
+        k_batch_stage2d<STAGE, MIXED><<<grid2d, 128, 0, s>>>(inst, wt, n_wt, times);
+        ++g_launches;
+    }
+}
+
 template <bool MIXED>
 void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const int4* tiles,
-                int n_tiles, int cfg, int grid, const BatchTime* times, cudaStream_t s)
+                int n_tiles, int cfg, int grid, const int2* wt, int n_wt, int grid2d,
+                const BatchTime* times, cudaStream_t s)
 {
-    const int nb = (n_rows + 127) / 128;
-    if (n_rows) { k_batch_cut_rows<MIXED, 0><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
-    batch_stage<0, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
-    if (n_rows) { k_batch_cut_rows<MIXED, 1><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
-    batch_stage<1, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
-    if (n_rows) { k_batch_cut_rows<MIXED, 2><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
-    batch_stage<2, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
-    if (n_rows) { k_batch_cut_rows<MIXED, 3><<<nb, 128, 0, s>>>(inst, row_inst, n_rows, times); ++g_launches; }
-    batch_stage<3, MIXED>(inst, tiles, n_tiles, cfg, grid, times, s);
+    batch_stage_all<0, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
+    batch_stage_all<1, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
+    batch_stage_all<2, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
+    batch_stage_all<3, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
 }
 } // namespace
 
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
                               const int4* tiles, int n_tiles, int tile_cfg, int grid,
+                              const int2* wtiles, int n_wtiles, int grid2d,
                               const BatchTime* times, int prec, cudaStream_t s)
 {
     if (prec == PREC_MIXED)
-        batch_step<true>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, times, s);
+        batch_step<true>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, wtiles, n_wtiles,
+                         grid2d, times, s);
     else
-        batch_step<false>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, times, s);
+        batch_step<false>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, wtiles, n_wtiles,
+                          grid2d, times, s);
     return cudaGetLastError();
+}
+
+int batch_stage2d_grid(int prec, int n_wtiles)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const void* fn = prec == PREC_MIXED ? (const void*)k_batch_stage2d<1, true>
+                                        : (const void*)k_batch_stage2d<1, false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 128, 0);
+    const long long g = (long long)std::max(1, per_sm) * std::max(1, sms);
+    return (int)std::max(1LL, std::min<long long>(g, ((long long)n_wtiles + 3) / 4));
+}
+
+int batch2d_tile_points() { return BATCH2D_TILE;
 }
 
 cudaError_t launch_batch_probe(const BatchInst* inst, const int4* tiles, int n_tiles,

@@ -1,10 +1,11 @@
 """Batched heat solves (shoccs_batch_*): independent 2-D heat instances of different grid
 sizes and circle geometries advanced together under one captured CUDA graph.
 
-The batch runs the single-system stage bodies with the same time points and boundary
+The batch runs the single-system stage arithmetic with the same time points and boundary
 products, so every instance must come out bit-identical to shoccs_system_rk4 run on that
-instance alone -- in FP64 and in the mixed path, for every tile shape, and across graph
-replays.  The instances are drawn by the batched configuration's own generator
+instance alone -- in FP64 and in the mixed path, through the flat 2-D stage (SHOCCS_BATCH_KERNEL=flat; the
+default for mixed 2-D instances) and the per-point stage (SHOCCS_BATCH_KERNEL=point; the
+default for FP64) with every tile shape, and across graph replays.  The instances are drawn by the batched configuration's own generator
 (shoccs_gb300.workloads.batch_heat_2d) with smaller grids.
 """
 import numpy as np
@@ -33,8 +34,10 @@ def _state(sys_, p):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["flat", "point"])
 @pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
-def test_batch_matches_single_systems_bitwise(prec):
+def test_batch_matches_single_systems_bitwise(prec, kernel, monkeypatch):
+    monkeypatch.setenv("SHOCCS_BATCH_KERNEL", kernel)
     insts = _instances()
     pb, sb = _make(insts, prec)
     ps, ss = _make(insts, prec)
@@ -73,12 +76,14 @@ def test_batch_graph_replay_continues_the_solve():
 @pytest.mark.parametrize("warps", [1, 2, 4, 8])
 def test_batch_tile_shapes_agree(warps, monkeypatch):
     insts = _instances(count=3, nmax=64)
+    monkeypatch.setenv("SHOCCS_BATCH_KERNEL", "point")  # tile shapes belong to the per-point stage
     monkeypatch.setenv("SHOCCS_BATCH_TILE_WARPS", str(warps))
     pb, sb = _make(insts, S.PREC_MIXED)
     batch = S.Batch(sb)
     assert batch.info()["tile_warps"] == warps
     batch.rk4(0.0, [it["dt"] for it in insts], 7)
     monkeypatch.delenv("SHOCCS_BATCH_TILE_WARPS")
+    monkeypatch.delenv("SHOCCS_BATCH_KERNEL")
     ps, ss = _make(insts, S.PREC_MIXED)
     for s, it in zip(ss, insts):
         s.rk4(0.0, it["dt"], 7)
