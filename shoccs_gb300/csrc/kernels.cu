@@ -1201,7 +1201,9 @@ __device__ __forceinline__ float f4(const float4& v, int q)
 template <int STAGE, int SYS, int FORM, int VK, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
 {
-    pdl_wait();
+    // The stage input, u0 and the accumulator were complete before the cut-row kernel that
+    // precedes this one could let it start, so their loads go out before the dependent-launch
+    // wait; what that kernel writes (line records, cut-cell values) is read after it.
     pdl_trigger();
     const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
@@ -1234,6 +1236,7 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
     // the line record (k_cut_rows): words 0..7 on lanes 0..7 of the warp that holds the
     // line's first point, words 8..15 on lanes 8..15 of the one that holds its last point
+    pdl_wait();
     const bool rec_l = blockIdx.x == 0, rec_r = blockIdx.x + 1 == gridDim.x;
     const float rec = (lane < 8 ? rec_l : (lane < 16 && rec_r))
                           ? __ldg(sa.lrec + (long long)(i * ny + j) * 16 + lane)
