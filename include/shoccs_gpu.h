@@ -157,6 +157,10 @@ typedef struct {
 shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* desc,
                                    shoccs_system** out);
 shoccs_status shoccs_system_destroy(shoccs_system* s);
+/* Time stepping takes Dirichlet and Floating faces and Dirichlet objects; a FP64 heat system
+ * also takes Floating objects, whose cut-point values are then state that evolves through
+ * the Laplacian's R-space rows (rk4 advances the whole field {D, Rx, Ry, Rz}, as
+ * src/temporal/rk4.cpp:16-47 does).  Neumann faces and Neumann objects: SHOCCS_EUNSUPPORTED. */
 /* u0 <- exact solution at time t on fluid D points, 0 on solid points, exact on R */
 shoccs_status shoccs_system_initialize(shoccs_system* s, double t, void* stream);
 /* copy the state in/out as FP64; where = 0 host pointers, 1 device pointers */
@@ -198,8 +202,9 @@ shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double*
  * point, tma, col1, col2, col4, vec, vec3 -- forces one):
  * 0 per-point kernel, 1 TMA plane-marching, 2/3/4 column-blocked with 1/2/4 planes per
  * thread, 5/6 vectorised (four z points per thread; nz a multiple of 4) with 4/3 resident
- * blocks per SM.  All variants give
- * the same bits.  FP64 systems and 2-D / 1-D grids always use the per-point kernel. */
+ * blocks per SM, 7 unfused whole-field step (FP64 heat systems with non-Dirichlet objects,
+ * whose cut-point values are state).  Variants 0-6 give the same bits.  FP64 systems and
+ * 2-D / 1-D grids otherwise use the per-point kernel. */
 shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);
 /* ---- batched heat solves ---------------------------------------------------------------
  * Many independent heat systems (each with the manufactured sin-sin solution, Dirichlet

@@ -273,7 +273,7 @@ class System:
         return vals, st == _capi.OK
 
     STAGE_KERNELS = {0: "point", 1: "tma", 2: "col1", 3: "col2", 4: "col4", 5: "vec",
-                     6: "vec3"}
+                     6: "vec3", 7: "unfused"}
 
     @property
     def stage_kernel(self):

@@ -106,6 +106,11 @@ struct shoccs_system {
     StepBuffers b{};
     double t = 0.0;
     AdjointState adj;
+    // heat systems with non-Dirichlet objects step the whole field {D, R} unfused (FP64):
+    // stage field, right-hand side and accumulator (D parts: b.sa, b.sb, b.acc)
+    bool unfused = false;
+    FieldF64 fy{}, fk{}, facc{};
+    FieldF64 state() const { return {(double*)b.u0, {b.R[0], b.R[1], b.R[2]}}; }
     ~shoccs_system()
     {
         if (b.side) cudaStreamDestroy(b.side);
@@ -603,11 +608,16 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         return fail(SHOCCS_EINVAL, "unknown system kind");
     if (d->prec != 0 && d->prec != 1) return fail(SHOCCS_EINVAL, "unknown precision");
     if (d->sol_kind < 0 || d->sol_kind > 3) return fail(SHOCCS_EINVAL, "unknown solution kind");
-    for (int b : p->bcs.obj)
-        if (b != Dirichlet)
-            return fail(SHOCCS_EUNSUPPORTED,
-                        "time stepping supports Dirichlet objects only (non-Dirichlet cut "
-                        "points evolve through R-space rows)");
+    bool non_dirichlet_objects = false;
+    for (int b : p->bcs.obj) {
+        if (b == Neumann)
+            return fail(SHOCCS_EUNSUPPORTED, "time stepping with Neumann objects");
+        non_dirichlet_objects = non_dirichlet_objects || b != Dirichlet;
+    }
+    if (non_dirichlet_objects && (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64))
+        return fail(SHOCCS_EUNSUPPORTED,
+                    "non-Dirichlet objects (whose cut-point values evolve through the R-space "
+                    "rows) are time-stepped by the FP64 heat system only");
     for (int a = 0; a < 3; a++)
         for (int side = 0; side < 2; side++)
             if (p->bcs.grid[a][side] == Neumann)
@@ -694,6 +704,19 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.Rhalf[r] = (double*)h;
         S->b.Rfull[r] = (double*)f;
         if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
+    }
+    if (non_dirichlet_objects) {
+        S->unfused = true;
+        S->fy.D = (double*)S->b.sa;
+        S->fk.D = (double*)S->b.sb;
+        S->facc.D = (double*)S->b.acc;
+        for (int r = 0; r < 3; r++) {
+            void* a = nullptr;
+            SH_CUDA(S->mem.alloc(p->mesh.R[r].size() * 8, &a));
+            S->fy.R[r] = S->b.Rhalf[r];
+            S->fk.R[r] = S->b.Rfull[r];
+            S->facc.R[r] = (double*)a;
+        }
     }
     if (d->prec == PREC_MIXED) {
         // exact values on the Dirichlet faces, evaluated once per step on a side stream
@@ -844,8 +867,12 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     const cudaStream_t s = (cudaStream_t)stream;
     double t = t0;
     for (int i = 0; i < nsteps; i++) {
-        SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
-                                nullptr, i + 1 < nsteps));
+        if (S->unfused)
+            SH_CUDA(launch_heat_step_unfused(S->P->op, S->P->dr, S->sp, S->state(), S->fy, S->fk,
+                                             S->facc, t, dt, s));
+        else
+            SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
+                                    nullptr, i + 1 < nsteps));
         t += dt; // step_controller advance (src/simulation/simulation_cycle.cpp:97)
     }
     SH_CUDA(cudaStreamSynchronize(s));
@@ -858,6 +885,24 @@ shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, in
 {
     if (!S || nsteps < 1 || !(dt > 0) || !kernel_ms) return fail(SHOCCS_EINVAL, "bad argument");
     const cudaStream_t s = (cudaStream_t)stream;
+    if (S->unfused) { // no fused stage kernels to time: the whole run is kernel_ms[0]
+        cudaEvent_t a, z;
+        SH_CUDA(cudaEventCreate(&a));
+        SH_CUDA(cudaEventCreate(&z));
+        SH_CUDA(cudaEventRecord(a, s));
+        const shoccs_status st = shoccs_system_rk4(S, t0, dt, nsteps, stream);
+        float ms = 0.f;
+        if (st == SHOCCS_OK) {
+            cudaEventRecord(z, s);
+            cudaEventSynchronize(z);
+            cudaEventElapsedTime(&ms, a, z);
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(z);
+        for (int k = 0; k < 6; k++) kernel_ms[k] = 0.0;
+        kernel_ms[0] = kernel_ms[5] = ms;
+        return st;
+    }
     constexpr int EV = 10;
     std::vector<cudaEvent_t> ev(EV * (size_t)nsteps, nullptr);
     shoccs_status st = SHOCCS_OK;
@@ -909,7 +954,11 @@ shoccs_status shoccs_system_rhs(shoccs_system* S, double t, shoccs_field* rhs, v
     if (!S || !rhs || !rhs->D) return fail(SHOCCS_EINVAL, "null argument");
     const cudaStream_t s = (cudaStream_t)stream;
     double* outR[3] = {(double*)rhs->Rx, (double*)rhs->Ry, (double*)rhs->Rz};
-    SH_CUDA(launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)rhs->D, outR, s));
+    if (S->unfused)
+        SH_CUDA(launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->state(), t,
+                                        FieldF64{(double*)rhs->D, {outR[0], outR[1], outR[2]}}, s));
+    else
+        SH_CUDA(launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)rhs->D, outR, s));
     SH_CUDA(cudaStreamSynchronize(s));
     return SHOCCS_OK;
 }
@@ -919,22 +968,37 @@ shoccs_status shoccs_system_stats(shoccs_system* S, double t, double out[11], vo
     if (!S || !out) return fail(SHOCCS_EINVAL, "null argument");
     const cudaStream_t s = (cudaStream_t)stream;
     double* dev = nullptr;
-    SH_CUDA(cudaMallocAsync((void**)&dev, 4 * sizeof(double), s));
+    SH_CUDA(cudaMallocAsync((void**)&dev, 16 * sizeof(double), s));
     cudaError_t e = launch_stats(S->P->op, S->P->dr, S->sp.sol, S->desc.prec, S->b.u0, S->b.R, t,
                                  dev, s);
-    double h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess && S->unfused) e = launch_stats_r(S->P->op, S->P->dr, S->sp.sol, S->b.R, t, dev + 4, s);
+    double h[16] = {};
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, dev, sizeof h, cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(dev, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(SHOCCS_ECUDA, std::string("stats: ") + cudaGetErrorString(e));
-    // all cut points of a time-stepped system are Dirichlet, so the R statistics are zero
-    // (compute_scalar_stats only visits non-Dirichlet cut points)
+    // compute_scalar_stats visits the fluid D points and the non-Dirichlet cut points; a
+    // system whose objects are all Dirichlet has no such cut point, so its R statistics are 0
+    const bool fluid = S->P->comp.n_fluid > 0;
     out[0] = h[0];
-    out[1] = S->P->comp.n_fluid ? h[2] : 0.0;
-    out[2] = S->P->comp.n_fluid ? h[3] : 0.0;
+    out[1] = fluid ? h[2] : 0.0;
+    out[2] = fluid ? h[3] : 0.0;
     out[3] = h[0];
     out[4] = h[1];
     for (int i = 5; i < 11; i++) out[i] = 0.0;
+    if (S->unfused) {
+        bool any = fluid;
+        for (int d = 0; d < 3; d++) {
+            const double* r = h + 4 + 4 * d; // {err, index (-1: none), min, max}
+            if (r[1] < 0) continue;
+            out[5 + 2 * d] = r[0];
+            out[6 + 2 * d] = r[1];
+            out[0] = std::max(out[0], r[0]);
+            out[1] = any ? std::min(out[1], r[2]) : r[2];
+            out[2] = any ? std::max(out[2], r[3]) : r[3];
+            any = true;
+        }
+    }
     const double bound = S->desc.kind == SHOCCS_SYS_HEAT ? 1e6 : S->desc.max_error;
     if (!std::isfinite(out[0]) || std::abs(out[0]) > bound)
         return fail(SHOCCS_ENONFINITE, "solution error is non-finite or above its bound");
@@ -945,6 +1009,9 @@ shoccs_status shoccs_system_stats_noalloc(shoccs_system* S, double t, double out
                                           void* stream)
 {
     if (!S || !out) return fail(SHOCCS_EINVAL, "null argument");
+    if (S->unfused)
+        return fail(SHOCCS_EUNSUPPORTED, "shoccs_system_stats_noalloc covers systems whose "
+                                         "objects are all Dirichlet; use shoccs_system_stats");
     const DevOp& op = S->P->op;
     const long long tiles = (long long)op.nzc * ((op.it1 + 7) / 8) * op.it0;
     if (tiles > stats_noalloc_max_tiles())
@@ -974,7 +1041,8 @@ shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
 {
     if (!S || !kernel) return fail(SHOCCS_EINVAL, "null argument");
     const StepBuffers& b = S->b;
-    *kernel = b.tma                ? 1
+    *kernel = S->unfused           ? 7
+              : b.tma              ? 1
               : b.col_nx == 1      ? 2
               : b.col_nx == 2      ? 3
               : b.col_nx == 4      ? 4
@@ -1139,6 +1207,8 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
             return fail(SHOCCS_EUNSUPPORTED,
                         "batched solves take heat systems with the sin-sin manufactured solution");
         if (S->desc.prec != B->prec) return fail(SHOCCS_EINVAL, "mixed precisions in one batch");
+        if (S->unfused)
+            return fail(SHOCCS_EUNSUPPORTED, "batched solves take systems whose objects are all Dirichlet");
         if (S->P->device != dev) return fail(SHOCCS_EINVAL, "systems on different devices");
         const DevOp& op = S->P->op;
         if (op.N >= (1LL << 31) - 64) return fail(SHOCCS_EUNSUPPORTED, "instance above 2^31 points");
@@ -1369,6 +1439,8 @@ shoccs_status adjoint_supported(const shoccs_system* S)
 {
     if (S->desc.kind != SHOCCS_SYS_HEAT)
         return fail(SHOCCS_EUNSUPPORTED, "the adjoint is implemented for heat systems");
+    if (S->unfused)
+        return fail(SHOCCS_EUNSUPPORTED, "the adjoint covers systems whose objects are all Dirichlet");
     return SHOCCS_OK;
 }
 } // namespace

@@ -73,6 +73,12 @@ struct DevR {
     const uint8_t* dirichlet[3]; // 1 where the cut point's shape is Dirichlet
 };
 
+// a whole FP64 scalar field {D, Rx, Ry, Rz} on the device
+struct FieldF64 {
+    double* D;
+    double* R[3];
+};
+
 // launch helpers implemented in kernels.cu -----------------------------------------------
 enum { PREC_FP64 = 0, PREC_MIXED = 1 };
 // interior stencil shared by every active axis: 5-point antisymmetric (first derivative),
@@ -231,6 +237,17 @@ cudaError_t launch_cast(long long n, int to_f32, const void* in, void* out, cuda
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev = nullptr, bool prefetch_next = false);
+// heat systems whose objects are not all Dirichlet (FP64): rhs of the whole field, and one
+// RK4 step of the whole field U with the scratch fields Y, K, ACC
+cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                    FieldF64 u, double t, FieldF64 out, cudaStream_t s);
+cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                     FieldF64 U, FieldF64 Y, FieldF64 K, FieldF64 ACC, double t,
+                                     double dt, cudaStream_t s);
+// statistics of the non-Dirichlet cut points: out12[4d..4d+3] = {err, index (-1: none),
+// min, max} per axis
+cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, double* const R[3],
+                           double t, double* out12, cudaStream_t s);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s);
 cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,

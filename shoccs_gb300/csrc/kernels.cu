@@ -2414,6 +2414,175 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
     return cudaGetLastError();
 }
 
+// ===========================================================================================
+// Unfused FP64 heat step, for systems whose objects are not all Dirichlet.  The values at the
+// cut points of Floating objects are state: the reference's rk4::operator()
+// (src/temporal/rk4.cpp:16-47) advances the whole scalar field {D, Rx, Ry, Rz}, the
+// Laplacian's R-space rows (Bf, Br) give their right-hand side, and heat::update_boundary
+// (src/systems/heat.cpp:296-354) resets the Dirichlet faces and the Dirichlet cut points to
+// the exact solution after every stage.  Each stage here is the standalone Laplacian (which
+// evaluates those rows), one kernel forming k*lap + source, and whole-field axpys.
+// ===========================================================================================
+namespace
+{
+// flat index over {D, Rx, Ry, Rz} -> (part 0..3, index within the part)
+__device__ __forceinline__ int field_part(const DevOp& op, long long g, long long& i)
+{
+    if (g < op.N) {
+        i = g;
+        return 0;
+    }
+    g -= op.N;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (g < op.nR[d]) {
+            i = g;
+            return 1 + d;
+        }
+        g -= op.nR[d];
+    }
+    return -1;
+}
+
+__device__ __forceinline__ double heat_source(const SysParams& sp, double u)
+{
+    return __dsub_rn(-u, __dmul_rn(sp.k, __dmul_rn(sp.sol.lapfac, u)));
+}
+
+__device__ __forceinline__ void phys_of_point(const DevOp& op, long long p, int ijk[3])
+{
+    const long long nyz = (long long)op.n[1] * op.n[2];
+    ijk[0] = (int)(p / nyz);
+    ijk[1] = (int)((p / op.n[2]) % op.n[1]);
+    ijk[2] = (int)(p % op.n[2]);
+}
+
+// K <- k * lap + source (heat::build_rhs_graph, heat.cpp:164-288): the source at fluid D
+// points and at non-Dirichlet cut points; 0 on Dirichlet faces and at Dirichlet cut points
+__global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, double et, FieldF64 K)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    const bool sinsin = sp.sol.kind == SOL_SINSIN;
+    if (part == 0) {
+        const unsigned c = op.cls[i];
+        double v = __dmul_rn(K.D[i], sp.k);
+        if ((c & CLS_FLUID) && sinsin) {
+            int ijk[3];
+            phys_of_point(op, i, ijk);
+            v = __dadd_rn(v, heat_source(sp, sol_at_point(op, sp.sol, t, et, ijk)));
+        }
+        if (c & CLS_DIRFACE) v = 0.0;
+        K.D[i] = v;
+    } else {
+        const int d = part - 1;
+        double v = __dmul_rn(K.R[d][i], sp.k);
+        if (dr.dirichlet[d][i])
+            v = 0.0;
+        else if (sinsin)
+            v = __dadd_rn(v, heat_source(sp, sol_at(sp.sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i)));
+        K.R[d][i] = v;
+    }
+}
+
+// out <- a + c * k over the whole field (slot_assign_lc / slot_accumulate, slot_ops.hpp:11-61)
+__global__ void k_field_lc(DevOp op, FieldF64 out, FieldF64 a, double c, FieldF64 k)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    if (part == 0)
+        out.D[i] = __dadd_rn(a.D[i], __dmul_rn(c, k.D[i]));
+    else
+        out.R[part - 1][i] = __dadd_rn(a.R[part - 1][i], __dmul_rn(c, k.R[part - 1][i]));
+}
+
+// heat::update_boundary: Dirichlet faces and Dirichlet cut points take the exact solution
+__global__ void k_update_boundary(DevOp op, DevR dr, DevSol sol, double t, double et, FieldF64 u)
+{
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < op.n_faces) {
+        const long long p = op.faces[g];
+        int ijk[3];
+        phys_of_point(op, p, ijk);
+        u.D[p] = sol_at_point(op, sol, t, et, ijk);
+        return;
+    }
+    g -= op.n_faces;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (g < op.nR[d]) {
+            if (dr.dirichlet[d][g]) u.R[d][g] = sol_at(sol, t, et, dr.pos[d] + 3 * g, nullptr, d, (int)g);
+            return;
+        }
+        g -= op.nR[d];
+    }
+}
+
+long long field_size(const DevOp& op) { return op.N + op.nR[0] + op.nR[1] + op.nR[2]; }
+
+cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, FieldF64 u,
+                             double t, FieldF64 K, cudaStream_t s)
+{
+    const void* uR[3] = {u.R[0], u.R[1], u.R[2]};
+    void* kR[3] = {K.R[0], K.R[1], K.R[2]};
+    cudaError_t e = launch_laplacian(op, PREC_FP64, u.D, uR, nullptr, K.D, kR, s);
+    if (e != cudaSuccess) return e;
+    const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    const long long n = field_size(op);
+    k_heat_rhs_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sp, t, et, K);
+    ++g_launches;
+    return cudaGetLastError();
+}
+} // namespace
+
+cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                    FieldF64 u, double t, FieldF64 out, cudaStream_t s)
+{
+    return heat_rhs_unfused(op, dr, sp, u, t, out, s);
+}
+
+// one RK4 step of the whole field U (rk4.cpp:16-47) with the scratch fields Y, K, ACC
+cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                     FieldF64 U, FieldF64 Y, FieldF64 K, FieldF64 ACC, double t,
+                                     double dt, cudaStream_t s)
+{
+    constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
+    constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    const long long n = field_size(op);
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    const long long nbnd = op.n_faces + op.nR[0] + op.nR[1] + op.nR[2];
+    const unsigned bb = (unsigned)std::max(1LL, (nbnd + 255) / 256);
+    auto et = [&](double tt) { return sp.sol.kind == SOL_SINSIN ? std::exp(-tt) : 0.0; };
+    // rk_rhs <- 0, then += dt rkf[i] k_i (rk4.cpp:21, 40)
+    cudaError_t e = cudaMemsetAsync(ACC.D, 0, op.N * sizeof(double), s);
+    for (int d = 0; d < 3 && e == cudaSuccess; d++)
+        if (op.nR[d]) e = cudaMemsetAsync(ACC.R[d], 0, op.nR[d] * sizeof(double), s);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+        const double ti = t + dt * rki[i];
+        FieldF64 in = U;
+        if (i > 0) {
+            k_field_lc<<<nb, 256, 0, s>>>(op, Y, U, dt * rki[i], K);
+            k_update_boundary<<<bb, 256, 0, s>>>(op, dr, sp.sol, ti, et(ti), Y);
+            g_launches += 2;
+            in = Y;
+        }
+        e = heat_rhs_unfused(op, dr, sp, in, ti, K, s);
+        if (e != cudaSuccess) break;
+        k_field_lc<<<nb, 256, 0, s>>>(op, ACC, ACC, dt * rkf[i], K);
+        ++g_launches;
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return e;
+    k_field_lc<<<nb, 256, 0, s>>>(op, U, U, 1.0, ACC);
+    k_update_boundary<<<bb, 256, 0, s>>>(op, dr, sp.sol, t + dt, et(t + dt), U);
+    g_launches += 2;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s)
 {
@@ -2465,6 +2634,69 @@ cudaError_t launch_state_convert(long long n, int to_mixed, const double* in_d, 
     const long long nb = (n + bs - 1) / bs;
     k_convert<<<(unsigned)nb, bs, 0, s>>>(n, to_mixed, in_d, (float*)out, (const float*)in_m,
                                           out_d);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// errors at the non-Dirichlet cut points (compute_scalar_stats,
+// src/systems/detail/scalar_system_utils.hpp:77-181): per axis (one block each) the largest
+// |u - exact| with its first index, and the min / max of the values; out[4d..4d+3] =
+// {err, index, min, max}, index -1 where the axis has no such point.  A non-finite value
+// counts as an infinite error, as in the D statistics.
+__global__ void __launch_bounds__(256) k_stats_r(DevOp op, DevR dr, DevSol sol, double t, double et,
+                                                 const double* R0, const double* R1,
+                                                 const double* R2, double* out)
+{
+    const int d = blockIdx.x;
+    const double* R = d == 0 ? R0 : (d == 1 ? R1 : R2);
+    const long long n = op.nR[d];
+    double be = -1.0, vmin = 1.0 / 0.0, vmax = -1.0 / 0.0;
+    long long bi = -1;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        if (dr.dirichlet[d][i]) continue;
+        const double v = R[i];
+        double e = fabs(v - sol_at(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, i));
+        if (!(e <= 1.0e300)) e = 1.0 / 0.0;
+        if (e > be) { // i grows along the loop, so the first index of a tie is kept
+            be = e;
+            bi = i;
+        }
+        vmin = fmin(vmin, v);
+        vmax = fmax(vmax, v);
+    }
+    __shared__ double se[256], smn[256], smx[256];
+    __shared__ long long si[256];
+    se[threadIdx.x] = be;
+    si[threadIdx.x] = bi;
+    smn[threadIdx.x] = vmin;
+    smx[threadIdx.x] = vmax;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const int o = threadIdx.x + w;
+            if (si[o] >= 0 && (si[threadIdx.x] < 0 || se[o] > se[threadIdx.x] ||
+                               (se[o] == se[threadIdx.x] && si[o] < si[threadIdx.x]))) {
+                se[threadIdx.x] = se[o];
+                si[threadIdx.x] = si[o];
+            }
+            smn[threadIdx.x] = fmin(smn[threadIdx.x], smn[o]);
+            smx[threadIdx.x] = fmax(smx[threadIdx.x], smx[o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[4 * d] = si[0] >= 0 ? se[0] : 0.0;
+        out[4 * d + 1] = (double)si[0];
+        out[4 * d + 2] = smn[0];
+        out[4 * d + 3] = smx[0];
+    }
+}
+
+cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, double* const R[3],
+                           double t, double* out12, cudaStream_t s)
+{
+    const double et = sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    k_stats_r<<<3, 256, 0, s>>>(op, dr, sol, t, et, R[0], R[1], R[2], out12);
     ++g_launches;
     return cudaGetLastError();
 }

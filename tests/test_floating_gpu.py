@@ -1,0 +1,117 @@
+"""Heat systems with Floating objects: the cut-point values of a Floating object are state,
+so the RK4 step advances the whole field {D, Rx, Ry, Rz} (src/temporal/rk4.cpp:16-47), their
+right-hand side comes from the Laplacian's R-space rows plus the source, and the statistics
+include them (compute_scalar_stats visits the non-Dirichlet cut points).  The FP64 heat system
+runs this unfused path; everything is checked against the oracle's heat rhs, rk4 and stats.
+
+Tolerances (max-norm, relative to the oracle array's max-norm): rhs 1e-11, RK4 state 1e-10
+(FP64 arithmetic in a different order); errors, min and max to 1e-8; each argmax index must
+carry the maximum error (ties to rounding on symmetric geometries).
+"""
+import numpy as np
+import pytest
+
+import shoccs_gb300 as S
+from oracle.oracle import OracleProblem
+from shoccs_gb300 import workloads as W
+
+CASES = {
+    "circle65_floating": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                              spheres=[((0.51, 0.49, 0.0), 0.2, "floating")],
+                              grid_bc=("dirichlet",) * 4 + ("floating",) * 2, scheme="E4_2"),
+    "sphere24_floating": dict(n=(24, 24, 24), lo=(0, 0, 0), hi=(1, 1, 1),
+                              spheres=[((0.5, 0.5, 0.5), 0.25, "floating")],
+                              grid_bc=("dirichlet",) * 6, scheme="E4_2"),
+    "two_objects": dict(n=(49, 49, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                        spheres=[((0.3, 0.3, 0.0), 0.12, "floating"),
+                                 ((0.7, 0.68, 0.0), 0.15, "dirichlet")],
+                        grid_bc=("dirichlet",) * 4 + ("floating",) * 2, scheme="E2_2"),
+}
+SOL = [1.0]  # sin(2 pi x) sin(2 pi y) (sin 2 pi z) e^-t
+
+
+def rel(got, want):
+    want = np.asarray(want)
+    if want.size == 0:
+        return 0.0
+    return float(np.abs(np.asarray(got) - want).max() / max(np.abs(want).max(), 1e-300))
+
+
+def _system(c):
+    p = S.Problem(**c)
+    h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
+    h.initialize(0.0)
+    return p, h
+
+
+def _state(h, p):
+    u = [np.zeros(p.size)] + [np.zeros(k) for k in p.nR]
+    h.get_state(S.ScalarField(*u))
+    return u
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_floating_rhs_matches_oracle(name):
+    import torch
+    c = CASES[name]
+    p, h = _system(c)
+    assert h.stage_kernel == "unfused"
+    o = OracleProblem(**c)
+    u = _state(h, p)
+    t = 0.013
+    want = o.heat_rhs(1.0, S.SOL_SINSIN, SOL, t, u)
+    got = h.rhs(t, p.zeros(torch.float64))
+    for k, (g, w) in enumerate(zip(got, want)):
+        assert rel(g.cpu().numpy(), w) <= 1e-11, (name, k)
+    # the Floating cut points have a nonzero right-hand side (they evolve)
+    assert any(np.abs(w).max() > 0 for w in want[1:])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_floating_rk4_and_stats_match_oracle(name):
+    c = CASES[name]
+    p, h = _system(c)
+    o = OracleProblem(**c)
+    u0 = _state(h, p)
+    n = max(c["n"])
+    dt = W.heat_dt(n)
+    steps = 20
+    h.rk4(0.0, dt, steps)
+    got = _state(h, p)
+    want = o.heat_rk4(1.0, S.SOL_SINSIN, SOL, 0.0, dt, steps, u0)
+    for k, (g, w) in enumerate(zip(got, want)):
+        assert rel(g, w) <= 1e-10, (name, k)
+    t = steps * dt
+    st, ok = h.stats(t)
+    ref = o.stats(S.SOL_SINSIN, SOL, t, want)
+    assert ok
+    for k in (0, 1, 2, 3, 5, 7, 9):  # errors, min, max
+        assert abs(st[k] - ref[k]) <= 1e-8 * max(abs(ref[k]), 1e-12), (name, k, st[k], ref[k])
+    # argmax of each R array: on a symmetric geometry several cut points share the largest
+    # error to rounding, so the oracle's error at the index returned must be that maximum
+    ex = o.exact(S.SOL_SINSIN, SOL, t)
+    for d, k in ((0, 6), (1, 8), (2, 10)):
+        err = np.abs(want[1 + d] - ex[1 + d])
+        if err.size == 0 or ref[k - 1] == 0:
+            continue
+        assert err[int(st[k])] >= err.max() * (1 - 1e-8), (name, k, st[k], ref[k])
+
+
+@pytest.mark.gpu
+def test_floating_systems_that_stay_unsupported():
+    c = dict(CASES["circle65_floating"])
+    p = S.Problem(**c)
+    with pytest.raises(S.ShoccsError):  # mixed precision: the fused path only
+        S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    with pytest.raises(S.ShoccsError):  # the wave system
+        S.ScalarWave(p, S.PREC_FP64)
+    h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
+    with pytest.raises(S.ShoccsError):  # the adjoint covers Dirichlet objects
+        h.forward(0.0, 1e-5, 2)
+    with pytest.raises(S.ShoccsError):  # and so do batched solves
+        S.Batch([h])
+    c["spheres"] = [((0.51, 0.49, 0.0), 0.2, "neumann")]
+    with pytest.raises(S.ShoccsError):
+        S.Heat(S.Problem(**c), 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
