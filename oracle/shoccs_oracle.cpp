@@ -1572,6 +1572,19 @@ struct solution {
         }
         return 0.0;
     }
+    // component dir of the gradient (manufactured_solution::gradient, the Neumann data of
+    // heat::update_boundary, src/systems/heat.cpp:324-352); the heat systems here use the
+    // sin-sin solution or zero
+    real gradient(real t, const real3& x, int dir) const
+    {
+        if (kind != SOL_SINSIN) return 0.0;
+        constexpr real twoPI = 2 * 3.14159265358979323846;
+        const real kk = twoPI * p[0];
+        real v = 1.0;
+        for (int d = 0; d < dims; d++)
+            v = v * (d == dir ? kk * std::cos(kk * x[d]) : std::sin(kk * x[d]));
+        return v * std::exp(-t);
+    }
 };
 
 // ---------------------------------------------------------------------------------------
@@ -1637,10 +1650,36 @@ struct heat_sys {
     solution sol;
     field_buf neu, src;
 
+    // Neumann data of heat::update_boundary (heat.cpp:324-352): the gradient component of
+    // the axis on that axis' Neumann faces, axes in order, so at an edge shared with a later
+    // axis' Neumann face the later axis' value stays.  update_boundary runs at every stage
+    // time before the right-hand side (and simulation_cycle runs it once after initialize),
+    // so the data a right-hand side sees is the one at its own time.
+    void fill_neumann(real time)
+    {
+        const mesh& m = P->m;
+        const auto& n = m.n;
+        if ((integer)neu.D.size() != m.size()) neu.resize(m);
+        for (int d = 0; d < 3; d++)
+            for (int side = 0; side < 2; side++) {
+                if (P->gbc[d][side] != Neumann) continue;
+                const int face = side == 0 ? 0 : n[d] - 1;
+                for (int i = 0; i < n[0]; i++)
+                    for (int j = 0; j < n[1]; j++)
+                        for (int k = 0; k < n[2]; k++) {
+                            const int3 ijk{i, j, k};
+                            if (ijk[d] != face) continue;
+                            const integer idx = m.ic(ijk);
+                            neu.D[idx] = sol.gradient(time, m.loc(idx), d);
+                        }
+            }
+    }
+
     // heat::build_rhs_graph order: src/systems/heat.cpp:164-288
     void rhs(cfield u, sfield du, real time)
     {
         const mesh& m = P->m;
+        fill_neumann(time);
         // fill_source: heat.cpp:111-117
         eval_at_locations(m, [&](const real3& loc) {
             return sol.ddt(time, loc) - k * sol.laplacian(time, loc);

@@ -110,6 +110,7 @@ struct shoccs_system {
     // stage field, right-hand side and accumulator (D parts: b.sa, b.sb, b.acc)
     bool unfused = false;
     FieldF64 fy{}, fk{}, facc{};
+    NeumannFaces nf{}; // Neumann domain faces (unfused heat systems)
     FieldF64 state() const { return {(double*)b.u0, {b.R[0], b.R[1], b.R[2]}}; }
     ~shoccs_system()
     {
@@ -618,10 +619,12 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         return fail(SHOCCS_EUNSUPPORTED,
                     "non-Dirichlet objects (whose cut-point values evolve through the R-space "
                     "rows) are time-stepped by the FP64 heat system only");
+    int neumann_mask = 0;
     for (int a = 0; a < 3; a++)
         for (int side = 0; side < 2; side++)
-            if (p->bcs.grid[a][side] == Neumann)
-                return fail(SHOCCS_EUNSUPPORTED, "time stepping with Neumann faces");
+            if (p->bcs.grid[a][side] == Neumann) neumann_mask |= 1 << (2 * a + side);
+    if (neumann_mask && (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64))
+        return fail(SHOCCS_EUNSUPPORTED, "Neumann faces are time-stepped by the FP64 heat system only");
     if (d->kind == SHOCCS_SYS_HEAT && !(d->diffusivity > 0))
         return fail(SHOCCS_EINVAL, "diffusivity must be > 0");
     const cudaStream_t s = nullptr;
@@ -655,6 +658,9 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
             SH_CUDA(S->mem.put(tab, &sol.S[a], s));
             std::vector<float> tabf(tab.begin(), tab.end());
             SH_CUDA(S->mem.put(tabf, &sol.Sf[a], s));
+            std::vector<double> ctab(p->mesh.n[a]);
+            for (int i = 0; i < p->mesh.n[a]; i++) ctab[i] = std::cos(twoPI * k * p->mesh.x[a][i]);
+            SH_CUDA(S->mem.put(ctab, &sol.C[a], s));
         }
         for (int r = 0; r < 3; r++) {
             std::vector<double> tab;
@@ -705,8 +711,14 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.Rfull[r] = (double*)f;
         if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
     }
-    if (non_dirichlet_objects) {
+    if (non_dirichlet_objects || neumann_mask) {
         S->unfused = true;
+        if (neumann_mask) {
+            void* nu = nullptr;
+            SH_CUDA(S->mem.alloc((size_t)N * 8, &nu));
+            SH_CUDA(cudaMemsetAsync(nu, 0, (size_t)N * 8, s));
+            S->nf = NeumannFaces{neumann_mask, (double*)nu};
+        }
         S->fy.D = (double*)S->b.sa;
         S->fk.D = (double*)S->b.sb;
         S->facc.D = (double*)S->b.acc;
@@ -868,8 +880,8 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     double t = t0;
     for (int i = 0; i < nsteps; i++) {
         if (S->unfused)
-            SH_CUDA(launch_heat_step_unfused(S->P->op, S->P->dr, S->sp, S->state(), S->fy, S->fk,
-                                             S->facc, t, dt, s));
+            SH_CUDA(launch_heat_step_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), S->fy,
+                                             S->fk, S->facc, t, dt, s));
         else
             SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
                                     nullptr, i + 1 < nsteps));
@@ -955,7 +967,7 @@ shoccs_status shoccs_system_rhs(shoccs_system* S, double t, shoccs_field* rhs, v
     const cudaStream_t s = (cudaStream_t)stream;
     double* outR[3] = {(double*)rhs->Rx, (double*)rhs->Ry, (double*)rhs->Rz};
     if (S->unfused)
-        SH_CUDA(launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->state(), t,
+        SH_CUDA(launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), t,
                                         FieldF64{(double*)rhs->D, {outR[0], outR[1], outR[2]}}, s));
     else
         SH_CUDA(launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)rhs->D, outR, s));

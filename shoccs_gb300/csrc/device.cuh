@@ -65,6 +65,7 @@ struct DevSol {
     const double* S[3];  // SINSIN: sin(2 pi k x) tables per physical axis
     const float* Sf[3];  // SINSIN: the same tables rounded to FP32 (mixed heat source)
     const double* SR[3]; // SINSIN: product of sines at the cut points of R(d)
+    const double* C[3];  // SINSIN: cos(2 pi k x) tables (the gradient, Neumann data)
     double lapfac;       // SINSIN: -(dims) (2 pi k)^2
 };
 
@@ -77,6 +78,13 @@ struct DevR {
 struct FieldF64 {
     double* D;
     double* R[3];
+};
+
+// Neumann domain faces of a system: bit 2a + side per face, and the D-size array of the
+// Neumann data (the gradient component of the face's axis at the face points), or none
+struct NeumannFaces {
+    int mask;
+    double* nu;
 };
 
 // launch helpers implemented in kernels.cu -----------------------------------------------
@@ -240,10 +248,11 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
 // heat systems whose objects are not all Dirichlet (FP64): rhs of the whole field, and one
 // RK4 step of the whole field U with the scratch fields Y, K, ACC
 cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                    FieldF64 u, double t, FieldF64 out, cudaStream_t s);
+                                    NeumannFaces nf, FieldF64 u, double t, FieldF64 out,
+                                    cudaStream_t s);
 cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                     FieldF64 U, FieldF64 Y, FieldF64 K, FieldF64 ACC, double t,
-                                     double dt, cudaStream_t s);
+                                     NeumannFaces nf, FieldF64 U, FieldF64 Y, FieldF64 K,
+                                     FieldF64 ACC, double t, double dt, cudaStream_t s);
 // statistics of the non-Dirichlet cut points: out12[4d..4d+3] = {err, index (-1: none),
 // min, max} per axis
 cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, double* const R[3],

@@ -2522,16 +2522,62 @@ __global__ void k_update_boundary(DevOp op, DevR dr, DevSol sol, double t, doubl
     }
 }
 
+// Neumann data of heat::update_boundary (heat.cpp:324-352) at time t: on each Neumann face
+// of axis a, the gradient component a of the solution (sin-sin: 2 pi k cos(2 pi k x_a) times
+// the other axes' sines, times e^-t; zero otherwise), axes in order, so at an edge shared
+// with a later axis' Neumann face the later axis' value is the one written.
+__global__ void k_neumann_faces(DevOp op, DevSol sol, int mask, double et, double* nu)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int f = 0; f < 6; f++) {
+        const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        const long long fn = (mask >> f) & 1 ? (long long)op.n[b] * op.n[c] : 0;
+        if (i >= fn) {
+            i -= fn;
+            continue;
+        }
+        int ijk[3];
+        ijk[a] = (f & 1) ? op.n[a] - 1 : 0;
+        ijk[b] = (int)(i / op.n[c]);
+        ijk[c] = (int)(i - (long long)ijk[b] * op.n[c]);
+        for (int a2 = a + 1; a2 < 3; a2++) // a later axis' Neumann face holds this point
+            if (((mask >> (2 * a2)) & 1 && ijk[a2] == 0) ||
+                ((mask >> (2 * a2 + 1)) & 1 && ijk[a2] == op.n[a2] - 1))
+                return;
+        double v = 0.0;
+        if (sol.kind == SOL_SINSIN) {
+            const double kk = 2 * 3.14159265358979323846 * sol.p[0];
+            v = 1.0;
+            for (int d = 0; d < sol.dims; d++)
+                v = __dmul_rn(v, d == a ? __dmul_rn(kk, sol.C[d][ijk[d]]) : sol.S[d][ijk[d]]);
+            v = __dmul_rn(v, et);
+        }
+        const long long nyz = (long long)op.n[1] * op.n[2];
+        nu[ijk[0] * nyz + (long long)ijk[1] * op.n[2] + ijk[2]] = v;
+        return;
+    }
+}
+
 long long field_size(const DevOp& op) { return op.N + op.nR[0] + op.nR[1] + op.nR[2]; }
 
-cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, FieldF64 u,
-                             double t, FieldF64 K, cudaStream_t s)
+cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
+                             FieldF64 u, double t, FieldF64 K, cudaStream_t s)
 {
+    const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    if (nf.mask) {
+        long long nface = 0;
+        for (int f = 0; f < 6; f++)
+            if ((nf.mask >> f) & 1) {
+                const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+                nface += (long long)op.n[b] * op.n[c];
+            }
+        k_neumann_faces<<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(op, sp.sol, nf.mask, et, nf.nu);
+        ++g_launches;
+    }
     const void* uR[3] = {u.R[0], u.R[1], u.R[2]};
     void* kR[3] = {K.R[0], K.R[1], K.R[2]};
-    cudaError_t e = launch_laplacian(op, PREC_FP64, u.D, uR, nullptr, K.D, kR, s);
+    cudaError_t e = launch_laplacian(op, PREC_FP64, u.D, uR, nf.mask ? nf.nu : nullptr, K.D, kR, s);
     if (e != cudaSuccess) return e;
-    const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
     const long long n = field_size(op);
     k_heat_rhs_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sp, t, et, K);
     ++g_launches;
@@ -2540,15 +2586,16 @@ cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& s
 } // namespace
 
 cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                    FieldF64 u, double t, FieldF64 out, cudaStream_t s)
+                                    NeumannFaces nf, FieldF64 u, double t, FieldF64 out,
+                                    cudaStream_t s)
 {
-    return heat_rhs_unfused(op, dr, sp, u, t, out, s);
+    return heat_rhs_unfused(op, dr, sp, nf, u, t, out, s);
 }
 
 // one RK4 step of the whole field U (rk4.cpp:16-47) with the scratch fields Y, K, ACC
 cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                     FieldF64 U, FieldF64 Y, FieldF64 K, FieldF64 ACC, double t,
-                                     double dt, cudaStream_t s)
+                                     NeumannFaces nf, FieldF64 U, FieldF64 Y, FieldF64 K,
+                                     FieldF64 ACC, double t, double dt, cudaStream_t s)
 {
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -2570,7 +2617,7 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
             g_launches += 2;
             in = Y;
         }
-        e = heat_rhs_unfused(op, dr, sp, in, ti, K, s);
+        e = heat_rhs_unfused(op, dr, sp, nf, in, ti, K, s);
         if (e != cudaSuccess) break;
         k_field_lc<<<nb, 256, 0, s>>>(op, ACC, ACC, dt * rkf[i], K);
         ++g_launches;

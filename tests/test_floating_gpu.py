@@ -1,8 +1,11 @@
-"""Heat systems with Floating objects: the cut-point values of a Floating object are state,
-so the RK4 step advances the whole field {D, Rx, Ry, Rz} (src/temporal/rk4.cpp:16-47), their
-right-hand side comes from the Laplacian's R-space rows plus the source, and the statistics
-include them (compute_scalar_stats visits the non-Dirichlet cut points).  The FP64 heat system
-runs this unfused path; everything is checked against the oracle's heat rhs, rk4 and stats.
+"""Heat systems with Floating objects or Neumann faces.  The cut-point values of a Floating
+object are state, so the RK4 step advances the whole field {D, Rx, Ry, Rz}
+(src/temporal/rk4.cpp:16-47), their right-hand side comes from the Laplacian's R-space rows plus
+the source, and the statistics include them (compute_scalar_stats visits the non-Dirichlet cut
+points).  On Neumann faces the Laplacian's N rows take the solution's gradient component as
+Neumann data, evaluated at each right-hand side's time (heat::update_boundary,
+src/systems/heat.cpp:324-352).  The FP64 heat system runs these cases on its unfused path;
+everything is checked against the oracle's heat rhs, rk4 and stats.
 
 Tolerances (max-norm, relative to the oracle array's max-norm): rhs 1e-11, RK4 state 1e-10
 (FP64 arithmetic in a different order); errors, min and max to 1e-8; each argmax index must
@@ -26,6 +29,18 @@ CASES = {
                         spheres=[((0.3, 0.3, 0.0), 0.12, "floating"),
                                  ((0.7, 0.68, 0.0), 0.15, "dirichlet")],
                         grid_bc=("dirichlet",) * 4 + ("floating",) * 2, scheme="E2_2"),
+    "neumann_x_circle65": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                               spheres=[((0.51, 0.49, 0.0), 0.2, "dirichlet")],
+                               grid_bc=("neumann", "neumann", "dirichlet", "dirichlet",
+                                        "floating", "floating"), scheme="E4_2"),
+    "neumann_faces24_floating": dict(n=(24, 24, 24), lo=(0, 0, 0), hi=(1, 1, 1),
+                                     spheres=[((0.5, 0.5, 0.5), 0.25, "floating")],
+                                     grid_bc=("neumann", "dirichlet", "dirichlet", "neumann",
+                                              "neumann", "neumann"), scheme="E4_2"),
+    "neumann_e22": dict(n=(41, 41, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                        spheres=[((0.5, 0.5, 0.0), 0.2, "dirichlet")],
+                        grid_bc=("dirichlet", "neumann", "neumann", "dirichlet",
+                                 "floating", "floating"), scheme="E2_2"),
 }
 SOL = [1.0]  # sin(2 pi x) sin(2 pi y) (sin 2 pi z) e^-t
 
@@ -64,8 +79,9 @@ def test_floating_rhs_matches_oracle(name):
     got = h.rhs(t, p.zeros(torch.float64))
     for k, (g, w) in enumerate(zip(got, want)):
         assert rel(g.cpu().numpy(), w) <= 1e-11, (name, k)
-    # the Floating cut points have a nonzero right-hand side (they evolve)
-    assert any(np.abs(w).max() > 0 for w in want[1:])
+    if any(s_[2] == "floating" for s_ in c["spheres"]):
+        # the Floating cut points have a nonzero right-hand side (they evolve)
+        assert any(np.abs(w).max() > 0 for w in want[1:])
 
 
 @pytest.mark.gpu
@@ -113,5 +129,8 @@ def test_floating_systems_that_stay_unsupported():
     with pytest.raises(S.ShoccsError):  # and so do batched solves
         S.Batch([h])
     c["spheres"] = [((0.51, 0.49, 0.0), 0.2, "neumann")]
-    with pytest.raises(S.ShoccsError):
+    with pytest.raises(S.ShoccsError):  # Neumann objects
         S.Heat(S.Problem(**c), 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
+    pn = S.Problem(**CASES["neumann_x_circle65"])
+    with pytest.raises(S.ShoccsError):  # Neumann faces: FP64 heat only
+        S.Heat(pn, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
