@@ -769,6 +769,9 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
             auto it = pool.find(key);
             int off;
             if (it == pool.end()) {
+                // blocks start at even offsets, so the FP32-pair copy of the pool is read two
+                // coefficients (16 bytes) at a time; the pool ends with a zero pad for that
+                if (T.coef.size() % 2) T.coef.push_back(0.0);
                 off = (int)T.coef.size();
                 T.coef.insert(T.coef.end(), blk.begin(), blk.end());
                 pool.emplace(std::move(key), off);
@@ -785,6 +788,8 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
             T.rows.push_back(cr);
             T.row_out.push_back(p.out);
         }
+        T.coef.push_back(0.0);
+        if (T.coef.size() % 2) T.coef.push_back(0.0);
         // chunk prefix counts over the iteration space
         T.chunk_base.assign(n_chunks + 1, 0);
         const i64 it2 = C.it[2];

@@ -248,15 +248,22 @@ __device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long
     const ClosureRow cr = A.rows[row];
     const float2* c = A.coef_ff + cr.coef_off;
     const long long q0 = p + (long long)cr.col0 * A.stride;
-    // issue every load of the row before the first use, so the gathers overlap
+    // issue every load of the row before the first use, so the gathers overlap; the
+    // coefficients come two at a time (a block starts at an even offset of the pool, and the
+    // pool has a pad after its last coefficient)
     constexpr int PF = 8;
     float2 cv[PF], xv[PF];
+    const float4* c4 = reinterpret_cast<const float4*>(c);
+#pragma unroll
+    for (int m = 0; m < PF / 2; ++m)
+        if (2 * m < cr.ncol) {
+            const float4 v = __ldg(c4 + m);
+            cv[2 * m] = make_float2(v.x, v.y);
+            cv[2 * m + 1] = make_float2(v.z, v.w);
+        }
 #pragma unroll
     for (int j = 0; j < PF; ++j)
-        if (j < cr.ncol) {
-            cv[j] = __ldg(c + j);
-            xv[j] = ldff(u, q0 + j * A.stride);
-        }
+        if (j < cr.ncol) xv[j] = ldff(u, q0 + j * A.stride);
     double r = 0.0;
     float2 cb = make_float2(0.f, 0.f);
     if (cr.flags & ROWF_B) {
