@@ -16,6 +16,8 @@
 //   ccs::systems::heat        src/systems/heat.hpp:16-70
 //   ccs::systems::scalar_wave src/systems/scalar_wave.hpp:16-80
 //   ccs::integrators::rk4     src/temporal/rk4.hpp:10-20
+//   ccs::step_controller      src/temporal/step_controller.hpp:10-50
+//   ccs::simulation_cycle     src/simulation/simulation_cycle.cpp:31-143 (run)
 //
 // Differences a caller sees.  Fields are device buffers (scalar_span / scalar_view hold
 // device pointers and sizes), because the kernels run on the GPU; the reference's fields are
@@ -30,8 +32,14 @@
 #include "shoccs_gpu.h"
 
 #include <array>
+#include <charconv>
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <ctime>
 #include <functional>
+#include <limits>
+#include <ostream>
 #include <memory>
 #include <span>
 #include <stdexcept>
@@ -608,4 +616,110 @@ public:
     }
 };
 } // namespace integrators
+
+// ---- step controller and simulation cycle (src/temporal/step_controller.hpp,
+// src/simulation/simulation_cycle.cpp:31-143) -------------------------------------------------
+// The step and the time are bounded [min, max): the cycle runs while both are in bounds.
+class step_controller
+{
+    int step_ = 0, max_step_ = 0;
+    real time_ = 0.0, max_time_ = 0.0;
+    real h_cfl_ = 0.0, p_cfl_ = 0.0, min_dt_ = 0.0;
+
+public:
+    step_controller() = default;
+    step_controller(int max_step, real max_time, real hyperbolic_cfl, real parabolic_cfl,
+                    real min_dt = 0.0, real start_time = 0.0)
+        : max_step_{max_step}, time_{start_time}, max_time_{max_time}, h_cfl_{hyperbolic_cfl},
+          p_cfl_{parabolic_cfl}, min_dt_{min_dt}
+    {
+    }
+    explicit operator bool() const { return step_ < max_step_ && time_ < max_time_; }
+    real simulation_time() const { return time_; }
+    int simulation_step() const { return step_; }
+    real hyperbolic_cfl() const { return h_cfl_; }
+    real parabolic_cfl() const { return p_cfl_; }
+    bool check_timestep_size(real dt) const { return dt >= min_dt_; }
+    void advance(real dt)
+    {
+        time_ += dt;
+        step_ += 1;
+    }
+};
+
+namespace detail
+{
+inline real cfl_of(const systems::heat&, const step_controller& c) { return c.parabolic_cfl(); }
+inline real cfl_of(const systems::scalar_wave&, const step_controller& c) { return c.hyperbolic_cfl(); }
+
+// shortest round-trip text of a double, as fmt's "{}" prints it
+inline std::string num(real v)
+{
+    char buf[64];
+    const auto r = std::to_chars(buf, buf + sizeof buf, v);
+    return std::string(buf, r.ptr);
+}
+
+// the system log line of heat::log / scalar_wave::log (heat.cpp:60-68) behind the
+// "%Y-%m-%d %H:%M:%S.%f," pattern the systems set: time,step,stats...,wall ms
+inline void log_line(std::ostream& os, const step_controller& c, const system_stats& st)
+{
+    const auto now = std::chrono::system_clock::now();
+    const std::time_t tt = std::chrono::system_clock::to_time_t(now);
+    const auto us = std::chrono::duration_cast<std::chrono::microseconds>(now.time_since_epoch()).count() % 1000000;
+    std::tm tm{};
+    localtime_r(&tt, &tm);
+    char ts[64];
+    std::strftime(ts, sizeof ts, "%Y-%m-%d %H:%M:%S", &tm);
+    char frac[16];
+    std::snprintf(frac, sizeof frac, ".%06lld", (long long)us);
+    os << ts << frac << ',' << num(c.simulation_time()) << ',' << c.simulation_step();
+    for (real v : st.stats) os << ',' << num(v);
+    char wall[32];
+    std::snprintf(wall, sizeof wall, "%.3f", st.wall_time_s * 1000.0);
+    os << ',' << wall << '\n';
+}
+} // namespace detail
+
+// simulation_cycle::run: initialize, then step while the controller is in bounds and the
+// system's statistics are valid, logging the statistics of every step.  Returns {time,
+// error, error} when the run reached its bound in a valid state, {time, max, max} when it
+// ended early in an invalid state, and {max, 0, 0} when the step size fell below the
+// controller's minimum, as the reference does with null_v.
+class simulation_cycle
+{
+    step_controller ctrl_;
+    std::ostream* log_ = nullptr;
+
+public:
+    simulation_cycle() = default;
+    explicit simulation_cycle(const step_controller& c, std::ostream* system_log = nullptr)
+        : ctrl_{c}, log_{system_log}
+    {
+    }
+    const step_controller& controller() const { return ctrl_; }
+
+    template <typename System>
+    real3 run(System& sys)
+    {
+        constexpr real null = std::numeric_limits<real>::max();
+        sys.initialize(ctrl_.simulation_time());
+        system_stats stats = sys.stats(ctrl_.simulation_time());
+        if (log_) detail::log_line(*log_, ctrl_, stats);
+        const integrators::rk4 rk;
+        while (ctrl_ && sys.valid(stats)) {
+            const real dt = sys.timestep_size(detail::cfl_of(sys, ctrl_));
+            if (!ctrl_.check_timestep_size(dt)) return {null, 0.0, 0.0}; // "timestep too small"
+            const auto t0 = std::chrono::steady_clock::now();
+            rk(sys, ctrl_.simulation_time(), dt);
+            ctrl_.advance(dt);
+            stats = sys.stats(ctrl_.simulation_time());
+            stats.wall_time_s =
+                std::chrono::duration<real>(std::chrono::steady_clock::now() - t0).count();
+            if (log_) detail::log_line(*log_, ctrl_, stats);
+        }
+        if (ctrl_) return {ctrl_.simulation_time(), null, null};
+        return {ctrl_.simulation_time(), stats.stats[0], stats.stats[0]};
+    }
+};
 } // namespace ccs

@@ -158,6 +158,14 @@ int main(int argc, char** argv)
             for (int i = 0; i < 100; i++) step(h, i * dt, dt);
             std::fprintf(out, "stepwise linf %.17g\n", h.stats(100 * dt).stats[0]);
         }
+        // the simulation cycle: 100 steps of the heat case, the system log to a file
+        {
+            systems::heat h(mesh{m}, bcs::Grid{g}, bcs::Object{o}, mms::sinsin(1.0), st, 1.0);
+            std::ofstream log(dir + "/system.csv");
+            simulation_cycle cycle(step_controller(100, 1e9, 0.5, 0.4), &log);
+            const real3 r = cycle.run(h);
+            std::fprintf(out, "cycle %.17g %.17g %d\n", r[0], r[1], cycle.controller().simulation_step());
+        }
         // error behaviour: E4_1's alpha bound, and a status the library refuses
         try {
             const real bad[2] = {0.1, 0.5};

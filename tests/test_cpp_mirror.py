@@ -6,7 +6,7 @@ alpha[1] < 197/288 with std::invalid_argument as src/stencils/E4_1.cpp:37-40 doe
 GPU: tests/cpp/mirror_ops.cpp runs the 2-D heat case (65^2, circle, E4_2) and the three
 operators through the classes; every array must equal, bit for bit, what the Python binding
 gets from the same library on the same inputs, and the FP64 Laplacian must agree with the
-oracle to 1e-12.
+oracle to 1e-12; simulation_cycle runs the case for 100 steps and writes the system log.
 """
 import os
 import subprocess
@@ -132,5 +132,17 @@ def test_cpp_classes_match_the_python_binding(tmp_path):
     assert e64 < 1e-3 and e32 <= 1.1 * e64
     # one rk4 call per step gives the error of the fused multi-step call
     assert abs(float(stats["stepwise"][1]) - e64) <= 1e-12 * e64
+    # simulation_cycle: 100 steps, one log line per step plus the initial one, each
+    # timestamp,time,step,11 statistics,wall ms; the run ends in a valid state with the error
+    # of 100 steps
+    t_end, e_cycle, nstep = float(stats["cycle"][0]), float(stats["cycle"][1]), int(stats["cycle"][2])
+    assert nstep == 100 and abs(e_cycle - e64) <= 1e-12 * e64
+    assert abs(t_end - 100 * float(stats["fp64"][5])) <= 1e-12
+    lines = (tmp_path / "system.csv").read_text().splitlines()
+    assert len(lines) == 101
+    for k, line in enumerate(lines):
+        f = line.split(",")
+        assert len(f) == 15 and int(f[2]) == k
+    assert abs(float(lines[-1].split(",")[3]) - e_cycle) <= 1e-15 * e_cycle
     assert stats["e4_1_bound"] == ["invalid_argument"]
     assert stats["floating_object"] == ["status", "6"]  # SHOCCS_EUNSUPPORTED
