@@ -266,7 +266,8 @@ def operator_microbench(stream, peak, n=MICRO_N, reps=10):
     return out
 
 
-def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1):
+def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1, looped=True,
+                  precisions=("fp64", "mixed")):
     """The batched configuration: 256 independent 2-D heat instances (N ~ U{32..192}, one
     circle each, manufactured solution with k in {1, 2, 3}), 200 RK4 steps at dt = 0.1 h^2,
     in FP64 and mixed.  Timed: one run of the batch (a replay of the captured graph) against
@@ -282,6 +283,8 @@ def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1):
     out = {"instances": count, "rk4_steps": steps, "points": sum(p.size for p in probs),
            "seed": W.SEED_BATCH}
     for pname, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+        if pname not in precisions:
+            continue
         systems = [S.Heat(p, 1.0, prec, S.SOL_SINSIN, [float(it["k"])])
                    for p, it in zip(probs, insts)]
         for s in systems:
@@ -299,15 +302,17 @@ def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1):
         e1.synchronize()
         ms = reduce_max(e0.elapsed_time(e1) / reps, pg)
         # the same instances one system after another (no batching, no graph)
-        for s in systems[:4]:
-            s.rk4(0.0, dts[0], 2, stream)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for s, dt in zip(systems, dts):
-            s.rk4(0.0, dt, steps, stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms_loop = reduce_max(e0.elapsed_time(e1), pg)
+        ms_loop = float("nan")
+        if looped:
+            for s in systems[:4]:
+                s.rk4(0.0, dts[0], 2, stream)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for s, dt in zip(systems, dts):
+                s.rk4(0.0, dt, steps, stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms_loop = reduce_max(e0.elapsed_time(e1), pg)
         errs = [s.stats(steps * dt, stream)[0][0] for s, dt in zip(systems[:16], dts[:16])]
         info = batch.info()
         dof_all = reduce_sum(dof, pg)
@@ -476,6 +481,12 @@ def main():
                     help="run the adjoint configuration alone and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
                     help="run the batched heat solves alone and print their JSON")
+    ap.add_argument("--batch-steps", type=int, default=200,
+                    help="RK4 steps of the batched section (--batched-only)")
+    ap.add_argument("--batch-no-loop", action="store_true",
+                    help="skip the one-system-after-another comparison (--batched-only)")
+    ap.add_argument("--batch-prec", default="fp64,mixed",
+                    help="precisions of the batched section (--batched-only)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -504,7 +515,8 @@ def main():
                 peak, _ = measured_peak()
                 print(json.dumps(operator_microbench(st, peak)), flush=True)
             elif args.batched_only:
-                print(json.dumps(batched_bench(st)), flush=True)
+                print(json.dumps(batched_bench(st, steps=args.batch_steps, looped=not args.batch_no_loop,
+                                               precisions=args.batch_prec.split(","))), flush=True)
             else:
                 print(json.dumps(adjoint_bench(st)), flush=True)
         return 0
