@@ -268,8 +268,11 @@ shoccs_status ensure_op_scratch(shoccs_problem* p)
     int form = f(op.ax[0]);
     for (int d = 1; d < 3; d++)
         if (f(op.ax[d]) != form) form = FORM_ANY;
-    const bool ok = it[0] > 1 && it[1] > 1 && it[2] > 1 && it[2] % 4 == 0 && form != FORM_ANY &&
-                    op.N < (1LL << 31) - 64 &&
+    // z-wall rows travel in 16-word line records: at most 6 rows per wall block, and the
+    // line's first and last points in different lanes
+    const WallBlock* Wz = op.ax[2].wall;
+    const bool ok = it[0] > 1 && it[1] > 1 && it[2] >= 8 && it[2] % 4 == 0 && form != FORM_ANY &&
+                    Wz[0].rows <= 6 && Wz[1].rows <= 6 && op.N < (1LL << 31) - 64 &&
                     (long long)op.n_cut_rows + (long long)it[0] * it[1] < (1LL << 31) - 256;
     if (!ok) {
         op.op_form = -1; // not applicable: the per-point kernels serve this problem
@@ -277,10 +280,9 @@ shoccs_status ensure_op_scratch(shoccs_problem* p)
     }
     void* r = nullptr;
     SH_CUDA(p->mem.alloc((size_t)3 * op.N * sizeof(float), &r));
-    const WallBlock* W = op.ax[2].wall;
-    const size_t nzw = (size_t)it[0] * it[1] * (W[0].rows + W[1].rows);
+    const size_t nzw = (size_t)it[0] * it[1] * 16; // one 16-word record per z line
     void* z = nullptr;
-    SH_CUDA(p->mem.alloc(std::max<size_t>(nzw, 1) * sizeof(float), &z));
+    SH_CUDA(p->mem.alloc(nzw * sizeof(float), &z));
     op.op_rowv = (float*)r;
     op.op_zw = (float*)z;
     op.op_form = form;

@@ -49,7 +49,8 @@ struct DevOp {
     int n_cut_rows;      // cut-cell rows of all axes
     DevAxis ax[3];
     // scratch of the vectorised FP32 operators (3-D grids, nz a multiple of 4): cut-cell row
-    // values at their points (3 x N floats, axis-major) and z-wall row values (slot-major);
+    // values at their points (3 x N floats, axis-major) and the z-wall rows of every z line
+    // (16-word records: words 0..5 the left block's rows, 8..13 the right block's);
     // allocated on the first mixed-precision apply, null before
     float* op_rowv = nullptr;
     float* op_zw = nullptr;

@@ -560,13 +560,6 @@ struct StageArgs {
 
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 
-// z-wall rows: slot of the row of z coordinate k (the left block's rows, then the right
-// block's) in the slot-major table of the vectorised operators
-__device__ __forceinline__ int zwall_slot(const DevAxis& A, int k)
-{
-    return k * 2 < A.n ? k - A.wall[0].first_row : A.wall[0].rows + (k - A.wall[1].first_row);
-}
-
 // cut-cell rows of all axes: value = sum_j c_j u_j + b R_d[b] (FP64 path: FP64; mixed path:
 // compensated FP32, closure_ff), stored compacted in row order (cval) or -- for the
 // vectorised mixed stage -- scattered to their points in rowv (3 x N, axis-major), where a
@@ -1860,8 +1853,11 @@ long long kernel_launch_count() { return g_launches.load(); }
 // The layout of k_stage_mixed_vec: four z points per thread, float4 loads of the field at
 // the points and their stencil neighbours, interior rows from registers kept where the class
 // says "interior".  Cut-cell rows (FP64 arithmetic as op_row, Neumann-aware) and the z-wall
-// rows are evaluated first by k_op_rows into the problem's scratch, at the points / in a
-// slot-major table; x- and y-wall rows (whole planes, uniform across a warp) inline.
+// rows are evaluated first by k_op_rows into the problem's scratch: cut-cell rows at their
+// points, z-wall rows as one 16-word record per z line (words 0..5 the left block's rows,
+// 8..13 the right block's) that lanes 0..15 of the warps at the line's ends load at entry and
+// hand to the lanes holding those rows by warp shuffles; x- and y-wall rows (whole planes,
+// uniform across a warp) inline.
 // MODE 0..2: derivative along x, y, z (eq or, PLUS, plus_eq: only points with a row are
 // written); 3: Laplacian (every point, 0 where no axis has a row); 4: gradient (three
 // outputs, 0 where the axis has no row).
@@ -1888,22 +1884,29 @@ __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
     if (d1 < 3 || i >= nlines) return; // z walls only with the z axis
     const DevAxis& A = op.ax[2];
     const long long base = (long long)i * op.it2;
-    int slot = 0;
+    float w[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) w[m] = 0.f;
 #pragma unroll
     for (int side = 0; side < 2; side++) {
         const WallBlock& W = A.wall[side];
         float x[7];
 #pragma unroll
         for (int jj = 0; jj < 7; jj++) x[jj] = jj < W.cols ? __ldg(u + base + W.col0 + jj) : 0.f;
-        for (int r = 0; r < W.rows; r++, slot++) {
+#pragma unroll
+        for (int r = 0; r < 6; r++) {
+            if (r >= W.rows) continue;
             float acc = 0.f;
 #pragma unroll
             for (int jj = 0; jj < 7; jj++)
                 if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
             if (W.has_n && nu) acc = (float)fma(W.n[r], __ldg(nu + base + W.wall), (double)acc);
-            op.op_zw[(long long)slot * nlines + i] = acc;
+            w[side * 8 + r] = acc;
         }
     }
+    float4* o = reinterpret_cast<float4*>(op.op_zw + (long long)i * 16);
+#pragma unroll
+    for (int m = 0; m < 4; m++) o[m] = make_float4(w[4 * m], w[4 * m + 1], w[4 * m + 2], w[4 * m + 3]);
 }
 
 template <int MODE, bool PLUS, int FORM>
@@ -1943,6 +1946,12 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
         zR = ld4(u, p + (kc + 8 <= nz ? 4 : 0));
     }
     const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
+    float rec = 0.f; // the line's z-wall record word of this lane (k_op_rows)
+    if constexpr (NZ) {
+        const int lane = threadIdx.x;
+        if (lane < 8 ? blockIdx.x == 0 : (lane < 16 && blockIdx.x + 1 == gridDim.x))
+            rec = __ldg(op.op_zw + (long long)(i * ny + j) * 16 + lane);
+    }
     float v[3][4] = {};
     unsigned kq[3][4];
     bool cut = false, zwall = false, xywall = false;
@@ -1982,13 +1991,16 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
                     v[d][q] = rv[d * op.N + q];
     }
     if constexpr (NZ) {
-        if (zwall) {
-            const long long nlines = (long long)nx * ny;
-            const float* __restrict__ zt =
-                op.op_zw + (long long)zwall_slot(op.ax[2], k) * nlines + (i * ny + j);
+        if (__any_sync(FULL, zwall)) { // the record word of each z-wall row to its lane
+            const DevAxis& A = op.ax[2];
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (kq[2][q] == ROW_WALL) v[2][q] = zt[q * nlines];
+            for (int q = 0; q < 4; q++) {
+                const int kk = k + q;
+                const bool use = kq[2][q] == ROW_WALL;
+                const int w = kk * 2 < nz ? kk - A.wall[0].first_row : 8 + kk - A.wall[1].first_row;
+                const float val = __shfl_sync(FULL, rec, use ? w : 0);
+                if (use) v[2][q] = val;
+            }
         }
     }
     if constexpr (NX || NY) {
