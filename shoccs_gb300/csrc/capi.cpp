@@ -498,19 +498,21 @@ shoccs_status shoccs_gradient_apply(shoccs_problem* p, int prec, const shoccs_fi
 // ---------------------------------------------------------------------------------------
 // The vectorised stage kernels take the z-wall rows of a line from its 16-word record
 // (k_cut_rows): at most 6 rows per wall block (words 0..5 and 8..13), each block entirely on
-// its side of the line's middle (wall_side), no Neumann term, and nz >= 8 so that the first
-// and last points of a line sit in different lanes.
+// its side of the line's middle (wall_side), the left block's columns starting at the wall
+// and the right block's ending there (the record threads read the eight points at each end
+// of the line), no Neumann term, and nz >= 8 so that the first and last points of a line sit
+// in different lanes.
 static bool line_records_fit(const DevOp& op)
 {
     const int nz = op.it2;
     const WallBlock& L = op.ax[2].wall[0];
     const WallBlock& R = op.ax[2].wall[1];
     if (nz < 8) return false;
-    if (L.rows && (L.has_n || L.rows > 6 || L.cols > 7 || L.first_row < 0 ||
+    if (L.rows && (L.has_n || L.rows > 6 || L.cols > 7 || L.col0 != 0 || L.first_row < 0 ||
                    2 * (L.first_row + L.rows - 1) >= nz))
         return false;
-    if (R.rows && (R.has_n || R.rows > 6 || R.cols > 7 || 2 * R.first_row < nz ||
-                   R.first_row + R.rows > nz))
+    if (R.rows && (R.has_n || R.rows > 6 || R.cols > 7 || R.col0 + R.cols != nz ||
+                   2 * R.first_row < nz || R.first_row + R.rows > nz))
         return false;
     return true;
 }

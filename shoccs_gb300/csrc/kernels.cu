@@ -565,7 +565,7 @@ enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 // vectorised mixed stage -- scattered to their points in rowv (3 x N, axis-major), where a
 // lane finds its value with one load at its own index.
 //
-// With line records (lrec), threads past the cut-cell rows each fill the 16-word record of
+// With line records (lrec), the first threads of the grid each fill the 16-word record of
 // one z line for the vectorised stage: words 0..5 the line's left z-wall rows (coordinate
 // first_row + w, wall32's arithmetic), 6..7 the stage output's value at the line's first
 // point where that point is on a Dirichlet face (face_entry, face_pick), 8..13 and 14..15
@@ -601,6 +601,10 @@ __device__ __forceinline__ float2 face_pick(const float4* f)
         return make_float2(f->z, f->w);
 }
 
+// the FP32 plane of a mixed-path row input: the stage field, or the hi words of the solution
+__device__ __forceinline__ const float* fp32_plane(const float* u) { return u; }
+__device__ __forceinline__ const float* fp32_plane(const PairU& u) { return u.hi; }
+
 template <class TIN, class TOUT>
 __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
                            const double* R1, const double* R2, TOUT* __restrict__ cval,
@@ -608,54 +612,80 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
 {
     pdl_wait();
     pdl_trigger();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= op.n_cut_rows) {
-        if constexpr (!std::is_same<TIN, const double*>::value) {
-            const int line = i - op.n_cut_rows;
-            const int nlines = op.it0 * op.it1;
-            if (!sa.lrec || line >= nlines) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (!std::is_same<TIN, const double*>::value) {
+        // the line records come first in the grid, so their threads run beside the cut-cell
+        // rows instead of after them
+        const int nlines = sa.lrec ? op.it0 * op.it1 : 0;
+        if (i < nlines) {
+            const int line = i;
             const DevAxis& A = op.ax[2];
             const int nz = op.it2;
             const long long base = (long long)line * nz;
+            const float* __restrict__ hi = fp32_plane(u);
+            // the face values and the two line ends (the left block's columns start at the
+            // wall, the right block's end there: eight values at each end, two float4s each)
+            const int li = line / op.it1, lj = line - li * op.it1;
+            const float4* f0 = face_entry(sa, op, li, lj, 0);
+            const float4* f1 = face_entry(sa, op, li, lj, nz - 1);
+            const float4 fa = f0 ? *f0 : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 fb = f1 ? *f1 : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 l0 = __ldg((const float4*)(hi + base)), l1 = __ldg((const float4*)(hi + base + 4));
+            const float4 r0 = __ldg((const float4*)(hi + base + nz - 8)),
+                         r1 = __ldg((const float4*)(hi + base + nz - 4));
+            const float xl[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+            const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
             float w[16];
 #pragma unroll
             for (int m = 0; m < 16; m++) w[m] = 0.f;
-#pragma unroll
-            for (int side = 0; side < 2; side++) {
-                const WallBlock& W = A.wall[side];
-                float x[7];
-#pragma unroll
-                for (int jj = 0; jj < 7; jj++)
-                    x[jj] = jj < W.cols ? ldf(u, base + W.col0 + jj) : 0.f;
+            {
+                const WallBlock& W = A.wall[0]; // columns 0 .. cols-1
 #pragma unroll
                 for (int r = 0; r < 6; r++) {
                     if (r >= W.rows) continue;
                     float acc = 0.f; // wall32's operation order
 #pragma unroll
                     for (int jj = 0; jj < 7; jj++)
-                        if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
-                    w[side * 8 + r] = acc;
+                        if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], xl[jj], acc);
+                    w[r] = acc;
                 }
             }
-            const int li = line / op.it1, lj = line - li * op.it1;
+            {
+                const WallBlock& W = A.wall[1]; // columns nz-cols .. nz-1
+                const int sh = 8 - W.cols;
 #pragma unroll
-            for (int side = 0; side < 2; side++) {
-                const float4* f = face_entry(sa, op, li, lj, side ? nz - 1 : 0);
-                if (!f) continue;
-                const float2 fv = stage == 0   ? face_pick<0>(f)
-                                  : stage == 1 ? face_pick<1>(f)
-                                  : stage == 2 ? face_pick<2>(f)
-                                               : face_pick<3>(f);
-                w[side * 8 + 6] = fv.x;
-                w[side * 8 + 7] = fv.y;
+                for (int r = 0; r < 6; r++) {
+                    if (r >= W.rows) continue;
+                    float acc = 0.f;
+#pragma unroll
+                    for (int m = 1; m < 8; m++)
+                        if (m >= sh) acc = fmaf(W.cf[r * 7 + m - sh], xr[m], acc);
+                    w[8 + r] = acc;
+                }
+            }
+            auto pick = [stage](const float4& f) {
+                return stage < 2 ? make_float2(f.x, 0.f)
+                                 : (stage == 2 ? make_float2(f.y, 0.f) : make_float2(f.z, f.w));
+            };
+            if (f0) {
+                const float2 v = pick(fa);
+                w[6] = v.x;
+                w[7] = v.y;
+            }
+            if (f1) {
+                const float2 v = pick(fb);
+                w[14] = v.x;
+                w[15] = v.y;
             }
             float4* o = (float4*)(sa.lrec + (long long)line * 16);
 #pragma unroll
             for (int m = 0; m < 4; m++)
                 o[m] = make_float4(w[4 * m], w[4 * m + 1], w[4 * m + 2], w[4 * m + 3]);
+            return;
         }
-        return;
+        i -= nlines;
     }
+    if (i >= op.n_cut_rows) return;
     const double* R[3] = {R0, R1, R2};
     const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
     const DevAxis& A = op.ax[d];
