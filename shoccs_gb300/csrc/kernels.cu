@@ -1317,11 +1317,39 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     }
     if (__any_sync(FULL, xywall)) { // whole x / y wall planes: uniform across the warp
 #pragma unroll
-        for (int d = 0; d < 2; d++)
+        for (int d = 0; d < 2; d++) {
+            const bool wd = kq[d][0] == ROW_WALL || kq[d][1] == ROW_WALL ||
+                            kq[d][2] == ROW_WALL || kq[d][3] == ROW_WALL;
+            if (!__any_sync(FULL, wd)) continue;
+            // the block's columns for the four points as float4s, in two groups of at most
+            // four (two round trips, at most 16 registers of loads in flight); wall32's order
+            const DevAxis& A = op.ax[d];
+            const int coord = d == 0 ? i : j;
+            const WallBlock& W = A.wall[wall_side(A, coord)];
+            const int r = coord - W.first_row;
+            const int stride = d == 0 ? plane : nz;
+            const int q0 = p + (W.col0 - coord) * stride;
+            float sw[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int g = 0; g < 2; g++) {
+                float4 xw[4];
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const int col = 4 * g + jj;
+                    xw[jj] = col < W.cols ? ld4(in, q0 + col * stride) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const int col = 4 * g + jj;
+                    if (col < W.cols)
+#pragma unroll
+                        for (int q = 0; q < 4; q++) sw[q] = fmaf(W.cf[r * 7 + col], f4(xw[jj], q), sw[q]);
+                }
+            }
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (kq[d][q] == ROW_WALL)
-                    v[d][q] = wall32(op.ax[d], (long long)(p + q), d == 0 ? i : j, in);
+                if (kq[d][q] == ROW_WALL) v[d][q] = sw[q];
+        }
     }
     float ao[4], so[4];
     float2 uo[4];
