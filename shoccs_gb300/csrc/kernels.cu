@@ -3336,6 +3336,8 @@ __device__ __forceinline__ T interior_t(const DevOp& op, long long p, const int 
 template <class T>
 __global__ void __launch_bounds__(256) k_adj_stage(DevOp op, int S, AdjArgs a)
 {
+    pdl_wait();
+    pdl_trigger();
     const Pt q = point_of(op);
     if (!q.valid) return;
     const unsigned c = op.cls[q.p];
@@ -3363,6 +3365,8 @@ __global__ void __launch_bounds__(256) k_adj_stage(DevOp op, int S, AdjArgs a)
 template <class T>
 __global__ void k_adj_closure(DevOp op, AdjClosure cl, int S, AdjArgs a)
 {
+    pdl_wait();
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cl.n_tgt) return;
     const T* z = (const T*)a.z;
@@ -3399,6 +3403,8 @@ __device__ __forceinline__ bool row_reads(unsigned c, int d)
 
 __global__ void __launch_bounds__(256, 4) k_adj_stage_vec(DevOp op, int S, AdjArgs a)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nx = op.it0, ny = op.it1, nz = op.it2;
     const int j = blockIdx.y * BY + threadIdx.y;
     if (j >= ny) return;
@@ -3533,20 +3539,26 @@ cudaError_t launch_adjoint_stage(const DevOp& op, const AdjClosure& cl, int S, c
 {
     const bool vec = prec == PREC_MIXED && S > 0 && op.it0 > 1 && op.it1 > 1 && op.it2 > 1 &&
                      op.it2 % 4 == 0 && op.N < (1LL << 31) - 64;
+    // every kernel of the reverse sweep waits for its predecessor before it reads anything,
+    // so each is launched to start while the previous one drains (dependent launch)
+    cudaError_t e;
     if (vec)
-        k_adj_stage_vec<<<dim3((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0),
-                          dim3(32, BY), 0, s>>>(op, S, a);
+        e = launch_ex(k_adj_stage_vec, dim3((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0),
+                      dim3(32, BY), s, true, op, S, a);
     else if (prec == PREC_MIXED)
-        k_adj_stage<float><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
+        e = launch_ex(k_adj_stage<float>, point_grid(op), dim3(32, BY), s, true, op, S, a);
     else
-        k_adj_stage<double><<<point_grid(op), dim3(32, BY), 0, s>>>(op, S, a);
+        e = launch_ex(k_adj_stage<double>, point_grid(op), dim3(32, BY), s, true, op, S, a);
     ++g_launches;
+    if (e != cudaSuccess) return e;
     if (cl.n_tgt) {
+        const dim3 g((cl.n_tgt + 127) / 128);
         if (prec == PREC_MIXED)
-            k_adj_closure<float><<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
+            e = launch_ex(k_adj_closure<float>, g, dim3(128), s, true, op, cl, S, a);
         else
-            k_adj_closure<double><<<(cl.n_tgt + 127) / 128, 128, 0, s>>>(op, cl, S, a);
+            e = launch_ex(k_adj_closure<double>, g, dim3(128), s, true, op, cl, S, a);
         ++g_launches;
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
