@@ -68,6 +68,24 @@ __device__ __forceinline__ double ldd(const PairU& u, long long i)
 {
     return (double)__ldg(u.hi + i) + (double)__ldg(u.hi + u.n + i);
 }
+
+// launch with programmatic stream serialisation when pdl is set (see pdl_wait)
+template <class... KArgs, class... Args>
+cudaError_t launch_ex(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, bool pdl,
+                      Args&&... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 __device__ __forceinline__ float ldf(const PairU& u, long long i) { return __ldg(u.hi + i); }
 __device__ __forceinline__ float2 ld_pair(const void* u0, long long n, long long i)
 {
@@ -1925,6 +1943,7 @@ __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
                           const float* R0, const float* R1, const float* R2,
                           const double* __restrict__ nu)
 {
+    pdl_trigger(); // the operator kernel after it may start and issue its stencil loads
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int r0 = op.ax[d0].row_base, r1 = d1 < 3 ? op.ax[d1].row_base : op.n_cut_rows;
     if (i < r1 - r0) {
@@ -1973,6 +1992,7 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
                                                    float* __restrict__ o0, float* __restrict__ o1,
                                                    float* __restrict__ o2)
 {
+    pdl_trigger();
     constexpr bool NX = MODE == 0 || MODE >= 3, NY = MODE == 1 || MODE >= 3,
                    NZ = MODE == 2 || MODE >= 3;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
@@ -2004,6 +2024,7 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
         zR = ld4(u, p + (kc + 8 <= nz ? 4 : 0));
     }
     const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
+    pdl_wait(); // what k_op_rows wrote is read below
     float rec = 0.f; // the line's z-wall record word of this lane (k_op_rows)
     if constexpr (NZ) {
         const int lane = threadIdx.x;
@@ -2115,13 +2136,15 @@ template <int MODE, bool PLUS>
 void op_vec(const DevOp& op, const float* u, const double* nu, float* o0, float* o1, float* o2,
             cudaStream_t s)
 {
+    // dependent launch after k_op_rows: the kernel issues its stencil loads and waits for
+    // the prepass before it reads the cut-cell values and the z-wall records
     const dim3 grid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0), block(32, BY);
     if (op.op_form == FORM_ANTI5)
-        k_op_vec<MODE, PLUS, FORM_ANTI5><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+        launch_ex(k_op_vec<MODE, PLUS, FORM_ANTI5>, grid, block, s, true, op, u, nu, o0, o1, o2);
     else if (op.op_form == FORM_SYM5)
-        k_op_vec<MODE, PLUS, FORM_SYM5><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+        launch_ex(k_op_vec<MODE, PLUS, FORM_SYM5>, grid, block, s, true, op, u, nu, o0, o1, o2);
     else
-        k_op_vec<MODE, PLUS, FORM_W3><<<grid, block, 0, s>>>(op, u, nu, o0, o1, o2);
+        launch_ex(k_op_vec<MODE, PLUS, FORM_W3>, grid, block, s, true, op, u, nu, o0, o1, o2);
     ++g_launches;
 }
 
@@ -2257,23 +2280,6 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
 
 namespace
 {
-// launch with programmatic stream serialisation when pdl is set (see pdl_wait)
-template <class... KArgs, class... Args>
-cudaError_t launch_ex(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, bool pdl,
-                      Args&&... args)
-{
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = pdl ? at : nullptr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
-}
 
 template <int STAGE, int SYS>
 void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArgs& a,
