@@ -759,7 +759,8 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         }
         int lo = 0, hi = 0;
         SH_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        SH_CUDA(cudaStreamCreateWithPriority(&S->b.side, cudaStreamNonBlocking, hi));
+        // normal priority: its work is needed a step later, so the stage kernels go first
+        SH_CUDA(cudaStreamCreateWithPriority(&S->b.side, cudaStreamNonBlocking, lo));
         SH_CUDA(cudaEventCreateWithFlags(&S->b.fork, cudaEventDisableTiming));
         SH_CUDA(cudaEventCreateWithFlags(&S->b.join, cudaEventDisableTiming));
         SH_CUDA(cudaEventCreateWithFlags(&S->b.join_next, cudaEventDisableTiming));

@@ -1724,10 +1724,22 @@ struct BcRArgs {
     int fn[6];         // points per face plane (0 where not filled)
 };
 // threads past the cut points fill the Dirichlet face planes of the mixed path
-__global__ void k_bc_r(DevOp op, DevR dr, DevSol sol, BcRArgs ra, double t1, double et1,
-                       double t2, double et2)
+// One item (a cut point or a face point) per iteration of a grid-stride loop: on the side
+// stream the kernel runs on a small grid, a step ahead of the stage kernels it feeds, so that
+// it holds few of the warp slots those occupancy-bound kernels run in.
+__device__ __forceinline__ void bc_r_item(const DevOp& op, const DevR& dr, const DevSol& sol,
+                                          const BcRArgs& ra, int i, double t1, double et1,
+                                          double t2, double et2);
+__global__ void k_bc_r(DevOp op, DevR dr, DevSol sol, BcRArgs ra, int total, double t1,
+                       double et1, double t2, double et2)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        bc_r_item(op, dr, sol, ra, i, t1, et1, t2, et2);
+}
+__device__ __forceinline__ void bc_r_item(const DevOp& op, const DevR& dr, const DevSol& sol,
+                                          const BcRArgs& ra, int i, double t1, double et1,
+                                          double t2, double et2)
+{
     int d = 0;
     while (d < 3 && i >= ra.n[d]) i -= ra.n[d++];
     if (d == 3) {
@@ -2429,8 +2441,17 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
             tot += ra.fn[k];
         }
         if (tot) {
-            k_bc_r<<<(unsigned)((tot + 127) / 128), 128, 0, bs>>>(op, dr, sp.sol, ra, h, et(h),
-                                                                  f, et(f));
+            // inline (no side stream): one thread per item; on the side stream: two blocks
+            // per SM, looping, a step ahead of the stage kernels
+            static int sms = 0;
+            if (!sms) {
+                int dev = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            }
+            const long long full = (tot + 127) / 128;
+            const unsigned nb = (unsigned)(bs == s ? full : std::min<long long>(full, 2LL * std::max(sms, 1)));
+            k_bc_r<<<nb, 128, 0, bs>>>(op, dr, sp.sol, ra, (int)tot, h, et(h), f, et(f));
             ++g_launches;
         }
     };
