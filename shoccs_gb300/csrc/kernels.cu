@@ -518,36 +518,76 @@ __global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict_
     }
 }
 
-// R-space rows (Bf then Br of one derivative) accumulated into du.R_r (always +=)
+// R-space rows (Bf then Br of each derivative) accumulated into du.R_r (always +=): one
+// launch for every target r and every axis in dmask.  A thread owns one row of one target
+// and adds the axes in order, rounding to T after each axis -- what one launch per (axis,
+// target) in that order stores -- so the result does not depend on how the rows are grouped.
+struct RspaceAll {
+    const int* u[3][3]; // [axis][target]
+    const int* col[3][3];
+    const unsigned char* src[3][3];
+    const double* w[3][3];
+    int n[3]; // rows of each target (0 where no axis in the mask has rows for it)
+};
+
 template <class T>
-__global__ void k_rspace(int nrows, const int* __restrict__ ru, const int* __restrict__ rc,
-                         const unsigned char* __restrict__ rs, const double* __restrict__ rw,
-                         const T* __restrict__ uD, const T* __restrict__ uR, T* __restrict__ duR)
+__global__ void k_rspace_all(RspaceAll ra, int dmask, const T* __restrict__ uD,
+                             const T* __restrict__ uR0, const T* __restrict__ uR1,
+                             const T* __restrict__ uR2, T* __restrict__ du0,
+                             T* __restrict__ du1, T* __restrict__ du2)
 {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= nrows) return;
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    int r = 0;
+    while (r < 3 && row >= ra.n[r]) row -= ra.n[r++];
+    if (r == 3) return;
+    const T* __restrict__ uR = r == 0 ? uR0 : (r == 1 ? uR1 : uR2);
+    T* __restrict__ duR = r == 0 ? du0 : (r == 1 ? du1 : du2);
     double t = (double)duR[row];
-    for (int q = ru[row]; q < ru[row + 1]; q++) {
-        const double x = rs[q] ? (double)uR[rc[q]] : (double)uD[rc[q]];
-        t = fma(rw[q], x, t);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (!((dmask >> d) & 1) || !ra.u[d][r]) continue;
+        const int* __restrict__ ru = ra.u[d][r];
+        for (int q = ru[row]; q < ru[row + 1]; q++) {
+            const double x = ra.src[d][r][q] ? (double)uR[ra.col[d][r][q]] : (double)uD[ra.col[d][r][q]];
+            t = fma(ra.w[d][r][q], x, t);
+        }
+        t = (double)(T)t;
     }
     duR[row] = (T)t;
+}
+
+// the R-space rows of the axes in dmask (active axes only), one launch
+template <class T>
+cudaError_t rspace_axes(const DevOp& op, int dmask, const void* uD, const void* const uR[3],
+                        void* const duR[3], cudaStream_t s)
+{
+    RspaceAll ra{};
+    long long total = 0;
+    for (int r = 0; r < 3; r++) {
+        for (int d = 0; d < 3; d++) {
+            const DevAxis& A = op.ax[d];
+            if (!((dmask >> d) & 1) || !A.active || A.rr_rows[r] == 0 || !A.rr_u[r]) continue;
+            ra.u[d][r] = A.rr_u[r];
+            ra.col[d][r] = A.rr_col[r];
+            ra.src[d][r] = A.rr_src[r];
+            ra.w[d][r] = A.rr_w[r];
+            ra.n[r] = A.rr_rows[r];
+        }
+        total += ra.n[r];
+    }
+    if (!total) return cudaSuccess;
+    k_rspace_all<T><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        ra, dmask, (const T*)uD, (const T*)uR[0], (const T*)uR[1], (const T*)uR[2], (T*)duR[0],
+        (T*)duR[1], (T*)duR[2]);
+    ++g_launches;
+    return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t rspace_for(const DevOp& op, int d, const void* uD, const void* const uR[3],
                        void* const duR[3], cudaStream_t s)
 {
-    const DevAxis& A = op.ax[d];
-    for (int r = 0; r < 3; r++) {
-        if (A.rr_rows[r] == 0 || !A.rr_u[r]) continue;
-        const int n = A.rr_rows[r];
-        k_rspace<T><<<(n + 127) / 128, 128, 0, s>>>(n, A.rr_u[r], A.rr_col[r], A.rr_src[r],
-                                                   A.rr_w[r], (const T*)uD, (const T*)uR[r],
-                                                   (T*)duR[r]);
-        ++g_launches;
-    }
-    return cudaGetLastError();
+    return rspace_axes<T>(op, 1 << d, uD, uR, duR, s);
 }
 
 // ===========================================================================================
@@ -2234,20 +2274,17 @@ cudaError_t launch_laplacian(const DevOp& op, int prec, const void* uD, const vo
                                                    (const double*)uR[1], (const double*)uR[2],
                                                    nuD, (double*)duD);
         ++g_launches;
-        for (int d = 0; d < 3; d++)
-            if (op.ax[d].active) rspace_for<double>(op, d, uD, uR, duR, s);
+        rspace_axes<double>(op, 7, uD, uR, duR, s);
     } else if (op_vec_ok(op)) {
         op_rows(op, 0, 3, (const float*)uD, uR, nuD, s);
         op_vec<3, false>(op, (const float*)uD, nuD, (float*)duD, nullptr, nullptr, s);
-        for (int d = 0; d < 3; d++)
-            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, duR, s);
+        rspace_axes<float>(op, 7, uD, uR, duR, s);
     } else {
         k_laplacian<float><<<grid, block, 0, s>>>(op, (const float*)uD, (const float*)uR[0],
                                                   (const float*)uR[1], (const float*)uR[2], nuD,
                                                   (float*)duD);
         ++g_launches;
-        for (int d = 0; d < 3; d++)
-            if (op.ax[d].active) rspace_for<float>(op, d, uD, uR, duR, s);
+        rspace_axes<float>(op, 7, uD, uR, duR, s);
     }
     return cudaGetLastError();
 }
