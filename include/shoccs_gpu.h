@@ -162,7 +162,8 @@ shoccs_status shoccs_system_destroy(shoccs_system* s);
  * the Laplacian's R-space rows (rk4 advances the whole field {D, Rx, Ry, Rz}, as
  * src/temporal/rk4.cpp:16-47 does), and Neumann faces, whose Neumann data is the solution's
  * gradient at each right-hand side's time (heat::update_boundary,
- * src/systems/heat.cpp:324-352).  Neumann objects: SHOCCS_EUNSUPPORTED. */
+ * src/systems/heat.cpp:324-352).  Neumann objects step like Floating ones (heat::rhs adds
+ * the source at every non-Dirichlet cut point and assigns no Neumann data to objects). */
 /* u0 <- exact solution at time t on fluid D points, 0 on solid points, exact on R */
 shoccs_status shoccs_system_initialize(shoccs_system* s, double t, void* stream);
 /* copy the state in/out as FP64; where = 0 host pointers, 1 device pointers */

@@ -613,12 +613,11 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         return fail(SHOCCS_EINVAL, "unknown system kind");
     if (d->prec != 0 && d->prec != 1) return fail(SHOCCS_EINVAL, "unknown precision");
     if (d->sol_kind < 0 || d->sol_kind > 3) return fail(SHOCCS_EINVAL, "unknown solution kind");
+    // Neumann objects step like Floating ones: heat::rhs adds the source at every
+    // non-Dirichlet cut point (heat.cpp:143-149) and the object part of the Neumann data
+    // (neumann_rx/ry/rz) is never assigned, so their closures carry no data term
     bool non_dirichlet_objects = false;
-    for (int b : p->bcs.obj) {
-        if (b == Neumann)
-            return fail(SHOCCS_EUNSUPPORTED, "time stepping with Neumann objects");
-        non_dirichlet_objects = non_dirichlet_objects || b != Dirichlet;
-    }
+    for (int b : p->bcs.obj) non_dirichlet_objects = non_dirichlet_objects || b != Dirichlet;
     if (non_dirichlet_objects && (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64))
         return fail(SHOCCS_EUNSUPPORTED,
                     "non-Dirichlet objects (whose cut-point values evolve through the R-space "

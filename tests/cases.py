@@ -55,6 +55,12 @@ def cases():
         "neumann_e22": dict(n=(17, 18, 16), lo=(0, 0, 0), hi=(1, 1, 1),
                             spheres=[((0.45, 0.52, 0.5), 0.27, FLT)],
                             grid_bc=(NEU, FLT, FLT, NEU, DIR, FLT), scheme="E2_2"),
+        # a Neumann sphere beside a Dirichlet one (E4_2): the object's Neumann closure rows
+        # keep its cut point as a column and carry no Neumann data; one Neumann face
+        "neumann_objects_e42": dict(n=(26, 24, 28), lo=(0, 0, 0), hi=(1, 1, 1),
+                                    spheres=[((0.3, 0.33, 0.36), 0.14, NEU),
+                                             ((0.66, 0.64, 0.62), 0.14, DIR)],
+                                    grid_bc=(DIR, FLT, NEU, DIR, FLT, DIR), scheme="E4_2"),
         # several seeded spheres, E4_1 (Dirichlet objects)
         "multi_sphere_e41": dict(n=(64, 60, 66), lo=(0, 0, 0), hi=(1, 1, 1),
                                  spheres=random_spheres(5, 20261204, lo=0.3, hi=0.7,

@@ -1,8 +1,9 @@
-"""Heat systems with Floating objects or Neumann faces.  The cut-point values of a Floating
-object are state, so the RK4 step advances the whole field {D, Rx, Ry, Rz}
+"""Heat systems with Floating or Neumann objects, or Neumann faces.  The cut-point values of a
+non-Dirichlet object are state, so the RK4 step advances the whole field {D, Rx, Ry, Rz}
 (src/temporal/rk4.cpp:16-47), their right-hand side comes from the Laplacian's R-space rows plus
-the source, and the statistics include them (compute_scalar_stats visits the non-Dirichlet cut
-points).  On Neumann faces the Laplacian's N rows take the solution's gradient component as
+the source (heat::rhs adds it at every non-Dirichlet cut point; a Neumann object's closure
+carries no Neumann data, the object part of the reference's Neumann data is never assigned),
+and the statistics include them (compute_scalar_stats visits the non-Dirichlet cut points).  On Neumann faces the Laplacian's N rows take the solution's gradient component as
 Neumann data, evaluated at each right-hand side's time (heat::update_boundary,
 src/systems/heat.cpp:324-352).  The FP64 heat system runs these cases on its unfused path;
 everything is checked against the oracle's heat rhs, rk4 and stats.
@@ -41,6 +42,15 @@ CASES = {
                         spheres=[((0.5, 0.5, 0.0), 0.2, "dirichlet")],
                         grid_bc=("dirichlet", "neumann", "neumann", "dirichlet",
                                  "floating", "floating"), scheme="E2_2"),
+    "neumann_circle49_e22": dict(n=(49, 49, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                                 spheres=[((0.52, 0.47, 0.0), 0.21, "neumann")],
+                                 grid_bc=("dirichlet",) * 4 + ("floating",) * 2, scheme="E2_2"),
+    "neumann_and_dirichlet_spheres26": dict(n=(26, 24, 28), lo=(0, 0, 0), hi=(1, 1, 1),
+                                            spheres=[((0.3, 0.33, 0.36), 0.14, "neumann"),
+                                                     ((0.66, 0.64, 0.62), 0.14, "dirichlet")],
+                                            grid_bc=("dirichlet", "floating", "neumann",
+                                                     "dirichlet", "floating", "dirichlet"),
+                                            scheme="E4_2"),
 }
 SOL = [1.0]  # sin(2 pi x) sin(2 pi y) (sin 2 pi z) e^-t
 
@@ -79,8 +89,8 @@ def test_floating_rhs_matches_oracle(name):
     got = h.rhs(t, p.zeros(torch.float64))
     for k, (g, w) in enumerate(zip(got, want)):
         assert rel(g.cpu().numpy(), w) <= 1e-11, (name, k)
-    if any(s_[2] == "floating" for s_ in c["spheres"]):
-        # the Floating cut points have a nonzero right-hand side (they evolve)
+    if any(s_[2] != "dirichlet" for s_ in c["spheres"]):
+        # the non-Dirichlet cut points have a nonzero right-hand side (they evolve)
         assert any(np.abs(w).max() > 0 for w in want[1:])
 
 
@@ -128,9 +138,12 @@ def test_floating_systems_that_stay_unsupported():
         h.forward(0.0, 1e-5, 2)
     with pytest.raises(S.ShoccsError):  # and so do batched solves
         S.Batch([h])
-    c["spheres"] = [((0.51, 0.49, 0.0), 0.2, "neumann")]
-    with pytest.raises(S.ShoccsError):  # Neumann objects
-        S.Heat(S.Problem(**c), 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
+    pno = S.Problem(**CASES["neumann_circle49_e22"])
+    assert S.Heat(pno, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL).stage_kernel == "unfused"
+    with pytest.raises(S.ShoccsError):  # Neumann objects: FP64 heat only
+        S.Heat(pno, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    with pytest.raises(S.ShoccsError):
+        S.ScalarWave(pno, S.PREC_FP64)
     pn = S.Problem(**CASES["neumann_x_circle65"])
     with pytest.raises(S.ShoccsError):  # Neumann faces: FP64 heat only
         S.Heat(pn, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
