@@ -18,6 +18,10 @@
 //   ccs::integrators::rk4     src/temporal/rk4.hpp:10-20
 //   ccs::step_controller      src/temporal/step_controller.hpp:10-50
 //   ccs::simulation_cycle     src/simulation/simulation_cycle.cpp:31-143 (run)
+//   ccs::interval, d_interval src/io/interval.hpp:9-97
+//   ccs::xdmf, field_data, field_io
+//                             src/io/xdmf.cpp:20-179, src/io/field_data.cpp:8-57,
+//                             src/io/field_io.cpp:29-103
 //
 // Differences a caller sees.  Fields are device buffers (scalar_span / scalar_view hold
 // device pointers and sizes), because the kernels run on the GPU; the reference's fields are
@@ -37,8 +41,12 @@
 #include <cstdint>
 #include <cstdio>
 #include <ctime>
+#include <filesystem>
+#include <fstream>
 #include <functional>
+#include <iterator>
 #include <limits>
+#include <optional>
 #include <ostream>
 #include <memory>
 #include <span>
@@ -456,6 +464,9 @@ inline manufactured_solution radial_sin(const real3& c, real r)
 }
 } // namespace mms
 
+class field_io;
+class step_controller;
+
 namespace systems
 {
 // the state, the RK4 registers and the boundary data of a system live on the device
@@ -525,6 +536,18 @@ public:
         detail::check(shoccs_system_timestep(s_.get(), cfl, &dt), "shoccs_system_timestep");
         return dt;
     }
+    // |u - exact(t)| at the fluid D points and the non-Dirichlet cut points, 0 elsewhere
+    // (FP64; on_device selects device or host buffers)
+    void error_field(real t, scalar_span err, bool on_device = true) const
+    {
+        shoccs_field f = detail::field(err);
+        detail::check(shoccs_system_error_field(s_.get(), t, &f, on_device ? 1 : 0, stream_),
+                      "shoccs_system_error_field");
+    }
+    // system::write: the fields "U" (the state) and "Error" through the field writer when
+    // its schedule fires at this step (write_scalar_error,
+    // src/systems/detail/scalar_system_utils.hpp:224-296); true when it wrote
+    bool write(field_io& io, const step_controller& c, real dt) const;
 };
 
 // dT/dt = k lap T + the manufactured source (src/systems/heat.hpp:16-70)
@@ -681,8 +704,365 @@ inline void log_line(std::ostream& os, const step_controller& c, const system_st
 }
 } // namespace detail
 
+// ---- field output (src/io/interval.hpp, src/io/field_data.cpp, src/io/xdmf.cpp,
+// src/io/field_io.cpp) ------------------------------------------------------------------------
+// interval: true once a value has moved at least `distance` (less a tolerance) past the last
+// accepted one; ++ accepts, so the next firing is measured from the last target, not from
+// the value that fired (rollover).  A default interval never fires.
+template <typename T>
+class interval
+{
+    std::optional<T> distance_;
+    T first_{};
+
+public:
+    interval() = default;
+    interval(T distance, T first = T{}) : distance_{distance}, first_{first} {}
+    bool operator()(T val, T tolerance = T{}) const
+    {
+        return distance_ && val - first_ >= *distance_ - tolerance;
+    }
+    explicit operator bool() const { return distance_.has_value(); }
+    interval& operator++()
+    {
+        first_ += distance_.value_or(T{});
+        return *this;
+    }
+    interval& operator--()
+    {
+        first_ -= distance_.value_or(T{});
+        return *this;
+    }
+};
+
+// the dump schedule: every so many steps and/or every so much simulation time (the time
+// test allows one step size of slack), and always at step 0 when either is set
+class d_interval
+{
+    interval<int> step_interval_;
+    interval<real> time_interval_;
+    int ndumps_ = 0;
+    bool step_ready_ = false, time_ready_ = false;
+
+public:
+    d_interval() = default;
+    d_interval(interval<int> step_interval, interval<real> time_interval)
+        : step_interval_{step_interval}, time_interval_{time_interval}
+    {
+    }
+    bool operator()(const step_controller& step, real dt);
+    int current_dump() const { return ndumps_; }
+    d_interval& operator++()
+    {
+        if (step_ready_) ++step_interval_;
+        if (time_ready_) ++time_interval_;
+        ++ndumps_;
+        return *this;
+    }
+};
+
+// cut-point positions of R(x), R(y), R(z) (mesh_object_info::position per cut point)
+using cut_positions = std::array<std::span<const real3>, 3>;
+
+namespace detail
+{
+// "%.17g": the text pugixml gives a double attribute
+inline std::string num17(real v)
+{
+    char buf[40];
+    std::snprintf(buf, sizeof buf, "%.17g", v);
+    return buf;
+}
+inline std::string xml_escape(const std::string& s)
+{
+    std::string o;
+    for (char c : s) {
+        if (c == '&') o += "&amp;";
+        else if (c == '<') o += "&lt;";
+        else if (c == '>') o += "&gt;";
+        else if (c == '"') o += "&quot;";
+        else o += c;
+    }
+    return o;
+}
+template <typename R>
+std::string join(const R& r)
+{
+    std::string o;
+    for (auto v : r) {
+        if (!o.empty()) o += ' ';
+        o += num(v);
+    }
+    return o;
+}
+} // namespace detail
+
+// xdmf: the XDMF 3.0 index of a run.  Grid 0 writes the outline (the co-rectilinear grid,
+// its origin and spacing, one polyvertex geometry per cut-point axis read from the binary
+// files rx, ry, rz, and an empty temporal collection); every grid appends one spatial
+// collection to the temporal one: the grid F and the cut points RX, RY, RZ (those with
+// points), each with one binary attribute per variable, the cut-point parts at the byte
+// offset (Seek) where they follow D in the variable's file.  The file is written in the
+// layout pugixml's default save gives the reference's document (tab indentation, empty
+// elements as "<name ... />", doubles as %.17g attributes), and each write appends to the
+// file on disk, as the reference reloads and saves it.
+class xdmf
+{
+    std::string xmf_filename_;
+    index_extents ix_;
+    domain_extents bounds_;
+
+    std::string header(const cut_positions& t) const
+    {
+        const auto& n = ix_.extents;
+        real3 dxyz;
+        for (int i = 0; i < 3; i++) dxyz[i] = (bounds_.max[i] - bounds_.min[i]) / std::max(n[i] - 1.0, 1.0);
+        std::string h = "<?xml version=\"1.0\" encoding=\"utf-8\"?>\n"
+                        "<!DOCTYPE Xdmf SYSTEM \"Xdmf.dtd\" []>\n"
+                        "<Xdmf Version=\"3.0\">\n\t<Domain>\n";
+        h += "\t\t<Topology TopologyType=\"3DCoRectMesh\" Dimensions=\"" + detail::join(n) + "\" />\n";
+        h += "\t\t<Geometry GeometryType=\"Origin_DxDyDz\">\n";
+        h += "\t\t\t<DataItem Format=\"XML\" NumberType=\"Float\" Dimensions=\"3\">" +
+             detail::join(bounds_.min) + "</DataItem>\n";
+        h += "\t\t\t<DataItem Format=\"XML\" NumberType=\"Float\" Dimensions=\"3\">" + detail::join(dxyz) +
+             "</DataItem>\n\t\t</Geometry>\n";
+        const char* names[3] = {"rx", "ry", "rz"};
+        for (int d = 0; d < 3; d++) {
+            const std::string c = std::to_string(t[d].size());
+            h += "\t\t<Topology TopologyType=\"Polyvertex\" NumberOfElements=\"" + c + "\" />\n";
+            h += "\t\t<Geometry GeometryType=\"XYZ\">\n";
+            h += "\t\t\t<DataItem NumberType=\"Float\" Precision=\"8\" Format=\"Binary\" Dimensions=\"" + c +
+                 " 3\">" + names[d] + "</DataItem>\n\t\t</Geometry>\n";
+        }
+        h += "\t\t<Grid Name=\"TimeSeries\" GridType=\"Collection\" CollectionType=\"Temporal\" />\n";
+        h += "\t</Domain>\n</Xdmf>\n";
+        return h;
+    }
+
+    std::string grid(int step, real time, std::span<const std::string> var_names,
+                     std::span<const std::string> file_names, const cut_positions& t) const
+    {
+        std::string g = "\t\t\t<Grid Name=\"" + std::to_string(step) +
+                        "\" GridType=\"Collection\" CollectionType=\"Spatial\">\n";
+        g += "\t\t\t\t<Time Value=\"" + detail::num17(time) + "\" />\n";
+        unsigned long offset = 0;
+        auto sub = [&](unsigned long sz, const char* name, int topo, const std::string& dims) {
+            if (sz == 0) return;
+            g += std::string("\t\t\t\t<Grid Name=\"") + name + "\" GridType=\"Uniform\">\n";
+            g += "\t\t\t\t\t<Topology Reference=\"/Xdmf/Domain/Topology[" + std::to_string(topo) + "]\" />\n";
+            g += "\t\t\t\t\t<Geometry Reference=\"/Xdmf/Domain/Geometry[" + std::to_string(topo) + "]\" />\n";
+            for (std::size_t i = 0; i < var_names.size(); ++i) {
+                g += "\t\t\t\t\t<Attribute Name=\"" + detail::xml_escape(var_names[i]) + "\">\n";
+                g += "\t\t\t\t\t\t<DataItem Dimensions=\"" + dims +
+                     "\" NumberType=\"Float\" Precision=\"8\" Format=\"Binary\"";
+                if (offset > 0) g += " Seek=\"" + std::to_string(offset) + "\"";
+                g += ">" + detail::xml_escape(file_names[i]) + "</DataItem>\n\t\t\t\t\t</Attribute>\n";
+            }
+            g += "\t\t\t\t</Grid>\n";
+            offset += sz * sizeof(real);
+        };
+        const auto& n = ix_.extents;
+        sub((unsigned long)n[0] * n[1] * n[2], "F", 1, detail::join(n));
+        const char* names[3] = {"RX", "RY", "RZ"};
+        for (int d = 0; d < 3; d++)
+            sub(t[d].size(), names[d], 2 + d, std::to_string(t[d].size()) + " 1");
+        g += "\t\t\t</Grid>\n";
+        return g;
+    }
+
+public:
+    xdmf() = default;
+    xdmf(std::string xmf_filename, index_extents ix, domain_extents bounds)
+        : xmf_filename_{std::move(xmf_filename)}, ix_{ix}, bounds_{bounds}
+    {
+    }
+    const std::string& filename() const { return xmf_filename_; }
+
+    void write(int grid_number, real time, std::span<const std::string> var_names,
+               std::span<const std::string> file_names, const cut_positions& t) const
+    {
+        if (grid_number == 0) {
+            std::ofstream o(xmf_filename_, std::ios::binary | std::ios::trunc);
+            o << header(t);
+            if (!o) throw std::runtime_error("xdmf: cannot write " + xmf_filename_);
+        }
+        std::string doc;
+        {
+            std::ifstream i(xmf_filename_, std::ios::binary);
+            if (!i) throw std::runtime_error("xdmf: cannot reload " + xmf_filename_);
+            doc.assign(std::istreambuf_iterator<char>(i), std::istreambuf_iterator<char>());
+        }
+        const std::string g = grid(grid_number, time, var_names, file_names, t);
+        const std::string empty =
+            "\t\t<Grid Name=\"TimeSeries\" GridType=\"Collection\" CollectionType=\"Temporal\" />\n";
+        const std::string close = "\t\t</Grid>\n\t</Domain>\n</Xdmf>\n";
+        if (const auto at = doc.rfind(empty); at != std::string::npos) {
+            doc.replace(at, empty.size(),
+                        "\t\t<Grid Name=\"TimeSeries\" GridType=\"Collection\" CollectionType=\"Temporal\">\n" +
+                            g + "\t\t</Grid>\n");
+        } else if (doc.size() >= close.size() && doc.compare(doc.size() - close.size(), close.size(), close) == 0) {
+            doc.insert(doc.size() - close.size(), g);
+        } else {
+            throw std::runtime_error("xdmf: " + xmf_filename_ + " has no temporal collection to append to");
+        }
+        std::ofstream o(xmf_filename_, std::ios::binary | std::ios::trunc);
+        o << doc;
+        if (!o) throw std::runtime_error("xdmf: cannot write " + xmf_filename_);
+    }
+};
+
+// field_data: one raw binary file per variable: D (nx*ny*nz doubles, z fastest), then Rx,
+// Ry, Rz where nonempty; and the cut-point positions (3 doubles per point, (z, y, x) on
+// grids with nz == 1) in one file per axis.  The views hold HOST memory.
+class field_data
+{
+    index_extents ix_;
+
+public:
+    field_data() = default;
+    explicit field_data(index_extents ix) : ix_{ix} {}
+
+    void write(std::span<const scalar_view> scalars, std::span<const std::string> filenames) const
+    {
+        const std::size_t sz = (std::size_t)ix_.extents[0] * ix_.extents[1] * ix_.extents[2];
+        for (std::size_t k = 0; k < filenames.size(); ++k) {
+            const auto& sc = scalars[k];
+            if (sc.D.size() < sz) throw std::invalid_argument("field_data: D holds fewer than nx*ny*nz values");
+            std::ofstream o(filenames[k], std::ios::binary | std::ios::trunc);
+            o.write(reinterpret_cast<const char*>(sc.D.data()), (std::streamsize)(sz * sizeof(real)));
+            for (auto r : {sc.Rx, sc.Ry, sc.Rz})
+                if (!r.empty())
+                    o.write(reinterpret_cast<const char*>(r.data()), (std::streamsize)(r.size() * sizeof(real)));
+            if (!o) throw std::runtime_error("field_data: cannot write " + filenames[k]);
+        }
+    }
+
+    void write_geom(std::span<const std::string> filenames, const cut_positions& t) const
+    {
+        for (int d = 0; d < 3; d++) {
+            std::ofstream o(filenames[d], std::ios::binary | std::ios::trunc);
+            for (const real3& p : t[d]) {
+                const real3 q = ix_.extents[2] == 1 ? real3{p[2], p[1], p[0]} : p;
+                o.write(reinterpret_cast<const char*>(q.data()), (std::streamsize)sizeof q);
+            }
+            if (!o) throw std::runtime_error("field_data: cannot write " + filenames[d]);
+        }
+    }
+};
+
+// the io table of a simulation (the keys of field_io::from_lua, src/io/field_io.cpp:71-103)
+struct io_config {
+    std::optional<int> write_every_step;
+    std::optional<real> write_every_time;
+    std::string dir = "io";
+    int suffix_length = 6;
+    std::string xdmf_filename = "view.xmf";
+};
+
+// field_io: on each dump (d_interval), the variables' binary files "<name>.<dump number>"
+// (zero-padded to suffix_length digits) under dir, the cut-point geometry files rx, ry, rz
+// with the first dump, and one grid appended to the xdmf index dir/xdmf_filename.  A
+// default field_io writes nothing.
+class field_io
+{
+    xdmf xdmf_w_;
+    field_data field_data_w_;
+    d_interval dump_interval_;
+    std::string io_dir_;
+    int suffix_length_ = 6;
+
+public:
+    field_io() = default;
+    field_io(xdmf&& xdmf_w, field_data&& field_data_w, d_interval&& dump_interval, std::string&& io_dir,
+             int suffix_length)
+        : xdmf_w_{std::move(xdmf_w)}, field_data_w_{std::move(field_data_w)},
+          dump_interval_{std::move(dump_interval)}, io_dir_{std::move(io_dir)}, suffix_length_{suffix_length}
+    {
+    }
+    // field_io::from_lua over a parsed io table (none: a writer that never fires)
+    static field_io from_config(const mesh& m, const std::optional<io_config>& cfg)
+    {
+        if (!cfg) return field_io{};
+        const std::filesystem::path d{cfg->dir};
+        const auto step = cfg->write_every_step ? interval<int>{*cfg->write_every_step} : interval<int>{};
+        const auto time = cfg->write_every_time ? interval<real>{*cfg->write_every_time} : interval<real>{};
+        return field_io{xdmf{(d / cfg->xdmf_filename).string(), m.extents(), m.bounds()},
+                        field_data{m.extents()}, d_interval{step, time}, std::string{cfg->dir},
+                        cfg->suffix_length};
+    }
+    // whether write() would fire at this step (the schedule is left unchanged)
+    bool due(const step_controller& step, real dt) const
+    {
+        d_interval probe = dump_interval_;
+        return probe(step, dt);
+    }
+    int current_dump() const { return dump_interval_.current_dump(); }
+    const std::string& xdmf_filename() const { return xdmf_w_.filename(); }
+
+    bool write(std::span<const std::string> names, std::span<const scalar_view> scalars,
+               const step_controller& step, real dt, const cut_positions& r);
+};
+
+inline bool d_interval::operator()(const step_controller& step, real dt)
+{
+    if (!(step_interval_ || time_interval_)) return false;
+    step_ready_ = step_interval_(step.simulation_step());
+    time_ready_ = time_interval_(step.simulation_time(), dt);
+    return step_ready_ || time_ready_ || step.simulation_step() == 0;
+}
+
+inline bool field_io::write(std::span<const std::string> names, std::span<const scalar_view> scalars,
+                            const step_controller& step, real dt, const cut_positions& r)
+{
+    if (!dump_interval_(step, dt)) return false;
+    const std::filesystem::path io{io_dir_};
+    if (step.simulation_step() == 0) std::filesystem::create_directories(io);
+    const int n = dump_interval_.current_dump();
+    std::vector<std::string> xmf_names, data_names;
+    for (const auto& name : names) {
+        char suffix[48];
+        std::snprintf(suffix, sizeof suffix, "%0*d", suffix_length_, n);
+        xmf_names.push_back(name + "." + suffix);
+        data_names.push_back((io / xmf_names.back()).string());
+    }
+    xdmf_w_.write(n, step.simulation_time(), names, xmf_names, r);
+    if (n == 0) {
+        const std::vector<std::string> geom{(io / "rx").string(), (io / "ry").string(), (io / "rz").string()};
+        field_data_w_.write_geom(geom, r);
+    }
+    field_data_w_.write(scalars, data_names);
+    ++dump_interval_;
+    return true;
+}
+
+inline bool systems::scalar_system::write(field_io& io, const step_controller& c, real dt) const
+{
+    if (!io.due(c, dt)) return false;
+    const integer N = p_.size();
+    std::vector<real> u(N), err(N);
+    std::array<std::vector<real>, 3> uR, eR;
+    std::array<std::vector<real3>, 3> pos;
+    for (int d = 0; d < 3; d++) {
+        const integer n = p_.R(d);
+        uR[d].resize(n);
+        eR[d].resize(n);
+        pos[d].resize(n);
+        if (n)
+            detail::check(shoccs_problem_cut_points(p_.get(), d, nullptr, pos[d].data()->data(), nullptr,
+                                                    nullptr, nullptr, nullptr),
+                          "shoccs_problem_cut_points");
+    }
+    get_state(scalar_span{u, uR[0], uR[1], uR[2]}, false);
+    error_field(c.simulation_time(), scalar_span{err, eR[0], eR[1], eR[2]}, false);
+    const std::array<std::string, 2> names{"U", "Error"};
+    const std::array<scalar_view, 2> fields{scalar_view{u, uR[0], uR[1], uR[2]},
+                                            scalar_view{err, eR[0], eR[1], eR[2]}};
+    return io.write(names, fields, c, dt, cut_positions{pos[0], pos[1], pos[2]});
+}
+
 // simulation_cycle::run: initialize, then step while the controller is in bounds and the
-// system's statistics are valid, logging the statistics of every step.  Returns {time,
+// system's statistics are valid, logging the statistics of every step and handing the
+// state to the field writer (which dumps on its own schedule).  Returns {time,
 // error, error} when the run reached its bound in a valid state, {time, max, max} when it
 // ended early in an invalid state, and {max, 0, 0} when the step size fell below the
 // controller's minimum, as the reference does with null_v.
@@ -690,14 +1070,17 @@ class simulation_cycle
 {
     step_controller ctrl_;
     std::ostream* log_ = nullptr;
+    field_io io_;
 
 public:
     simulation_cycle() = default;
-    explicit simulation_cycle(const step_controller& c, std::ostream* system_log = nullptr)
-        : ctrl_{c}, log_{system_log}
+    explicit simulation_cycle(const step_controller& c, std::ostream* system_log = nullptr,
+                              field_io io = {})
+        : ctrl_{c}, log_{system_log}, io_{std::move(io)}
     {
     }
     const step_controller& controller() const { return ctrl_; }
+    const field_io& io() const { return io_; }
 
     template <typename System>
     real3 run(System& sys)
@@ -706,6 +1089,7 @@ public:
         sys.initialize(ctrl_.simulation_time());
         system_stats stats = sys.stats(ctrl_.simulation_time());
         if (log_) detail::log_line(*log_, ctrl_, stats);
+        sys.write(io_, ctrl_, 0.0); // the initial dump
         const integrators::rk4 rk;
         while (ctrl_ && sys.valid(stats)) {
             const real dt = sys.timestep_size(detail::cfl_of(sys, ctrl_));
@@ -714,6 +1098,7 @@ public:
             rk(sys, ctrl_.simulation_time(), dt);
             ctrl_.advance(dt);
             stats = sys.stats(ctrl_.simulation_time());
+            sys.write(io_, ctrl_, dt);
             stats.wall_time_s =
                 std::chrono::duration<real>(std::chrono::steady_clock::now() - t0).count();
             if (log_) detail::log_line(*log_, ctrl_, stats);

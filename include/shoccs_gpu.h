@@ -28,6 +28,8 @@
  *   shoccs_system_rhs       system::rhs             src/systems/heat.cpp:119-162,
  *                                                   src/systems/scalar_wave.cpp:195-239
  *   shoccs_system_stats     system::stats           src/systems/detail/scalar_system_utils.hpp:77-181
+ *   shoccs_system_error_field  the Error field of system::write
+ *                                                   src/systems/detail/scalar_system_utils.hpp:224-296
  *   shoccs_system_timestep  system::timestep_size   src/systems/heat.cpp:356-361,
  *                                                   src/systems/scalar_wave.cpp:357-362
  *
@@ -185,6 +187,13 @@ shoccs_status shoccs_system_rhs(shoccs_system* s, double t, shoccs_field* rhs, v
 /* out[11] = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry,
  *            Linf_Rz, argmax_Rz} of the current state against the exact solution at t */
 shoccs_status shoccs_system_stats(shoccs_system* s, double t, double out[11], void* stream);
+/* err <- |u - exact(t)| (FP64) at the fluid D points and at the non-Dirichlet cut points, 0
+ * on the Dirichlet faces, the solid points and the Dirichlet cut points: the "Error" field
+ * system::write hands to the field writer (write_scalar_error,
+ * src/systems/detail/scalar_system_utils.hpp:224-296).  where = 0 host pointers, 1 device
+ * pointers; every cut-point buffer of a nonempty R(dir) must be given. */
+shoccs_status shoccs_system_error_field(shoccs_system* s, double t, shoccs_field* err, int where,
+                                        void* stream);
 /* Allocation-free variant of shoccs_system_stats; it has no counterpart in the reference.
  * Some callers cannot allocate device memory while they call in: an application that has
  * handed the whole device memory to its own pool allocator, or a time loop that must never

@@ -49,7 +49,7 @@ def lib():
         for n in ["orc_destroy", "orc_size", "orc_cut_points", "orc_lines", "orc_fluid",
                   "orc_block", "orc_csr", "orc_derivative", "orc_laplacian", "orc_gradient",
                   "orc_initialize", "orc_exact", "orc_heat_rhs", "orc_heat_rk4",
-                  "orc_wave_rhs", "orc_wave_rk4", "orc_stats"]:
+                  "orc_wave_rhs", "orc_wave_rk4", "orc_stats", "orc_error_field"]:
             getattr(_lib, n).argtypes = None
     return _lib
 
@@ -207,3 +207,11 @@ class OracleProblem:
         lib().orc_stats(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u],
                         _p(out))
         return out
+
+    def error_field(self, sol_kind, params, t, u):
+        """the Error field of write_scalar_error (scalar_system_utils.hpp:224-296)"""
+        e = self.zeros()
+        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        lib().orc_error_field(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u],
+                              *[_p(a) for a in e])
+        return e

@@ -2206,6 +2206,27 @@ void orc_stats(orc_problem* o, int sol_kind, const double* params, double t,
     out[10] = ci[2];
 }
 
+// write_scalar_error: src/systems/detail/scalar_system_utils.hpp:224-296 -- zero the error
+// field, |u - sol| at the fluid D points and at the non-Dirichlet cut points, then zero the
+// Dirichlet grid faces and the Dirichlet cut points
+void orc_error_field(orc_problem* o, int sol_kind, const double* params, double t,
+                     const double* uD, const double* uRx, const double* uRy, const double* uRz,
+                     double* eD, double* eRx, double* eRy, double* eRz)
+{
+    const auto& m = o->P.m;
+    solution s = make_solution(o, sol_kind, params);
+    std::fill(eD, eD + m.size(), 0.0);
+    for (integer i : m.fluid) eD[i] = std::abs(uD[i] - s(t, m.loc(i)));
+    const double* uR[3] = {uRx, uRy, uRz};
+    double* eR[3] = {eRx, eRy, eRz};
+    for (int d = 0; d < 3; d++)
+        for (size_t i = 0; i < m.R[d].size(); i++)
+            eR[d][i] = o->P.obc[m.R[d][i].shape_id] == Dirichlet
+                           ? 0.0
+                           : std::abs(uR[d][i] - s(t, m.R[d][i].position));
+    for_each_dirichlet_face(o->P, [&](integer i) { eD[i] = 0.0; });
+}
+
 } // extern "C"
 
 extern "C" int orc_sphere_hit(const double* center, double radius, const double* origin,

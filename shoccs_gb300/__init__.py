@@ -247,6 +247,16 @@ class System:
         _capi.check(_capi.lib().shoccs_system_get_state(self._h, f, where, _stream(stream)))
         return u
 
+    def error_field(self, t, err, stream=None):
+        """err <- |u - exact(t)| at the fluid D points and the non-Dirichlet cut points, 0
+        elsewhere (the Error field of the reference's system::write); FP64 host arrays or
+        CUDA tensors"""
+        where = 1 if getattr(err.D, "is_cuda", False) else 0
+        f = _field(err) if where == 1 else ctypes.byref(_capi.Field(*[_np_ptr(a) for a in err]))
+        _capi.check(_capi.lib().shoccs_system_error_field(self._h, float(t), f, where,
+                                                          _stream(stream)))
+        return err
+
     def rk4(self, t0, dt, nsteps, stream=None):
         _capi.check(_capi.lib().shoccs_system_rk4(self._h, float(t0), float(dt), int(nsteps),
                                                   _stream(stream)))

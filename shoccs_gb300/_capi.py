@@ -94,6 +94,8 @@ SIGNATURES = {
     "shoccs_system_rhs": [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(Field),
                           ctypes.c_void_p],
     "shoccs_system_stats": [ctypes.c_void_p, ctypes.c_double, c_double_p, ctypes.c_void_p],
+    "shoccs_system_error_field": [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(Field),
+                                  ctypes.c_int, ctypes.c_void_p],
     "shoccs_system_stats_noalloc": [ctypes.c_void_p, ctypes.c_double, c_double_p,
                                     ctypes.c_void_p],
     "shoccs_system_timestep": [ctypes.c_void_p, ctypes.c_double, c_double_p],

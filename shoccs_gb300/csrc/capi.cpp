@@ -863,6 +863,47 @@ shoccs_status shoccs_system_get_state(shoccs_system* S, shoccs_field* u, int whe
     return SHOCCS_OK;
 }
 
+shoccs_status shoccs_system_error_field(shoccs_system* S, double t, shoccs_field* err, int where,
+                                        void* stream)
+{
+    if (!S || !err || !err->D) return fail(SHOCCS_EINVAL, "null argument");
+    if (where != 0 && where != 1) return fail(SHOCCS_EINVAL, "where must be 0 (host) or 1 (device)");
+    const cudaStream_t s = (cudaStream_t)stream;
+    const long long N = S->P->mesh.size();
+    long long nR[3], total = N;
+    void* out[4] = {err->D, err->Rx, err->Ry, err->Rz};
+    for (int r = 0; r < 3; r++) {
+        nR[r] = (long long)S->P->mesh.R[r].size();
+        if (nR[r] && !out[1 + r]) return fail(SHOCCS_EINVAL, "null cut-point buffer");
+        total += nR[r];
+    }
+    double* tmp = nullptr;
+    FieldF64 f{};
+    if (where == 1) {
+        f = FieldF64{(double*)err->D, {(double*)err->Rx, (double*)err->Ry, (double*)err->Rz}};
+    } else {
+        SH_CUDA(cudaMallocAsync((void**)&tmp, total * sizeof(double), s));
+        f.D = tmp;
+        long long off = N;
+        for (int r = 0; r < 3; r++) {
+            f.R[r] = tmp + off;
+            off += nR[r];
+        }
+    }
+    cudaError_t e = launch_error_field(S->P->op, S->P->dr, S->sp.sol, S->desc.prec, S->b.u0, S->b.R,
+                                       t, f, s);
+    if (where == 0) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out[0], f.D, N * 8, cudaMemcpyDeviceToHost, s);
+        for (int r = 0; r < 3; r++)
+            if (e == cudaSuccess && nR[r])
+                e = cudaMemcpyAsync(out[1 + r], f.R[r], nR[r] * 8, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(tmp, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(SHOCCS_ECUDA, std::string("error field: ") + cudaGetErrorString(e));
+    return SHOCCS_OK;
+}
+
 static shoccs_status check_wait_flag(shoccs_system* S, cudaStream_t s)
 {
     if (!S->b.tma) return SHOCCS_OK;

@@ -258,6 +258,10 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
 // min, max} per axis
 cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, double* const R[3],
                            double t, double* out12, cudaStream_t s);
+// err <- |u - exact(t)| at the fluid D points and the non-Dirichlet cut points, 0 elsewhere
+cudaError_t launch_error_field(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
+                               const void* u0, double* const R[3], double t, FieldF64 err,
+                               cudaStream_t s);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s);
 cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,

@@ -2889,6 +2889,51 @@ cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, d
     return cudaGetLastError();
 }
 
+// err <- |u - exact(t)| at the fluid D points and at the non-Dirichlet cut points, 0 on the
+// Dirichlet faces, the solid points and the Dirichlet cut points: the "Error" field that
+// write_scalar_error (src/systems/detail/scalar_system_utils.hpp:224-296) hands to the field
+// writer.  u0 is the D state (FP64, or the FP32 hi/lo pair of a mixed system); R is the
+// FP64 cut-point state (read only at non-Dirichlet cut points).
+__global__ void __launch_bounds__(256) k_error_field(DevOp op, DevR dr, DevSol sol, double t, double et,
+                                                     int mixed, const void* u0, const double* R0,
+                                                     const double* R1, const double* R2, FieldF64 err)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    if (part == 0) {
+        const unsigned c = op.cls[i];
+        double e = 0.0;
+        if ((c & CLS_FLUID) && !(c & CLS_DIRFACE)) {
+            const double u = mixed ? ldd(PairU{(const float*)u0, op.N}, i) : ((const double*)u0)[i];
+            int ijk[3];
+            phys_of_point(op, i, ijk);
+            e = fabs(u - sol_at_point(op, sol, t, et, ijk));
+        }
+        err.D[i] = e;
+    } else {
+        const int d = part - 1;
+        const double* R = d == 0 ? R0 : (d == 1 ? R1 : R2);
+        err.R[d][i] = dr.dirichlet[d][i]
+                          ? 0.0
+                          : fabs(R[i] - sol_at(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i));
+    }
+}
+
+cudaError_t launch_error_field(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
+                               const void* u0, double* const R[3], double t, FieldF64 err,
+                               cudaStream_t s)
+{
+    const long long n = op.N + op.nR[0] + op.nR[1] + op.nR[2];
+    if (n == 0) return cudaSuccess;
+    const double et = sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    k_error_field<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sol, t, et, prec == PREC_MIXED,
+                                                             u0, R[0], R[1], R[2], err);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stats(const DevOp& op, const DevR&, const DevSol& sol, int prec,
                          const void* u0, double* const*, double t, double* dev_out,
                          cudaStream_t s)

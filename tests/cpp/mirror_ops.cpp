@@ -6,7 +6,8 @@
 // compares the bits):
 //   in:  u.f64 (D then Rx, Ry, Rz of the problem; FP64)
 //   out: dx.f64, dx_plus.f64, lap.f64, gx.f64, gy.f64, lap_mixed.f32, heat_fp64.f64,
-//        heat_mixed.f64 (the state after 100 steps), stats.txt
+//        heat_mixed.f64 (the state after 100 steps), stats.txt, system.csv, and the field
+//        writer's output of two simulation cycles under io2d/ and io3d/
 #include "shoccs_gb300.hpp"
 
 #include <cuda_runtime.h>
@@ -162,9 +163,32 @@ int main(int argc, char** argv)
         {
             systems::heat h(mesh{m}, bcs::Grid{g}, bcs::Object{o}, mms::sinsin(1.0), st, 1.0);
             std::ofstream log(dir + "/system.csv");
-            simulation_cycle cycle(step_controller(100, 1e9, 0.5, 0.4), &log);
+            io_config cfg;
+            cfg.write_every_step = 40;
+            cfg.dir = dir + "/io2d";
+            simulation_cycle cycle(step_controller(100, 1e9, 0.5, 0.4), &log, field_io::from_config(m, cfg));
             const real3 r = cycle.run(h);
             std::fprintf(out, "cycle %.17g %.17g %d\n", r[0], r[1], cycle.controller().simulation_step());
+            std::fprintf(out, "io2d_dumps %d\n", cycle.io().current_dump());
+        }
+        // field output on a time schedule: FP64 heat around a Floating sphere (cut-point values
+        // are state, so the Error field has nonzero cut-point parts), 10 steps, a dump every
+        // 3 dt of simulation time
+        {
+            const mesh m3{index_extents{{24, 24, 24}}, domain_extents{{0, 0, 0}, {1, 1, 1}},
+                          {make_sphere(0, {0.5, 0.5, 0.5}, 0.25)}};
+            systems::heat h(mesh{m3}, bcs::Grid{bcs::dd, bcs::dd, bcs::dd}, bcs::Object{bcs::Floating},
+                            mms::sinsin(1.0), stencils::make_E4_2(), 1.0);
+            const real dt = h.timestep_size(0.4);
+            io_config cfg;
+            cfg.write_every_time = 3 * dt;
+            cfg.dir = dir + "/io3d";
+            cfg.suffix_length = 4;
+            cfg.xdmf_filename = "floating.xmf";
+            simulation_cycle cycle(step_controller(10, 1e9, 0.5, 0.4), nullptr, field_io::from_config(m3, cfg));
+            const real3 r = cycle.run(h);
+            std::fprintf(out, "io3d %.17g %d %d %.17g\n", r[0], cycle.controller().simulation_step(),
+                         cycle.io().current_dump(), dt);
         }
         // error behaviour: E4_1's alpha bound, and a status the library refuses
         try {

@@ -6,7 +6,10 @@ alpha[1] < 197/288 with std::invalid_argument as src/stencils/E4_1.cpp:37-40 doe
 GPU: tests/cpp/mirror_ops.cpp runs the 2-D heat case (65^2, circle, E4_2) and the three
 operators through the classes; every array must equal, bit for bit, what the Python binding
 gets from the same library on the same inputs, and the FP64 Laplacian must agree with the
-oracle to 1e-12; simulation_cycle runs the case for 100 steps and writes the system log.
+oracle to 1e-12; simulation_cycle runs the case for 100 steps and writes the system log, and two cycles write
+their fields through ccs::field_io (every 40 steps; every 3 dt of simulation time around a
+Floating sphere): the U files must hold the Python binding's states at the dump steps, the
+Error files the oracle's write_scalar_error of them, rx/ry/rz the cut-point positions.
 """
 import os
 import subprocess
@@ -146,3 +149,69 @@ def test_cpp_classes_match_the_python_binding(tmp_path):
     assert abs(float(lines[-1].split(",")[3]) - e_cycle) <= 1e-15 * e_cycle
     assert stats["e4_1_bound"] == ["invalid_argument"]
     assert stats["floating_object"] == ["status", "6"]  # SHOCCS_EUNSUPPORTED
+
+    # the field writer of both simulation cycles (ccs::field_io through system::write)
+    _check_cycle_io(tmp_path, p, float(stats["fp64"][5]), stats)
+
+
+def _check_cycle_io(tmp_path, p, dt2, stats):
+    import xml.etree.ElementTree as ET
+    import shoccs_gb300 as S
+    from oracle.oracle import OracleProblem
+    from tests.test_field_io import _d_interval_dumps
+
+    def times(steps, dt):
+        t, out = 0.0, []
+        for s in range(max(steps) + 1):
+            if s in steps:
+                out.append(t)
+            t += dt
+        return out
+
+    def check_run(case, io, steps, dt, suffix, xmf, make, swap):
+        q = S.Problem(**case)
+        o = OracleProblem(**case)
+        sizes = [q.size] + list(q.nR)
+        root = ET.parse(str(io / xmf)).getroot()
+        dom = root.find("Domain")
+        grids = [g for g in dom.findall("Grid") if g.get("Name") == "TimeSeries"][0].findall("Grid")
+        assert [g.get("Name") for g in grids] == [str(k) for k in range(len(steps))]
+        assert [float(g.find("Time").get("Value")) for g in grids] == times(steps, dt)
+        assert [t.get("NumberOfElements") for t in dom.findall("Topology")[1:]] == [str(k) for k in q.nR]
+        for d, name in enumerate(("rx", "ry", "rz")):
+            pos = np.fromfile(str(io / name)).reshape(-1, 3)
+            want = q.cut_points(d)["position"]
+            assert np.array_equal(pos, want[:, ::-1] if swap else want)
+        for k, (s, t) in enumerate(zip(steps, times(steps, dt))):
+            u = np.split(np.fromfile(str(io / ("U.%0*d" % (suffix, k)))), np.cumsum(sizes)[:-1])
+            e = np.split(np.fromfile(str(io / ("Error.%0*d" % (suffix, k)))), np.cumsum(sizes)[:-1])
+            h = make(q)
+            h.initialize(0.0)
+            if s:
+                h.rk4(0.0, dt, s)
+            ref = [np.zeros(m) for m in sizes]
+            h.get_state(S.ScalarField(*ref))
+            scale = max(np.abs(a).max() for a in ref if a.size)
+            for a, b in zip(u, ref):
+                assert np.abs(a - b).max(initial=0.0) <= 1e-12 * scale, (k, s)
+            want = o.error_field(S.SOL_SINSIN, [1.0], t, u)
+            for a, b in zip(e, want):
+                assert np.array_equal(a == 0, b == 0)
+                assert np.abs(a - b).max(initial=0.0) <= 1e-14 * scale
+        return e
+
+    # 2-D heat cycle: a dump every 40 steps of 100
+    steps2 = [0, 40, 80]
+    assert stats["io2d_dumps"] == [str(len(steps2))]
+    check_run(CASE, tmp_path / "io2d", steps2, dt2, 6, "view.xmf",
+              lambda q: S.Heat(q, 1.0, S.PREC_FP64, S.SOL_SINSIN, [1.0]), True)
+    # 3-D Floating sphere: a dump every 3 dt of simulation time over 10 steps
+    err3, nstep3, ndump3, dt3 = stats["io3d"]
+    dt3 = float(dt3)
+    steps3 = _d_interval_dumps(3 * dt3, dt3, 10)
+    assert int(nstep3) == 10 and int(ndump3) == len(steps3)
+    case3 = dict(n=(24, 24, 24), lo=(0, 0, 0), hi=(1, 1, 1), spheres=[((0.5, 0.5, 0.5), 0.25, "floating")],
+                 grid_bc=("dirichlet",) * 6, scheme="E4_2")
+    e = check_run(case3, tmp_path / "io3d", steps3, dt3, 4, "floating.xmf",
+                  lambda q: S.Heat(q, 1.0, S.PREC_FP64, S.SOL_SINSIN, [1.0]), False)
+    assert all(np.abs(r).max() > 0 for r in e[1:])  # Floating cut points evolve
