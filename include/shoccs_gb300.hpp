@@ -1066,11 +1066,20 @@ inline bool systems::scalar_system::write(field_io& io, const step_controller& c
 // error, error} when the run reached its bound in a valid state, {time, max, max} when it
 // ended early in an invalid state, and {max, 0, 0} when the step size fell below the
 // controller's minimum, as the reference does with null_v.
+// the header line heat / scalar_wave write into system.csv before the first statistics line
+// (src/systems/heat.cpp:44-48)
+inline void write_system_log_header(std::ostream& os)
+{
+    os << "Timestamp,Time,Step,Linf,Min,Max,Domain_Linf,Domain_ic,Rx_Linf,Rx_ic,Ry_Linf,Ry_ic,Rz_Linf,"
+          "Rz_ic,Wall_ms\n";
+}
+
 class simulation_cycle
 {
     step_controller ctrl_;
     std::ostream* log_ = nullptr;
     field_io io_;
+    std::ostream* console_ = nullptr;
 
 public:
     simulation_cycle() = default;
@@ -1081,6 +1090,9 @@ public:
     }
     const step_controller& controller() const { return ctrl_; }
     const field_io& io() const { return io_; }
+    // the cycle's progress messages (one per step, the cumulative wall time, an early end),
+    // as the reference's simulation_cycle logger prints them (simulation_cycle.cpp:113-140)
+    void set_console(std::ostream* console) { console_ = console; }
 
     template <typename System>
     real3 run(System& sys)
@@ -1091,9 +1103,13 @@ public:
         if (log_) detail::log_line(*log_, ctrl_, stats);
         sys.write(io_, ctrl_, 0.0); // the initial dump
         const integrators::rk4 rk;
+        const auto start = std::chrono::steady_clock::now();
         while (ctrl_ && sys.valid(stats)) {
             const real dt = sys.timestep_size(detail::cfl_of(sys, ctrl_));
-            if (!ctrl_.check_timestep_size(dt)) return {null, 0.0, 0.0}; // "timestep too small"
+            if (!ctrl_.check_timestep_size(dt)) {
+                if (console_) *console_ << "required timestep too small\n";
+                return {null, 0.0, 0.0};
+            }
             const auto t0 = std::chrono::steady_clock::now();
             rk(sys, ctrl_.simulation_time(), dt);
             ctrl_.advance(dt);
@@ -1102,8 +1118,26 @@ public:
             stats.wall_time_s =
                 std::chrono::duration<real>(std::chrono::steady_clock::now() - t0).count();
             if (log_) detail::log_line(*log_, ctrl_, stats);
+            if (console_) {
+                char wall[32];
+                std::snprintf(wall, sizeof wall, "%.3f", stats.wall_time_s * 1000.0);
+                *console_ << "time= " << detail::num(ctrl_.simulation_time())
+                          << "  step=" << ctrl_.simulation_step() << ", dt=" << detail::num(dt)
+                          << ", s0=" << detail::num(stats.stats[0]) << ", wall=" << wall << "ms\n";
+            }
         }
-        if (ctrl_) return {ctrl_.simulation_time(), null, null};
+        if (console_) {
+            char total[32];
+            std::snprintf(total, sizeof total, "%.3f",
+                          std::chrono::duration<real>(std::chrono::steady_clock::now() - start).count());
+            *console_ << "cumulative wall time: " << total << "s\n";
+        }
+        if (ctrl_) {
+            if (console_)
+                *console_ << "simulation ended prematurely at time/step  "
+                          << detail::num(ctrl_.simulation_time()) << " / " << ctrl_.simulation_step() << "\n";
+            return {ctrl_.simulation_time(), null, null};
+        }
         return {ctrl_.simulation_time(), stats.stats[0], stats.stats[0]};
     }
 };

@@ -1,4 +1,5 @@
-"""Build the in-tree CUDA library libshoccs_gb300.so for sm_103a (and nothing else).
+"""Build the in-tree CUDA library libshoccs_gb300.so for sm_103a and the shoccs command line
+over it.
 
 Compiles the device kernels with nvcc and the host setup / C ABI with g++, in parallel,
 into shoccs_gb300/_build/.  Host code is built with -ffp-contract=off so the setup
@@ -11,8 +12,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+APP = os.path.join(HERE, "app")
+INCLUDE = os.path.join(HERE, "..", "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libshoccs_gb300.so")
+CLI = os.path.join(BUILD, "shoccs")  # the command line (app/shoccs.cpp) over the library
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -43,10 +47,22 @@ def _deps():
     return out
 
 
+def _build_cli(force):
+    deps = [os.path.join(APP, f) for f in os.listdir(APP) if f.endswith((".cpp", ".hpp"))]
+    deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)] + [LIB]
+    if not force and _newer(CLI, deps + [os.path.abspath(__file__)]):
+        return
+    _run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-I" + INCLUDE, "-I" + APP,
+          "-I" + os.path.join(CUDA_HOME, "include"), os.path.join(APP, "shoccs.cpp"), "-o", CLI,
+          "-L" + BUILD, "-lshoccs_gb300", "-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart",
+          "-Wl,-rpath,$ORIGIN"])
+
+
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
     if not force and _newer(LIB, deps + [os.path.abspath(__file__)]):
+        _build_cli(force)
         return LIB
     inc = ["-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
     jobs = []
@@ -67,6 +83,7 @@ def build(verbose=False, force=False):
         for l in logs:
             sys.stderr.write(l)
     _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    _build_cli(True)
     return LIB
 
 

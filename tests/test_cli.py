@@ -1,0 +1,218 @@
+"""The shoccs command line (shoccs_gb300/app/shoccs.cpp) and its Lua reader
+(shoccs_gb300/app/lua_subset.hpp), on the host.
+
+* The Lua subset gives the values Lua 5.4 gives for the constructs input files use
+  (arithmetic and its precedence, floor division and modulo signs, comparisons, and/or,
+  strings in every quote form, table constructors with all key forms, locals and scopes,
+  math.*), and rejects what it does not evaluate with the line of the error.
+* The command line behaves as src/app/shoccs.cpp does: usage with no arguments or --help,
+  --check stops after the Lua has run (exit 0, or non-zero on a Lua error), --script runs
+  after the file and takes precedence, and a section the readers reject is reported while
+  the program still exits 0.  None of these cases reaches the GPU.
+* A driver script's template (markers in Lua comments replaced by plain text substitution)
+  gives a runnable input once filled in.
+"""
+import os
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LUA = os.path.join(HERE, "lua")
+CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+@pytest.fixture(scope="module")
+def lua_eval(tmp_path_factory):
+    d = tmp_path_factory.mktemp("lua_eval")
+    exe = d / "lua_eval"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra",
+                        "-I" + os.path.join(ROOT, "shoccs_gb300", "app"),
+                        os.path.join(HERE, "cpp", "lua_eval.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+    def run(src, *scripts):
+        f = d / "chunk.lua"
+        f.write_text(src)
+        r = subprocess.run([str(exe), str(f), *scripts], capture_output=True, text=True, timeout=60)
+        out = {}
+        for line in r.stdout.splitlines():
+            k, *v = line.split("\t")
+            out[k] = v
+        return r.returncode, out
+    return run
+
+
+@pytest.fixture(scope="module")
+def cli():
+    exe = os.path.join(ROOT, "shoccs_gb300", "_build", "shoccs")
+    if not os.path.exists(exe):
+        pytest.fail("command line not built: " + exe)
+    return exe
+
+
+CHUNK = r'''
+local a, b = 3, 4
+local unused
+g = 10
+result = {
+  arith = {1 + 2 * 3, (1 + 2) * 3, 2 ^ 3 ^ 2, -2 ^ 2, 7 // 2, -7 // 2, 7 % 3, -7 % 3, 7 % -3,
+           5.5 % 2, 1 / 4, 10 - 2 - 3, 2 ^ -1, "3" + 1},
+  cmp = {1 < 2, 2 <= 1, "a" < "b", 1 == 1.0, "1" == 1, nil == false, 3 ~= 4},
+  logic = {nil or 5, false and 1, 1 and 2, not nil, not 0, false or nil},
+  str = {"a" .. "b" .. 1 .. 2.5, #"hello", 'single', "esc\t\"q\"\65", #[[long
+string]], [==[with ]] inside]==]},
+  len = #{1, 2, 3, nil},
+  keys = {[1] = "one", [2.5] = "real", ["k"] = "v", x = a * b, [g] = "ten"; "positional"},
+  math = {math.pi, math.sqrt(2), math.floor(-2.5), math.max(1, 7, 3), math.min(4, -1),
+          math.abs(-3), math.huge > 1e308, math.fmod(7, 3), math.log(8, 2), math.exp(0),
+          math.atan(1, 1), math.ceil(1.2), math.tointeger(3.0)},
+  fn = function(t, x) if t > 0 then return x end return 0 end,
+  nested = {{1, {2, {3}}}},
+  hex = 0x1F,
+  expo = 1.5e3,
+  unary = - -3,
+}
+result.assigned = g + 1
+result.nested[1][2][2][2] = "deep"
+do local g = 99; result.shadow = g end
+result.after = g
+local function helper(x) return x end
+result.has_helper = helper ~= nil
+'''
+
+
+def _num(out, key):
+    typ, v = out[key]
+    assert typ == "number", (key, typ)
+    return float(v)
+
+
+def test_lua_subset_values(lua_eval):
+    rc, out = lua_eval(CHUNK)
+    assert rc == 0, out
+    arith = [7, 9, 512, -4, 3, -4, 1, 2, -2, 1.5, 0.25, 5, 0.5, 4]
+    assert [_num(out, "result.arith[%d]" % (i + 1)) for i in range(len(arith))] == arith
+    cmp = ["true", "false", "true", "true", "false", "false", "true"]
+    assert [out["result.cmp[%d]" % (i + 1)][1] for i in range(len(cmp))] == cmp
+    assert _num(out, "result.logic[1]") == 5
+    assert out["result.logic[2]"] == ["boolean", "false"]
+    assert _num(out, "result.logic[3]") == 2
+    assert out["result.logic[4]"] == ["boolean", "true"] and out["result.logic[5]"] == ["boolean", "false"]
+    assert "result.logic[6]" not in out  # nil is not stored
+    assert out["result.str[1]"] == ["string", "ab12.5"]
+    assert _num(out, "result.str[2]") == 5
+    assert out["result.str[3]"] == ["string", "single"]
+    assert out["result.str[4]"] == ["string", 'esc', '"q"A']  # the tab splits the field
+    assert _num(out, "result.str[5]") == 11  # the newline after [[ is not skipped here: 4+1+6
+    assert out["result.str[6]"] == ["string", "with ]] inside"]
+    assert _num(out, "result.len") == 3
+    assert out["result.keys[1]"] == ["string", "positional"]  # positional fields win over [1]
+    assert out["result.keys[2.5]"] == ["string", "real"]
+    assert out["result.keys.k"] == ["string", "v"]
+    assert _num(out, "result.keys.x") == 12
+    assert out["result.keys[10]"] == ["string", "ten"]
+    import math
+    m = [math.pi, math.sqrt(2), -3, 7, -1, 3, None, 1, 3, 1, math.pi / 4, 2, 3]
+    for i, want in enumerate(m):
+        if want is None:
+            assert out["result.math[%d]" % (i + 1)] == ["boolean", "true"]
+        else:
+            assert _num(out, "result.math[%d]" % (i + 1)) == want, i
+    assert out["result.fn"] == ["function", "function"]
+    assert _num(out, "result.nested[1][1]") == 1
+    assert out["result.nested[1][2][2][2]"] == ["string", "deep"]
+    assert _num(out, "result.hex") == 31 and _num(out, "result.expo") == 1500
+    assert _num(out, "result.unary") == 3
+    assert _num(out, "result.assigned") == 11
+    assert _num(out, "result.shadow") == 99 and _num(out, "result.after") == 10
+    assert out["result.has_helper"] == ["boolean", "true"]
+
+
+def test_lua_subset_script_after_file(lua_eval):
+    rc, out = lua_eval("result = {a = 1, b = {c = 2}}", "result.b.c = 3; result.d = result.a + 1")
+    assert rc == 0
+    assert _num(out, "result.a") == 1 and _num(out, "result.b.c") == 3 and _num(out, "result.d") == 2
+
+
+@pytest.mark.parametrize("src,msg", [
+    ("x = = 1", ":1:"),
+    ("\n\nfor i = 1, 2 do end", ":3: unsupported statement"),
+    ("f = function() return 1 end\nx = f()", ":2: functions defined in the input"),
+    ("x = y.z", "attempt to index a nil value"),
+    ("x = {1, 2", "'}' expected"),
+    ("x = 'open", "unfinished string"),
+    ("x = 1 + {}", "attempt to perform arithmetic"),
+    ("x = math.sqrt('a')", "bad argument to 'math.sqrt'"),
+])
+def test_lua_subset_errors(lua_eval, src, msg):
+    rc, out = lua_eval(src)
+    assert rc == 1
+    assert msg in out["error"][0], out
+
+
+def _run(cli, args, cwd):
+    return subprocess.run([cli] + args, cwd=str(cwd), capture_output=True, text=True, timeout=60)
+
+
+def test_cli_usage_and_check(cli, tmp_path):
+    for args in ([], ["--help"]):
+        r = _run(cli, args, tmp_path)
+        assert r.returncode == 0 and "--check" in r.stdout and "--script" in r.stdout
+    for name in ("wave_radial_2d.lua", "heat_circle_2d.lua"):
+        r = _run(cli, ["--check", os.path.join(LUA, name)], tmp_path)
+        assert r.returncode == 0, r.stderr
+    # the template is not runnable until its markers are replaced
+    r = _run(cli, ["--check", os.path.join(LUA, "wave_template.lua")], tmp_path)
+    assert r.returncode != 0 and "wave_template.lua:" in r.stderr
+    # --script runs after the file; an error there is an error too
+    r = _run(cli, ["--check", os.path.join(LUA, "wave_radial_2d.lua"), "--script", "simulation.x = ="], tmp_path)
+    assert r.returncode != 0 and "script:1:" in r.stderr
+    r = _run(cli, ["--check", "--script=simulation = {}"], tmp_path)
+    assert r.returncode == 0
+    r = _run(cli, ["--bogus"], tmp_path)
+    assert r.returncode != 0
+    assert not os.listdir(str(tmp_path))  # --check writes nothing
+
+
+@pytest.mark.parametrize("script,msg", [
+    ('simulation.scheme.type = "E6u"', "scheme.order/type = 1 / E6u is not available"),
+    ('simulation.scheme = {order = 3, type = "E4"}', "scheme.order/type = 3 / E4 not recognized"),
+    ('simulation.scheme = nil', "simulation.scheme must be specified"),
+    ('simulation.system.type = "euler"', "unrecognized system.type"),
+    ('simulation.system = nil', "simulation.system must be specified"),
+    ('simulation.mesh.index_extents = nil', "simulation.mesh.index_extents is required"),
+    ('simulation.mesh.domain_bounds = {min = {0, 0}}', "domain_bounds.max"),
+    ('simulation.domain_boundaries.xmin = "periodic"', "incorrect boundary condition"),
+    ('simulation.shapes = {{type = "yz_rect"}}', "shape type 'yz_rect' is not supported"),
+    ('simulation.integrator.type = "euler"', "integrator.type euler is not available"),
+    ('simulation.system.precision = "fp16"', "system.precision must be fp64 or mixed"),
+    ('simulation = 3', "the global table `simulation` is required"),
+])
+def test_cli_rejected_sections_exit_zero(cli, tmp_path, script, msg):
+    r = _run(cli, [os.path.join(LUA, "wave_radial_2d.lua"), "--script", script], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert msg in r.stderr, r.stderr
+
+
+def test_cli_heat_rejects_host_manufactured_solutions(cli, tmp_path):
+    r = _run(cli, [os.path.join(LUA, "heat_circle_2d.lua"), "--script",
+                   'simulation.manufactured_solution = {type = "lua"}'], tmp_path)
+    assert r.returncode == 0 and "is evaluated by host code in the reference" in r.stderr
+
+
+def fill_template(n, t_final, scheme_type, alpha):
+    """The driver's substitution: three markers replaced by plain text"""
+    src = open(os.path.join(LUA, "wave_template.lua")).read()
+    scheme = '{ order = 1, type = "%s", alpha = {%s} }' % (scheme_type, ", ".join(repr(float(a)) for a in alpha))
+    return (src.replace("--{{N}}--", str(int(n))).replace("--{{T_FINAL}}--", repr(float(t_final)))
+            .replace("--{{SCHEME_TABLE}}--", scheme))
+
+
+def test_template_filled_in_is_valid(cli, tmp_path):
+    f = tmp_path / "filled.lua"
+    f.write_text(fill_template(31, 0.1, "E4", (0.1, 0.7)))
+    r = _run(cli, ["--check", str(f)], tmp_path)
+    assert r.returncode == 0, r.stderr
