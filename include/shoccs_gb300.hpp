@@ -446,21 +446,38 @@ struct system_stats {
 struct manufactured_solution {
     int kind = SHOCCS_SOL_ZERO;
     std::array<real, 8> params{};
+    std::vector<real> terms; // SHOCCS_SOL_GAUSSIAN: 8 values per term
 };
 namespace mms
 {
 inline manufactured_solution zero() { return {}; }
 // prod_d sin(2 pi k x_d) e^{-t}
-inline manufactured_solution sinsin(real k) { return {SHOCCS_SOL_SINSIN, {k}}; }
+inline manufactured_solution sinsin(real k) { return {SHOCCS_SOL_SINSIN, {k}, {}}; }
 // exp(-|x - x0 - a t|^2 / (2 sigma^2)), the translated pulse of a constant velocity a
 inline manufactured_solution gauss_pulse(const real3& x0, const real3& a, real sigma)
 {
-    return {SHOCCS_SOL_GAUSS_PULSE, {x0[0], x0[1], x0[2], a[0], a[1], a[2], sigma}};
+    return {SHOCCS_SOL_GAUSS_PULSE, {x0[0], x0[1], x0[2], a[0], a[1], a[2], sigma}, {}};
 }
 // sin(2 pi (|x - c| - r - t)), the reference's circular wave (src/systems/scalar_wave.cpp:28-40)
 inline manufactured_solution radial_sin(const real3& c, real r)
 {
-    return {SHOCCS_SOL_RADIAL_SIN, {c[0], c[1], c[2], r}};
+    return {SHOCCS_SOL_RADIAL_SIN, {c[0], c[1], c[2], r}, {}};
+}
+// the reference's "gaussian" solution (build_ms_gauss, src/mms/mms.cpp:16-31): the sum over
+// terms of amplitude cos(frequency t) exp(-1/2 sum_d (x_d - center_d)^2 / variance_d^2) over
+// the mesh's dimensions; FP64 heat systems only
+inline manufactured_solution gaussian(std::span<const real3> center, std::span<const real3> variance,
+                                      std::span<const real> amplitude, std::span<const real> frequency)
+{
+    manufactured_solution m{SHOCCS_SOL_GAUSSIAN, {}, {}};
+    for (std::size_t i = 0; i < center.size(); i++) {
+        m.terms.insert(m.terms.end(), center[i].begin(), center[i].end());
+        const real3 v = i < variance.size() ? variance[i] : real3{};
+        m.terms.insert(m.terms.end(), v.begin(), v.end());
+        m.terms.push_back(i < amplitude.size() ? amplitude[i] : 0.0);
+        m.terms.push_back(i < frequency.size() ? frequency[i] : 0.0);
+    }
+    return m;
 }
 } // namespace mms
 
@@ -561,6 +578,8 @@ class heat : public scalar_system
         d.diffusivity = k;
         d.sol_kind = ms.kind;
         for (int i = 0; i < 8; i++) d.sol[i] = ms.params[i];
+        d.sol_n_terms = (int)(ms.terms.size() / 8);
+        d.sol_terms = ms.terms.empty() ? nullptr : ms.terms.data(); // copied by shoccs_system_create
         d.max_error = 1e6; // src/systems/heat.cpp:54-58
         return d;
     }

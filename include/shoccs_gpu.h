@@ -140,7 +140,12 @@ enum {
     SHOCCS_SOL_ZERO = 0,        /* u = 0 */
     SHOCCS_SOL_SINSIN = 1,      /* prod_d sin(2 pi k x_d) exp(-t); sol[0] = k */
     SHOCCS_SOL_GAUSS_PULSE = 2, /* exp(-|x - x0 - a t|^2 / (2 s^2)); sol = x0[3], a[3], s */
-    SHOCCS_SOL_RADIAL_SIN = 3   /* sin(2 pi (|x - c| - r - t)); sol = c[3], r */
+    SHOCCS_SOL_RADIAL_SIN = 3,  /* sin(2 pi (|x - c| - r - t)); sol = c[3], r */
+    SHOCCS_SOL_GAUSSIAN = 4     /* the reference's "gaussian" manufactured solution
+                                 * (src/mms/gauss1d.cpp, gauss2d.cpp, gauss3d.cpp):
+                                 * sum_i A_i cos(f_i t) exp(-1/2 sum_{d<D} (x_d - c_id)^2 / s_id^2),
+                                 * D the mesh's dimension count; terms in sol_terms.  FP64 heat
+                                 * systems only (stepped on the unfused whole-field path) */
 };
 enum { SHOCCS_VEL_CONSTANT = 0, SHOCCS_VEL_RADIAL = 1 };
 
@@ -154,6 +159,9 @@ typedef struct {
     int sol_kind;      /* SHOCCS_SOL_*: Dirichlet data, heat source and error reference */
     double sol[8];
     double max_error;  /* validity bound on the max-norm error (heat uses 1e6) */
+    int sol_n_terms;   /* SHOCCS_SOL_GAUSSIAN: number of terms */
+    const double* sol_terms; /* SHOCCS_SOL_GAUSSIAN: 8 doubles per term: centre[3],
+                              * variance[3], amplitude, frequency (copied at create) */
 } shoccs_system_desc;
 
 shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* desc,

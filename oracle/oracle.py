@@ -49,9 +49,18 @@ def lib():
         for n in ["orc_destroy", "orc_size", "orc_cut_points", "orc_lines", "orc_fluid",
                   "orc_block", "orc_csr", "orc_derivative", "orc_laplacian", "orc_gradient",
                   "orc_initialize", "orc_exact", "orc_heat_rhs", "orc_heat_rk4",
-                  "orc_wave_rhs", "orc_wave_rk4", "orc_stats", "orc_error_field"]:
+                  "orc_wave_rhs", "orc_wave_rk4", "orc_stats", "orc_error_field",
+                  "orc_set_gaussian"]:
             getattr(_lib, n).argtypes = None
     return _lib
+
+
+def gaussian_terms(terms):
+    """flatten Gaussian terms (centre[3], variance[3], amplitude, frequency) to 8 doubles each"""
+    flat = []
+    for c, v, a, f in terms:
+        flat += [float(x) for x in c] + [float(x) for x in v] + [float(a), float(f)]
+    return flat
 
 
 def _p(a):
@@ -161,28 +170,38 @@ class OracleProblem:
         lib().orc_gradient(self._h, *[_p(a) for a in u], ptrs)
         return outs
 
+    def _params(self, sol_kind, params):
+        """the 8 closed-form parameters; for the Gaussian sum (kind 4) `params` is its list
+        of terms (centre[3], variance[3], amplitude, frequency), set on the problem"""
+        if sol_kind == 4:
+            flat = gaussian_terms(params)
+            arr = (D * max(len(flat), 1))(*flat)
+            lib().orc_set_gaussian(self._h, ctypes.c_int(len(flat) // 8), arr)
+            return (D * 8)()
+        return (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+
     def initialize(self, sol_kind, params, t=0.0):
         u = self.zeros()
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_initialize(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u])
         return u
 
     def exact(self, sol_kind, params, t):
         u = self.zeros()
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_exact(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u])
         return u
 
     def heat_rhs(self, kappa, sol_kind, params, t, u):
         du = self.zeros()
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_heat_rhs(self._h, D(kappa), ctypes.c_int(sol_kind), pr, D(t),
                            *[_p(a) for a in u], *[_p(a) for a in du])
         return du
 
     def heat_rk4(self, kappa, sol_kind, params, t0, dt, nsteps, u):
         u = [a.copy() for a in u]
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_heat_rk4(self._h, D(kappa), ctypes.c_int(sol_kind), pr, D(t0), D(dt),
                            ctypes.c_int(nsteps), *[_p(a) for a in u])
         return u
@@ -195,7 +214,7 @@ class OracleProblem:
 
     def wave_rk4(self, vel_kind, vel, center, sol_kind, params, t0, dt, nsteps, u):
         u = [a.copy() for a in u]
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_wave_rk4(self._h, ctypes.c_int(vel_kind), (D * 3)(*vel), (D * 3)(*center),
                            ctypes.c_int(sol_kind), pr, D(t0), D(dt), ctypes.c_int(nsteps),
                            *[_p(a) for a in u])
@@ -203,7 +222,7 @@ class OracleProblem:
 
     def stats(self, sol_kind, params, t, u):
         out = np.zeros(11)
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_stats(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u],
                         _p(out))
         return out
@@ -211,7 +230,7 @@ class OracleProblem:
     def error_field(self, sol_kind, params, t, u):
         """the Error field of write_scalar_error (scalar_system_utils.hpp:224-296)"""
         e = self.zeros()
-        pr = (D * 8)(*(list(params) + [0.0] * (8 - len(params))))
+        pr = self._params(sol_kind, params)
         lib().orc_error_field(self._h, ctypes.c_int(sol_kind), pr, D(t), *[_p(a) for a in u],
                               *[_p(a) for a in e])
         return e

@@ -1527,11 +1527,45 @@ enum sol_kind {
     SOL_SINSIN = 1,      // u = prod_d sin(2 pi k x_d) * exp(-t) over the active dims
     SOL_GAUSS_PULSE = 2, // u = exp(-|x - x0 - a t|^2 / (2 sigma^2))
     SOL_RADIAL_SIN = 3,  // u = sin(2 pi (|x - c| - r - t))   (scalar_wave.cpp:35-40)
+    SOL_GAUSSIAN = 4,    // u = sum_i A_i cos(f_i t) exp(-1/2 sum_{d<D} (x_d - c_id)^2 / s_id^2)
+                         //   (src/mms/gauss1d.cpp:10-68, gauss2d.cpp:10-87, gauss3d.cpp:10-122)
 };
+
+// the Gaussian sum of SOL_GAUSSIAN and its derivatives at (t, x): D = the mesh's dimension
+// count, term i = G[8i..8i+7] = centre[3], variance[3], amplitude A, frequency f.  The
+// reference's gauss{1,2,3}d spell the same functions out per dimension count.
+struct gauss_terms {
+    real u = 0, ddt = 0, lap = 0, grad[3] = {0, 0, 0};
+};
+static gauss_terms gauss_eval(const std::vector<real>& G, int D, real t, const real3& x)
+{
+    gauss_terms r;
+    for (size_t i = 0; i + 8 <= G.size(); i += 8) {
+        const real* g = G.data() + i;
+        real e = 0.0, lp = 0.0, dv[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < D; d++) {
+            const real dx = x[d] - g[d];
+            const real is2 = 1.0 / (g[3 + d] * g[3 + d]);
+            e = e - 0.5 * (dx * dx) * is2;
+            dv[d] = dx * is2;
+            lp = lp + (dv[d] * dv[d] - is2);
+        }
+        const real E = std::exp(e);
+        const real ac = g[6] * std::cos(g[7] * t) * E;
+        r.u = r.u + ac;
+        r.ddt = r.ddt - g[6] * g[7] * std::sin(g[7] * t) * E;
+        r.lap = r.lap + ac * lp;
+        for (int d = 0; d < 3; d++) r.grad[d] = r.grad[d] - ac * dv[d];
+    }
+    return r;
+}
+
 struct solution {
     int kind = SOL_ZERO;
     int dims = 3;
     real p[8] = {0};
+    std::vector<real> G; // SOL_GAUSSIAN terms
+    int gdims = 0;       // SOL_GAUSSIAN: the mesh's dimension count
     // SINSIN: p[0] = k ; GAUSS_PULSE: p[0..2] = x0, p[3..5] = a, p[6] = sigma;
     // RADIAL_SIN: p[0..2] = c, p[3] = r
 
@@ -1555,16 +1589,19 @@ struct solution {
             real3 d{x[0] - p[0], x[1] - p[1], x[2] - p[2]};
             return std::sin(twoPI * (length3(d) - p[3] - t));
         }
+        case SOL_GAUSSIAN: return gauss_eval(G, gdims, t, x).u;
         default: return 0.0;
         }
     }
     real ddt(real t, const real3& x) const
     {
         if (kind == SOL_SINSIN) return -(*this)(t, x);
+        if (kind == SOL_GAUSSIAN) return gauss_eval(G, gdims, t, x).ddt;
         return 0.0;
     }
     real laplacian(real t, const real3& x) const
     {
+        if (kind == SOL_GAUSSIAN) return gauss_eval(G, gdims, t, x).lap;
         if (kind == SOL_SINSIN) {
             constexpr real twoPI = 2 * 3.14159265358979323846;
             real kk = twoPI * p[0];
@@ -1577,6 +1614,7 @@ struct solution {
     // sin-sin solution or zero
     real gradient(real t, const real3& x, int dir) const
     {
+        if (kind == SOL_GAUSSIAN) return gauss_eval(G, gdims, t, x).grad[dir];
         if (kind != SOL_SINSIN) return 0.0;
         constexpr real twoPI = 2 * 3.14159265358979323846;
         const real kk = twoPI * p[0];
@@ -1830,6 +1868,7 @@ using namespace orc;
 
 struct orc_problem {
     problem P;
+    std::vector<real> gauss; // SOL_GAUSSIAN terms (orc_set_gaussian)
 };
 
 extern "C" {
@@ -2026,7 +2065,17 @@ static solution make_solution(const orc_problem* o, int kind, const double* para
     s.kind = kind;
     s.dims = o->P.m.n[2] > 1 ? 3 : 2;
     for (int i = 0; i < 8 && params; i++) s.p[i] = params[i];
+    if (kind == SOL_GAUSSIAN) {
+        // manufactured_solution::from_lua picks gauss1d/2d/3d by mesh::dims (mms.cpp:16-31)
+        s.G = o->gauss;
+        s.gdims = (o->P.m.n[0] > 1) + (o->P.m.n[1] > 1) + (o->P.m.n[2] > 1);
+    }
     return s;
+}
+
+extern "C" void orc_set_gaussian(orc_problem* o, int n_terms, const double* terms)
+{
+    o->gauss.assign(terms, terms + 8 * (size_t)n_terms);
 }
 
 static void load_field(field_buf& f, const orc_problem* o, const double* D, const double* Rx,

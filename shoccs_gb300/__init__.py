@@ -21,8 +21,8 @@ from collections import namedtuple
 
 from . import _capi
 from ._capi import (BC_DIRICHLET, BC_FLOATING, BC_NEUMANN, PREC_FP64, PREC_MIXED,
-                    SCHEME_E2_2, SCHEME_E4_1, SCHEME_E4_2, SOL_GAUSS_PULSE, SOL_RADIAL_SIN,
-                    SOL_SINSIN, SOL_ZERO, VEL_CONSTANT, VEL_RADIAL, ShoccsError)
+                    SCHEME_E2_2, SCHEME_E4_1, SCHEME_E4_2, SOL_GAUSS_PULSE, SOL_GAUSSIAN,
+                    SOL_RADIAL_SIN, SOL_SINSIN, SOL_ZERO, VEL_CONSTANT, VEL_RADIAL, ShoccsError)
 
 ScalarField = namedtuple("ScalarField", ["D", "Rx", "Ry", "Rz"])
 
@@ -214,10 +214,20 @@ class System:
         d.vel[:] = [float(v) for v in vel]
         d.center[:] = [float(v) for v in center]
         d.sol_kind = sol_kind
+        terms = None
+        if sol_kind == SOL_GAUSSIAN:
+            # sol: the Gaussian terms (centre[3], variance[3], amplitude, frequency)
+            flat = []
+            for c, v, a, f in sol:
+                flat += [float(x) for x in c] + [float(x) for x in v] + [float(a), float(f)]
+            terms = (ctypes.c_double * max(len(flat), 1))(*flat)
+            d.sol_n_terms, d.sol_terms = len(flat) // 8, terms
+            sol = ()
         sol = list(sol) + [0.0] * (8 - len(sol))
         d.sol[:] = [float(v) for v in sol]
         d.max_error = float(max_error)
         self.desc = d
+        self._terms = terms  # the desc points at them
         self.p = problem
         h = ctypes.c_void_p()
         _capi.check(_capi.lib().shoccs_system_create(problem.handle, ctypes.byref(d),

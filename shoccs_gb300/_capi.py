@@ -16,7 +16,7 @@ BC_DIRICHLET, BC_FLOATING, BC_NEUMANN = 0, 1, 2
 SCHEME_E2_2, SCHEME_E4_2, SCHEME_E4_1, SCHEME_E4U_1 = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 SYS_HEAT, SYS_WAVE = 0, 1
-SOL_ZERO, SOL_SINSIN, SOL_GAUSS_PULSE, SOL_RADIAL_SIN = 0, 1, 2, 3
+SOL_ZERO, SOL_SINSIN, SOL_GAUSS_PULSE, SOL_RADIAL_SIN, SOL_GAUSSIAN = 0, 1, 2, 3, 4
 VEL_CONSTANT, VEL_RADIAL = 0, 1
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -55,6 +55,8 @@ class SystemDesc(ctypes.Structure):
         ("sol_kind", ctypes.c_int),
         ("sol", ctypes.c_double * 8),
         ("max_error", ctypes.c_double),
+        ("sol_n_terms", ctypes.c_int),
+        ("sol_terms", ctypes.POINTER(ctypes.c_double)),
     ]
 
 

@@ -29,12 +29,15 @@
 //   simulation.logging, logging_dir
 //                              simulation_cycle::from_lua   src/simulation/simulation_cycle.cpp:145-162
 //
+// Manufactured solutions: the reference's "gaussian" (terms {center, variance, amplitude,
+// frequency} in the table's array part; FP64 heat systems) is evaluated on the device; its
+// "lua" kind (functions run by the Lua interpreter) is not available.  A heat system without
+// a manufactured solution uses the zero solution (homogeneous Dirichlet data, no source),
+// where the reference requires one.
+//
 // Extensions (keys the reference does not read): system.precision = "fp64" (default) or
 // "mixed" selects the arithmetic of the time stepping; manufactured_solution.type =
-// "sinsin" with frequency = k is the closed form prod_d sin(2 pi k x_d) e^-t.  The reference's
-// "gaussian" and "lua" manufactured solutions are evaluated by its host code and are not
-// available here; a heat system without a manufactured solution uses the zero solution
-// (homogeneous Dirichlet data, no source).
+// "sinsin" with frequency = k is the closed form prod_d sin(2 pi k x_d) e^-t.
 #include "lua_subset.hpp"
 #include "shoccs_gb300.hpp"
 
@@ -271,9 +274,25 @@ std::variant<std::monostate, manufactured_solution, std::string> read_mms(const 
     std::string t = str_or(at(ms, "type"), "");
     for (auto& ch : t) ch = (char)std::tolower((unsigned char)ch);
     if (t == "sinsin") return mms::sinsin(num_or(at(ms, "frequency"), 1.0));
-    if (t == "gaussian" || t == "lua")
-        return "manufactured_solution.type = `" + t +
-               "` is evaluated by host code in the reference and is not available here (use `sinsin`)";
+    if (t == "gaussian") {
+        log.info("building gaussian manufactured solution");
+        std::vector<real3> center, variance;
+        std::vector<real> amplitude, frequency;
+        for (long long i = 1; valid(at(ms, i)); ++i) {
+            const value g = at(ms, i);
+            const value c = at(g, "center"), v = at(g, "variance");
+            center.push_back({num_or(at(c, 1), 0.0), num_or(at(c, 2), 0.0), num_or(at(c, 3), 0.0)});
+            variance.push_back({num_or(at(v, 1), 0.0), num_or(at(v, 2), 0.0), num_or(at(v, 3), 0.0)});
+            amplitude.push_back(num_or(at(g, "amplitude"), 0.0));
+            frequency.push_back(num_or(at(g, "frequency"), 0.0));
+        }
+        // no terms: the reference builds no solution either
+        if (center.empty()) return std::monostate{};
+        return mms::gaussian(center, variance, amplitude, frequency);
+    }
+    if (t == "lua")
+        return "manufactured_solution.type = `lua` (functions evaluated by the reference's Lua "
+               "interpreter) is not available here (use `gaussian` or `sinsin`)";
     return "Got manufactured_solution.type = `" + t + "`.  Expected one of: `gaussian, lua, sinsin`";
 }
 

@@ -612,7 +612,18 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     if (d->kind != SHOCCS_SYS_HEAT && d->kind != SHOCCS_SYS_WAVE)
         return fail(SHOCCS_EINVAL, "unknown system kind");
     if (d->prec != 0 && d->prec != 1) return fail(SHOCCS_EINVAL, "unknown precision");
-    if (d->sol_kind < 0 || d->sol_kind > 3) return fail(SHOCCS_EINVAL, "unknown solution kind");
+    if (d->sol_kind < 0 || d->sol_kind > 4) return fail(SHOCCS_EINVAL, "unknown solution kind");
+    const bool gaussian = d->sol_kind == SHOCCS_SOL_GAUSSIAN;
+    if (gaussian) {
+        if (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64)
+            return fail(SHOCCS_EUNSUPPORTED, "the gaussian manufactured solution is time-stepped by the "
+                                             "FP64 heat system only");
+        if (d->sol_n_terms < 0 || (d->sol_n_terms > 0 && !d->sol_terms))
+            return fail(SHOCCS_EINVAL, "gaussian manufactured solution: bad term list");
+        for (int i = 0; i < 8 * d->sol_n_terms; i++)
+            if (!std::isfinite(d->sol_terms[i]))
+                return fail(SHOCCS_EINVAL, "gaussian manufactured solution: non-finite parameter");
+    }
     // Neumann objects step like Floating ones: heat::rhs adds the source at every
     // non-Dirichlet cut point (heat.cpp:143-149) and the object part of the Neumann data
     // (neumann_rx/ry/rz) is never assigned, so their closures carry no data term
@@ -677,6 +688,15 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         const double kk = twoPI * k;
         sol.lapfac = -(double)sol.dims * kk * kk;
     }
+    if (gaussian) {
+        // gauss1d / gauss2d / gauss3d by the mesh's dimension count (mms.cpp:16-31)
+        sol.gdims = (p->mesh.n[0] > 1) + (p->mesh.n[1] > 1) + (p->mesh.n[2] > 1);
+        sol.nG = d->sol_n_terms;
+        if (sol.nG > 0) {
+            std::vector<double> terms(d->sol_terms, d->sol_terms + 8 * sol.nG);
+            SH_CUDA(S->mem.put(terms, &sol.G, s));
+        }
+    }
     const long long N = p->mesh.size();
     const size_t es_u = 8; // double or float2
     const size_t es_s = d->prec == PREC_FP64 ? 8 : 4;
@@ -714,7 +734,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.Rfull[r] = (double*)f;
         if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
     }
-    if (non_dirichlet_objects || neumann_mask) {
+    if (non_dirichlet_objects || neumann_mask || gaussian) {
         S->unfused = true;
         if (neumann_mask) {
             void* nu = nullptr;

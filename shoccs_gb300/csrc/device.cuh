@@ -68,6 +68,9 @@ struct DevSol {
     const double* SR[3]; // SINSIN: product of sines at the cut points of R(d)
     const double* C[3];  // SINSIN: cos(2 pi k x) tables (the gradient, Neumann data)
     double lapfac;       // SINSIN: -(dims) (2 pi k)^2
+    const double* G;     // GAUSSIAN: nG terms of 8 doubles (centre[3], variance[3], A, f)
+    int nG;
+    int gdims;           // GAUSSIAN: the mesh's dimension count (axes with more than one point)
 };
 
 struct DevR {

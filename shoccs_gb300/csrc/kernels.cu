@@ -349,7 +349,7 @@ __device__ __forceinline__ float wall_neumann32(const DevAxis& A, long long p, i
 }
 
 // ---- closed-form solutions -------------------------------------------------------------
-enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3 };
+enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3, SOL_GAUSSIAN = 4 };
 
 __device__ __forceinline__ double sol_at(const DevSol& s, double t, double et, const double x[3],
                                          const int* ijk, int rdir, long long ridx)
@@ -386,6 +386,58 @@ __device__ __forceinline__ double sol_at_point(const DevOp& op, const DevSol& s,
 {
     const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
     return sol_at(s, t, et, x, ijk, 0, 0);
+}
+
+// A sum of separable Gaussians, the reference's "gaussian" manufactured solution
+// (src/mms/gauss1d.cpp, gauss2d.cpp, gauss3d.cpp): with D the mesh's dimension count and term
+// i = (centre c_i, variance s_i, amplitude A_i, frequency f_i),
+//   u = sum_i A_i cos(f_i t) E_i,  E_i = exp(-1/2 sum_{d<D} (x_d - c_id)^2 / s_id^2),
+// so du/dt = -sum_i A_i f_i sin(f_i t) E_i, du/dx_d = -sum_i A_i cos(f_i t) E_i (x_d - c_id) / s_id^2
+// and lap u = sum_i A_i cos(f_i t) E_i sum_{d<D} ((x_d - c_id)^2 / s_id^4 - 1 / s_id^2).
+// Only the generic kernels (unfused heat step, initialisation, statistics, boundary data)
+// evaluate it; the fused stage kernels never see this kind.
+struct GaussEval {
+    double u, ddt, lap, grad[3];
+};
+__device__ __forceinline__ GaussEval gauss_eval(const DevSol& s, double t, const double x[3])
+{
+    GaussEval r{0.0, 0.0, 0.0, {0.0, 0.0, 0.0}};
+    for (int i = 0; i < s.nG; i++) {
+        const double* g = s.G + 8 * i; // c[3], s[3], A, f
+        double e = 0.0, lp = 0.0, dv[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (d < s.gdims) {
+                const double dx = x[d] - g[d];
+                const double is2 = 1.0 / (g[3 + d] * g[3 + d]);
+                e = e - 0.5 * (dx * dx) * is2;
+                dv[d] = dx * is2;
+                lp = lp + (dv[d] * dv[d] - is2);
+            }
+        }
+        const double E = exp(e);
+        const double ac = g[6] * cos(g[7] * t) * E;
+        r.u = r.u + ac;
+        r.ddt = r.ddt - g[6] * g[7] * sin(g[7] * t) * E;
+        r.lap = r.lap + ac * lp;
+#pragma unroll
+        for (int d = 0; d < 3; d++) r.grad[d] = r.grad[d] - ac * dv[d];
+    }
+    return r;
+}
+
+// sol_at / sol_at_point for the generic kernels: every solution kind, the Gaussian sum too
+__device__ __forceinline__ double sol_any(const DevSol& s, double t, double et, const double x[3],
+                                          const int* ijk, int rdir, long long ridx)
+{
+    if (s.kind == SOL_GAUSSIAN) return gauss_eval(s, t, x).u;
+    return sol_at(s, t, et, x, ijk, rdir, ridx);
+}
+__device__ __forceinline__ double sol_point_any(const DevOp& op, const DevSol& s, double t,
+                                                double et, const int ijk[3])
+{
+    const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+    return sol_any(s, t, et, x, ijk, 0, 0);
 }
 
 // ---- compensated FP32 pairs ("float-float", ~2^-46 relative) ------------------------------
@@ -1877,7 +1929,7 @@ __global__ void __launch_bounds__(256) k_init(DevOp op, DevSol sol, double t, do
     if (c & CLS_FLUID) {
         int ijk[3];
         phys_ijk(op, q, ijk);
-        v = sol_at_point(op, sol, t, et, ijk);
+        v = sol_point_any(op, sol, t, et, ijk);
     }
     if (mixed)
         st_pair(u0, op.N, q.p, ff_from_double(v));
@@ -1889,7 +1941,7 @@ __global__ void k_init_r(DevR dr, DevSol sol, int n, int d, double t, double et,
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    out[i] = sol_at(sol, t, et, dr.pos[d] + 3 * (long long)i, nullptr, d, i);
+    out[i] = sol_any(sol, t, et, dr.pos[d] + 3 * (long long)i, nullptr, d, i);
 }
 
 __global__ void k_convert(long long n, int to_mixed, const double* in_d, float* out_m,
@@ -1931,7 +1983,7 @@ __global__ void __launch_bounds__(256) k_stats(DevOp op, DevSol sol, double t, d
         const double u = mixed ? ldd(PairU{(const float*)u0, op.N}, q.p) : ((const double*)u0)[q.p];
         int ijk[3];
         phys_ijk(op, q, ijk);
-        double e = fabs(u - sol_at_point(op, sol, t, et, ijk));
+        double e = fabs(u - sol_point_any(op, sol, t, et, ijk));
         // a non-finite value counts as an infinite error so that system validity trips
         if (!(e <= 1.7976931348623157e308)) e = __longlong_as_double(0x7ff0000000000000LL);
         s = StatPart{e, q.p, isnan(u) ? 0.0 : u, isnan(u) ? 0.0 : u};
@@ -2607,13 +2659,24 @@ __global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, dou
     const int part = field_part(op, g, i);
     if (part < 0) return;
     const bool sinsin = sp.sol.kind == SOL_SINSIN;
+    const bool gauss = sp.sol.kind == SOL_GAUSSIAN;
+    // the source ddt - k lap of the Gaussian sum at x
+    auto gauss_source = [&](const double x[3]) {
+        const GaussEval ge = gauss_eval(sp.sol, t, x);
+        return __dsub_rn(ge.ddt, __dmul_rn(sp.k, ge.lap));
+    };
     if (part == 0) {
         const unsigned c = op.cls[i];
         double v = __dmul_rn(K.D[i], sp.k);
-        if ((c & CLS_FLUID) && sinsin) {
+        if ((c & CLS_FLUID) && (sinsin || gauss)) {
             int ijk[3];
             phys_of_point(op, i, ijk);
-            v = __dadd_rn(v, heat_source(sp, sol_at_point(op, sp.sol, t, et, ijk)));
+            if (sinsin) {
+                v = __dadd_rn(v, heat_source(sp, sol_at_point(op, sp.sol, t, et, ijk)));
+            } else {
+                const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+                v = __dadd_rn(v, gauss_source(x));
+            }
         }
         if (c & CLS_DIRFACE) v = 0.0;
         K.D[i] = v;
@@ -2624,6 +2687,8 @@ __global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, dou
             v = 0.0;
         else if (sinsin)
             v = __dadd_rn(v, heat_source(sp, sol_at(sp.sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i)));
+        else if (gauss)
+            v = __dadd_rn(v, gauss_source(dr.pos[d] + 3 * i));
         K.R[d][i] = v;
     }
 }
@@ -2649,14 +2714,14 @@ __global__ void k_update_boundary(DevOp op, DevR dr, DevSol sol, double t, doubl
         const long long p = op.faces[g];
         int ijk[3];
         phys_of_point(op, p, ijk);
-        u.D[p] = sol_at_point(op, sol, t, et, ijk);
+        u.D[p] = sol_point_any(op, sol, t, et, ijk);
         return;
     }
     g -= op.n_faces;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         if (g < op.nR[d]) {
-            if (dr.dirichlet[d][g]) u.R[d][g] = sol_at(sol, t, et, dr.pos[d] + 3 * g, nullptr, d, (int)g);
+            if (dr.dirichlet[d][g]) u.R[d][g] = sol_any(sol, t, et, dr.pos[d] + 3 * g, nullptr, d, (int)g);
             return;
         }
         g -= op.nR[d];
@@ -2665,9 +2730,10 @@ __global__ void k_update_boundary(DevOp op, DevR dr, DevSol sol, double t, doubl
 
 // Neumann data of heat::update_boundary (heat.cpp:324-352) at time t: on each Neumann face
 // of axis a, the gradient component a of the solution (sin-sin: 2 pi k cos(2 pi k x_a) times
-// the other axes' sines, times e^-t; zero otherwise), axes in order, so at an edge shared
-// with a later axis' Neumann face the later axis' value is the one written.
-__global__ void k_neumann_faces(DevOp op, DevSol sol, int mask, double et, double* nu)
+// the other axes' sines, times e^-t; the Gaussian sum's gradient; zero otherwise), axes in
+// order, so at an edge shared with a later axis' Neumann face the later axis' value is the
+// one written.
+__global__ void k_neumann_faces(DevOp op, DevSol sol, int mask, double t, double et, double* nu)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     for (int f = 0; f < 6; f++) {
@@ -2692,6 +2758,9 @@ __global__ void k_neumann_faces(DevOp op, DevSol sol, int mask, double et, doubl
             for (int d = 0; d < sol.dims; d++)
                 v = __dmul_rn(v, d == a ? __dmul_rn(kk, sol.C[d][ijk[d]]) : sol.S[d][ijk[d]]);
             v = __dmul_rn(v, et);
+        } else if (sol.kind == SOL_GAUSSIAN) {
+            const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+            v = gauss_eval(sol, t, x).grad[a];
         }
         const long long nyz = (long long)op.n[1] * op.n[2];
         nu[ijk[0] * nyz + (long long)ijk[1] * op.n[2] + ijk[2]] = v;
@@ -2712,7 +2781,7 @@ cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& s
                 const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
                 nface += (long long)op.n[b] * op.n[c];
             }
-        k_neumann_faces<<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(op, sp.sol, nf.mask, et, nf.nu);
+        k_neumann_faces<<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(op, sp.sol, nf.mask, t, et, nf.nu);
         ++g_launches;
     }
     const void* uR[3] = {u.R[0], u.R[1], u.R[2]};
@@ -2843,7 +2912,7 @@ __global__ void __launch_bounds__(256) k_stats_r(DevOp op, DevR dr, DevSol sol, 
     for (long long i = threadIdx.x; i < n; i += blockDim.x) {
         if (dr.dirichlet[d][i]) continue;
         const double v = R[i];
-        double e = fabs(v - sol_at(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, i));
+        double e = fabs(v - sol_any(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, i));
         if (!(e <= 1.0e300)) e = 1.0 / 0.0;
         if (e > be) { // i grows along the loop, so the first index of a tie is kept
             be = e;
@@ -2909,7 +2978,7 @@ __global__ void __launch_bounds__(256) k_error_field(DevOp op, DevR dr, DevSol s
             const double u = mixed ? ldd(PairU{(const float*)u0, op.N}, i) : ((const double*)u0)[i];
             int ijk[3];
             phys_of_point(op, i, ijk);
-            e = fabs(u - sol_at_point(op, sol, t, et, ijk));
+            e = fabs(u - sol_point_any(op, sol, t, et, ijk));
         }
         err.D[i] = e;
     } else {
@@ -2917,7 +2986,7 @@ __global__ void __launch_bounds__(256) k_error_field(DevOp op, DevR dr, DevSol s
         const double* R = d == 0 ? R0 : (d == 1 ? R1 : R2);
         err.R[d][i] = dr.dirichlet[d][i]
                           ? 0.0
-                          : fabs(R[i] - sol_at(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i));
+                          : fabs(R[i] - sol_any(sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i));
     }
 }
 
