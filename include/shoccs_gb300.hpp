@@ -15,7 +15,8 @@
 //   ccs::gradient             src/operators/gradient.hpp:10-30
 //   ccs::systems::heat        src/systems/heat.hpp:16-70
 //   ccs::systems::scalar_wave src/systems/scalar_wave.hpp:16-80
-//   ccs::integrators::rk4     src/temporal/rk4.hpp:10-20
+//   ccs::integrators::rk4, euler, integrator
+//                             src/temporal/rk4.hpp:10-20, euler.cpp:11-27, integrator.hpp
 //   ccs::step_controller      src/temporal/step_controller.hpp:10-50
 //   ccs::simulation_cycle     src/simulation/simulation_cycle.cpp:31-143 (run)
 //   ccs::interval, d_interval src/io/interval.hpp:9-97
@@ -657,6 +658,39 @@ public:
         detail::check(shoccs_system_rk4(sys.get(), t0, dt, nsteps, stream), "shoccs_system_rk4");
     }
 };
+
+// forward Euler (src/temporal/euler.cpp:11-27): u <- u + dt rhs(u, t), then the boundary
+// data at t + dt; FP64 systems
+class euler
+{
+public:
+    euler() = default;
+    void operator()(systems::scalar_system& sys, real t, real dt, void* stream = nullptr) const
+    {
+        run(sys, t, dt, 1, stream);
+    }
+    void run(systems::scalar_system& sys, real t0, real dt, int nsteps, void* stream = nullptr) const
+    {
+        detail::check(shoccs_system_euler(sys.get(), t0, dt, nsteps, stream), "shoccs_system_euler");
+    }
+};
+
+// the integrator of a simulation (src/temporal/integrator.hpp: a variant over the
+// integrators), rk4 unless chosen otherwise
+class integrator
+{
+    bool euler_ = false;
+
+public:
+    integrator(rk4 = {}) {}
+    integrator(euler) : euler_{true} {}
+    bool is_euler() const { return euler_; }
+    void operator()(systems::scalar_system& sys, real t, real dt, void* stream = nullptr) const
+    {
+        if (euler_) euler{}(sys, t, dt, stream);
+        else rk4{}(sys, t, dt, stream);
+    }
+};
 } // namespace integrators
 
 // ---- step controller and simulation cycle (src/temporal/step_controller.hpp,
@@ -1099,12 +1133,13 @@ class simulation_cycle
     std::ostream* log_ = nullptr;
     field_io io_;
     std::ostream* console_ = nullptr;
+    integrators::integrator integ_;
 
 public:
     simulation_cycle() = default;
     explicit simulation_cycle(const step_controller& c, std::ostream* system_log = nullptr,
-                              field_io io = {})
-        : ctrl_{c}, log_{system_log}, io_{std::move(io)}
+                              field_io io = {}, integrators::integrator integ = integrators::rk4{})
+        : ctrl_{c}, log_{system_log}, io_{std::move(io)}, integ_{integ}
     {
     }
     const step_controller& controller() const { return ctrl_; }
@@ -1121,7 +1156,6 @@ public:
         system_stats stats = sys.stats(ctrl_.simulation_time());
         if (log_) detail::log_line(*log_, ctrl_, stats);
         sys.write(io_, ctrl_, 0.0); // the initial dump
-        const integrators::rk4 rk;
         const auto start = std::chrono::steady_clock::now();
         while (ctrl_ && sys.valid(stats)) {
             const real dt = sys.timestep_size(detail::cfl_of(sys, ctrl_));
@@ -1130,7 +1164,7 @@ public:
                 return {null, 0.0, 0.0};
             }
             const auto t0 = std::chrono::steady_clock::now();
-            rk(sys, ctrl_.simulation_time(), dt);
+            integ_(sys, ctrl_.simulation_time(), dt);
             ctrl_.advance(dt);
             stats = sys.stats(ctrl_.simulation_time());
             sys.write(io_, ctrl_, dt);

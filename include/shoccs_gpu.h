@@ -25,6 +25,8 @@
  *   shoccs_system_rk4       integrators::rk4::operator() applied nsteps times with the
  *                           simulation_cycle u0 <- u1 copy   src/temporal/rk4.cpp:16-47,
  *                                                   src/simulation/simulation_cycle.cpp:79-126
+ *   shoccs_system_euler     integrators::euler::operator() applied nsteps times
+ *                                                   src/temporal/euler.cpp:11-27
  *   shoccs_system_rhs       system::rhs             src/systems/heat.cpp:119-162,
  *                                                   src/systems/scalar_wave.cpp:195-239
  *   shoccs_system_stats     system::stats           src/systems/detail/scalar_system_utils.hpp:77-181
@@ -191,6 +193,10 @@ shoccs_status shoccs_system_rk4(shoccs_system* s, double t0, double dt, int nste
 shoccs_status shoccs_system_rk4_timed(shoccs_system* s, double t0, double dt, int nsteps,
                                       void* stream, double kernel_ms[6]);
 /* one right-hand-side evaluation of the current state at time t into rhs (FP64, device) */
+/* integrators::euler::operator() applied nsteps times (src/temporal/euler.cpp:11-27): the
+ * state u <- u + dt * rhs(u, t), then the boundary data at t + dt.  FP64 systems. */
+shoccs_status shoccs_system_euler(shoccs_system* s, double t0, double dt, int nsteps,
+                                  void* stream);
 shoccs_status shoccs_system_rhs(shoccs_system* s, double t, shoccs_field* rhs, void* stream);
 /* out[11] = {Linf, min, max, Linf_D, argmax_D, Linf_Rx, argmax_Rx, Linf_Ry, argmax_Ry,
  *            Linf_Rz, argmax_Rz} of the current state against the exact solution at t */

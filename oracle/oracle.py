@@ -50,7 +50,7 @@ def lib():
                   "orc_block", "orc_csr", "orc_derivative", "orc_laplacian", "orc_gradient",
                   "orc_initialize", "orc_exact", "orc_heat_rhs", "orc_heat_rk4",
                   "orc_wave_rhs", "orc_wave_rk4", "orc_stats", "orc_error_field",
-                  "orc_set_gaussian"]:
+                  "orc_set_gaussian", "orc_heat_euler", "orc_wave_euler"]:
             getattr(_lib, n).argtypes = None
     return _lib
 
@@ -204,6 +204,21 @@ class OracleProblem:
         pr = self._params(sol_kind, params)
         lib().orc_heat_rk4(self._h, D(kappa), ctypes.c_int(sol_kind), pr, D(t0), D(dt),
                            ctypes.c_int(nsteps), *[_p(a) for a in u])
+        return u
+
+    def heat_euler(self, kappa, sol_kind, params, t0, dt, nsteps, u):
+        u = [a.copy() for a in u]
+        pr = self._params(sol_kind, params)
+        lib().orc_heat_euler(self._h, D(kappa), ctypes.c_int(sol_kind), pr, D(t0), D(dt),
+                             ctypes.c_int(nsteps), *[_p(a) for a in u])
+        return u
+
+    def wave_euler(self, vel_kind, vel, center, sol_kind, params, t0, dt, nsteps, u):
+        u = [a.copy() for a in u]
+        pr = self._params(sol_kind, params)
+        lib().orc_wave_euler(self._h, ctypes.c_int(vel_kind), (D * 3)(*vel), (D * 3)(*center),
+                             ctypes.c_int(sol_kind), pr, D(t0), D(dt), ctypes.c_int(nsteps),
+                             *[_p(a) for a in u])
         return u
 
     def wave_rhs(self, vel_kind, vel, center, u):

@@ -1859,6 +1859,18 @@ static void rk4_step(Sys& sys, field_buf& u0, field_buf& u1, field_buf& rk, fiel
     sys.update_boundary(u1.span(), time + dt);
 }
 
+// integrators::euler::operator(): src/temporal/euler.cpp:11-27 -- output <- u0, the right-hand
+// side of output at `time`, output <- u0 + dt rhs, then the boundary data at time + dt
+template <typename Sys>
+static void euler_step(Sys& sys, field_buf& u0, field_buf& u1, field_buf& srhs, real time, real dt)
+{
+    u1 = u0;
+    srhs.zero();
+    sys.rhs(u1.view(), srhs.span(), time);
+    lc_assign(u1, u0, dt, srhs);
+    sys.update_boundary(u1.span(), time + dt);
+}
+
 } // namespace orc
 
 // =======================================================================================
@@ -2153,6 +2165,26 @@ void orc_heat_rk4(orc_problem* o, double kappa, int sol_kind, const double* para
     store_field(u0, D, Rx, Ry, Rz);
 }
 
+void orc_heat_euler(orc_problem* o, double kappa, int sol_kind, const double* params,
+                    double t0, double dt, int nsteps, double* D, double* Rx, double* Ry,
+                    double* Rz)
+{
+    heat_sys H{&o->P, kappa, make_solution(o, sol_kind, params), {}, {}};
+    H.neu.resize(o->P.m);
+    H.src.resize(o->P.m);
+    field_buf u0, u1, srhs;
+    load_field(u0, o, D, Rx, Ry, Rz);
+    u1.resize(o->P.m);
+    srhs.resize(o->P.m);
+    real t = t0;
+    for (int s = 0; s < nsteps; s++) {
+        euler_step(H, u0, u1, srhs, t, dt);
+        u0 = u1;
+        t += dt;
+    }
+    store_field(u0, D, Rx, Ry, Rz);
+}
+
 // wave: vel_kind 0 -> constant velocity a = vel (u_t + a.grad u = 0, gG = -a);
 //       vel_kind 1 -> radial velocity about `center` (scalar_wave.cpp:28-33)
 void orc_wave_rhs(orc_problem* o, int vel_kind, const double* vel, const double* center,
@@ -2191,6 +2223,32 @@ void orc_wave_rk4(orc_problem* o, int vel_kind, const double* vel, const double*
     real t = t0;
     for (int s = 0; s < nsteps; s++) {
         rk4_step(W, u0, u1, rk, srhs, t, dt);
+        u0 = u1;
+        t += dt;
+    }
+    store_field(u0, D, Rx, Ry, Rz);
+}
+
+void orc_wave_euler(orc_problem* o, int vel_kind, const double* vel, const double* center,
+                    int sol_kind, const double* params, double t0, double dt, int nsteps,
+                    double* D, double* Rx, double* Ry, double* Rz)
+{
+    wave_sys W;
+    W.P = &o->P;
+    W.vel_kind = vel_kind;
+    for (int c = 0; c < 3; c++) {
+        W.vel[c] = vel ? vel[c] : 0.0;
+        W.center[c] = center ? center[c] : 0.0;
+    }
+    W.sol = make_solution(o, sol_kind, params);
+    W.init();
+    field_buf u0, u1, srhs;
+    load_field(u0, o, D, Rx, Ry, Rz);
+    u1.resize(o->P.m);
+    srhs.resize(o->P.m);
+    real t = t0;
+    for (int s = 0; s < nsteps; s++) {
+        euler_step(W, u0, u1, srhs, t, dt);
         u0 = u1;
         t += dt;
     }

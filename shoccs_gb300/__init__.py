@@ -271,6 +271,11 @@ class System:
         _capi.check(_capi.lib().shoccs_system_rk4(self._h, float(t0), float(dt), int(nsteps),
                                                   _stream(stream)))
 
+    def euler(self, t0, dt, nsteps, stream=None):
+        """forward Euler steps (integrators::euler), FP64 systems"""
+        _capi.check(_capi.lib().shoccs_system_euler(self._h, float(t0), float(dt), int(nsteps),
+                                                    _stream(stream)))
+
     def rk4_timed(self, t0, dt, nsteps, stream=None):
         """rk4 with per-kernel CUDA-event timing: returns dict of total milliseconds."""
         ms = (ctypes.c_double * 6)()

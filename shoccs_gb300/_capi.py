@@ -91,6 +91,8 @@ SIGNATURES = {
                                 ctypes.c_void_p],
     "shoccs_system_rk4": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                           ctypes.c_void_p],
+    "shoccs_system_euler": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                            ctypes.c_void_p],
     "shoccs_system_rk4_timed": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
                                 ctypes.c_int, ctypes.c_void_p, c_double_p],
     "shoccs_system_rhs": [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(Field),

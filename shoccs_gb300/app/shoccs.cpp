@@ -24,6 +24,7 @@
 //   simulation.manufactured_solution
 //                              manufactured_solution::from_lua  src/mms/mms.cpp:34-98
 //   simulation.integrator      integrator::from_lua         src/temporal/integrator.cpp:27-49
+//                              (rk4, or euler for FP64 systems)
 //   simulation.step_controller step_controller::from_lua    src/temporal/step_controller.cpp:7-29
 //   simulation.io              field_io::from_lua           src/io/field_io.cpp:71-103
 //   simulation.logging, logging_dir
@@ -333,12 +334,14 @@ int run_simulation(const value& sim)
         log.err("simulation.integrator not specified (the empty integrator is not available in this build)");
         return 0;
     }
-    if (const std::string it = str_or(at(integ, "type"), ""); it != "rk4") {
-        log.err(it == "euler" ? "integrator.type euler is not available in this build (rk4)"
-                              : "integrator.type must be one of: [rk4, euler]");
+    const std::string it = str_or(at(integ, "type"), "");
+    if (it != "rk4" && it != "euler") {
+        log.err("integrator.type must be one of: [rk4, euler]");
         return 0;
     }
-    log.info("building rk4 integrator");
+    log.info("building " + it + " integrator");
+    const integrators::integrator integrator =
+        it == "euler" ? integrators::integrator{integrators::euler{}} : integrators::integrator{integrators::rk4{}};
     const step_controller ctrl = read_step_controller(sim, log);
     const auto io_cfg = read_io(sim, log);
 
@@ -348,7 +351,7 @@ int run_simulation(const value& sim)
         syslog.emplace(std::filesystem::path{logging_dir} / "system.csv", std::ios::trunc);
         write_system_log_header(*syslog);
     }
-    simulation_cycle cycle(ctrl, syslog ? &*syslog : nullptr, field_io::from_config(*m, io_cfg));
+    simulation_cycle cycle(ctrl, syslog ? &*syslog : nullptr, field_io::from_config(*m, io_cfg), integrator);
     cycle.set_console(enable_logging ? &std::cout : nullptr);
 
     real3 r{};

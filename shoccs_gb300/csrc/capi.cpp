@@ -957,6 +957,27 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     return check_wait_flag(S, s);
 }
 
+shoccs_status shoccs_system_euler(shoccs_system* S, double t0, double dt, int nsteps,
+                                  void* stream)
+{
+    if (!S || nsteps < 0 || !(dt > 0)) return fail(SHOCCS_EINVAL, "bad argument");
+    if (S->desc.prec != PREC_FP64)
+        return fail(SHOCCS_EUNSUPPORTED, "the forward Euler integrator steps FP64 systems");
+    const cudaStream_t s = (cudaStream_t)stream;
+    // the right-hand side's scratch: the unfused step's whole-field register, or (fused
+    // systems) the stage field sa and the Rhalf arrays, which every RK4 step rewrites
+    const FieldF64 K = S->unfused ? S->fk
+                                  : FieldF64{(double*)S->b.sa, {S->b.Rhalf[0], S->b.Rhalf[1], S->b.Rhalf[2]}};
+    double t = t0;
+    for (int i = 0; i < nsteps; i++) {
+        SH_CUDA(launch_euler_fp64(S->P->op, S->P->dr, S->sp, S->nf, S->unfused, S->b, S->state(), K, t, dt, s));
+        t += dt;
+    }
+    SH_CUDA(cudaStreamSynchronize(s));
+    S->t = t;
+    return SHOCCS_OK;
+}
+
 shoccs_status shoccs_system_rk4_timed(shoccs_system* S, double t0, double dt, int nsteps,
                                       void* stream, double kernel_ms[6])
 {

@@ -265,6 +265,11 @@ cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, d
 cudaError_t launch_error_field(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
                                const void* u0, double* const R[3], double t, FieldF64 err,
                                cudaStream_t s);
+// one forward Euler step of an FP64 system (fused: U = {b.u0, b.R}; unfused heat: the whole
+// field); K is scratch for the right-hand side
+cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
+                              bool unfused, const StepBuffers& b, FieldF64 U, FieldF64 K, double t,
+                              double dt, cudaStream_t s);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s);
 cudaError_t launch_initialize(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,

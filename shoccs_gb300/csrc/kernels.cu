@@ -2840,6 +2840,28 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
     return cudaGetLastError();
 }
 
+// One forward Euler step of an FP64 system (integrators::euler, src/temporal/euler.cpp:11-27):
+// K <- rhs(U, t) (the unfused heat right-hand side, or the fused systems' k_rhs with a zero
+// right-hand side at the Dirichlet cut points), U <- U + dt K, then the boundary data at
+// t + dt (Dirichlet faces and Dirichlet cut points).  For fused systems U.D is b.u0 and U.R
+// the state's cut-point values b.R.
+cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
+                              bool unfused, const StepBuffers& b, FieldF64 U, FieldF64 K, double t,
+                              double dt, cudaStream_t s)
+{
+    cudaError_t e = unfused ? heat_rhs_unfused(op, dr, sp, nf, U, t, K, s)
+                            : launch_rhs(op, sp, PREC_FP64, b, t, K.D, K.R, s);
+    if (e != cudaSuccess) return e;
+    const long long n = field_size(op);
+    const long long nbnd = op.n_faces + op.nR[0] + op.nR[1] + op.nR[2];
+    const double t1 = t + dt;
+    k_field_lc<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, U, U, dt, K);
+    k_update_boundary<<<(unsigned)std::max(1LL, (nbnd + 255) / 256), 256, 0, s>>>(
+        op, dr, sp.sol, t1, sp.sol.kind == SOL_SINSIN ? std::exp(-t1) : 0.0, U);
+    g_launches += 2;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,
                        double t, double* out, double* const outR[3], cudaStream_t s)
 {

@@ -187,7 +187,7 @@ def test_cli_usage_and_check(cli, tmp_path):
     ('simulation.mesh.domain_bounds = {min = {0, 0}}', "domain_bounds.max"),
     ('simulation.domain_boundaries.xmin = "periodic"', "incorrect boundary condition"),
     ('simulation.shapes = {{type = "yz_rect"}}', "shape type 'yz_rect' is not supported"),
-    ('simulation.integrator.type = "euler"', "integrator.type euler is not available"),
+    ('simulation.integrator.type = "ab3"', "integrator.type must be one of: [rk4, euler]"),
     ('simulation.system.precision = "fp16"', "system.precision must be fp64 or mixed"),
     ('simulation = 3', "the global table `simulation` is required"),
 ])
