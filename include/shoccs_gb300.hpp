@@ -675,20 +675,27 @@ public:
     }
 };
 
+// no time integration: the state keeps its value while the cycle advances the time
+// (src/temporal/empty_integrator.hpp; integrator::operator() does nothing for it)
+struct empty {
+};
+
 // the integrator of a simulation (src/temporal/integrator.hpp: a variant over the
 // integrators), rk4 unless chosen otherwise
 class integrator
 {
-    bool euler_ = false;
+    int kind_ = 0; // 0 rk4, 1 euler, 2 empty
 
 public:
     integrator(rk4 = {}) {}
-    integrator(euler) : euler_{true} {}
-    bool is_euler() const { return euler_; }
+    integrator(euler) : kind_{1} {}
+    integrator(empty) : kind_{2} {}
+    bool is_euler() const { return kind_ == 1; }
+    bool is_empty() const { return kind_ == 2; }
     void operator()(systems::scalar_system& sys, real t, real dt, void* stream = nullptr) const
     {
-        if (euler_) euler{}(sys, t, dt, stream);
-        else rk4{}(sys, t, dt, stream);
+        if (kind_ == 1) euler{}(sys, t, dt, stream);
+        else if (kind_ == 0) rk4{}(sys, t, dt, stream);
     }
 };
 } // namespace integrators

@@ -24,7 +24,7 @@
 //   simulation.manufactured_solution
 //                              manufactured_solution::from_lua  src/mms/mms.cpp:34-98
 //   simulation.integrator      integrator::from_lua         src/temporal/integrator.cpp:27-49
-//                              (rk4, or euler for FP64 systems)
+//                              (rk4, euler for FP64 systems; none: the empty integrator)
 //   simulation.step_controller step_controller::from_lua    src/temporal/step_controller.cpp:7-29
 //   simulation.io              field_io::from_lua           src/io/field_io.cpp:71-103
 //   simulation.logging, logging_dir
@@ -330,18 +330,19 @@ int run_simulation(const value& sim)
 
     // integrator::from_lua
     const value integ = at(sim, "integrator");
+    integrators::integrator integrator{integrators::empty{}};
     if (!valid(integ)) {
-        log.err("simulation.integrator not specified (the empty integrator is not available in this build)");
-        return 0;
+        log.warn("simulation.integrator not specified.  Defaulting to empty");
+    } else {
+        const std::string it = str_or(at(integ, "type"), "");
+        if (it != "rk4" && it != "euler") {
+            log.err("integrator.type must be one of: [rk4, euler]");
+            return 0;
+        }
+        log.info("building " + it + " integrator");
+        integrator = it == "euler" ? integrators::integrator{integrators::euler{}}
+                                   : integrators::integrator{integrators::rk4{}};
     }
-    const std::string it = str_or(at(integ, "type"), "");
-    if (it != "rk4" && it != "euler") {
-        log.err("integrator.type must be one of: [rk4, euler]");
-        return 0;
-    }
-    log.info("building " + it + " integrator");
-    const integrators::integrator integrator =
-        it == "euler" ? integrators::integrator{integrators::euler{}} : integrators::integrator{integrators::rk4{}};
     const step_controller ctrl = read_step_controller(sim, log);
     const auto io_cfg = read_io(sim, log);
 

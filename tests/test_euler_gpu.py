@@ -98,3 +98,26 @@ def test_cli_euler(tmp_path):
         assert float(row[1]) == t
         assert [float(v) for v in row[3:14]] == list(w.stats(t)[0])
     assert len(rows) == 8  # t < 0.1 with dt = 1/64: 7 steps
+
+
+@pytest.mark.gpu
+def test_cli_without_integrator_keeps_the_state(tmp_path):
+    """no integrator table: the reference's empty integrator, the state stays the initial one
+    while the cycle advances the time and logs the statistics"""
+    cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "shoccs_gb300", "_build", "shoccs")
+    r = subprocess.run([cli, os.path.join(LUA, "wave_radial_2d.lua"), "--script",
+                        "simulation.integrator = nil; simulation.step_controller.max_time = 0.05"],
+                       cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "[error]" not in r.stderr, r.stderr
+    assert "Defaulting to empty" in r.stdout
+    rows = _system_csv(str(tmp_path / "logs" / "system.csv"))
+    assert len(rows) == 5  # t < 0.05 with dt = 1/64: 4 steps
+    p = S.Problem(**WAVE)
+    sol = list(WAVE_CENTER) + [0.0]
+    w = S.ScalarWave(p, S.PREC_FP64, S.VEL_RADIAL, (0, 0, 0), WAVE_CENTER, S.SOL_RADIAL_SIN, sol, 10.0)
+    w.initialize(0.0)
+    t = 0.0
+    for k, row in enumerate(rows):
+        assert float(row[1]) == t
+        assert [float(v) for v in row[3:14]] == list(w.stats(t)[0])  # the initial state at time t
+        t += 0.5 * 1.25 / 40
