@@ -1,8 +1,8 @@
 // shoccs_oracle.cpp -- CPU oracle for the SHOCCS derivative-operator / RHS / RK4 path.
 //
 // TEST INFRASTRUCTURE ONLY.  This file is a plain, serial-by-default restatement of the
-// reference algorithm (pbrady/shoccs, C++20 on Kokkos host) used as the correctness
-// checker for the CUDA product path and as the timed CPU baseline.  Nothing in the product
+// reference algorithm (pbrady/shoccs, C++20 on Kokkos host): the tests compare the CUDA
+// product path with it, and it is the timed CPU baseline.  Nothing in the product
 // library links, loads or calls it; only tests/, __graft_entry__.smoke() and bench.py's
 // CPU-baseline leg do.
 //
