@@ -324,6 +324,45 @@ def batched_bench(stream, count=256, steps=200, pg=None, rank=0, world=1, looped
     return out
 
 
+def unfused_bench(stream, n=128, steps=10):
+    """Floating closures at scale: FP64 heat, n^3, sphere (0.5, 0.5, 0.5) r = 0.25, sin-sin
+    manufactured solution.  With a Floating sphere the cut-point values are state and the
+    system runs the unfused whole-field step (standalone Laplacian with its R-space rows, the
+    source, whole-field axpys, the boundary update); the same grid with a Dirichlet sphere runs
+    the fused FP64 stage kernels and is timed alongside.  `steps` RK4 steps after a warm-up,
+    timed with CUDA events on the launching stream (10 steps: this scheme's Floating closure
+    grows without bound after a few tens of steps on this geometry)."""
+    import torch
+    import shoccs_gb300 as S
+    from shoccs_gb300 import workloads as W
+    dt = W.heat_dt(n)
+    res = {"grid": [n, n, n], "rk4_steps": steps, "dtype": "f64"}
+    for name, bc in (("floating_unfused", "floating"), ("dirichlet_fused", "dirichlet")):
+        c = dict(W.adjoint_case(n), spheres=[((0.5, 0.5, 0.5), 0.25, bc)])
+        p = S.Problem(**c)
+        h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, [1.0])
+        h.initialize(0.0, stream)
+        h.rk4(0.0, dt, 2, stream)  # warm-up
+        h.initialize(0.0, stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        n0 = S.kernel_launches()
+        e0.record(stream)
+        h.rk4(0.0, dt, steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        st, ok = h.stats(steps * dt, stream)
+        res[name] = {"ms_per_step": ms / steps, "dof_updates_per_s": (p.size + sum(p.nR)) * steps / (ms * 1e-3),
+                     "stage_kernel": h.stage_kernel, "cut_points": int(sum(p.nR)), "max_error": st[0],
+                     "valid": bool(ok)}
+        res[name]["launches_per_step"] = (S.kernel_launches() - n0) / steps
+        del h, p
+    res["unfused_over_fused"] = res["floating_unfused"]["ms_per_step"] / res["dirichlet_fused"]["ms_per_step"]
+    return res
+
+
 def adjoint_bench(stream, n=128, steps=200, every=20, ndir=32, eps=1e-6, cg_iters=10):
     """The adjoint configuration: 3-D heat 128^3, sphere r = 0.25, homogeneous Dirichlet,
     u0 = seeded sum of 16 Gaussians, 200 RK4 steps (FP64) with a checkpoint every 20.
@@ -477,6 +516,10 @@ def main():
                     help="run the operator microbenchmark alone and print its JSON")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched heat solves")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint configuration")
+    ap.add_argument("--no-unfused", action="store_true",
+                    help="skip the Floating-sphere (unfused FP64 step) timing")
+    ap.add_argument("--unfused-only", action="store_true",
+                    help="only the Floating-sphere (unfused FP64 step) timing")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run the adjoint configuration alone and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
@@ -508,10 +551,12 @@ def main():
             pg.barrier()
         torch.cuda.synchronize()
 
-    if args.micro_only or args.batched_only or args.adjoint_only:
+    if args.micro_only or args.batched_only or args.adjoint_only or args.unfused_only:
         st = torch.cuda.Stream()
         with torch.cuda.stream(st):  # torch arithmetic and library calls on one stream
-            if args.micro_only:
+            if args.unfused_only:
+                print(json.dumps(unfused_bench(st)), flush=True)
+            elif args.micro_only:
                 peak, _ = measured_peak()
                 print(json.dumps(operator_microbench(st, peak)), flush=True)
             elif args.batched_only:
@@ -686,6 +731,11 @@ def main():
             line["batched"] = batched_bench(stream, pg=pg, rank=rank, world=ws)
         if not args.no_adjoint:
             line["adjoint"] = adjoint_bench(stream)
+        if not args.no_unfused:
+            try:
+                line["floating_closures"] = unfused_bench(stream)
+            except Exception as e:  # a secondary figure never costs the headline line
+                line["floating_closures"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0 and not args.no_cpu_baseline:
         cb, _, _ = cpu_rate(8, 15.0)
         line["cpu_baseline"] = cb
