@@ -2650,9 +2650,24 @@ __device__ __forceinline__ void phys_of_point(const DevOp& op, long long p, int 
     ijk[2] = (int)(p % op.n[2]);
 }
 
+// The RK4 bookkeeping folded into the right-hand side's last pass (an unfused stage):
+// instead of storing the right-hand side v, acc <- acc + c_acc v and, before the last
+// stage, y <- u + c_y v (the next stage's input), with the arithmetic of k_field_lc.
+struct StageFold {
+    int on;
+    FieldF64 acc;
+    double c_acc;
+    int has_y;
+    FieldF64 y;
+    FieldF64 u;
+    double c_y;
+};
+
 // K <- k * lap + source (heat::build_rhs_graph, heat.cpp:164-288): the source at fluid D
-// points and at non-Dirichlet cut points; 0 on Dirichlet faces and at Dirichlet cut points
-__global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, double et, FieldF64 K)
+// points and at non-Dirichlet cut points; 0 on Dirichlet faces and at Dirichlet cut points.
+// With f.on the value goes into the RK4 registers instead (StageFold).
+__global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, double et, FieldF64 K,
+                                  StageFold f)
 {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long i = 0;
@@ -2660,6 +2675,14 @@ __global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, dou
     if (part < 0) return;
     const bool sinsin = sp.sol.kind == SOL_SINSIN;
     const bool gauss = sp.sol.kind == SOL_GAUSSIAN;
+    auto put = [&](double* k, double* acc, double* y, const double* u, long long j, double v) {
+        if (!f.on) {
+            k[j] = v;
+            return;
+        }
+        acc[j] = __dadd_rn(acc[j], __dmul_rn(f.c_acc, v));
+        if (f.has_y) y[j] = __dadd_rn(u[j], __dmul_rn(f.c_y, v));
+    };
     // the source ddt - k lap of the Gaussian sum at x
     auto gauss_source = [&](const double x[3]) {
         const GaussEval ge = gauss_eval(sp.sol, t, x);
@@ -2679,7 +2702,7 @@ __global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, dou
             }
         }
         if (c & CLS_DIRFACE) v = 0.0;
-        K.D[i] = v;
+        put(K.D, f.acc.D, f.y.D, f.u.D, i, v);
     } else {
         const int d = part - 1;
         double v = __dmul_rn(K.R[d][i], sp.k);
@@ -2689,7 +2712,7 @@ __global__ void k_heat_rhs_finish(DevOp op, DevR dr, SysParams sp, double t, dou
             v = __dadd_rn(v, heat_source(sp, sol_at(sp.sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i)));
         else if (gauss)
             v = __dadd_rn(v, gauss_source(dr.pos[d] + 3 * i));
-        K.R[d][i] = v;
+        put(K.R[d], f.acc.R[d], f.y.R[d], f.u.R[d], i, v);
     }
 }
 
@@ -2771,7 +2794,7 @@ __global__ void k_neumann_faces(DevOp op, DevSol sol, int mask, double t, double
 long long field_size(const DevOp& op) { return op.N + op.nR[0] + op.nR[1] + op.nR[2]; }
 
 cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
-                             FieldF64 u, double t, FieldF64 K, cudaStream_t s)
+                             FieldF64 u, double t, FieldF64 K, cudaStream_t s, StageFold fold = {})
 {
     const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
     if (nf.mask) {
@@ -2789,7 +2812,7 @@ cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& s
     cudaError_t e = launch_laplacian(op, PREC_FP64, u.D, uR, nf.mask ? nf.nu : nullptr, K.D, kR, s);
     if (e != cudaSuccess) return e;
     const long long n = field_size(op);
-    k_heat_rhs_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sp, t, et, K);
+    k_heat_rhs_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sp, t, et, K, fold);
     ++g_launches;
     return cudaGetLastError();
 }
@@ -2818,19 +2841,20 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
     cudaError_t e = cudaMemsetAsync(ACC.D, 0, op.N * sizeof(double), s);
     for (int d = 0; d < 3 && e == cudaSuccess; d++)
         if (op.nR[d]) e = cudaMemsetAsync(ACC.R[d], 0, op.nR[d] * sizeof(double), s);
+    // stage i: K <- lap(in), then the last pass adds dt rkf[i] k_i into ACC and (i < 3)
+    // writes the next stage's input Y <- U + dt rki[i+1] k_i, whose boundary data is then
+    // set at its time; the input of stage i > 0 is Y, which the Laplacian has finished
+    // reading before that pass overwrites it
     for (int i = 0; i < 4 && e == cudaSuccess; i++) {
         const double ti = t + dt * rki[i];
-        FieldF64 in = U;
-        if (i > 0) {
-            k_field_lc<<<nb, 256, 0, s>>>(op, Y, U, dt * rki[i], K);
-            k_update_boundary<<<bb, 256, 0, s>>>(op, dr, sp.sol, ti, et(ti), Y);
-            g_launches += 2;
-            in = Y;
-        }
-        e = heat_rhs_unfused(op, dr, sp, nf, in, ti, K, s);
+        const StageFold fold{1, ACC, dt * rkf[i], i < 3, Y, U, i < 3 ? dt * rki[i + 1] : 0.0};
+        e = heat_rhs_unfused(op, dr, sp, nf, i == 0 ? U : Y, ti, K, s, fold);
         if (e != cudaSuccess) break;
-        k_field_lc<<<nb, 256, 0, s>>>(op, ACC, ACC, dt * rkf[i], K);
-        ++g_launches;
+        if (i < 3) {
+            const double tn = t + dt * rki[i + 1];
+            k_update_boundary<<<bb, 256, 0, s>>>(op, dr, sp.sol, tn, et(tn), Y);
+            ++g_launches;
+        }
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
