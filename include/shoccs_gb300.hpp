@@ -498,7 +498,11 @@ protected:
 
     scalar_system(const mesh& m, const stencil& st, const bcs::Grid& g, const bcs::Object& o,
                   const shoccs_system_desc& d)
-        : p_{m, st, g, o}, max_error_{d.max_error}
+        : scalar_system(problem{m, st, g, o}, d)
+    {
+    }
+    // on operators already built for the (mesh, stencil, bcs) triple
+    scalar_system(const problem& p, const shoccs_system_desc& d) : p_{p}, max_error_{d.max_error}
     {
         shoccs_system* raw = nullptr;
         detail::check(shoccs_system_create(p_.get(), &d, &raw), "shoccs_system_create");
@@ -591,6 +595,11 @@ public:
         : scalar_system(m, st, grid_bcs, object_bcs, desc(m_sol, diffusivity, prec))
     {
     }
+    // on a problem's operators (shared with derivative / laplacian / gradient of the same triple)
+    heat(const problem& p, manufactured_solution&& m_sol, real diffusivity, precision prec = precision::fp64)
+        : scalar_system(p, desc(m_sol, diffusivity, prec))
+    {
+    }
 };
 
 // u_t + a . grad u = 0 written as u_t = gG . grad u (src/systems/scalar_wave.hpp:16-80)
@@ -628,6 +637,11 @@ public:
     scalar_wave(mesh&& m, bcs::Grid&& grid_bcs, bcs::Object&& object_bcs, stencil st, real3 center,
                 real radius, real max_error = 100.0, precision prec = precision::fp64)
         : scalar_system(m, st, grid_bcs, object_bcs, radial(center, radius, max_error, prec))
+    {
+    }
+    scalar_wave(const problem& p, real3 center, real radius, real max_error = 100.0,
+                precision prec = precision::fp64)
+        : scalar_system(p, radial(center, radius, max_error, prec))
     {
     }
     // extension: a constant velocity a with a closed-form exact solution (e.g. mms::gauss_pulse)
@@ -745,7 +759,8 @@ inline std::string num(real v)
 
 // the system log line of heat::log / scalar_wave::log (heat.cpp:60-68) behind the
 // "%Y-%m-%d %H:%M:%S.%f," pattern the systems set: time,step,stats...,wall ms
-inline void log_line(std::ostream& os, const step_controller& c, const system_stats& st)
+// "%Y-%m-%d %H:%M:%S.%f", the timestamp of the reference's log lines
+inline std::string timestamp()
 {
     const auto now = std::chrono::system_clock::now();
     const std::time_t tt = std::chrono::system_clock::to_time_t(now);
@@ -756,7 +771,12 @@ inline void log_line(std::ostream& os, const step_controller& c, const system_st
     std::strftime(ts, sizeof ts, "%Y-%m-%d %H:%M:%S", &tm);
     char frac[16];
     std::snprintf(frac, sizeof frac, ".%06lld", (long long)us);
-    os << ts << frac << ',' << num(c.simulation_time()) << ',' << c.simulation_step();
+    return std::string(ts) + frac;
+}
+
+inline void log_line(std::ostream& os, const step_controller& c, const system_stats& st)
+{
+    os << timestamp() << ',' << num(c.simulation_time()) << ',' << c.simulation_step();
     for (real v : st.stats) os << ',' << num(v);
     char wall[32];
     std::snprintf(wall, sizeof wall, "%.3f", st.wall_time_s * 1000.0);
@@ -1132,6 +1152,28 @@ inline void write_system_log_header(std::ostream& os)
 {
     os << "Timestamp,Time,Step,Linf,Min,Max,Domain_Linf,Domain_ic,Rx_Linf,Rx_ic,Ry_Linf,Ry_ic,Rz_Linf,"
           "Rz_ic,Wall_ms\n";
+}
+
+// the geometry log the mesh writes when it is built (src/mesh/mesh.cpp:139-151): a header
+// line, then per cut point "timestamp,direction,index,psi,x, y, z,i, j, k" (position and
+// the solid point's index triple each joined by ", ")
+inline void write_geometry_log(std::ostream& os, const problem& p)
+{
+    os << "Timestamp,direction,ic,psi,x,y,z,i,j,k\n";
+    for (int d = 0; d < 3; d++) {
+        const integer n = p.R(d);
+        if (!n) continue;
+        std::vector<real> psi(n), pos(3 * n);
+        std::vector<int> sc(3 * n);
+        detail::check(shoccs_problem_cut_points(p.get(), d, psi.data(), pos.data(), nullptr, nullptr,
+                                                sc.data(), nullptr),
+                      "shoccs_problem_cut_points");
+        for (integer i = 0; i < n; i++)
+            os << detail::timestamp() << ',' << d << ',' << i << ',' << detail::num(psi[i]) << ','
+               << detail::num(pos[3 * i]) << ", " << detail::num(pos[3 * i + 1]) << ", "
+               << detail::num(pos[3 * i + 2]) << ',' << sc[3 * i] << ", " << sc[3 * i + 1] << ", "
+               << sc[3 * i + 2] << '\n';
+    }
 }
 
 class simulation_cycle

@@ -5,7 +5,8 @@
 // Runs the Lua input file (and then the --script text, whose assignments take precedence),
 // reads the global table `simulation` section by section as the reference's from_lua
 // readers do, and runs the simulation cycle on the GPU: the system log goes to
-// <logging_dir>/system.csv (header line, then one line per step), the field dumps to the io
+// <logging_dir>/system.csv (header line, then one line per step) and geometry.csv (the cut
+// points, src/mesh/mesh.cpp:139-151), the field dumps to the io
 // table's directory, the progress messages to standard output.  --check stops after the Lua
 // has run, as the reference does.  As in the reference, a section that cannot be read is
 // reported and the program still exits 0; a Lua error exits non-zero.
@@ -346,9 +347,14 @@ int run_simulation(const value& sim)
     const step_controller ctrl = read_step_controller(sim, log);
     const auto io_cfg = read_io(sim, log);
 
+    // the operators of the (mesh, stencil, bcs) triple, built once on the host; the mesh's
+    // geometry log comes from them, and the system runs on them
+    const problem prob{*m, *st, bc->first, bc->second};
     std::optional<std::ofstream> syslog;
     if (enable_logging) {
         std::filesystem::create_directories(logging_dir);
+        std::ofstream geo(std::filesystem::path{logging_dir} / "geometry.csv", std::ios::trunc);
+        write_geometry_log(geo, prob);
         syslog.emplace(std::filesystem::path{logging_dir} / "system.csv", std::ios::trunc);
         write_system_log_header(*syslog);
     }
@@ -367,7 +373,7 @@ int run_simulation(const value& sim)
         manufactured_solution sol = std::holds_alternative<manufactured_solution>(ms)
                                         ? std::get<manufactured_solution>(ms)
                                         : mms::zero();
-        systems::heat h(mesh{*m}, bcs::Grid{bc->first}, bcs::Object{bc->second}, std::move(sol), *st, diff, prec);
+        systems::heat h(prob, std::move(sol), diff, prec);
         r = cycle.run(h);
     } else {
         log.info("building scalar_wave system");
@@ -397,8 +403,7 @@ int run_simulation(const value& sim)
             log.err("a system.center / system.radius must be specified for scalar_wave");
             return 0;
         }
-        systems::scalar_wave w(mesh{*m}, bcs::Grid{bc->first}, bcs::Object{bc->second}, *st, center, radius,
-                               max_error, prec);
+        systems::scalar_wave w(prob, center, radius, max_error, prec);
         r = cycle.run(w);
     }
     std::cout << "result " << detail::num(r[0]) << " " << detail::num(r[1]) << " " << detail::num(r[2]) << "\n";

@@ -217,3 +217,30 @@ def test_template_filled_in_is_valid(cli, tmp_path):
     f.write_text(fill_template(31, 0.1, "E4", (0.1, 0.7)))
     r = _run(cli, ["--check", str(f)], tmp_path)
     assert r.returncode == 0, r.stderr
+
+
+def test_cli_geometry_log(cli, tmp_path):
+    """logs/geometry.csv (src/mesh/mesh.cpp:139-151) is written from the host-side operators
+    before the system is created: header, then per cut point direction, index, psi, the
+    position and the solid point's indices (each triple joined by ", "), equal to the library's
+    cut points.  Without a GPU the run stops at the system; only the log is checked."""
+    import shoccs_gb300 as S
+    _run(cli, [os.path.join(LUA, "heat_circle_2d.lua"), "--script", "simulation.step_controller.max_step = 1"],
+         tmp_path)
+    lines = (tmp_path / "mylogs" / "geometry.csv").read_text().splitlines()
+    assert lines[0] == "Timestamp,direction,ic,psi,x,y,z,i,j,k"
+    p = S.Problem(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0), spheres=[((0.51, 0.49, 0.0), 0.2, "dirichlet")],
+                  grid_bc=("dirichlet",) * 4 + ("floating",) * 2, scheme="E4_2")
+    want = []
+    for d in range(3):
+        cp = p.cut_points(d)
+        for i in range(p.nR[d]):
+            want.append((d, i, cp["psi"][i], tuple(cp["position"][i]), tuple(cp["solid_coord"][i])))
+    rows = []
+    for line in lines[1:]:
+        ts, d, i, psi, rest = line.split(",", 4)
+        pos_s, ijk_s = rest.split(",", 3)[:3], rest.split(",", 3)[3]
+        rows.append((int(d), int(i), float(psi), tuple(float(v) for v in pos_s),
+                     tuple(int(v) for v in ijk_s.split(", "))))
+        assert ts[:4].isdigit() and ", " in rest
+    assert rows == want
