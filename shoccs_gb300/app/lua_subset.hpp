@@ -7,7 +7,8 @@
 // This header evaluates exactly that subset:
 //
 //   statements   [local] name {, name} = exp {, exp};  target.field = exp;  target[exp] = exp;
-//                do ... end;  function calls (print, math.*);  function name(...) ... end
+//                do ... end;  if ... then ... elseif ... else ... end;  numeric for;  while;
+//                break;  function calls (print, math.*);  function name(...) ... end
 //   expressions  nil true false numbers strings (all quote forms, long brackets) tables
 //                or and < > <= >= == ~= .. + - * / // % ^ (right-associative) not # unary -
 //                name, .field, [key], calls f(...), f{...}, f"..."
@@ -17,8 +18,8 @@
 //                acos atan fmod min max tointeger type modf ult
 //
 // Numbers are doubles (integer-valued ones index array parts and print as integers).  Any
-// other construct (loops, if, methods, metatables, goto) is rejected with a message naming
-// the line.
+// other construct (generic for, repeat, methods, metatables, goto) is rejected with a
+// message naming the line; a loop that runs more than 1e7 iterations is stopped.
 #pragma once
 
 #include <cctype>
@@ -438,11 +439,147 @@ struct state::parser {
         while (!(cur().kind == tk::eof || (end_kw && is_kw(end_kw)))) statement();
     }
 
+    // ---- control flow ----
+    struct break_signal {
+    };
+    bool at_kw(std::size_t q, const char* k) const { return t[q].kind == tk::name && t[q].text == k; }
+    // from q (just inside a block), the index of the first of `stops` (end, else, elseif)
+    // at nesting depth 0
+    std::size_t scan_block(std::size_t q, bool if_branch) const
+    {
+        int depth = 0;
+        for (; t[q].kind != tk::eof; ++q) {
+            if (t[q].kind != tk::name) continue;
+            const std::string& w = t[q].text;
+            if (depth == 0 && (w == "end" || (if_branch && (w == "else" || w == "elseif")))) return q;
+            if (w == "function" || w == "if" || w == "do" || w == "repeat") ++depth;
+            else if (w == "end" || w == "until") --depth;
+        }
+        throw error(chunk + ":" + std::to_string(t[q].line) + ": 'end' expected");
+    }
+    // run the statements of [p, stop) in a new scope
+    void run_block(std::size_t stop)
+    {
+        scopes.emplace_back();
+        try {
+            while (p < stop) statement();
+        } catch (...) {
+            scopes.pop_back();
+            throw;
+        }
+        scopes.pop_back();
+        if (p != stop) fail("unexpected '" + cur().text + "'");
+    }
+    static constexpr long long max_iterations = 10000000;
+
+    void if_statement()
+    {
+        // if cond then block {elseif cond then block} [else block] end
+        bool done = false;
+        for (;;) {
+            const bool is_else = is_kw("else");
+            ++p; // if / elseif / else
+            bool take = false;
+            if (!is_else) {
+                const value c = expr();
+                expect_kw("then");
+                take = !done && c.truthy();
+            } else {
+                take = !done;
+            }
+            const std::size_t stop = scan_block(p, true);
+            if (take) {
+                run_block(stop);
+                done = true;
+            }
+            p = stop;
+            if (is_kw("end")) {
+                ++p;
+                return;
+            }
+            if (is_else) fail("'end' expected near '" + cur().text + "'");
+        }
+    }
+
+    void for_statement()
+    {
+        ++p; // for
+        const std::string var = name();
+        if (!is_op("=")) fail("only numeric for loops are supported");
+        ++p;
+        const double a = num(expr(), "for initial value");
+        expect_op(",");
+        const double b = num(expr(), "for limit");
+        double step = 1.0;
+        if (is_op(",")) {
+            ++p;
+            step = num(expr(), "for step");
+        }
+        if (step == 0) fail("'for' step is zero");
+        expect_kw("do");
+        const std::size_t body = p, stop = scan_block(p, false);
+        long long n = 0;
+        try {
+            for (double v = a; step > 0 ? v <= b : v >= b; v += step) {
+                if (++n > max_iterations) fail("loop runs too long");
+                p = body;
+                scopes.push_back({{var, value{v}}});
+                try {
+                    run_block(stop);
+                } catch (...) {
+                    scopes.pop_back();
+                    throw;
+                }
+                scopes.pop_back();
+            }
+        } catch (const break_signal&) {
+        }
+        p = stop + 1;
+    }
+
+    void while_statement()
+    {
+        ++p; // while
+        const std::size_t cond = p;
+        bool go = expr().truthy();
+        expect_kw("do");
+        const std::size_t body = p, stop = scan_block(p, false);
+        long long n = 0;
+        try {
+            while (go) {
+                if (++n > max_iterations) fail("loop runs too long");
+                p = body;
+                run_block(stop);
+                p = cond;
+                go = expr().truthy();
+                expect_kw("do");
+            }
+        } catch (const break_signal&) {
+        }
+        p = stop + 1;
+    }
+
     void statement()
     {
         if (is_op(";")) {
             ++p;
             return;
+        }
+        if (is_kw("if")) {
+            if_statement();
+            return;
+        }
+        if (is_kw("for")) {
+            for_statement();
+            return;
+        }
+        if (is_kw("while")) {
+            while_statement();
+            return;
+        }
+        if (is_kw("break")) {
+            ++p;
+            throw break_signal{};
         }
         if (is_kw("local")) {
             ++p;
@@ -927,6 +1064,10 @@ inline void state::script(const std::string& source, const std::string& chunk)
         std::string rest = nl == std::string::npos ? "" : source.substr(nl);
         ps.t = detail::lexer(rest, chunk).run();
     }
-    ps.block_until(nullptr);
+    try {
+        ps.block_until(nullptr);
+    } catch (const parser::break_signal&) {
+        throw error(chunk + ": break outside a loop");
+    }
 }
 } // namespace ccs::lua

@@ -137,9 +137,56 @@ def test_lua_subset_script_after_file(lua_eval):
     assert _num(out, "result.a") == 1 and _num(out, "result.b.c") == 3 and _num(out, "result.d") == 2
 
 
+CONTROL = r'''
+result = {shapes = {}}
+for i = 1, 4 do
+  local r = 0.05 * i
+  if i % 2 == 0 then
+    result.shapes[#result.shapes + 1] = {radius = r, kind = "even"}
+  elseif i == 3 then
+    result.shapes[#result.shapes + 1] = {radius = r, kind = "three"}
+  else
+    result.shapes[#result.shapes + 1] = {radius = r, kind = "odd"}
+  end
+end
+local n = 0
+while true do
+  n = n + 1
+  if n >= 5 then break end
+end
+result.n = n
+for k = 10, 1, -3 do result.last = k end
+for k = 1, 0 do result.never = true end
+local s = 0
+for i = 1, 10 do
+  if i > 3 then break end
+  s = s + i
+end
+result.s = s
+result.i_after = i
+if false then result.x = 1 elseif nil then result.x = 2 else result.x = 3 end
+if true then result.y = 1 end
+'''
+
+
+def test_lua_subset_control_flow(lua_eval):
+    rc, out = lua_eval(CONTROL)
+    assert rc == 0, out
+    kinds = [out["result.shapes[%d].kind" % i][1] for i in range(1, 5)]
+    assert kinds == ["odd", "even", "three", "even"]
+    assert [_num(out, "result.shapes[%d].radius" % i) for i in range(1, 5)] == [0.05 * i for i in range(1, 5)]
+    assert _num(out, "result.n") == 5 and _num(out, "result.s") == 6 and _num(out, "result.last") == 1
+    assert "result.never" not in out and "result.i_after" not in out  # loop variables are local
+    assert _num(out, "result.x") == 3 and _num(out, "result.y") == 1
+
+
 @pytest.mark.parametrize("src,msg", [
+    ("break", "break outside a loop"),
+    ("for k, v in pairs({}) do end", "only numeric for loops are supported"),
+    ("for i = 1, 2, 0 do end", "'for' step is zero"),
+    ("if true then x = 1", "'end' expected"),
     ("x = = 1", ":1:"),
-    ("\n\nfor i = 1, 2 do end", ":3: unsupported statement"),
+    ("\n\nrepeat x = 1 until true", ":3: unsupported statement"),
     ("f = function() return 1 end\nx = f()", ":2: functions defined in the input"),
     ("x = y.z", "attempt to index a nil value"),
     ("x = {1, 2", "'}' expected"),
