@@ -12,8 +12,9 @@
 //   expressions  nil true false numbers strings (all quote forms, long brackets) tables
 //                or and < > <= >= == ~= .. + - * / // % ^ (right-associative) not # unary -
 //                name, .field, [key], calls f(...), f{...}, f"..."
-//   functions    function literals are kept as opaque values (their bodies are skipped);
-//                they can be stored and compared with nil but not called
+//   functions    function literals and definitions (global, local, a.b.c) with named
+//                parameters and return; calls run the body (one result; the enclosing
+//                locals are captured by value when the function is defined; 200 levels)
 //   math         pi huge maxinteger mininteger abs ceil floor sqrt exp log sin cos tan asin
 //                acos atan fmod min max tointeger type modf ult
 //
@@ -44,9 +45,11 @@ struct error : std::runtime_error {
 
 struct table;
 struct value;
-// a function literal of the input (not callable here)
+struct fn_body;
+// a function defined in the input: where it was defined and its body
 struct function_ref {
     std::string where;
+    std::shared_ptr<const fn_body> body;
     bool operator==(const function_ref&) const = default;
 };
 struct builtin {
@@ -351,6 +354,16 @@ public:
 };
 } // namespace detail
 
+// a function's parameters, its body (tokens [start, end) of its chunk; t[end] is its `end`)
+// and the locals visible where it was defined, captured by value
+struct fn_body {
+    std::shared_ptr<const std::vector<detail::token>> toks;
+    std::vector<std::string> params;
+    std::size_t start = 0, end = 0;
+    std::string chunk;
+    std::vector<std::map<std::string, value>> upvalues;
+};
+
 // The interpreter state: the global table (with `math` and `print`) and the chunk's locals.
 class state
 {
@@ -379,11 +392,21 @@ struct state::parser {
     using token = detail::token;
     using tk = detail::tk;
 
-    std::vector<token> t;
+    std::shared_ptr<const std::vector<token>> toks;
+    const std::vector<token>& t;
     std::size_t p = 0;
     std::shared_ptr<table> G;
     std::vector<std::map<std::string, value>> scopes{1};
     std::string chunk;
+    int depth = 0; // calls of input-defined functions in progress
+
+    parser(std::shared_ptr<const std::vector<token>> tokens, std::shared_ptr<table> g, std::string c)
+        : toks{std::move(tokens)}, t{*toks}, G{std::move(g)}, chunk{std::move(c)}
+    {
+    }
+    struct return_signal {
+        std::vector<value> values;
+    };
 
     [[noreturn]] void fail(const std::string& m) const
     {
@@ -581,12 +604,21 @@ struct state::parser {
             ++p;
             throw break_signal{};
         }
+        if (is_kw("return")) {
+            ++p;
+            std::vector<value> v;
+            if (!(cur().kind == tk::eof || is_op(";") || is_kw("end") || is_kw("else") || is_kw("elseif") ||
+                  is_kw("until")))
+                v = exprlist();
+            if (is_op(";")) ++p;
+            throw return_signal{std::move(v)};
+        }
         if (is_kw("local")) {
             ++p;
             if (is_kw("function")) {
                 ++p;
                 const std::string n = name();
-                scopes.back()[n] = skip_function_body(n);
+                scopes.back()[n] = skip_function_body(n, true);
                 return;
             }
             std::vector<std::string> names{name()};
@@ -697,26 +729,38 @@ struct state::parser {
     }
 
     // function literal / definition: skip the parameter list and the body up to its `end`
-    value skip_function_body(const std::string& n)
+    // function body: parameters, then the statements up to the matching `end`; `self_name`
+    // (a `local function`) is visible inside its own body
+    value skip_function_body(const std::string& n, bool self_visible = false)
     {
         const int line = cur().line;
+        auto body = std::make_shared<fn_body>();
         expect_op("(");
         while (!is_op(")")) {
-            if (cur().kind == tk::eof) fail("unfinished parameter list");
-            ++p;
+            if (is_op("...")) fail("varargs are not supported");
+            body->params.push_back(name());
+            if (is_op(",")) ++p;
+            else if (!is_op(")")) fail("')' expected near '" + cur().text + "'");
         }
         ++p;
-        int depth = 1;
-        while (depth > 0) {
+        body->start = p;
+        int nest = 1;
+        while (nest > 0) {
             if (cur().kind == tk::eof) fail("'end' expected (to close function at line " + std::to_string(line) + ")");
             if (cur().kind == tk::name) {
                 const std::string& w = cur().text;
-                if (w == "function" || w == "if" || w == "do" || w == "repeat") ++depth;
-                else if (w == "end" || w == "until") --depth;
+                if (w == "function" || w == "if" || w == "do" || w == "repeat") ++nest;
+                else if (w == "end" || w == "until") --nest;
             }
             ++p;
         }
-        return value{function_ref{chunk + ":" + std::to_string(line) + (n.empty() ? "" : " " + n)}};
+        body->end = p - 1;
+        body->toks = toks;
+        body->chunk = chunk;
+        body->upvalues = scopes;
+        const value f{function_ref{chunk + ":" + std::to_string(line) + (n.empty() ? "" : " " + n), body}};
+        if (self_visible) body->upvalues.back()[n] = f; // recursion (a reference cycle, kept)
+        return f;
     }
 
     // ---- expressions ----
@@ -862,8 +906,25 @@ struct state::parser {
                 fail("bad argument to '" + (*b)->name + "': " + e.what());
             }
         }
-        if (std::holds_alternative<function_ref>(fn.v))
-            fail("functions defined in the input (" + std::get<function_ref>(fn.v).where + ") cannot be called here");
+        if (auto f = std::get_if<function_ref>(&fn.v); f && f->body) {
+            if (depth >= 200) fail("stack overflow (calls nested more than 200 deep)");
+            const fn_body& b = *f->body;
+            parser sub(b.toks, G, b.chunk);
+            sub.depth = depth + 1;
+            sub.scopes = b.upvalues;
+            std::map<std::string, value> args;
+            for (std::size_t i = 0; i < b.params.size(); i++) args[b.params[i]] = i < a.size() ? a[i] : value{};
+            sub.scopes.push_back(std::move(args));
+            sub.p = b.start;
+            try {
+                while (sub.p < b.end) sub.statement();
+            } catch (const return_signal& r) {
+                return r.values.empty() ? value{} : r.values[0];
+            } catch (const break_signal&) {
+                throw error(b.chunk + ": break outside a loop");
+            }
+            return value{};
+        }
         fail(std::string("attempt to call a ") + fn.type_name() + " value");
     }
 
@@ -1055,19 +1116,19 @@ inline state::state()
 
 inline void state::script(const std::string& source, const std::string& chunk)
 {
-    parser ps;
-    ps.t = detail::lexer(source, chunk).run();
-    ps.G = globals_;
-    ps.chunk = chunk;
-    if (source.rfind("#", 0) == 0) { // a first line starting with '#' is skipped
-        std::size_t nl = source.find('\n');
-        std::string rest = nl == std::string::npos ? "" : source.substr(nl);
-        ps.t = detail::lexer(rest, chunk).run();
+    std::string text = source;
+    if (text.rfind("#", 0) == 0) { // a first line starting with '#' is skipped
+        const std::size_t nl = text.find('\n');
+        text = nl == std::string::npos ? "" : text.substr(nl);
     }
+    parser ps(std::make_shared<const std::vector<detail::token>>(detail::lexer(text, chunk).run()), globals_,
+              chunk);
     try {
         ps.block_until(nullptr);
     } catch (const parser::break_signal&) {
         throw error(chunk + ": break outside a loop");
+    } catch (const parser::return_signal&) {
+        // a chunk may end with return
     }
 }
 } // namespace ccs::lua

@@ -33,7 +33,7 @@
 //
 // Manufactured solutions: the reference's "gaussian" (terms {center, variance, amplitude,
 // frequency} in the table's array part; FP64 heat systems) is evaluated on the device; its
-// "lua" kind (functions run by the Lua interpreter) is not available.  A heat system without
+// "lua" kind (Lua functions evaluated at every point for every stage) is not available.  A heat system without
 // a manufactured solution uses the zero solution (homogeneous Dirichlet data, no source),
 // where the reference requires one.
 //
@@ -293,8 +293,8 @@ std::variant<std::monostate, manufactured_solution, std::string> read_mms(const 
         return mms::gaussian(center, variance, amplitude, frequency);
     }
     if (t == "lua")
-        return "manufactured_solution.type = `lua` (functions evaluated by the reference's Lua "
-               "interpreter) is not available here (use `gaussian` or `sinsin`)";
+        return "manufactured_solution.type = `lua` (Lua functions evaluated at every point for "
+               "every stage) is not available here (use `gaussian` or `sinsin`)";
     return "Got manufactured_solution.type = `" + t + "`.  Expected one of: `gaussian, lua, sinsin`";
 }
 

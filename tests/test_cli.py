@@ -169,6 +169,32 @@ if true then result.y = 1 end
 '''
 
 
+FUNCS = r'''
+local function sphere(c, r, bc)
+  return {type = "sphere", center = c, radius = r, boundary_condition = bc or "dirichlet"}
+end
+function fact(n) if n <= 1 then return 1 end return n * fact(n - 1) end
+local function fib(n) if n < 2 then return n end return fib(n - 1) + fib(n - 2) end
+local scale = 3
+local mul = function(x) return x * scale end
+result = {s = sphere({0.5, 0.5}, 0.2, "floating"), f = fact(10), g = fib(15), m = mul(7),
+          none = (function() end)()}
+result.shapes = {}
+for i = 1, 3 do result.shapes[i] = sphere({0.2 * i, 0.5}, 0.05) end
+'''
+
+
+def test_lua_subset_functions(lua_eval):
+    rc, out = lua_eval(FUNCS, "result.after = fact(5)")  # a function of the file, called by --script
+    assert rc == 0, out
+    assert out["result.s.type"] == ["string", "sphere"] and out["result.s.boundary_condition"][1] == "floating"
+    assert _num(out, "result.s.radius") == 0.2 and _num(out, "result.s.center[2]") == 0.5
+    assert _num(out, "result.f") == 3628800 and _num(out, "result.g") == 610 and _num(out, "result.m") == 21
+    assert "result.none" not in out and _num(out, "result.after") == 120
+    assert [_num(out, "result.shapes[%d].center[1]" % i) for i in (1, 2, 3)] == [0.2 * i for i in (1, 2, 3)]
+    assert all(out["result.shapes[%d].boundary_condition" % i][1] == "dirichlet" for i in (1, 2, 3))
+
+
 def test_lua_subset_control_flow(lua_eval):
     rc, out = lua_eval(CONTROL)
     assert rc == 0, out
@@ -187,7 +213,8 @@ def test_lua_subset_control_flow(lua_eval):
     ("if true then x = 1", "'end' expected"),
     ("x = = 1", ":1:"),
     ("\n\nrepeat x = 1 until true", ":3: unsupported statement"),
-    ("f = function() return 1 end\nx = f()", ":2: functions defined in the input"),
+    ("function f(n) return f(n + 1) end\nx = f(1)", "stack overflow"),
+    ("f = function(...) end", "varargs are not supported"),
     ("x = y.z", "attempt to index a nil value"),
     ("x = {1, 2", "'}' expected"),
     ("x = 'open", "unfinished string"),
