@@ -17,6 +17,7 @@
 //                locals are captured by value when the function is defined; 200 levels)
 //   math         pi huge maxinteger mininteger abs ceil floor sqrt exp log sin cos tan asin
 //                acos atan fmod min max tointeger type modf ult
+//   base         print type tostring tonumber string.format
 //
 // Numbers are doubles (integer-valued ones index array parts and print as integers).  Any
 // other construct (generic for, repeat, methods, metatables, goto) is rejected with a
@@ -27,6 +28,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -1105,6 +1107,68 @@ inline state::state()
     math->set(value{"maxinteger"}, value{9.223372036854775807e18});
     math->set(value{"mininteger"}, value{-9.223372036854775808e18});
     globals_->set(value{"math"}, value{math});
+    // base and string functions: type, tostring, tonumber, string.format (%d %i %u %c %x %X %o
+    // %e %E %f %g %G %q-less subset, %s, %%)
+    auto gput = [&](std::shared_ptr<table> tb, const char* n, std::function<value(const std::vector<value>&)> f) {
+        tb->set(value{n}, value{std::make_shared<builtin>(builtin{n, std::move(f)})});
+    };
+    gput(globals_, "type", [](const std::vector<value>& a) {
+        return value{a.empty() ? "nil" : a[0].type_name()};
+    });
+    gput(globals_, "tostring", [](const std::vector<value>& a) { return value{a.empty() ? "nil" : to_display(a[0])}; });
+    gput(globals_, "tonumber", [](const std::vector<value>& a) {
+        if (a.empty()) throw error("value expected");
+        if (a[0].number()) return a[0];
+        if (auto str = a[0].string()) {
+            char* end = nullptr;
+            const double d = std::strtod(str->c_str(), &end);
+            if (end && end != str->c_str()) {
+                while (*end == ' ') ++end;
+                if (*end == '\0') return value{d};
+            }
+        }
+        return value{};
+    });
+    auto strlib = std::make_shared<table>();
+    gput(strlib, "format", [](const std::vector<value>& a) {
+        if (a.empty() || !a[0].string()) throw error("format string expected");
+        const std::string& f = *a[0].string();
+        std::string out;
+        std::size_t arg = 1;
+        for (std::size_t i = 0; i < f.size(); i++) {
+            if (f[i] != '%') {
+                out += f[i];
+                continue;
+            }
+            if (++i >= f.size()) throw error("invalid conversion '%' to 'format'");
+            if (f[i] == '%') {
+                out += '%';
+                continue;
+            }
+            std::string spec = "%";
+            while (i < f.size() && std::strchr("-+ #0123456789.", f[i])) spec += f[i++];
+            if (i >= f.size()) throw error("invalid conversion to 'format'");
+            const char c = f[i];
+            if (arg >= a.size()) throw error("bad argument #" + std::to_string(arg + 1) + " to 'format' (no value)");
+            const value& v = a[arg++];
+            char buf[512];
+            if (c == 's') {
+                const std::string str = to_display(v);
+                std::snprintf(buf, sizeof buf, (spec + "s").c_str(), str.c_str());
+            } else if (std::strchr("dicxXou", c)) {
+                if (!v.number()) throw error("number expected");
+                std::snprintf(buf, sizeof buf, (spec + "ll" + (c == 'i' ? 'd' : c)).c_str(), (long long)*v.number());
+            } else if (std::strchr("eEfgGaA", c)) {
+                if (!v.number()) throw error("number expected");
+                std::snprintf(buf, sizeof buf, (spec + c).c_str(), *v.number());
+            } else {
+                throw error(std::string("invalid conversion '%") + c + "' to 'format'");
+            }
+            out += buf;
+        }
+        return value{out};
+    });
+    globals_->set(value{"string"}, value{strlib});
     globals_->set(value{"print"}, value{std::make_shared<builtin>(builtin{"print", [](const std::vector<value>& a) {
                                            std::string line;
                                            for (std::size_t k = 0; k < a.size(); k++)

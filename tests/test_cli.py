@@ -195,6 +195,22 @@ def test_lua_subset_functions(lua_eval):
     assert all(out["result.shapes[%d].boundary_condition" % i][1] == "dirichlet" for i in (1, 2, 3))
 
 
+def test_lua_subset_base_functions(lua_eval):
+    rc, out = lua_eval('local n = 33\n'
+                       'result = {dir = string.format("io_%03d_%s_%.3f", n, "heat", 0.5), t = type(3), '
+                       'ts = tostring(2.5), tn = tonumber("1e-3"), bad = tonumber("abc"), '
+                       'pct = string.format("%d%%", 7), e = string.format("%.2e", 12345.678), '
+                       'tt = type({}), tf = type(print)}')
+    assert rc == 0, out
+    assert out["result.dir"] == ["string", "io_033_heat_0.500"]
+    assert out["result.t"] == ["string", "number"] and out["result.ts"] == ["string", "2.5"]
+    assert _num(out, "result.tn") == 1e-3 and "result.bad" not in out
+    assert out["result.pct"] == ["string", "7%"] and out["result.e"] == ["string", "1.23e+04"]
+    assert out["result.tt"] == ["string", "table"] and out["result.tf"] == ["string", "function"]
+    rc, out = lua_eval('x = string.format("%d")')
+    assert rc == 1 and "bad argument #2 to 'format'" in out["error"][0]
+
+
 def test_lua_subset_control_flow(lua_eval):
     rc, out = lua_eval(CONTROL)
     assert rc == 0, out
