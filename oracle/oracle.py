@@ -50,7 +50,7 @@ def lib():
                   "orc_block", "orc_csr", "orc_derivative", "orc_laplacian", "orc_gradient",
                   "orc_initialize", "orc_exact", "orc_heat_rhs", "orc_heat_rk4",
                   "orc_wave_rhs", "orc_wave_rk4", "orc_stats", "orc_error_field",
-                  "orc_set_gaussian", "orc_heat_euler", "orc_wave_euler"]:
+                  "orc_set_gaussian", "orc_heat_euler", "orc_wave_euler", "orc_block_layout"]:
             getattr(_lib, n).argtypes = None
     return _lib
 
@@ -148,6 +148,18 @@ class OracleProblem:
         lib().orc_csr(self._h, ctypes.c_int(d), ctypes.c_int(which), None,
                       u.ctypes.data_as(LP), v.ctypes.data_as(LP), _p(w))
         return rows.value, u, v, w
+
+    def block_layout(self, lines):
+        """metadata of hand-built line blocks: each line is (columns, row offset, column
+        offset, stride, (left rows, left columns), interior rows, stencil width,
+        (right rows, right columns))"""
+        spec = np.zeros((len(lines), 10), dtype=np.int64)
+        for i, (cols, ro, co, st, (lr, lc), ni, w, (rr, rc)) in enumerate(lines):
+            spec[i] = (cols, ro, co, st, lr, lc, ni, w, rr, rc)
+        meta = np.zeros((len(lines), 13), dtype=np.int32)
+        lib().orc_block_layout(ctypes.c_int(len(lines)), spec.ctypes.data_as(LP),
+                               meta.ctypes.data_as(IP))
+        return meta
 
     # ---- operators (numpy float64 arrays) ----
     def zeros(self):

@@ -1184,6 +1184,32 @@ struct block {
     std::vector<inner_block_meta> meta;
     std::vector<real> coeffs;
 
+    // one line's block: inner_block ctor (src/matrices/inner_block.cpp:73-96) and its
+    // entry in block::build_device_arrays (src/matrices/block.hpp:30-94)
+    void append_line(integer columns, integer row_offset, integer col_offset, integer stride,
+                     const dense& L, integer n_interior, const std::vector<real>& interior,
+                     const dense& R)
+    {
+        inner_block_meta mt{};
+        mt.row_offset = (int)row_offset;
+        mt.col_offset = (int)col_offset;
+        mt.stride = (int)stride;
+        mt.left_rows = (int)L.rows;
+        mt.left_cols = (int)L.cols;
+        mt.left_coeff_offset = (int)coeffs.size();
+        coeffs.insert(coeffs.end(), L.v.begin(), L.v.end());
+        mt.interior_rows = (int)n_interior;
+        mt.interior_coeff_offset = (int)coeffs.size();
+        mt.stencil_width = (int)interior.size();
+        coeffs.insert(coeffs.end(), interior.begin(), interior.end());
+        mt.right_rows = (int)R.rows;
+        mt.right_cols = (int)R.cols;
+        mt.right_coeff_offset = (int)coeffs.size();
+        mt.right_col_offset = (int)(col_offset + stride * (columns - R.cols));
+        coeffs.insert(coeffs.end(), R.v.begin(), R.v.end());
+        meta.push_back(mt);
+    }
+
     // src/matrices/block.hpp:118-178 with the TeamPolicy flattened to one line per
     // iteration; each row's dot is a sequential j-loop starting from 0.
     template <bool PlusEq>
@@ -1333,27 +1359,8 @@ static void domain_discretization(int dir, const mesh& m, const stencil& st,
             }
         }
         const integer n_interior = sub.rows - leftMat.rows - rightMat.rows;
-
-        // inner_block ctor: src/matrices/inner_block.cpp:73-96;
-        // block::build_device_arrays: src/matrices/block.hpp:30-94
-        inner_block_meta mt{};
-        mt.row_offset = (int)sub.row_offset;
-        mt.col_offset = (int)sub.col_offset;
-        mt.stride = (int)stride;
-        mt.left_rows = (int)leftMat.rows;
-        mt.left_cols = (int)leftMat.cols;
-        mt.left_coeff_offset = (int)D.O.coeffs.size();
-        D.O.coeffs.insert(D.O.coeffs.end(), leftMat.v.begin(), leftMat.v.end());
-        mt.interior_rows = (int)n_interior;
-        mt.interior_coeff_offset = (int)D.O.coeffs.size();
-        mt.stencil_width = (int)interior.size();
-        D.O.coeffs.insert(D.O.coeffs.end(), interior.begin(), interior.end());
-        mt.right_rows = (int)rightMat.rows;
-        mt.right_cols = (int)rightMat.cols;
-        mt.right_coeff_offset = (int)D.O.coeffs.size();
-        mt.right_col_offset = (int)(sub.col_offset + stride * (sub.columns - rightMat.cols));
-        D.O.coeffs.insert(D.O.coeffs.end(), rightMat.v.begin(), rightMat.v.end());
-        D.O.meta.push_back(mt);
+        D.O.append_line(sub.columns, sub.row_offset, sub.col_offset, stride, leftMat,
+                        n_interior, interior, rightMat);
     }
     D.B = B_builder.to_csr(m.size());
     D.N = N_builder.to_csr(m.size());
@@ -1981,6 +1988,22 @@ long orc_block(orc_problem* o, int dir, int* meta, double* coeffs, long* ncoeffs
     if (coeffs) std::copy(O.coeffs.begin(), O.coeffs.end(), coeffs);
     if (ncoeffs) *ncoeffs = (long)O.coeffs.size();
     return (long)O.meta.size();
+}
+
+// block layout of hand-built lines (the known-answer cases of src/matrices/block.t.cpp):
+// 9 longs per line: columns, row offset, column offset, stride, left rows, left columns,
+// interior rows, stencil width, right rows, right columns (coefficients are zeros); writes
+// 13 ints of metadata per line
+void orc_block_layout(int nlines, const long* spec, int* meta)
+{
+    block O;
+    for (int l = 0; l < nlines; l++) {
+        const long* q = spec + 10 * l;
+        dense L{q[4], q[5], std::vector<real>(q[4] * q[5], 0.0)};
+        dense R{q[8], q[9], std::vector<real>(q[8] * q[9], 0.0)};
+        O.append_line(q[0], q[1], q[2], q[3], L, q[6], std::vector<real>(q[7], 0.0), R);
+    }
+    std::memcpy(meta, O.meta.data(), O.meta.size() * sizeof(inner_block_meta));
 }
 
 // which: 0 B, 1 N, 2+r Bf[r], 5+r Br[r]; returns nnz, fills rows+1 offsets, cols, vals

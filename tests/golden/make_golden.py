@@ -5,11 +5,16 @@ Sources:
   * src/mesh/object_geometry.t.cpp:11-330 ("sphere intersections"): expected cut-point
     positions, solid coordinates and psi per axis, parsed from the reference test file as
     text -> object_geometry_sphere.json
-  * oracle/_ref/libshoccs_ref.so: the reference's own src/stencils/{E2_2,E4_2,E4_1}.cpp and
-    src/mesh/sphere.cpp compiled unmodified by oracle/build_ref.sh -> stencils_ref.json
-    (closure blocks, interior rows, interpolants) and sphere_hits_ref.json (ray/sphere hits)
+  * oracle/_ref/libshoccs_ref.so: the reference's own code compiled unmodified by
+    oracle/build_ref.sh -> stencils_ref.json (closure blocks, interior rows, interpolants of
+    src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp), sphere_hits_ref.json (src/mesh/sphere.cpp ray /
+    sphere hits) and reference_pins.json (SHA-256 digests of the arrays of
+    tests/golden/pins.py -- setup, operators, heat and scalar-wave systems -- on every case
+    of tests/cases.py)
 
 Usage: python tests/golden/make_golden.py [reference_root]
+(the reference root defaults to SHOCCS_REFERENCE_ROOT, else the directory `reference` beside
+this repository)
 """
 import ctypes
 import json
@@ -22,8 +27,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SHOCCS_REFERENCE_ROOT",
-                                                             "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(
+    "SHOCCS_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference"))
+sys.path.insert(0, REPO)
 
 
 def parse_sphere_intersections():
@@ -53,7 +59,8 @@ def parse_sphere_intersections():
 
 
 def ref_fixtures():
-    subprocess.check_call([os.path.join(REPO, "oracle", "build_ref.sh")])
+    subprocess.check_call(["sh", os.path.join(REPO, "oracle", "build_ref.sh")],
+                          env=dict(os.environ, SHOCCS_REFERENCE_ROOT=REF))
     lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libshoccs_ref.so"))
     D = ctypes.c_double
     alpha = (D * 2)(0.1, 0.7)
@@ -117,6 +124,41 @@ def ref_fixtures():
             dict(source="src/mesh/sphere.cpp via oracle/_ref", hits=hits))
 
 
+def reference_pins():
+    """digests (plus size and max |value|) of the arrays of tests/golden/pins.py computed by
+    the reference's own code"""
+    from oracle import reference as ref
+    from tests.cases import cases
+    from tests.golden import pins
+
+    def summary(arrays):
+        out = {}
+        for k, a in arrays.items():
+            v = np.asarray(a)
+            out[k] = dict(sha256=pins.digest(v), n=int(v.size),
+                          maxabs=float(np.abs(v.astype(np.float64)).max(initial=0.0)))
+        return out
+
+    C = cases()
+    res = {}
+    for name in sorted(C):
+        c = C[name]
+        r = ref.RefProblem(**c)
+        e = dict(setup=summary(pins.setup_arrays(r)), operators=summary(pins.operator_arrays(r, name)))
+        if c["scheme"] in pins.HEAT_SCHEMES:
+            s = ref.RefSystem("heat", **c, diffusivity=pins.KAPPA, sol_kind=1, sol=(pins.SINSIN_K,))
+            e["heat"] = summary(pins.system_arrays(s, name, pins.heat_steps(c), pins.heat_dt(c),
+                                                   s.update_boundary))
+        if name in pins.WAVE_CASES:
+            cen, rad = pins.wave_center(c, name)
+            s = ref.RefSystem("wave", **c, center=cen, radius=rad)
+            e["wave"] = summary(pins.system_arrays(s, name, 3, pins.wave_dt(c), s.update_boundary))
+        res[name] = e
+    return dict(source="the reference's code compiled unmodified into oracle/_ref "
+                       "(oracle/build_ref.sh); arrays of tests/golden/pins.py",
+                kappa=pins.KAPPA, sinsin_k=pins.SINSIN_K, cases=res)
+
+
 if __name__ == "__main__":
     with open(os.path.join(HERE, "object_geometry_sphere.json"), "w") as f:
         json.dump(parse_sphere_intersections(), f, indent=1)
@@ -125,4 +167,6 @@ if __name__ == "__main__":
         json.dump(st, f)
     with open(os.path.join(HERE, "sphere_hits_ref.json"), "w") as f:
         json.dump(hits, f)
+    with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
+        json.dump(reference_pins(), f, indent=0, sort_keys=True)
     print("wrote fixtures to", HERE)
