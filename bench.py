@@ -8,9 +8,10 @@ dt = 0.5 h, 1000 RK4 steps.
 
 One benchmark "step" is one full solve of that workload (initial condition + 1000 RK4
 steps).  value = RK4 DOF-updates/s = nx*ny*nz * 1000 * K / time of the mixed-precision
-path (FP32 stage fields and interior stencils, FP64 closure rows, compensated FP32-pair
-solution/accumulator), with every buffer resident in HBM (the working set, ~470 MB, is
-larger than the 129 MB L2).  The FP64 path is timed beside it; both report their max-norm
+path (FP32 stage fields; interior and domain-wall rows in FP32 in difference form; cut-cell
+rows from FP32-pair coefficients with compensated FP32 products and sums, ~44 bits; FP32
+stage accumulator; compensated FP32-pair solution), with every buffer resident in HBM (the
+working set, ~470 MB, is larger than the 129 MB L2).  The FP64 path is timed beside it; both report their max-norm
 error against the exact solution.  e2e repeats the mixed solve through the C ABI with the
 initial state copied from pinned host memory and the final state copied back inside the
 timed region.
@@ -19,9 +20,11 @@ The reference's E4_1 closures are unstable under explicit RK4 on this geometry (
 evaluated at psi = 1, which its psi clamp turns into ~1e5/h coefficients, and small cut
 cells give large ones), so the workload's solution overflows within a few dozen steps in
 the reference algorithm and here alike; kernel time does not depend on the values.  The
-mixed-versus-FP64 equal-accuracy criterion is therefore measured on a stable companion on
-the same 256^3 grid and kernels: the same pulse and velocity with the reference's E4u_1
-scheme and no embedded sphere, 300 RK4 steps.
+mixed-versus-FP64 equal-accuracy criterion is therefore measured on two stable companions
+on the same 256^3 grid: the same pulse and velocity with the reference's E4u_1 scheme and no
+embedded sphere, 300 RK4 steps; and the heat equation around a Dirichlet sphere with E4_2
+cut-cell rows (the reference's heat system), manufactured solution sin 2 pi x sin 2 pi y
+sin 2 pi z e^-t, dt = 0.1 h^2, 200 RK4 steps, both precisions timed.
 
 --impl reference times the reference algorithm's CPU path (the oracle restatement of
 pbrady/shoccs, OpenMP over all host cores) on the same workload, one RK4 step per
@@ -53,6 +56,12 @@ ACC_CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1), spheres=
                          "floating"),
                 scheme="E4u_1", alpha=(-0.7733323791884821, 0.1623961700641681))
 ACC_STEPS = 300
+# the cut-cell equal-accuracy companion: heat, E4_2, Dirichlet walls and sphere (off the grid
+# points), sin-sin-sin e^-t, dt = 0.1 h^2
+HEAT_ACC_CASE = dict(n=(N_GRID, N_GRID, N_GRID), lo=(0, 0, 0), hi=(1, 1, 1),
+                     spheres=[((0.51, 0.49, 0.503), 0.3, "dirichlet")],
+                     grid_bc=("dirichlet",) * 6, scheme="E4_2")
+HEAT_ACC_STEPS = 200
 # algorithmic HBM bytes per grid point per RK4 step (u0, accumulator, stage field each read
 # and written once per stage): FP64 (8-byte everything) 8+8+8 | 24+16 | 24+16 | 24+8 = 136;
 # mixed (4-byte stage field and accumulator, 8-byte compensated u0 of which stages 0-2 read
@@ -501,6 +510,40 @@ def adjoint_bench(stream, n=128, steps=200, every=20, ndir=32, eps=1e-6, cg_iter
                           "u0_rel_error": float(torch.linalg.norm((x - u_true) * fluid)) / err0}}
 
 
+def heat_sphere_accuracy(stream, steps=HEAT_ACC_STEPS):
+    """Mixed against FP64 where cut cells exist: the heat equation on 256^3 around a
+    Dirichlet sphere (E4_2 cut-cell rows), each precision timed over `steps` RK4 steps with
+    CUDA events on the launching stream after one warm-up solve; max-norm errors against the
+    exact solution at the end."""
+    import torch
+    import shoccs_gb300 as S
+    p = S.Problem(**HEAT_ACC_CASE)
+    h = 1.0 / (N_GRID - 1)
+    dt = 0.1 * h * h
+    out = {"case": "256^3 heat, E4_2, Dirichlet sphere r = 0.3, sin-sin-sin e^-t, "
+                   "dt = 0.1 h^2, %d RK4 steps" % steps, "cut_points": int(sum(p.nR))}
+    for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+        hs = S.Heat(p, 1.0, prec, S.SOL_SINSIN, [1.0])
+        hs.initialize(0.0, stream)
+        hs.rk4(0.0, dt, 4, stream)
+        hs.initialize(0.0, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        hs.rk4(0.0, dt, steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        st, ok = hs.stats(steps * dt, stream)
+        out[name] = {"max_error": st[0], "valid": bool(ok), "ms_per_step": ms / steps,
+                     "dof_updates_per_s": p.size * steps / (ms * 1e-3),
+                     "stage_kernel": hs.stage_kernel}
+        del hs
+    out["error_ratio_mixed_vs_fp64"] = out["mixed"]["max_error"] / out["fp64"]["max_error"]
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["dof_updates_per_s"] / out["fp64"]["dof_updates_per_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -657,6 +700,7 @@ def main():
     acc["error_ratio_mixed_vs_fp64"] = acc["mixed"]["max_error"] / acc["fp64"]["max_error"]
     acc["case"] = "256^3, E4u_1 (alpha -0.7733, 0.1624), no sphere, %d RK4 steps" % ACC_STEPS
     del pa
+    acc_cc = heat_sphere_accuracy(stream)
 
     # ---- e2e through the C ABI with host buffers ----
     host_in = [torch.empty(N, dtype=torch.float64).pin_memory()] + \
@@ -720,6 +764,7 @@ def main():
                  "valid": bool(valid_d)},
         "mixed": {"workload_error": stats_m[0], "valid": bool(valid_m)},
         "equal_accuracy": acc,
+        "equal_accuracy_cut_cells": acc_cc,
         "speedup_mixed_vs_fp64": value / value64,
     }
     del sysm, sysd, p
@@ -739,6 +784,19 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb, _, _ = cpu_rate(8, 15.0)
         line["cpu_baseline"] = cb
+    # the figures the metric names, repeated at the end of the line (a reader that keeps only
+    # the line's tail still has them)
+    summ = {"value": value, "e2e": e2e, "roofline_frac": achieved / peak,
+            "fp64_value": value64, "speedup_mixed_vs_fp64": value / value64,
+            "equal_accuracy_ratio_e4u_box": acc["error_ratio_mixed_vs_fp64"],
+            "equal_accuracy_ratio_heat_sphere": acc_cc["error_ratio_mixed_vs_fp64"],
+            "heat_sphere_speedup_mixed_vs_fp64": acc_cc["speedup_mixed_vs_fp64"]}
+    if "batched" in line:
+        summ["batched_mixed_dof_updates_per_s"] = line["batched"]["mixed"]["dof_updates_per_s"]
+    if "adjoint" in line:
+        summ["adjoint_backward_over_forward"] = line["adjoint"]["backward_over_forward"]
+        summ["adjoint_mixed_backward_over_forward"] = line["adjoint"]["mixed"]["backward_over_forward"]
+    line["summary"] = summ
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:

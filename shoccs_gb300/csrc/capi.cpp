@@ -175,6 +175,12 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
         A.antisym = T.width == 5 && T.interior[2] == 0.0 && T.interior[0] == -T.interior[4] &&
                     T.interior[1] == -T.interior[3];
         if (!T.active) continue;
+        // the FP32 kernels evaluate a non-antisymmetric interior as a symmetric
+        // zero-sum second-derivative row in difference form (sym5 / sym3)
+        if (!A.antisym && !(T.width == 5 ? T.interior[0] == T.interior[4] &&
+                                                T.interior[1] == T.interior[3]
+                                          : T.width == 3 && T.interior[0] == T.interior[2]))
+            return fail(SHOCCS_EINVAL, "interior stencil neither symmetric nor antisymmetric");
         SH_CUDA(p->mem.put(T.rows, &A.rows, s));
         SH_CUDA(p->mem.put(T.row_out, (const long long**)&A.row_out, s));
         SH_CUDA(p->mem.put(T.coef, &A.coef, s));

@@ -35,6 +35,7 @@ struct WallBlock {
     double c[5 * 7];
     double n[5];
     float cf[5 * 7];
+    float sf[5]; // row sums of c, rounded to FP32 (zero up to rounding; difference form)
 };
 enum : unsigned { CLS_DIRFACE = 0x40, CLS_FLUID = 0x80 };
 

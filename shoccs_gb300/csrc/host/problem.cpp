@@ -707,11 +707,18 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
             W.first_row = wall_first[side];
             W.col0 = wall_col0[side];
             if (W.rows > 5 || W.cols > 7) throw std::runtime_error("wall block exceeds 5 x 7");
-            for (int r = 0; r < W.rows; r++)
+            for (int r = 0; r < W.rows; r++) {
+                real sum = 0.0;
                 for (int j = 0; j < W.cols; j++) {
                     W.c[r * 7 + j] = wall_rows[side][r][j];
                     W.cf[r * 7 + j] = (float)wall_rows[side][r][j];
+                    sum += wall_rows[side][r][j];
                 }
+                const int self = W.first_row + r - W.col0;
+                if (self < 0 || self >= W.cols)
+                    throw std::runtime_error("wall closure row without its own point as a column");
+                W.sf[r] = (float)sum;
+            }
         }
         std::sort(pend.begin(), pend.end(),
                   [](const Pending& a, const Pending& b) { return a.out < b.out; });

@@ -173,6 +173,29 @@ __device__ __forceinline__ double interior64(const DevAxis& A, TIN u, long long 
     return fma(A.ic[2], ldd(u, p + s), r);
 }
 
+// ---- FP32 rows in difference form (mixed path) -------------------------------------------
+// Every row of a derivative operator sums to zero (the derivative of a constant vanishes), so
+// sum_j c_j x_j = sum_j c_j (x_j - x_s) + x_s sum_j c_j for any x_s.  With x_s the row's own
+// point, the differences of neighbouring values are exact or nearly so in FP32 (Sterbenz),
+// and the row's rounding error is relative to its result instead of to the cancelling
+// products c_j x_j ~ |u| / h^2 (at h = 1/128 that is the difference between 6e-8 |Lu| and
+// 1e-3 absolute); the FP32 rounding of the coefficients cancels the same way.  The
+// symmetric second-derivative interiors (E2_2, E4_2: a0 = -2 (a1 + a2)) take
+// a1 ((m1 - c0) + (p1 - c0)) + a2 ((m2 - c0) + (p2 - c0)); the antisymmetric first-derivative
+// interiors are already differences.  Roundings are explicit, so every kernel that calls
+// these helpers gets the same bits.
+__device__ __forceinline__ float sym5(float a1, float a2, float m2, float m1, float c0, float p1,
+                                      float p2)
+{
+    const float d1 = __fadd_rn(__fsub_rn(m1, c0), __fsub_rn(p1, c0));
+    const float d2 = __fadd_rn(__fsub_rn(m2, c0), __fsub_rn(p2, c0));
+    return fmaf(a1, d1, __fmul_rn(a2, d2));
+}
+__device__ __forceinline__ float sym3(float a1, float m1, float c0, float p1)
+{
+    return __fmul_rn(a1, __fadd_rn(__fsub_rn(m1, c0), __fsub_rn(p1, c0)));
+}
+
 template <class TIN>
 __device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p)
 {
@@ -183,15 +206,10 @@ __device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p
             const float d2 = ldf(u, p + 2 * s) - ldf(u, p - 2 * s);
             return fmaf(A.icf[3], d1, A.icf[4] * d2);
         }
-        float r = A.icf[0] * ldf(u, p - 2 * s);
-        r = fmaf(A.icf[1], ldf(u, p - s), r);
-        r = fmaf(A.icf[2], ldf(u, p), r);
-        r = fmaf(A.icf[3], ldf(u, p + s), r);
-        return fmaf(A.icf[4], ldf(u, p + 2 * s), r);
+        return sym5(A.icf[1], A.icf[0], ldf(u, p - 2 * s), ldf(u, p - s), ldf(u, p),
+                    ldf(u, p + s), ldf(u, p + 2 * s));
     }
-    float r = A.icf[0] * ldf(u, p - s);
-    r = fmaf(A.icf[1], ldf(u, p), r);
-    return fmaf(A.icf[2], ldf(u, p + s), r);
+    return sym3(A.icf[0], ldf(u, p - s), ldf(u, p), ldf(u, p + s));
 }
 
 // ---- closure rows (always FP64) ----------------------------------------------------------
@@ -321,6 +339,23 @@ __device__ __forceinline__ double wall64(const DevAxis& A, long long p, int coor
     return v;
 }
 
+// row r of a wall block over its columns x[0 .. cols-1] in difference form (see sym5):
+// S_r x_s + sum_j c_j (x_j - x_s), x_s the row's own point (column first_row + r - col0),
+// S_r the row sum of the FP64 coefficients rounded to FP32 (zero up to rounding)
+__device__ __forceinline__ float wall_row_diff(const WallBlock& W, int r, const float (&x)[7])
+{
+    const int self = W.first_row + r - W.col0;
+    float xs = 0.f;
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j == self) xs = x[j];
+    float s = __fmul_rn(W.sf[r], xs);
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j < W.cols) s = fmaf(W.cf[r * 7 + j], __fsub_rn(x[j], xs), s);
+    return s;
+}
+
 template <class TIN>
 __device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord, TIN u)
 {
@@ -330,11 +365,7 @@ __device__ __forceinline__ float wall32(const DevAxis& A, long long p, int coord
     float x[7]; // a wall block has at most 7 columns; all loads issued before the first use
 #pragma unroll
     for (int j = 0; j < 7; ++j) x[j] = j < W.cols ? ldf(u, q + j * A.stride) : 0.f;
-    float s = 0.f;
-#pragma unroll
-    for (int j = 0; j < 7; ++j)
-        if (j < W.cols) s = fmaf(W.cf[r * 7 + j], x[j], s);
-    return s;
+    return wall_row_diff(W, r, x);
 }
 
 // the Neumann term of a wall row (FP64 data, FP64 product) added to an FP32 row value
@@ -750,28 +781,25 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
             for (int m = 0; m < 16; m++) w[m] = 0.f;
             {
                 const WallBlock& W = A.wall[0]; // columns 0 .. cols-1
+                const float x[7] = {xl[0], xl[1], xl[2], xl[3], xl[4], xl[5], xl[6]};
 #pragma unroll
-                for (int r = 0; r < 6; r++) {
-                    if (r >= W.rows) continue;
-                    float acc = 0.f; // wall32's operation order
-#pragma unroll
-                    for (int jj = 0; jj < 7; jj++)
-                        if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], xl[jj], acc);
-                    w[r] = acc;
-                }
+                for (int r = 0; r < 6; r++)
+                    if (r < W.rows) w[r] = wall_row_diff(W, r, x); // wall32's arithmetic
             }
             {
-                const WallBlock& W = A.wall[1]; // columns nz-cols .. nz-1
+                const WallBlock& W = A.wall[1]; // columns nz-cols .. nz-1: xr[8-cols ..]
                 const int sh = 8 - W.cols;
+                float x[7];
 #pragma unroll
-                for (int r = 0; r < 6; r++) {
-                    if (r >= W.rows) continue;
-                    float acc = 0.f;
+                for (int jj = 0; jj < 7; jj++) {
+                    x[jj] = 0.f;
 #pragma unroll
                     for (int m = 1; m < 8; m++)
-                        if (m >= sh) acc = fmaf(W.cf[r * 7 + m - sh], xr[m], acc);
-                    w[8 + r] = acc;
+                        if (m == sh + jj) x[jj] = xr[m];
                 }
+#pragma unroll
+                for (int r = 0; r < 6; r++)
+                    if (r < W.rows) w[8 + r] = wall_row_diff(W, r, x);
             }
             auto pick = [stage](const float4& f) {
                 return stage < 2 ? make_float2(f.x, 0.f)
@@ -860,15 +888,9 @@ __device__ __forceinline__ float interior_f(const DevAxis& A, const float* u, ID
             const float d2 = L(p + 2 * s) - L(p - 2 * s);
             return fmaf(A.icf[3], d1, A.icf[4] * d2);
         }
-        float r = A.icf[0] * L(p - 2 * s);
-        r = fmaf(A.icf[1], L(p - s), r);
-        r = fmaf(A.icf[2], L(p), r);
-        r = fmaf(A.icf[3], L(p + s), r);
-        return fmaf(A.icf[4], L(p + 2 * s), r);
+        return sym5(A.icf[1], A.icf[0], L(p - 2 * s), L(p - s), L(p), L(p + s), L(p + 2 * s));
     }
-    float r = A.icf[0] * L(p - s);
-    r = fmaf(A.icf[1], L(p), r);
-    return fmaf(A.icf[2], L(p + s), r);
+    return sym3(A.icf[0], L(p - s), L(p), L(p + s));
 }
 
 template <class IDX>
@@ -1111,15 +1133,9 @@ __device__ __forceinline__ float interior_row(const DevAxis& A, float m2, float 
 {
     if (A.width == 5) {
         if (A.antisym) return fmaf(A.icf[3], p1 - m1, A.icf[4] * (p2 - m2));
-        float r = A.icf[0] * m2;
-        r = fmaf(A.icf[1], m1, r);
-        r = fmaf(A.icf[2], c0, r);
-        r = fmaf(A.icf[3], p1, r);
-        return fmaf(A.icf[4], p2, r);
+        return sym5(A.icf[1], A.icf[0], m2, m1, c0, p1, p2);
     }
-    float r = A.icf[0] * m1;
-    r = fmaf(A.icf[1], c0, r);
-    return fmaf(A.icf[2], p1, r);
+    return sym3(A.icf[0], m1, c0, p1);
 }
 
 // ---- column-blocked mixed stage (3-D grids) ------------------------------------------------
@@ -1314,15 +1330,9 @@ __device__ __forceinline__ float interior_row_t(const DevAxis& A, float m2, floa
     if constexpr (FORM == FORM_ANTI5) {
         return fmaf(A.icf[3], p1 - m1, A.icf[4] * (p2 - m2));
     } else if constexpr (FORM == FORM_SYM5) {
-        float r = A.icf[0] * m2;
-        r = fmaf(A.icf[1], m1, r);
-        r = fmaf(A.icf[2], c0, r);
-        r = fmaf(A.icf[3], p1, r);
-        return fmaf(A.icf[4], p2, r);
+        return sym5(A.icf[1], A.icf[0], m2, m1, c0, p1, p2);
     } else if constexpr (FORM == FORM_W3) {
-        float r = A.icf[0] * m1;
-        r = fmaf(A.icf[1], c0, r);
-        return fmaf(A.icf[2], p1, r);
+        return sym3(A.icf[0], m1, c0, p1);
     } else {
         return interior_row(A, m2, m1, c0, p1, p2);
     }
@@ -1439,7 +1449,12 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
             const int r = coord - W.first_row;
             const int stride = d == 0 ? plane : nz;
             const int q0 = p + (W.col0 - coord) * stride;
-            float sw[4] = {0.f, 0.f, 0.f, 0.f};
+            // wall_row_diff's arithmetic: the points' own values (the row's column
+            // first_row + r - col0) are the differences' reference
+            const float4 xs = ld4(in, p);
+            float sw[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) sw[q] = __fmul_rn(W.sf[r], f4(xs, q));
 #pragma unroll
             for (int g = 0; g < 2; g++) {
                 float4 xw[4];
@@ -1453,7 +1468,8 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
                     const int col = 4 * g + jj;
                     if (col < W.cols)
 #pragma unroll
-                        for (int q = 0; q < 4; q++) sw[q] = fmaf(W.cf[r * 7 + col], f4(xw[jj], q), sw[q]);
+                        for (int q = 0; q < 4; q++)
+                            sw[q] = fmaf(W.cf[r * 7 + col], __fsub_rn(f4(xw[jj], q), f4(xs, q)), sw[q]);
                 }
             }
 #pragma unroll
@@ -1746,11 +1762,7 @@ __global__ void __launch_bounds__(288) k_stage_mixed_tma(const __grid_constant__
                     if (A.antisym) {
                         v = fmaf(A.icf[3], xp1 - xm1, A.icf[4] * (xp2 - xm2));
                     } else {
-                        float t = A.icf[0] * xm2;
-                        t = fmaf(A.icf[1], xm1, t);
-                        t = fmaf(A.icf[2], x0v, t);
-                        t = fmaf(A.icf[3], xp1, t);
-                        v = fmaf(A.icf[4], xp2, t);
+                        v = sym5(A.icf[1], A.icf[0], xm2, xm1, x0v, xp1, xp2);
                     }
                 } else {
                     const long long chunk = (long long)i * ny * op.nzc + chunk0;
@@ -2077,10 +2089,7 @@ __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
 #pragma unroll
         for (int r = 0; r < 6; r++) {
             if (r >= W.rows) continue;
-            float acc = 0.f;
-#pragma unroll
-            for (int jj = 0; jj < 7; jj++)
-                if (jj < W.cols) acc = fmaf(W.cf[r * 7 + jj], x[jj], acc);
+            float acc = wall_row_diff(W, r, x); // wall32's arithmetic
             if (W.has_n && nu) acc = (float)fma(W.n[r], __ldg(nu + base + W.wall), (double)acc);
             w[side * 8 + r] = acc;
         }
