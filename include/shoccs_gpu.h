@@ -216,9 +216,12 @@ shoccs_status shoccs_system_error_field(shoccs_system* s, double t, shoccs_field
  * 65536 tiles of 256 grid points (16.7 M points, 2 MB), which every GPU that loads the
  * library keeps until the process exits.  Larger grids are rejected with SHOCCS_EINVAL.
  * The first call on a device looks up the array's device address (with that device
- * current), so make that first call before any stream capture.  All calls share the array
- * and it keeps the last call's contents (each call writes every slot it reads); calls that
- * overlap on the GPU race on it.  Results equal shoccs_system_stats. */
+ * current), so make that first call before any stream capture.  The address is kept per
+ * device for the life of the process: it assumes the device's primary context is not reset
+ * (cudaDeviceReset) in between.  Every call copies the eleven statistics to `out` and
+ * synchronizes `stream` before it returns.  All calls share the array and it keeps the last
+ * call's contents (each call writes every slot it reads); calls that overlap on the GPU race
+ * on it.  Results equal shoccs_system_stats. */
 shoccs_status shoccs_system_stats_noalloc(shoccs_system* s, double t, double out[11],
                                           void* stream);
 /* dt from the CFL number: heat p*h_min^2/(4k), wave c*h_min */

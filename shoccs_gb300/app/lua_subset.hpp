@@ -506,9 +506,16 @@ struct state::parser {
             ++p; // if / elseif / else
             bool take = false;
             if (!is_else) {
-                const value c = expr();
-                expect_kw("then");
-                take = !done && c.truthy();
+                // after a taken branch the remaining conditions are not evaluated (Lua runs
+                // none of their calls or indexing)
+                if (done) {
+                    skip_expr();
+                    expect_kw("then");
+                } else {
+                    const value c = expr();
+                    expect_kw("then");
+                    take = c.truthy();
+                }
             } else {
                 take = !done;
             }
@@ -834,12 +841,95 @@ struct state::parser {
             if (op.empty() || prec_left(op) <= limit) return lhs;
             ++p;
             if (op == "and" || op == "or") {
-                value rhs = expr(prec_right(op));
-                lhs = op == "and" ? (lhs.truthy() ? rhs : lhs) : (lhs.truthy() ? lhs : rhs);
+                // short circuit: when the left operand decides the result (false or nil for
+                // `and`, anything else for `or`) the right one is parsed but not evaluated
+                if (op == "and" ? !lhs.truthy() : lhs.truthy()) skip_expr(prec_right(op));
+                else lhs = expr(prec_right(op));
                 continue;
             }
             value rhs = expr(prec_right(op));
             lhs = arith(op, lhs, rhs);
+        }
+    }
+
+    // ---- skipping an expression without evaluating it (short-circuit operands, the
+    // conditions after a taken branch): the same grammar as expr(), tokens only ----
+    void skip_balanced(const char* open, const char* close)
+    {
+        int nest = 0;
+        do {
+            if (cur().kind == tk::eof) fail(std::string("'") + close + "' expected");
+            if (is_op(open)) ++nest;
+            else if (is_op(close)) --nest;
+            ++p;
+        } while (nest > 0);
+    }
+    void skip_function_literal()
+    {
+        const int line = cur().line;
+        ++p; // function
+        skip_balanced("(", ")");
+        int nest = 1;
+        while (nest > 0) {
+            if (cur().kind == tk::eof) fail("'end' expected (to close function at line " + std::to_string(line) + ")");
+            if (cur().kind == tk::name) {
+                const std::string& w = cur().text;
+                if (w == "function" || w == "if" || w == "do" || w == "repeat") ++nest;
+                else if (w == "end" || w == "until") --nest;
+            }
+            ++p;
+        }
+    }
+    void skip_simple()
+    {
+        if (cur().kind == tk::number || cur().kind == tk::string || is_kw("nil") || is_kw("true") ||
+            is_kw("false") || is_op("...")) {
+            ++p;
+            return;
+        }
+        if (is_kw("function")) {
+            skip_function_literal();
+            return;
+        }
+        if (is_op("{")) {
+            skip_balanced("{", "}");
+            return;
+        }
+        if (is_op("(")) {
+            skip_balanced("(", ")");
+        } else {
+            name();
+        }
+        for (;;) { // suffixes: fields, indexing, calls
+            if (is_op(".") || is_op(":")) {
+                ++p;
+                name();
+            } else if (is_op("[")) {
+                skip_balanced("[", "]");
+            } else if (is_op("(")) {
+                skip_balanced("(", ")");
+            } else if (is_op("{")) {
+                skip_balanced("{", "}");
+            } else if (cur().kind == tk::string) {
+                ++p;
+            } else {
+                return;
+            }
+        }
+    }
+    void skip_expr(int limit = 0)
+    {
+        if (is_kw("not") || is_op("-") || is_op("#")) {
+            ++p;
+            skip_expr(12);
+        } else {
+            skip_simple();
+        }
+        for (;;) {
+            const std::string op = binop();
+            if (op.empty() || prec_left(op) <= limit) return;
+            ++p;
+            skip_expr(prec_right(op));
         }
     }
 
@@ -1120,11 +1210,18 @@ inline state::state()
         if (a.empty()) throw error("value expected");
         if (a[0].number()) return a[0];
         if (auto str = a[0].string()) {
-            char* end = nullptr;
-            const double d = std::strtod(str->c_str(), &end);
-            if (end && end != str->c_str()) {
-                while (*end == ' ') ++end;
-                if (*end == '\0') return value{d};
+            // a decimal or hexadecimal numeral with optional surrounding white space; Lua's
+            // tonumber has no inf or nan numerals
+            const char* b = str->c_str();
+            while (std::isspace((unsigned char)*b)) ++b;
+            const char* q = (*b == '+' || *b == '-') ? b + 1 : b;
+            if (std::isdigit((unsigned char)*q) || (*q == '.' && std::isdigit((unsigned char)q[1]))) {
+                char* end = nullptr;
+                const double d = std::strtod(b, &end);
+                if (end && end != b) {
+                    while (std::isspace((unsigned char)*end)) ++end;
+                    if (*end == '\0') return value{d};
+                }
             }
         }
         return value{};
@@ -1151,16 +1248,29 @@ inline state::state()
             const char c = f[i];
             if (arg >= a.size()) throw error("bad argument #" + std::to_string(arg + 1) + " to 'format' (no value)");
             const value& v = a[arg++];
-            char buf[512];
+            const std::string bad = "bad argument #" + std::to_string(arg) + " to 'format' ";
+            std::string buf;
+            auto put = [&](const std::string& fmt, auto x) {
+                const int n = std::snprintf(nullptr, 0, fmt.c_str(), x);
+                if (n < 0) throw error(bad + "(invalid conversion)");
+                buf.assign((std::size_t)n + 1, '\0');
+                std::snprintf(buf.data(), buf.size(), fmt.c_str(), x);
+                buf.resize((std::size_t)n);
+            };
             if (c == 's') {
                 const std::string str = to_display(v);
-                std::snprintf(buf, sizeof buf, (spec + "s").c_str(), str.c_str());
+                put(spec + "s", str.c_str());
             } else if (std::strchr("dicxXou", c)) {
-                if (!v.number()) throw error("number expected");
-                std::snprintf(buf, sizeof buf, (spec + "ll" + (c == 'i' ? 'd' : c)).c_str(), (long long)*v.number());
+                if (!v.number()) throw error(bad + "(number expected, got " + v.type_name() + ")");
+                const double x = *v.number();
+                // the integer conversions take numbers with an exact integer value in range
+                if (!(x == std::floor(x)) || !(x >= -9.223372036854775808e18 && x < 9.223372036854775808e18))
+                    throw error(bad + "(number has no integer representation)");
+                if (c == 'c') put(spec + "c", (int)(long long)x);
+                else put(spec + "ll" + (c == 'i' ? 'd' : c), (long long)x);
             } else if (std::strchr("eEfgGaA", c)) {
-                if (!v.number()) throw error("number expected");
-                std::snprintf(buf, sizeof buf, (spec + c).c_str(), *v.number());
+                if (!v.number()) throw error(bad + "(number expected, got " + v.type_name() + ")");
+                put(spec + c, *v.number());
             } else {
                 throw error(std::string("invalid conversion '%") + c + "' to 'format'");
             }

@@ -222,6 +222,52 @@ def test_lua_subset_control_flow(lua_eval):
     assert _num(out, "result.x") == 3 and _num(out, "result.y") == 1
 
 
+SHORT_CIRCUIT = r'''
+local t = nil
+calls = 0
+local function bump() calls = calls + 1 return true end
+local function fact(n) return n <= 1 and 1 or n * fact(n - 1) end
+local guard
+if t == nil then guard = "nil" elseif t.x > 0 then guard = "x" else guard = "other" end
+local second
+if false then second = 1 elseif true then second = 2 elseif bump() then second = 3 end
+result = {a = (t ~= nil and t.x) or 3, b = t and t.y, c = false or "c", d = t and t.x.y,
+          e = 1 or error_not_called(), fact = fact(6), guard = guard, second = second,
+          f = (1 > 2) and bump() or "f"}
+result.calls = calls
+'''
+
+
+def test_lua_subset_short_circuit(lua_eval):
+    """`and` / `or` evaluate their right operand only when the left one does not decide, and
+    the conditions after a taken branch of an if are not evaluated (Lua's semantics): nil
+    guards, the recursion idiom `n <= 1 and 1 or n * f(n - 1)`, and no side effects from the
+    skipped calls"""
+    rc, out = lua_eval(SHORT_CIRCUIT)
+    assert rc == 0, out
+    assert _num(out, "result.a") == 3 and "result.b" not in out and "result.d" not in out
+    assert out["result.c"] == ["string", "c"] and _num(out, "result.e") == 1
+    assert _num(out, "result.fact") == 720 and out["result.guard"] == ["string", "nil"]
+    assert _num(out, "result.second") == 2 and out["result.f"] == ["string", "f"]
+    assert _num(out, "result.calls") == 0
+
+
+def test_lua_subset_format_and_tonumber_edges(lua_eval):
+    rc, out = lua_eval('result = {c = string.format("%c%c", 72, 105), '
+                       'long = string.format("%s", string.format("%0700d", 1)), '
+                       'ws = tonumber(" 12\\t\\n"), hex = tonumber("0x10"), inf = tonumber("inf"), '
+                       'nan = tonumber("nan"), neg = tonumber("-2.5e1"), bad = tonumber("1 2")}')
+    assert rc == 0, out
+    assert out["result.c"] == ["string", "Hi"]
+    assert len(out["result.long"][1]) == 700 and out["result.long"][1].endswith("01")
+    assert _num(out, "result.ws") == 12 and _num(out, "result.hex") == 16
+    assert _num(out, "result.neg") == -25
+    assert "result.inf" not in out and "result.nan" not in out and "result.bad" not in out
+    for src in ('x = string.format("%d", 2.5)', 'x = string.format("%d", 1e300)'):
+        rc, out = lua_eval(src)
+        assert rc == 1 and "number has no integer representation" in out["error"][0], out
+
+
 @pytest.mark.parametrize("src,msg", [
     ("break", "break outside a loop"),
     ("for k, v in pairs({}) do end", "only numeric for loops are supported"),
