@@ -1348,50 +1348,59 @@ __device__ __forceinline__ float f4(const float4& v, int q)
     return q == 0 ? v.x : (q == 1 ? v.y : (q == 2 ? v.z : v.w));
 }
 
-template <int STAGE, int SYS, int FORM, int VK, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
+// the loads of one thread's four points of plane i (stage input at the point and its y / z
+// neighbours, class bytes, u0 hi word and accumulator); the x neighbours are the caller's
+struct VecLoads {
+    float4 C, ya, yb, yc, yd, zL, zR, uh, av;
+    unsigned c4;
+};
+
+// C: the stage input at the four points (loaded by the caller)
+template <int STAGE>
+__device__ __forceinline__ VecLoads vec_loads(const DevOp& op, const StageArgs& sa, const float* in,
+                                              int i, int j, int k, float4 C)
 {
-    // The stage input, u0 and the accumulator were complete before the cut-row kernel that
-    // precedes this one could let it start, so their loads go out before the dependent-launch
-    // wait; what that kernel writes (line records, cut-cell values) is read after it.
-    pdl_trigger();
-    const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
-    const int nx = op.it0, ny = op.it1, nz = op.it2;
-    const int lane = threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
-    if (j >= ny) return; // whole warp
-    const int i = blockIdx.z;
-    const int k = blockIdx.x * 128 + 4 * lane;
-    const bool kvalid = k < nz;
+    const int ny = op.it1, nz = op.it2;
     const int plane = ny * nz;
     const int kc = min(k, nz - 4);
     const int p = i * plane + j * nz + kc;
-    const int xm2 = (max(i - 2, 0) - i) * plane, xm1 = (max(i - 1, 0) - i) * plane;
-    const int xp1 = (min(i + 1, nx - 1) - i) * plane, xp2 = (min(i + 2, nx - 1) - i) * plane;
     const int ym2 = (max(j - 2, 0) - j) * nz, ym1 = (max(j - 1, 0) - j) * nz;
     const int yp1 = (min(j + 1, ny - 1) - j) * nz, yp2 = (min(j + 2, ny - 1) - j) * nz;
     const int zl = kc >= 4 ? -4 : 0, zr = kc + 8 <= nz ? 4 : 0;
-
-    const unsigned c4 = kvalid ? __ldg((const unsigned*)(op.cls + p)) : 0u;
-    const float4 C = ld4(in, p);
-    const float4 xa = ld4(in, p + xm2), xb = ld4(in, p + xm1), xc = ld4(in, p + xp1),
-                 xd = ld4(in, p + xp2);
-    const float4 ya = ld4(in, p + ym2), yb = ld4(in, p + ym1), yc = ld4(in, p + yp1),
-                 yd = ld4(in, p + yp2);
-    const float4 zL = ld4(in, p + zl), zR = ld4(in, p + zr);
+    VecLoads L;
+    L.c4 = k < nz ? __ldg((const unsigned*)(op.cls + p)) : 0u;
+    L.C = C;
+    L.ya = ld4(in, p + ym2);
+    L.yb = ld4(in, p + ym1);
+    L.yc = ld4(in, p + yp1);
+    L.yd = ld4(in, p + yp2);
+    L.zL = ld4(in, p + zl);
+    L.zR = ld4(in, p + zr);
     const float* __restrict__ u0 = (const float*)sa.u0;
-    const float4 uh = STAGE == 0 ? C : *(const float4*)(u0 + p);
-    float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
-    if constexpr (STAGE > 0) av = *((const float4*)((const float*)sa.acc + p));
-    const float zz[8] = {zL.z, zL.w, C.x, C.y, C.z, C.w, zR.x, zR.y};
-    // the line record (k_cut_rows): words 0..7 on lanes 0..7 of the warp that holds the
-    // line's first point, words 8..15 on lanes 8..15 of the one that holds its last point
-    pdl_wait();
-    const bool rec_l = blockIdx.x == 0, rec_r = blockIdx.x + 1 == gridDim.x;
-    const float rec = (lane < 8 ? rec_l : (lane < 16 && rec_r))
-                          ? __ldg(sa.lrec + (long long)(i * ny + j) * 16 + lane)
-                          : 0.f;
+    L.uh = STAGE == 0 ? L.C : *(const float4*)(u0 + p);
+    L.av = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (STAGE > 0) L.av = *((const float4*)((const float*)sa.acc + p));
+    return L;
+}
 
+// Everything of one thread's four points of plane i after the loads: interior rows from the
+// registers, cut-cell rows (rowv), z-wall rows and z-face values (the line record `rec`),
+// x / y wall rows, the right-hand side, the RK4 registers, Dirichlet faces, the stores.
+template <int STAGE, int SYS, int FORM, int VK>
+__device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParams& sp,
+                                                 const StageArgs& sa, const float* in, int i,
+                                                 int j, int k, int lane, const VecLoads& L,
+                                                 const float4 xa, const float4 xb,
+                                                 const float4 xc, const float4 xd, float rec)
+{
+    const int nz = op.it2;
+    const int plane = op.it1 * nz;
+    const bool kvalid = k < nz;
+    const int p = i * plane + j * nz + min(k, nz - 4);
+    const float4 C = L.C, ya = L.ya, yb = L.yb, yc = L.yc, yd = L.yd, uh = L.uh, av = L.av;
+    const unsigned c4 = L.c4;
+    const float zz[8] = {L.zL.z, L.zL.w, C.x, C.y, C.z, C.w, L.zR.x, L.zR.y};
+    const float* __restrict__ u0 = (const float*)sa.u0;
     float v[3][4];
     unsigned kq[3][4];
     bool cut = false, zwall = false, xywall = false; // cut-cell rows; z-wall rows; x/y walls
@@ -1526,6 +1535,37 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
         *((float4*)(w0 + p)) = make_float4(uo[0].x, uo[1].x, uo[2].x, uo[3].x);
         *((float4*)(w0 + op.N + p)) = make_float4(uo[0].y, uo[1].y, uo[2].y, uo[3].y);
     }
+}
+
+template <int STAGE, int SYS, int FORM, int VK, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
+{
+    // The stage input, u0 and the accumulator were complete before the cut-row kernel that
+    // precedes this one could let it start, so their loads go out before the dependent-launch
+    // wait; what that kernel writes (line records, cut-cell values) is read after it.
+    pdl_trigger();
+    const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
+    const int nx = op.it0, ny = op.it1, nz = op.it2;
+    const int lane = threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (j >= ny) return; // whole warp
+    const int i = blockIdx.z;
+    const int k = blockIdx.x * 128 + 4 * lane;
+    const int plane = ny * nz;
+    const int p = i * plane + j * nz + min(k, nz - 4);
+    const int xm2 = (max(i - 2, 0) - i) * plane, xm1 = (max(i - 1, 0) - i) * plane;
+    const int xp1 = (min(i + 1, nx - 1) - i) * plane, xp2 = (min(i + 2, nx - 1) - i) * plane;
+    const VecLoads L = vec_loads<STAGE>(op, sa, in, i, j, k, ld4(in, p));
+    const float4 xa = ld4(in, p + xm2), xb = ld4(in, p + xm1), xc = ld4(in, p + xp1),
+                 xd = ld4(in, p + xp2);
+    // the line record (k_cut_rows): words 0..7 on lanes 0..7 of the warp that holds the
+    // line's first point, words 8..15 on lanes 8..15 of the one that holds its last point
+    pdl_wait();
+    const bool rec_l = blockIdx.x == 0, rec_r = blockIdx.x + 1 == gridDim.x;
+    const float rec = (lane < 8 ? rec_l : (lane < 16 && rec_r))
+                          ? __ldg(sa.lrec + (long long)(i * ny + j) * 16 + lane)
+                          : 0.f;
+    vec_stage_points<STAGE, SYS, FORM, VK>(op, sp, sa, in, i, j, k, lane, L, xa, xb, xc, xd, rec);
 }
 
 // ---- TMA plane-marching mixed stage (3-D grids) -----------------------------------------
