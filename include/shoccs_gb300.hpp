@@ -13,6 +13,10 @@
 //   ccs::derivative           src/operators/derivative.hpp:20-80
 //   ccs::laplacian            src/operators/laplacian.hpp:10-33
 //   ccs::gradient             src/operators/gradient.hpp:10-30
+//   ccs::graph, build_graph / submit_graph / add_graph_nodes of the operators,
+//   build_rhs_graph / submit_rhs_graph of the systems
+//                             src/operators/derivative.hpp:71-151, laplacian.hpp:35-118,
+//                             gradient.hpp:31-122, src/systems/system.cpp:57-69
 //   ccs::systems::heat        src/systems/heat.hpp:16-70
 //   ccs::systems::scalar_wave src/systems/scalar_wave.hpp:16-80
 //   ccs::integrators::rk4, euler, integrator
@@ -39,6 +43,7 @@
 #include <array>
 #include <charconv>
 #include <chrono>
+#include <concepts>
 #include <cstdint>
 #include <cstdio>
 #include <ctime>
@@ -304,6 +309,38 @@ inline int plus(eq_t) { return 0; }
 inline int plus(plus_eq_t) { return 1; }
 } // namespace detail
 
+// ---- graphs (Kokkos::Experimental::Graph as the reference builds them) -------------------------
+// A graph records operator applies (add_graph_nodes) and system right-hand sides with their
+// buffers baked in and replays them, in the order they were added, as one captured CUDA
+// graph.  The reference chains graph nodes from a parent (add_graph_nodes(parent, ...)
+// returns the node to chain from); here the parent is the graph itself and the recording
+// order is the chain.  submit() runs the graph and returns after the stream has finished
+// (derivative::submit_graph, src/operators/derivative.cpp:591-596); t is the time of its
+// right-hand sides (heat::submit_rhs_graph fills the source at that time).
+class graph
+{
+    std::shared_ptr<shoccs_graph> g_;
+    void* stream_ = nullptr;
+
+public:
+    graph()
+    {
+        shoccs_graph* raw = nullptr;
+        detail::check(shoccs_graph_create(&raw), "shoccs_graph_create");
+        g_.reset(raw, [](shoccs_graph* q) { shoccs_graph_destroy(q); });
+    }
+    shoccs_graph* get() const { return g_.get(); }
+    void set_stream(void* cuda_stream) { stream_ = cuda_stream; }
+    void submit(real t = 0.0) const { detail::check(shoccs_graph_submit(g_.get(), t, stream_), "shoccs_graph_submit"); }
+    // {recorded applies, kernel and memset nodes of the captured graph, captures so far}
+    std::array<std::int64_t, 3> info() const
+    {
+        std::array<std::int64_t, 3> v{};
+        detail::check(shoccs_graph_info(g_.get(), v.data()), "shoccs_graph_info");
+        return v;
+    }
+};
+
 // ---- derivative (src/operators/derivative.hpp:20-80) -------------------------------------------
 // du (=|+=) D_dir u, with optional Neumann data nu (FP64 in both precisions).
 // precision::mixed applies the FP32 operator to float fields (scalar_view_f / scalar_span_f).
@@ -351,6 +388,54 @@ public:
     {
         apply(u, &nu, du, detail::plus(op));
     }
+
+    // graph forms (src/operators/derivative.hpp:71-151): add_graph_nodes records the apply
+    // in a graph; build_graph makes the operator's own graph of one apply, submit_graph runs it
+    template <typename Op = eq_t>
+    graph& add_graph_nodes(graph& g, scalar_view u, scalar_span du, Op op = {}) const
+    {
+        return record(g, u, nullptr, du, detail::plus(op));
+    }
+    template <typename Op = eq_t>
+    graph& add_graph_nodes(graph& g, scalar_view u, scalar_view nu, scalar_span du, Op op = {}) const
+    {
+        return record(g, u, &nu, du, detail::plus(op));
+    }
+    template <typename Op = eq_t>
+    graph& add_graph_nodes(graph& g, scalar_view_f u, scalar_span_f du, Op op = {}) const
+    {
+        return record(g, u, nullptr, du, detail::plus(op));
+    }
+    template <typename Op = eq_t>
+    graph& add_graph_nodes(graph& g, scalar_view_f u, scalar_view nu, scalar_span_f du, Op op = {}) const
+    {
+        return record(g, u, &nu, du, detail::plus(op));
+    }
+    template <typename... A>
+    void build_graph(A&&... a)
+    {
+        graph_ = graph{};
+        add_graph_nodes(*graph_, std::forward<A>(a)...);
+    }
+    void submit_graph()
+    {
+        if (!graph_) throw error(SHOCCS_EINVAL, "derivative::submit_graph: no graph built");
+        graph_->set_stream(stream_);
+        graph_->submit();
+    }
+
+private:
+    std::optional<graph> graph_;
+    template <typename V, typename S>
+    graph& record(graph& g, const V& u, const scalar_view* nu, const S& du, int plus) const
+    {
+        shoccs_field fu = detail::field(u), fdu = detail::field(du), fnu{};
+        if (nu) fnu = detail::field(*nu);
+        detail::check(shoccs_graph_add_derivative(g.get(), p_.get(), dir_, (int)prec_, &fu,
+                                                  nu ? &fnu : nullptr, &fdu, plus),
+                      "shoccs_graph_add_derivative");
+        return g;
+    }
 };
 
 // ---- laplacian (src/operators/laplacian.hpp:10-33) ---------------------------------------------
@@ -396,6 +481,42 @@ public:
     {
         return [this, u, nu](scalar_span_f du) { apply(u, &nu, du); };
     }
+
+    // graph forms (src/operators/laplacian.hpp:35-118)
+    graph& add_graph_nodes(graph& g, scalar_view u, scalar_span du) const { return record(g, u, nullptr, du); }
+    graph& add_graph_nodes(graph& g, scalar_view u, scalar_view nu, scalar_span du) const
+    {
+        return record(g, u, &nu, du);
+    }
+    graph& add_graph_nodes(graph& g, scalar_view_f u, scalar_span_f du) const { return record(g, u, nullptr, du); }
+    graph& add_graph_nodes(graph& g, scalar_view_f u, scalar_view nu, scalar_span_f du) const
+    {
+        return record(g, u, &nu, du);
+    }
+    template <typename... A>
+    void build_graph(A&&... a)
+    {
+        graph_ = graph{};
+        add_graph_nodes(*graph_, std::forward<A>(a)...);
+    }
+    void submit_graph()
+    {
+        if (!graph_) throw error(SHOCCS_EINVAL, "laplacian::submit_graph: no graph built");
+        graph_->set_stream(stream_);
+        graph_->submit();
+    }
+
+private:
+    std::optional<graph> graph_;
+    template <typename V, typename S>
+    graph& record(graph& g, const V& u, const scalar_view* nu, const S& du) const
+    {
+        shoccs_field fu = detail::field(u), fdu = detail::field(du), fnu{};
+        if (nu) fnu = detail::field(*nu);
+        detail::check(shoccs_graph_add_laplacian(g.get(), p_.get(), (int)prec_, &fu, nu ? &fnu : nullptr, &fdu),
+                      "shoccs_graph_add_laplacian");
+        return g;
+    }
 };
 
 // ---- gradient (src/operators/gradient.hpp:10-30) -----------------------------------------------
@@ -431,6 +552,27 @@ public:
     std::function<void(scalar_span_f, scalar_span_f, scalar_span_f)> operator()(scalar_view_f u) const
     {
         return [this, u](scalar_span_f dx, scalar_span_f dy, scalar_span_f dz) { apply(u, dx, dy, dz); };
+    }
+
+    // graph form (src/operators/gradient.hpp:31-122): du_x, du_y, du_z of u
+    graph& add_graph_nodes(graph& g, scalar_view u, scalar_span dx, scalar_span dy, scalar_span dz) const
+    {
+        return record(g, u, dx, dy, dz);
+    }
+    graph& add_graph_nodes(graph& g, scalar_view_f u, scalar_span_f dx, scalar_span_f dy, scalar_span_f dz) const
+    {
+        return record(g, u, dx, dy, dz);
+    }
+
+private:
+    template <typename V, typename S>
+    graph& record(graph& g, const V& u, const S& dx, const S& dy, const S& dz) const
+    {
+        shoccs_field fu = detail::field(u), fx = detail::field(dx), fy = detail::field(dy),
+                     fz = detail::field(dz);
+        detail::check(shoccs_graph_add_gradient(g.get(), p_.get(), (int)prec_, &fu, &fx, &fy, &fz),
+                      "shoccs_graph_add_gradient");
+        return g;
     }
 };
 
@@ -570,6 +712,29 @@ public:
     // its schedule fires at this step (write_scalar_error,
     // src/systems/detail/scalar_system_utils.hpp:224-296); true when it wrote
     bool write(field_io& io, const step_controller& c, real dt) const;
+
+    // graph forms (src/systems/system.cpp:57-69, heat.cpp:164-294): the right-hand side of
+    // the current state into du as a graph, run at a given time
+    graph& add_graph_nodes(graph& g, scalar_span du) const
+    {
+        shoccs_field f = detail::field(du);
+        detail::check(shoccs_graph_add_rhs(g.get(), s_.get(), &f), "shoccs_graph_add_rhs");
+        return g;
+    }
+    void build_rhs_graph(scalar_span du)
+    {
+        rhs_graph_ = graph{};
+        add_graph_nodes(*rhs_graph_, du);
+    }
+    void submit_rhs_graph(real t)
+    {
+        if (!rhs_graph_) throw error(SHOCCS_EINVAL, "submit_rhs_graph: no graph built");
+        rhs_graph_->set_stream(stream_);
+        rhs_graph_->submit(t);
+    }
+
+private:
+    std::optional<graph> rhs_graph_;
 };
 
 // dT/dt = k lap T + the manufactured source (src/systems/heat.hpp:16-70)

@@ -34,6 +34,10 @@
  *                                                   src/systems/detail/scalar_system_utils.hpp:224-296
  *   shoccs_system_timestep  system::timestep_size   src/systems/heat.cpp:356-361,
  *                                                   src/systems/scalar_wave.cpp:357-362
+ *   shoccs_graph_*          derivative / laplacian / gradient add_graph_nodes, build_graph,
+ *                           submit_graph; system::build_rhs_graph / submit_rhs_graph
+ *                                                   src/operators/derivative.hpp:71-151,
+ *                                                   src/systems/system.cpp:57-69
  *
  * Conventions.  Fields are the reference's scalar {D, Rx, Ry, Rz} (src/fields/scalar.hpp:13-67):
  * D is the full nx*ny*nz grid (z fastest, solid points included), Rx/Ry/Rz hold one value
@@ -282,6 +286,47 @@ shoccs_status shoccs_system_backward(shoccs_system* s, const shoccs_tape* tape,
 shoccs_status shoccs_tape_checkpoint(const shoccs_tape* tape, int i, double* state,
                                      int* count, void* stream);
 shoccs_status shoccs_tape_destroy(shoccs_tape* tape);
+
+/* ---- captured graphs ----------------------------------------------------------------------
+ * The reference's graph forms: derivative::build_graph / submit_graph / add_graph_nodes
+ * (src/operators/derivative.hpp:71-151, derivative.cpp:521-596), laplacian and gradient
+ * add_graph_nodes (src/operators/laplacian.hpp:35-118, gradient.hpp:31-122) and
+ * system::build_rhs_graph / submit_rhs_graph (src/systems/system.cpp:57-69,
+ * heat.cpp:164-294).  A graph records operator applies and system right-hand sides with
+ * their buffers (pointers are baked in, as in the reference: the buffers must stay where they
+ * are) and runs them in the order they were added.  On its first submit -- and, when it holds
+ * a right-hand side, on a submit at another time than the last or after the system's RK4
+ * steps have moved its state buffers -- the graph's kernels are captured into a CUDA graph
+ * (instantiated once, later captures update the instantiated graph in place); every submit
+ * replays it on `stream` and returns after the stream has finished (the reference's
+ * submit_graph fences).  A right-hand side takes the system's
+ * current state as its input, like shoccs_system_rhs.  Results equal the eager entry points'
+ * bit for bit.  A graph is not re-entrant, and two graphs over the same problem must not run
+ * at the same time (the mixed-precision operators share the problem's scratch). */
+typedef struct shoccs_graph shoccs_graph;
+shoccs_status shoccs_graph_create(shoccs_graph** out);
+shoccs_status shoccs_graph_destroy(shoccs_graph* g);
+/* derivative::add_graph_nodes(parent, u[, nu], du, eq|plus_eq) */
+shoccs_status shoccs_graph_add_derivative(shoccs_graph* g, shoccs_problem* p, int dir, int prec,
+                                          const shoccs_field* u, const shoccs_field* nu,
+                                          shoccs_field* du, int plus_eq);
+/* laplacian::add_graph_nodes(parent, u[, nu], du) */
+shoccs_status shoccs_graph_add_laplacian(shoccs_graph* g, shoccs_problem* p, int prec,
+                                         const shoccs_field* u, const shoccs_field* nu,
+                                         shoccs_field* du);
+/* gradient::add_graph_nodes(parent, u, du_x, du_y, du_z) */
+shoccs_status shoccs_graph_add_gradient(shoccs_graph* g, shoccs_problem* p, int prec,
+                                        const shoccs_field* u, shoccs_field* dx, shoccs_field* dy,
+                                        shoccs_field* dz);
+/* system::build_rhs_graph: the right-hand side of the system's state at the submit's time
+ * into rhs (FP64 device field) */
+shoccs_status shoccs_graph_add_rhs(shoccs_graph* g, shoccs_system* s, shoccs_field* rhs);
+/* submit_graph / submit_rhs_graph(time): t is the time of the graph's right-hand sides (the
+ * operators ignore it) */
+shoccs_status shoccs_graph_submit(shoccs_graph* g, double t, void* stream);
+/* info[3] = {recorded applies, kernel launches and memsets in the captured graph (0 before
+ *            the first submit), captures so far} */
+shoccs_status shoccs_graph_info(const shoccs_graph* g, int64_t info[3]);
 
 /* kernels launched by this library since load (for launch-count accounting) */
 int64_t shoccs_kernel_launches(void);

@@ -448,5 +448,57 @@ def rk4_solve(system, u0, t0, dt, nsteps, checkpoint_every=0):
     return _Solve.apply(u0)
 
 
+class Graph:
+    """Operator applies and system right-hand sides recorded with their buffers and replayed
+    as one captured CUDA graph (the reference's add_graph_nodes / build_graph /
+    submit_graph; see shoccs_graph_* in include/shoccs_gpu.h).  The fields handed to the add_*
+    methods must stay alive and in place while the graph exists."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().shoccs_graph_create(ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _capi.lib().shoccs_graph_destroy(self._h)
+            self._h = None
+
+    def add_derivative(self, problem, d, u, du, nu=None, plus_eq=False, prec=PREC_FP64):
+        self._keep += [u, du, nu]
+        _capi.check(_capi.lib().shoccs_graph_add_derivative(self._h, problem.handle, d, prec,
+                                                            _field(u), _field(nu), _field(du),
+                                                            1 if plus_eq else 0))
+        return self
+
+    def add_laplacian(self, problem, u, du, nu=None, prec=PREC_FP64):
+        self._keep += [u, du, nu]
+        _capi.check(_capi.lib().shoccs_graph_add_laplacian(self._h, problem.handle, prec,
+                                                           _field(u), _field(nu), _field(du)))
+        return self
+
+    def add_gradient(self, problem, u, dx, dy, dz, prec=PREC_FP64):
+        self._keep += [u, dx, dy, dz]
+        _capi.check(_capi.lib().shoccs_graph_add_gradient(self._h, problem.handle, prec,
+                                                          _field(u), _field(dx), _field(dy),
+                                                          _field(dz)))
+        return self
+
+    def add_rhs(self, system, du):
+        self._keep += [system, du]
+        _capi.check(_capi.lib().shoccs_graph_add_rhs(self._h, system._h, _field(du)))
+        return self
+
+    def submit(self, t=0.0, stream=None):
+        _capi.check(_capi.lib().shoccs_graph_submit(self._h, float(t), _stream(stream)))
+
+    def info(self):
+        """(recorded applies, captured graph nodes, captures so far)"""
+        v = (ctypes.c_int64 * 3)()
+        _capi.check(_capi.lib().shoccs_graph_info(self._h, v))
+        return tuple(v)
+
+
 __all__ = ["Problem", "Derivative", "Laplacian", "Gradient", "Heat", "ScalarWave", "System",
-           "Batch", "Tape", "rk4_solve", "ScalarField", "ShoccsError", "kernel_launches"]
+           "Batch", "Tape", "Graph", "rk4_solve", "ScalarField", "ShoccsError", "kernel_launches"]

@@ -118,6 +118,20 @@ SIGNATURES = {
     "shoccs_tape_checkpoint": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                ctypes.POINTER(ctypes.c_int), ctypes.c_void_p],
     "shoccs_tape_destroy": [ctypes.c_void_p],
+    "shoccs_graph_create": [ctypes.POINTER(ctypes.c_void_p)],
+    "shoccs_graph_destroy": [ctypes.c_void_p],
+    "shoccs_graph_add_derivative": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(Field), ctypes.POINTER(Field),
+                                    ctypes.POINTER(Field), ctypes.c_int],
+    "shoccs_graph_add_laplacian": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                   ctypes.POINTER(Field), ctypes.POINTER(Field),
+                                   ctypes.POINTER(Field)],
+    "shoccs_graph_add_gradient": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                  ctypes.POINTER(Field), ctypes.POINTER(Field),
+                                  ctypes.POINTER(Field), ctypes.POINTER(Field)],
+    "shoccs_graph_add_rhs": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Field)],
+    "shoccs_graph_submit": [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p],
+    "shoccs_graph_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)],
     "shoccs_kernel_launches": [],
     "shoccs_last_error": [ctypes.c_char_p, ctypes.c_size_t],
 }

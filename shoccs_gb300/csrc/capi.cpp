@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -1138,6 +1139,214 @@ shoccs_status shoccs_system_stats_noalloc(shoccs_system* S, double t, double out
     const double bound = S->desc.kind == SHOCCS_SYS_HEAT ? 1e6 : S->desc.max_error;
     if (!std::isfinite(out[0]) || std::abs(out[0]) > bound)
         return fail(SHOCCS_ENONFINITE, "solution error is non-finite or above its bound");
+    return SHOCCS_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// captured graphs: the recorded applies are launched, in order, on a private capturing
+// stream (the launchers below issue kernels and memsets only; every allocation and upload
+// happens when an apply is added), and the capture is instantiated -- or, after the first
+// capture, applied to the instantiated graph with cudaGraphExecUpdate.
+// ---------------------------------------------------------------------------------------
+struct shoccs_graph {
+    struct op {
+        bool timed; // depends on the submit's time (a system right-hand side)
+        std::function<cudaError_t(cudaStream_t, double)> run;
+        // the buffers the op reads that may move between submits (a system's state and its
+        // cut-point values, which its RK4 steps exchange with their next-step copies)
+        std::function<std::array<const void*, 4>()> inputs;
+        std::array<const void*, 4> captured{};
+    };
+    std::vector<op> ops;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    double t_captured = 0.0;
+    bool stale = true;
+    int64_t nodes = 0, captures = 0;
+    ~shoccs_graph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cap) cudaStreamDestroy(cap);
+    }
+};
+
+shoccs_status shoccs_graph_create(shoccs_graph** out)
+{
+    if (!out) return fail(SHOCCS_EINVAL, "null argument");
+    *out = nullptr;
+    auto g = std::make_unique<shoccs_graph>();
+    SH_CUDA(cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking));
+    *out = g.release();
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_destroy(shoccs_graph* g)
+{
+    delete g;
+    return SHOCCS_OK;
+}
+
+namespace
+{
+// the problem's device tables (and, for the FP32 operators, their scratch) before capture
+shoccs_status graph_prepare(shoccs_graph* g, shoccs_problem* p, int prec)
+{
+    if (auto st = do_upload(p, g->cap); st != SHOCCS_OK) return st;
+    if (prec == PREC_MIXED)
+        if (auto st = ensure_op_scratch(p); st != SHOCCS_OK) return st;
+    g->stale = true;
+    return SHOCCS_OK;
+}
+struct field_ptrs {
+    void* D;
+    void* R[3];
+    explicit field_ptrs(const shoccs_field* f) : D{f ? f->D : nullptr}, R{nullptr, nullptr, nullptr}
+    {
+        if (f) {
+            R[0] = f->Rx;
+            R[1] = f->Ry;
+            R[2] = f->Rz;
+        }
+    }
+};
+} // namespace
+
+shoccs_status shoccs_graph_add_derivative(shoccs_graph* g, shoccs_problem* p, int dir, int prec,
+                                          const shoccs_field* u, const shoccs_field* nu,
+                                          shoccs_field* du, int plus_eq)
+{
+    if (!g || !p || !u || !du || dir < 0 || dir > 2 || (prec != 0 && prec != 1))
+        return fail(SHOCCS_EINVAL, "bad argument");
+    if (auto st = graph_prepare(g, p, prec); st != SHOCCS_OK) return st;
+    const field_ptrs fu{u}, fdu{du};
+    const double* nuD = nu ? (const double*)nu->D : nullptr;
+    g->ops.push_back({false, [p, dir, prec, fu, fdu, nuD, plus_eq](cudaStream_t s, double) {
+                          const void* uR[3] = {fu.R[0], fu.R[1], fu.R[2]};
+                          void* duR[3] = {fdu.R[0], fdu.R[1], fdu.R[2]};
+                          return launch_derivative(p->op, dir, prec, fu.D, uR[dir], nuD, fdu.D, duR,
+                                                   uR, plus_eq, s);
+                      },
+                      {},
+                      {}});
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_add_laplacian(shoccs_graph* g, shoccs_problem* p, int prec,
+                                         const shoccs_field* u, const shoccs_field* nu,
+                                         shoccs_field* du)
+{
+    if (!g || !p || !u || !du || (prec != 0 && prec != 1)) return fail(SHOCCS_EINVAL, "bad argument");
+    if (auto st = graph_prepare(g, p, prec); st != SHOCCS_OK) return st;
+    const field_ptrs fu{u}, fdu{du};
+    const double* nuD = nu ? (const double*)nu->D : nullptr;
+    g->ops.push_back({false, [p, prec, fu, fdu, nuD](cudaStream_t s, double) {
+                          const void* uR[3] = {fu.R[0], fu.R[1], fu.R[2]};
+                          void* duR[3] = {fdu.R[0], fdu.R[1], fdu.R[2]};
+                          return launch_laplacian(p->op, prec, fu.D, uR, nuD, fdu.D, duR, s);
+                      },
+                      {},
+                      {}});
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_add_gradient(shoccs_graph* g, shoccs_problem* p, int prec,
+                                        const shoccs_field* u, shoccs_field* dx, shoccs_field* dy,
+                                        shoccs_field* dz)
+{
+    if (!g || !p || !u || !dx || !dy || !dz || (prec != 0 && prec != 1))
+        return fail(SHOCCS_EINVAL, "bad argument");
+    if (auto st = graph_prepare(g, p, prec); st != SHOCCS_OK) return st;
+    const field_ptrs fu{u}, fx{dx}, fy{dy}, fz{dz};
+    g->ops.push_back({false, [p, prec, fu, fx, fy, fz](cudaStream_t s, double) {
+                          const void* uR[3] = {fu.R[0], fu.R[1], fu.R[2]};
+                          void* const out[3][4] = {{fx.D, fx.R[0], fx.R[1], fx.R[2]},
+                                                   {fy.D, fy.R[0], fy.R[1], fy.R[2]},
+                                                   {fz.D, fz.R[0], fz.R[1], fz.R[2]}};
+                          return launch_gradient(p->op, prec, fu.D, uR, out, s);
+                      },
+                      {},
+                      {}});
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_add_rhs(shoccs_graph* g, shoccs_system* S, shoccs_field* rhs)
+{
+    if (!g || !S || !rhs || !rhs->D) return fail(SHOCCS_EINVAL, "null argument");
+    const field_ptrs fr{rhs};
+    g->stale = true;
+    g->ops.push_back({true,
+                      [S, fr](cudaStream_t s, double t) {
+                          double* outR[3] = {(double*)fr.R[0], (double*)fr.R[1], (double*)fr.R[2]};
+                          if (S->unfused)
+                              return launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), t,
+                                                             FieldF64{(double*)fr.D, {outR[0], outR[1], outR[2]}},
+                                                             s);
+                          return launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)fr.D, outR, s);
+                      },
+                      [S]() {
+                          return std::array<const void*, 4>{S->b.u0, S->b.R[0], S->b.R[1], S->b.R[2]};
+                      },
+                      {}});
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_submit(shoccs_graph* g, double t, void* stream)
+{
+    if (!g) return fail(SHOCCS_EINVAL, "null graph");
+    const cudaStream_t s = (cudaStream_t)stream;
+    bool timed = false, moved = false;
+    for (const auto& o : g->ops) {
+        timed = timed || o.timed;
+        if (o.inputs) moved = moved || o.inputs() != o.captured;
+    }
+    if (g->stale || !g->exec || moved || (timed && t != g->t_captured)) {
+        for (auto& o : g->ops)
+            if (o.inputs) o.captured = o.inputs();
+        SH_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (const auto& o : g->ops) {
+            e = o.run(g->cap, t);
+            if (e != cudaSuccess) break;
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e_end = cudaStreamEndCapture(g->cap, &graph);
+        if (e == cudaSuccess) e = e_end;
+        if (e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return fail(SHOCCS_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        size_t n = 0;
+        cudaGraphGetNodes(graph, nullptr, &n);
+        bool updated = false;
+        if (g->exec) {
+            cudaGraphExecUpdateResultInfo info{};
+            updated = cudaGraphExecUpdate(g->exec, graph, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(g->exec);
+                g->exec = nullptr;
+            }
+        }
+        if (!updated) e = cudaGraphInstantiate(&g->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        SH_CUDA(e);
+        g->nodes = (int64_t)n;
+        g->t_captured = t;
+        g->stale = false;
+        g->captures++;
+    }
+    SH_CUDA(cudaGraphLaunch(g->exec, s));
+    SH_CUDA(cudaStreamSynchronize(s));
+    return SHOCCS_OK;
+}
+
+shoccs_status shoccs_graph_info(const shoccs_graph* g, int64_t info[3])
+{
+    if (!g || !info) return fail(SHOCCS_EINVAL, "null argument");
+    info[0] = (int64_t)g->ops.size();
+    info[1] = g->nodes;
+    info[2] = g->captures;
     return SHOCCS_OK;
 }
 
