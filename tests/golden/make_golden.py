@@ -124,6 +124,37 @@ def ref_fixtures():
             dict(source="src/mesh/sphere.cpp via oracle/_ref", hits=hits))
 
 
+# the reference's own input files (paths within its tree)
+REFERENCE_INPUTS = ["heat.lua", "scalar_wave.lua", "scalar_wave_1d.lua", "eigenvalues.lua",
+                    "lua-configs/brady_livescu_4_3_n61.lua", "lua-configs/brady_livescu_4_3.lua"]
+
+
+def reference_inputs():
+    """The `simulation` table of each of the reference's input files as the command line's
+    Lua reader evaluates it (tests/cpp/lua_eval.cpp), with the exit status of
+    `shoccs --check` on the file (the template brady_livescu_4_3.lua holds unfilled markers
+    and is not valid Lua)"""
+    import tempfile
+    sys.path.insert(0, REPO)
+    from tests.reference_inputs import parse_dump
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "lua_eval")
+        subprocess.check_call(["g++", "-std=c++20", "-O2", "-I" + os.path.join(REPO, "shoccs_gb300", "app"),
+                               os.path.join(REPO, "tests", "cpp", "lua_eval.cpp"), "-o", exe])
+        cli = os.path.join(REPO, "shoccs_gb300", "_build", "shoccs")
+        out = {}
+        for name in REFERENCE_INPUTS:
+            path = os.path.join(REF, name)
+            r = subprocess.run([exe, path, "result = simulation"], capture_output=True, text=True)
+            chk = subprocess.run([cli, "--check", path], capture_output=True, text=True, cwd=d)
+            def keys_to_str(t):
+                return {str(k): keys_to_str(v) for k, v in t.items()} if isinstance(t, dict) else t
+            out[name] = dict(check_rc=chk.returncode,
+                             table=keys_to_str(parse_dump(r.stdout)) if r.returncode == 0 else None)
+    return dict(source="the reference's input files, evaluated by tests/cpp/lua_eval.cpp",
+                inputs=out)
+
+
 def reference_pins():
     """digests (plus size and max |value|) of the arrays of tests/golden/pins.py computed by
     the reference's own code"""
@@ -169,4 +200,6 @@ if __name__ == "__main__":
         json.dump(hits, f)
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(reference_pins(), f, indent=0, sort_keys=True)
+    with open(os.path.join(HERE, "reference_inputs.json"), "w") as f:
+        json.dump(reference_inputs(), f, indent=1, sort_keys=True)
     print("wrote fixtures to", HERE)
