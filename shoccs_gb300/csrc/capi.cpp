@@ -808,6 +808,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         }
         // the trial steps of the autotuner need every register allocated and zeroed; the
         // column and vectorised kernels index with 32-bit integers
+        if (const char* f = std::getenv("SHOCCS_CUT_ROWS_FP64")) S->b.cut_fp64 = std::atoi(f) != 0;
         if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
             // the vectorised stage: cut-cell row values at their points, line records; the
             // cut-row kernel runs one thread per cut-cell row and per z line

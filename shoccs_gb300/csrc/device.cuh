@@ -135,6 +135,10 @@ struct StepBuffers {
     // read, at their points (3 x N floats, axis-major), and the line records (z-wall rows
     // and z-face values of every z line, 16 floats per line)
     int vec = 0;      // stencil form (FORM_*) of the vectorised kernel, 0 = not used
+    // mixed path: the cut-cell rows in FP64 arithmetic (their FP32 stage inputs and FP64
+    // coefficients, rounded to FP32 at the end) instead of compensated FP32; chosen at
+    // creation by SHOCCS_CUT_ROWS_FP64=1
+    int cut_fp64 = 0;
     int vec_minb = 4; // its resident blocks per SM (4: 64 registers, 3: 85 registers)
     float* rowv = nullptr;
     float* lrec = nullptr;

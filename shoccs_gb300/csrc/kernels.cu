@@ -697,6 +697,7 @@ struct StageArgs {
     double t_stage, t_next; // RHS time and Dirichlet time of the stage output
     double et_stage, et_next;
     float etf_stage;
+    int cut_fp64; // mixed path: cut-cell rows in FP64 arithmetic instead of compensated FP32
 };
 
 enum { SYS_HEAT = 0, SYS_WAVE = 1 };
@@ -832,7 +833,8 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
     if constexpr (std::is_same<TOUT, double>::value) {
         cval[i] = closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
     } else {
-        const float v = closure_ff(A, row, p, u, R[d]);
+        const float v = sa.cut_fp64 ? (float)closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true)
+                                    : closure_ff(A, row, p, u, R[d]);
         if (rowv)
             rowv[d * op.N + p] = v;
         else
@@ -2647,6 +2649,7 @@ cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp
         a.et_stage = et(a.t_stage);
         a.et_next = et(a.t_next);
         a.etf_stage = (float)a.et_stage;
+        a.cut_fp64 = b.cut_fp64;
     }
     if (sp.kind == SYS_HEAT)
         launch_stages<SYS_HEAT>(op, sp, prec, sa, b, s, ev);
