@@ -1383,6 +1383,16 @@ struct shoccs_batch {
     // 2-D instances go to the flat stage: warp tiles (instance, first point) of BATCH2D_TILE points
     const int2* d_wtiles = nullptr;
     int n_wtiles = 0, grid2d = 1;
+    // or to the split stage (uniform tiles, special points; no cut-cell row pass)
+    BatchSplit split;
+    // every instance split 2-D and SHOCCS_BATCH_PERSIST=1: the whole solve in one persistent
+    // launch of n_clusters clusters (kernels.cu k_batch_persist), cluster c owning the
+    // instances of ctab[c]
+    bool persist = false;
+    int n_clusters = 0;
+    const int4* d_psp = nullptr;
+    const int2* d_put = nullptr;
+    const int4* d_ctab = nullptr;
     const int* d_r_inst = nullptr;
     int n_r = 0;
     int cfg = 3, grid = 1;
@@ -1396,6 +1406,9 @@ struct shoccs_batch {
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (cap) cudaStreamDestroy(cap);
+        if (split.aux) cudaStreamDestroy(split.aux);
+        if (split.fork) cudaEventDestroy(split.fork);
+        if (split.join) cudaEventDestroy(split.join);
     }
 };
 
@@ -1505,13 +1518,17 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
     std::vector<int> row_inst, r_inst;
     std::vector<int4> tiles[4];
     std::vector<int2> wtiles;
-    // SHOCCS_BATCH_KERNEL=point sends every instance through the per-point stage
+    std::vector<int2> ut;
+    std::vector<int4> sp;
+    std::vector<int> sp_kind; // row kinds along it1, it2 and the face bit of each special point
+    std::vector<std::pair<int, int>> inst_ut(n), inst_sp(n); // (begin, end) of each instance
+    bool all2d = true;
+    // SHOCCS_BATCH_KERNEL=point sends every instance through the per-point stage, =flat the
+    // 2-D instances through the flat stage; by default they take the split stage
     const char* kenv = std::getenv("SHOCCS_BATCH_KERNEL");
-    // FP64 batches take the per-point stage unless SHOCCS_BATCH_KERNEL=flat asks otherwise:
-    // with FP64 arithmetic at 1/64 of the FP32 rate the flat stage's register-heavy body
-    // measured slower there
-    const bool allow2d = kenv ? std::string(kenv) == "flat"
-                              : B->prec == PREC_MIXED;
+    const std::string kname = kenv ? std::string(kenv) : std::string("split");
+    const bool allow2d = kname == "flat" || kname == "split";
+    const bool use_split = kname == "split";
     for (int i = 0; i < n; i++) {
         shoccs_system* S = systems[i];
         if (!S) return fail(SHOCCS_EINVAL, "null system");
@@ -1539,6 +1556,7 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         I.row0 = (int)row_inst.size();
         const bool flat2d = allow2d && op.it0 == 1 && op.it1 > 1 && op.phys_of_it[1] >= 0 &&
                             op.phys_of_it[2] >= 0 && op.N < (1LL << 31) - 256;
+        all2d = all2d && flat2d;
         if (flat2d) {
             // cut-cell row values at their points, per axis (3 x N, the batch's own buffer)
             void* rv = nullptr;
@@ -1548,11 +1566,39 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
             I.rowv = rv;
             if ((long long)wtiles.size() + op.N / BATCH2D_TILE + 1 >= (1LL << 31))
                 return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 tiles");
-            for (long long t = 0; t < op.N; t += BATCH2D_TILE) wtiles.push_back(make_int2(i, (int)t));
+            if (use_split) {
+                inst_ut[i].first = (int)ut.size();
+                for (long long t = 0; t < op.N; t += BATCH_UTILE) ut.push_back(make_int2(i, (int)t));
+                inst_ut[i].second = (int)ut.size();
+                // special points: a wall or cut-cell row along either axis, or a Dirichlet face
+                const Compiled& cp = S->P->comp;
+                const int da = op.phys_of_it[1], db = op.phys_of_it[2];
+                auto row_of = [&](int d, long long q) {
+                    const auto& ro = cp.ax[d].row_out;
+                    const auto it = std::lower_bound(ro.begin(), ro.end(), (i64)q);
+                    return it != ro.end() && *it == q ? (int)(it - ro.begin()) : -1;
+                };
+                inst_sp[i].first = (int)sp.size();
+                for (long long q = 0; q < op.N; q++) {
+                    const unsigned c = cp.cls[q];
+                    const unsigned ka = (c >> (2 * da)) & 3u, kb = (c >> (2 * db)) & 3u;
+                    if (ka < ROW_CLOSURE && kb < ROW_CLOSURE && !(c & CLS_DIRFACE)) continue;
+                    const int ra = ka == ROW_CLOSURE ? row_of(da, q) : -1;
+                    const int rb = kb == ROW_CLOSURE ? row_of(db, q) : -1;
+                    if ((ka == ROW_CLOSURE && ra < 0) || (kb == ROW_CLOSURE && rb < 0))
+                        return fail(SHOCCS_EINVAL, "cut-cell point without its row");
+                    sp.push_back(make_int4(i, (int)q, ra, rb));
+                    sp_kind.push_back((int)(((ka << 2 | kb) << 1) | ((c & CLS_DIRFACE) ? 1u : 0u)));
+                }
+                inst_sp[i].second = (int)sp.size();
+            } else {
+                for (long long t = 0; t < op.N; t += BATCH2D_TILE) wtiles.push_back(make_int2(i, (int)t));
+            }
         }
         if ((long long)row_inst.size() + op.n_cut_rows >= (1LL << 31))
             return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 cut-cell rows");
-        row_inst.insert(row_inst.end(), op.n_cut_rows, i);
+        // the split stage evaluates its cut-cell rows at their points: no row pass
+        if (!(flat2d && use_split)) row_inst.insert(row_inst.end(), op.n_cut_rows, i);
         for (int c = 0; c < 4 && !flat2d; c++) {
             const int w = BATCH_TILE_WARPS[c];
             const int nyb = (op.it1 + w - 1) / w;
@@ -1587,9 +1633,87 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
     SH_CUDA(B->mem.put(wtiles, &B->d_wtiles, s));
     B->n_wtiles = (int)wtiles.size();
     B->grid2d = batch_stage2d_grid(B->prec, B->n_wtiles);
+    if ((long long)sp.size() + ((long long)ut.size() + 3) / 4 * 128 >= (1LL << 31))
+        return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 points");
+    // special points grouped by their kinds of rows, so that the threads of a warp mostly
+    // take the same path (instance and point order within a group)
+    auto by_kind = [&](std::vector<int4>& v, std::vector<int>& kind, size_t b, size_t e) {
+        std::vector<size_t> ord(e - b);
+        for (size_t k = 0; k < ord.size(); k++) ord[k] = b + k;
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return kind[x] < kind[y]; });
+        std::vector<int4> tmp(ord.size());
+        std::vector<int> tk(ord.size());
+        for (size_t k = 0; k < ord.size(); k++) {
+            tmp[k] = v[ord[k]];
+            tk[k] = kind[ord[k]];
+        }
+        std::copy(tmp.begin(), tmp.end(), v.begin() + b);
+        std::copy(tk.begin(), tk.end(), kind.begin() + b);
+    };
+    {
+        std::vector<int4> sps = sp;
+        std::vector<int> spk = sp_kind;
+        by_kind(sps, spk, 0, sps.size());
+        SH_CUDA(B->mem.put(sps, &B->split.sp, s));
+    }
+    SH_CUDA(B->mem.put(ut, &B->split.ut, s));
+    B->split.n_ut = (int)ut.size();
+    B->split.n_sp = (int)sp.size();
     SH_CUDA(B->mem.put(r_inst, &B->d_r_inst, s));
     B->n_r = (int)(r_inst.size() / 3);
+    // SHOCCS_BATCH_PERSIST=0 keeps a batch of 2-D instances on the launch-per-stage kernels
+    const char* penv = std::getenv("SHOCCS_BATCH_PERSIST");
+    if (all2d && use_split && penv && std::string(penv) == "1") {
+        const int maxc = batch_persist_clusters(B->prec);
+        if (maxc > 0) {
+            // instances to clusters by their work (points, plus a cut-cell row as 8 points),
+            // the largest first, each to the least loaded cluster
+            const int C = std::min(maxc, n);
+            std::vector<int> order(n);
+            std::vector<double> work(n);
+            for (int i = 0; i < n; i++) {
+                order[i] = i;
+                work[i] = (double)B->h_inst[i].op.N + 8.0 * B->h_inst[i].op.n_cut_rows;
+            }
+            std::stable_sort(order.begin(), order.end(),
+                             [&](int a, int b) { return work[a] > work[b]; });
+            std::vector<double> load(C, 0.0);
+            std::vector<std::vector<int>> own(C);
+            for (int i : order) {
+                const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+                load[c] += work[i];
+                own[c].push_back(i);
+            }
+            std::vector<int4> psp;
+            std::vector<int> pspk;
+            std::vector<int2> put;
+            std::vector<int4> ctab(C);
+            for (int c = 0; c < C; c++) {
+                std::sort(own[c].begin(), own[c].end());
+                ctab[c].x = (int)psp.size();
+                ctab[c].z = (int)put.size();
+                for (int i : own[c]) {
+                    psp.insert(psp.end(), sp.begin() + inst_sp[i].first, sp.begin() + inst_sp[i].second);
+                    pspk.insert(pspk.end(), sp_kind.begin() + inst_sp[i].first, sp_kind.begin() + inst_sp[i].second);
+                    put.insert(put.end(), ut.begin() + inst_ut[i].first, ut.begin() + inst_ut[i].second);
+                }
+                ctab[c].y = (int)psp.size();
+                ctab[c].w = (int)put.size();
+                by_kind(psp, pspk, ctab[c].x, ctab[c].y);
+            }
+            SH_CUDA(B->mem.put(psp, &B->d_psp, s));
+            SH_CUDA(B->mem.put(put, &B->d_put, s));
+            SH_CUDA(B->mem.put(ctab, &B->d_ctab, s));
+            B->persist = true;
+            B->n_clusters = C;
+        }
+    }
     SH_CUDA(cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking));
+    if (B->split.n_sp && B->split.n_ut) {
+        SH_CUDA(cudaStreamCreateWithFlags(&B->split.aux, cudaStreamNonBlocking));
+        SH_CUDA(cudaEventCreateWithFlags(&B->split.fork, cudaEventDisableTiming));
+        SH_CUDA(cudaEventCreateWithFlags(&B->split.join, cudaEventDisableTiming));
+    }
     if (auto st = batch_autotune(B.get(), s); st != SHOCCS_OK) return st;
     SH_CUDA(cudaStreamSynchronize(s));
     *out = B.release();
@@ -1621,11 +1745,14 @@ shoccs_status shoccs_batch_rk4(shoccs_batch* B, const double* t0, const double* 
         }
         SH_CUDA(cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;
-        for (int k = 0; k < nsteps && e == cudaSuccess; k++)
+        if (B->persist)
+            e = launch_batch_persist(B->d_inst, B->d_psp, B->d_put, B->d_ctab, B->n_clusters,
+                                     B->d_times, n, nsteps, B->prec, B->cap);
+        for (int k = 0; k < nsteps && e == cudaSuccess && !B->persist; k++)
             e = launch_batch_step(B->d_inst, B->d_row_inst, B->n_rows, B->d_tiles[B->cfg],
                                   B->n_tiles[B->cfg], B->cfg, B->grid, B->d_wtiles,
-                                  B->n_wtiles, B->grid2d, B->d_times + (size_t)k * n, B->prec,
-                                  B->cap);
+                                  B->n_wtiles, B->grid2d, B->split, B->d_times + (size_t)k * n,
+                                  B->prec, B->cap);
         cudaGraph_t g = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(B->cap, &g);
         if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -1657,10 +1784,10 @@ shoccs_status shoccs_batch_info(const shoccs_batch* B, int64_t info[6])
 {
     if (!B || !info) return fail(SHOCCS_EINVAL, "null argument");
     info[0] = (int64_t)B->sys.size();
-    info[1] = B->n_tiles[B->cfg] + B->n_wtiles;
+    info[1] = B->n_tiles[B->cfg] + B->n_wtiles + B->split.n_ut;
     info[2] = B->n_rows;
     info[3] = BATCH_TILE_WARPS[B->cfg];
-    info[4] = B->grid;
+    info[4] = B->persist ? B->n_clusters * BATCH_CLUSTER : B->grid;
     info[5] = B->graph_nodes;
     return SHOCCS_OK;
 }

@@ -194,16 +194,38 @@ struct BatchTime {
 constexpr int BATCH_TILE_WARPS[4] = {1, 2, 4, 8};
 // one RK4 step of every instance: per stage, the cut-cell rows of all instances, then the
 // stage update of all instances (persistent blocks over the (instance, tile) list)
+// the split 2-D stage's work lists: uniform tiles (instance, first point; BATCH_UTILE points
+// each, a multiple of BATCH2D_TILE) and special points (instance, point, cut-cell row along
+// it1, along it2; -1: none)
+constexpr int BATCH_UTILE = 256;
+struct BatchSplit {
+    const int2* ut = nullptr;
+    int n_ut = 0;
+    const int4* sp = nullptr;
+    int n_sp = 0;
+    // stream and events of the special points' branch (null: both on the launch stream)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
 // per stage: the cut-cell rows of every instance, then the per-point stage over `tiles`
 // (instances that are not 2-D) and the flat 2-D stage over the warp tiles `wtiles`
-// (instance, first point; BATCH2D_TILE points each)
+// (instance, first point; BATCH2D_TILE points each), or the split 2-D stage, which needs no
+// cut-cell row pass
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
                               const int4* tiles, int n_tiles, int tile_cfg, int grid,
-                              const int2* wtiles, int n_wtiles, int grid2d,
+                              const int2* wtiles, int n_wtiles, int grid2d, const BatchSplit& sp,
                               const BatchTime* times, int prec, cudaStream_t s);
 // persistent grid of the flat 2-D batched stage (128-thread blocks), and the points of one
 // of its warp tiles
 int batch_stage2d_grid(int prec, int n_wtiles);
+// the whole solve of a batch of 2-D instances in one persistent launch of the split stage:
+// clusters of BATCH_CLUSTER blocks, cluster c owning whole instances -- ctab[c] = its ranges
+// of the special-point list psp and of the uniform-tile list put
+constexpr int BATCH_CLUSTER = 8;
+int batch_persist_clusters(int prec); // clusters resident at once (0: unavailable)
+cudaError_t launch_batch_persist(const BatchInst* inst, const int4* psp, const int2* put,
+                                 const int4* ctab, int n_clusters, const BatchTime* times,
+                                 int n_inst, int nsteps, int prec, cudaStream_t s);
 constexpr int BATCH2D_PPL = 4;                // points per lane
 constexpr int BATCH2D_TILE = 32 * BATCH2D_PPL; // points per warp tile
 int batch2d_tile_points();

@@ -21,6 +21,8 @@
 //   compute_scalar_stats             src/systems/detail/scalar_system_utils.hpp:77-181
 #include "device.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <atomic>
 #include <mutex>
@@ -30,6 +32,7 @@
 
 namespace sgb
 {
+namespace cg = cooperative_groups;
 namespace
 {
 std::atomic<long long> g_launches{0};
@@ -87,6 +90,27 @@ cudaError_t launch_ex(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_
     return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 __device__ __forceinline__ float ldf(const PairU& u, long long i) { return __ldg(u.hi + i); }
+// Loads of values that other blocks wrote earlier in the same launch (the persistent batched
+// solve, whose stages follow one another inside one kernel): from L2 (ld.global.cg), never
+// through the read-only non-coherent path that __ldg takes.
+struct CgF {
+    const float* p;
+};
+struct CgD {
+    const double* p;
+};
+struct CgPair {
+    const float* hi;
+    long long n;
+};
+__device__ __forceinline__ float ldf(const CgF& u, long long i) { return __ldcg(u.p + i); }
+__device__ __forceinline__ double ldd(const CgF& u, long long i) { return (double)__ldcg(u.p + i); }
+__device__ __forceinline__ double ldd(const CgD& u, long long i) { return __ldcg(u.p + i); }
+__device__ __forceinline__ float ldf(const CgPair& u, long long i) { return __ldcg(u.hi + i); }
+__device__ __forceinline__ double ldd(const CgPair& u, long long i)
+{
+    return (double)__ldcg(u.hi + i) + (double)__ldcg(u.hi + u.n + i);
+}
 __device__ __forceinline__ float2 ld_pair(const void* u0, long long n, long long i)
 {
     const float* h = (const float*)u0;
@@ -257,6 +281,11 @@ __device__ __forceinline__ double closure64(const DevAxis& A, int row, long long
 // of the inputs themselves, and at FP32 rather than FP64 throughput.  All roundings are
 // explicit (__f*_rn), so no step is contracted into an FMA.
 __device__ __forceinline__ float2 ldff(const float* u, long long i) { return make_float2(__ldg(u + i), 0.f); }
+__device__ __forceinline__ float2 ldff(const CgF& u, long long i) { return make_float2(__ldcg(u.p + i), 0.f); }
+__device__ __forceinline__ float2 ldff(const CgPair& u, long long i)
+{
+    return make_float2(__ldcg(u.hi + i), __ldcg(u.hi + u.n + i));
+}
 __device__ __forceinline__ float2 ldff(const PairU& u, long long i)
 {
     return make_float2(__ldg(u.hi + i), __ldg(u.hi + u.n + i));
@@ -278,7 +307,8 @@ __device__ __forceinline__ void ff_mac(float& sh, float& sl, float2 c, float2 x)
 
 // cut-cell row of the mixed path: sum_j c_j u_j + b R_d[b] (no Neumann term: systems have
 // no Neumann faces or objects)
-template <class TIN, class TR>
+// (PF: terms whose loads are issued before the first use; the sum's order does not depend on it)
+template <class TIN, class TR, int PF = 8>
 __device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long p, TIN u, TR Rd)
 {
     const ClosureRow cr = A.rows[row];
@@ -287,7 +317,7 @@ __device__ __forceinline__ float closure_ff(const DevAxis& A, int row, long long
     // issue every load of the row before the first use, so the gathers overlap; the
     // coefficients come two at a time (a block starts at an even offset of the pool, and the
     // pool has a pad after its last coefficient)
-    constexpr int PF = 8;
+    static_assert(PF % 2 == 0, "coefficients are loaded in pairs");
     float2 cv[PF], xv[PF];
     const float4* c4 = reinterpret_cast<const float4*>(c);
 #pragma unroll
@@ -382,19 +412,33 @@ __device__ __forceinline__ float wall_neumann32(const DevAxis& A, long long p, i
 // ---- closed-form solutions -------------------------------------------------------------
 enum { SOL_ZERO = 0, SOL_SINSIN = 1, SOL_GAUSS_PULSE = 2, SOL_RADIAL_SIN = 3, SOL_GAUSSIAN = 4 };
 
+// the sin-sin solution at a grid point from its per-axis table values s0, s1, s2 (physical
+// axis order; s2 read only in 3-D): (s0 s1 [s2]) e^-t
+__device__ __forceinline__ double sinsin_value(double s0, double s1, double s2, bool dims3, double et)
+{
+    double v = s0 * s1;
+    if (dims3) v = v * s2;
+    return v * et;
+}
+// the mixed heat path's manufactured source -u - k lapfac u, u = (s0 s1 [s2]) e^-t in FP32
+__device__ __forceinline__ float sinsin_heat_src_f(float s0, float s1, float s2, bool dims3,
+                                                   float etf, float kf, float lapff)
+{
+    float u = __fmul_rn(s0, s1);
+    if (dims3) u = __fmul_rn(u, s2);
+    u = __fmul_rn(u, etf);
+    return __fsub_rn(-u, __fmul_rn(kf, __fmul_rn(lapff, u)));
+}
+
 __device__ __forceinline__ double sol_at(const DevSol& s, double t, double et, const double x[3],
                                          const int* ijk, int rdir, long long ridx)
 {
     switch (s.kind) {
     case SOL_SINSIN: {
-        double v;
-        if (ijk) {
-            v = s.S[0][ijk[0]] * s.S[1][ijk[1]];
-            if (s.dims == 3) v = v * s.S[2][ijk[2]];
-        } else {
-            v = s.SR[rdir][ridx];
-        }
-        return v * et;
+        if (ijk)
+            return sinsin_value(s.S[0][ijk[0]], s.S[1][ijk[1]], s.dims == 3 ? s.S[2][ijk[2]] : 0.0,
+                                s.dims == 3, et);
+        return s.SR[rdir][ridx] * et;
     }
     case SOL_GAUSS_PULSE: {
         const double d0 = (x[0] - s.p[0]) - s.p[3] * t;
@@ -1020,10 +1064,9 @@ __device__ __forceinline__ float rhs_mixed(const DevOp& op, const SysParams& sp,
     if constexpr (SYS == SYS_HEAT) {
         float src = 0.f;
         if (sp.sol.kind == SOL_SINSIN) {
-            float u = __fmul_rn(sp.sol.Sf[0][i], sp.sol.Sf[1][j]);
-            if (sp.sol.dims == 3) u = __fmul_rn(u, sp.sol.Sf[2][k]);
-            u = __fmul_rn(u, etf);
-            src = __fsub_rn(-u, __fmul_rn(sp.kf, __fmul_rn((float)sp.sol.lapfac, u)));
+            const bool d3 = sp.sol.dims == 3;
+            src = sinsin_heat_src_f(sp.sol.Sf[0][i], sp.sol.Sf[1][j], d3 ? sp.sol.Sf[2][k] : 0.f, d3,
+                                    etf, sp.kf, (float)sp.sol.lapfac);
         }
         return fmaf(lap, sp.kf, src);
     } else {
@@ -1129,8 +1172,9 @@ __global__ void __launch_bounds__(256) k_stage_mixed(DevOp op, SysParams sp, Sta
 }
 
 // interior row from five register values (m2 .. p2 along the axis); the operation order is
-// interior_f's
-__device__ __forceinline__ float interior_row(const DevAxis& A, float m2, float m1, float c0,
+// interior_f's.  AX: DevAxis, or a register copy of its interior fields (IRow)
+template <class AX>
+__device__ __forceinline__ float interior_row(const AX& A, float m2, float m1, float c0,
                                               float p1, float p2)
 {
     if (A.width == 5) {
@@ -3189,15 +3233,12 @@ cudaError_t launch_stats_noalloc(const DevOp& op, const DevSol& sol, int prec, c
 // ===========================================================================================
 namespace
 {
-template <bool MIXED, int STAGE>
-__global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restrict__ B,
-                                                        const int* __restrict__ row_inst,
-                                                        int n_rows, const BatchTime* __restrict__ bt)
+// cut-cell row g of the batch's row list; COH: inputs written earlier in the same launch
+template <bool MIXED, int STAGE, bool COH>
+__device__ __forceinline__ void batch_cut_row(const BatchInst* __restrict__ B,
+                                              const int* __restrict__ row_inst, int g,
+                                              const BatchTime* __restrict__ bt)
 {
-    pdl_wait();
-    pdl_trigger();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n_rows) return;
     const int ii = row_inst[g];
     const BatchInst& I = B[ii];
     const DevOp& op = I.op;
@@ -3211,15 +3252,36 @@ __global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restr
     const void* in = STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa);
     // compacted in row order (the per-point stage) and, for the 2-D stage, at the point
     if constexpr (MIXED) {
-        const float v = STAGE == 0 ? closure_ff(A, row, p, PairU{(const float*)in, op.N}, R)
-                                   : closure_ff(A, row, p, (const float*)in, R);
+        float v;
+        if constexpr (COH)
+            v = STAGE == 0 ? closure_ff<CgPair, RScaled, 4>(A, row, p, CgPair{(const float*)in, op.N}, R)
+                           : closure_ff<CgF, RScaled, 4>(A, row, p, CgF{(const float*)in}, R);
+        else
+            v = STAGE == 0 ? closure_ff(A, row, p, PairU{(const float*)in, op.N}, R)
+                           : closure_ff(A, row, p, (const float*)in, R);
         ((float*)I.cval)[i] = v;
         if (I.rowv) ((float*)I.rowv)[(long long)d * op.N + p] = v;
     } else {
-        const double v = closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
+        double v;
+        if constexpr (COH)
+            v = closure64(A, row, p, CgD{(const double*)in}, R, (const double*)nullptr, 0.0, true);
+        else
+            v = closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
         ((double*)I.cval)[i] = v;
         if (I.rowv) ((double*)I.rowv)[(long long)d * op.N + p] = v;
     }
+}
+
+template <bool MIXED, int STAGE>
+__global__ void __launch_bounds__(128) k_batch_cut_rows(const BatchInst* __restrict__ B,
+                                                        const int* __restrict__ row_inst,
+                                                        int n_rows, const BatchTime* __restrict__ bt)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_rows) return;
+    batch_cut_row<MIXED, STAGE, false>(B, row_inst, g, bt);
 }
 
 template <int STAGE, bool MIXED, int WARPS>
@@ -3281,7 +3343,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_batch_stage(const BatchInst* __r
 }
 
 // interior row of the FP64 path from register values, in interior_d's operation order
-__device__ __forceinline__ double interior_row64(const DevAxis& A, double m2, double m1, double c0,
+template <class AX>
+__device__ __forceinline__ double interior_row64(const AX& A, double m2, double m1, double c0,
                                                 double p1, double p2)
 {
     if (A.width == 5) {
@@ -3310,65 +3373,63 @@ __device__ __forceinline__ double interior_row64(const DevAxis& A, double m2, do
 // single-system solve gives it.  Cut-cell row values come from the dense per-point array
 // (BatchInst::rowv) that k_batch_cut_rows fills.  No warp-collective operation is used, so
 // lanes past an instance's last point simply skip the tile.
-template <int STAGE, bool MIXED>
-__global__ void __launch_bounds__(128) k_batch_stage2d(const BatchInst* __restrict__ B,
-                                                       const int2* __restrict__ wt, int n_wt,
-                                                       const BatchTime* __restrict__ bt)
+// One warp tile (instance, first point) of the flat 2-D batched stage, PPL points per lane
+// in BATCH2D_TILE / (32 PPL) passes.  COH: the stage input and the cut-cell row values were written earlier in the
+// same launch by other blocks (the persistent solve), so they are loaded from L2.
+template <int STAGE, bool MIXED, bool COH, int PPL = BATCH2D_PPL>
+__device__ __forceinline__ void batch2d_tile(const BatchInst* __restrict__ B, int2 tl,
+                                             const BatchTime* __restrict__ bt, int lane)
 {
     using T = typename std::conditional<MIXED, float, double>::type;
-    pdl_wait();
-    pdl_trigger();
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n_wt; w += nwarps) {
-        const int2 tl = __ldg(wt + w); // (instance, first point of the tile)
-        const BatchInst& I = B[tl.x];
-        const DevOp& op = I.op;
-        const int n2 = op.it2, N = (int)op.N;
-        const int da = op.phys_of_it[1], db = op.phys_of_it[2]; // physical axes of it1, it2
-        const DevAxis& Aa = op.ax[da];
-        const DevAxis& Ab = op.ax[db];
-        const T* __restrict__ in = (const T*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
-        auto cl = [N](int x) { return min(max(x, 0), N - 1); };
-        const BatchTime& tm = bt[tl.x];
-        const int ts = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // stage time
-        const int tn = STAGE < 2 ? 1 : 2;                      // time of the stage output
-        StageArgs sa{};
-        sa.u0 = I.u0;
-        sa.acc = I.acc;
-        sa.s_out = STAGE == 1 ? I.sb : I.sa;
-        sa.cf = I.cf[STAGE];
-        sa.ci = I.ci[STAGE];
-        sa.cf_ff = I.cf_ff[STAGE];
-        sa.ci_ff = I.ci_ff[STAGE];
-        sa.t_stage = tm.t[ts];
-        sa.t_next = tm.t[tn];
-        sa.et_stage = tm.et[ts];
-        sa.et_next = tm.et[tn];
-        sa.etf_stage = (float)tm.et[ts];
-        const T* __restrict__ rowv = (const T*)I.rowv;
-        // the tile's 512 points in four passes of 128 (the parameters above are read once)
-        for (int sub = 0; sub < BATCH2D_TILE / (32 * BATCH2D_PPL); sub++) {
-        const int p0 = tl.y + sub * (32 * BATCH2D_PPL) + BATCH2D_PPL * lane;
+    const BatchInst& I = B[tl.x];
+    const DevOp& op = I.op;
+    const int n2 = op.it2, N = (int)op.N;
+    const int da = op.phys_of_it[1], db = op.phys_of_it[2]; // physical axes of it1, it2
+    const DevAxis& Aa = op.ax[da];
+    const DevAxis& Ab = op.ax[db];
+    const T* __restrict__ in = (const T*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
+    auto cl = [N](int x) { return min(max(x, 0), N - 1); };
+    auto LD = [in](int x) -> T { return COH ? __ldcg(in + x) : __ldg(in + x); };
+    const BatchTime& tm = bt[tl.x];
+    const int ts = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // stage time
+    const int tn = STAGE < 2 ? 1 : 2;                      // time of the stage output
+    StageArgs sa{};
+    sa.u0 = I.u0;
+    sa.acc = I.acc;
+    sa.s_out = STAGE == 1 ? I.sb : I.sa;
+    sa.cf = I.cf[STAGE];
+    sa.ci = I.ci[STAGE];
+    sa.cf_ff = I.cf_ff[STAGE];
+    sa.ci_ff = I.ci_ff[STAGE];
+    sa.t_stage = tm.t[ts];
+    sa.t_next = tm.t[tn];
+    sa.et_stage = tm.et[ts];
+    sa.et_next = tm.et[tn];
+    sa.etf_stage = (float)tm.et[ts];
+    const T* __restrict__ rowv = (const T*)I.rowv;
+    auto RV = [rowv](long long x) -> T { return COH ? __ldcg(rowv + x) : rowv[x]; };
+    // the parameters above are read once per tile
+    for (int sub = 0; sub < BATCH2D_TILE / (32 * PPL); sub++) {
+        const int p0 = tl.y + sub * (32 * PPL) + PPL * lane;
         if (p0 >= N) break;
-        T wv[BATCH2D_PPL + 4]; // it2 neighbours: points p0-2 .. p0+PPL+1
+        T wv[PPL + 4]; // it2 neighbours: points p0-2 .. p0+PPL+1
 #pragma unroll
-        for (int m = 0; m < BATCH2D_PPL + 4; m++) wv[m] = __ldg(in + cl(p0 - 2 + m));
-        T am2[BATCH2D_PPL], am1[BATCH2D_PPL], ap1[BATCH2D_PPL], ap2[BATCH2D_PPL]; // it1 neighbours
-        unsigned c[BATCH2D_PPL];
+        for (int m = 0; m < PPL + 4; m++) wv[m] = LD(cl(p0 - 2 + m));
+        T am2[PPL], am1[PPL], ap1[PPL], ap2[PPL]; // it1 neighbours
+        unsigned c[PPL];
 #pragma unroll
-        for (int q = 0; q < BATCH2D_PPL; q++) {
+        for (int q = 0; q < PPL; q++) {
             const int p = p0 + q;
-            am2[q] = __ldg(in + cl(p - 2 * n2));
-            am1[q] = __ldg(in + cl(p - n2));
-            ap1[q] = __ldg(in + cl(p + n2));
-            ap2[q] = __ldg(in + cl(p + 2 * n2));
+            am2[q] = LD(cl(p - 2 * n2));
+            am1[q] = LD(cl(p - n2));
+            ap1[q] = LD(cl(p + n2));
+            ap2[q] = LD(cl(p + 2 * n2));
             c[q] = p < N ? (unsigned)op.cls[p] : 0u;
         }
         const int i0 = p0 / n2;
         int ja = i0, jb = p0 - i0 * n2; // iteration coordinates (it1, it2) of the point
 #pragma unroll
-        for (int q = 0; q < BATCH2D_PPL; q++) {
+        for (int q = 0; q < PPL; q++) {
             const int p = p0 + q;
             if (p >= N) break;
             if (q > 0 && ++jb == n2) {
@@ -3380,16 +3441,20 @@ __global__ void __launch_bounds__(128) k_batch_stage2d(const BatchInst* __restri
             if constexpr (MIXED) {
                 if (ka == ROW_INTERIOR) va = interior_row(Aa, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
                 if (kb == ROW_INTERIOR) vb = interior_row(Ab, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
-                if (ka == ROW_WALL) va = wall32(Aa, (long long)p, ja, in);
-                if (kb == ROW_WALL) vb = wall32(Ab, (long long)p, jb, in);
+                if (ka == ROW_WALL) va = COH ? wall32(Aa, (long long)p, ja, CgF{(const float*)in}) : wall32(Aa, (long long)p, ja, in);
+                if (kb == ROW_WALL) vb = COH ? wall32(Ab, (long long)p, jb, CgF{(const float*)in}) : wall32(Ab, (long long)p, jb, in);
             } else {
                 if (ka == ROW_INTERIOR) va = interior_row64(Aa, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
                 if (kb == ROW_INTERIOR) vb = interior_row64(Ab, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
-                if (ka == ROW_WALL) va = wall64(Aa, (long long)p, ja, in, (const double*)nullptr, 0.0, true);
-                if (kb == ROW_WALL) vb = wall64(Ab, (long long)p, jb, in, (const double*)nullptr, 0.0, true);
+                if (ka == ROW_WALL)
+                    va = COH ? wall64(Aa, (long long)p, ja, CgD{(const double*)in}, (const double*)nullptr, 0.0, true)
+                             : wall64(Aa, (long long)p, ja, in, (const double*)nullptr, 0.0, true);
+                if (kb == ROW_WALL)
+                    vb = COH ? wall64(Ab, (long long)p, jb, CgD{(const double*)in}, (const double*)nullptr, 0.0, true)
+                             : wall64(Ab, (long long)p, jb, in, (const double*)nullptr, 0.0, true);
             }
-            if (ka == ROW_CLOSURE) va = rowv[(long long)da * N + p];
-            if (kb == ROW_CLOSURE) vb = rowv[(long long)db * N + p];
+            if (ka == ROW_CLOSURE) va = RV((long long)da * N + p);
+            if (kb == ROW_CLOSURE) vb = RV((long long)db * N + p);
             // physical coordinates (da < db; the third axis has extent 1)
             const int ijk[3] = {da == 0 ? ja : 0, da == 1 ? ja : (db == 1 ? jb : 0), db == 2 ? jb : 0};
             const bool face = (c[q] & CLS_DIRFACE) != 0;
@@ -3440,7 +3505,525 @@ __global__ void __launch_bounds__(128) k_batch_stage2d(const BatchInst* __restri
                 }
             }
         }
+    }
+}
+
+template <int STAGE, bool MIXED>
+__global__ void __launch_bounds__(128) k_batch_stage2d(const BatchInst* __restrict__ B,
+                                                       const int2* __restrict__ wt, int n_wt,
+                                                       const BatchTime* __restrict__ bt)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n_wt; w += nwarps)
+        batch2d_tile<STAGE, MIXED, false>(B, __ldg(wt + w), bt, lane);
+}
+
+// ---- split 2-D batched stage -------------------------------------------------------------
+// The points of a 2-D instance fall in two sets.  Uniform points have along each axis an
+// interior row or no row and are not on a Dirichlet face: their update is the same short
+// branch-free sequence everywhere.  Special points (a domain-wall or cut-cell row along
+// either axis, or a Dirichlet face) take the general path, each on a thread of its own, with
+// the cut-cell rows evaluated at the point (no separate row pass).  Warp tiles of
+// BATCH2D_TILE consecutive points cover every point and write the uniform ones; a list of
+// special points (instance, point, cut-cell row along it1, along it2) covers the rest.
+// Every value is formed by the same helpers, in the same order, as in the single-system
+// stage, so each instance gets its bits.
+
+// the interior fields of an axis in registers
+struct IRow {
+    int width, antisym;
+    float icf[5];
+    double ic[5];
+};
+__device__ __forceinline__ IRow irow_of(const DevAxis& A)
+{
+    IRow r;
+    r.width = A.width;
+    r.antisym = A.antisym;
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        r.icf[m] = A.icf[m];
+        r.ic[m] = A.ic[m];
+    }
+    return r;
+}
+// values a, b, t at the physical axes da < db and the third axis 3 - da - db, in physical order
+template <class T>
+__device__ __forceinline__ void phys_order(int dt3, T a, T b, T t, T& s0, T& s1, T& s2)
+{
+    s0 = dt3 == 0 ? t : a;
+    s1 = dt3 == 0 ? a : (dt3 == 1 ? t : b);
+    s2 = dt3 == 2 ? t : b;
+}
+
+// What a point update reads of its instance, loaded once per tile or point: the update's
+// stores could alias the instance record as far as the compiler knows, so fields read after
+// a store would be re-loaded.
+template <int STAGE, bool MIXED>
+struct BatchPt {
+    using T = typename std::conditional<MIXED, float, double>::type;
+    int N, n2, da, db, dt3;
+    bool sinsin, d3;
+    const float* Sfa;
+    const float* Sfb;
+    float Sft;
+    const double* Sda;
+    const double* Sdb;
+    double Sdt;
+    float kf, lapff;
+    double kd, lapfac;
+    double et_stage, et_next;
+    void* u0;
+    T* acc;
+    T* sout;
+    StageArgs sa;
+};
+template <int STAGE, bool MIXED>
+__device__ __forceinline__ BatchPt<STAGE, MIXED> batch_pt_of(const BatchInst& I, const BatchTime& tm)
+{
+    using T = typename BatchPt<STAGE, MIXED>::T;
+    BatchPt<STAGE, MIXED> P;
+    const DevOp& op = I.op;
+    P.N = (int)op.N;
+    P.n2 = op.it2;
+    P.da = op.phys_of_it[1];
+    P.db = op.phys_of_it[2];
+    P.dt3 = 3 - P.da - P.db;
+    const DevSol& sol = I.sp.sol;
+    P.sinsin = sol.kind == SOL_SINSIN;
+    P.d3 = sol.dims == 3;
+    const bool need_t = P.sinsin && (P.dt3 < 2 || P.d3);
+    P.Sfa = sol.Sf[P.da];
+    P.Sfb = sol.Sf[P.db];
+    P.Sft = MIXED && need_t ? sol.Sf[P.dt3][0] : 0.f;
+    P.Sda = sol.S[P.da];
+    P.Sdb = sol.S[P.db];
+    P.Sdt = need_t ? sol.S[P.dt3][0] : 0.0;
+    P.kf = I.sp.kf;
+    P.lapff = (float)sol.lapfac;
+    P.kd = I.sp.k;
+    P.lapfac = sol.lapfac;
+    const int ts = STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1); // stage time
+    const int tn = STAGE < 2 ? 1 : 2;                      // time of the stage output
+    P.et_stage = tm.et[ts];
+    P.et_next = tm.et[tn];
+    P.u0 = I.u0;
+    P.acc = (T*)I.acc;
+    P.sout = (T*)(STAGE == 1 ? I.sb : I.sa);
+    P.sa = StageArgs{};
+    P.sa.cf = I.cf[STAGE];
+    P.sa.ci = I.ci[STAGE];
+    P.sa.cf_ff = I.cf_ff[STAGE];
+    P.sa.ci_ff = I.ci_ff[STAGE];
+    P.sa.etf_stage = (float)tm.et[ts];
+    return P;
+}
+
+// the update of point p = (ia, ib) from its two axis values: right-hand side, RK4 stage,
+// the exact value on a Dirichlet face, stores
+template <int STAGE, bool MIXED, int DA = -1, int DB = -1>
+__device__ __forceinline__ void batch_point_update(const BatchPt<STAGE, MIXED>& P, int p, int ia,
+                                                   int ib, unsigned c,
+                                                   typename BatchPt<STAGE, MIXED>::T va,
+                                                   typename BatchPt<STAGE, MIXED>::T vb)
+{
+    const int dt3 = DA >= 0 ? 3 - DA - DB : P.dt3, db = DB >= 0 ? DB : P.db;
+    const bool face = (c & CLS_DIRFACE) != 0;
+    auto face_value = [&]() {
+        double s0, s1, s2;
+        phys_order(dt3, P.Sda[ia], P.d3 || db < 2 ? P.Sdb[ib] : 0.0, P.Sdt, s0, s1, s2);
+        return sinsin_value(s0, s1, s2, P.d3, P.et_next);
+    };
+    if constexpr (MIXED) {
+        const float lap = __fadd_rn(__fadd_rn(0.f, va), vb);
+        float rhs = 0.f;
+        if (c & 0x3Fu) {
+            float src = 0.f;
+            if (P.sinsin) {
+                float s0, s1, s2;
+                phys_order(dt3, P.Sfa[ia], P.d3 || db < 2 ? P.Sfb[ib] : 0.f, P.Sft, s0, s1, s2);
+                src = sinsin_heat_src_f(s0, s1, s2, P.d3, P.sa.etf_stage, P.kf, P.lapff);
+            }
+            rhs = fmaf(lap, P.kf, src);
         }
+        float a_out = 0.f, s_out = 0.f;
+        float2 u_out;
+        rk_mixed<STAGE>(P.sa, rhs, ld_u0<STAGE>(P.u0, P.N, p), STAGE == 0 ? 0.f : P.acc[p], a_out,
+                        s_out, u_out);
+        if (face) {
+            const double v = P.sinsin ? face_value() : 0.0;
+            if constexpr (STAGE < 3)
+                s_out = (float)v;
+            else
+                u_out = ff_from_double(v);
+        }
+        if constexpr (STAGE < 3) {
+            P.acc[p] = a_out;
+            P.sout[p] = s_out;
+        } else {
+            st_pair(P.u0, P.N, p, u_out);
+        }
+    } else {
+        const double lap = (0.0 + va) + vb;
+        double rhs = 0.0;
+        if (c & 0x3Fu) {
+            double src = 0.0;
+            if (P.sinsin) {
+                double s0, s1, s2;
+                phys_order(dt3, P.Sda[ia], P.d3 || db < 2 ? P.Sdb[ib] : 0.0, P.Sdt, s0, s1, s2);
+                const double u = sinsin_value(s0, s1, s2, P.d3, P.et_stage);
+                src = __dsub_rn(-u, __dmul_rn(P.kd, __dmul_rn(P.lapfac, u)));
+            }
+            rhs = fma(lap, P.kd, src);
+        }
+        double* const ud = (double*)P.u0;
+        if constexpr (STAGE < 3) {
+            P.acc[p] = STAGE == 0 ? P.sa.cf * rhs : fma(P.sa.cf, rhs, P.acc[p]);
+            double so = fma(P.sa.ci, rhs, ud[p]);
+            if (face) so = P.sinsin ? face_value() : 0.0;
+            P.sout[p] = so;
+        } else {
+            double un = ud[p] + fma(P.sa.cf, rhs, P.acc[p]);
+            if (face) un = P.sinsin ? face_value() : 0.0;
+            ud[p] = un;
+        }
+    }
+}
+
+// BATCH2D_TILE consecutive points of one instance, BATCH2D_PPL per lane; writes the uniform
+// points only.  DA, DB: the physical axes of it1, it2 when known at compile time (-1: read
+// from the instance).  CLAMP: neighbour loads that may fall outside the grid are clamped
+// into it (their values reach only points that are not written); tiles at least two it1
+// lines away from both ends of the grid load without clamping.  COH: inputs written
+// earlier in the same launch.
+template <int STAGE, bool MIXED, bool COH, int DA, int DB, bool CLAMP>
+__device__ __forceinline__ void uniform_tile_body(const BatchInst& I,
+                                                  const BatchPt<STAGE, MIXED>& P, int2 tl, int lane)
+{
+    using T = typename std::conditional<MIXED, float, double>::type;
+    constexpr int PPL = BATCH2D_PPL;
+    const DevOp& op = I.op;
+    const int da = DA >= 0 ? DA : P.da, db = DB >= 0 ? DB : P.db;
+    const IRow ra = irow_of(op.ax[da]), rb = irow_of(op.ax[db]);
+    const uint8_t* __restrict__ cls = op.cls;
+    const T* __restrict__ in = (const T*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
+    const int N = P.n2 * op.it1, n2 = P.n2;
+    auto LD = [in, N](int x) -> T {
+        if (CLAMP) x = min(max(x, 0), N - 1);
+        return COH ? __ldcg(in + x) : __ldg(in + x);
+    };
+    const int p0 = tl.y + PPL * lane;
+    if (CLAMP && p0 >= N) return;
+    T wv[PPL + 4]; // it2 neighbours: points p0-2 .. p0+PPL+1
+#pragma unroll
+    for (int m = 0; m < PPL + 4; m++) wv[m] = LD(p0 - 2 + m);
+    T am2[PPL], am1[PPL], ap1[PPL], ap2[PPL]; // it1 neighbours
+    unsigned c[PPL];
+#pragma unroll
+    for (int q = 0; q < PPL; q++) {
+        const int p = p0 + q;
+        am2[q] = LD(p - 2 * n2);
+        am1[q] = LD(p - n2);
+        ap1[q] = LD(p + n2);
+        ap2[q] = LD(p + 2 * n2);
+        c[q] = !CLAMP || p < N ? (unsigned)cls[p] : 0u;
+    }
+    const int i0 = p0 / n2;
+    int ia = i0, ib = p0 - i0 * n2; // iteration coordinates (it1, it2) of the point
+#pragma unroll
+    for (int q = 0; q < PPL; q++) {
+        const int p = p0 + q;
+        if (CLAMP && p >= N) break;
+        if (q > 0 && ++ib == n2) {
+            ib = 0;
+            ++ia;
+        }
+        const unsigned ka = (c[q] >> (2 * da)) & 3u, kb = (c[q] >> (2 * db)) & 3u;
+        if (ka >= ROW_CLOSURE || kb >= ROW_CLOSURE || (c[q] & CLS_DIRFACE)) continue;
+        T va = 0, vb = 0;
+        if constexpr (MIXED) {
+            if (ka == ROW_INTERIOR) va = interior_row(ra, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+            if (kb == ROW_INTERIOR) vb = interior_row(rb, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+        } else {
+            if (ka == ROW_INTERIOR) va = interior_row64(ra, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+            if (kb == ROW_INTERIOR) vb = interior_row64(rb, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+        }
+        batch_point_update<STAGE, MIXED, DA, DB>(P, p, ia, ib, c[q], va, vb);
+    }
+}
+
+// four consecutive floats at p (a multiple of four points from a field's start): one float4
+// access when the field is 16-byte aligned (`al`, warp-uniform), else four scalar ones
+template <bool COH>
+__device__ __forceinline__ float4 ld_quad(const float* p, bool al)
+{
+    if (al) return COH ? __ldcg((const float4*)p) : __ldg((const float4*)p);
+    if (COH) return make_float4(__ldcg(p), __ldcg(p + 1), __ldcg(p + 2), __ldcg(p + 3));
+    return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+}
+// the same for a field this thread wrote itself (plain loads)
+__device__ __forceinline__ float4 ld_quad_own(const float* p, bool al)
+{
+    if (al) return *(const float4*)p;
+    return make_float4(p[0], p[1], p[2], p[3]);
+}
+__device__ __forceinline__ void st_quad(float* p, bool al, float4 v)
+{
+    if (al) {
+        *(float4*)p = v;
+    } else {
+        p[0] = v.x;
+        p[1] = v.y;
+        p[2] = v.z;
+        p[3] = v.w;
+    }
+}
+__device__ __forceinline__ bool al16(const void* p) { return ((unsigned long long)p & 15u) == 0; }
+
+// The mixed uniform tile in the x-y plane, away from the grid's first and last two lines:
+// four consecutive points per lane (a quad starting at a multiple of four), each field read
+// and written as float4 where it is 16-byte aligned.  A quad whose four points are uniform is
+// stored whole, any other point by point (the special points are written by the other
+// kernel).
+template <int STAGE, bool COH>
+__device__ __forceinline__ void uniform_quads_xy(const BatchInst& I, const BatchPt<STAGE, true>& P,
+                                                 int2 tl, int lane)
+{
+    const DevOp& op = I.op;
+    const IRow ra = irow_of(op.ax[0]), rb = irow_of(op.ax[1]);
+    const float* __restrict__ in = (const float*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
+    const int n2 = P.n2, N = P.N;
+    float* const hi = (float*)P.u0;
+    float* const lo = hi + N;
+    const bool ain = al16(in), a1 = ain && (n2 & 3) == 0, aout = al16(P.sout), alo = al16(lo);
+#pragma unroll 1
+    for (int pass = 0; pass < BATCH_UTILE / 128; pass++) {
+        const int p0 = tl.y + pass * 128 + 4 * lane;
+        const float4 cw = ld_quad<COH>(in + p0, ain);
+        const float4 lw = ld_quad<COH>(in + p0 - 4, ain), rw = ld_quad<COH>(in + p0 + 4, ain);
+        const float4 m2 = ld_quad<COH>(in + p0 - 2 * n2, a1), m1 = ld_quad<COH>(in + p0 - n2, a1);
+        const float4 q1 = ld_quad<COH>(in + p0 + n2, a1), q2 = ld_quad<COH>(in + p0 + 2 * n2, a1);
+        const unsigned c4 = __ldg((const unsigned*)(op.cls + p0));
+        const float4 acc4 = STAGE == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_quad_own(P.acc + p0, true);
+        const float4 uh4 = STAGE == 0 ? cw : ld_quad_own(hi + p0, true);
+        float4 ul4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (STAGE == 3) ul4 = ld_quad_own(lo + p0, alo);
+        const float wv[8] = {lw.z, lw.w, cw.x, cw.y, cw.z, cw.w, rw.x, rw.y};
+        const float am2[4] = {m2.x, m2.y, m2.z, m2.w}, am1[4] = {m1.x, m1.y, m1.z, m1.w};
+        const float ap1[4] = {q1.x, q1.y, q1.z, q1.w}, ap2[4] = {q2.x, q2.y, q2.z, q2.w};
+        const float av[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
+        const float uh[4] = {uh4.x, uh4.y, uh4.z, uh4.w}, ul[4] = {ul4.x, ul4.y, ul4.z, ul4.w};
+        const int i0 = p0 / n2;
+        int ia = i0, ib = p0 - i0 * n2;
+        float ao[4], so[4];
+        float2 uo[4];
+        unsigned wmask = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (q > 0 && ++ib == n2) {
+                ib = 0;
+                ++ia;
+            }
+            const unsigned c = (c4 >> (8 * q)) & 0xFFu;
+            const unsigned ka = c & 3u, kb = (c >> 2) & 3u;
+            ao[q] = so[q] = 0.f;
+            uo[q] = make_float2(0.f, 0.f);
+            if (ka >= ROW_CLOSURE || kb >= ROW_CLOSURE || (c & CLS_DIRFACE)) continue;
+            wmask |= 1u << q;
+            float va = 0.f, vb = 0.f;
+            if (ka == ROW_INTERIOR) va = interior_row(ra, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+            if (kb == ROW_INTERIOR) vb = interior_row(rb, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+            const float lap = __fadd_rn(__fadd_rn(0.f, va), vb);
+            float rhs = 0.f;
+            if (c & 0x3Fu) {
+                float src = 0.f;
+                if (P.sinsin)
+                    src = sinsin_heat_src_f(P.Sfa[ia], P.Sfb[ib], P.Sft, P.d3, P.sa.etf_stage, P.kf, P.lapff);
+                rhs = fmaf(lap, P.kf, src);
+            }
+            rk_mixed<STAGE>(P.sa, rhs, make_float2(uh[q], ul[q]), av[q], ao[q], so[q], uo[q]);
+        }
+        if (wmask == 15u) {
+            if constexpr (STAGE < 3) {
+                st_quad(P.acc + p0, true, make_float4(ao[0], ao[1], ao[2], ao[3]));
+                st_quad(P.sout + p0, aout, make_float4(so[0], so[1], so[2], so[3]));
+            } else {
+                st_quad(hi + p0, true, make_float4(uo[0].x, uo[1].x, uo[2].x, uo[3].x));
+                st_quad(lo + p0, alo, make_float4(uo[0].y, uo[1].y, uo[2].y, uo[3].y));
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (wmask >> q & 1u) {
+                    if constexpr (STAGE < 3) {
+                        P.acc[p0 + q] = ao[q];
+                        P.sout[p0 + q] = so[q];
+                    } else {
+                        hi[p0 + q] = uo[q].x;
+                        lo[p0 + q] = uo[q].y;
+                    }
+                }
+        }
+    }
+}
+
+template <int STAGE, bool MIXED, bool COH>
+__device__ __forceinline__ void batch_uniform_tile(const BatchInst* __restrict__ B, int2 tl,
+                                                   const BatchTime* __restrict__ bt, int lane)
+{
+    const BatchInst& I = B[tl.x];
+    const BatchPt<STAGE, MIXED> P = batch_pt_of<STAGE, MIXED>(I, bt[tl.x]);
+    const int N = P.n2 * I.op.it1, n2 = P.n2;
+    // the x-y plane (the batched configuration's instances), away from the first and last
+    // two lines: no clamping, and quads in the mixed path
+    if (MIXED && P.da == 0 && P.db == 1 && tl.y >= 2 * n2 && tl.y + BATCH_UTILE + 2 * n2 <= N) {
+        if constexpr (MIXED) uniform_quads_xy<STAGE, COH>(I, P, tl, lane);
+        return;
+    }
+#pragma unroll 1
+    for (int pass = 0; pass < BATCH_UTILE / BATCH2D_TILE; pass++) {
+        const int2 t = make_int2(tl.x, tl.y + pass * BATCH2D_TILE);
+        if (t.y >= N) return;
+        if (P.da == 0 && P.db == 1) {
+            if (t.y >= 2 * n2 && t.y + BATCH2D_TILE + 2 * n2 <= N)
+                uniform_tile_body<STAGE, MIXED, COH, 0, 1, false>(I, P, t, lane);
+            else
+                uniform_tile_body<STAGE, MIXED, COH, 0, 1, true>(I, P, t, lane);
+        } else {
+            uniform_tile_body<STAGE, MIXED, COH, -1, -1, true>(I, P, t, lane);
+        }
+    }
+}
+
+// one special point: item (instance, point, cut-cell row along it1, along it2; -1 for none)
+template <int STAGE, bool MIXED, bool COH>
+__device__ __forceinline__ void batch_special_point(const BatchInst* __restrict__ B, int4 it,
+                                                    const BatchTime* __restrict__ bt)
+{
+    using T = typename std::conditional<MIXED, float, double>::type;
+    const BatchInst& I = B[it.x];
+    const DevOp& op = I.op;
+    const BatchTime& tm = bt[it.x];
+    const BatchPt<STAGE, MIXED> P = batch_pt_of<STAGE, MIXED>(I, tm);
+    const int p = it.y, n2 = P.n2;
+    const int ia = p / n2, ib = p - ia * n2;
+    const T* __restrict__ in = (const T*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
+    const unsigned c = op.cls[p];
+    // R at the stage time (t, t + dt/2, t + dt), as the cut-cell row pass forms it
+    const double etR = tm.et[STAGE == 0 ? 0 : (STAGE == 3 ? 2 : 1)];
+    T v[2];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const int d = a == 0 ? P.da : P.db;
+        const DevAxis& A = op.ax[d];
+        const unsigned k = (c >> (2 * d)) & 3u;
+        const int coord = a == 0 ? ia : ib;
+        const int s = a == 0 ? n2 : 1;
+        T x = 0;
+        if (k == ROW_INTERIOR) {
+            auto L = [&](int q) -> T { return COH ? __ldcg(in + q) : __ldg(in + q); };
+            if constexpr (MIXED)
+                x = interior_row(A, L(p - 2 * s), L(p - s), L(p), L(p + s), L(p + 2 * s));
+            else
+                x = interior_row64(A, L(p - 2 * s), L(p - s), L(p), L(p + s), L(p + 2 * s));
+        } else if (k == ROW_WALL) {
+            if constexpr (MIXED)
+                x = COH ? wall32(A, (long long)p, coord, CgF{(const float*)in}) : wall32(A, (long long)p, coord, in);
+            else
+                x = COH ? wall64(A, (long long)p, coord, CgD{(const double*)in}, (const double*)nullptr, 0.0, true)
+                        : wall64(A, (long long)p, coord, in, (const double*)nullptr, 0.0, true);
+        } else if (k == ROW_CLOSURE) {
+            const int row = a == 0 ? it.z : it.w;
+            const RScaled R{I.sp.sol.SR[d], etR};
+            if constexpr (MIXED) {
+                if constexpr (COH)
+                    x = STAGE == 0 ? closure_ff<CgPair, RScaled, 4>(A, row, p, CgPair{(const float*)in, op.N}, R)
+                                   : closure_ff<CgF, RScaled, 4>(A, row, p, CgF{(const float*)in}, R);
+                else
+                    x = STAGE == 0 ? closure_ff(A, row, p, PairU{(const float*)in, op.N}, R)
+                                   : closure_ff(A, row, p, (const float*)in, R);
+            } else {
+                if constexpr (COH)
+                    x = closure64(A, row, p, CgD{(const double*)in}, R, (const double*)nullptr, 0.0, true);
+                else
+                    x = closure64(A, row, p, (const double*)in, R, (const double*)nullptr, 0.0, true);
+            }
+        }
+        v[a] = x;
+    }
+    batch_point_update<STAGE, MIXED>(P, p, ia, ib, c, v[0], v[1]);
+}
+
+// one stage of the split form: the uniform tiles (a warp each) and the special points (a
+// thread each), two kernels with disjoint outputs that may run concurrently
+template <int STAGE, bool MIXED>
+__global__ void __launch_bounds__(128) k_batch_uniform(const BatchInst* __restrict__ B,
+                                                       const int2* __restrict__ ut, int n_ut,
+                                                       const BatchTime* __restrict__ bt)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int w = (int)blockIdx.x * 4 + (int)(threadIdx.x >> 5);
+    if (w < n_ut) batch_uniform_tile<STAGE, MIXED, false>(B, __ldg(ut + w), bt, threadIdx.x & 31);
+}
+
+template <int STAGE, bool MIXED>
+__global__ void __launch_bounds__(128) k_batch_special(const BatchInst* __restrict__ B,
+                                                       const int4* __restrict__ sp, int n_sp,
+                                                       const BatchTime* __restrict__ bt)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int g = blockIdx.x * 128 + threadIdx.x;
+    if (g < n_sp) batch_special_point<STAGE, MIXED, false>(B, __ldg(sp + g), bt);
+}
+
+// ---- the whole batched solve in one persistent launch -------------------------------------
+// Thread-block clusters of BATCH_CLUSTER blocks; each cluster owns a set of whole instances
+// (ctab[c] = its ranges of the special-point list psp and of the uniform-tile list put, the
+// instances balanced over the clusters by their work).  A cluster runs every RK4 step of its
+// instances, a stage at a time with a cluster barrier after each.  Instances are independent,
+// so no block ever waits for another cluster; the barrier is the hardware cluster barrier
+// (release / acquire at cluster scope), which every block reaches the same number of times.
+// Inputs written by other blocks of the cluster are loaded from L2 (the COH forms); the
+// arithmetic is the split stage's, so each instance gets the single-system bits.
+template <int STAGE, bool MIXED>
+__device__ __forceinline__ void persist_stage(cg::cluster_group& cl, const BatchInst* __restrict__ B,
+                                              const int4* __restrict__ psp,
+                                              const int2* __restrict__ put, int4 W,
+                                              const BatchTime* __restrict__ bt, int tid, int nth,
+                                              int warp, int nwarp, int lane)
+{
+#pragma unroll 1
+    for (int g = W.x + tid; g < W.y; g += nth) batch_special_point<STAGE, MIXED, true>(B, __ldg(psp + g), bt);
+#pragma unroll 1
+    for (int w = W.z + warp; w < W.w; w += nwarp) batch_uniform_tile<STAGE, MIXED, true>(B, __ldg(put + w), bt, lane);
+    cl.sync();
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 2) k_batch_persist(const BatchInst* __restrict__ B,
+                                                          const int4* __restrict__ psp,
+                                                          const int2* __restrict__ put,
+                                                          const int4* __restrict__ ctab,
+                                                          const BatchTime* __restrict__ times,
+                                                          int n_inst, int nsteps)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    const int cs = (int)cl.num_blocks();
+    const int4 W = __ldg(ctab + blockIdx.x / cs);
+    const int tid = (int)cl.block_rank() * blockDim.x + threadIdx.x, nth = cs * blockDim.x;
+    const int lane = threadIdx.x & 31, warp = tid >> 5, nwarp = nth >> 5;
+#pragma unroll 1
+    for (int k = 0; k < nsteps; k++) {
+        const BatchTime* bt = times + (long long)k * n_inst;
+        persist_stage<0, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
+        persist_stage<1, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
+        persist_stage<2, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
+        persist_stage<3, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
     }
 }
 
@@ -3471,7 +4054,7 @@ void batch_stage(const BatchInst* inst, const int4* tiles, int n_tiles, int cfg,
 template <int STAGE, bool MIXED>
 void batch_stage_all(const BatchInst* inst, const int* row_inst, int n_rows, const int4* tiles,
                      int n_tiles, int cfg, int grid, const int2* wt, int n_wt, int grid2d,
-                     const BatchTime* times, cudaStream_t s)
+                     const BatchSplit& sp, const BatchTime* times, cudaStream_t s)
 {
     if (n_rows) {
         k_batch_cut_rows<MIXED, STAGE><<<(n_rows + 127) / 128, 128, 0, s>>>(inst, row_inst, n_rows, times);
@@ -3482,32 +4065,107 @@ void batch_stage_all(const BatchInst* inst, const int* row_inst, int n_rows, con
         k_batch_stage2d<STAGE, MIXED><<<grid2d, 128, 0, s>>>(inst, wt, n_wt, times);
         ++g_launches;
     }
+    // the special points on a forked stream (a parallel branch when captured), the uniform
+    // tiles on s; s waits for both
+    const bool fork = sp.n_sp && sp.n_ut && sp.aux;
+    cudaStream_t ss = fork ? sp.aux : s;
+    if (fork) {
+        cudaEventRecord(sp.fork, s);
+        cudaStreamWaitEvent(sp.aux, sp.fork, 0);
+    }
+    if (sp.n_sp) {
+        k_batch_special<STAGE, MIXED><<<(sp.n_sp + 127) / 128, 128, 0, ss>>>(inst, sp.sp, sp.n_sp, times);
+        ++g_launches;
+    }
+    if (sp.n_ut) {
+        k_batch_uniform<STAGE, MIXED><<<(sp.n_ut + 3) / 4, 128, 0, s>>>(inst, sp.ut, sp.n_ut, times);
+        ++g_launches;
+    }
+    if (fork) {
+        cudaEventRecord(sp.join, sp.aux);
+        cudaStreamWaitEvent(s, sp.join, 0);
+    }
 }
 
 template <bool MIXED>
 void batch_step(const BatchInst* inst, const int* row_inst, int n_rows, const int4* tiles,
                 int n_tiles, int cfg, int grid, const int2* wt, int n_wt, int grid2d,
-                const BatchTime* times, cudaStream_t s)
+                const BatchSplit& sp, const BatchTime* times, cudaStream_t s)
 {
-    batch_stage_all<0, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
-    batch_stage_all<1, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
-    batch_stage_all<2, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
-    batch_stage_all<3, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, times, s);
+    batch_stage_all<0, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, sp, times, s);
+    batch_stage_all<1, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, sp, times, s);
+    batch_stage_all<2, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, sp, times, s);
+    batch_stage_all<3, MIXED>(inst, row_inst, n_rows, tiles, n_tiles, cfg, grid, wt, n_wt, grid2d, sp, times, s);
 }
 } // namespace
 
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
                               const int4* tiles, int n_tiles, int tile_cfg, int grid,
-                              const int2* wtiles, int n_wtiles, int grid2d,
+                              const int2* wtiles, int n_wtiles, int grid2d, const BatchSplit& sp,
                               const BatchTime* times, int prec, cudaStream_t s)
 {
     if (prec == PREC_MIXED)
         batch_step<true>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, wtiles, n_wtiles,
-                         grid2d, times, s);
+                         grid2d, sp, times, s);
     else
         batch_step<false>(inst, row_inst, n_rows, tiles, n_tiles, tile_cfg, grid, wtiles, n_wtiles,
-                          grid2d, times, s);
+                          grid2d, sp, times, s);
     return cudaGetLastError();
+}
+
+namespace
+{
+template <bool MIXED>
+cudaLaunchConfig_t persist_config(int n_clusters, cudaStream_t s, cudaLaunchAttribute* at)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(n_clusters * BATCH_CLUSTER);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = BATCH_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+} // namespace
+
+int batch_persist_clusters(int prec)
+{
+    cudaLaunchAttribute at[1];
+    int n = 0;
+    cudaError_t e;
+    if (prec == PREC_MIXED) {
+        auto cfg = persist_config<true>(1, nullptr, at);
+        e = cudaOccupancyMaxActiveClusters(&n, k_batch_persist<true>, &cfg);
+    } else {
+        auto cfg = persist_config<false>(1, nullptr, at);
+        e = cudaOccupancyMaxActiveClusters(&n, k_batch_persist<false>, &cfg);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+cudaError_t launch_batch_persist(const BatchInst* inst, const int4* psp, const int2* put,
+                                 const int4* ctab, int n_clusters, const BatchTime* times,
+                                 int n_inst, int nsteps, int prec, cudaStream_t s)
+{
+    cudaLaunchAttribute at[1];
+    ++g_launches;
+    if (prec == PREC_MIXED) {
+        auto cfg = persist_config<true>(n_clusters, s, at);
+        return cudaLaunchKernelEx(&cfg, k_batch_persist<true>, inst, psp, put, ctab,
+                                  times, n_inst, nsteps);
+    }
+    auto cfg = persist_config<false>(n_clusters, s, at);
+    return cudaLaunchKernelEx(&cfg, k_batch_persist<false>, inst, psp, put, ctab, times,
+                              n_inst, nsteps);
 }
 
 int batch_stage2d_grid(int prec, int n_wtiles)

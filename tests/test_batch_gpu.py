@@ -3,9 +3,10 @@ sizes and circle geometries advanced together under one captured CUDA graph.
 
 The batch runs the single-system stage arithmetic with the same time points and boundary
 products, so every instance must come out bit-identical to shoccs_system_rk4 run on that
-instance alone -- in FP64 and in the mixed path, through the flat 2-D stage (SHOCCS_BATCH_KERNEL=flat; the
-default for mixed 2-D instances) and the per-point stage (SHOCCS_BATCH_KERNEL=point; the
-default for FP64) with every tile shape, and across graph replays.  The instances are drawn by the batched configuration's own generator
+instance alone -- in FP64 and in the mixed path, through the split 2-D stage (uniform tiles
+and special points; the default), the same in one persistent launch for the whole solve
+(SHOCCS_BATCH_PERSIST=1), the flat 2-D stage (SHOCCS_BATCH_KERNEL=flat) and the per-point
+stage (SHOCCS_BATCH_KERNEL=point) with every tile shape, and across graph replays.  The instances are drawn by the batched configuration's own generator
 (shoccs_gb300.workloads.batch_heat_2d) with smaller grids.
 """
 import numpy as np
@@ -34,10 +35,11 @@ def _state(sys_, p):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", ["flat", "point"])
+@pytest.mark.parametrize("kernel", ["split", "persist", "flat", "point"])
 @pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
 def test_batch_matches_single_systems_bitwise(prec, kernel, monkeypatch):
-    monkeypatch.setenv("SHOCCS_BATCH_KERNEL", kernel)
+    monkeypatch.setenv("SHOCCS_BATCH_KERNEL", "split" if kernel == "persist" else kernel)
+    monkeypatch.setenv("SHOCCS_BATCH_PERSIST", "1" if kernel == "persist" else "0")
     insts = _instances()
     pb, sb = _make(insts, prec)
     ps, ss = _make(insts, prec)
@@ -53,6 +55,33 @@ def test_batch_matches_single_systems_bitwise(prec, kernel, monkeypatch):
             assert np.array_equal(a, b), i
     info = batch.info()
     assert info["instances"] == len(insts) and info["graph_nodes"] > 0
+    if kernel == "persist":  # the whole solve is one launch
+        assert info["graph_nodes"] == 1 and info["grid"] % 8 == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("persist", [0, 1])
+@pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
+def test_split_batch_many_instances(prec, persist, monkeypatch):
+    """96 instances: the split stage, and the persistent launch whose clusters each own
+    several instances of unequal work, give every instance its single-system solve bit for
+    bit."""
+    monkeypatch.setenv("SHOCCS_BATCH_KERNEL", "split")
+    monkeypatch.setenv("SHOCCS_BATCH_PERSIST", str(persist))
+    insts = W.batch_heat_2d(count=96, nmin=32, nmax=56)
+    pb, sb = _make(insts, prec)
+    ps, ss = _make(insts, prec)
+    batch = S.Batch(sb)
+    dts = [it["dt"] for it in insts]
+    batch.rk4(0.0, dts, 9)
+    info = batch.info()
+    if persist:
+        assert info["graph_nodes"] == 1 and info["grid"] // 8 < len(insts)
+    for s, dt in zip(ss, dts):
+        s.rk4(0.0, dt, 9)
+    for i in range(len(insts)):
+        for a, b in zip(_state(sb[i], pb[i]), _state(ss[i], ps[i])):
+            assert np.array_equal(a, b), i
 
 
 @pytest.mark.gpu
