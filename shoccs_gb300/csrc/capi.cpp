@@ -1385,6 +1385,11 @@ struct shoccs_batch {
     int n_wtiles = 0, grid2d = 1;
     // or to the split stage (uniform tiles, special points; no cut-cell row pass)
     BatchSplit split;
+    // every instance split: groups of consecutive instances whose fields fit well inside L2
+    // (SHOCCS_BATCH_GROUP_MB), each advanced through all its steps before the next, so that
+    // a group's stages find their inputs in L2 (instances are independent: the order of
+    // their work does not matter)
+    std::vector<BatchSplit> groups;
     // every instance split 2-D and SHOCCS_BATCH_PERSIST=1: the whole solve in one persistent
     // launch of n_clusters clusters (kernels.cu k_batch_persist), cluster c owning the
     // instances of ctab[c]
@@ -1524,9 +1529,14 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
     std::vector<std::pair<int, int>> inst_ut(n), inst_sp(n); // (begin, end) of each instance
     bool all2d = true;
     // SHOCCS_BATCH_KERNEL=point sends every instance through the per-point stage, =flat the
-    // 2-D instances through the flat stage; by default they take the split stage
+    // 2-D instances through the flat stage, =split through the split stage.  By default the
+    // 2-D instances of a mixed batch take the split stage and FP64 batches the per-point
+    // stage (with FP64 arithmetic at a small fraction of the FP32 rate, the 2-D forms'
+    // register-heavy bodies measured slower there: 212 ms against 164 ms for the batched
+    // configuration's 200 steps)
     const char* kenv = std::getenv("SHOCCS_BATCH_KERNEL");
-    const std::string kname = kenv ? std::string(kenv) : std::string("split");
+    const std::string kname =
+        kenv ? std::string(kenv) : std::string(B->prec == PREC_MIXED ? "split" : "point");
     const bool allow2d = kname == "flat" || kname == "split";
     const bool use_split = kname == "split";
     for (int i = 0; i < n; i++) {
@@ -1557,13 +1567,23 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         const bool flat2d = allow2d && op.it0 == 1 && op.it1 > 1 && op.phys_of_it[1] >= 0 &&
                             op.phys_of_it[2] >= 0 && op.N < (1LL << 31) - 256;
         all2d = all2d && flat2d;
-        if (flat2d) {
+        if (flat2d && !use_split) {
             // cut-cell row values at their points, per axis (3 x N, the batch's own buffer)
             void* rv = nullptr;
             const size_t elem = B->prec == PREC_MIXED ? sizeof(float) : sizeof(double);
             SH_CUDA(B->mem.alloc((size_t)3 * op.N * elem, &rv));
             SH_CUDA(cudaMemset(rv, 0, (size_t)3 * op.N * elem));
             I.rowv = rv;
+        }
+        if (flat2d && use_split && B->prec == PREC_MIXED && op.phys_of_it[1] == 0 &&
+            op.phys_of_it[2] == 1 && S->sp.sol.kind == SHOCCS_SOL_SINSIN && S->sp.sol.dims != 3) {
+            // the source's spatial factor at every point (the batch's own buffer)
+            void* s2 = nullptr;
+            SH_CUDA(B->mem.alloc((size_t)op.N * sizeof(float), &s2));
+            SH_CUDA(launch_sinsin_xy(S->sp.sol.Sf[0], S->sp.sol.Sf[1], op.it1, op.it2, (float*)s2, nullptr));
+            I.s2f = (const float*)s2;
+        }
+        if (flat2d) {
             if ((long long)wtiles.size() + op.N / BATCH2D_TILE + 1 >= (1LL << 31))
                 return fail(SHOCCS_EUNSUPPORTED, "batch above 2^31 tiles");
             if (use_split) {
@@ -1650,15 +1670,51 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         std::copy(tmp.begin(), tmp.end(), v.begin() + b);
         std::copy(tk.begin(), tk.end(), kind.begin() + b);
     };
+    // groups (every instance split): consecutive instances up to the byte budget
+    std::vector<std::pair<int, int>> grp; // (first, end) instance of each group
+    if (all2d && use_split && n > 1) {
+        const char* genv = std::getenv("SHOCCS_BATCH_GROUP_MB");
+        const double budget = (genv ? std::atof(genv) : 48.0) * 1048576.0;
+        const double per_pt = B->prec == PREC_MIXED ? 25.0 : 33.0; // field bytes per point
+        int first = 0;
+        double bytes = 0.0;
+        for (int i = 0; i < n; i++) {
+            const double b = per_pt * (double)B->h_inst[i].op.N;
+            if (i > first && bytes + b > budget) {
+                grp.emplace_back(first, i);
+                first = i;
+                bytes = 0.0;
+            }
+            bytes += b;
+        }
+        grp.emplace_back(first, n);
+        if (budget <= 0.0 || grp.size() < 2) grp.clear();
+    }
     {
         std::vector<int4> sps = sp;
         std::vector<int> spk = sp_kind;
-        by_kind(sps, spk, 0, sps.size());
+        if (grp.empty()) {
+            by_kind(sps, spk, 0, sps.size());
+        } else {
+            for (const auto& g : grp)
+                by_kind(sps, spk, (size_t)inst_sp[g.first].first, (size_t)inst_sp[g.second - 1].second);
+        }
         SH_CUDA(B->mem.put(sps, &B->split.sp, s));
     }
     SH_CUDA(B->mem.put(ut, &B->split.ut, s));
     B->split.n_ut = (int)ut.size();
     B->split.n_sp = (int)sp.size();
+
+    for (const auto& g : grp) {
+        BatchSplit G;
+        const int u0 = inst_ut[g.first].first, u1 = inst_ut[g.second - 1].second;
+        const int s0 = inst_sp[g.first].first, s1 = inst_sp[g.second - 1].second;
+        G.ut = B->split.ut + u0;
+        G.n_ut = u1 - u0;
+        G.sp = B->split.sp + s0;
+        G.n_sp = s1 - s0;
+        B->groups.push_back(G);
+    }
     SH_CUDA(B->mem.put(r_inst, &B->d_r_inst, s));
     B->n_r = (int)(r_inst.size() / 3);
     // SHOCCS_BATCH_PERSIST=0 keeps a batch of 2-D instances on the launch-per-stage kernels
@@ -1713,6 +1769,11 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         SH_CUDA(cudaStreamCreateWithFlags(&B->split.aux, cudaStreamNonBlocking));
         SH_CUDA(cudaEventCreateWithFlags(&B->split.fork, cudaEventDisableTiming));
         SH_CUDA(cudaEventCreateWithFlags(&B->split.join, cudaEventDisableTiming));
+        for (auto& G : B->groups) {
+            G.aux = B->split.aux;
+            G.fork = B->split.fork;
+            G.join = B->split.join;
+        }
     }
     if (auto st = batch_autotune(B.get(), s); st != SHOCCS_OK) return st;
     SH_CUDA(cudaStreamSynchronize(s));
@@ -1748,7 +1809,12 @@ shoccs_status shoccs_batch_rk4(shoccs_batch* B, const double* t0, const double* 
         if (B->persist)
             e = launch_batch_persist(B->d_inst, B->d_psp, B->d_put, B->d_ctab, B->n_clusters,
                                      B->d_times, n, nsteps, B->prec, B->cap);
-        for (int k = 0; k < nsteps && e == cudaSuccess && !B->persist; k++)
+        for (size_t g = 0; g < B->groups.size() && !B->persist; g++)
+            for (int k = 0; k < nsteps && e == cudaSuccess; k++)
+                e = launch_batch_step(B->d_inst, B->d_row_inst, 0, nullptr, 0, B->cfg, B->grid,
+                                      nullptr, 0, B->grid2d, B->groups[g],
+                                      B->d_times + (size_t)k * n, B->prec, B->cap);
+        for (int k = 0; k < nsteps && e == cudaSuccess && !B->persist && B->groups.empty(); k++)
             e = launch_batch_step(B->d_inst, B->d_row_inst, B->n_rows, B->d_tiles[B->cfg],
                                   B->n_tiles[B->cfg], B->cfg, B->grid, B->d_wtiles,
                                   B->n_wtiles, B->grid2d, B->split, B->d_times + (size_t)k * n,

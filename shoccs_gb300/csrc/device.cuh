@@ -179,6 +179,8 @@ struct BatchInst {
     void* sb;
     void* cval;
     void* rowv;              // 2-D instances: cut-cell row values at their points (3 x N), else null
+    const float* s2f;        // mixed x-y instances of the split stage: the sin-sin tables'
+                             // FP32 product Sf_x[i] * Sf_y[j] at every point, else null
     double* R[3];
     double cf[4], ci[4];     // dt*rkf[s], dt*rki[s+1] (ci[3] unused)
     float2 cf_ff[4], ci_ff[4];
@@ -197,7 +199,7 @@ constexpr int BATCH_TILE_WARPS[4] = {1, 2, 4, 8};
 // the split 2-D stage's work lists: uniform tiles (instance, first point; BATCH_UTILE points
 // each, a multiple of BATCH2D_TILE) and special points (instance, point, cut-cell row along
 // it1, along it2; -1: none)
-constexpr int BATCH_UTILE = 256;
+constexpr int BATCH_UTILE = 128;
 struct BatchSplit {
     const int2* ut = nullptr;
     int n_ut = 0;
@@ -211,6 +213,9 @@ struct BatchSplit {
 // (instances that are not 2-D) and the flat 2-D stage over the warp tiles `wtiles`
 // (instance, first point; BATCH2D_TILE points each), or the split 2-D stage, which needs no
 // cut-cell row pass
+// out[i n2 + j] = fl(sx[i] * sy[j]) over an n1 x n2 grid
+cudaError_t launch_sinsin_xy(const float* sx, const float* sy, int n1, int n2, float* out,
+                             cudaStream_t s);
 cudaError_t launch_batch_step(const BatchInst* inst, const int* row_inst, int n_rows,
                               const int4* tiles, int n_tiles, int tile_cfg, int grid,
                               const int2* wtiles, int n_wtiles, int grid2d, const BatchSplit& sp,

@@ -420,14 +420,20 @@ __device__ __forceinline__ double sinsin_value(double s0, double s1, double s2, 
     if (dims3) v = v * s2;
     return v * et;
 }
-// the mixed heat path's manufactured source -u - k lapfac u, u = (s0 s1 [s2]) e^-t in FP32
-__device__ __forceinline__ float sinsin_heat_src_f(float s0, float s1, float s2, bool dims3,
-                                                   float etf, float kf, float lapff)
+// the mixed heat path's manufactured source -u - k lapfac u, u = (s0 s1 [s2]) e^-t in FP32;
+// s01 = fl(s0 s1)
+__device__ __forceinline__ float sinsin_heat_src_p(float s01, float s2, bool dims3, float etf,
+                                                   float kf, float lapff)
 {
-    float u = __fmul_rn(s0, s1);
+    float u = s01;
     if (dims3) u = __fmul_rn(u, s2);
     u = __fmul_rn(u, etf);
     return __fsub_rn(-u, __fmul_rn(kf, __fmul_rn(lapff, u)));
+}
+__device__ __forceinline__ float sinsin_heat_src_f(float s0, float s1, float s2, bool dims3,
+                                                   float etf, float kf, float lapff)
+{
+    return sinsin_heat_src_p(__fmul_rn(s0, s1), s2, dims3, etf, kf, lapff);
 }
 
 __device__ __forceinline__ double sol_at(const DevSol& s, double t, double et, const double x[3],
@@ -3783,17 +3789,22 @@ __device__ __forceinline__ void st_quad(float* p, bool al, float4 v)
 }
 __device__ __forceinline__ bool al16(const void* p) { return ((unsigned long long)p & 15u) == 0; }
 
-// The mixed uniform tile in the x-y plane, away from the grid's first and last two lines:
-// four consecutive points per lane (a quad starting at a multiple of four), each field read
-// and written as float4 where it is 16-byte aligned.  A quad whose four points are uniform is
+// The mixed uniform tile in the x-y plane (sin-sin solution), away from the grid's first and
+// last two lines: four consecutive points per lane (a quad starting at a multiple of four),
+// each field read and written as float4 where it is 16-byte aligned, and the source's
+// spatial factor read from the instance's product table s2f.  A quad whose four points are uniform is
 // stored whole, any other point by point (the special points are written by the other
 // kernel).
-template <int STAGE, bool COH>
+template <int STAGE, bool COH, bool SYM5>
 __device__ __forceinline__ void uniform_quads_xy(const BatchInst& I, const BatchPt<STAGE, true>& P,
                                                  int2 tl, int lane)
 {
     const DevOp& op = I.op;
     const IRow ra = irow_of(op.ax[0]), rb = irow_of(op.ax[1]);
+    // the interior rows: five-point symmetric ones (E4_2) inline, any other through interior_row
+    auto row = [](const IRow& r, float m2, float m1, float c0, float p1, float p2) {
+        return SYM5 ? sym5(r.icf[1], r.icf[0], m2, m1, c0, p1, p2) : interior_row(r, m2, m1, c0, p1, p2);
+    };
     const float* __restrict__ in = (const float*)(STAGE == 0 ? I.u0 : (STAGE == 2 ? I.sb : I.sa));
     const int n2 = P.n2, N = P.N;
     float* const hi = (float*)P.u0;
@@ -3816,17 +3827,13 @@ __device__ __forceinline__ void uniform_quads_xy(const BatchInst& I, const Batch
         const float ap1[4] = {q1.x, q1.y, q1.z, q1.w}, ap2[4] = {q2.x, q2.y, q2.z, q2.w};
         const float av[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
         const float uh[4] = {uh4.x, uh4.y, uh4.z, uh4.w}, ul[4] = {ul4.x, ul4.y, ul4.z, ul4.w};
-        const int i0 = p0 / n2;
-        int ia = i0, ib = p0 - i0 * n2;
+        const float4 s24 = __ldg((const float4*)(I.s2f + p0));
+        const float s2[4] = {s24.x, s24.y, s24.z, s24.w};
         float ao[4], so[4];
         float2 uo[4];
         unsigned wmask = 0;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            if (q > 0 && ++ib == n2) {
-                ib = 0;
-                ++ia;
-            }
             const unsigned c = (c4 >> (8 * q)) & 0xFFu;
             const unsigned ka = c & 3u, kb = (c >> 2) & 3u;
             ao[q] = so[q] = 0.f;
@@ -3834,16 +3841,12 @@ __device__ __forceinline__ void uniform_quads_xy(const BatchInst& I, const Batch
             if (ka >= ROW_CLOSURE || kb >= ROW_CLOSURE || (c & CLS_DIRFACE)) continue;
             wmask |= 1u << q;
             float va = 0.f, vb = 0.f;
-            if (ka == ROW_INTERIOR) va = interior_row(ra, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
-            if (kb == ROW_INTERIOR) vb = interior_row(rb, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
+            if (ka == ROW_INTERIOR) va = row(ra, am2[q], am1[q], wv[q + 2], ap1[q], ap2[q]);
+            if (kb == ROW_INTERIOR) vb = row(rb, wv[q], wv[q + 1], wv[q + 2], wv[q + 3], wv[q + 4]);
             const float lap = __fadd_rn(__fadd_rn(0.f, va), vb);
             float rhs = 0.f;
-            if (c & 0x3Fu) {
-                float src = 0.f;
-                if (P.sinsin)
-                    src = sinsin_heat_src_f(P.Sfa[ia], P.Sfb[ib], P.Sft, P.d3, P.sa.etf_stage, P.kf, P.lapff);
-                rhs = fmaf(lap, P.kf, src);
-            }
+            if (c & 0x3Fu)
+                rhs = fmaf(lap, P.kf, sinsin_heat_src_p(s2[q], 0.f, false, P.sa.etf_stage, P.kf, P.lapff));
             rk_mixed<STAGE>(P.sa, rhs, make_float2(uh[q], ul[q]), av[q], ao[q], so[q], uo[q]);
         }
         if (wmask == 15u) {
@@ -3879,8 +3882,15 @@ __device__ __forceinline__ void batch_uniform_tile(const BatchInst* __restrict__
     const int N = P.n2 * I.op.it1, n2 = P.n2;
     // the x-y plane (the batched configuration's instances), away from the first and last
     // two lines: no clamping, and quads in the mixed path
-    if (MIXED && P.da == 0 && P.db == 1 && tl.y >= 2 * n2 && tl.y + BATCH_UTILE + 2 * n2 <= N) {
-        if constexpr (MIXED) uniform_quads_xy<STAGE, COH>(I, P, tl, lane);
+    if (MIXED && I.s2f && P.da == 0 && P.db == 1 && tl.y >= 2 * n2 && tl.y + BATCH_UTILE + 2 * n2 <= N) {
+        if constexpr (MIXED) {
+            const DevAxis& A0 = I.op.ax[0];
+            const DevAxis& A1 = I.op.ax[1];
+            if (A0.width == 5 && !A0.antisym && A1.width == 5 && !A1.antisym)
+                uniform_quads_xy<STAGE, COH, true>(I, P, tl, lane);
+            else
+                uniform_quads_xy<STAGE, COH, false>(I, P, tl, lane);
+        }
         return;
     }
 #pragma unroll 1
@@ -3959,8 +3969,9 @@ __device__ __forceinline__ void batch_special_point(const BatchInst* __restrict_
 
 // one stage of the split form: the uniform tiles (a warp each) and the special points (a
 // thread each), two kernels with disjoint outputs that may run concurrently
+// (mixed: 64 registers, measured faster than the unbounded 80-94 at 128-point tiles)
 template <int STAGE, bool MIXED>
-__global__ void __launch_bounds__(128) k_batch_uniform(const BatchInst* __restrict__ B,
+__global__ void __launch_bounds__(128, MIXED ? 8 : 1) k_batch_uniform(const BatchInst* __restrict__ B,
                                                        const int2* __restrict__ ut, int n_ut,
                                                        const BatchTime* __restrict__ bt)
 {
@@ -4025,6 +4036,15 @@ __global__ void __launch_bounds__(256, 2) k_batch_persist(const BatchInst* __res
         persist_stage<2, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
         persist_stage<3, MIXED>(cl, B, psp, put, W, bt, tid, nth, warp, nwarp, lane);
     }
+}
+
+__global__ void k_sinsin_xy(const float* __restrict__ sx, const float* __restrict__ sy, int n1,
+                            int n2, float* __restrict__ out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n1 * n2) return;
+    const int i = p / n2;
+    out[p] = __fmul_rn(sx[i], sy[p - i * n2]);
 }
 
 __global__ void k_batch_finish(const BatchInst* __restrict__ B, const BatchTime* __restrict__ last,
@@ -4213,6 +4233,17 @@ int batch_stage_grid(int tile_cfg, int prec, int n_tiles)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * warps, 0);
     const long long g = (long long)std::max(1, per_sm) * std::max(1, sms);
     return (int)std::max(1LL, std::min<long long>(g, n_tiles));
+}
+
+cudaError_t launch_sinsin_xy(const float* sx, const float* sy, int n1, int n2, float* out,
+                             cudaStream_t s)
+{
+    const long long n = (long long)n1 * n2;
+    if (n > 0) {
+        k_sinsin_xy<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(sx, sy, n1, n2, out);
+        ++g_launches;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_finish(const BatchInst* inst, int n_inst, const BatchTime* last,

@@ -60,14 +60,16 @@ def test_batch_matches_single_systems_bitwise(prec, kernel, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("persist", [0, 1])
+@pytest.mark.parametrize("mode", ["one_group", "groups", "persist"])
 @pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
-def test_split_batch_many_instances(prec, persist, monkeypatch):
-    """96 instances: the split stage, and the persistent launch whose clusters each own
-    several instances of unequal work, give every instance its single-system solve bit for
-    bit."""
+def test_split_batch_many_instances(prec, mode, monkeypatch):
+    """96 instances: the split stage over the whole batch at once, over groups of a few
+    instances each advanced through all its steps in turn (a 0.2 MB group budget), and the
+    persistent launch whose clusters each own several instances of unequal work, give every
+    instance its single-system solve bit for bit."""
     monkeypatch.setenv("SHOCCS_BATCH_KERNEL", "split")
-    monkeypatch.setenv("SHOCCS_BATCH_PERSIST", str(persist))
+    monkeypatch.setenv("SHOCCS_BATCH_PERSIST", "1" if mode == "persist" else "0")
+    monkeypatch.setenv("SHOCCS_BATCH_GROUP_MB", "0.2" if mode == "groups" else "0")
     insts = W.batch_heat_2d(count=96, nmin=32, nmax=56)
     pb, sb = _make(insts, prec)
     ps, ss = _make(insts, prec)
@@ -75,8 +77,10 @@ def test_split_batch_many_instances(prec, persist, monkeypatch):
     dts = [it["dt"] for it in insts]
     batch.rk4(0.0, dts, 9)
     info = batch.info()
-    if persist:
+    if mode == "persist":
         assert info["graph_nodes"] == 1 and info["grid"] // 8 < len(insts)
+    if mode == "groups":  # two kernels per stage, and the groups one after another
+        assert info["graph_nodes"] > 2 * 4 * 9 * 4
     for s, dt in zip(ss, dts):
         s.rk4(0.0, dt, 9)
     for i in range(len(insts)):
