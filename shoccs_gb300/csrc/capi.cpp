@@ -514,12 +514,13 @@ static bool line_records_fit(const DevOp& op)
     const int nz = op.it2;
     const WallBlock& L = op.ax[2].wall[0];
     const WallBlock& R = op.ax[2].wall[1];
-    if (nz < 8) return false;
-    if (L.rows && (L.has_n || L.rows > 6 || L.cols > 7 || L.col0 != 0 || L.first_row < 0 ||
-                   2 * (L.first_row + L.rows - 1) >= nz))
+    // the record holds the wall rows of z = 0..7 and nz-8 .. nz-1
+    if (nz < 16) return false;
+    if (L.rows && (L.has_n || L.cols > 7 || L.col0 != 0 || L.first_row < 0 ||
+                   L.first_row + L.rows > 8))
         return false;
-    if (R.rows && (R.has_n || R.rows > 6 || R.cols > 7 || R.col0 + R.cols != nz ||
-                   2 * R.first_row < nz || R.first_row + R.rows > nz))
+    if (R.rows && (R.has_n || R.cols > 7 || R.col0 + R.cols != nz || R.first_row < nz - 8 ||
+                   R.first_row + R.rows > nz))
         return false;
     return true;
 }
@@ -817,7 +818,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
                 void* z = nullptr;
                 SH_CUDA(S->mem.alloc((size_t)3 * N * sizeof(float), &z));
                 S->b.rowv = (float*)z;
-                SH_CUDA(S->mem.alloc((size_t)it[0] * it[1] * 16 * sizeof(float), &z));
+                SH_CUDA(S->mem.alloc((size_t)it[0] * it[1] * LREC_WORDS * sizeof(float), &z));
                 S->b.lrec = (float*)z;
             }
             if (auto st = autotune_stage_kernel(S.get(), s); st != SHOCCS_OK) return st;

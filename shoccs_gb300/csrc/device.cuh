@@ -117,6 +117,9 @@ struct SysParams {
     DevSol sol;
 };
 
+// words of a z line's record for the vectorised mixed stage (kernels.cu, k_cut_rows)
+constexpr int LREC_WORDS = 20;
+
 struct StepBuffers {
     void* u0;      // double (FP64), or the hi plane then the lo plane of FP32 pairs (MIXED)
     void* acc;     // double (FP64) or float (MIXED)

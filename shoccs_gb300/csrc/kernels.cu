@@ -247,6 +247,7 @@ struct RScaled {
 __device__ __forceinline__ double ldr(const double* R, long long i) { return __ldg(R + i); }
 __device__ __forceinline__ double ldr(const float* R, long long i) { return (double)__ldg(R + i); }
 __device__ __forceinline__ double ldr(const RScaled& R, long long i) { return __ldg(R.tab + i) * R.et; }
+__device__ __forceinline__ double ldr(const CgD& R, long long i) { return __ldcg(R.p + i); }
 // v = (first ? 0 : acc) + sum_j c_j x_j ; v += b * R[b_idx] ; v += n * nu[n_idx]
 // in the order of derivative::apply_kernels (O, then B, then N).
 template <class TIN, class TR>
@@ -739,7 +740,7 @@ struct StageArgs {
     const void* cval;
     float* rowv;            // vectorised mixed stages: cut-cell row values of the stage at
                             // their points, axis-major (3 x N), or null
-    float* lrec;            // and the line records (16 words per z line, k_cut_rows)
+    float* lrec;            // and the line records (LREC_WORDS per z line, k_cut_rows)
     const float4* fplane[6]; // Dirichlet face values of the step (mixed path), see StepBuffers
     const double* R[3];
     double cf, ci;          // dt*rkf[s], dt*rki[s+1]
@@ -757,13 +758,14 @@ enum { SYS_HEAT = 0, SYS_WAVE = 1 };
 // vectorised mixed stage -- scattered to their points in rowv (3 x N, axis-major), where a
 // lane finds its value with one load at its own index.
 //
-// With line records (lrec), the first threads of the grid each fill the 16-word record of
-// one z line for the vectorised stage: words 0..5 the line's left z-wall rows (coordinate
-// first_row + w, wall32's arithmetic), 6..7 the stage output's value at the line's first
-// point where that point is on a Dirichlet face (face_entry, face_pick), 8..13 and 14..15
-// the same for the right wall and the last point.  The record is written as four aligned
-// float4s, and the stage kernel reads it with one load per lane at entry: it needs no class
-// byte to know where the words are.
+// With line records (lrec), the first threads of the grid each fill the record of one z line
+// for the vectorised stage, in the point order of the lanes that use it: words 0..7 the
+// z-wall row values at z = 0..7 (wall32's arithmetic; 0 where z holds no wall row), 8..15
+// the same at z = nz-8 .. nz-1, 16..17 and 18..19 the stage output's value (hi, lo words) at
+// the line's first and last point where that point is on a Dirichlet face (face_entry,
+// face_pick).  The record is written as five aligned float4s; a warp holding either end of
+// the line reads it with one load on each of its lanes 0..19, and a lane takes the word of
+// each of its points by a shuffle from a fixed lane (its coordinate's place in the record).
 // plane entry of the face point (i, j, k): the first Dirichlet face that holds it (every
 // face holding it has the same values)
 __device__ __forceinline__ const float4* face_entry(const StageArgs& sa, const DevOp& op, int i,
@@ -794,8 +796,13 @@ __device__ __forceinline__ float2 face_pick(const float4* f)
 }
 
 // the FP32 plane of a mixed-path row input: the stage field, or the hi words of the solution
-__device__ __forceinline__ const float* fp32_plane(const float* u) { return u; }
-__device__ __forceinline__ const float* fp32_plane(const PairU& u) { return u.hi; }
+__device__ __forceinline__ const float* fp32_plane(const CgF& u) { return u.p; }
+__device__ __forceinline__ const float* fp32_plane(const CgPair& u) { return u.hi; }
+
+// The row inputs of k_cut_rows were written by the kernel it follows by programmatic
+// dependent launch, and the boundary values by the side stream: every load of them goes to
+// L2 (TIN is CgD, CgF or CgPair; the R arrays are read through CgD), never through the
+// non-coherent read-only path.
 
 template <class TIN, class TOUT>
 __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
@@ -805,7 +812,7 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
     pdl_wait();
     pdl_trigger();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if constexpr (!std::is_same<TIN, const double*>::value) {
+    if constexpr (!std::is_same<TIN, CgD>::value) {
         // the line records come first in the grid, so their threads run beside the cut-cell
         // rows instead of after them
         const int nlines = sa.lrec ? op.it0 * op.it1 : 0;
@@ -820,22 +827,24 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
             const int li = line / op.it1, lj = line - li * op.it1;
             const float4* f0 = face_entry(sa, op, li, lj, 0);
             const float4* f1 = face_entry(sa, op, li, lj, nz - 1);
-            const float4 fa = f0 ? *f0 : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 fb = f1 ? *f1 : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 l0 = __ldg((const float4*)(hi + base)), l1 = __ldg((const float4*)(hi + base + 4));
-            const float4 r0 = __ldg((const float4*)(hi + base + nz - 8)),
-                         r1 = __ldg((const float4*)(hi + base + nz - 4));
+            const float4 fa = f0 ? __ldcg(f0) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 fb = f1 ? __ldcg(f1) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 l0 = __ldcg((const float4*)(hi + base)), l1 = __ldcg((const float4*)(hi + base + 4));
+            const float4 r0 = __ldcg((const float4*)(hi + base + nz - 8)),
+                         r1 = __ldcg((const float4*)(hi + base + nz - 4));
             const float xl[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
             const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-            float w[16];
+            float w[LREC_WORDS];
 #pragma unroll
-            for (int m = 0; m < 16; m++) w[m] = 0.f;
+            for (int m = 0; m < LREC_WORDS; m++) w[m] = 0.f;
             {
                 const WallBlock& W = A.wall[0]; // columns 0 .. cols-1
                 const float x[7] = {xl[0], xl[1], xl[2], xl[3], xl[4], xl[5], xl[6]};
 #pragma unroll
-                for (int r = 0; r < 6; r++)
-                    if (r < W.rows) w[r] = wall_row_diff(W, r, x); // wall32's arithmetic
+                for (int z = 0; z < 8; z++) {
+                    const int r = z - W.first_row;
+                    if (r >= 0 && r < W.rows) w[z] = wall_row_diff(W, r, x); // wall32's arithmetic
+                }
             }
             {
                 const WallBlock& W = A.wall[1]; // columns nz-cols .. nz-1: xr[8-cols ..]
@@ -849,8 +858,10 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
                         if (m == sh + jj) x[jj] = xr[m];
                 }
 #pragma unroll
-                for (int r = 0; r < 6; r++)
-                    if (r < W.rows) w[8 + r] = wall_row_diff(W, r, x);
+                for (int m = 0; m < 8; m++) {
+                    const int r = nz - 8 + m - W.first_row;
+                    if (r >= 0 && r < W.rows) w[8 + m] = wall_row_diff(W, r, x);
+                }
             }
             auto pick = [stage](const float4& f) {
                 return stage < 2 ? make_float2(f.x, 0.f)
@@ -858,24 +869,24 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
             };
             if (f0) {
                 const float2 v = pick(fa);
-                w[6] = v.x;
-                w[7] = v.y;
+                w[16] = v.x;
+                w[17] = v.y;
             }
             if (f1) {
                 const float2 v = pick(fb);
-                w[14] = v.x;
-                w[15] = v.y;
+                w[18] = v.x;
+                w[19] = v.y;
             }
-            float4* o = (float4*)(sa.lrec + (long long)line * 16);
+            float4* o = (float4*)(sa.lrec + (long long)line * LREC_WORDS);
 #pragma unroll
-            for (int m = 0; m < 4; m++)
+            for (int m = 0; m < LREC_WORDS / 4; m++)
                 o[m] = make_float4(w[4 * m], w[4 * m + 1], w[4 * m + 2], w[4 * m + 3]);
             return;
         }
         i -= nlines;
     }
     if (i >= op.n_cut_rows) return;
-    const double* R[3] = {R0, R1, R2};
+    const CgD R[3] = {{R0}, {R1}, {R2}};
     const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
     const DevAxis& A = op.ax[d];
     const int row = i - A.row_base;
@@ -1008,7 +1019,7 @@ __device__ __forceinline__ void stage64_at(const DevOp& op, const SysParams& sp,
                 stage_ijk(op, q, ijk);
                 v = wall64(A, (long long)q.p, ijk[d], in, (const double*)nullptr, 0.0, true);
             } else if (kind == ROW_CLOSURE) {
-                v = cval[A.row_base + row];
+                v = __ldcg(cval + A.row_base + row); // k_cut_rows, the dependent-launch predecessor
             }
         }
         if (SYS == SYS_HEAT)
@@ -1367,10 +1378,9 @@ __global__ void k_faces_mixed(DevOp op, StageArgs sa)
 //    k_cut_rows fills, issued as soon as the class word arrives;
 //  * x- and y-wall rows (whole planes / rows, uniform across a warp): the wall block's
 //    columns of the four points as float4s, all in one round trip;
-//  * z-wall rows (a lane or two at either end of every line): from the z window already in
-//    registers (zwall_row), no load at all;
-//  * Dirichlet z-face points (the first and last point of a line): their values are loaded
-//    with the stencil inputs; x- and y-face planes (uniform across a warp) after the update.
+//  * z-wall rows and Dirichlet z-face points (the lanes at either end of every line): from
+//    the line record, one word per lane loaded at entry and moved by shuffles; x- and y-face
+//    planes (uniform across a warp) after the update.
 // FORM fixes the interior stencil (5-point antisymmetric, 5-point symmetric, 3-point) and VK
 // the velocity field of the wave system (constant or radial), so the per-point code has no
 // run-time branch on either.  The arithmetic of each point is the per-point kernel's,
@@ -1393,6 +1403,11 @@ __device__ __forceinline__ float interior_row_t(const DevAxis& A, float m2, floa
 __device__ __forceinline__ float4 ld4(const float* base, int idx)
 {
     return __ldg((const float4*)(base + idx));
+}
+// the same from L2, for data the dependent-launch predecessor wrote
+__device__ __forceinline__ float4 ld4cg(const float* base, int idx)
+{
+    return __ldcg((const float4*)(base + idx));
 }
 
 __device__ __forceinline__ float f4(const float4& v, int q)
@@ -1436,8 +1451,9 @@ __device__ __forceinline__ VecLoads vec_loads(const DevOp& op, const StageArgs& 
 }
 
 // Everything of one thread's four points of plane i after the loads: interior rows from the
-// registers, cut-cell rows (rowv), z-wall rows and z-face values (the line record `rec`),
-// x / y wall rows, the right-hand side, the RK4 registers, Dirichlet faces, the stores.
+// registers, cut-cell rows (rowv), z-wall rows and z-face values (the line record, word
+// `lane` of it in rec), x / y wall rows, the right-hand side, the RK4 registers, Dirichlet
+// faces, the stores.
 template <int STAGE, int SYS, int FORM, int VK>
 __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParams& sp,
                                                  const StageArgs& sa, const float* in, int i,
@@ -1478,22 +1494,19 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
     // free: issued before it, it pushed stage 3 past the 64-register budget
     const float4 ul = STAGE == 3 ? *(const float4*)(u0 + op.N + p) : make_float4(0.f, 0.f, 0.f, 0.f);
     if (cut) { // cut-cell rows: one load each, at the point's own index
-        const float* __restrict__ rv = sa.rowv + p;
+        const float* rv = sa.rowv + p; // written by k_cut_rows, the dependent-launch predecessor
 #pragma unroll
         for (int d = 0; d < 3; d++)
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (kq[d][q] == ROW_CLOSURE) v[d][q] = rv[d * op.N + q];
+                if (kq[d][q] == ROW_CLOSURE) v[d][q] = __ldcg(rv + d * op.N + q);
     }
-    if (__any_sync(FULL, zwall)) { // z-wall rows: the record word of each row to its lane
-        const DevAxis& A = op.ax[2];
+    if (__any_sync(FULL, zwall)) { // z-wall rows: the record words of the four points
+        const int w0 = k < 8 ? k : 8 + k - (nz - 8);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const int kk = k + q;
-            const bool use = kq[2][q] == ROW_WALL;
-            const int w = kk * 2 < nz ? kk - A.wall[0].first_row : 8 + kk - A.wall[1].first_row;
-            const float val = __shfl_sync(FULL, rec, use ? w : 0);
-            if (use) v[2][q] = val;
+            const float val = __shfl_sync(FULL, rec, (w0 + q) & 31);
+            if (kq[2][q] == ROW_WALL) v[2][q] = val;
         }
     }
     if (__any_sync(FULL, xywall)) { // whole x / y wall planes: uniform across the warp
@@ -1555,9 +1568,9 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
         rk_mixed<STAGE>(sa, rhs, make_float2(f4(uh, q), f4(ul, q)), f4(av, q), ao[q], so[q],
                         uo[q]);
     }
-    // the z-face values of the line's first and last point (record words 6, 7 and 14, 15);
+    // the z-face values of the line's first and last point (record words 16, 17 and 18, 19);
     // every lane takes part in the shuffles, lanes past the line's end store nothing
-    const int fw = k == 0 ? 6 : 14;
+    const int fw = k == 0 ? 16 : 18;
     const float fa = __shfl_sync(FULL, rec, fw);
     const float fb = STAGE == 3 ? __shfl_sync(FULL, rec, fw + 1) : 0.f;
     if (!kvalid) return;
@@ -1610,12 +1623,12 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     const VecLoads L = vec_loads<STAGE>(op, sa, in, i, j, k, ld4(in, p));
     const float4 xa = ld4(in, p + xm2), xb = ld4(in, p + xm1), xc = ld4(in, p + xp1),
                  xd = ld4(in, p + xp2);
-    // the line record (k_cut_rows): words 0..7 on lanes 0..7 of the warp that holds the
-    // line's first point, words 8..15 on lanes 8..15 of the one that holds its last point
+    // the line record (k_cut_rows): word `lane` on lanes 0..19 of a warp that holds either
+    // end of the line
     pdl_wait();
-    const bool rec_l = blockIdx.x == 0, rec_r = blockIdx.x + 1 == gridDim.x;
-    const float rec = (lane < 8 ? rec_l : (lane < 16 && rec_r))
-                          ? __ldg(sa.lrec + (long long)(i * ny + j) * 16 + lane)
+    const int kw = blockIdx.x * 128;
+    const float rec = lane < LREC_WORDS && (kw < 8 || kw + 128 > nz - 8)
+                          ? __ldcg(sa.lrec + (long long)(i * ny + j) * LREC_WORDS + lane)
                           : 0.f;
     vec_stage_points<STAGE, SYS, FORM, VK>(op, sp, sa, in, i, j, k, lane, L, xa, xb, xc, xd, rec);
 }
@@ -2234,7 +2247,7 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
     if constexpr (NZ) {
         const int lane = threadIdx.x;
         if (lane < 8 ? blockIdx.x == 0 : (lane < 16 && blockIdx.x + 1 == gridDim.x))
-            rec = __ldg(op.op_zw + (long long)(i * ny + j) * 16 + lane);
+            rec = __ldcg(op.op_zw + (long long)(i * ny + j) * 16 + lane);
     }
     float v[3][4] = {};
     unsigned kq[3][4];
@@ -2266,13 +2279,13 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
                           : 0.f;
     }
     if (cut) {
-        const float* __restrict__ rv = op.op_rowv + p;
+        const float* rv = op.op_rowv + p; // written by k_op_rows, the dependent-launch predecessor
 #pragma unroll
         for (int d = 0; d < 3; d++)
 #pragma unroll
             for (int q = 0; q < 4; q++)
                 if ((d == 0 ? NX : (d == 1 ? NY : NZ)) && kq[d][q] == ROW_CLOSURE)
-                    v[d][q] = rv[d * op.N + q];
+                    v[d][q] = __ldcg(rv + d * op.N + q);
     }
     if constexpr (NZ) {
         if (__any_sync(FULL, zwall)) { // the record word of each z-wall row to its lane
@@ -2500,16 +2513,16 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         const int nb = (int)((op.n_cut_rows + n_lines + 127) / 128);
         const double* const* R = a.R;
         if (!mixed)
-            launch_ex(k_cut_rows<const double*, double>, dim3(nb), dim3(128), s, true, op,
-                      (const double*)(STAGE == 0 ? a.u0 : a.s_in), R[0], R[1], R[2],
+            launch_ex(k_cut_rows<CgD, double>, dim3(nb), dim3(128), s, true, op,
+                      CgD{(const double*)(STAGE == 0 ? a.u0 : a.s_in)}, R[0], R[1], R[2],
                       (double*)a.cval, nullptr, ca, STAGE);
         else if (STAGE == 0)
-            launch_ex(k_cut_rows<PairU, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
-                      PairU{(const float*)a.u0, op.N}, R[0], R[1], R[2], (float*)a.cval, rowv,
+            launch_ex(k_cut_rows<CgPair, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
+                      CgPair{(const float*)a.u0, op.N}, R[0], R[1], R[2], (float*)a.cval, rowv,
                       ca, STAGE);
         else
-            launch_ex(k_cut_rows<const float*, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
-                      (const float*)a.s_in, R[0], R[1], R[2], (float*)a.cval, rowv, ca, STAGE);
+            launch_ex(k_cut_rows<CgF, float>, dim3(nb), dim3(128), s, b.vec != 0, op,
+                      CgF{(const float*)a.s_in}, R[0], R[1], R[2], (float*)a.cval, rowv, ca, STAGE);
         ++g_launches;
     }
     if (ev) cudaEventRecord(ev[0], s);
@@ -4290,9 +4303,9 @@ __device__ __forceinline__ T interior_t(const DevOp& op, long long p, const int 
             const unsigned c = op.cls[i];
             if (((c >> (2 * d)) & 3u) != ROW_INTERIOR || (c & CLS_DIRFACE)) continue;
             if constexpr (sizeof(T) == 8)
-                y = fma(A.ic[half + m], __ldg(z + i), y); // row i's weight on offset m
+                y = fma(A.ic[half + m], __ldcg(z + i), y); // row i's weight on offset m
             else
-                y = fmaf(A.icf[half + m], __ldg(z + i), y);
+                y = fmaf(A.icf[half + m], __ldcg(z + i), y);
         }
     }
     return y;
@@ -4339,7 +4352,7 @@ __global__ void k_adj_closure(DevOp op, AdjClosure cl, int S, AdjArgs a)
     T* out = (T*)a.out;
     double yd = 0.0;
     for (int e = cl.ptr[t]; e < cl.ptr[t + 1]; e++)
-        yd = fma(cl.w[e], (double)__ldg(z + cl.src[e]), yd);
+        yd = fma(cl.w[e], (double)__ldcg(z + cl.src[e]), yd);
     const T y = (T)(a.k * (yd * a.zscale));
     const long long p = cl.tgt[t];
     const unsigned c = op.cls[p];
@@ -4393,13 +4406,13 @@ __global__ void __launch_bounds__(256, 4) k_adj_stage_vec(DevOp op, int S, AdjAr
     unsigned cx[5], cy[5];
 #pragma unroll
     for (int m = 0; m < 5; m++) {
-        zx[m] = ld4(z, p + ox[m]);
+        zx[m] = ld4cg(z, p + ox[m]);
         cx[m] = C4(p + ox[m]);
-        zy[m] = ld4(z, p + oy[m]);
+        zy[m] = ld4cg(z, p + oy[m]);
         cy[m] = C4(p + oy[m]);
     }
     const int zl = k >= 4 ? -4 : 0, zr = k + 8 <= nz ? 4 : 0;
-    const float4 zL = ld4(z, p + zl), zR = ld4(z, p + zr);
+    const float4 zL = ld4cg(z, p + zl), zR = ld4cg(z, p + zr);
     const unsigned cL = C4(p + zl), cR = C4(p + zr);
     const float4 zc = zx[2];
     const unsigned cc = cx[2];
