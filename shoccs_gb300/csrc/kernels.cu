@@ -1471,18 +1471,16 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
     const float* __restrict__ u0 = (const float*)sa.u0;
     float v[3][4];
     unsigned kq[3][4];
-    bool cut = false, zwall = false, xywall = false; // cut-cell rows; z-wall rows; x/y walls
+    // the twelve row kinds (2-bit fields, bits 0-5 of each class byte) tested at once: hb holds
+    // each field's high bit, lb its low bit moved to the high bit's position
+    const unsigned hb = c4 & 0x2A2A2A2Au, lb = (c4 << 1) & 0x2A2A2A2Au;
+    const bool cut = (hb & ~lb) != 0u;                      // cut-cell rows (kind 2)
+    const bool zwall = (hb & lb & 0x20202020u) != 0u;       // z-wall rows (kind 3)
+    const bool xywall = (hb & lb & 0x0A0A0A0Au) != 0u;      // x / y wall rows
 #pragma unroll
     for (int q = 0; q < 4; q++) {
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-            kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
-            cut = cut || kq[d][q] == ROW_CLOSURE;
-            if (d == 2)
-                zwall = zwall || kq[d][q] == ROW_WALL;
-            else
-                xywall = xywall || kq[d][q] == ROW_WALL;
-        }
+        for (int d = 0; d < 3; d++) kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
         const float sx = interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q));
         const float sy = interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q));
         const float sz = interior_row_t<FORM>(op.ax[2], zz[q], zz[q + 1], zz[q + 2], zz[q + 3], zz[q + 4]);
