@@ -248,16 +248,23 @@ shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);
  * such solves one after another through integrators::rk4 (src/temporal/rk4.cpp:16-47);
  * the batch itself has no counterpart there. */
 typedef struct shoccs_batch shoccs_batch;
-/* the systems stay owned by the caller and must outlive the batch; creation picks the tile
- * shape of the stage kernel by timing the candidates on the batch */
+/* the systems stay owned by the caller and must outlive the batch.  Mixed 2-D instances take
+ * the split stage (uniform tiles and special points, two kernels per stage on parallel graph
+ * branches), in groups of instances of about 48 MB of fields advanced one group after
+ * another (SHOCCS_BATCH_GROUP_MB; 0: the whole batch at once), or with SHOCCS_BATCH_PERSIST=1
+ * the whole solve as one persistent launch of thread-block clusters; FP64 batches take the
+ * per-point stage, whose tile shape creation picks by timing the candidates on the batch
+ * (SHOCCS_BATCH_KERNEL=point|flat|split overrides the choice of stage).  Every form gives each
+ * instance the bits of its single-system solve. */
 shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_batch** out);
 shoccs_status shoccs_batch_destroy(shoccs_batch* b);
 /* nsteps RK4 steps of instance i from t0[i] with step dt[i]; afterwards each system holds
  * its state as after shoccs_system_rk4(system_i, t0[i], dt[i], nsteps) */
 shoccs_status shoccs_batch_rk4(shoccs_batch* b, const double* t0, const double* dt, int nsteps,
                                void* stream);
-/* info[6] = {instances, tiles, cut-cell rows, tile warps (autotuned), persistent grid,
- *            kernel nodes of the captured graph (0 before the first run)} */
+/* info[6] = {instances, tiles (per-point, flat and uniform tiles), cut-cell rows of the row
+ *            pass, tile warps (autotuned), grid (blocks of the per-point stage, or of the
+ *            persistent launch), kernel nodes of the captured graph (0 before the first run)} */
 shoccs_status shoccs_batch_info(const shoccs_batch* b, int64_t info[6]);
 
 /* ---- discrete adjoint (FP64 heat systems) ------------------------------------------------
