@@ -151,6 +151,7 @@ namespace stencils
 struct stencil {
     int scheme;                  // SHOCCS_SCHEME_*
     std::array<real, 2> alpha{}; // E4_1 / E4u_1 closure parameters
+    std::array<real, 13> poly{}; // E2-poly: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]
 };
 
 inline stencil make_E2_2() { return {SHOCCS_SCHEME_E2_2, {}}; }
@@ -175,6 +176,17 @@ inline stencil make_E4_1(std::span<const real> alpha)
 inline stencil make_E4u_1(std::span<const real> alpha)
 {
     return {SHOCCS_SCHEME_E4U_1, {alpha.size() > 0 ? alpha[0] : 0.0, alpha.size() > 1 ? alpha[1] : 0.0}};
+}
+// src/stencils/polyE2_1.cpp:260-265; each parameter span copied zero-padded to its length
+// (polyE2_1.cpp:21-28)
+inline stencil make_polyE2_1(std::span<const real> floating_alpha, std::span<const real> dirichlet_alpha,
+                             std::span<const real> interpolant_alpha)
+{
+    stencil st{SHOCCS_SCHEME_POLYE2_1, {}};
+    for (size_t i = 0; i < 6 && i < floating_alpha.size(); i++) st.poly[i] = floating_alpha[i];
+    for (size_t i = 0; i < 3 && i < dirichlet_alpha.size(); i++) st.poly[6 + i] = dirichlet_alpha[i];
+    for (size_t i = 0; i < 4 && i < interpolant_alpha.size(); i++) st.poly[9 + i] = interpolant_alpha[i];
+    return st;
 }
 } // namespace stencils
 using stencils::stencil;
@@ -288,6 +300,7 @@ public:
         d.scheme = st.scheme;
         d.alpha[0] = st.alpha[0];
         d.alpha[1] = st.alpha[1];
+        for (int i = 0; i < 13; i++) d.poly_alpha[i] = st.poly[i];
         shoccs_problem* raw = nullptr;
         detail::check(shoccs_problem_create(&d, &raw), "shoccs_problem_create");
         p_.reset(raw, [](shoccs_problem* q) { shoccs_problem_destroy(q); });

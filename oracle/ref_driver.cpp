@@ -72,8 +72,16 @@ REF_MEMBER(csr_w, matrix::csr, std::vector<real>, w)
 REF_MEMBER(csr_v, matrix::csr, std::vector<integer>, v)
 REF_MEMBER(csr_u, matrix::csr, std::vector<integer>, u)
 
+// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1; alpha: 2 values, or for polyE2_1 13
+// (floating alpha[6], dirichlet alpha[3], interpolant alpha[4], stencil.cpp:79-87's order)
 static stencil make(int scheme, const double* alpha)
 {
+    if (scheme == 5) {
+        std::vector<real> a(13, 0.0);
+        if (alpha) std::copy(alpha, alpha + 13, a.begin());
+        auto s = std::span<const real>{a};
+        return make_polyE2_1(s.subspan(0, 6), s.subspan(6, 3), s.subspan(9, 4));
+    }
     std::vector<real> a{alpha ? alpha[0] : 0.0, alpha ? alpha[1] : 0.0};
     switch (scheme) {
     case 0: return make_E2_2();
@@ -577,9 +585,10 @@ int ref_stencil_interior(int scheme, const double* alpha, double h, double* c)
     return 2 * mx.p + 1;
 }
 
-int ref_stencil_interp_wall(int scheme, int i, double y, double psi, int right, double* c)
+int ref_stencil_interp_wall(int scheme, const double* alpha, int i, double y, double psi,
+                            int right, double* c)
 {
-    auto st = make(scheme, nullptr);
+    auto st = make(scheme, alpha);
     std::vector<real> cc(8, 0.0);
     auto s = st.interp_wall(i, y, psi, cc, right != 0);
     for (size_t k = 0; k < s.size(); k++) c[k] = s[k];

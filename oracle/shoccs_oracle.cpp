@@ -368,8 +368,9 @@ struct interp_info {
 };
 
 struct stencil {
-    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1, 3: E4u_1
+    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1, 3: E4u_1, 5: polyE2_1 (type "E2-poly")
     real alpha[2] = {0, 0};
+    real pa[13] = {}; // polyE2_1: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]
 
     info query_max() const
     {
@@ -377,13 +378,14 @@ struct stencil {
         case 0: return {1, 2, 4, 2};
         case 1: return {2, 3, 5, 3};
         case 3: return {2, 3, 5, 0};
+        case 5: return {1, 3, 4, 0}; // polyE2_1.cpp:11-14
         default: return {2, 5, 7, 0};
         }
     }
     info query(int b) const
     {
         info mx = query_max();
-        if ((kind == 2 || kind == 3) && b == Neumann) return {0, 0, 0, 0};
+        if ((kind == 2 || kind == 3 || kind == 5) && b == Neumann) return {0, 0, 0, 0};
         switch (b) {
         case Dirichlet: return {mx.p, mx.r - 1, mx.t, 0};
         case Floating: return {mx.p, mx.r, mx.t, 0};
@@ -395,6 +397,7 @@ struct stencil {
         switch (kind) {
         case 0: return {2, 3};
         case 1: return {5, 5};
+        case 5: return {2, 4}; // polyE2_1.cpp:44
         default: return {0, 0};
         }
     }
@@ -412,6 +415,8 @@ struct stencil {
             c[2] = -5 / (2. * (h * h));
             c[3] = 4 / (3. * (h * h));
             c[4] = -1 / (12. * (h * h));
+        } else if (kind == 5) {
+            pe2_interior(h, c);
         } else if (kind == 3) { // E4u_1.cpp:49-58
             c[0] = 1 / (12 * h);
             c[1] = -2 / (3 * h);
@@ -442,10 +447,136 @@ struct stencil {
         } else if (kind == 3) {
             if (b == Floating) e4u_floating(h, c, right);
             else if (b == Dirichlet) e4u_dirichlet(h, c, right);
+        } else if (kind == 5) {
+            if (b == Floating) pe2_floating(h, psi, c, right);
+            else if (b == Dirichlet) pe2_dirichlet(h, psi, c, right);
         } else {
             if (b == Floating) e41_floating(h, psi, c, right);
             else if (b == Dirichlet) e41_dirichlet(h, psi, c, right);
         }
+    }
+
+    // ---- polyE2_1 (type "E2-poly"): src/stencils/polyE2_1.cpp.  Parameters pa[13]: the
+    // floating alpha fa = pa[0..5], the dirichlet alpha da = pa[6..8] and the interpolant
+    // alpha ia = pa[9..12] (the reference's single-array order, stencil.cpp:79-87).  The
+    // closed forms keep the reference's operation order term for term (bit-exact).
+    void pe2_interior(real h, real* c) const // polyE2_1.cpp:169-177
+    {
+        c[0] = -0.5;
+        c[1] = 0;
+        c[2] = 0.5;
+        for (int i = 0; i < 3; i++) c[i] /= h;
+    }
+    void pe2_floating(real h, real psi, real* c, bool right) const // polyE2_1.cpp:194-230
+    {
+        const real* fa = pa;
+        const real a0 = fa[0], b0 = fa[1], a1 = fa[2], b1 = fa[3], a2 = fa[4], b2 = fa[5];
+        const real inv = 1.0 / (1 + psi);
+        const real p2 = 2 + psi;
+        const real b0m = -1 + b0, b1m = -1 + b1, b2m = -1 + b2;
+        c[0] = 0.5 * inv * b0m;
+        c[1] = (-1 + a0) * 0.5;
+        c[2] = -1 * a0 + -0.5 * p2 * inv * b0m;
+        c[3] = (a0 + b0) * 0.5;
+        c[4] = 0.5 * b1m * inv;
+        c[5] = (-1 + a1) * 0.5;
+        c[6] = -1 * a1 + -0.5 * p2 * b1m * inv;
+        c[7] = (b1 + a1) * 0.5;
+        c[8] = 0.5 * b2m * inv;
+        c[9] = (-1 + a2) * 0.5;
+        c[10] = -1 * a2 + -0.5 * p2 * b2m * inv;
+        c[11] = (b2 + a2) * 0.5;
+        for (int i = 0; i < 12; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 12; i++) c[i] *= -1;
+            reverse(c, 12);
+        }
+    }
+    void pe2_dirichlet(real h, real psi, real* c, bool right) const // polyE2_1.cpp:232-280
+    {
+        const real* da = pa + 6;
+        const real d0 = da[0], d1 = da[1], d2 = da[2];
+        const real inv = 1.0 / (1 + psi);
+        const real d0m = -1 + d0;
+        const real tp = 2 * psi;
+        const real d2x3 = 3 * d2;
+        const real tpd2 = 2 * psi * d2;
+        const real den = 1.0 / (1 + tp + d2x3 + tpd2);
+        const real tpd1 = 2 * psi * d1;
+        const real d1d0x3 = 3 * d1 * d0;
+        const real tpd1d0 = 2 * psi * d1 * d0;
+        const real md1 = -1 * d1;
+        const real p2 = 2 + psi;
+        const real d2m = -1 + d2;
+        c[0] = 0.5 * inv * d0m;
+        c[1] = (-1 + -2 * psi + d1 + tpd1 + d1d0x3 + tpd1d0 + -3 * d0 + -2 * psi * d0) * 0.5 * den;
+        c[2] = (-2 * psi * d1 + -3 * d2 + -2 * psi * d2 + md1 + 3 * d0 + 2 * psi * d0 +
+                -3 * d1 * d0 + -2 * psi * d1 * d0) *
+                   den +
+               -0.5 * p2 * inv * d0m;
+        c[3] = (d1 + tpd1 + d1d0x3 + tpd1d0 + d2x3 + tpd2 + -2 * d0 + 3 * d2 * d0 +
+                2 * psi * d2 * d0) *
+               0.5 * den;
+        c[4] = 0.5 * d2m * inv;
+        c[5] = (-1 + d1) * 0.5;
+        c[6] = md1 + -0.5 * p2 * d2m * inv;
+        c[7] = (d1 + d2) * 0.5;
+        for (int i = 0; i < 8; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 8; i++) c[i] *= -1;
+            reverse(c, 8);
+        }
+    }
+    int pe2_interp_wall(int i, real y, real psi, real* c, bool right) const // polyE2_1.cpp:58-141
+    {
+        const real* fa = pa;
+        const real* ia = pa + 9;
+        const real inv = 1.0 / (1 + psi);
+        const real my = -1 * y;
+        if (right) {
+            if (i == 0) {
+                const real f0y = fa[0] * y, f1y = fa[1] * y;
+                c[0] = (f0y + f1y + ia[0] + ia[1]) * 0.5;
+                c[1] = (-1 * psi + my + (f0y + ia[0]) * -2 +
+                        (my + -2 * ia[1] + -1 * psi * ia[1] + -2 * fa[1] * y + -1 * psi * fa[1] * y) *
+                            inv) *
+                       0.5;
+                c[2] = (1 + psi + f0y + ia[0] + y) * 0.5;
+                c[3] = (1 + psi + f1y + ia[1] + y) * 0.5 * inv;
+            } else {
+                const real f2y = fa[2] * y, f3y = fa[3] * y;
+                c[0] = (ia[3] + f2y + f3y + ia[2]) * 0.5;
+                c[1] = (my + (f2y + ia[2]) * -2 +
+                        (psi + -2 * ia[3] + -1 * psi * ia[3] + my + -2 * fa[3] * y +
+                         -1 * psi * fa[3] * y) *
+                            inv) *
+                       0.5;
+                c[2] = (1 + f2y + ia[2] + y) * 0.5;
+                c[3] = (1 + ia[3] + f3y + y) * 0.5 * inv;
+            }
+        } else {
+            if (i == 0) {
+                const real f0y = fa[0] * y, f1y = fa[1] * y;
+                c[0] = (1 + psi + ia[1] + my + f1y) * 0.5 * inv;
+                c[1] = (1 + psi + f0y + ia[0] + my) * 0.5;
+                c[2] = (-1 * psi + (f0y + ia[0]) * -2 + y +
+                        (-2 * ia[1] + -1 * psi * ia[1] + y + -2 * fa[1] * y + -1 * psi * fa[1] * y) *
+                            inv) *
+                       0.5;
+                c[3] = (ia[1] + f0y + ia[0] + f1y) * 0.5;
+            } else {
+                const real f2y = fa[2] * y, f3y = fa[3] * y;
+                c[0] = (1 + f3y + ia[3] + my) * 0.5 * inv;
+                c[1] = (1 + f2y + ia[2] + my) * 0.5;
+                c[2] = ((f2y + ia[2]) * -2 + y +
+                        (psi + -2 * ia[3] + -1 * psi * ia[3] + y + -2 * fa[3] * y +
+                         -1 * psi * fa[3] * y) *
+                            inv) *
+                       0.5;
+                c[3] = (f3y + ia[3] + f2y + ia[2]) * 0.5;
+            }
+        }
+        return 4;
     }
 
     // ---- E4u_1 (uniform-grid closures, psi ignored): src/stencils/E4u_1.cpp:77-127
@@ -878,7 +1009,7 @@ struct stencil {
     // interpolants: E2_2.cpp:32-102, E4_2.cpp:44-185
     int interp_interior(real y, real* c) const
     {
-        if (kind == 0) {
+        if (kind == 0 || kind == 5) { // polyE2_1.cpp:46-56: E2_2's
             if (y > 0) {
                 c[0] = 1 + -1 * y;
                 c[1] = y;
@@ -901,6 +1032,7 @@ struct stencil {
 
     int interp_wall(int i, real y, real psi, real* c, bool right) const
     {
+        if (kind == 5) return pe2_interp_wall(i, y, psi, c, right);
         if (kind == 0) {
             if (right) {
                 const real t6 = 1 + psi;
@@ -1904,10 +2036,23 @@ int orc_num_threads(int n)
 }
 
 // grid_bc: xmin,xmax,ymin,ymax,zmin,zmax (0 Dirichlet, 1 Floating, 2 Neumann)
-// scheme: 0 E2_2, 1 E4_2, 2 E4_1
+// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1; alpha: 2 values (E4_1, E4u_1), or
+// for polyE2_1 13 (floating alpha[6], dirichlet alpha[3], interpolant alpha[4])
+static void set_params(stencil& st, int scheme, const double* alpha)
+{
+    st.kind = scheme;
+    if (!alpha) return;
+    if (scheme == 5) {
+        for (int i = 0; i < 13; i++) st.pa[i] = alpha[i];
+    } else {
+        st.alpha[0] = alpha[0];
+        st.alpha[1] = alpha[1];
+    }
+}
+
 orc_problem* orc_create(const int n[3], const double lo[3], const double hi[3], int nsph,
                         const double* centers, const double* radii, const int* obj_bc,
-                        const int grid_bc[6], int scheme, const double alpha[2])
+                        const int grid_bc[6], int scheme, const double* alpha)
 {
     auto* o = new orc_problem;
     std::vector<sphere> shapes;
@@ -1915,11 +2060,7 @@ orc_problem* orc_create(const int n[3], const double lo[3], const double hi[3], 
         shapes.push_back(sphere{{centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]},
                                 radii[i], i});
     o->P.m = make_mesh(n, lo, hi, shapes);
-    o->P.st.kind = scheme;
-    if (alpha) {
-        o->P.st.alpha[0] = alpha[0];
-        o->P.st.alpha[1] = alpha[1];
-    }
+    set_params(o->P.st, scheme, alpha);
     // src/operators/boundaries.cpp:11-38: Dirichlet/Neumann on a trivial axis -> Floating
     for (int d = 0; d < 3; d++)
         for (int s = 0; s < 2; s++) {
@@ -2020,15 +2161,11 @@ long orc_csr(orc_problem* o, int dir, int which, long* nrows, long* u, long* v, 
 }
 
 // stencil coefficients (for golden-vector pinning)
-void orc_stencil_nbs(int scheme, const double alpha[2], double h, int bc, double psi,
+void orc_stencil_nbs(int scheme, const double* alpha, double h, int bc, double psi,
                      int right, double* c, double* x)
 {
     stencil st;
-    st.kind = scheme;
-    if (alpha) {
-        st.alpha[0] = alpha[0];
-        st.alpha[1] = alpha[1];
-    }
+    set_params(st, scheme, alpha);
     st.nbs(h, bc, psi, right != 0, c, x);
 }
 void orc_stencil_interior(int scheme, double h, double* c)
@@ -2037,10 +2174,11 @@ void orc_stencil_interior(int scheme, double h, double* c)
     st.kind = scheme;
     st.interior(h, c);
 }
-int orc_stencil_interp_wall(int scheme, int i, double y, double psi, int right, double* c)
+int orc_stencil_interp_wall(int scheme, const double* alpha, int i, double y, double psi,
+                            int right, double* c)
 {
     stencil st;
-    st.kind = scheme;
+    set_params(st, scheme, alpha);
     return st.interp_wall(i, y, psi, c, right != 0);
 }
 int orc_stencil_interp_interior(int scheme, double y, double* c)

@@ -27,7 +27,8 @@ from ._capi import (BC_DIRICHLET, BC_FLOATING, BC_NEUMANN, PREC_FP64, PREC_MIXED
 ScalarField = namedtuple("ScalarField", ["D", "Rx", "Ry", "Rz"])
 
 _BC = {"dirichlet": BC_DIRICHLET, "floating": BC_FLOATING, "neumann": BC_NEUMANN}
-_SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1, "E4u_1": 3}
+_SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1, "E4u_1": 3,
+           "polyE2_1": 5}
 
 
 def _bc(b):
@@ -58,7 +59,10 @@ class Problem:
     """Mesh, boundary conditions and scheme; builds the three derivative operators.
 
     n, lo, hi: index_extents and domain_bounds; spheres: [(center3, radius, bc)];
-    grid_bc: (xmin, xmax, ymin, ymax, zmin, zmax); scheme: "E2_2" | "E4_2" | "E4_1".
+    grid_bc: (xmin, xmax, ymin, ymax, zmin, zmax); scheme: "E2_2" | "E4_2" | "E4_1" | "E4u_1"
+    | "polyE2_1" (type "E2-poly"); alpha: the two alpha of E4_1 / E4u_1, or the thirteen of
+    E2-poly (floating_alpha[6], dirichlet_alpha[3], interpolant_alpha[4], the reference's
+    single-array order).
     """
 
     def __init__(self, n, lo, hi, spheres=(), grid_bc=("floating",) * 6, scheme="E4_2",
@@ -86,7 +90,12 @@ class Problem:
         d.sphere_bc = ctypes.cast(self._sbc, _capi.c_int_p)
         d.grid_bc[:] = [_bc(b) for b in grid_bc]
         d.scheme = _SCHEME[scheme] if isinstance(scheme, str) else int(scheme)
-        d.alpha[:] = [float(alpha[0]), float(alpha[1])]
+        if d.scheme == _SCHEME["polyE2_1"]:
+            if len(alpha) != 13:
+                raise ValueError("E2-poly takes 13 alpha values")
+            d.poly_alpha[:] = [float(v) for v in alpha]
+        else:
+            d.alpha[:] = [float(alpha[0]), float(alpha[1])]
         self.desc = d
         h = ctypes.c_void_p()
         _capi.check(lib.shoccs_problem_create(ctypes.byref(d), ctypes.byref(h)))

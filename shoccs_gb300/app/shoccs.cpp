@@ -18,7 +18,7 @@
 //   simulation.domain_boundaries, shapes[i].boundary_condition
 //                              bcs::from_lua                src/operators/boundaries.cpp:7-90
 //   simulation.scheme          stencil::from_lua            src/stencils/stencil.cpp:8-106
-//                              (E2 / E4 second-derivative, E4 / E4u first-derivative)
+//                              (E2 / E4 second-derivative, E4 / E4u / E2-poly first-derivative)
 //   simulation.system          system::from_lua, heat::from_lua, scalar_wave::from_lua
 //                              src/systems/system.cpp:103-132, heat.cpp:78-104,
 //                              scalar_wave.cpp:134-193
@@ -43,6 +43,8 @@
 #include "lua_subset.hpp"
 #include "shoccs_gb300.hpp"
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <filesystem>
 #include <fstream>
@@ -180,6 +182,17 @@ std::optional<std::pair<bcs::Grid, bcs::Object>> read_bcs(const value& sim, cons
     return std::pair{g, o};
 }
 
+// a number as fmt's "{}" prints it (shortest representation that reads back the same)
+std::string fmt_real(real v)
+{
+    char buf[40];
+    for (int prec = 1; prec <= 17; prec++) {
+        std::snprintf(buf, sizeof buf, "%.*g", prec, v);
+        if (std::strtod(buf, nullptr) == v) break;
+    }
+    return buf;
+}
+
 // ---- scheme: stencil::from_lua ---------------------------------------------------------------
 std::optional<stencil> read_stencil(const value& sim, const logger& log)
 {
@@ -188,12 +201,19 @@ std::optional<stencil> read_stencil(const value& sim, const logger& log)
         log.err("simulation.scheme must be specified");
         return std::nullopt;
     }
-    std::vector<real> alpha;
-    if (const value as = at(m, "alpha"); valid(as))
-        for (long long i = 1; valid(at(as, i)); ++i) {
-            if (!at(as, i).number()) throw lua::error("scheme.alpha must hold numbers");
-            alpha.push_back(*at(as, i).number());
-        }
+    // the numeric arrays scheme.alpha, floating_alpha, dirichlet_alpha, interpolant_alpha
+    // (stencil.cpp:10-30: read_alpha)
+    auto read_alpha = [&](const char* key) {
+        std::vector<real> a;
+        if (const value as = at(m, key); valid(as))
+            for (long long i = 1; valid(at(as, i)); ++i) {
+                if (!at(as, i).number())
+                    throw lua::error(std::string("scheme.") + key + " must hold numbers");
+                a.push_back(*at(as, i).number());
+            }
+        return a;
+    };
+    std::vector<real> alpha = read_alpha("alpha");
     const int order = int_or(at(m, "order"), 1);
     const std::string type = str_or(at(m, "type"), "");
     if (order == 2 && type == "E2") {
@@ -216,8 +236,30 @@ std::optional<stencil> read_stencil(const value& sim, const logger& log)
         log.info("E4 uniform first scheme chosen");
         return stencils::make_E4u_1(alpha);
     }
+    if (order == 1 && type == "E2-poly") { // stencil.cpp:78-100
+        log.info("E2-poly scheme chosen");
+        auto join = [](const std::vector<real>& v) {
+            std::string out;
+            for (size_t i = 0; i < v.size(); i++) out += (i ? ", " : "") + fmt_real(v[i]);
+            return out;
+        };
+        if (!alpha.empty()) {
+            // one array holding the floating, dirichlet and interpolant alpha in turn
+            log.info("alpha = " + join(alpha));
+            std::vector<real> a = alpha;
+            a.resize(std::max<std::size_t>(a.size(), 13), 0.0);
+            const std::span<const real> sa{a};
+            return stencils::make_polyE2_1(sa.subspan(0, 6), sa.subspan(6, 3), sa.subspan(9, 4));
+        }
+        const std::vector<real> fa = read_alpha("floating_alpha"), da = read_alpha("dirichlet_alpha"),
+                                ia = read_alpha("interpolant_alpha");
+        log.info("floating alpha = " + join(fa));
+        log.info("dirichlet alpha = " + join(da));
+        log.info("interpolant alpha = " + join(ia));
+        return stencils::make_polyE2_1(fa, da, ia);
+    }
     if (order == 1 && (type == "E2" || type == "E6u" || type == "E8u" || type == "tension_E4u" ||
-                       type == "gaussian_E4u" || type == "multiquadric_E4u" || type == "E2-poly")) {
+                       type == "gaussian_E4u" || type == "multiquadric_E4u")) {
         log.err("scheme.order/type = 1 / " + type + " is not available in this build");
         return std::nullopt;
     }

@@ -111,7 +111,7 @@ struct shoccs_system {
     // stage field, right-hand side and accumulator (D parts: b.sa, b.sb, b.acc)
     bool unfused = false;
     FieldF64 fy{}, fk{}, facc{};
-    NeumannFaces nf{}; // Neumann domain faces (unfused heat systems)
+    UnfusedAux ux{}; // Neumann domain faces (unfused heat), gradient scratch (unfused wave)
     FieldF64 state() const { return {(double*)b.u0, {b.R[0], b.R[1], b.R[2]}}; }
     ~shoccs_system()
     {
@@ -173,8 +173,9 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
             A.ic[j] = T.interior[j];
             A.icf[j] = (float)T.interior[j];
         }
-        A.antisym = T.width == 5 && T.interior[2] == 0.0 && T.interior[0] == -T.interior[4] &&
-                    T.interior[1] == -T.interior[3];
+        A.antisym = T.width == 5 ? T.interior[2] == 0.0 && T.interior[0] == -T.interior[4] &&
+                                       T.interior[1] == -T.interior[3]
+                                 : T.width == 3 && T.interior[1] == 0.0 && T.interior[0] == -T.interior[2];
         if (!T.active) continue;
         // the FP32 kernels evaluate a non-antisymmetric interior as a symmetric
         // zero-sum second-derivative row in difference form (sym5 / sym3)
@@ -315,13 +316,23 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
     *out = nullptr;
     for (int i = 0; i < 3; i++)
         if (d->n[i] < 1) return fail(SHOCCS_EINVAL, "index_extents must be >= 1");
-    if (d->scheme < 0 || d->scheme > 3) return fail(SHOCCS_EINVAL, "unknown scheme");
+    if (d->scheme < 0 || d->scheme > 5 || d->scheme == 4) return fail(SHOCCS_EINVAL, "unknown scheme");
     if (d->n_spheres < 0 || (d->n_spheres && (!d->centers || !d->radii || !d->sphere_bc)))
         return fail(SHOCCS_EINVAL, "sphere arrays missing");
     for (int i = 0; i < 6; i++)
         if (bad_bc(d->grid_bc[i])) return fail(SHOCCS_EINVAL, "bad grid boundary condition");
     for (int i = 0; i < d->n_spheres; i++)
         if (bad_bc(d->sphere_bc[i])) return fail(SHOCCS_EINVAL, "bad shape boundary condition");
+    if (d->scheme == SHOCCS_SCHEME_POLYE2_1) {
+        for (int i = 0; i < 13; i++)
+            if (!std::isfinite(d->poly_alpha[i])) return fail(SHOCCS_EINVAL, "E2-poly: non-finite alpha");
+        for (int i = 0; i < 6; i++)
+            if (d->grid_bc[i] == SHOCCS_BC_NEUMANN && d->n[i / 2] > 1)
+                return fail(SHOCCS_EUNSUPPORTED, "first-derivative schemes have no Neumann closure");
+        for (int i = 0; i < d->n_spheres; i++)
+            if (d->sphere_bc[i] == SHOCCS_BC_NEUMANN)
+                return fail(SHOCCS_EUNSUPPORTED, "first-derivative schemes have no Neumann closure");
+    }
     if (d->scheme == SHOCCS_SCHEME_E4_1 || d->scheme == SHOCCS_SCHEME_E4U_1) {
         // src/stencils/E4_1.cpp:34-41
         if (d->scheme == SHOCCS_SCHEME_E4_1 && d->alpha[1] < 197.0 / 288.0)
@@ -350,6 +361,7 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
         p->st.kind = d->scheme;
         p->st.alpha[0] = d->alpha[0];
         p->st.alpha[1] = d->alpha[1];
+        for (int i = 0; i < 13; i++) p->st.pa[i] = d->poly_alpha[i];
         // a boundary condition on a trivial axis is Floating (src/operators/boundaries.cpp:15-24)
         for (int a = 0; a < 3; a++)
             for (int side = 0; side < 2; side++) {
@@ -637,10 +649,16 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     // (neumann_rx/ry/rz) is never assigned, so their closures carry no data term
     bool non_dirichlet_objects = false;
     for (int b : p->bcs.obj) non_dirichlet_objects = non_dirichlet_objects || b != Dirichlet;
-    if (non_dirichlet_objects && (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64))
+    if (non_dirichlet_objects && d->prec != PREC_FP64)
         return fail(SHOCCS_EUNSUPPORTED,
                     "non-Dirichlet objects (whose cut-point values evolve through the R-space "
-                    "rows) are time-stepped by the FP64 heat system only");
+                    "rows) are time-stepped by the FP64 systems only");
+    if (non_dirichlet_objects && d->kind == SHOCCS_SYS_WAVE) {
+        for (int b : p->bcs.obj)
+            if (b == Neumann)
+                return fail(SHOCCS_EUNSUPPORTED, "Neumann objects in the wave system: the reference's "
+                                                 "first-derivative schemes have no Neumann closures");
+    }
     int neumann_mask = 0;
     for (int a = 0; a < 3; a++)
         for (int side = 0; side < 2; side++)
@@ -748,7 +766,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
             void* nu = nullptr;
             SH_CUDA(S->mem.alloc((size_t)N * 8, &nu));
             SH_CUDA(cudaMemsetAsync(nu, 0, (size_t)N * 8, s));
-            S->nf = NeumannFaces{neumann_mask, (double*)nu};
+            S->ux.nf = NeumannFaces{neumann_mask, (double*)nu};
         }
         S->fy.D = (double*)S->b.sa;
         S->fk.D = (double*)S->b.sb;
@@ -759,6 +777,18 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
             S->fy.R[r] = S->b.Rhalf[r];
             S->fk.R[r] = S->b.Rfull[r];
             S->facc.R[r] = (double*)a;
+        }
+        if (d->kind == SHOCCS_SYS_WAVE) { // the gradient's components over the whole field
+            for (int c = 0; c < 3; c++) {
+                void* g = nullptr;
+                SH_CUDA(S->mem.alloc((size_t)N * 8, &g));
+                S->ux.grad[c].D = (double*)g;
+                for (int r = 0; r < 3; r++) {
+                    void* a = nullptr;
+                    SH_CUDA(S->mem.alloc(p->mesh.R[r].size() * 8, &a));
+                    S->ux.grad[c].R[r] = (double*)a;
+                }
+            }
         }
     }
     if (d->prec == PREC_MIXED) {
@@ -796,7 +826,10 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     {
         const int* it = p->comp.it;
         const bool three_d = it[0] > 1 && it[1] > 1 && it[2] > 1;
-        if (d->prec == PREC_MIXED && three_d && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
+        // its interior rows are the 5-point ones (sym5, or antisymmetric)
+        bool w5 = true;
+        for (int a = 0; a < 3; a++) w5 = w5 && (!p->op.ax[a].active || p->op.ax[a].width == 5);
+        if (d->prec == PREC_MIXED && three_d && w5 && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
             !std::getenv("SHOCCS_DISABLE_TMA")) {
             float* hi = (float*)S->b.u0;
             S->b.tma = make_plane_map(&S->b.tm_u0, hi, 4, it) &&
@@ -954,7 +987,7 @@ shoccs_status shoccs_system_rk4(shoccs_system* S, double t0, double dt, int nste
     double t = t0;
     for (int i = 0; i < nsteps; i++) {
         if (S->unfused)
-            SH_CUDA(launch_heat_step_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), S->fy,
+            SH_CUDA(launch_step_unfused(S->P->op, S->P->dr, S->sp, S->ux, S->state(), S->fy,
                                              S->fk, S->facc, t, dt, s));
         else
             SH_CUDA(launch_rk4_step(S->P->op, S->P->dr, S->sp, S->desc.prec, S->b, t, dt, s,
@@ -979,7 +1012,7 @@ shoccs_status shoccs_system_euler(shoccs_system* S, double t0, double dt, int ns
                                   : FieldF64{(double*)S->b.sa, {S->b.Rhalf[0], S->b.Rhalf[1], S->b.Rhalf[2]}};
     double t = t0;
     for (int i = 0; i < nsteps; i++) {
-        SH_CUDA(launch_euler_fp64(S->P->op, S->P->dr, S->sp, S->nf, S->unfused, S->b, S->state(), K, t, dt, s));
+        SH_CUDA(launch_euler_fp64(S->P->op, S->P->dr, S->sp, S->ux, S->unfused, S->b, S->state(), K, t, dt, s));
         t += dt;
     }
     SH_CUDA(cudaStreamSynchronize(s));
@@ -1062,7 +1095,7 @@ shoccs_status shoccs_system_rhs(shoccs_system* S, double t, shoccs_field* rhs, v
     const cudaStream_t s = (cudaStream_t)stream;
     double* outR[3] = {(double*)rhs->Rx, (double*)rhs->Ry, (double*)rhs->Rz};
     if (S->unfused)
-        SH_CUDA(launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), t,
+        SH_CUDA(launch_rhs_unfused(S->P->op, S->P->dr, S->sp, S->ux, S->state(), t,
                                         FieldF64{(double*)rhs->D, {outR[0], outR[1], outR[2]}}, s));
     else
         SH_CUDA(launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)rhs->D, outR, s));
@@ -1280,7 +1313,7 @@ shoccs_status shoccs_graph_add_rhs(shoccs_graph* g, shoccs_system* S, shoccs_fie
                       [S, fr](cudaStream_t s, double t) {
                           double* outR[3] = {(double*)fr.R[0], (double*)fr.R[1], (double*)fr.R[2]};
                           if (S->unfused)
-                              return launch_heat_rhs_unfused(S->P->op, S->P->dr, S->sp, S->nf, S->state(), t,
+                              return launch_rhs_unfused(S->P->op, S->P->dr, S->sp, S->ux, S->state(), t,
                                                              FieldF64{(double*)fr.D, {outR[0], outR[1], outR[2]}},
                                                              s);
                           return launch_rhs(S->P->op, S->sp, S->desc.prec, S->b, t, (double*)fr.D, outR, s);

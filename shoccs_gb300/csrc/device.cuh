@@ -91,6 +91,13 @@ struct NeumannFaces {
     double* nu;
 };
 
+// what the unfused whole-field step needs beyond the state: the Neumann face data (heat) and
+// the gradient's three components over the whole field (wave)
+struct UnfusedAux {
+    NeumannFaces nf{};
+    FieldF64 grad[3]{};
+};
+
 // launch helpers implemented in kernels.cu -----------------------------------------------
 enum { PREC_FP64 = 0, PREC_MIXED = 1 };
 // interior stencil shared by every active axis: 5-point antisymmetric (first derivative),
@@ -283,14 +290,15 @@ cudaError_t launch_cast(long long n, int to_f32, const void* in, void* out, cuda
 cudaError_t launch_rk4_step(const DevOp& op, const DevR& dr, const SysParams& sp, int prec,
                             StepBuffers& b, double t, double dt, cudaStream_t s,
                             cudaEvent_t* ev = nullptr, bool prefetch_next = false);
-// heat systems whose objects are not all Dirichlet (FP64): rhs of the whole field, and one
-// RK4 step of the whole field U with the scratch fields Y, K, ACC
-cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                    NeumannFaces nf, FieldF64 u, double t, FieldF64 out,
-                                    cudaStream_t s);
-cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                     NeumannFaces nf, FieldF64 U, FieldF64 Y, FieldF64 K,
-                                     FieldF64 ACC, double t, double dt, cudaStream_t s);
+// FP64 systems whose objects are not all Dirichlet (heat: also Neumann faces and the Gaussian
+// manufactured solution): rhs of the whole field, and one RK4 step of the whole field U with
+// the scratch fields Y, K, ACC
+cudaError_t launch_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                               const UnfusedAux& ux, FieldF64 u, double t, FieldF64 out,
+                               cudaStream_t s);
+cudaError_t launch_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                const UnfusedAux& ux, FieldF64 U, FieldF64 Y, FieldF64 K,
+                                FieldF64 ACC, double t, double dt, cudaStream_t s);
 // statistics of the non-Dirichlet cut points: out12[4d..4d+3] = {err, index (-1: none),
 // min, max} per axis
 cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, double* const R[3],
@@ -299,9 +307,9 @@ cudaError_t launch_stats_r(const DevOp& op, const DevR& dr, const DevSol& sol, d
 cudaError_t launch_error_field(const DevOp& op, const DevR& dr, const DevSol& sol, int prec,
                                const void* u0, double* const R[3], double t, FieldF64 err,
                                cudaStream_t s);
-// one forward Euler step of an FP64 system (fused: U = {b.u0, b.R}; unfused heat: the whole
+// one forward Euler step of an FP64 system (fused: U = {b.u0, b.R}; unfused: the whole
 // field); K is scratch for the right-hand side
-cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
+cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, const UnfusedAux& ux,
                               bool unfused, const StepBuffers& b, FieldF64 U, FieldF64 K, double t,
                               double dt, cudaStream_t s);
 cudaError_t launch_rhs(const DevOp& op, const SysParams& sp, int prec, const StepBuffers& b,

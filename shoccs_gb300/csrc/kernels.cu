@@ -233,6 +233,7 @@ __device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p
         return sym5(A.icf[1], A.icf[0], ldf(u, p - 2 * s), ldf(u, p - s), ldf(u, p),
                     ldf(u, p + s), ldf(u, p + 2 * s));
     }
+    if (A.antisym) return A.icf[2] * (ldf(u, p + s) - ldf(u, p - s)); // 3-point, zero centre
     return sym3(A.icf[0], ldf(u, p - s), ldf(u, p), ldf(u, p + s));
 }
 
@@ -953,6 +954,7 @@ __device__ __forceinline__ float interior_f(const DevAxis& A, const float* u, ID
         }
         return sym5(A.icf[1], A.icf[0], L(p - 2 * s), L(p - s), L(p), L(p + s), L(p + 2 * s));
     }
+    if (A.antisym) return A.icf[2] * (L(p + s) - L(p - s)); // 3-point, zero centre
     return sym3(A.icf[0], L(p - s), L(p), L(p + s));
 }
 
@@ -1198,6 +1200,7 @@ __device__ __forceinline__ float interior_row(const AX& A, float m2, float m1, f
         if (A.antisym) return fmaf(A.icf[3], p1 - m1, A.icf[4] * (p2 - m2));
         return sym5(A.icf[1], A.icf[0], m2, m1, c0, p1, p2);
     }
+    if (A.antisym) return A.icf[2] * (p1 - m1); // 3-point, zero centre
     return sym3(A.icf[0], m1, c0, p1);
 }
 
@@ -2931,17 +2934,106 @@ cudaError_t heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& s
 }
 } // namespace
 
-cudaError_t launch_heat_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                    NeumannFaces nf, FieldF64 u, double t, FieldF64 out,
-                                    cudaStream_t s)
+namespace
 {
-    return heat_rhs_unfused(op, dr, sp, nf, u, t, out, s);
+// the radial velocity field's -(x - c) / |x - c| at a point x (scalar_wave.cpp:28-33), in
+// radial_g64's operation order
+__device__ __forceinline__ void radial_g64x(const SysParams& sp, const double x[3], double g[3])
+{
+    const double r[3] = {x[0] - sp.center[0], x[1] - sp.center[1], x[2] - sp.center[2]};
+    const double len = sqrt(r[0] * r[0] + (r[1] * r[1] + r[2] * r[2]));
+    g[0] = -r[0] / len;
+    g[1] = -r[1] / len;
+    g[2] = -r[2] / len;
 }
 
-// one RK4 step of the whole field U (rk4.cpp:16-47) with the scratch fields Y, K, ACC
-cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
-                                     NeumannFaces nf, FieldF64 U, FieldF64 Y, FieldF64 K,
-                                     FieldF64 ACC, double t, double dt, cudaStream_t s)
+// scalar_wave::build_rhs_graph on the whole field (src/systems/scalar_wave.cpp:241-321):
+// K <- gG . grad u with gG = -a (constant velocity) or the radial field, and gG zero on
+// Dirichlet faces and at Dirichlet cut points (scalar_wave.cpp:79-95).  G0..G2: the
+// gradient's components over the whole field (D rows, then the R-space rows at the cut
+// points).  Points without a row (solid points) take 0, as in the fused stage kernels; the
+// dot product is the fused kernels' (fma(g2, d2, fma(g1, d1, g0 d0))).  With f.on the value
+// goes into the RK4 registers instead (StageFold).
+__global__ void k_wave_rhs_finish(DevOp op, DevR dr, SysParams sp, FieldF64 G0, FieldF64 G1,
+                                  FieldF64 G2, FieldF64 K, StageFold f)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    auto put = [&](double* k, double* acc, double* y, const double* u, long long j, double v) {
+        if (!f.on) {
+            k[j] = v;
+            return;
+        }
+        acc[j] = __dadd_rn(acc[j], __dmul_rn(f.c_acc, v));
+        if (f.has_y) y[j] = __dadd_rn(u[j], __dmul_rn(f.c_y, v));
+    };
+    double gv[3] = {-sp.vel[0], -sp.vel[1], -sp.vel[2]};
+    if (part == 0) {
+        const unsigned c = op.cls[i];
+        double v = 0.0;
+        if ((c & 0x3Fu) && !(c & CLS_DIRFACE)) {
+            if (sp.vel_kind != 0) {
+                int ijk[3];
+                phys_of_point(op, i, ijk);
+                radial_g64(sp, op, ijk, gv);
+            }
+            v = fma(gv[2], G2.D[i], fma(gv[1], G1.D[i], gv[0] * G0.D[i]));
+        }
+        put(K.D, f.acc.D, f.y.D, f.u.D, i, v);
+    } else {
+        const int d = part - 1;
+        double v = 0.0;
+        if (!dr.dirichlet[d][i]) {
+            if (sp.vel_kind != 0) radial_g64x(sp, dr.pos[d] + 3 * i, gv);
+            v = fma(gv[2], G2.R[d][i], fma(gv[1], G1.R[d][i], gv[0] * G0.R[d][i]));
+        }
+        put(K.R[d], f.acc.R[d], f.y.R[d], f.u.R[d], i, v);
+    }
+}
+
+cudaError_t wave_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                             const UnfusedAux& ux, FieldF64 u, double t, FieldF64 K, cudaStream_t s,
+                             StageFold fold = {})
+{
+    (void)t; // the wave's right-hand side has no time-dependent term
+    const void* uR[3] = {u.R[0], u.R[1], u.R[2]};
+    void* const out[3][4] = {
+        {ux.grad[0].D, ux.grad[0].R[0], ux.grad[0].R[1], ux.grad[0].R[2]},
+        {ux.grad[1].D, ux.grad[1].R[0], ux.grad[1].R[1], ux.grad[1].R[2]},
+        {ux.grad[2].D, ux.grad[2].R[0], ux.grad[2].R[1], ux.grad[2].R[2]}};
+    cudaError_t e = launch_gradient(op, PREC_FP64, u.D, uR, out, s);
+    if (e != cudaSuccess) return e;
+    const long long n = field_size(op);
+    k_wave_rhs_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, dr, sp, ux.grad[0], ux.grad[1],
+                                                                  ux.grad[2], K, fold);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, const UnfusedAux& ux,
+                        FieldF64 u, double t, FieldF64 K, cudaStream_t s, StageFold fold = {})
+{
+    if (sp.kind == SYS_WAVE) return wave_rhs_unfused(op, dr, sp, ux, u, t, K, s, fold);
+    return heat_rhs_unfused(op, dr, sp, ux.nf, u, t, K, s, fold);
+}
+} // namespace
+
+cudaError_t launch_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                               const UnfusedAux& ux, FieldF64 u, double t, FieldF64 out,
+                               cudaStream_t s)
+{
+    return rhs_unfused(op, dr, sp, ux, u, t, out, s);
+}
+
+// one RK4 step of the whole field U (rk4.cpp:16-47) with the scratch fields Y, K, ACC; the
+// boundary data of each stage input and of the result are the exact solution on Dirichlet
+// faces and at Dirichlet cut points (heat::update_boundary and scalar_wave::update_boundary
+// set the same values there)
+cudaError_t launch_step_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
+                                const UnfusedAux& ux, FieldF64 U, FieldF64 Y, FieldF64 K,
+                                FieldF64 ACC, double t, double dt, cudaStream_t s)
 {
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -2961,7 +3053,7 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
     for (int i = 0; i < 4 && e == cudaSuccess; i++) {
         const double ti = t + dt * rki[i];
         const StageFold fold{1, ACC, dt * rkf[i], i < 3, Y, U, i < 3 ? dt * rki[i + 1] : 0.0};
-        e = heat_rhs_unfused(op, dr, sp, nf, i == 0 ? U : Y, ti, K, s, fold);
+        e = rhs_unfused(op, dr, sp, ux, i == 0 ? U : Y, ti, K, s, fold);
         if (e != cudaSuccess) break;
         if (i < 3) {
             const double tn = t + dt * rki[i + 1];
@@ -2982,11 +3074,11 @@ cudaError_t launch_heat_step_unfused(const DevOp& op, const DevR& dr, const SysP
 // right-hand side at the Dirichlet cut points), U <- U + dt K, then the boundary data at
 // t + dt (Dirichlet faces and Dirichlet cut points).  For fused systems U.D is b.u0 and U.R
 // the state's cut-point values b.R.
-cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, NeumannFaces nf,
+cudaError_t launch_euler_fp64(const DevOp& op, const DevR& dr, const SysParams& sp, const UnfusedAux& ux,
                               bool unfused, const StepBuffers& b, FieldF64 U, FieldF64 K, double t,
                               double dt, cudaStream_t s)
 {
-    cudaError_t e = unfused ? heat_rhs_unfused(op, dr, sp, nf, U, t, K, s)
+    cudaError_t e = unfused ? rhs_unfused(op, dr, sp, ux, U, t, K, s)
                             : launch_rhs(op, sp, PREC_FP64, b, t, K.D, K.R, s);
     if (e != cudaSuccess) return e;
     const long long n = field_size(op);

@@ -19,9 +19,28 @@ def random_spheres(n_spheres, seed, lo=0.15, hi=0.85, rmin=0.03, rmax=0.08, gap=
     return out
 
 
+# E2-poly (polyE2_1) parameters of the reference's scalar_wave.lua: floating alpha[6],
+# dirichlet alpha[3], interpolant alpha[4] (the single-array order of stencil.cpp:79-87)
+POLY_ALPHA_LUA = (0.7039278390946743, 0.5390086175376538, -0.647109821986589, 0.2051508287133347,
+                  0.6062051039572746, 0.8148425279273044, -0.10739761225713096,
+                  0.8736492896991024, 0.40413606410467495, 0.01, -0.01, 0.01, 0.04)
+
+
 def cases():
     from shoccs_gb300 import workloads as W
     return {
+        # E2-poly on the geometry of the reference's scalar_wave.lua: a Dirichlet quarter
+        # circle at (0, 0) and a Floating one at (2, 2) on [0, 2]^2, inflow faces Dirichlet
+        "poly_scalar_wave_2d": dict(n=(71, 71, 1), lo=(0, 0, 0), hi=(2, 2, 0),
+                                    spheres=[((0.0, 0.0, 0.0), np.pi / 10, DIR),
+                                             ((2.0, 2.0, 0.0), np.pi / 10, FLT)],
+                                    grid_bc=(DIR, FLT, DIR, FLT, FLT, FLT), scheme="polyE2_1",
+                                    alpha=POLY_ALPHA_LUA),
+        # E2-poly in 3-D: a Floating and a Dirichlet sphere
+        "poly_spheres_3d": dict(n=(28, 26, 30), lo=(0, 0, 0), hi=(1, 1, 1),
+                                spheres=[((0.35, 0.37, 0.4), 0.14, FLT),
+                                         ((0.66, 0.64, 0.62), 0.12, DIR)],
+                                grid_bc=(DIR, FLT) * 3, scheme="polyE2_1", alpha=POLY_ALPHA_LUA),
         # the operator microbenchmark's generator (8 seeded spheres, gap >= 8h) at 96^3:
         # E4_1 derivative with Dirichlet spheres, E4_2 Laplacian with Dirichlet and Floating
         "micro_e41_96": W.micro_case(96, "E4_1", (DIR,)),

@@ -7,7 +7,8 @@ Sources:
     text -> object_geometry_sphere.json
   * oracle/_ref/libshoccs_ref.so: the reference's own code compiled unmodified by
     oracle/build_ref.sh -> stencils_ref.json (closure blocks, interior rows, interpolants of
-    src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp), sphere_hits_ref.json (src/mesh/sphere.cpp ray /
+    src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp), stencils_poly_ref.json (the same of
+    src/stencils/polyE2_1.cpp for two parameter sets), sphere_hits_ref.json (src/mesh/sphere.cpp ray /
     sphere hits) and reference_pins.json (SHA-256 digests of the arrays of
     tests/golden/pins.py -- setup, operators, heat and scalar-wave systems -- on every case
     of tests/cases.py)
@@ -98,7 +99,7 @@ def ref_fixtures():
                 for psi in (0.1, 0.5, 0.95):
                     for right in (0, 1):
                         c = (D * 8)()
-                        n = lib.ref_stencil_interp_wall(scheme, i, D(y), D(psi), right, c)
+                        n = lib.ref_stencil_interp_wall(scheme, None, i, D(y), D(psi), right, c)
                         interp.append(dict(kind="wall", scheme=scheme, i=i, y=y, psi=psi,
                                            right=right, c=[float(v).hex() for v in c[:n]]))
     hits = []
@@ -127,6 +128,57 @@ def ref_fixtures():
 # the reference's own input files (paths within its tree)
 REFERENCE_INPUTS = ["heat.lua", "scalar_wave.lua", "scalar_wave_1d.lua", "eigenvalues.lua",
                     "lua-configs/brady_livescu_4_3_n61.lua", "lua-configs/brady_livescu_4_3.lua"]
+
+
+# E2-poly (polyE2_1) parameter sets: the one of the reference's scalar_wave.lua (floating,
+# dirichlet and interpolant alpha, in the single-array order of stencil.cpp:79-87) and a
+# seeded random one
+POLY_ALPHA = [
+    [0.7039278390946743, 0.5390086175376538, -0.647109821986589, 0.2051508287133347,
+     0.6062051039572746, 0.8148425279273044, -0.10739761225713096, 0.8736492896991024,
+     0.40413606410467495, 0.01, -0.01, 0.01, 0.04],
+    [float(v) for v in np.random.default_rng(20261206).uniform(-1.0, 1.0, 13)],
+]
+
+
+def poly_fixtures():
+    """polyE2_1's closure blocks, interior row and interpolants from the reference's own
+    src/stencils/polyE2_1.cpp (oracle/_ref) -> stencils_poly_ref.json"""
+    subprocess.check_call(["sh", os.path.join(REPO, "oracle", "build_ref.sh")],
+                          env=dict(os.environ, SHOCCS_REFERENCE_ROOT=REF))
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libshoccs_ref.so"))
+    D = ctypes.c_double
+    rng = np.random.default_rng(20261207)
+    psis = [1e-12, 1e-5, 0.01, 0.25, 0.5, 0.75, 0.999, 1.0] + list(rng.uniform(0.0, 1.0, 4))
+    out = dict(source="src/stencils/polyE2_1.cpp compiled in oracle/_ref", scheme=5,
+               alpha=POLY_ALPHA, nbs=[], interior=[], interp=[])
+    for ai, a in enumerate(POLY_ALPHA):
+        al = (D * 13)(*a)
+        for bc, n in ((0, 8), (1, 12)):
+            for psi in psis:
+                for right in (0, 1):
+                    for h in (2.0, 1.0 / 64, 0.1):
+                        c, x = (D * 64)(), (D * 8)()
+                        lib.ref_stencil_nbs(5, al, D(h), bc, D(psi), right, c, x)
+                        out["nbs"].append(dict(alpha=ai, bc=bc, psi=float(psi), right=right, h=h,
+                                               c=[float(v).hex() for v in c[:n]]))
+        for h in (2.0, 1.0 / 64, 1.0 / 255):
+            c = (D * 8)()
+            n = lib.ref_stencil_interior(5, al, D(h), c)
+            out["interior"].append(dict(alpha=ai, h=h, c=[float(v).hex() for v in c[:n]]))
+        for y in (-0.7, -0.3, 0.0, 0.2, 0.5, 0.9):
+            c = (D * 8)()
+            n = lib.ref_stencil_interp_interior(5, D(y), c)
+            out["interp"].append(dict(alpha=ai, kind="interior", y=y,
+                                      c=[float(v).hex() for v in c[:n]]))
+            for i in (0, 1):
+                for psi in (0.1, 0.5, 0.95, 1.0):
+                    for right in (0, 1):
+                        c = (D * 8)()
+                        n = lib.ref_stencil_interp_wall(5, al, i, D(y), D(psi), right, c)
+                        out["interp"].append(dict(alpha=ai, kind="wall", i=i, y=y, psi=psi,
+                                                  right=right, c=[float(v).hex() for v in c[:n]]))
+    return out
 
 
 def reference_inputs():
@@ -196,6 +248,8 @@ if __name__ == "__main__":
     st, hits = ref_fixtures()
     with open(os.path.join(HERE, "stencils_ref.json"), "w") as f:
         json.dump(st, f)
+    with open(os.path.join(HERE, "stencils_poly_ref.json"), "w") as f:
+        json.dump(poly_fixtures(), f)
     with open(os.path.join(HERE, "sphere_hits_ref.json"), "w") as f:
         json.dump(hits, f)
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:

@@ -21,6 +21,9 @@ WAVE_CASES = {
     "multi_sphere_e41": (None, 0.05),  # the first sphere's centre
     "micro_e41_96": (None, 0.05),
     "box_e4u": ((-0.3, -0.2, -0.1), 0.1),
+    # scalar_wave.lua's system: radial wave about (-1, -1), radius 0
+    "poly_scalar_wave_2d": ((-1.0, -1.0, 0.0), 0.0),
+    "poly_spheres_3d": ((-0.3, -0.2, -0.1), 0.1),
 }
 HEAT_SCHEMES = ("E2_2", "E4_2")
 KAPPA = 0.7

@@ -8,6 +8,10 @@ Neumann data, evaluated at each right-hand side's time (heat::update_boundary,
 src/systems/heat.cpp:324-352).  The FP64 heat system runs these cases on its unfused path;
 everything is checked against the oracle's heat rhs, rk4 and stats.
 
+The FP64 scalar wave with Floating objects takes the same unfused path (right-hand side
+gG . grad u over the whole field) and is checked against the oracle's wave rhs, rk4 and stats,
+with constant and radial velocity.
+
 Tolerances (max-norm, relative to the oracle array's max-norm): rhs 1e-11, RK4 state 1e-10
 (FP64 arithmetic in a different order); errors, min and max to 1e-8; each argmax index must
 carry the maximum error (ties to rounding on symmetric geometries).
@@ -18,6 +22,7 @@ import pytest
 import shoccs_gb300 as S
 from oracle.oracle import OracleProblem
 from shoccs_gb300 import workloads as W
+from tests.cases import cases
 
 CASES = {
     "circle65_floating": dict(n=(65, 65, 1), lo=(0, 0, 0), hi=(1, 1, 0),
@@ -125,14 +130,97 @@ def test_floating_rk4_and_stats_match_oracle(name):
         assert err[int(st[k])] >= err.max() * (1 - 1e-8), (name, k, st[k], ref[k])
 
 
+# the scalar wave with Floating objects (FP64, unfused): the cut-point values of a Floating
+# object evolve by gG . grad u from the gradient's R-space rows (scalar_wave.cpp:241-321);
+# Dirichlet faces and Dirichlet cut points take the exact solution (scalar_wave.cpp:329-355)
+# (the first-derivative schemes E4_1 and E4u_1 have no cross-direction interpolant, so the
+# reference takes Floating objects with the E2-poly scheme; cases of tests/cases.py)
+WAVE_CASES = {name: cases()[name] for name in ("poly_scalar_wave_2d", "poly_spheres_3d")}
+VEL = (1.0, 0.7, 0.4)
+PULSE = [0.3, 0.3, 0.3, 1.0, 0.7, 0.4, 0.08]  # Gaussian pulse (x0, a, sigma)
+
+
+WAVE_CENTER = (-1.0, -1.0, 0.0)  # the radial velocity's centre, outside both domains
+
+
+def _wave(c, vel_kind):
+    p = S.Problem(**c)
+    w = S.ScalarWave(p, S.PREC_FP64, vel_kind, VEL, WAVE_CENTER, 2, PULSE)
+    w.initialize(0.0)
+    return p, w
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vel_kind", [S.VEL_CONSTANT, S.VEL_RADIAL])
+@pytest.mark.parametrize("name", sorted(WAVE_CASES))
+def test_wave_floating_rhs_matches_oracle(name, vel_kind):
+    import torch
+    c = WAVE_CASES[name]
+    p, w = _wave(c, vel_kind)
+    assert w.stage_kernel == "unfused"
+    o = OracleProblem(**c)
+    u = _state(w, p)
+    want = o.wave_rhs(vel_kind, VEL, WAVE_CENTER, u)
+    got = w.rhs(0.01, p.zeros(torch.float64))
+    for k, (g, wv) in enumerate(zip(got, want)):
+        assert rel(g.cpu().numpy(), wv) <= 1e-11, (name, k)
+    # the Floating object's cut points have a nonzero right-hand side (they evolve)
+    assert any(np.abs(wv).max() > 0 for wv in want[1:])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vel_kind", [S.VEL_CONSTANT, S.VEL_RADIAL])
+@pytest.mark.parametrize("name", sorted(WAVE_CASES))
+def test_wave_floating_rk4_and_stats_match_oracle(name, vel_kind):
+    c = WAVE_CASES[name]
+    p, w = _wave(c, vel_kind)
+    o = OracleProblem(**c)
+    u0 = _state(w, p)
+    h = min((c["hi"][a] - c["lo"][a]) / (c["n"][a] - 1) for a in range(3) if c["n"][a] > 1)
+    dt, steps = 0.4 * h, 20
+    w.rk4(0.0, dt, steps)
+    got = _state(w, p)
+    want = o.wave_rk4(vel_kind, VEL, WAVE_CENTER, 2, PULSE, 0.0, dt, steps, u0)
+    for k, (g, wv) in enumerate(zip(got, want)):
+        assert rel(g, wv) <= 1e-10, (name, k)
+    t = steps * dt
+    st, ok = w.stats(t)
+    ref = o.stats(2, PULSE, t, want)
+    for k in (0, 1, 2, 3, 5, 7, 9):  # errors, min, max
+        assert abs(st[k] - ref[k]) <= 1e-8 * max(abs(ref[k]), 1e-12), (name, k, st[k], ref[k])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
+def test_wave_poly_e2_dirichlet_fused_matches_oracle(prec):
+    """E2-poly (3-point antisymmetric interior) with Dirichlet objects only: the fused stage
+    kernels, FP64 and mixed, against the oracle's RK4"""
+    c = dict(WAVE_CASES["poly_spheres_3d"])
+    c["spheres"] = [(cc, r, "dirichlet") for cc, r, _ in c["spheres"]]
+    p = S.Problem(**c)
+    o = OracleProblem(**c)
+    w = S.ScalarWave(p, prec, S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE)
+    w.initialize(0.0)
+    assert w.stage_kernel != "unfused"
+    u0 = o.initialize(2, PULSE, 0.0)
+    h = 1.0 / (max(c["n"]) - 1)
+    dt, steps = 0.4 * h, 20
+    w.rk4(0.0, dt, steps)
+    got = _state(w, p)
+    want = o.wave_rk4(S.VEL_CONSTANT, VEL, (0, 0, 0), 2, PULSE, 0.0, dt, steps, u0)
+    assert rel(got[0], want[0]) <= (1e-10 if prec == S.PREC_FP64 else 2e-5)
+
+
 @pytest.mark.gpu
 def test_floating_systems_that_stay_unsupported():
     c = dict(CASES["circle65_floating"])
     p = S.Problem(**c)
     with pytest.raises(S.ShoccsError):  # mixed precision: the fused path only
         S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
-    with pytest.raises(S.ShoccsError):  # the wave system
-        S.ScalarWave(p, S.PREC_FP64)
+    pw = S.Problem(**WAVE_CASES["poly_scalar_wave_2d"])
+    assert S.ScalarWave(pw, S.PREC_FP64).stage_kernel == "unfused"
+    with pytest.raises(S.ShoccsError):  # the mixed wave: the fused path only
+        S.ScalarWave(pw, S.PREC_MIXED)
     h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
     with pytest.raises(S.ShoccsError):  # the adjoint covers Dirichlet objects
         h.forward(0.0, 1e-5, 2)
@@ -142,7 +230,7 @@ def test_floating_systems_that_stay_unsupported():
     assert S.Heat(pno, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL).stage_kernel == "unfused"
     with pytest.raises(S.ShoccsError):  # Neumann objects: FP64 heat only
         S.Heat(pno, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
-    with pytest.raises(S.ShoccsError):
+    with pytest.raises(S.ShoccsError):  # Neumann objects: no first-derivative closures
         S.ScalarWave(pno, S.PREC_FP64)
     pn = S.Problem(**CASES["neumann_x_circle65"])
     with pytest.raises(S.ShoccsError):  # Neumann faces: FP64 heat only

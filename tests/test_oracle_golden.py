@@ -1,7 +1,8 @@
 """Pin the CPU oracle against the reference's own golden vectors and code.
 
-* stencils_ref.json / sphere_hits_ref.json: produced by the reference's own
-  src/stencils/{E2_2,E4_2,E4_1}.cpp and src/mesh/sphere.cpp (oracle/_ref) -> bit-exact.
+* stencils_ref.json / stencils_poly_ref.json / sphere_hits_ref.json: produced by the
+  reference's own src/stencils/{E2_2,E4_2,E4_1,E4u_1,polyE2_1}.cpp and src/mesh/sphere.cpp
+  (oracle/_ref) -> bit-exact.
 * object_geometry_sphere.json: the expected values of src/mesh/object_geometry.t.cpp:11-330.
 * line segmentation: the assertions of src/mesh/mesh.t.cpp:71-141.
 * known-answer polynomial tests in the style of src/operators/derivative.t.cpp:235-261,
@@ -49,7 +50,36 @@ def test_stencils_bit_exact_vs_reference_code():
         if e["kind"] == "interior":
             n = L.orc_stencil_interp_interior(e["scheme"], D(e["y"]), c)
         else:
-            n = L.orc_stencil_interp_wall(e["scheme"], e["i"], D(e["y"]), D(e["psi"]),
+            n = L.orc_stencil_interp_wall(e["scheme"], None, e["i"], D(e["y"]), D(e["psi"]),
+                                          e["right"], c)
+        want = _hex(e["c"])
+        assert n == len(want)
+        assert np.array_equal(np.array(c[:n]).view(np.int64), want.view(np.int64)), e
+
+
+def test_poly_e2_stencil_bit_exact_vs_reference_code():
+    """E2-poly (polyE2_1): closure blocks (Dirichlet 2 x 4, Floating 3 x 4), interior row and
+    interpolants of src/stencils/polyE2_1.cpp compiled in oracle/_ref, for the parameters of
+    the reference's scalar_wave.lua and a random set."""
+    g = json.load(open(os.path.join(GOLD, "stencils_poly_ref.json")))
+    L = orc.lib()
+    als = [(D * 13)(*a) for a in g["alpha"]]
+    for e in g["nbs"]:
+        c, x = (D * 64)(), (D * 8)()
+        L.orc_stencil_nbs(5, als[e["alpha"]], D(e["h"]), e["bc"], D(e["psi"]), e["right"], c, x)
+        want = _hex(e["c"])
+        assert np.array_equal(np.array(c[:len(want)]).view(np.int64), want.view(np.int64)), e
+    for e in g["interior"]:
+        c = (D * 8)()
+        L.orc_stencil_interior(5, D(e["h"]), c)
+        want = _hex(e["c"])
+        assert np.array_equal(np.array(c[:len(want)]).view(np.int64), want.view(np.int64)), e
+    for e in g["interp"]:
+        c = (D * 8)()
+        if e["kind"] == "interior":
+            n = L.orc_stencil_interp_interior(5, D(e["y"]), c)
+        else:
+            n = L.orc_stencil_interp_wall(5, als[e["alpha"]], e["i"], D(e["y"]), D(e["psi"]),
                                           e["right"], c)
         want = _hex(e["c"])
         assert n == len(want)

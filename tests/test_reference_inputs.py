@@ -10,10 +10,12 @@ reader evaluates them, with the exit status of `shoccs --check` on each.
   not Lua), and the reader still gives the recorded tables.
 * CPU: a table written back out as Lua source reads back as the same table.
 * GPU: heat.lua (2-D heat, E2, a Floating circle, the gaussian manufactured solution,
-  diffusivity 1/30, to t = 0.3) and brady_livescu_4_3_n61.lua (the Brady-Livescu radial wave
-  with E4u, shortened to t = 0.2 by --script) run through the command line from their
-  recorded tables; every step's Linf error in logs/system.csv equals the oracle's (the
-  reference's heat / scalar_wave RK4 restated) within 1e-10 of the solution's scale.
+  diffusivity 1/30, to t = 0.3), brady_livescu_4_3_n61.lua (the Brady-Livescu radial wave
+  with E4u, shortened to t = 0.2 by --script) and scalar_wave.lua (the radial wave with the
+  E2-poly scheme around a Dirichlet and a Floating quarter circle, its 20 steps) run through
+  the command line from their recorded tables; every step's Linf error in logs/system.csv
+  equals the oracle's (the reference's heat / scalar_wave RK4 restated) within 1e-10 of the
+  solution's scale.
 """
 import json
 import os
@@ -146,5 +148,30 @@ def test_reference_brady_livescu_input_runs(tmp_path):
     sol = list(c) + [sy["radius"]]
     o = OracleProblem(**case)
     assert rows[-1][0] >= 0.2 - 1e-12 and len(rows) > 5
+    _compare(rows, lambda u, t, dt: o.wave_rk4(1, (0, 0, 0), c, 3, sol, t, dt, 1, u),
+             lambda t, u: o.stats(3, sol, t, u)[0], o.initialize(3, sol, 0.0))
+
+
+@pytest.mark.gpu
+def test_reference_scalar_wave_input_runs(tmp_path):
+    from oracle.oracle import OracleProblem
+    table = _inputs()["scalar_wave.lua"]["table"]
+    rows = _run_cli(table, tmp_path)
+    m, sc, sy = table["mesh"], table["scheme"], table["system"]
+    n = (int(m["index_extents"]["1"]), int(m["index_extents"]["2"]), 1)
+    hi = (m["domain_bounds"]["1"], m["domain_bounds"]["2"], 0.0)
+    arr = lambda t: [t[str(i + 1)] for i in range(len(t))]
+    alpha = arr(sc["floating_alpha"]) + arr(sc["dirichlet_alpha"]) + arr(sc["interpolant_alpha"])
+    shapes = [table["shapes"][k] for k in sorted(table["shapes"], key=int)]
+    spheres = [((s_["center"]["1"], s_["center"]["2"], 0.0), s_["radius"], s_["boundary_condition"])
+               for s_ in shapes]
+    case = dict(n=n, lo=(0, 0, 0), hi=hi, spheres=spheres,
+                grid_bc=("dirichlet", "floating", "dirichlet", "floating", "floating", "floating"),
+                scheme="polyE2_1", alpha=alpha)
+    c = (sy["center"]["1"], sy["center"]["2"], 0.0)
+    sol = list(c) + [sy["radius"]]
+    o = OracleProblem(**case)
+    # max_step = 20 ends the run (max_time = 500)
+    assert len(rows) == 21
     _compare(rows, lambda u, t, dt: o.wave_rk4(1, (0, 0, 0), c, 3, sol, t, dt, 1, u),
              lambda t, u: o.stats(3, sol, t, u)[0], o.initialize(3, sol, 0.0))
