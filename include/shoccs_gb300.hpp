@@ -151,7 +151,9 @@ namespace stencils
 struct stencil {
     int scheme;                  // SHOCCS_SCHEME_*
     std::array<real, 2> alpha{}; // E4_1 / E4u_1 closure parameters
-    std::array<real, 13> poly{}; // E2-poly: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]
+    // E2-poly: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]; E6u: alpha[5];
+    // E8u: alpha[7]
+    std::array<real, 13> params{};
 };
 
 inline stencil make_E2_2() { return {SHOCCS_SCHEME_E2_2, {}}; }
@@ -183,9 +185,22 @@ inline stencil make_polyE2_1(std::span<const real> floating_alpha, std::span<con
                              std::span<const real> interpolant_alpha)
 {
     stencil st{SHOCCS_SCHEME_POLYE2_1, {}};
-    for (size_t i = 0; i < 6 && i < floating_alpha.size(); i++) st.poly[i] = floating_alpha[i];
-    for (size_t i = 0; i < 3 && i < dirichlet_alpha.size(); i++) st.poly[6 + i] = dirichlet_alpha[i];
-    for (size_t i = 0; i < 4 && i < interpolant_alpha.size(); i++) st.poly[9 + i] = interpolant_alpha[i];
+    for (size_t i = 0; i < 6 && i < floating_alpha.size(); i++) st.params[i] = floating_alpha[i];
+    for (size_t i = 0; i < 3 && i < dirichlet_alpha.size(); i++) st.params[6 + i] = dirichlet_alpha[i];
+    for (size_t i = 0; i < 4 && i < interpolant_alpha.size(); i++) st.params[9 + i] = interpolant_alpha[i];
+    return st;
+}
+// src/stencils/E6u_1.cpp:207, E8u_1.cpp:303; alpha copied zero-padded to 5 / 7 values
+inline stencil make_E6u_1(std::span<const real> alpha)
+{
+    stencil st{SHOCCS_SCHEME_E6U_1, {}};
+    for (size_t i = 0; i < 5 && i < alpha.size(); i++) st.params[i] = alpha[i];
+    return st;
+}
+inline stencil make_E8u_1(std::span<const real> alpha)
+{
+    stencil st{SHOCCS_SCHEME_E8U_1, {}};
+    for (size_t i = 0; i < 7 && i < alpha.size(); i++) st.params[i] = alpha[i];
     return st;
 }
 } // namespace stencils
@@ -300,7 +315,7 @@ public:
         d.scheme = st.scheme;
         d.alpha[0] = st.alpha[0];
         d.alpha[1] = st.alpha[1];
-        for (int i = 0; i < 13; i++) d.poly_alpha[i] = st.poly[i];
+        for (int i = 0; i < 13; i++) d.scheme_alpha[i] = st.params[i];
         shoccs_problem* raw = nullptr;
         detail::check(shoccs_problem_create(&d, &raw), "shoccs_problem_create");
         p_.reset(raw, [](shoccs_problem* q) { shoccs_problem_destroy(q); });

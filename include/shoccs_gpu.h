@@ -74,7 +74,9 @@ enum { SHOCCS_BC_DIRICHLET = 0, SHOCCS_BC_FLOATING = 1, SHOCCS_BC_NEUMANN = 2 };
 /* schemes: scheme.order/type of stencil::from_lua (src/stencils/stencil.cpp:35-50) */
 enum { SHOCCS_SCHEME_E2_2 = 0, SHOCCS_SCHEME_E4_2 = 1, SHOCCS_SCHEME_E4_1 = 2,
        SHOCCS_SCHEME_E4U_1 = 3 /* type "E4u" (src/stencils/stencil.cpp:51-53) */,
-       SHOCCS_SCHEME_POLYE2_1 = 5 /* type "E2-poly" (src/stencils/stencil.cpp:78-100) */ };
+       SHOCCS_SCHEME_POLYE2_1 = 5 /* type "E2-poly" (src/stencils/stencil.cpp:78-100) */,
+       SHOCCS_SCHEME_E6U_1 = 6 /* type "E6u" (src/stencils/stencil.cpp:54-56) */,
+       SHOCCS_SCHEME_E8U_1 = 7 /* type "E8u" (src/stencils/stencil.cpp:57-59) */ };
 
 /* arithmetic of the operator and system kernels */
 enum {
@@ -93,8 +95,9 @@ typedef struct {
     int grid_bc[6];           /* xmin, xmax, ymin, ymax, zmin, zmax */
     int scheme;               /* SHOCCS_SCHEME_* */
     double alpha[2];          /* scheme.alpha (E4_1, E4u_1) */
-    double poly_alpha[13];    /* E2-poly: floating_alpha[6], dirichlet_alpha[3],
-                                 interpolant_alpha[4] (src/stencils/polyE2_1.cpp:16-28) */
+    double scheme_alpha[13];  /* E2-poly: floating_alpha[6], dirichlet_alpha[3],
+                                 interpolant_alpha[4] (src/stencils/polyE2_1.cpp:16-28);
+                                 E6u: alpha[5]; E8u: alpha[7] (E6u_1.cpp:18, E8u_1.cpp:18) */
 } shoccs_problem_desc;
 
 typedef struct shoccs_problem shoccs_problem;

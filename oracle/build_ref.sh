@@ -16,7 +16,7 @@ REF=${SHOCCS_REFERENCE_ROOT:-$(dirname "$(dirname "$HERE")")/reference}
 FMT_INC=$(python3 -c "import torch, os; print(os.path.join(os.path.dirname(torch.__file__), 'include'))")
 OBJ="$HERE/_ref/obj"
 mkdir -p "$OBJ"
-TUS="stencils/E2_2 stencils/E4_2 stencils/E4_1 stencils/E4u_1 stencils/polyE2_1 stencils/stencil
+TUS="stencils/E2_2 stencils/E4_2 stencils/E4_1 stencils/E4u_1 stencils/polyE2_1 stencils/E6u_1 stencils/E8u_1 stencils/stencil
      mesh/sphere mesh/rect mesh/cartesian mesh/object_geometry mesh/mesh
      matrices/csr matrices/inner_block matrices/circulant matrices/dense
      matrices/coefficient_visitor matrices/unit_stride_visitor

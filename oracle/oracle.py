@@ -20,7 +20,7 @@ IP = ctypes.POINTER(ctypes.c_int)
 LP = ctypes.POINTER(ctypes.c_long)
 
 BC = {"dirichlet": 0, "floating": 1, "neumann": 2}
-SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2, "E4u_1": 3, "polyE2_1": 5}
+SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2, "E4u_1": 3, "polyE2_1": 5, "E6u_1": 6, "E8u_1": 7}
 
 
 def build(force=False):
@@ -95,8 +95,9 @@ class OracleProblem:
             sbc[i] = _bc(b)
         self.n = n
         gbc = (ctypes.c_int * 6)(*[_bc(b) for b in grid_bc])
-        # E2-poly takes 13 parameters (floating, dirichlet, interpolant alpha), the others 2
-        al = (D * len(alpha))(*alpha) if len(alpha) == 13 else (D * 2)(*alpha)
+        # E2-poly takes 13 parameters (floating, dirichlet, interpolant alpha), E6u 5, E8u 7,
+        # the others 2
+        al = (D * max(2, len(alpha)))(*alpha)
         self._h = ctypes.c_void_p(L.orc_create(
             (ctypes.c_int * 3)(*n), (D * 3)(*lo), (D * 3)(*hi), ctypes.c_int(len(spheres)),
             _p(cen), _p(rad), sbc.ctypes.data_as(IP), gbc,

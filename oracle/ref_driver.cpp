@@ -72,8 +72,9 @@ REF_MEMBER(csr_w, matrix::csr, std::vector<real>, w)
 REF_MEMBER(csr_v, matrix::csr, std::vector<integer>, v)
 REF_MEMBER(csr_u, matrix::csr, std::vector<integer>, u)
 
-// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1; alpha: 2 values, or for polyE2_1 13
-// (floating alpha[6], dirichlet alpha[3], interpolant alpha[4], stencil.cpp:79-87's order)
+// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1, 6 E6u_1, 7 E8u_1; alpha: 2 values,
+// 13 for polyE2_1 (floating alpha[6], dirichlet alpha[3], interpolant alpha[4],
+// stencil.cpp:79-87's order), 5 for E6u_1, 7 for E8u_1
 static stencil make(int scheme, const double* alpha)
 {
     if (scheme == 5) {
@@ -81,6 +82,12 @@ static stencil make(int scheme, const double* alpha)
         if (alpha) std::copy(alpha, alpha + 13, a.begin());
         auto s = std::span<const real>{a};
         return make_polyE2_1(s.subspan(0, 6), s.subspan(6, 3), s.subspan(9, 4));
+    }
+    if (scheme == 6 || scheme == 7) {
+        const int n = scheme == 6 ? 5 : 7;
+        std::vector<real> a(n, 0.0);
+        if (alpha) std::copy(alpha, alpha + n, a.begin());
+        return scheme == 6 ? make_E6u_1(a) : make_E8u_1(a);
     }
     std::vector<real> a{alpha ? alpha[0] : 0.0, alpha ? alpha[1] : 0.0};
     switch (scheme) {

@@ -21,7 +21,7 @@ IP = ctypes.POINTER(ctypes.c_int)
 LP = ctypes.POINTER(ctypes.c_long)
 
 BC = {"dirichlet": 0, "floating": 1, "neumann": 2}
-SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2, "E4u_1": 3, "polyE2_1": 5}
+SCHEME = {"E2_2": 0, "E4_2": 1, "E4_1": 2, "E4u_1": 3, "polyE2_1": 5, "E6u_1": 6, "E8u_1": 7}
 
 _lib = None
 
@@ -72,7 +72,7 @@ class RefProblem:
             _p(cen), _p(rad), sbc.ctypes.data_as(IP),
             (ctypes.c_int * 6)(*[_bc(b) for b in grid_bc]),
             ctypes.c_int(SCHEME[scheme] if isinstance(scheme, str) else scheme),
-            (D * len(alpha))(*alpha) if len(alpha) == 13 else (D * 2)(*alpha)))
+            (D * max(2, len(alpha)))(*alpha)))
         self.size = L.ref_problem_size(self._h, 0)
         self.nR = tuple(L.ref_problem_size(self._h, d + 1) for d in range(3))
 
@@ -162,7 +162,7 @@ def _problem_args(n, lo, hi, spheres, grid_bc, scheme, alpha):
             _p(cen), _p(rad), sbc.ctypes.data_as(IP),
             (ctypes.c_int * 6)(*[_bc(b) for b in grid_bc]),
             ctypes.c_int(SCHEME[scheme] if isinstance(scheme, str) else scheme),
-            (D * len(alpha))(*alpha) if len(alpha) == 13 else (D * 2)(*alpha))
+            (D * max(2, len(alpha)))(*alpha))
     return n, args, keep
 
 

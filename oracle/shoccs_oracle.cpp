@@ -368,9 +368,12 @@ struct interp_info {
 };
 
 struct stencil {
-    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1, 3: E4u_1, 5: polyE2_1 (type "E2-poly")
+    int kind = 1; // 0: E2_2, 1: E4_2, 2: E4_1, 3: E4u_1, 5: polyE2_1 (type "E2-poly"),
+                  // 6: E6u_1, 7: E8u_1
     real alpha[2] = {0, 0};
-    real pa[13] = {}; // polyE2_1: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]
+    // polyE2_1: floating alpha[6], dirichlet alpha[3], interpolant alpha[4]; E6u_1: alpha[5];
+    // E8u_1: alpha[7]
+    real pa[13] = {};
 
     info query_max() const
     {
@@ -379,13 +382,15 @@ struct stencil {
         case 1: return {2, 3, 5, 3};
         case 3: return {2, 3, 5, 0};
         case 5: return {1, 3, 4, 0}; // polyE2_1.cpp:11-14
+        case 6: return {3, 5, 8, 0};  // E6u_1.cpp:13-16
+        case 7: return {4, 7, 11, 0}; // E8u_1.cpp:13-16
         default: return {2, 5, 7, 0};
         }
     }
     info query(int b) const
     {
         info mx = query_max();
-        if ((kind == 2 || kind == 3 || kind == 5) && b == Neumann) return {0, 0, 0, 0};
+        if ((kind == 2 || kind == 3 || kind >= 5) && b == Neumann) return {0, 0, 0, 0};
         switch (b) {
         case Dirichlet: return {mx.p, mx.r - 1, mx.t, 0};
         case Floating: return {mx.p, mx.r, mx.t, 0};
@@ -417,6 +422,24 @@ struct stencil {
             c[4] = -1 / (12. * (h * h));
         } else if (kind == 5) {
             pe2_interior(h, c);
+        } else if (kind == 6) { // E6u_1.cpp:49-60
+            c[0] = -1 / (60 * h);
+            c[1] = 3 / (20 * h);
+            c[2] = -3 / (4 * h);
+            c[3] = 0;
+            c[4] = -c[2];
+            c[5] = -c[1];
+            c[6] = -c[0];
+        } else if (kind == 7) { // E8u_1.cpp:48-61
+            c[0] = 1 / (280 * h);
+            c[1] = -4 / (105 * h);
+            c[2] = 1 / (5 * h);
+            c[3] = -4 / (5 * h);
+            c[4] = 0;
+            c[5] = -c[3];
+            c[6] = -c[2];
+            c[7] = -c[1];
+            c[8] = -c[0];
         } else if (kind == 3) { // E4u_1.cpp:49-58
             c[0] = 1 / (12 * h);
             c[1] = -2 / (3 * h);
@@ -450,6 +473,12 @@ struct stencil {
         } else if (kind == 5) {
             if (b == Floating) pe2_floating(h, psi, c, right);
             else if (b == Dirichlet) pe2_dirichlet(h, psi, c, right);
+        } else if (kind == 6) { // uniform-grid closures, psi ignored
+            if (b == Floating) e6u_floating(h, c, right);
+            else if (b == Dirichlet) e6u_dirichlet(h, c, right);
+        } else if (kind == 7) {
+            if (b == Floating) e8u_floating(h, c, right);
+            else if (b == Dirichlet) e8u_dirichlet(h, c, right);
         } else {
             if (b == Floating) e41_floating(h, psi, c, right);
             else if (b == Dirichlet) e41_dirichlet(h, psi, c, right);
@@ -577,6 +606,260 @@ struct stencil {
             }
         }
         return 4;
+    }
+
+    // ---- E6u_1, E8u_1 (uniform-grid closures, psi ignored): src/stencils/E6u_1.cpp:78-205,
+    // E8u_1.cpp:78-301, the generated expressions term for term
+    void e6u_floating(real h, real* c, bool right) const // E6u_1.cpp nbs_floating
+    {
+        const real* alpha = pa;
+        c[0] = (60 * alpha[0] - 137) / 60;
+        c[1] = 5 - 6 * alpha[0];
+        c[2] = 15 * alpha[0] - 5;
+        c[3] = -(60 * alpha[0] - 10) / 3;
+        c[4] = (60 * alpha[0] - 5) / 4;
+        c[5] = -(30 * alpha[0] - 1) / 5;
+        c[6] = alpha[0];
+        c[7] = 0;
+        c[8] = (5 * alpha[1] - 1) / 5;
+        c[9] = -(72 * alpha[1] + 13) / 12;
+        c[10] = 15 * alpha[1] + 2;
+        c[11] = (-20 * alpha[1]) - 1;
+        c[12] = (45 * alpha[1] + 1) / 3;
+        c[13] = -(120 * alpha[1] + 1) / 20;
+        c[14] = alpha[1];
+        c[15] = 0;
+        c[16] = (20 * alpha[2] + 1) / 20;
+        c[17] = -(12 * alpha[2] + 1) / 2;
+        c[18] = (45 * alpha[2] - 1) / 3;
+        c[19] = 1 - 20 * alpha[2];
+        c[20] = (60 * alpha[2] - 1) / 4;
+        c[21] = -(180 * alpha[2] - 1) / 30;
+        c[22] = alpha[2];
+        c[23] = 0;
+        c[24] = (180 * alpha[4] + 30 * alpha[3] - 1) / 30;
+        c[25] = -(140 * alpha[4] + 24 * alpha[3] - 1) / 4;
+        c[26] = 84 * alpha[4] + 15 * alpha[3] - 1;
+        c[27] = -(315 * alpha[4] + 60 * alpha[3] - 1) / 3;
+        c[28] = (140 * alpha[4] + 30 * alpha[3] + 1) / 2;
+        c[29] = -(420 * alpha[4] + 120 * alpha[3] + 1) / 20;
+        c[30] = alpha[3];
+        c[31] = alpha[4];
+        c[32] = -(190320 * alpha[4] + 31720 * alpha[3] + 22080 * alpha[2] + 38040 * alpha[1] + 9500 * alpha[0] - 453) / 28260;
+        c[33] = (55510 * alpha[4] + 9516 * alpha[3] + 6624 * alpha[2] + 11412 * alpha[1] + 2850 * alpha[0] - 159) / 1413;
+        c[34] = -(44408 * alpha[4] + 7930 * alpha[3] + 5520 * alpha[2] + 9510 * alpha[1] + 2375 * alpha[0] - 183) / 471;
+        c[35] = (166530 * alpha[4] + 31720 * alpha[3] + 22080 * alpha[2] + 38040 * alpha[1] + 9500 * alpha[0] - 1506) / 1413;
+        c[36] = -(444080 * alpha[4] + 95160 * alpha[3] + 66240 * alpha[2] + 114120 * alpha[1] + 28500 * alpha[0] - 1323) / 5652;
+        c[37] = (55510 * alpha[4] + 15860 * alpha[3] + 11040 * alpha[2] + 19020 * alpha[1] + 4750 * alpha[0] + 1551) / 2355;
+        c[38] = -(1586 * alpha[3] + 1104 * alpha[2] + 1902 * alpha[1] + 475 * alpha[0] + 192) / 1413;
+        c[39] = -(1586 * alpha[4] - 24) / 1413;
+        for (int i = 0; i < 40; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 40; i++) c[i] *= -1;
+            reverse(c, 40);
+        }
+    }
+    void e6u_dirichlet(real h, real* c, bool right) const // E6u_1.cpp nbs_dirichlet
+    {
+        const real* alpha = pa;
+        c[0] = (5 * alpha[1] - 1) / 5;
+        c[1] = -(72 * alpha[1] + 13) / 12;
+        c[2] = 15 * alpha[1] + 2;
+        c[3] = (-20 * alpha[1]) - 1;
+        c[4] = (45 * alpha[1] + 1) / 3;
+        c[5] = -(120 * alpha[1] + 1) / 20;
+        c[6] = alpha[1];
+        c[7] = 0;
+        c[8] = (20 * alpha[2] + 1) / 20;
+        c[9] = -(12 * alpha[2] + 1) / 2;
+        c[10] = (45 * alpha[2] - 1) / 3;
+        c[11] = 1 - 20 * alpha[2];
+        c[12] = (60 * alpha[2] - 1) / 4;
+        c[13] = -(180 * alpha[2] - 1) / 30;
+        c[14] = alpha[2];
+        c[15] = 0;
+        c[16] = (180 * alpha[4] + 30 * alpha[3] - 1) / 30;
+        c[17] = -(140 * alpha[4] + 24 * alpha[3] - 1) / 4;
+        c[18] = 84 * alpha[4] + 15 * alpha[3] - 1;
+        c[19] = -(315 * alpha[4] + 60 * alpha[3] - 1) / 3;
+        c[20] = (140 * alpha[4] + 30 * alpha[3] + 1) / 2;
+        c[21] = -(420 * alpha[4] + 120 * alpha[3] + 1) / 20;
+        c[22] = alpha[3];
+        c[23] = alpha[4];
+        c[24] = -(190320 * alpha[4] + 31720 * alpha[3] + 22080 * alpha[2] + 38040 * alpha[1] + 9500 * alpha[0] - 453) / 28260;
+        c[25] = (55510 * alpha[4] + 9516 * alpha[3] + 6624 * alpha[2] + 11412 * alpha[1] + 2850 * alpha[0] - 159) / 1413;
+        c[26] = -(44408 * alpha[4] + 7930 * alpha[3] + 5520 * alpha[2] + 9510 * alpha[1] + 2375 * alpha[0] - 183) / 471;
+        c[27] = (166530 * alpha[4] + 31720 * alpha[3] + 22080 * alpha[2] + 38040 * alpha[1] + 9500 * alpha[0] - 1506) / 1413;
+        c[28] = -(444080 * alpha[4] + 95160 * alpha[3] + 66240 * alpha[2] + 114120 * alpha[1] + 28500 * alpha[0] - 1323) / 5652;
+        c[29] = (55510 * alpha[4] + 15860 * alpha[3] + 11040 * alpha[2] + 19020 * alpha[1] + 4750 * alpha[0] + 1551) / 2355;
+        c[30] = -(1586 * alpha[3] + 1104 * alpha[2] + 1902 * alpha[1] + 475 * alpha[0] + 192) / 1413;
+        c[31] = -(1586 * alpha[4] - 24) / 1413;
+        for (int i = 0; i < 32; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 32; i++) c[i] *= -1;
+            reverse(c, 32);
+        }
+    }
+    void e8u_floating(real h, real* c, bool right) const // E8u_1.cpp nbs_floating
+    {
+        const real* alpha = pa;
+        c[0] = (140 * alpha[0] - 363) / 140;
+        c[1] = 7 - 8 * alpha[0];
+        c[2] = (56 * alpha[0] - 21) / 2;
+        c[3] = -(168 * alpha[0] - 35) / 3;
+        c[4] = (280 * alpha[0] - 35) / 4;
+        c[5] = -(280 * alpha[0] - 21) / 5;
+        c[6] = (168 * alpha[0] - 7) / 6;
+        c[7] = -(56 * alpha[0] - 1) / 7;
+        c[8] = alpha[0];
+        c[9] = 0;
+        c[10] = 0;
+        c[11] = (7 * alpha[1] - 1) / 7;
+        c[12] = -(160 * alpha[1] + 29) / 20;
+        c[13] = 28 * alpha[1] + 3;
+        c[14] = -(112 * alpha[1] + 5) / 2;
+        c[15] = (210 * alpha[1] + 5) / 3;
+        c[16] = -(224 * alpha[1] + 3) / 4;
+        c[17] = (140 * alpha[1] + 1) / 5;
+        c[18] = -(336 * alpha[1] + 1) / 42;
+        c[19] = alpha[1];
+        c[20] = 0;
+        c[21] = 0;
+        c[22] = (42 * alpha[2] + 1) / 42;
+        c[23] = -(24 * alpha[2] + 1) / 3;
+        c[24] = (1680 * alpha[2] - 47) / 60;
+        c[25] = -(168 * alpha[2] - 5) / 3;
+        c[26] = (420 * alpha[2] - 5) / 6;
+        c[27] = -(168 * alpha[2] - 1) / 3;
+        c[28] = (336 * alpha[2] - 1) / 12;
+        c[29] = -(840 * alpha[2] - 1) / 105;
+        c[30] = alpha[2];
+        c[31] = 0;
+        c[32] = 0;
+        c[33] = (105 * alpha[3] - 1) / 105;
+        c[34] = -(80 * alpha[3] - 1) / 10;
+        c[35] = (140 * alpha[3] - 3) / 5;
+        c[36] = -(224 * alpha[3] + 1) / 4;
+        c[37] = 70 * alpha[3] + 1;
+        c[38] = -(560 * alpha[3] + 3) / 10;
+        c[39] = (420 * alpha[3] + 1) / 15;
+        c[40] = -(1120 * alpha[3] + 1) / 140;
+        c[41] = alpha[3];
+        c[42] = 0;
+        c[43] = 0;
+        c[44] = (140 * alpha[4] + 1) / 140;
+        c[45] = -(120 * alpha[4] + 1) / 15;
+        c[46] = (280 * alpha[4] + 3) / 10;
+        c[47] = (-56 * alpha[4]) - 1;
+        c[48] = (280 * alpha[4] + 1) / 4;
+        c[49] = -(280 * alpha[4] - 3) / 5;
+        c[50] = (280 * alpha[4] - 1) / 10;
+        c[51] = -(840 * alpha[4] - 1) / 105;
+        c[52] = alpha[4];
+        c[53] = 0;
+        c[54] = 0;
+        c[55] = (840 * alpha[6] + 105 * alpha[5] - 1) / 105;
+        c[56] = -(756 * alpha[6] + 96 * alpha[5] - 1) / 12;
+        c[57] = (648 * alpha[6] + 84 * alpha[5] - 1) / 3;
+        c[58] = -(2520 * alpha[6] + 336 * alpha[5] - 5) / 6;
+        c[59] = (1512 * alpha[6] + 210 * alpha[5] - 5) / 3;
+        c[60] = -(22680 * alpha[6] + 3360 * alpha[5] - 47) / 60;
+        c[61] = (504 * alpha[6] + 84 * alpha[5] + 1) / 3;
+        c[62] = -(1512 * alpha[6] + 336 * alpha[5] + 1) / 42;
+        c[63] = alpha[5];
+        c[64] = alpha[6];
+        c[65] = 0;
+        c[66] = -(43994496 * alpha[6] + 5499312 * alpha[5] + 3756354 * alpha[4] + 7475328 * alpha[3] + 2303742 * alpha[2] + 7419216 * alpha[1] + 1545558 * alpha[0] - 28865) / 5022570;
+        c[67] = (8248968 * alpha[6] + 1047488 * alpha[5] + 715496 * alpha[4] + 1423872 * alpha[3] + 438808 * alpha[2] + 1413184 * alpha[1] + 294392 * alpha[0] - 5917) / 119585;
+        c[68] = -(113128704 * alpha[6] + 14664832 * alpha[5] + 10016944 * alpha[4] + 19934208 * alpha[3] + 6143312 * alpha[2] + 19784576 * alpha[1] + 4121488 * alpha[0] - 92067) / 478340;
+        c[69] = (164979360 * alpha[6] + 21997248 * alpha[5] + 15025416 * alpha[4] + 29901312 * alpha[3] + 9214968 * alpha[2] + 29676864 * alpha[1] + 6182232 * alpha[0] - 164197) / 358755;
+        c[70] = -(131983488 * alpha[6] + 18331040 * alpha[5] + 12521180 * alpha[4] + 24917760 * alpha[3] + 7679140 * alpha[2] + 24730720 * alpha[1] + 5151860 * alpha[0] - 190693) / 239170;
+        c[71] = (49493808 * alpha[6] + 7332416 * alpha[5] + 5008472 * alpha[4] + 9967104 * alpha[3] + 3071656 * alpha[2] + 9892288 * alpha[1] + 2060744 * alpha[0] - 163203) / 119585;
+        c[72] = -(87988992 * alpha[6] + 14664832 * alpha[5] + 10016944 * alpha[4] + 19934208 * alpha[3] + 6143312 * alpha[2] + 19784576 * alpha[1] + 4121488 * alpha[0] - 169433) / 478340;
+        c[73] = (32995872 * alpha[6] + 7332416 * alpha[5] + 5008472 * alpha[4] + 9967104 * alpha[3] + 3071656 * alpha[2] + 9892288 * alpha[1] + 2060744 * alpha[0] + 551009) / 837095;
+        c[74] = -(130936 * alpha[5] + 89437 * alpha[4] + 177984 * alpha[3] + 54851 * alpha[2] + 176648 * alpha[1] + 36799 * alpha[0] + 20016) / 119585;
+        c[75] = -(130936 * alpha[6] - 4176) / 119585;
+        c[76] = -432.0 / 119585;
+        for (int i = 0; i < 77; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 77; i++) c[i] *= -1;
+            reverse(c, 77);
+        }
+    }
+    void e8u_dirichlet(real h, real* c, bool right) const // E8u_1.cpp nbs_dirichlet
+    {
+        const real* alpha = pa;
+        c[0] = (7 * alpha[1] - 1) / 7;
+        c[1] = -(160 * alpha[1] + 29) / 20;
+        c[2] = 28 * alpha[1] + 3;
+        c[3] = -(112 * alpha[1] + 5) / 2;
+        c[4] = (210 * alpha[1] + 5) / 3;
+        c[5] = -(224 * alpha[1] + 3) / 4;
+        c[6] = (140 * alpha[1] + 1) / 5;
+        c[7] = -(336 * alpha[1] + 1) / 42;
+        c[8] = alpha[1];
+        c[9] = 0;
+        c[10] = 0;
+        c[11] = (42 * alpha[2] + 1) / 42;
+        c[12] = -(24 * alpha[2] + 1) / 3;
+        c[13] = (1680 * alpha[2] - 47) / 60;
+        c[14] = -(168 * alpha[2] - 5) / 3;
+        c[15] = (420 * alpha[2] - 5) / 6;
+        c[16] = -(168 * alpha[2] - 1) / 3;
+        c[17] = (336 * alpha[2] - 1) / 12;
+        c[18] = -(840 * alpha[2] - 1) / 105;
+        c[19] = alpha[2];
+        c[20] = 0;
+        c[21] = 0;
+        c[22] = (105 * alpha[3] - 1) / 105;
+        c[23] = -(80 * alpha[3] - 1) / 10;
+        c[24] = (140 * alpha[3] - 3) / 5;
+        c[25] = -(224 * alpha[3] + 1) / 4;
+        c[26] = 70 * alpha[3] + 1;
+        c[27] = -(560 * alpha[3] + 3) / 10;
+        c[28] = (420 * alpha[3] + 1) / 15;
+        c[29] = -(1120 * alpha[3] + 1) / 140;
+        c[30] = alpha[3];
+        c[31] = 0;
+        c[32] = 0;
+        c[33] = (140 * alpha[4] + 1) / 140;
+        c[34] = -(120 * alpha[4] + 1) / 15;
+        c[35] = (280 * alpha[4] + 3) / 10;
+        c[36] = (-56 * alpha[4]) - 1;
+        c[37] = (280 * alpha[4] + 1) / 4;
+        c[38] = -(280 * alpha[4] - 3) / 5;
+        c[39] = (280 * alpha[4] - 1) / 10;
+        c[40] = -(840 * alpha[4] - 1) / 105;
+        c[41] = alpha[4];
+        c[42] = 0;
+        c[43] = 0;
+        c[44] = (840 * alpha[6] + 105 * alpha[5] - 1) / 105;
+        c[45] = -(756 * alpha[6] + 96 * alpha[5] - 1) / 12;
+        c[46] = (648 * alpha[6] + 84 * alpha[5] - 1) / 3;
+        c[47] = -(2520 * alpha[6] + 336 * alpha[5] - 5) / 6;
+        c[48] = (1512 * alpha[6] + 210 * alpha[5] - 5) / 3;
+        c[49] = -(22680 * alpha[6] + 3360 * alpha[5] - 47) / 60;
+        c[50] = (504 * alpha[6] + 84 * alpha[5] + 1) / 3;
+        c[51] = -(1512 * alpha[6] + 336 * alpha[5] + 1) / 42;
+        c[52] = alpha[5];
+        c[53] = alpha[6];
+        c[54] = 0;
+        c[55] = -(43994496 * alpha[6] + 5499312 * alpha[5] + 3756354 * alpha[4] + 7475328 * alpha[3] + 2303742 * alpha[2] + 7419216 * alpha[1] + 1545558 * alpha[0] - 28865) / 5022570;
+        c[56] = (8248968 * alpha[6] + 1047488 * alpha[5] + 715496 * alpha[4] + 1423872 * alpha[3] + 438808 * alpha[2] + 1413184 * alpha[1] + 294392 * alpha[0] - 5917) / 119585;
+        c[57] = -(113128704 * alpha[6] + 14664832 * alpha[5] + 10016944 * alpha[4] + 19934208 * alpha[3] + 6143312 * alpha[2] + 19784576 * alpha[1] + 4121488 * alpha[0] - 92067) / 478340;
+        c[58] = (164979360 * alpha[6] + 21997248 * alpha[5] + 15025416 * alpha[4] + 29901312 * alpha[3] + 9214968 * alpha[2] + 29676864 * alpha[1] + 6182232 * alpha[0] - 164197) / 358755;
+        c[59] = -(131983488 * alpha[6] + 18331040 * alpha[5] + 12521180 * alpha[4] + 24917760 * alpha[3] + 7679140 * alpha[2] + 24730720 * alpha[1] + 5151860 * alpha[0] - 190693) / 239170;
+        c[60] = (49493808 * alpha[6] + 7332416 * alpha[5] + 5008472 * alpha[4] + 9967104 * alpha[3] + 3071656 * alpha[2] + 9892288 * alpha[1] + 2060744 * alpha[0] - 163203) / 119585;
+        c[61] = -(87988992 * alpha[6] + 14664832 * alpha[5] + 10016944 * alpha[4] + 19934208 * alpha[3] + 6143312 * alpha[2] + 19784576 * alpha[1] + 4121488 * alpha[0] - 169433) / 478340;
+        c[62] = (32995872 * alpha[6] + 7332416 * alpha[5] + 5008472 * alpha[4] + 9967104 * alpha[3] + 3071656 * alpha[2] + 9892288 * alpha[1] + 2060744 * alpha[0] + 551009) / 837095;
+        c[63] = -(130936 * alpha[5] + 89437 * alpha[4] + 177984 * alpha[3] + 54851 * alpha[2] + 176648 * alpha[1] + 36799 * alpha[0] + 20016) / 119585;
+        c[64] = -(130936 * alpha[6] - 4176) / 119585;
+        c[65] = -432.0 / 119585;
+        for (int i = 0; i < 66; i++) c[i] /= h;
+        if (right) {
+            for (int i = 0; i < 66; i++) c[i] *= -1;
+            reverse(c, 66);
+        }
     }
 
     // ---- E4u_1 (uniform-grid closures, psi ignored): src/stencils/E4u_1.cpp:77-127
@@ -1509,7 +1792,7 @@ static interp_deriv_info interp_deriv_coefficients(int dir, int n, real h,
 {
     auto q = st.query(bc);
     const int p = q.p, r = q.r, t = q.t;
-    std::vector<real> c(64), ex(8);
+    std::vector<real> c(128), ex(8);
     if (std::abs(obj.normal[dir]) > 1e-12) {
         const bool right_interp_wall = obj.normal[dir] < 0.0;
         st.nbs(h, bc, 1.0, right_interp_wall, c.data(), ex.data());
@@ -2036,14 +2319,16 @@ int orc_num_threads(int n)
 }
 
 // grid_bc: xmin,xmax,ymin,ymax,zmin,zmax (0 Dirichlet, 1 Floating, 2 Neumann)
-// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1; alpha: 2 values (E4_1, E4u_1), or
-// for polyE2_1 13 (floating alpha[6], dirichlet alpha[3], interpolant alpha[4])
+// scheme: 0 E2_2, 1 E4_2, 2 E4_1, 3 E4u_1, 5 polyE2_1, 6 E6u_1, 7 E8u_1; alpha: 2 values
+// (E4_1, E4u_1), 13 for polyE2_1 (floating alpha[6], dirichlet alpha[3], interpolant
+// alpha[4]), 5 for E6u_1, 7 for E8u_1
 static void set_params(stencil& st, int scheme, const double* alpha)
 {
     st.kind = scheme;
     if (!alpha) return;
-    if (scheme == 5) {
-        for (int i = 0; i < 13; i++) st.pa[i] = alpha[i];
+    if (scheme >= 5) { // polyE2_1: 13 values; E6u_1: 5; E8u_1: 7
+        const int n = scheme == 5 ? 13 : (scheme == 6 ? 5 : 7);
+        for (int i = 0; i < n; i++) st.pa[i] = alpha[i];
     } else {
         st.alpha[0] = alpha[0];
         st.alpha[1] = alpha[1];

@@ -28,7 +28,9 @@ ScalarField = namedtuple("ScalarField", ["D", "Rx", "Ry", "Rz"])
 
 _BC = {"dirichlet": BC_DIRICHLET, "floating": BC_FLOATING, "neumann": BC_NEUMANN}
 _SCHEME = {"E2_2": SCHEME_E2_2, "E4_2": SCHEME_E4_2, "E4_1": SCHEME_E4_1, "E4u_1": 3,
-           "polyE2_1": 5}
+           "polyE2_1": 5, "E6u_1": 6, "E8u_1": 7}
+# schemes whose parameters go in scheme_alpha, and how many each takes
+_SCHEME_ALPHA = {5: 13, 6: 5, 7: 7}
 
 
 def _bc(b):
@@ -60,9 +62,9 @@ class Problem:
 
     n, lo, hi: index_extents and domain_bounds; spheres: [(center3, radius, bc)];
     grid_bc: (xmin, xmax, ymin, ymax, zmin, zmax); scheme: "E2_2" | "E4_2" | "E4_1" | "E4u_1"
-    | "polyE2_1" (type "E2-poly"); alpha: the two alpha of E4_1 / E4u_1, or the thirteen of
-    E2-poly (floating_alpha[6], dirichlet_alpha[3], interpolant_alpha[4], the reference's
-    single-array order).
+    | "polyE2_1" (type "E2-poly") | "E6u_1" | "E8u_1"; alpha: the two alpha of E4_1 / E4u_1,
+    the thirteen of E2-poly (floating_alpha[6], dirichlet_alpha[3], interpolant_alpha[4], the
+    reference's single-array order), the five of E6u or the seven of E8u.
     """
 
     def __init__(self, n, lo, hi, spheres=(), grid_bc=("floating",) * 6, scheme="E4_2",
@@ -90,10 +92,11 @@ class Problem:
         d.sphere_bc = ctypes.cast(self._sbc, _capi.c_int_p)
         d.grid_bc[:] = [_bc(b) for b in grid_bc]
         d.scheme = _SCHEME[scheme] if isinstance(scheme, str) else int(scheme)
-        if d.scheme == _SCHEME["polyE2_1"]:
-            if len(alpha) != 13:
-                raise ValueError("E2-poly takes 13 alpha values")
-            d.poly_alpha[:] = [float(v) for v in alpha]
+        if d.scheme in _SCHEME_ALPHA:
+            na = _SCHEME_ALPHA[d.scheme]
+            if len(alpha) > na:
+                raise ValueError("scheme takes at most %d alpha values" % na)
+            d.scheme_alpha[:] = [float(v) for v in alpha] + [0.0] * (13 - len(alpha))
         else:
             d.alpha[:] = [float(alpha[0]), float(alpha[1])]
         self.desc = d

@@ -36,7 +36,7 @@ class ProblemDesc(ctypes.Structure):
         ("grid_bc", ctypes.c_int * 6),
         ("scheme", ctypes.c_int),
         ("alpha", ctypes.c_double * 2),
-        ("poly_alpha", ctypes.c_double * 13),
+        ("scheme_alpha", ctypes.c_double * 13),
     ]
 
 

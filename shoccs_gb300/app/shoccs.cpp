@@ -18,7 +18,8 @@
 //   simulation.domain_boundaries, shapes[i].boundary_condition
 //                              bcs::from_lua                src/operators/boundaries.cpp:7-90
 //   simulation.scheme          stencil::from_lua            src/stencils/stencil.cpp:8-106
-//                              (E2 / E4 second-derivative, E4 / E4u / E2-poly first-derivative)
+//                              (E2 / E4 second-derivative, E4 / E4u / E6u / E8u / E2-poly
+//                              first-derivative)
 //   simulation.system          system::from_lua, heat::from_lua, scalar_wave::from_lua
 //                              src/systems/system.cpp:103-132, heat.cpp:78-104,
 //                              scalar_wave.cpp:134-193
@@ -258,8 +259,16 @@ std::optional<stencil> read_stencil(const value& sim, const logger& log)
         log.info("interpolant alpha = " + join(ia));
         return stencils::make_polyE2_1(fa, da, ia);
     }
-    if (order == 1 && (type == "E2" || type == "E6u" || type == "E8u" || type == "tension_E4u" ||
-                       type == "gaussian_E4u" || type == "multiquadric_E4u")) {
+    if (order == 1 && type == "E6u") {
+        log.info("E6 uniform first scheme chosen");
+        return stencils::make_E6u_1(alpha);
+    }
+    if (order == 1 && type == "E8u") {
+        log.info("E8 uniform first scheme chosen");
+        return stencils::make_E8u_1(alpha);
+    }
+    if (order == 1 && (type == "E2" || type == "tension_E4u" || type == "gaussian_E4u" ||
+                       type == "multiquadric_E4u")) {
         log.err("scheme.order/type = 1 / " + type + " is not available in this build");
         return std::nullopt;
     }

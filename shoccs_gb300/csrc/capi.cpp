@@ -169,19 +169,22 @@ shoccs_status do_upload(shoccs_problem* p, cudaStream_t s)
         A.row_base = op.n_cut_rows;
         A.n_rows = (int)T.rows.size();
         op.n_cut_rows += A.n_rows;
-        for (int j = 0; j < 5; j++) {
+        for (int j = 0; j < 9; j++) {
             A.ic[j] = T.interior[j];
             A.icf[j] = (float)T.interior[j];
         }
-        A.antisym = T.width == 5 ? T.interior[2] == 0.0 && T.interior[0] == -T.interior[4] &&
-                                       T.interior[1] == -T.interior[3]
-                                 : T.width == 3 && T.interior[1] == 0.0 && T.interior[0] == -T.interior[2];
+        // antisymmetric (first derivative, zero centre) or symmetric interior rows
+        const int hw = T.width / 2;
+        bool anti = T.width >= 3 && T.interior[hw] == 0.0, sym = T.width >= 3;
+        for (int k = 1; k <= hw; k++) {
+            anti = anti && T.interior[hw - k] == -T.interior[hw + k];
+            sym = sym && T.interior[hw - k] == T.interior[hw + k];
+        }
+        A.antisym = anti;
         if (!T.active) continue;
-        // the FP32 kernels evaluate a non-antisymmetric interior as a symmetric
-        // zero-sum second-derivative row in difference form (sym5 / sym3)
-        if (!A.antisym && !(T.width == 5 ? T.interior[0] == T.interior[4] &&
-                                                T.interior[1] == T.interior[3]
-                                          : T.width == 3 && T.interior[0] == T.interior[2]))
+        // the FP32 kernels evaluate a non-antisymmetric interior as a symmetric zero-sum
+        // second-derivative row in difference form (sym5 / sym3: 3- and 5-point rows only)
+        if (!A.antisym && !(sym && T.width <= 5))
             return fail(SHOCCS_EINVAL, "interior stencil neither symmetric nor antisymmetric");
         SH_CUDA(p->mem.put(T.rows, &A.rows, s));
         SH_CUDA(p->mem.put(T.row_out, (const long long**)&A.row_out, s));
@@ -316,7 +319,7 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
     *out = nullptr;
     for (int i = 0; i < 3; i++)
         if (d->n[i] < 1) return fail(SHOCCS_EINVAL, "index_extents must be >= 1");
-    if (d->scheme < 0 || d->scheme > 5 || d->scheme == 4) return fail(SHOCCS_EINVAL, "unknown scheme");
+    if (d->scheme < 0 || d->scheme > 7 || d->scheme == 4) return fail(SHOCCS_EINVAL, "unknown scheme");
     if (d->n_spheres < 0 || (d->n_spheres && (!d->centers || !d->radii || !d->sphere_bc)))
         return fail(SHOCCS_EINVAL, "sphere arrays missing");
     for (int i = 0; i < 6; i++)
@@ -325,7 +328,7 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
         if (bad_bc(d->sphere_bc[i])) return fail(SHOCCS_EINVAL, "bad shape boundary condition");
     if (d->scheme == SHOCCS_SCHEME_POLYE2_1) {
         for (int i = 0; i < 13; i++)
-            if (!std::isfinite(d->poly_alpha[i])) return fail(SHOCCS_EINVAL, "E2-poly: non-finite alpha");
+            if (!std::isfinite(d->scheme_alpha[i])) return fail(SHOCCS_EINVAL, "E2-poly: non-finite alpha");
         for (int i = 0; i < 6; i++)
             if (d->grid_bc[i] == SHOCCS_BC_NEUMANN && d->n[i / 2] > 1)
                 return fail(SHOCCS_EUNSUPPORTED, "first-derivative schemes have no Neumann closure");
@@ -333,7 +336,8 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
             if (d->sphere_bc[i] == SHOCCS_BC_NEUMANN)
                 return fail(SHOCCS_EUNSUPPORTED, "first-derivative schemes have no Neumann closure");
     }
-    if (d->scheme == SHOCCS_SCHEME_E4_1 || d->scheme == SHOCCS_SCHEME_E4U_1) {
+    if (d->scheme == SHOCCS_SCHEME_E4_1 || d->scheme == SHOCCS_SCHEME_E4U_1 ||
+        d->scheme == SHOCCS_SCHEME_E6U_1 || d->scheme == SHOCCS_SCHEME_E8U_1) {
         // src/stencils/E4_1.cpp:34-41
         if (d->scheme == SHOCCS_SCHEME_E4_1 && d->alpha[1] < 197.0 / 288.0)
             return fail(SHOCCS_EINVAL,
@@ -361,7 +365,7 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
         p->st.kind = d->scheme;
         p->st.alpha[0] = d->alpha[0];
         p->st.alpha[1] = d->alpha[1];
-        for (int i = 0; i < 13; i++) p->st.pa[i] = d->poly_alpha[i];
+        for (int i = 0; i < 13; i++) p->st.pa[i] = d->scheme_alpha[i];
         // a boundary condition on a trivial axis is Floating (src/operators/boundaries.cpp:15-24)
         for (int a = 0; a < 3; a++)
             for (int side = 0; side < 2; side++) {
@@ -567,9 +571,14 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         cands.push_back({"vec", 0, 0, form, 4});
         cands.push_back({"vec3", 0, 0, form, 3});
     }
-    cands.push_back({"col1", 0, 1, 0});
-    cands.push_back({"col2", 0, 2, 0});
-    cands.push_back({"col4", 0, 4, 0});
+    // the column kernels keep a five-point window along each axis: interiors of up to 5 points
+    bool w5 = true;
+    for (int a = 0; a < 3; a++) w5 = w5 && (!S->P->op.ax[a].active || S->P->op.ax[a].width <= 5);
+    if (w5) {
+        cands.push_back({"col1", 0, 1, 0});
+        cands.push_back({"col2", 0, 2, 0});
+        cands.push_back({"col4", 0, 4, 0});
+    }
     cands.push_back({"point", 0, 0, 0});
     auto use = [&](const Cand& c) {
         S->b.tma = c.tma;
@@ -1585,6 +1594,9 @@ shoccs_status shoccs_batch_create(shoccs_system* const* systems, int n, shoccs_b
         if (S->unfused)
             return fail(SHOCCS_EUNSUPPORTED, "batched solves take systems whose objects are all Dirichlet");
         if (S->P->device != dev) return fail(SHOCCS_EINVAL, "systems on different devices");
+        for (int a = 0; a < 3; a++)
+            if (S->P->op.ax[a].active && S->P->op.ax[a].width > 5)
+                return fail(SHOCCS_EUNSUPPORTED, "batched solves take interiors of up to 5 points");
         const DevOp& op = S->P->op;
         if (op.N >= (1LL << 31) - 64) return fail(SHOCCS_EUNSUPPORTED, "instance above 2^31 points");
         B->sys.push_back(S);

@@ -13,12 +13,12 @@ namespace sgb
 
 struct DevAxis {
     int active;
-    int width;   // 2p+1 interior stencil width (3 or 5)
+    int width;   // 2p+1 interior stencil width (3, 5, 7 or 9)
     int antisym; // interior coefficients are antisymmetric with a zero centre (E4_1, E4u_1)
     int n;       // grid points along the axis
     long long stride;
-    double ic[5];
-    float icf[5];
+    double ic[9];   // interior coefficients, 2p+1 <= 9 (E8u_1)
+    float icf[9];
     WallBlock wall[2]; // rows shared by every line ending at the left / right wall
     // cut-cell closure rows, sorted by output index
     int n_rows;

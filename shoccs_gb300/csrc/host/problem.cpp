@@ -346,7 +346,7 @@ DerivRow interp_deriv_coefficients(int dir, int n, real h, const CutPoint& obj, 
 {
     const auto q = st.query(bc);
     const int p = q.p, r = q.r, t = q.t;
-    real c[64], ex[8];
+    real c[128], ex[8];
     if (std::abs(obj.nrm[dir]) > 1e-12) {
         const bool right_wall = obj.nrm[dir] < 0.0;
         st.nbs(h, bc, 1.0, right_wall, c, ex);
@@ -381,7 +381,7 @@ void cut_rows(int r, int dir, const Mesh& m, const Stencil& st, const Bcs& bcs, 
     const real h = m.h[dir];
     const i64 stride = m.stride(dir);
     std::vector<Coo> O, B;
-    real c[64], ex[8];
+    real c[128], ex[8];
     for (i64 row = 0; row < sz; ++row) {
         const auto& obj = cps[row];
         const int bc = bcs.obj[obj.shape_id];
@@ -450,7 +450,7 @@ AxisOp assemble_axis(int dir, const Mesh& m, const Stencil& st, const Bcs& bcs)
     A.interior.resize(2 * mx.p + 1);
     st.interior(h, A.interior.data());
 
-    real left[64], right[64], extra[8];
+    real left[128], right[128], extra[8];
     std::vector<Coo> B, N;
     for (const auto& ln : m.lines[dir]) {
         if (dirichlet_line(m, ln.s.ijk, dir, bcs)) continue;
@@ -662,7 +662,11 @@ Compiled compile_operators(const Mesh& m, const AxisOp ops[3], const Bcs& bcs)
         };
         for (size_t b = 0; b < A.meta.size(); b++) {
             const auto& bm = A.meta[b];
-            const bool lwall = A.block_wall[b] & 1, rwall = A.block_wall[b] & 2;
+            // a domain-wall block is stored once per axis and side when it fits the 5 x 7
+            // WallBlock (E6u_1's and E8u_1's do not); otherwise its rows are per-row records
+            // like the cut-cell rows
+            const bool lwall = (A.block_wall[b] & 1) && bm.left_rows <= 5 && bm.left_cols <= 7;
+            const bool rwall = (A.block_wall[b] & 2) && bm.right_rows <= 5 && bm.right_cols <= 7;
             const i64 st = bm.stride;
             for (int r = 0; r < bm.left_rows; r++) {
                 const i64 out = bm.row_offset + (i64)r * st;

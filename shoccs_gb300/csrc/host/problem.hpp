@@ -120,7 +120,7 @@ struct AxisTables {
     bool active = false;
     i64 stride = 1;
     int width = 0;
-    real interior[5] = {0, 0, 0, 0, 0};
+    real interior[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}; // 2p+1 <= 9 (E8u_1)
     WallBlock wall[2] = {};       // left / right domain-wall closure blocks
     std::vector<ClosureRow> rows; // cut-cell closure rows, sorted by output index
     std::vector<i64> row_out;     // output flat index of each row

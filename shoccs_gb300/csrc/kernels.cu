@@ -180,6 +180,12 @@ template <class TIN>
 __device__ __forceinline__ double interior64(const DevAxis& A, TIN u, long long p)
 {
     const long long s = A.stride;
+    if (A.width > 5) { // 7- and 9-point interiors (E6u_1, E8u_1), width 5's order
+        const int hw = A.width / 2;
+        double r = A.ic[0] * ldd(u, p - hw * s);
+        for (int k = 1; k < A.width; k++) r = fma(A.ic[k], ldd(u, p + (k - hw) * s), r);
+        return r;
+    }
     if (A.width == 5) {
         if (A.antisym) {
             const double d1 = ldd(u, p + s) - ldd(u, p - s);
@@ -224,6 +230,12 @@ template <class TIN>
 __device__ __forceinline__ float interior32(const DevAxis& A, TIN u, long long p)
 {
     const long long s = A.stride;
+    if (A.width > 5) { // 7- and 9-point antisymmetric interiors (E6u_1, E8u_1): differences
+        const int hw = A.width / 2;
+        float r = A.icf[2 * hw] * (ldf(u, p + hw * s) - ldf(u, p - hw * s));
+        for (int k = hw - 1; k >= 1; k--) r = fmaf(A.icf[hw + k], ldf(u, p + k * s) - ldf(u, p - k * s), r);
+        return r;
+    }
     if (A.width == 5) {
         if (A.antisym) {
             const float d1 = ldf(u, p + s) - ldf(u, p - s);
@@ -946,6 +958,12 @@ template <class IDX>
 __device__ __forceinline__ float interior_f(const DevAxis& A, const float* u, IDX p, IDX s)
 {
     auto L = [&](IDX i) -> float { return __ldg(u + i); };
+    if (A.width > 5) { // 7- and 9-point antisymmetric interiors (E6u_1, E8u_1), interior32's order
+        const int hw = A.width / 2;
+        float r = A.icf[2 * hw] * (L(p + hw * s) - L(p - hw * s));
+        for (int k = hw - 1; k >= 1; k--) r = fmaf(A.icf[hw + k], L(p + k * s) - L(p - k * s), r);
+        return r;
+    }
     if (A.width == 5) {
         if (A.antisym) {
             const float d1 = L(p + s) - L(p - s);
@@ -961,6 +979,12 @@ __device__ __forceinline__ float interior_f(const DevAxis& A, const float* u, ID
 template <class IDX>
 __device__ __forceinline__ double interior_d(const DevAxis& A, const double* u, IDX p, IDX s)
 {
+    if (A.width > 5) { // 7- and 9-point interiors (E6u_1, E8u_1), interior64's order
+        const int hw = A.width / 2;
+        double r = A.ic[0] * __ldg(u + p - hw * s);
+        for (int k = 1; k < A.width; k++) r = fma(A.ic[k], __ldg(u + p + (k - hw) * s), r);
+        return r;
+    }
     if (A.width == 5) {
         if (A.antisym) {
             const double d1 = __ldg(u + p + s) - __ldg(u + p - s);

@@ -26,9 +26,24 @@ POLY_ALPHA_LUA = (0.7039278390946743, 0.5390086175376538, -0.647109821986589, 0.
                   0.8736492896991024, 0.40413606410467495, 0.01, -0.01, 0.01, 0.04)
 
 
+# the alpha of the reference's own E6u_1 and E8u_1 tests (src/stencils/E6u_1.t.cpp:25,
+# E8u_1.t.cpp:25-31)
+E6U_ALPHA = (0.1, 0.2, 0.3, 0.4, 0.5)
+E8U_ALPHA = (-0.6484343281044554, 0.1546307245964576, -0.0024361150534464, -0.0767677234359209,
+             0.0395245547501803, -0.25779890216368, 0.0527307049447768)
+
+
 def cases():
     from shoccs_gb300 import workloads as W
     return {
+        # the uniform-grid 6th- and 8th-order first derivatives: a Dirichlet sphere (their
+        # closures have no cross-direction interpolant, so objects are Dirichlet)
+        "e6u_sphere_3d": dict(n=(30, 28, 32), lo=(0, 0, 0), hi=(1, 1, 1),
+                              spheres=[((0.5, 0.48, 0.52), 0.16, DIR)],
+                              grid_bc=(DIR, FLT) * 3, scheme="E6u_1", alpha=E6U_ALPHA),
+        "e8u_circle_2d": dict(n=(61, 57, 1), lo=(0, 0, 0), hi=(1, 1, 0),
+                              spheres=[((0.52, 0.47, 0.0), 0.17, DIR)],
+                              grid_bc=(DIR, FLT, DIR, FLT, FLT, FLT), scheme="E8u_1", alpha=E8U_ALPHA),
         # E2-poly on the geometry of the reference's scalar_wave.lua: a Dirichlet quarter
         # circle at (0, 0) and a Floating one at (2, 2) on [0, 2]^2, inflow faces Dirichlet
         "poly_scalar_wave_2d": dict(n=(71, 71, 1), lo=(0, 0, 0), hi=(2, 2, 0),

@@ -8,7 +8,8 @@ Sources:
   * oracle/_ref/libshoccs_ref.so: the reference's own code compiled unmodified by
     oracle/build_ref.sh -> stencils_ref.json (closure blocks, interior rows, interpolants of
     src/stencils/{E2_2,E4_2,E4_1,E4u_1}.cpp), stencils_poly_ref.json (the same of
-    src/stencils/polyE2_1.cpp for two parameter sets), sphere_hits_ref.json (src/mesh/sphere.cpp ray /
+    src/stencils/polyE2_1.cpp for two parameter sets), stencils_wide_ref.json (E6u_1, E8u_1),
+    sphere_hits_ref.json (src/mesh/sphere.cpp ray /
     sphere hits) and reference_pins.json (SHA-256 digests of the arrays of
     tests/golden/pins.py -- setup, operators, heat and scalar-wave systems -- on every case
     of tests/cases.py)
@@ -181,6 +182,38 @@ def poly_fixtures():
     return out
 
 
+# E6u / E8u alpha: the values of the reference's own tests (src/stencils/E6u_1.t.cpp:25,
+# E8u_1.t.cpp:25-31)
+WIDE_ALPHA = {6: [0.1, 0.2, 0.3, 0.4, 0.5],
+              7: [-0.6484343281044554, 0.1546307245964576, -0.0024361150534464,
+                  -0.0767677234359209, 0.0395245547501803, -0.25779890216368, 0.0527307049447768]}
+
+
+def wide_fixtures():
+    """E6u_1's and E8u_1's closure blocks and interior rows from the reference's own
+    src/stencils/E6u_1.cpp and E8u_1.cpp (oracle/_ref) -> stencils_wide_ref.json"""
+    subprocess.check_call(["sh", os.path.join(REPO, "oracle", "build_ref.sh")],
+                          env=dict(os.environ, SHOCCS_REFERENCE_ROOT=REF))
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libshoccs_ref.so"))
+    D = ctypes.c_double
+    out = dict(source="src/stencils/E6u_1.cpp, E8u_1.cpp compiled in oracle/_ref",
+               alpha={str(k): v for k, v in WIDE_ALPHA.items()}, nbs=[], interior=[])
+    for scheme, a in WIDE_ALPHA.items():
+        al = (D * len(a))(*a)
+        for bc in (0, 1):
+            for right in (0, 1):
+                for h in (2.0, 1.0 / 64, 0.1):
+                    c, x = (D * 128)(), (D * 8)()
+                    n = lib.ref_stencil_nbs(scheme, al, D(h), bc, D(1.0), right, c, x)
+                    out["nbs"].append(dict(scheme=scheme, bc=bc, right=right, h=h,
+                                           c=[float(v).hex() for v in c[:n]]))
+        for h in (2.0, 1.0 / 64, 1.0 / 255):
+            c = (D * 16)()
+            n = lib.ref_stencil_interior(scheme, al, D(h), c)
+            out["interior"].append(dict(scheme=scheme, h=h, c=[float(v).hex() for v in c[:n]]))
+    return out
+
+
 def reference_inputs():
     """The `simulation` table of each of the reference's input files as the command line's
     Lua reader evaluates it (tests/cpp/lua_eval.cpp), with the exit status of
@@ -250,6 +283,8 @@ if __name__ == "__main__":
         json.dump(st, f)
     with open(os.path.join(HERE, "stencils_poly_ref.json"), "w") as f:
         json.dump(poly_fixtures(), f)
+    with open(os.path.join(HERE, "stencils_wide_ref.json"), "w") as f:
+        json.dump(wide_fixtures(), f)
     with open(os.path.join(HERE, "sphere_hits_ref.json"), "w") as f:
         json.dump(hits, f)
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:

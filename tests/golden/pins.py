@@ -24,6 +24,8 @@ WAVE_CASES = {
     # scalar_wave.lua's system: radial wave about (-1, -1), radius 0
     "poly_scalar_wave_2d": ((-1.0, -1.0, 0.0), 0.0),
     "poly_spheres_3d": ((-0.3, -0.2, -0.1), 0.1),
+    "e6u_sphere_3d": ((-0.3, -0.2, -0.1), 0.1),
+    "e8u_circle_2d": ((-0.3, -0.2, 0.0), 0.1),
 }
 HEAT_SCHEMES = ("E2_2", "E4_2")
 KAPPA = 0.7

@@ -314,7 +314,7 @@ def test_cli_usage_and_check(cli, tmp_path):
 
 
 @pytest.mark.parametrize("script,msg", [
-    ('simulation.scheme.type = "E6u"', "scheme.order/type = 1 / E6u is not available"),
+    ('simulation.scheme.type = "E2"', "scheme.order/type = 1 / E2 is not available"),
     ('simulation.scheme = {order = 3, type = "E4"}', "scheme.order/type = 3 / E4 not recognized"),
     ('simulation.scheme = nil', "simulation.scheme must be specified"),
     ('simulation.system.type = "euler"', "unrecognized system.type"),
@@ -331,6 +331,21 @@ def test_cli_rejected_sections_exit_zero(cli, tmp_path, script, msg):
     r = _run(cli, [os.path.join(LUA, "wave_radial_2d.lua"), "--script", script], tmp_path)
     assert r.returncode == 0, r.stderr
     assert msg in r.stderr, r.stderr
+
+
+@pytest.mark.parametrize("scheme,msg", [
+    ('{order = 1, type = "E6u", alpha = {0.1, 0.2, 0.3, 0.4, 0.5}}', "E6 uniform first scheme chosen"),
+    ('{order = 1, type = "E8u", alpha = {-0.65, 0.15, 0, -0.08, 0.04, -0.26, 0.05}}',
+     "E8 uniform first scheme chosen"),
+])
+def test_cli_reads_wide_uniform_schemes(cli, tmp_path, scheme, msg):
+    """the scheme section is read and the builder goes on to the system (which needs a GPU
+    here; on a machine without one the run ends at the system's creation)"""
+    r = _run(cli, [os.path.join(LUA, "wave_radial_2d.lua"), "--script",
+                   "simulation.scheme = " + scheme], tmp_path)
+    out = r.stdout + r.stderr
+    assert msg in out and "building scalar_wave system" in out, out
+    assert "not available" not in out and "not recognized" not in out, out
 
 
 def test_cli_heat_rejects_lua_manufactured_solutions(cli, tmp_path):

@@ -1,8 +1,8 @@
 """Pin the CPU oracle against the reference's own golden vectors and code.
 
-* stencils_ref.json / stencils_poly_ref.json / sphere_hits_ref.json: produced by the
-  reference's own src/stencils/{E2_2,E4_2,E4_1,E4u_1,polyE2_1}.cpp and src/mesh/sphere.cpp
-  (oracle/_ref) -> bit-exact.
+* stencils_ref.json / stencils_poly_ref.json / stencils_wide_ref.json / sphere_hits_ref.json:
+  produced by the reference's own src/stencils/{E2_2,E4_2,E4_1,E4u_1,polyE2_1,E6u_1,
+  E8u_1}.cpp and src/mesh/sphere.cpp (oracle/_ref) -> bit-exact.
 * object_geometry_sphere.json: the expected values of src/mesh/object_geometry.t.cpp:11-330.
 * line segmentation: the assertions of src/mesh/mesh.t.cpp:71-141.
 * known-answer polynomial tests in the style of src/operators/derivative.t.cpp:235-261,
@@ -84,6 +84,25 @@ def test_poly_e2_stencil_bit_exact_vs_reference_code():
         want = _hex(e["c"])
         assert n == len(want)
         assert np.array_equal(np.array(c[:n]).view(np.int64), want.view(np.int64)), e
+
+
+def test_wide_uniform_stencils_bit_exact_vs_reference_code():
+    """E6u_1 (7-point interior, 5 x 8 closures) and E8u_1 (9-point interior, 7 x 11) of
+    src/stencils/E6u_1.cpp, E8u_1.cpp compiled in oracle/_ref, with the alpha of the
+    reference's own tests"""
+    g = json.load(open(os.path.join(GOLD, "stencils_wide_ref.json")))
+    L = orc.lib()
+    als = {int(k): (D * len(v))(*v) for k, v in g["alpha"].items()}
+    for e in g["nbs"]:
+        c, x = (D * 128)(), (D * 8)()
+        L.orc_stencil_nbs(e["scheme"], als[e["scheme"]], D(e["h"]), e["bc"], D(1.0), e["right"], c, x)
+        want = _hex(e["c"])
+        assert np.array_equal(np.array(c[:len(want)]).view(np.int64), want.view(np.int64)), e
+    for e in g["interior"]:
+        c = (D * 16)()
+        L.orc_stencil_interior(e["scheme"], D(e["h"]), c)
+        want = _hex(e["c"])
+        assert np.array_equal(np.array(c[:len(want)]).view(np.int64), want.view(np.int64)), e
 
 
 def test_sphere_hits_bit_exact_vs_reference_code():
