@@ -238,12 +238,13 @@ shoccs_status shoccs_system_stats_noalloc(shoccs_system* s, double t, double out
 shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double* dt);
 /* Stage-kernel variant of the system's RK4 path, chosen at creation by timing the
  * candidates on the system's own grid (the SHOCCS_STAGE_KERNEL environment variable --
- * point, tma, col1, col2, col4, vec, vec3 -- forces one):
+ * point, tma, col1, col2, col4, vec, vec3, vecx2, vecx4 -- forces one):
  * 0 per-point kernel, 1 TMA plane-marching, 2/3/4 column-blocked with 1/2/4 planes per
  * thread, 5/6 vectorised (four z points per thread; nz a multiple of 4) with 4/3 resident
  * blocks per SM, 7 unfused whole-field step (FP64 heat systems with non-Dirichlet objects,
- * whose cut-point values are state).  Variants 0-6 give the same bits.  FP64 systems and
- * 2-D / 1-D grids otherwise use the per-point kernel. */
+ * whose cut-point values are state), 8/9 vectorised marching over 2/4 x planes per thread
+ * (the x stencil's planes kept in registers).  Variants 0-6, 8 and 9 give the same bits.
+ * FP64 systems and 2-D / 1-D grids otherwise use the per-point kernel. */
 shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);
 /* ---- batched heat solves ---------------------------------------------------------------
  * Many independent heat systems (each with the manufactured sin-sin solution, Dirichlet

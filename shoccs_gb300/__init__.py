@@ -310,7 +310,7 @@ class System:
         return vals, st == _capi.OK
 
     STAGE_KERNELS = {0: "point", 1: "tma", 2: "col1", 3: "col2", 4: "col4", 5: "vec",
-                     6: "vec3", 7: "unfused"}
+                     6: "vec3", 7: "unfused", 8: "vecx2", 9: "vecx4"}
 
     @property
     def stage_kernel(self):

@@ -80,6 +80,9 @@ struct shoccs_problem {
     Bcs bcs;
     AxisOp ops[3];
     Compiled comp;
+    // every point with a row and not on a Dirichlet face has a row along every active axis
+    // (the vectorised stage kernel evaluates the interior row everywhere and relies on it)
+    bool rows_complete = false;
     // device side
     bool uploaded = false;
     int device = -1;
@@ -376,6 +379,12 @@ shoccs_status shoccs_problem_create(const shoccs_problem_desc* d, shoccs_problem
         p->bcs.obj.assign(d->sphere_bc, d->sphere_bc + d->n_spheres);
         for (int a = 0; a < 3; a++) p->ops[a] = assemble_axis(a, p->mesh, p->st, p->bcs);
         p->comp = compile_operators(p->mesh, p->ops, p->bcs);
+        p->rows_complete = true;
+        for (const uint8_t c : p->comp.cls) {
+            if (!(c & 0x3F) || (c & CLS_DIRFACE)) continue;
+            for (int a = 0; a < 3; a++)
+                if (p->ops[a].active && ((c >> (2 * a)) & 3) == 0) p->rows_complete = false;
+        }
         *out = p.release();
         return SHOCCS_OK;
     } catch (const std::bad_alloc&) {
@@ -548,7 +557,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
 {
     struct Cand {
         const char* name;
-        int tma, col, vec, minb = 4;
+        int tma, col, vec, minb = 4, px = 1;
     };
     std::vector<Cand> cands;
     if (S->b.tma) cands.push_back({"tma", 1, 0, 0});
@@ -567,9 +576,12 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         const bool wave = S->desc.kind == SHOCCS_SYS_WAVE;
         if (wave ? form != FORM_ANTI5 : (form != FORM_SYM5 && form != FORM_W3)) form = FORM_ANY;
     }
-    if (S->P->comp.it[2] % 4 == 0 && S->b.rowv && S->b.lrec && form != FORM_ANY) {
+    if (S->P->comp.it[2] % 4 == 0 && S->b.rowv && S->b.lrec && form != FORM_ANY &&
+        S->P->rows_complete) {
         cands.push_back({"vec", 0, 0, form, 4});
         cands.push_back({"vec3", 0, 0, form, 3});
+        cands.push_back({"vecx2", 0, 0, form, 4, 2});
+        cands.push_back({"vecx4", 0, 0, form, 4, 4});
     }
     // the column kernels keep a five-point window along each axis: interiors of up to 5 points
     bool w5 = true;
@@ -585,6 +597,7 @@ static shoccs_status autotune_stage_kernel(shoccs_system* S, cudaStream_t s)
         S->b.col_nx = c.col;
         S->b.vec = c.vec;
         S->b.vec_minb = c.minb;
+        S->b.vec_px = c.px;
     };
     if (const char* force = std::getenv("SHOCCS_STAGE_KERNEL")) {
         for (const auto& c : cands)
@@ -1403,6 +1416,8 @@ shoccs_status shoccs_system_path(const shoccs_system* S, int* kernel)
               : b.col_nx == 1      ? 2
               : b.col_nx == 2      ? 3
               : b.col_nx == 4      ? 4
+              : b.vec_px == 2      ? 8
+              : b.vec_px == 4      ? 9
               : b.vec              ? (b.vec_minb == 4 ? 5 : 6)
                                    : 0;
     return SHOCCS_OK;

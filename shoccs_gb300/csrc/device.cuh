@@ -150,6 +150,7 @@ struct StepBuffers {
     // creation by SHOCCS_CUT_ROWS_FP64=1
     int cut_fp64 = 0;
     int vec_minb = 4; // its resident blocks per SM (4: 64 registers, 3: 85 registers)
+    int vec_px = 1;   // its x planes per thread (1, 2 or 4; 64 registers when above 1)
     float* rowv = nullptr;
     float* lrec = nullptr;
     unsigned* err = nullptr;

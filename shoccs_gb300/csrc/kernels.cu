@@ -1397,8 +1397,11 @@ __global__ void k_faces_mixed(DevOp op, StageArgs sa)
 // the float4s on either side, the y neighbours from the float4s of rows j-2..j+2, the x
 // neighbours from those of planes i-2..i+2; all loads are issued before any class byte is
 // decoded, with coordinates clamped into the grid so they stay in bounds.  Per axis every
-// point evaluates its interior row from these registers and keeps it where the row is
-// interior (points without a row contribute 0).  The rows that are not interior cost each
+// point evaluates the interior row from these registers, and the points whose row is a
+// closure or wall row replace it.  A point without a row along some axis is a solid point
+// (right-hand side 0) or a Dirichlet face point (value replaced by the face's): the host
+// offers this kernel only when no other point lacks a row, so no row kind is tested on the
+// common path.  The rows that are not interior cost each
 // warp at most one extra round trip to memory, overlapped with the stencil loads where the
 // position alone says what is needed:
 //  * cut-cell rows: one load at the point's own index of the dense per-axis value array that
@@ -1497,23 +1500,41 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
     const float zz[8] = {L.zL.z, L.zL.w, C.x, C.y, C.z, C.w, L.zR.x, L.zR.y};
     const float* __restrict__ u0 = (const float*)sa.u0;
     float v[3][4];
-    unsigned kq[3][4];
-    // the twelve row kinds (2-bit fields, bits 0-5 of each class byte) tested at once: hb holds
-    // each field's high bit, lb its low bit moved to the high bit's position
+    // the kind of row d of point q (2-bit fields, bits 0-5 of each class byte): decoded where
+    // it is used in stages 0-2, held in registers in stage 3 (each the faster form measured)
+    unsigned kqa[3][4];
+    auto kq = [&kqa, c4](int d, int q) -> unsigned {
+        if constexpr (STAGE == 3)
+            return kqa[d][q];
+        else
+            return (c4 >> (8 * q + 2 * d)) & 3u;
+    };
+    // the twelve row kinds tested at once: hb holds each field's high bit, lb its low bit
+    // moved to the high bit's position
     const unsigned hb = c4 & 0x2A2A2A2Au, lb = (c4 << 1) & 0x2A2A2A2Au;
     const bool cut = (hb & ~lb) != 0u;                      // cut-cell rows (kind 2)
     const bool zwall = (hb & lb & 0x20202020u) != 0u;       // z-wall rows (kind 3)
     const bool xywall = (hb & lb & 0x0A0A0A0Au) != 0u;      // x / y wall rows
 #pragma unroll
     for (int q = 0; q < 4; q++) {
+        if constexpr (STAGE == 3) {
 #pragma unroll
-        for (int d = 0; d < 3; d++) kq[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
+            for (int d = 0; d < 3; d++) kqa[d][q] = (c4 >> (8 * q + 2 * d)) & 3u;
+        }
         const float sx = interior_row_t<FORM>(op.ax[0], f4(xa, q), f4(xb, q), f4(C, q), f4(xc, q), f4(xd, q));
         const float sy = interior_row_t<FORM>(op.ax[1], f4(ya, q), f4(yb, q), f4(C, q), f4(yc, q), f4(yd, q));
         const float sz = interior_row_t<FORM>(op.ax[2], zz[q], zz[q + 1], zz[q + 2], zz[q + 3], zz[q + 4]);
-        v[0][q] = kq[0][q] == ROW_INTERIOR ? sx : 0.f;
-        v[1][q] = kq[1][q] == ROW_INTERIOR ? sy : 0.f;
-        v[2][q] = kq[2][q] == ROW_INTERIOR ? sz : 0.f;
+        if constexpr (STAGE < 3) {
+            v[0][q] = sx;
+            v[1][q] = sy;
+            v[2][q] = sz;
+        } else {
+            // stage 3 keeps only the interior rows here: without these selects the
+            // compiler's schedule of its u0 and accumulator registers spills (measured slower)
+            v[0][q] = kqa[0][q] == ROW_INTERIOR ? sx : 0.f;
+            v[1][q] = kqa[1][q] == ROW_INTERIOR ? sy : 0.f;
+            v[2][q] = kqa[2][q] == ROW_INTERIOR ? sz : 0.f;
+        }
     }
     // the lo plane of u0 (stage 3 only) is loaded here, after the stencil registers are
     // free: issued before it, it pushed stage 3 past the 64-register budget
@@ -1524,21 +1545,21 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
         for (int d = 0; d < 3; d++)
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (kq[d][q] == ROW_CLOSURE) v[d][q] = __ldcg(rv + d * op.N + q);
+                if (kq(d, q) == ROW_CLOSURE) v[d][q] = __ldcg(rv + d * op.N + q);
     }
     if (__any_sync(FULL, zwall)) { // z-wall rows: the record words of the four points
         const int w0 = k < 8 ? k : 8 + k - (nz - 8);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const float val = __shfl_sync(FULL, rec, (w0 + q) & 31);
-            if (kq[2][q] == ROW_WALL) v[2][q] = val;
+            if (kq(2, q) == ROW_WALL) v[2][q] = val;
         }
     }
     if (__any_sync(FULL, xywall)) { // whole x / y wall planes: uniform across the warp
 #pragma unroll
         for (int d = 0; d < 2; d++) {
-            const bool wd = kq[d][0] == ROW_WALL || kq[d][1] == ROW_WALL ||
-                            kq[d][2] == ROW_WALL || kq[d][3] == ROW_WALL;
+            const bool wd = kq(d, 0) == ROW_WALL || kq(d, 1) == ROW_WALL ||
+                            kq(d, 2) == ROW_WALL || kq(d, 3) == ROW_WALL;
             if (!__any_sync(FULL, wd)) continue;
             // the block's columns for the four points as float4s, in two groups of at most
             // four (two round trips, at most 16 registers of loads in flight); wall32's order
@@ -1573,7 +1594,7 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
             }
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (kq[d][q] == ROW_WALL) v[d][q] = sw[q];
+                if (kq(d, q) == ROW_WALL) v[d][q] = sw[q];
         }
     }
     float ao[4], so[4];
@@ -1627,7 +1648,10 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
     }
 }
 
-template <int STAGE, int SYS, int FORM, int VK, int MINB>
+// PX > 1: a thread marches over PX consecutive x planes at its (j, k) and keeps the five
+// planes of the x stencil in registers, so each further plane costs one x load instead of
+// five (the window shifts by one plane per step); the per-point arithmetic is unchanged.
+template <int STAGE, int SYS, int FORM, int VK, int MINB, int PX = 1>
 __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
 {
     // The stage input, u0 and the accumulator were complete before the cut-row kernel that
@@ -1639,23 +1663,36 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     const int lane = threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     if (j >= ny) return; // whole warp
-    const int i = blockIdx.z;
     const int k = blockIdx.x * 128 + 4 * lane;
     const int plane = ny * nz;
-    const int p = i * plane + j * nz + min(k, nz - 4);
-    const int xm2 = (max(i - 2, 0) - i) * plane, xm1 = (max(i - 1, 0) - i) * plane;
-    const int xp1 = (min(i + 1, nx - 1) - i) * plane, xp2 = (min(i + 2, nx - 1) - i) * plane;
-    const VecLoads L = vec_loads<STAGE>(op, sa, in, i, j, k, ld4(in, p));
-    const float4 xa = ld4(in, p + xm2), xb = ld4(in, p + xm1), xc = ld4(in, p + xp1),
-                 xd = ld4(in, p + xp2);
+    const int pj = j * nz + min(k, nz - 4); // the four points' offset within a plane
+    // plane ii of the stage input at the thread's four points, ii clamped into the grid (the
+    // clamped planes only feed rows that are not interior)
+    auto ldx = [&](int ii) { return ld4(in, min(max(ii, 0), nx - 1) * plane + pj); };
+    const int kw = blockIdx.x * 128;
+    const bool rec_lane = lane < LREC_WORDS && (kw < 8 || kw + 128 > nz - 8);
+    const int i0 = blockIdx.z * PX;
+    float4 xa = ldx(i0 - 2), xb = ldx(i0 - 1), C = ldx(i0), xc = ldx(i0 + 1), xd = ldx(i0 + 2);
+    VecLoads L = vec_loads<STAGE>(op, sa, in, i0, j, k, C);
     // the line record (k_cut_rows): word `lane` on lanes 0..19 of a warp that holds either
     // end of the line
     pdl_wait();
-    const int kw = blockIdx.x * 128;
-    const float rec = lane < LREC_WORDS && (kw < 8 || kw + 128 > nz - 8)
-                          ? __ldcg(sa.lrec + (long long)(i * ny + j) * LREC_WORDS + lane)
-                          : 0.f;
-    vec_stage_points<STAGE, SYS, FORM, VK>(op, sp, sa, in, i, j, k, lane, L, xa, xb, xc, xd, rec);
+    const int i1 = min(i0 + PX, nx);
+    for (int i = i0;;) {
+        const float rec = rec_lane ? __ldcg(sa.lrec + (long long)(i * ny + j) * LREC_WORDS + lane) : 0.f;
+        vec_stage_points<STAGE, SYS, FORM, VK>(op, sp, sa, in, i, j, k, lane, L, xa, xb, xc, xd, rec);
+        if constexpr (PX == 1) {
+            break;
+        } else {
+            if (++i >= i1) break;
+            xa = xb;
+            xb = L.C;
+            C = xc;
+            xc = xd;
+            xd = ldx(i + 2);
+            L = vec_loads<STAGE>(op, sa, in, i, j, k, C);
+        }
+    }
 }
 
 // ---- TMA plane-marching mixed stage (3-D grids) -----------------------------------------
@@ -2572,24 +2609,34 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
         k_stage_mixed_tma<STAGE, SYS><<<grid, dim3(32, TMA_TY + 1), smem, s>>>(
             tm, b.tm_u0t, b.tm_u0l, b.tm_acct, b.tm_cls, op, sp, a, b.err);
     } else if (mixed && b.vec) {
-        const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0);
-        // 4 or 3 resident blocks per SM (64 or 85 registers per thread)
+        const int px = b.vec_px;
+        const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, (op.it0 + px - 1) / px);
+        // 4 or 3 resident blocks per SM (64 or 85 registers per thread); 1, 2 or 4 x planes
+        // per thread
         auto go = [&](auto kern) { launch_ex(kern, vgrid, block, s, true, op, sp, a); };
-        const bool b4 = b.vec_minb == 4;
+        auto pick = [&](auto form, auto vk) {
+            constexpr int F = decltype(form)::value, V = decltype(vk)::value;
+            if (px == 4)
+                go(k_stage_mixed_vec<STAGE, SYS, F, V, 3, 4>);
+            else if (px == 2)
+                go(k_stage_mixed_vec<STAGE, SYS, F, V, 3, 2>);
+            else if (b.vec_minb == 4)
+                go(k_stage_mixed_vec<STAGE, SYS, F, V, 4, 1>);
+            else
+                go(k_stage_mixed_vec<STAGE, SYS, F, V, 3, 1>);
+        };
+        using I0 = std::integral_constant<int, 0>;
+        using I1 = std::integral_constant<int, 1>;
         if constexpr (SYS == SYS_WAVE) {
             if (sp.vel_kind)
-                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1, 4>)
-                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 1, 3>);
+                pick(std::integral_constant<int, FORM_ANTI5>{}, I1{});
             else
-                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0, 4>)
-                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_ANTI5, 0, 3>);
+                pick(std::integral_constant<int, FORM_ANTI5>{}, I0{});
         } else {
             if (b.vec == FORM_SYM5)
-                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0, 4>)
-                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_SYM5, 0, 3>);
+                pick(std::integral_constant<int, FORM_SYM5>{}, I0{});
             else
-                b4 ? go(k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0, 4>)
-                   : go(k_stage_mixed_vec<STAGE, SYS, FORM_W3, 0, 3>);
+                pick(std::integral_constant<int, FORM_W3>{}, I0{});
         }
     } else if (mixed && b.col_nx) {
         const dim3 cgrid(op.nzc, (op.it1 + BY - 1) / BY, (op.it0 + b.col_nx - 1) / b.col_nx);

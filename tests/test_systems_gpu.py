@@ -226,7 +226,7 @@ def test_nonfinite_detected():
     assert not valid
 
 
-STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec", "vec3")
+STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec", "vec3", "vecx2", "vecx4")
 
 
 @pytest.mark.gpu
@@ -234,7 +234,8 @@ STAGE_VARIANTS = ("point", "tma", "col1", "col2", "col4", "vec", "vec3")
                                      ("wave_radial", 128), ("wave_sphere_radial", 128)])
 def test_stage_kernel_variants_agree_bitwise(kind, nz, monkeypatch):
     """Every mixed stage-kernel variant (TMA plane marching, column-blocked with 1/2/4
-    planes per thread, vectorised with four z points per thread, per-point) gives the same
+    planes per thread, vectorised with four z points per thread over 1, 2 or 4 x planes,
+    per-point) gives the same
     bits: same arithmetic, different data movement.  The autotuner may therefore pick any of
     them.  The cases cover warps without special rows (nz = 128), partially filled warps
     (nz = 48), cut-cell rows, domain-wall rows and both velocity fields."""
