@@ -340,16 +340,21 @@ def unfused_bench(stream, n=128, steps=10):
     source, whole-field axpys, the boundary update); the same grid with a Dirichlet sphere runs
     the fused FP64 stage kernels and is timed alongside.  `steps` RK4 steps after a warm-up,
     timed with CUDA events on the launching stream (10 steps: this scheme's Floating closure
-    grows without bound after a few tens of steps on this geometry)."""
+    grows without bound after a few tens of steps on this geometry).  The Floating sphere is
+    also timed in mixed precision (FP32 stage fields at the D points, FP64 cut points and
+    state; `floating_unfused_mixed`), next to the fused mixed stages with a Dirichlet sphere."""
     import torch
     import shoccs_gb300 as S
     from shoccs_gb300 import workloads as W
     dt = W.heat_dt(n)
     res = {"grid": [n, n, n], "rk4_steps": steps, "dtype": "f64"}
-    for name, bc in (("floating_unfused", "floating"), ("dirichlet_fused", "dirichlet")):
+    for name, bc, prec in (("floating_unfused", "floating", S.PREC_FP64),
+                           ("dirichlet_fused", "dirichlet", S.PREC_FP64),
+                           ("floating_unfused_mixed", "floating", S.PREC_MIXED),
+                           ("dirichlet_fused_mixed", "dirichlet", S.PREC_MIXED)):
         c = dict(W.adjoint_case(n), spheres=[((0.5, 0.5, 0.5), 0.25, bc)])
         p = S.Problem(**c)
-        h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, [1.0])
+        h = S.Heat(p, 1.0, prec, S.SOL_SINSIN, [1.0])
         h.initialize(0.0, stream)
         h.rk4(0.0, dt, 2, stream)  # warm-up
         h.initialize(0.0, stream)
@@ -369,6 +374,8 @@ def unfused_bench(stream, n=128, steps=10):
         res[name]["launches_per_step"] = (S.kernel_launches() - n0) / steps
         del h, p
     res["unfused_over_fused"] = res["floating_unfused"]["ms_per_step"] / res["dirichlet_fused"]["ms_per_step"]
+    res["unfused_mixed_speedup_over_fp64"] = (res["floating_unfused"]["ms_per_step"] /
+                                              res["floating_unfused_mixed"]["ms_per_step"])
     return res
 
 

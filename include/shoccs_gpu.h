@@ -156,7 +156,7 @@ enum {
     SHOCCS_SOL_GAUSSIAN = 4     /* the reference's "gaussian" manufactured solution
                                  * (src/mms/gauss1d.cpp, gauss2d.cpp, gauss3d.cpp):
                                  * sum_i A_i cos(f_i t) exp(-1/2 sum_{d<D} (x_d - c_id)^2 / s_id^2),
-                                 * D the mesh's dimension count; terms in sol_terms.  FP64 heat
+                                 * D the mesh's dimension count; terms in sol_terms.  Heat
                                  * systems only (stepped on the unfused whole-field path) */
 };
 enum { SHOCCS_VEL_CONSTANT = 0, SHOCCS_VEL_RADIAL = 1 };
@@ -179,13 +179,17 @@ typedef struct {
 shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* desc,
                                    shoccs_system** out);
 shoccs_status shoccs_system_destroy(shoccs_system* s);
-/* Time stepping takes Dirichlet and Floating faces and Dirichlet objects; a FP64 heat system
+/* Time stepping takes Dirichlet and Floating faces and Dirichlet objects; a heat system
  * also takes Floating objects, whose cut-point values are then state that evolves through
  * the Laplacian's R-space rows (rk4 advances the whole field {D, Rx, Ry, Rz}, as
  * src/temporal/rk4.cpp:16-47 does), and Neumann faces, whose Neumann data is the solution's
  * gradient at each right-hand side's time (heat::update_boundary,
  * src/systems/heat.cpp:324-352).  Neumann objects step like Floating ones (heat::rhs adds
- * the source at every non-Dirichlet cut point and assigns no Neumann data to objects). */
+ * the source at every non-Dirichlet cut point and assigns no Neumann data to objects).  A
+ * wave system takes Floating objects (the gradient's R-space rows).  These systems step
+ * the whole field unfused; their state is FP64 in either precision, and a SHOCCS_PREC_MIXED
+ * system computes each step in FP32 (stage inputs, right-hand sides, stage accumulator;
+ * the mixed operators' rows) and adds the step's increment to the FP64 state. */
 /* u0 <- exact solution at time t on fluid D points, 0 on solid points, exact on R */
 shoccs_status shoccs_system_initialize(shoccs_system* s, double t, void* stream);
 /* copy the state in/out as FP64; where = 0 host pointers, 1 device pointers */
@@ -241,8 +245,8 @@ shoccs_status shoccs_system_timestep(const shoccs_system* s, double cfl, double*
  * point, tma, col1, col2, col4, vec, vec3, vecx2, vecx4 -- forces one):
  * 0 per-point kernel, 1 TMA plane-marching, 2/3/4 column-blocked with 1/2/4 planes per
  * thread, 5/6 vectorised (four z points per thread; nz a multiple of 4) with 4/3 resident
- * blocks per SM, 7 unfused whole-field step (FP64 heat systems with non-Dirichlet objects,
- * whose cut-point values are state), 8/9 vectorised marching over 2/4 x planes per thread
+ * blocks per SM, 7 unfused whole-field step (systems with non-Dirichlet objects, whose
+ * cut-point values are state, Neumann faces or the Gaussian solution), 8/9 vectorised marching over 2/4 x planes per thread
  * (the x stencil's planes kept in registers).  Variants 0-6, 8 and 9 give the same bits.
  * FP64 systems and 2-D / 1-D grids otherwise use the per-point kernel. */
 shoccs_status shoccs_system_path(const shoccs_system* s, int* kernel);

@@ -657,9 +657,9 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     if (d->sol_kind < 0 || d->sol_kind > 4) return fail(SHOCCS_EINVAL, "unknown solution kind");
     const bool gaussian = d->sol_kind == SHOCCS_SOL_GAUSSIAN;
     if (gaussian) {
-        if (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64)
+        if (d->kind != SHOCCS_SYS_HEAT)
             return fail(SHOCCS_EUNSUPPORTED, "the gaussian manufactured solution is time-stepped by the "
-                                             "FP64 heat system only");
+                                             "heat system only");
         if (d->sol_n_terms < 0 || (d->sol_n_terms > 0 && !d->sol_terms))
             return fail(SHOCCS_EINVAL, "gaussian manufactured solution: bad term list");
         for (int i = 0; i < 8 * d->sol_n_terms; i++)
@@ -671,10 +671,6 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     // (neumann_rx/ry/rz) is never assigned, so their closures carry no data term
     bool non_dirichlet_objects = false;
     for (int b : p->bcs.obj) non_dirichlet_objects = non_dirichlet_objects || b != Dirichlet;
-    if (non_dirichlet_objects && d->prec != PREC_FP64)
-        return fail(SHOCCS_EUNSUPPORTED,
-                    "non-Dirichlet objects (whose cut-point values evolve through the R-space "
-                    "rows) are time-stepped by the FP64 systems only");
     if (non_dirichlet_objects && d->kind == SHOCCS_SYS_WAVE) {
         for (int b : p->bcs.obj)
             if (b == Neumann)
@@ -685,8 +681,15 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     for (int a = 0; a < 3; a++)
         for (int side = 0; side < 2; side++)
             if (p->bcs.grid[a][side] == Neumann) neumann_mask |= 1 << (2 * a + side);
-    if (neumann_mask && (d->kind != SHOCCS_SYS_HEAT || d->prec != PREC_FP64))
-        return fail(SHOCCS_EUNSUPPORTED, "Neumann faces are time-stepped by the FP64 heat system only");
+    if (neumann_mask && d->kind != SHOCCS_SYS_HEAT)
+        return fail(SHOCCS_EUNSUPPORTED, "Neumann faces are time-stepped by the heat system only");
+    // Non-Dirichlet objects (whose cut-point values are state), Neumann faces and the
+    // Gaussian solution step the whole field unfused.  Its state is FP64 in either
+    // precision; a mixed system computes the step in FP32 (UnfusedAux::mixed) and is
+    // otherwise handled as an FP64 one (initialisation, state access, statistics).
+    const bool unfused = non_dirichlet_objects || neumann_mask || gaussian;
+    const bool mixed_step = unfused && d->prec == PREC_MIXED;
+    const int prec = unfused ? PREC_FP64 : d->prec;
     if (d->kind == SHOCCS_SYS_HEAT && !(d->diffusivity > 0))
         return fail(SHOCCS_EINVAL, "diffusivity must be > 0");
     const cudaStream_t s = nullptr;
@@ -695,6 +698,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     auto S = std::make_unique<shoccs_system>();
     S->P = p;
     S->desc = *d;
+    S->desc.prec = prec;
     SysParams& sp = S->sp;
     sp.kind = d->kind;
     sp.k = d->diffusivity;
@@ -747,11 +751,11 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
     }
     const long long N = p->mesh.size();
     const size_t es_u = 8; // double or float2
-    const size_t es_s = d->prec == PREC_FP64 ? 8 : 4;
+    const size_t es_s = prec == PREC_FP64 ? 8 : 4;
     SH_CUDA(S->mem.alloc(N * es_u, &S->b.u0));
     // the mixed path keeps its stage accumulator in FP32 (the increments are FP32-accurate)
-    SH_CUDA(S->mem.alloc(N * (d->prec == PREC_FP64 ? 8 : 4), &S->b.acc));
-    if (d->prec == PREC_FP64) {
+    SH_CUDA(S->mem.alloc(N * (prec == PREC_FP64 ? 8 : 4), &S->b.acc));
+    if (prec == PREC_FP64) {
         SH_CUDA(S->mem.alloc(N * es_s, &S->b.sa));
         SH_CUDA(S->mem.alloc(N * es_s, &S->b.sb));
     } else {
@@ -770,7 +774,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         SH_CUDA(cudaMemsetAsync(e, 0, sizeof(unsigned), s));
     }
     SH_CUDA(cudaMemsetAsync(S->b.u0, 0, N * es_u, s));
-    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (d->prec == PREC_FP64 ? 8 : 4), s));
+    SH_CUDA(cudaMemsetAsync(S->b.acc, 0, N * (prec == PREC_FP64 ? 8 : 4), s));
     for (int r = 0; r < 3; r++) {
         const size_t n = p->mesh.R[r].size();
         void *a, *h, *f;
@@ -782,7 +786,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         S->b.Rfull[r] = (double*)f;
         if (n) SH_CUDA(cudaMemsetAsync(a, 0, n * 8, s));
     }
-    if (non_dirichlet_objects || neumann_mask || gaussian) {
+    if (unfused) {
         S->unfused = true;
         if (neumann_mask) {
             void* nu = nullptr;
@@ -800,7 +804,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
             S->fk.R[r] = S->b.Rfull[r];
             S->facc.R[r] = (double*)a;
         }
-        if (d->kind == SHOCCS_SYS_WAVE) { // the gradient's components over the whole field
+        if (d->kind == SHOCCS_SYS_WAVE && !mixed_step) { // the gradient over the whole field
             for (int c = 0; c < 3; c++) {
                 void* g = nullptr;
                 SH_CUDA(S->mem.alloc((size_t)N * 8, &g));
@@ -812,8 +816,26 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
                 }
             }
         }
+        if (mixed_step) { // stage input, right-hand side, accumulator (and gradient): FP32 D
+            S->ux.mixed = 1;  // values, FP64 cut-point values
+            auto field_mx = [&](FieldMx& f) -> shoccs_status {
+                void* a = nullptr;
+                SH_CUDA(S->mem.alloc((size_t)N * sizeof(float), &a));
+                f.D = (float*)a;
+                for (int r = 0; r < 3; r++) {
+                    SH_CUDA(S->mem.alloc(std::max<size_t>(1, p->mesh.R[r].size()) * sizeof(double), &a));
+                    f.R[r] = (double*)a;
+                }
+                return SHOCCS_OK;
+            };
+            for (FieldMx* f : {&S->ux.y_mx, &S->ux.k_mx, &S->ux.acc_mx})
+                if (auto st = field_mx(*f); st != SHOCCS_OK) return st;
+            if (d->kind == SHOCCS_SYS_WAVE)
+                for (int c = 0; c < 3; c++)
+                    if (auto st = field_mx(S->ux.grad_mx[c]); st != SHOCCS_OK) return st;
+        }
     }
-    if (d->prec == PREC_MIXED) {
+    if (prec == PREC_MIXED) {
         // exact values on the Dirichlet faces, evaluated once per step on a side stream
         for (int f = 0; f < 6; f++) {
             if (p->bcs.grid[f / 2][f % 2] != Dirichlet) continue;
@@ -851,7 +873,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         // its interior rows are the 5-point ones (sym5, or antisymmetric)
         bool w5 = true;
         for (int a = 0; a < 3; a++) w5 = w5 && (!p->op.ax[a].active || p->op.ax[a].width == 5);
-        if (d->prec == PREC_MIXED && three_d && w5 && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
+        if (prec == PREC_MIXED && three_d && w5 && it[2] % 16 == 0 && N < (1LL << 31) - 64 &&
             !std::getenv("SHOCCS_DISABLE_TMA")) {
             float* hi = (float*)S->b.u0;
             S->b.tma = make_plane_map(&S->b.tm_u0, hi, 4, it) &&
@@ -865,7 +887,7 @@ shoccs_status shoccs_system_create(shoccs_problem* p, const shoccs_system_desc* 
         // the trial steps of the autotuner need every register allocated and zeroed; the
         // column and vectorised kernels index with 32-bit integers
         if (const char* f = std::getenv("SHOCCS_CUT_ROWS_FP64")) S->b.cut_fp64 = std::atoi(f) != 0;
-        if (d->prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
+        if (prec == PREC_MIXED && three_d && N < (1LL << 31) - 64) {
             // the vectorised stage: cut-cell row values at their points, line records; the
             // cut-row kernel runs one thread per cut-cell row and per z line
             const long long nthreads = (long long)it[0] * it[1] + p->op.n_cut_rows;
@@ -1025,7 +1047,7 @@ shoccs_status shoccs_system_euler(shoccs_system* S, double t0, double dt, int ns
                                   void* stream)
 {
     if (!S || nsteps < 0 || !(dt > 0)) return fail(SHOCCS_EINVAL, "bad argument");
-    if (S->desc.prec != PREC_FP64)
+    if (S->desc.prec != PREC_FP64 || S->ux.mixed)
         return fail(SHOCCS_EUNSUPPORTED, "the forward Euler integrator steps FP64 systems");
     const cudaStream_t s = (cudaStream_t)stream;
     // the right-hand side's scratch: the unfused step's whole-field register, or (fused

@@ -91,11 +91,23 @@ struct NeumannFaces {
     double* nu;
 };
 
+// a whole scalar field of the mixed unfused step: FP32 D values, FP64 cut-point values
+struct FieldMx {
+    float* D;
+    double* R[3];
+};
+
 // what the unfused whole-field step needs beyond the state: the Neumann face data (heat) and
-// the gradient's three components over the whole field (wave)
+// the gradient's three components over the whole field (wave).  With mixed set the step
+// computes at the D points in FP32 (interior and wall rows) and at the cut points in FP64
+// (cut-cell and R-space rows; stage input y_mx, right-hand side k_mx, stage accumulator
+// acc_mx, gradient grad_mx) and adds the accumulated increment to the FP64 state once per
+// step.
 struct UnfusedAux {
     NeumannFaces nf{};
     FieldF64 grad[3]{};
+    int mixed = 0;
+    FieldMx y_mx{}, k_mx{}, acc_mx{}, grad_mx[3]{};
 };
 
 // launch helpers implemented in kernels.cu -----------------------------------------------

@@ -571,9 +571,9 @@ inline dim3 point_grid(const DevOp& op)
 // ===========================================================================================
 // value of axis d's row at point q (kind != ROW_NONE); FP64 fields compute in FP64, FP32
 // fields compute interior and wall rows in FP32 and cut-cell rows in FP64
-template <class T>
+template <class T, class TR = T>
 __device__ __forceinline__ T op_row(const DevAxis& A, unsigned kind, int row, long long p,
-                                    int coord, const T* u, const T* Rd, const double* nu,
+                                    int coord, const T* u, const TR* Rd, const double* nu,
                                     T acc, bool first)
 {
     if constexpr (sizeof(T) == 8) {
@@ -593,8 +593,7 @@ __device__ __forceinline__ T op_row(const DevAxis& A, unsigned kind, int row, lo
             v = wall_neumann32(A, p, coord, nu, v);
             return first ? v : acc + v;
         }
-        return (float)closure64(A, row, p, (const float*)u, (const float*)Rd, nu, (double)acc,
-                                first);
+        return (float)closure64(A, row, p, (const float*)u, Rd, nu, (double)acc, first);
     }
 }
 
@@ -615,15 +614,15 @@ __global__ void __launch_bounds__(256) k_derivative(DevOp op, int dir, const T* 
     du[q.p] = op_row<T>(A, kind, row, q.p, ijk[dir], u, Rd, nu, prev, !PLUS);
 }
 
-template <class T>
+template <class T, class TR = T> // TR: the R values' type (FP64 R with FP32 D: mixed unfused step)
 __global__ void __launch_bounds__(256) k_laplacian(DevOp op, const T* __restrict__ u,
-                                                   const T* R0, const T* R1, const T* R2,
+                                                   const TR* R0, const TR* R1, const TR* R2,
                                                    const double* __restrict__ nu,
                                                    T* __restrict__ du)
 {
     const Pt q = point_of(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
-    const T* R[3] = {R0, R1, R2};
+    const TR* R[3] = {R0, R1, R2};
     int ijk[3];
     phys_ijk(op, q, ijk);
     T acc = 0;
@@ -633,19 +632,19 @@ __global__ void __launch_bounds__(256) k_laplacian(DevOp op, const T* __restrict
         if (!A.active) continue;
         const unsigned kind = (c >> (2 * d)) & 3u;
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
-        if (kind != ROW_NONE) acc = op_row<T>(A, kind, row, q.p, ijk[d], u, R[d], nu, acc, false);
+        if (kind != ROW_NONE) acc = op_row<T, TR>(A, kind, row, q.p, ijk[d], u, R[d], nu, acc, false);
     }
     if (q.valid) du[q.p] = acc;
 }
 
-template <class T>
+template <class T, class TR = T>
 __global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict__ u,
-                                                  const T* R0, const T* R1, const T* R2,
+                                                  const TR* R0, const TR* R1, const TR* R2,
                                                   T* o0, T* o1, T* o2)
 {
     const Pt q = point_of(op);
     const unsigned c = q.valid ? op.cls[q.p] : 0u;
-    const T* R[3] = {R0, R1, R2};
+    const TR* R[3] = {R0, R1, R2};
     T* out[3] = {o0, o1, o2};
     int ijk[3];
     phys_ijk(op, q, ijk);
@@ -660,7 +659,7 @@ __global__ void __launch_bounds__(256) k_gradient(DevOp op, const T* __restrict_
         const int row = closure_row(A, kind == ROW_CLOSURE, q.chunk);
         T v = 0;
         if (kind != ROW_NONE)
-            v = op_row<T>(A, kind, row, q.p, ijk[d], u, R[d], (const double*)nullptr, (T)0, true);
+            v = op_row<T, TR>(A, kind, row, q.p, ijk[d], u, R[d], (const double*)nullptr, (T)0, true);
         if (q.valid) out[d][q.p] = v;
     }
 }
@@ -677,18 +676,18 @@ struct RspaceAll {
     int n[3]; // rows of each target (0 where no axis in the mask has rows for it)
 };
 
-template <class T>
+template <class T, class TR = T> // TR: the R values' type, in and out
 __global__ void k_rspace_all(RspaceAll ra, int dmask, const T* __restrict__ uD,
-                             const T* __restrict__ uR0, const T* __restrict__ uR1,
-                             const T* __restrict__ uR2, T* __restrict__ du0,
-                             T* __restrict__ du1, T* __restrict__ du2)
+                             const TR* __restrict__ uR0, const TR* __restrict__ uR1,
+                             const TR* __restrict__ uR2, TR* __restrict__ du0,
+                             TR* __restrict__ du1, TR* __restrict__ du2)
 {
     int row = blockIdx.x * blockDim.x + threadIdx.x;
     int r = 0;
     while (r < 3 && row >= ra.n[r]) row -= ra.n[r++];
     if (r == 3) return;
-    const T* __restrict__ uR = r == 0 ? uR0 : (r == 1 ? uR1 : uR2);
-    T* __restrict__ duR = r == 0 ? du0 : (r == 1 ? du1 : du2);
+    const TR* __restrict__ uR = r == 0 ? uR0 : (r == 1 ? uR1 : uR2);
+    TR* __restrict__ duR = r == 0 ? du0 : (r == 1 ? du1 : du2);
     double t = (double)duR[row];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -698,13 +697,13 @@ __global__ void k_rspace_all(RspaceAll ra, int dmask, const T* __restrict__ uD,
             const double x = ra.src[d][r][q] ? (double)uR[ra.col[d][r][q]] : (double)uD[ra.col[d][r][q]];
             t = fma(ra.w[d][r][q], x, t);
         }
-        t = (double)(T)t;
+        t = (double)(TR)t;
     }
-    duR[row] = (T)t;
+    duR[row] = (TR)t;
 }
 
 // the R-space rows of the axes in dmask (active axes only), one launch
-template <class T>
+template <class T, class TR = T>
 cudaError_t rspace_axes(const DevOp& op, int dmask, const void* uD, const void* const uR[3],
                         void* const duR[3], cudaStream_t s)
 {
@@ -723,18 +722,18 @@ cudaError_t rspace_axes(const DevOp& op, int dmask, const void* uD, const void* 
         total += ra.n[r];
     }
     if (!total) return cudaSuccess;
-    k_rspace_all<T><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
-        ra, dmask, (const T*)uD, (const T*)uR[0], (const T*)uR[1], (const T*)uR[2], (T*)duR[0],
-        (T*)duR[1], (T*)duR[2]);
+    k_rspace_all<T, TR><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        ra, dmask, (const T*)uD, (const TR*)uR[0], (const TR*)uR[1], (const TR*)uR[2],
+        (TR*)duR[0], (TR*)duR[1], (TR*)duR[2]);
     ++g_launches;
     return cudaGetLastError();
 }
 
-template <class T>
+template <class T, class TR = T>
 cudaError_t rspace_for(const DevOp& op, int d, const void* uD, const void* const uR[3],
                        void* const duR[3], cudaStream_t s)
 {
-    return rspace_axes<T>(op, 1 << d, uD, uR, duR, s);
+    return rspace_axes<T, TR>(op, 1 << d, uD, uR, duR, s);
 }
 
 // ===========================================================================================
@@ -2222,8 +2221,9 @@ long long kernel_launch_count() { return g_launches.load(); }
 // outputs, 0 where the axis has no row).
 namespace
 {
+template <class TR> // the R values' type: FP32, or FP64 (the mixed unfused step)
 __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
-                          const float* R0, const float* R1, const float* R2,
+                          const TR* R0, const TR* R1, const TR* R2,
                           const double* __restrict__ nu)
 {
     pdl_trigger(); // the operator kernel after it may start and issue its stencil loads
@@ -2235,7 +2235,7 @@ __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
         const DevAxis& A = op.ax[d];
         const int row = g - A.row_base;
         const long long p = A.row_out[row];
-        const float* Rd = d == 0 ? R0 : (d == 1 ? R1 : R2);
+        const TR* Rd = d == 0 ? R0 : (d == 1 ? R1 : R2);
         op.op_rowv[d * op.N + p] = (float)closure64(A, row, p, u, Rd, nu, 0.0, true);
         return;
     }
@@ -2429,13 +2429,18 @@ void op_vec(const DevOp& op, const float* u, const double* nu, float* o0, float*
 }
 
 void op_rows(const DevOp& op, int d0, int d1, const float* u, const void* const R[3],
-             const double* nu, cudaStream_t s)
+             const double* nu, cudaStream_t s, bool r64 = false)
 {
     const int r0 = op.ax[d0].row_base, r1 = d1 < 3 ? op.ax[d1].row_base : op.n_cut_rows;
     const long long n = (long long)(r1 - r0) + (d1 == 3 ? (long long)op.it0 * op.it1 : 0);
     if (n <= 0) return;
-    k_op_rows<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
-        op, d0, d1, u, (const float*)R[0], (const float*)R[1], (const float*)R[2], nu);
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (r64)
+        k_op_rows<double><<<nb, 128, 0, s>>>(op, d0, d1, u, (const double*)R[0],
+                                             (const double*)R[1], (const double*)R[2], nu);
+    else
+        k_op_rows<float><<<nb, 128, 0, s>>>(op, d0, d1, u, (const float*)R[0],
+                                            (const float*)R[1], (const float*)R[2], nu);
     ++g_launches;
 }
 
@@ -2554,6 +2559,54 @@ cudaError_t launch_gradient(const DevOp& op, int prec, const void* uD, const voi
     }
     return cudaGetLastError();
 }
+
+namespace
+{
+// The mixed Laplacian and gradient with FP32 D values and FP64 R values in and out (the
+// mixed unfused step, whose cut-point values are state): interior and wall rows in FP32,
+// cut-cell rows in FP64 from the FP64 cut-point values, R-space rows accumulated and stored
+// in FP64.
+cudaError_t laplacian_mixed_r64(const DevOp& op, const float* uD, double* const uR[3],
+                                const double* nuD, float* duD, double* const duR[3], cudaStream_t s)
+{
+    for (int r = 0; r < 3; r++)
+        if (op.nR[r] && duR[r]) cudaMemsetAsync(duR[r], 0, op.nR[r] * sizeof(double), s);
+    const void* uRv[3] = {uR[0], uR[1], uR[2]};
+    void* const duRv[3] = {duR[0], duR[1], duR[2]};
+    if (op_vec_ok(op)) {
+        op_rows(op, 0, 3, uD, uRv, nuD, s, true);
+        op_vec<3, false>(op, uD, nuD, duD, nullptr, nullptr, s);
+    } else {
+        k_laplacian<float, double><<<point_grid(op), dim3(32, BY), 0, s>>>(op, uD, uR[0], uR[1],
+                                                                           uR[2], nuD, duD);
+        ++g_launches;
+    }
+    rspace_axes<float, double>(op, 7, uD, uRv, duRv, s);
+    return cudaGetLastError();
+}
+
+cudaError_t gradient_mixed_r64(const DevOp& op, const float* uD, double* const uR[3],
+                               float* const outD[3], double* const outR[3][3], cudaStream_t s)
+{
+    for (int d = 0; d < 3; d++)
+        for (int r = 0; r < 3; r++)
+            if (op.nR[r] && outR[d][r]) cudaMemsetAsync(outR[d][r], 0, op.nR[r] * sizeof(double), s);
+    const void* uRv[3] = {uR[0], uR[1], uR[2]};
+    if (op_vec_ok(op)) {
+        op_rows(op, 0, 3, uD, uRv, nullptr, s, true);
+        op_vec<4, false>(op, uD, nullptr, outD[0], outD[1], outD[2], s);
+    } else {
+        k_gradient<float, double><<<point_grid(op), dim3(32, BY), 0, s>>>(
+            op, uD, uR[0], uR[1], uR[2], outD[0], outD[1], outD[2]);
+        ++g_launches;
+    }
+    for (int d = 0; d < 3; d++) {
+        void* const dR[3] = {outR[d][0], outR[d][1], outR[d][2]};
+        if (op.ax[d].active) rspace_for<float, double>(op, d, uD, uRv, dR, s);
+    }
+    return cudaGetLastError();
+}
+} // namespace
 
 namespace
 {
@@ -3089,13 +3142,287 @@ cudaError_t rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp, co
     if (sp.kind == SYS_WAVE) return wave_rhs_unfused(op, dr, sp, ux, u, t, K, s, fold);
     return heat_rhs_unfused(op, dr, sp, ux.nf, u, t, K, s, fold);
 }
+
+// ---- the unfused whole-field step in mixed precision ------------------------------------
+// FP32 stage input, right-hand side and stage accumulator at the D points, FP64 at the cut
+// points (whose values are state and enter cut-cell rows with large coefficients); the
+// operators are the mixed ones with FP64 R values (FP32 interior and wall rows, FP64
+// cut-cell and R-space rows); the state stays FP64 and receives the step's accumulated
+// increment once.  The D points' arithmetic of the right-hand side and of the RK4 registers
+// is the fused mixed stage's (rhs_mixed, rk_mixed); the cut points' is the FP64 step's.
+struct StageFoldMx {
+    int on;
+    FieldMx acc;
+    float2 c_acc_f; // dt rkf[i] as a compensated FP32 pair (D points)
+    double c_acc;   // and in FP64 (cut points)
+    int has_y;
+    FieldMx y;
+    FieldF64 u;
+    float c_y_f; // dt rki[i+1]
+    double c_y;
+};
+
+__device__ __forceinline__ void fold_d(const StageFoldMx& f, float* k, long long j, float v,
+                                       const FieldF64& u)
+{
+    if (!f.on) {
+        k[j] = v;
+        return;
+    }
+    f.acc.D[j] = __fadd_rn(f.acc.D[j], fmaf(f.c_acc_f.x, v, __fmul_rn(f.c_acc_f.y, v)));
+    if (f.has_y) f.y.D[j] = fmaf(f.c_y_f, v, (float)u.D[j]);
+}
+
+__device__ __forceinline__ void fold_r(const StageFoldMx& f, double* k, int d, long long j, double v)
+{
+    if (!f.on) {
+        k[j] = v;
+        return;
+    }
+    f.acc.R[d][j] = __dadd_rn(f.acc.R[d][j], __dmul_rn(f.c_acc, v));
+    if (f.has_y) f.y.R[d][j] = __dadd_rn(f.u.R[d][j], __dmul_rn(f.c_y, v));
+}
+
+// K <- k lap + source: FP32 at the D points (the source evaluated in FP64 as
+// k_heat_rhs_finish does, then rounded), FP64 at the cut points (k_heat_rhs_finish's
+// arithmetic); 0 on Dirichlet faces and at Dirichlet cut points
+__global__ void k_heat_rhs_finish_mx(DevOp op, DevR dr, SysParams sp, double t, double et, FieldMx K,
+                                     StageFoldMx f)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    const bool sinsin = sp.sol.kind == SOL_SINSIN;
+    const bool gauss = sp.sol.kind == SOL_GAUSSIAN;
+    auto gauss_source = [&](const double x[3]) {
+        const GaussEval ge = gauss_eval(sp.sol, t, x);
+        return __dsub_rn(ge.ddt, __dmul_rn(sp.k, ge.lap));
+    };
+    if (part == 0) {
+        const unsigned c = op.cls[i];
+        double src = 0.0;
+        if ((c & CLS_FLUID) && (sinsin || gauss)) {
+            int ijk[3];
+            phys_of_point(op, i, ijk);
+            if (sinsin) {
+                src = heat_source(sp, sol_at_point(op, sp.sol, t, et, ijk));
+            } else {
+                const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
+                src = gauss_source(x);
+            }
+        }
+        float v = fmaf(K.D[i], sp.kf, (float)src);
+        if (c & CLS_DIRFACE) v = 0.f;
+        fold_d(f, K.D, i, v, f.u);
+    } else {
+        const int d = part - 1;
+        double v = __dmul_rn(K.R[d][i], sp.k);
+        if (dr.dirichlet[d][i])
+            v = 0.0;
+        else if (sinsin)
+            v = __dadd_rn(v, heat_source(sp, sol_at(sp.sol, t, et, dr.pos[d] + 3 * i, nullptr, d, (int)i)));
+        else if (gauss)
+            v = __dadd_rn(v, gauss_source(dr.pos[d] + 3 * i));
+        fold_r(f, K.R[d], d, i, v);
+    }
+}
+
+// K <- gG . grad u: rhs_mixed's FP32 arithmetic at the D points, k_wave_rhs_finish's FP64
+// arithmetic at the cut points; 0 at points without a row, on Dirichlet faces and at
+// Dirichlet cut points
+__global__ void k_wave_rhs_finish_mx(DevOp op, DevR dr, SysParams sp, FieldMx G0, FieldMx G1,
+                                     FieldMx G2, FieldMx K, StageFoldMx f)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part < 0) return;
+    if (part == 0) {
+        const unsigned c = op.cls[i];
+        float v = 0.f;
+        if ((c & 0x3Fu) && !(c & CLS_DIRFACE)) {
+            float g0 = sp.gf[0], g1 = sp.gf[1], g2 = sp.gf[2];
+            if (sp.vel_kind != 0) {
+                int ijk[3];
+                phys_of_point(op, i, ijk);
+                const float r0 = __fsub_rn((float)op.xc[0][ijk[0]], sp.centerf[0]);
+                const float r1 = __fsub_rn((float)op.xc[1][ijk[1]], sp.centerf[1]);
+                const float r2 = __fsub_rn((float)op.xc[2][ijk[2]], sp.centerf[2]);
+                const float il = rsqrtf(fmaf(r2, r2, fmaf(r1, r1, __fmul_rn(r0, r0))));
+                g0 = __fmul_rn(-r0, il);
+                g1 = __fmul_rn(-r1, il);
+                g2 = __fmul_rn(-r2, il);
+            }
+            v = fmaf(g2, G2.D[i], fmaf(g1, G1.D[i], __fmul_rn(g0, G0.D[i])));
+        }
+        fold_d(f, K.D, i, v, f.u);
+    } else {
+        const int d = part - 1;
+        double v = 0.0;
+        if (!dr.dirichlet[d][i]) {
+            double gv[3] = {-sp.vel[0], -sp.vel[1], -sp.vel[2]};
+            if (sp.vel_kind != 0) radial_g64x(sp, dr.pos[d] + 3 * i, gv);
+            v = fma(gv[2], G2.R[d][i], fma(gv[1], G1.R[d][i], gv[0] * G0.R[d][i]));
+        }
+        fold_r(f, K.R[d], d, i, v);
+    }
+}
+
+// Dirichlet faces (FP32) and Dirichlet cut points (FP64) of a stage input take the exact
+// solution
+__global__ void k_update_boundary_mx(DevOp op, DevR dr, DevSol sol, double t, double et, FieldMx u)
+{
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < op.n_faces) {
+        const long long p = op.faces[g];
+        int ijk[3];
+        phys_of_point(op, p, ijk);
+        u.D[p] = (float)sol_point_any(op, sol, t, et, ijk);
+        return;
+    }
+    g -= op.n_faces;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (g < op.nR[d]) {
+            if (dr.dirichlet[d][g]) u.R[d][g] = sol_any(sol, t, et, dr.pos[d] + 3 * g, nullptr, d, (int)g);
+            return;
+        }
+        g -= op.nR[d];
+    }
+}
+
+// out <- the state with its D values rounded to FP32; out <- in widened; u <- u + acc (the
+// step's increment)
+__global__ void k_field_to_mx(DevOp op, FieldMx out, FieldF64 in)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part == 0)
+        out.D[i] = (float)in.D[i];
+    else if (part > 0)
+        out.R[part - 1][i] = in.R[part - 1][i];
+}
+
+__global__ void k_field_from_mx(DevOp op, FieldF64 out, FieldMx in)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part == 0)
+        out.D[i] = (double)in.D[i];
+    else if (part > 0)
+        out.R[part - 1][i] = in.R[part - 1][i];
+}
+
+__global__ void k_field_acc_mx(DevOp op, FieldF64 u, FieldMx acc)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long i = 0;
+    const int part = field_part(op, g, i);
+    if (part == 0)
+        u.D[i] = __dadd_rn(u.D[i], (double)acc.D[i]);
+    else if (part > 0)
+        u.R[part - 1][i] = __dadd_rn(u.R[part - 1][i], acc.R[part - 1][i]);
+}
+
+cudaError_t rhs_unfused_mx(const DevOp& op, const DevR& dr, const SysParams& sp, const UnfusedAux& ux,
+                           FieldMx u, double t, FieldMx K, cudaStream_t s, StageFoldMx fold = {})
+{
+    const long long n = field_size(op);
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (sp.kind == SYS_WAVE) {
+        const FieldMx* G = ux.grad_mx;
+        float* const outD[3] = {G[0].D, G[1].D, G[2].D};
+        double* const outR[3][3] = {{G[0].R[0], G[0].R[1], G[0].R[2]},
+                                    {G[1].R[0], G[1].R[1], G[1].R[2]},
+                                    {G[2].R[0], G[2].R[1], G[2].R[2]}};
+        cudaError_t e = gradient_mixed_r64(op, u.D, u.R, outD, outR, s);
+        if (e != cudaSuccess) return e;
+        k_wave_rhs_finish_mx<<<nb, 256, 0, s>>>(op, dr, sp, G[0], G[1], G[2], K, fold);
+        ++g_launches;
+        return cudaGetLastError();
+    }
+    const double et = sp.sol.kind == SOL_SINSIN ? std::exp(-t) : 0.0;
+    const NeumannFaces& nf = ux.nf;
+    if (nf.mask) {
+        long long nface = 0;
+        for (int f = 0; f < 6; f++)
+            if ((nf.mask >> f) & 1) {
+                const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+                nface += (long long)op.n[b] * op.n[c];
+            }
+        k_neumann_faces<<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(op, sp.sol, nf.mask, t, et, nf.nu);
+        ++g_launches;
+    }
+    cudaError_t e = laplacian_mixed_r64(op, u.D, u.R, nf.mask ? nf.nu : nullptr, K.D, K.R, s);
+    if (e != cudaSuccess) return e;
+    k_heat_rhs_finish_mx<<<nb, 256, 0, s>>>(op, dr, sp, t, et, K, fold);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t step_unfused_mx(const DevOp& op, const DevR& dr, const SysParams& sp, const UnfusedAux& ux,
+                            FieldF64 U, double t, double dt, cudaStream_t s)
+{
+    constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
+    constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    const long long n = field_size(op);
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    const long long nbnd = op.n_faces + op.nR[0] + op.nR[1] + op.nR[2];
+    const unsigned bb = (unsigned)std::max(1LL, (nbnd + 255) / 256);
+    auto et = [&](double tt) { return sp.sol.kind == SOL_SINSIN ? std::exp(-tt) : 0.0; };
+    const FieldMx Y = ux.y_mx, K = ux.k_mx, ACC = ux.acc_mx;
+    cudaError_t e = cudaMemsetAsync(ACC.D, 0, op.N * sizeof(float), s);
+    for (int d = 0; d < 3 && e == cudaSuccess; d++)
+        if (op.nR[d]) e = cudaMemsetAsync(ACC.R[d], 0, op.nR[d] * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    // stage 0's input: the state, its D values rounded to FP32 (the fused mixed stage reads
+    // the hi words)
+    k_field_to_mx<<<nb, 256, 0, s>>>(op, Y, U);
+    ++g_launches;
+    // stage i: K <- rhs(Y); its last pass adds dt rkf[i] k_i into ACC and (i < 3) writes the
+    // next stage's input Y <- U + dt rki[i+1] k_i after the operators have finished reading Y
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+        const double ti = t + dt * rki[i];
+        const double ca = dt * rkf[i];
+        const float cah = (float)ca;
+        const double cy = i < 3 ? dt * rki[i + 1] : 0.0;
+        const StageFoldMx fold{1, ACC, make_float2(cah, (float)(ca - (double)cah)), ca, i < 3, Y, U,
+                               (float)cy, cy};
+        e = rhs_unfused_mx(op, dr, sp, ux, Y, ti, K, s, fold);
+        if (e != cudaSuccess) break;
+        if (i < 3) {
+            const double tn = t + dt * rki[i + 1];
+            k_update_boundary_mx<<<bb, 256, 0, s>>>(op, dr, sp.sol, tn, et(tn), Y);
+            ++g_launches;
+        }
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return e;
+    k_field_acc_mx<<<nb, 256, 0, s>>>(op, U, ACC);
+    k_update_boundary<<<bb, 256, 0, s>>>(op, dr, sp.sol, t + dt, et(t + dt), U);
+    g_launches += 2;
+    return cudaGetLastError();
+}
 } // namespace
 
 cudaError_t launch_rhs_unfused(const DevOp& op, const DevR& dr, const SysParams& sp,
                                const UnfusedAux& ux, FieldF64 u, double t, FieldF64 out,
                                cudaStream_t s)
 {
-    return rhs_unfused(op, dr, sp, ux, u, t, out, s);
+    if (!ux.mixed) return rhs_unfused(op, dr, sp, ux, u, t, out, s);
+    // mixed: the state with its D values rounded to FP32, the mixed right-hand side, widened
+    // into out
+    const unsigned nb = (unsigned)((field_size(op) + 255) / 256);
+    k_field_to_mx<<<nb, 256, 0, s>>>(op, ux.y_mx, u);
+    ++g_launches;
+    cudaError_t e = rhs_unfused_mx(op, dr, sp, ux, ux.y_mx, t, ux.k_mx, s);
+    if (e != cudaSuccess) return e;
+    k_field_from_mx<<<nb, 256, 0, s>>>(op, out, ux.k_mx);
+    ++g_launches;
+    return cudaGetLastError();
 }
 
 // one RK4 step of the whole field U (rk4.cpp:16-47) with the scratch fields Y, K, ACC; the
@@ -3106,6 +3433,7 @@ cudaError_t launch_step_unfused(const DevOp& op, const DevR& dr, const SysParams
                                 const UnfusedAux& ux, FieldF64 U, FieldF64 Y, FieldF64 K,
                                 FieldF64 ACC, double t, double dt, cudaStream_t s)
 {
+    if (ux.mixed) return step_unfused_mx(op, dr, sp, ux, U, t, dt, s);
     constexpr double rki[4] = {0.0, 0.5, 0.5, 1.0};
     constexpr double rkf[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
     const long long n = field_size(op);

@@ -130,6 +130,79 @@ def test_floating_rk4_and_stats_match_oracle(name):
         assert err[int(st[k])] >= err.max() * (1 - 1e-8), (name, k, st[k], ref[k])
 
 
+# ---- mixed precision on the unfused step --------------------------------------------------
+# FP32 stage inputs, right-hand sides and stage accumulator, FP64 state.  The right-hand side
+# of an FP32-representable state against the oracle's: 2e-5 of the max norm (FP32
+# arithmetic on k lap and the source, each about 40x the right-hand side they sum to); the
+# RK4 state after 20 steps against the FP64 oracle's: within max(1e-4, 4 s) of the max norm,
+# s the case's own sensitivity -- how far the FP64 oracle's 20 steps move when only the
+# initial data is rounded to FP32 (a 3e-8 change).  The reference's Floating heat cases
+# amplify that change up to 1e5-fold (s = 3.9e-3 for circle65_floating's cut points, 1.5e-4
+# for the 24^3 spheres; 1e-8 for the stable cases); on the stable Neumann-face cases the
+# error against the exact solution equals the FP64 system's within 10 % (equal accuracy).
+def _round32(u):
+    return [np.asarray(a, dtype=np.float32).astype(np.float64) for a in u]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_floating_mixed_rhs_matches_oracle(name):
+    import torch
+    c = CASES[name]
+    p = S.Problem(**c)
+    h = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    h.initialize(0.0)
+    assert h.stage_kernel == "unfused"
+    o = OracleProblem(**c)
+    u = _round32(_state(h, p))
+    h.set_state(S.ScalarField(*[a.copy() for a in u]))
+    t = 0.013
+    want = o.heat_rhs(1.0, S.SOL_SINSIN, SOL, t, u)
+    got = h.rhs(t, p.zeros(torch.float64))
+    scale = max(np.abs(w).max() for w in want if w.size)
+    for k, (g, w) in enumerate(zip(got, want)):
+        if w.size:
+            assert np.abs(g.cpu().numpy() - w).max() <= 2e-5 * scale, (name, k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_floating_mixed_rk4_close_to_fp64_oracle(name):
+    c = CASES[name]
+    p = S.Problem(**c)
+    o = OracleProblem(**c)
+    h = S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    h.initialize(0.0)
+    u0 = _state(h, p)
+    dt, steps = W.heat_dt(max(c["n"])), 20
+    h.rk4(0.0, dt, steps)
+    got = _state(h, p)
+    want = o.heat_rk4(1.0, S.SOL_SINSIN, SOL, 0.0, dt, steps, u0)
+    moved = o.heat_rk4(1.0, S.SOL_SINSIN, SOL, 0.0, dt, steps, _round32(u0))
+    for k, (g, w, m) in enumerate(zip(got, want, moved)):
+        sens = rel(m, w)
+        assert rel(g, w) <= max(1e-4, 4 * sens), (name, k, rel(g, w), sens)
+    with pytest.raises(S.ShoccsError):  # forward Euler steps FP64 systems
+        h.euler(0.0, dt, 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["neumann_x_circle65", "neumann_e22"])
+def test_neumann_faces_mixed_equal_accuracy(name):
+    c = CASES[name]
+    p = S.Problem(**c)
+    dt, steps = W.heat_dt(max(c["n"])), 100
+    err = {}
+    for prec in (S.PREC_FP64, S.PREC_MIXED):
+        h = S.Heat(p, 1.0, prec, S.SOL_SINSIN, SOL)
+        h.initialize(0.0)
+        h.rk4(0.0, dt, steps)
+        st, ok = h.stats(steps * dt)
+        assert ok
+        err[prec] = st[0]
+    assert abs(err[S.PREC_MIXED] - err[S.PREC_FP64]) <= 0.1 * err[S.PREC_FP64], err
+
+
 # the scalar wave with Floating objects (FP64, unfused): the cut-point values of a Floating
 # object evolve by gG . grad u from the gradient's R-space rows (scalar_wave.cpp:241-321);
 # Dirichlet faces and Dirichlet cut points take the exact solution (scalar_wave.cpp:329-355)
@@ -191,6 +264,42 @@ def test_wave_floating_rk4_and_stats_match_oracle(name, vel_kind):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("vel_kind", [S.VEL_CONSTANT, S.VEL_RADIAL])
+@pytest.mark.parametrize("name", sorted(WAVE_CASES))
+def test_wave_floating_mixed_matches_oracle(name, vel_kind):
+    """the mixed unfused wave: right-hand side of an FP32-representable state (2e-6 of the
+    max norm), 20 RK4 steps against the FP64 oracle (2e-5), statistics (1e-3)"""
+    import torch
+    c = WAVE_CASES[name]
+    p = S.Problem(**c)
+    w = S.ScalarWave(p, S.PREC_MIXED, vel_kind, VEL, WAVE_CENTER, 2, PULSE)
+    w.initialize(0.0)
+    assert w.stage_kernel == "unfused"
+    o = OracleProblem(**c)
+    u = _round32(_state(w, p))
+    w.set_state(S.ScalarField(*[a.copy() for a in u]))
+    want = o.wave_rhs(vel_kind, VEL, WAVE_CENTER, u)
+    got = w.rhs(0.0, p.zeros(torch.float64))
+    scale = max(np.abs(x).max() for x in want if x.size)
+    for k, (g, wv) in enumerate(zip(got, want)):
+        if wv.size:
+            assert np.abs(g.cpu().numpy() - wv).max() <= 2e-6 * scale, (name, k)
+    h = min((c["hi"][a] - c["lo"][a]) / (c["n"][a] - 1) for a in range(3) if c["n"][a] > 1)
+    dt, steps = 0.4 * h, 20
+    w.rk4(0.0, dt, steps)
+    got = _state(w, p)
+    want = o.wave_rk4(vel_kind, VEL, WAVE_CENTER, 2, PULSE, 0.0, dt, steps, u)
+    for k, (g, wv) in enumerate(zip(got, want)):
+        assert rel(g, wv) <= 2e-5, (name, k, rel(g, wv))
+    t = steps * dt
+    st, ok = w.stats(t)
+    ref = o.stats(2, PULSE, t, want)
+    assert ok
+    for k in (0, 1, 2):
+        assert abs(st[k] - ref[k]) <= 1e-3 * max(abs(ref[k]), 1e-12), (name, k, st[k], ref[k])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("prec", [S.PREC_FP64, S.PREC_MIXED])
 def test_wave_poly_e2_dirichlet_fused_matches_oracle(prec):
     """E2-poly (3-point antisymmetric interior) with Dirichlet objects only: the fused stage
@@ -215,12 +324,10 @@ def test_wave_poly_e2_dirichlet_fused_matches_oracle(prec):
 def test_floating_systems_that_stay_unsupported():
     c = dict(CASES["circle65_floating"])
     p = S.Problem(**c)
-    with pytest.raises(S.ShoccsError):  # mixed precision: the fused path only
-        S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    assert S.Heat(p, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL).stage_kernel == "unfused"
     pw = S.Problem(**WAVE_CASES["poly_scalar_wave_2d"])
     assert S.ScalarWave(pw, S.PREC_FP64).stage_kernel == "unfused"
-    with pytest.raises(S.ShoccsError):  # the mixed wave: the fused path only
-        S.ScalarWave(pw, S.PREC_MIXED)
+    assert S.ScalarWave(pw, S.PREC_MIXED).stage_kernel == "unfused"
     h = S.Heat(p, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL)
     with pytest.raises(S.ShoccsError):  # the adjoint covers Dirichlet objects
         h.forward(0.0, 1e-5, 2)
@@ -228,10 +335,8 @@ def test_floating_systems_that_stay_unsupported():
         S.Batch([h])
     pno = S.Problem(**CASES["neumann_circle49_e22"])
     assert S.Heat(pno, 1.0, S.PREC_FP64, S.SOL_SINSIN, SOL).stage_kernel == "unfused"
-    with pytest.raises(S.ShoccsError):  # Neumann objects: FP64 heat only
-        S.Heat(pno, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    assert S.Heat(pno, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL).stage_kernel == "unfused"
     with pytest.raises(S.ShoccsError):  # Neumann objects: no first-derivative closures
         S.ScalarWave(pno, S.PREC_FP64)
-    pn = S.Problem(**CASES["neumann_x_circle65"])
-    with pytest.raises(S.ShoccsError):  # Neumann faces: FP64 heat only
-        S.Heat(pn, 1.0, S.PREC_MIXED, S.SOL_SINSIN, SOL)
+    with pytest.raises(S.ShoccsError):
+        S.ScalarWave(pno, S.PREC_MIXED)
