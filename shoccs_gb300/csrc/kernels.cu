@@ -3183,11 +3183,11 @@ __device__ __forceinline__ void fold_r(const StageFoldMx& f, double* k, int d, l
     if (f.has_y) f.y.R[d][j] = __dadd_rn(f.u.R[d][j], __dmul_rn(f.c_y, v));
 }
 
-// K <- k lap + source: FP32 at the D points (the source evaluated in FP64 as
-// k_heat_rhs_finish does, then rounded), FP64 at the cut points (k_heat_rhs_finish's
-// arithmetic); 0 on Dirichlet faces and at Dirichlet cut points
-__global__ void k_heat_rhs_finish_mx(DevOp op, DevR dr, SysParams sp, double t, double et, FieldMx K,
-                                     StageFoldMx f)
+// K <- k lap + source: FP32 at the D points (rhs_mixed's arithmetic: the sin-sin source from
+// the FP32 sine tables; the Gaussian source evaluated in FP64 and rounded), FP64 at the cut
+// points (k_heat_rhs_finish's arithmetic); 0 on Dirichlet faces and at Dirichlet cut points
+__global__ void k_heat_rhs_finish_mx(DevOp op, DevR dr, SysParams sp, double t, double et, float etf,
+                                     FieldMx K, StageFoldMx f)
 {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long i = 0;
@@ -3201,18 +3201,21 @@ __global__ void k_heat_rhs_finish_mx(DevOp op, DevR dr, SysParams sp, double t, 
     };
     if (part == 0) {
         const unsigned c = op.cls[i];
-        double src = 0.0;
+        float src = 0.f;
         if ((c & CLS_FLUID) && (sinsin || gauss)) {
             int ijk[3];
             phys_of_point(op, i, ijk);
             if (sinsin) {
-                src = heat_source(sp, sol_at_point(op, sp.sol, t, et, ijk));
+                const bool d3 = sp.sol.dims == 3;
+                src = sinsin_heat_src_f(sp.sol.Sf[0][ijk[0]], sp.sol.Sf[1][ijk[1]],
+                                        d3 ? sp.sol.Sf[2][ijk[2]] : 0.f, d3, etf, sp.kf,
+                                        (float)sp.sol.lapfac);
             } else {
                 const double x[3] = {op.xc[0][ijk[0]], op.xc[1][ijk[1]], op.xc[2][ijk[2]]};
-                src = gauss_source(x);
+                src = (float)gauss_source(x);
             }
         }
-        float v = fmaf(K.D[i], sp.kf, (float)src);
+        float v = fmaf(K.D[i], sp.kf, src);
         if (c & CLS_DIRFACE) v = 0.f;
         fold_d(f, K.D, i, v, f.u);
     } else {
@@ -3358,7 +3361,7 @@ cudaError_t rhs_unfused_mx(const DevOp& op, const DevR& dr, const SysParams& sp,
     }
     cudaError_t e = laplacian_mixed_r64(op, u.D, u.R, nf.mask ? nf.nu : nullptr, K.D, K.R, s);
     if (e != cudaSuccess) return e;
-    k_heat_rhs_finish_mx<<<nb, 256, 0, s>>>(op, dr, sp, t, et, K, fold);
+    k_heat_rhs_finish_mx<<<nb, 256, 0, s>>>(op, dr, sp, t, et, (float)et, K, fold);
     ++g_launches;
     return cudaGetLastError();
 }
