@@ -1650,8 +1650,12 @@ __device__ __forceinline__ void vec_stage_points(const DevOp& op, const SysParam
 // PX > 1: a thread marches over PX consecutive x planes at its (j, k) and keeps the five
 // planes of the x stencil in registers, so each further plane costs one x load instead of
 // five (the window shifts by one plane per step); the per-point arithmetic is unchanged.
+// VEC_BY warps (z lines) per block: a block's slot frees when its slowest warp -- one with
+// cut-cell or wall rows -- finishes, so small blocks keep more warp slots busy; MINB counts
+// resident 256-thread blocks per SM (4: 64 registers, 3: 85 registers)
+constexpr int VEC_BY = 4;
 template <int STAGE, int SYS, int FORM, int VK, int MINB, int PX = 1>
-__global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
+__global__ void __launch_bounds__(32 * VEC_BY, MINB * 8 / VEC_BY) k_stage_mixed_vec(DevOp op, SysParams sp, StageArgs sa)
 {
     // The stage input, u0 and the accumulator were complete before the cut-row kernel that
     // precedes this one could let it start, so their loads go out before the dependent-launch
@@ -1660,7 +1664,7 @@ __global__ void __launch_bounds__(256, MINB) k_stage_mixed_vec(DevOp op, SysPara
     const float* __restrict__ in = STAGE == 0 ? (const float*)sa.u0 : (const float*)sa.s_in;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
     const int lane = threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
+    const int j = blockIdx.y * VEC_BY + threadIdx.y;
     if (j >= ny) return; // whole warp
     const int k = blockIdx.x * 128 + 4 * lane;
     const int plane = ny * nz;
@@ -2663,10 +2667,10 @@ void launch_stage(const DevOp& op, const SysParams& sp, int prec, const StageArg
             tm, b.tm_u0t, b.tm_u0l, b.tm_acct, b.tm_cls, op, sp, a, b.err);
     } else if (mixed && b.vec) {
         const int px = b.vec_px;
-        const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, (op.it0 + px - 1) / px);
+        const dim3 vgrid((op.it2 + 127) / 128, (op.it1 + VEC_BY - 1) / VEC_BY, (op.it0 + px - 1) / px);
         // 4 or 3 resident blocks per SM (64 or 85 registers per thread); 1, 2 or 4 x planes
         // per thread
-        auto go = [&](auto kern) { launch_ex(kern, vgrid, block, s, true, op, sp, a); };
+        auto go = [&](auto kern) { launch_ex(kern, vgrid, dim3(32, VEC_BY), s, true, op, sp, a); };
         auto pick = [&](auto form, auto vk) {
             constexpr int F = decltype(form)::value, V = decltype(vk)::value;
             if (px == 4)
