@@ -81,8 +81,12 @@ enum { SHOCCS_SCHEME_E2_2 = 0, SHOCCS_SCHEME_E4_2 = 1, SHOCCS_SCHEME_E4_1 = 2,
 /* arithmetic of the operator and system kernels */
 enum {
     SHOCCS_PREC_FP64 = 0,  /* every value and coefficient in FP64 */
-    SHOCCS_PREC_MIXED = 1  /* FP32 fields and interior stencils; FP64 closure rows;
-                              compensated FP32-pair (~2^-46) solution and RK4 accumulator */
+    SHOCCS_PREC_MIXED = 1  /* FP32 stage fields, interior and wall rows; cut-cell rows in
+                              compensated FP32 over FP32-pair coefficients (FP64 with
+                              SHOCCS_CUT_ROWS_FP64=1); FP32 stage accumulator; the solution a
+                              compensated FP32 pair (~2^-46), updated by an error-free
+                              two-sum -- FP64 on the unfused whole-field step, whose cut-point
+                              stage values and rows are FP64 too */
 };
 
 typedef struct {
