@@ -898,16 +898,16 @@ __global__ void k_cut_rows(DevOp op, TIN u, const double* R0,
         i -= nlines;
     }
     if (i >= op.n_cut_rows) return;
-    const CgD R[3] = {{R0}, {R1}, {R2}};
     const int d = i < op.ax[1].row_base ? 0 : (i < op.ax[2].row_base ? 1 : 2);
+    const CgD Rd{d == 0 ? R0 : (d == 1 ? R1 : R2)}; // a select, not an indexed local array
     const DevAxis& A = op.ax[d];
     const int row = i - A.row_base;
     const long long p = A.row_out[row];
     if constexpr (std::is_same<TOUT, double>::value) {
-        cval[i] = closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true);
+        cval[i] = closure64(A, row, p, u, Rd, (const double*)nullptr, 0.0, true);
     } else {
-        const float v = sa.cut_fp64 ? (float)closure64(A, row, p, u, R[d], (const double*)nullptr, 0.0, true)
-                                    : closure_ff(A, row, p, u, R[d]);
+        const float v = sa.cut_fp64 ? (float)closure64(A, row, p, u, Rd, (const double*)nullptr, 0.0, true)
+                                    : closure_ff(A, row, p, u, Rd);
         if (rowv)
             rowv[d * op.N + p] = v;
         else
