@@ -2020,11 +2020,13 @@ __device__ __forceinline__ void bc_r_item(const DevOp& op, const DevR& dr, const
         int f = 0;
         while (f < 6 && i >= ra.fn[f]) i -= ra.fn[f++];
         if (f == 6) return;
-        const int a = f >> 1, b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
-        int ijk[3];
-        ijk[a] = (f & 1) ? op.n[a] - 1 : 0;
-        ijk[b] = i / op.n[c];
-        ijk[c] = i - ijk[b] * op.n[c];
+        const int a = f >> 1, c = a == 2 ? 1 : 2;
+        // the face's fixed coordinate and its two running ones (b, c = the other axes in
+        // order), placed by selects: indexed writes would put ijk in local memory
+        const int fixed = (f & 1) ? op.n[a] - 1 : 0;
+        const int vb = i / op.n[c], vc = i - vb * op.n[c];
+        const int ijk[3] = {a == 0 ? fixed : vb, a == 1 ? fixed : (a == 0 ? vb : vc),
+                            a == 2 ? fixed : vc};
         const float2 u = ff_from_double(sol_at_point(op, sol, t2, et2, ijk));
         ra.fplane[f][i] = make_float4(face_f32(op, sol, t1, et1, ijk),
                                       face_f32(op, sol, t2, et2, ijk), u.x, u.y);

@@ -201,11 +201,13 @@ int main(int argc, char** argv)
         try {
             const mesh m3{index_extents{{24, 24, 24}}, domain_extents{{0, 0, 0}, {1, 1, 1}},
                           {make_sphere(0, {0.5, 0.5, 0.5}, 0.25)}};
-            // a Floating object's cut-point values are state: only the FP64 heat system steps them
+            // a Floating object's cut-point values are state (the unfused step, FP64 state in
+            // either precision); the forward Euler integrator steps FP64 systems only
             systems::heat h(mesh{m3}, bcs::Grid{bcs::dd, bcs::dd, bcs::dd}, bcs::Object{bcs::Floating},
                             mms::zero(), stencils::make_E4_2(), 1.0, precision::mixed);
             h.initialize(0.0);
             integrators::rk4{}.run(h, 0.0, 1e-4, 1);
+            integrators::euler{}.run(h, 0.0, 1e-4, 1);
             std::fprintf(out, "floating_object none\n");
         } catch (const ccs::error& e) {
             std::fprintf(out, "floating_object status %d\n", (int)e.status());

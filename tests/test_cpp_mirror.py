@@ -148,6 +148,7 @@ def test_cpp_classes_match_the_python_binding(tmp_path):
         assert len(f) == 15 and int(f[2]) == k
     assert abs(float(lines[-1].split(",")[3]) - e_cycle) <= 1e-15 * e_cycle
     assert stats["e4_1_bound"] == ["invalid_argument"]
+    # a mixed system with a Floating object steps by RK4; forward Euler refuses it
     assert stats["floating_object"] == ["status", "6"]  # SHOCCS_EUNSUPPORTED
 
     # the field writer of both simulation cycles (ccs::field_io through system::write)
