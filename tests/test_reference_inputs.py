@@ -15,7 +15,8 @@ reader evaluates them, with the exit status of `shoccs --check` on each.
   E2-poly scheme around a Dirichlet and a Floating quarter circle, its 20 steps) run through
   the command line from their recorded tables; every step's Linf error in logs/system.csv
   equals the oracle's (the reference's heat / scalar_wave RK4 restated) within 1e-10 of the
-  solution's scale.
+  solution's scale; scalar_wave.lua also in mixed precision (`system.precision = "mixed"`),
+  within 2e-5 of the FP64 oracle's.
 """
 import json
 import os
@@ -107,6 +108,39 @@ def _compare(rows, step, stats, u0, scale_tol=1e-10):
         want = stats(t1, u)
         assert abs(rows[k][1] - want) <= scale_tol * max(scale, np.abs(u[0]).max()), (k, rows[k], want)
     return u
+
+
+def _scalar_wave_case(table):
+    m, sc = table["mesh"], table["scheme"]
+    n = (int(m["index_extents"]["1"]), int(m["index_extents"]["2"]), 1)
+    hi = (m["domain_bounds"]["1"], m["domain_bounds"]["2"], 0.0)
+    arr = lambda t: [t[str(i + 1)] for i in range(len(t))]
+    alpha = arr(sc["floating_alpha"]) + arr(sc["dirichlet_alpha"]) + arr(sc["interpolant_alpha"])
+    shapes = [table["shapes"][k] for k in sorted(table["shapes"], key=int)]
+    spheres = [((s_["center"]["1"], s_["center"]["2"], 0.0), s_["radius"], s_["boundary_condition"])
+               for s_ in shapes]
+    return dict(n=n, lo=(0, 0, 0), hi=hi, spheres=spheres,
+                grid_bc=("dirichlet", "floating", "dirichlet", "floating", "floating", "floating"),
+                scheme="polyE2_1", alpha=alpha)
+
+
+@pytest.mark.gpu
+def test_reference_scalar_wave_input_runs_mixed(tmp_path):
+    """The reference's scalar_wave.lua (E2-poly, a Dirichlet and a Floating quarter circle) in
+    mixed precision -- the unfused whole-field step with FP32 stage fields at the grid points
+    and FP64 cut points and state: every logged step's error equals the FP64 oracle's to 2e-5
+    of max |u| (the case itself moves its errors by 5e-8 of max |u| when its initial data is
+    rounded to FP32)"""
+    from oracle.oracle import OracleProblem
+    table = _inputs()["scalar_wave.lua"]["table"]
+    rows = _run_cli(table, tmp_path, 'simulation.system.precision = "mixed"')
+    sy = table["system"]
+    c = (sy["center"]["1"], sy["center"]["2"], 0.0)
+    sol = list(c) + [sy["radius"]]
+    o = OracleProblem(**_scalar_wave_case(table))
+    assert len(rows) == 21
+    _compare(rows, lambda u, t, dt: o.wave_rk4(1, (0, 0, 0), c, 3, sol, t, dt, 1, u),
+             lambda t, u: o.stats(3, sol, t, u)[0], o.initialize(3, sol, 0.0), scale_tol=2e-5)
 
 
 @pytest.mark.gpu
