@@ -2272,8 +2272,13 @@ __global__ void k_op_rows(DevOp op, int d0, int d1, const float* __restrict__ u,
     for (int m = 0; m < 4; m++) o[m] = make_float4(w[4 * m], w[4 * m + 1], w[4 * m + 2], w[4 * m + 3]);
 }
 
+// z lines per block: four for the Laplacian (its 13 float4 loads a lane make the block's
+// slowest warp matter most), eight for a derivative or the gradient (measured each way)
+template <int MODE>
+__host__ __device__ constexpr int op_vec_by() { return MODE == 3 ? 4 : 8; }
+
 template <int MODE, bool PLUS, int FORM>
-__global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __restrict__ u,
+__global__ void __launch_bounds__(32 * op_vec_by<MODE>(), 32 / op_vec_by<MODE>()) k_op_vec(DevOp op, const float* __restrict__ u,
                                                    const double* __restrict__ nu,
                                                    float* __restrict__ o0, float* __restrict__ o1,
                                                    float* __restrict__ o2)
@@ -2282,7 +2287,7 @@ __global__ void __launch_bounds__(256, 4) k_op_vec(DevOp op, const float* __rest
     constexpr bool NX = MODE == 0 || MODE >= 3, NY = MODE == 1 || MODE >= 3,
                    NZ = MODE == 2 || MODE >= 3;
     const int nx = op.it0, ny = op.it1, nz = op.it2;
-    const int j = blockIdx.y * BY + threadIdx.y;
+    const int j = blockIdx.y * op_vec_by<MODE>() + threadIdx.y;
     if (j >= ny) return; // whole warp
     const int i = blockIdx.z;
     const int k = blockIdx.x * 128 + 4 * threadIdx.x;
@@ -2424,7 +2429,8 @@ void op_vec(const DevOp& op, const float* u, const double* nu, float* o0, float*
 {
     // dependent launch after k_op_rows: the kernel issues its stencil loads and waits for
     // the prepass before it reads the cut-cell values and the z-wall records
-    const dim3 grid((op.it2 + 127) / 128, (op.it1 + BY - 1) / BY, op.it0), block(32, BY);
+    constexpr int by = op_vec_by<MODE>();
+    const dim3 grid((op.it2 + 127) / 128, (op.it1 + by - 1) / by, op.it0), block(32, by);
     if (op.op_form == FORM_ANTI5)
         launch_ex(k_op_vec<MODE, PLUS, FORM_ANTI5>, grid, block, s, true, op, u, nu, o0, o1, o2);
     else if (op.op_form == FORM_SYM5)
