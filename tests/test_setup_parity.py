@@ -68,3 +68,16 @@ def test_overlapping_closures_rejected():
         S.Problem(n=(30, 28, 26), lo=(0, 0, 0), hi=(1, 1, 1),
                   spheres=[((0.5, 0.5, 0.5), 0.3, "dirichlet")],
                   grid_bc=("dirichlet", "floating") * 3, scheme="E4_1", alpha=(0.1, 0.7))
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if c["n"][2] > 1))
+def test_points_with_rows_have_a_row_on_every_axis(name):
+    """The vectorised stage kernel evaluates the interior row at every point and lets only
+    cut-cell and wall rows replace it: a point without a row along some axis must be a solid
+    point (no row at all: right-hand side 0) or a Dirichlet face point (value replaced).  The
+    host checks this before it offers that kernel; the cases here all satisfy it."""
+    p = S.Problem(**CASES[name])
+    cls = p.classes()
+    used = ((cls & 0x3F) != 0) & ((cls & 0x40) == 0)
+    for d in range(3):
+        assert not np.any(used & (((cls >> (2 * d)) & 3) == 0)), (name, d)
