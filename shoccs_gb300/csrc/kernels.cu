@@ -1399,10 +1399,10 @@ __global__ void k_faces_mixed(DevOp op, StageArgs sa)
 // point evaluates the interior row from these registers, and the points whose row is a
 // closure or wall row replace it.  A point without a row along some axis is a solid point
 // (right-hand side 0) or a Dirichlet face point (value replaced by the face's): the host
-// offers this kernel only when no other point lacks a row, so no row kind is tested on the
-// common path.  The rows that are not interior cost each
-// warp at most one extra round trip to memory, overlapped with the stencil loads where the
-// position alone says what is needed:
+// offers this kernel only when no other point lacks a row, so stages 0-2 test no row kind on
+// the common path (stage 3 keeps a select per row kind: without it its registers spill).
+// The rows that are not interior cost each warp at most one extra round trip to memory,
+// overlapped with the stencil loads where the position alone says what is needed:
 //  * cut-cell rows: one load at the point's own index of the dense per-axis value array that
 //    k_cut_rows fills, issued as soon as the class word arrives;
 //  * x- and y-wall rows (whole planes / rows, uniform across a warp): the wall block's
