@@ -215,7 +215,13 @@ class Gradient:
 
 
 class System:
-    """A heat or scalar-wave system with its RK4 registers on the device."""
+    """A heat or scalar-wave system with its RK4 registers on the device.
+
+    prec: PREC_FP64, or PREC_MIXED (FP32 stage fields and interior rows).  Systems whose
+    cut-point values are state (Floating or Neumann objects), with Neumann faces or the
+    Gaussian solution step the whole field unfused (stage_kernel "unfused"); their state is
+    FP64 in either precision, and a mixed one computes its steps with FP32 stage fields at the
+    grid points and FP64 cut points."""
 
     def __init__(self, problem, kind, prec=PREC_FP64, diffusivity=1.0, vel_kind=VEL_CONSTANT,
                  vel=(0.0, 0.0, 0.0), center=(0.0, 0.0, 0.0), sol_kind=SOL_ZERO,
